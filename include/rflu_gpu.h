@@ -1,0 +1,182 @@
+/*
+ * rflu_gpu.h -- C ABI of the GB300 (sm_103a) implementation of RocfluMP's
+ * explicit residual-and-update path (thierrydaoud/Rocflu).
+ *
+ * The reference's Fortran driver calls one subroutine per piece of the path;
+ * each entry point below names the subroutine it replaces (file:line in the
+ * reference).  The Fortran host keeps owning t_region and all its arrays and
+ * passes plain pointers (C_LOC) and sizes; nothing is transferred in
+ * ownership.  Index arguments are 1-based Fortran ids, translated once at
+ * rflu_gpu_create.  Real arrays use the reference's column-major layouts:
+ *   cv(5,nCells), dv(3,nCells), rhs(5,nCells), gradCell(3,5,nCells),
+ *   fn(4,nFaces) = (nx,ny,nz,|A|), fc(3,nFaces), cofg(3,nCells),
+ *   xyzMoms(10,nCells) in XYZ_MOM_11..XYZ_MOM_44 order.
+ *
+ * Return codes: 0 = success; negative = usage or CUDA error (the message is
+ * available from rflu_gpu_last_error); positive = numerical event reported
+ * by the kernels (RFLU_EVENT_*), with details in rflu_status.  The library
+ * never traps or aborts; the caller maps a nonzero code to ErrorStop.
+ * A context is not re-entrant; all its work runs on one CUDA stream it owns.
+ */
+#ifndef RFLU_GPU_H
+#define RFLU_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RFLU_OK 0
+#define RFLU_ERR_ARG (-1)
+#define RFLU_ERR_CUDA (-2)
+#define RFLU_ERR_UNSUPPORTED (-3)
+#define RFLU_ERR_STATE (-4)
+#define RFLU_EVENT_NAN 1          /* invalid (NaN) cells after an update */
+#define RFLU_EVENT_POSITIVITY 2   /* p <= 0 cells floored (RFLU_CheckPositivity) */
+
+/* Precision of the device path. */
+#define RFLU_PREC_FP64 0        /* all FP64, fused multiply-add allowed */
+#define RFLU_PREC_FP64_EXACT 1  /* all FP64, reference evaluation order, no FMA: bit-exact with the CPU restatement */
+#define RFLU_PREC_MIXED 2       /* FP32 state/gradients/fluxes, FP64 master cv, p/c recovery, checks, RK combination */
+
+/* Boundary types, modfloflu/ModParameters.F90:401,413 */
+#define RFLU_BC_OUTFLOW 20
+#define RFLU_BC_SLIPWALL 60
+
+/* The reference's setup products for one region, as RFLU_InitFlowSolver
+ * leaves them (rocflu/RFLU_InitFlowSolver.F90:496,646,888-931):
+ * RFLU_BuildFaceList, RFLU_BuildGeometry, RFLU_BuildC2CStencil,
+ * RFLU_ComputeWtsC2C. */
+typedef struct {
+  int nCells;
+  int nFaces;               /* interior faces, pGrid%nFaces */
+  const int *f2c;           /* (2,nFaces), 1-based */
+  const double *fn;         /* (4,nFaces) */
+  const double *fc;         /* (3,nFaces) */
+  const double *vol;        /* (nCells) */
+  const double *cofg;       /* (3,nCells) */
+  int nPatches;
+  const int *patchFaceOff;  /* nPatches+1 offsets (0-based) into the patch-face arrays */
+  const int *bf2c;          /* (nBFaces), 1-based, patch after patch */
+  const double *bfn;        /* (4,nBFaces) */
+  const double *bfc;        /* (3,nBFaces) */
+  const int *patchBcType;   /* RFLU_BC_* */
+  const int *patchOutflowType; /* BCOPT_SUPERSONIC 0, SUBSONIC 1, MIXED 2 */
+  const double *patchPout;  /* outflow static pressure */
+  const int *patchOrder;    /* pPatch%spaceOrder, 1 or 2 */
+  /* C2C stencils (pGrid%c2cs(icg)%cellMembs) as CSR; ignored for ORDER 1 */
+  const int *c2csOff;       /* nCells+1, 0-based offsets */
+  const int *c2csMembs;     /* 1-based cell ids */
+  const double *xyzMoms;    /* (10,nCells) */
+} rflu_grid_desc;
+
+/* Numerics, the reference input deck keys (libfloflu/ReadNumericsSection.F90,
+ * ReadTimestepSection.F90, ReadReferenceSection.F90). */
+typedef struct {
+  int spaceOrder;   /* ORDER: 1 or 2 */
+  int spaceDiscr;   /* DISCR: 1 Roe, 3 HLLC, 4 AUSM+ */
+  int reconst;      /* RECONST: 0 none, 10 Barth-Jespersen (frame-invariant velocity), 11 Venkatakrishnan, 100 componentwise BJ */
+  int rkScheme;     /* RKSCHEME: 1 classical RK4, 2 Wray RK3, 3 Euler */
+  int piclBuild;    /* 1 when reproducing the reference built with PICL (its CMake default) */
+  int precision;    /* RFLU_PREC_* */
+  double cp, gamma; /* CP, GAMMA */
+  double cfl, epsEntr, dissFact; /* CFL, ENTROPY, DISSFACT */
+  double dtImposed, dtMinLimit;  /* TIMESTEP, DTMINLIMIT */
+} rflu_num_desc;
+
+typedef struct {
+  long long nanCells;      /* RFLU_CheckValidity events */
+  long long posFixCells;   /* RFLU_CheckPositivity energy-floor fixes */
+  long long negPCells;     /* RFLU_EnforceBounds tiny-negative-pressure clamps */
+  int firstBadCell;        /* 1-based reference id of the first NaN cell, 0 if none */
+  int stepsDone;
+  double time;             /* device-side current time after rflu_gpu_step */
+  double dtMin;            /* last dtMin */
+} rflu_status;
+
+typedef struct rflu_gpu_ctx rflu_gpu_ctx;
+
+/* Create the device mirror of one region: uploads geometry, renumbers cells
+ * (Morton order of cofg) and builds the cell-centric CSR structures.
+ * Call once after RFLU_InitFlowSolver (rocflu/RFLU_InitFlowSolver.F90:270-1065). */
+int rflu_gpu_create(const rflu_grid_desc *grid, const rflu_num_desc *num, rflu_gpu_ctx **ctx);
+int rflu_gpu_destroy(rflu_gpu_ctx *ctx);
+const char *rflu_gpu_last_error(void);
+/* The CUDA stream (cudaStream_t) the context launches on. */
+void *rflu_gpu_stream(rflu_gpu_ctx *ctx);
+
+/* cv(5,nCells) host -> device, then RFLU_SetVarsContWrapper
+ * (libflu/RFLU_SetVarsContWrapper.F90:79-167) on the device. */
+int rflu_gpu_upload_state(rflu_gpu_ctx *ctx, const double *cv);
+/* cv(5,nCells), dv(3,nCells) device -> host; either may be NULL. */
+int rflu_gpu_download_state(rflu_gpu_ctx *ctx, double *cv, double *dv);
+
+/* RFLU_TimeStepInviscid + RFLU_MinimumTimeStep
+ * (rocflu/RFLU_TimeStepInviscid.F90:75-333, rocflu/RFLU_MinimumTimeStep.F90:75-245):
+ * dtMin of the current state at currentTime. */
+int rflu_gpu_timestep(rflu_gpu_ctx *ctx, double currentTime, double *dtMin);
+
+/* One stage of RungeKuttaMP (libfloflu/RungeKuttaMP.F90:148-508): RKInitMP,
+ * CellGradientsMP, ConvectiveFluxesMP, RKUpdateMP, RFLU_SetVarsContWrapper,
+ * AfterUpdateMP, with the given global dtMin. */
+int rflu_gpu_rk_stage(rflu_gpu_ctx *ctx, int iStage, double dtMin);
+/* RungeKuttaMP (libfloflu/RungeKuttaMP.F90:75-514): all stages. */
+int rflu_gpu_runge_kutta(rflu_gpu_ctx *ctx, double dtMin);
+/* The stepping loop of RFLU_TimeStepping (rocflu/RFLU_TimeStepping.F90:429-628)
+ * on the device: per step timestep, RungeKuttaMP, currentTime += dtMin, the
+ * last step clipped to endTime (endTime <= 0: no clip).  *time in/out. */
+int rflu_gpu_step(rflu_gpu_ctx *ctx, int nSteps, double *time, double endTime, int *stepsDone);
+/* nSteps RungeKuttaMP calls with a fixed dtMin (no CFL evaluation). */
+int rflu_gpu_run_fixed_dt(rflu_gpu_ctx *ctx, int nSteps, double dtMin);
+
+/* One residual evaluation, CellGradientsMP (libfloflu/CellGradientsMP.F90:75)
+ * + ConvectiveFluxesMP (libfloflu/ConvectiveFluxesMP.F90:73), for the host
+ * state cv(5,nCells): rhs(5,nCells) and the limited gradCell(3,5,nCells)
+ * (grad may be NULL).  Leaves the context state untouched. */
+int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *grad);
+
+/* Discrete adjoint of the same residual (no reference counterpart; it
+ * differentiates rflu_gpu_residual): cvBar = (dR/dcv)^T rhsBar, through the
+ * limiter's active branch.  Arrays (5,nCells). */
+int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar);
+/* Tangent of the same residual: rhsDot = (dR/dcv) cvDot. */
+int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, double *rhsDot);
+/* Boundary-pressure functional J = sum over the faces of patch iPatch
+ * (0-based) of p_f*|A_f|, p_f the limited second-order face pressure of the
+ * owning cell, and its gradient dJ/dcv(5,nCells) (no reference counterpart). */
+int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, double *J, double *cvBar);
+
+int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status);
+
+/* ------------------------------------------------------------------------ */
+/* Host set-up: builds the reference's setup products from a raw mesh, for   */
+/* hosts that do not run RFLU_InitFlowSolver.  Reproduces RFLU_BuildFaceList */
+/* numbering (modflu/RFLU_ModFaceList.F90:784-1585), RFLU_BuildGeometry      */
+/* (modflu/RFLU_ModGeometry.F90:307-700), RFLU_BuildC2CStencil               */
+/* (modflu/RFLU_ModStencilsCells.F90:750-1440) and RFLU_ComputeWtsC2C        */
+/* (modflu/RFLU_ModWeights.F90:1025-1915).                                   */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int nVert, nCells, nVertPerCell;  /* 4 tetrahedra or 8 hexahedra */
+  const double *xyz;                /* (3,nVert) */
+  const int *c2v;                   /* (nVertPerCell,nCells), 1-based, Rocflu local vertex order */
+  int nPatches;
+  const int *patchFaceOff;          /* nPatches+1 */
+  const int *bf2v;                  /* (4,nBFaces), 1-based, 0 in slot 4 for triangles */
+} rflu_mesh_desc;
+
+typedef struct rflu_setup rflu_setup;
+
+/* spaceOrder > 1 also builds the C2C stencils and their moments. */
+int rflu_setup_build(const rflu_mesh_desc *mesh, int spaceOrder, rflu_setup **setup);
+/* Fills the geometry/stencil fields of grid (pointers into setup-owned
+ * memory, valid until rflu_setup_destroy); patch boundary data stay the
+ * caller's to set. */
+int rflu_setup_grid(rflu_setup *setup, rflu_grid_desc *grid);
+int rflu_setup_destroy(rflu_setup *setup);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

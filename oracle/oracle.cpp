@@ -1,0 +1,1435 @@
+/*
+ * CPU oracle: FP64 restatement of the RocfluMP explicit residual-and-update
+ * path (thierrydaoud/Rocflu).  TEST INFRASTRUCTURE ONLY -- see oracle.h.
+ *
+ * Build: g++ -O2 -ffp-contract=off -fPIC -shared (oracle/Makefile).  The
+ * reference release flags are -O / -O2 -ffp-contract=off (CMakeLists.txt:44,
+ * machines/dane.sh:6): no fused multiply-add, left-to-right evaluation.
+ */
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <array>
+#include <vector>
+
+namespace {
+
+/* ------------------------------------------------------------------------ */
+/* Perfect-gas relations, libfloflu/MixtPerf_*.F90                           */
+/* ------------------------------------------------------------------------ */
+inline double MixtPerf_R_CpG(double cp, double g) { return cp - cp / g; }         /* MixtPerf_R.F90:78 */
+inline double MixtPerf_R_M(double m) { return 8314.3 / m; }                       /* MixtPerf_R.F90:93 */
+inline double MixtPerf_M_R(double r) { return 8314.3 / r; }                       /* MixtPerf_M.F90:78 */
+inline double MixtPerf_G_CpR(double cp, double r) { return cp / (cp - r); }       /* MixtPerf_G.F90:78 */
+inline double MixtPerf_P_DEoGVm2(double d, double eo, double g, double vm2) {    /* MixtPerf_P.F90:78 */
+  return (g - 1.0) * d * (eo - 0.5 * vm2);
+}
+inline double MixtPerf_T_DPR(double d, double p, double r) { return p / (d * r); } /* MixtPerf_T.F90:124 */
+inline double MixtPerf_C_GRT(double g, double r, double t) { return std::sqrt(g * r * t); } /* MixtPerf_C.F90:125 */
+inline double MixtPerf_C_DGP(double d, double g, double p) { return std::sqrt(g * p / d); } /* MixtPerf_C.F90:95 */
+inline double MixtPerf_C_GHoVm2(double g, double ho, double vm2) {                 /* MixtPerf_C.F90:110 */
+  return std::sqrt((g - 1.0) * (ho - 0.5 * vm2));
+}
+inline double MixtPerf_Eo_DGPUVW(double d, double g, double p, double u, double v, double w) { /* MixtPerf_E.F90:79 */
+  return p / (d * (g - 1.0)) + 0.5 * (u * u + v * v + w * w);
+}
+inline double MixtPerf_Ho_CpTUVW(double cp, double t, double u, double v, double w) { /* MixtPerf_H.F90:78 */
+  return cp * t + 0.5 * (u * u + v * v + w * w);
+}
+/* modflu/RFLU_ModEntropyFixes.F90:95-106 */
+inline double EntropyFixHartenHyman(double l, double d) {
+  if (l > d) return l;
+  return (l * l + d * d) / (2.0 * d);
+}
+/* Fortran MIN/MAX for two reals as gfortran emits them for finite inputs. */
+inline double fmin2(double a, double b) { return (b < a) ? b : a; }
+inline double fmax2(double a, double b) { return (b > a) ? b : a; }
+
+/* ------------------------------------------------------------------------ */
+/* modfloflu/ModSortSearch.F90:990-1091 QuickSortRFREALInteger (Wirth).      */
+/* The tie order of this unstable sort decides which equal-fraction          */
+/* neighbours survive stencil truncation, so it is restated step by step.    */
+/* a, b are 1-based views of length n.                                       */
+/* ------------------------------------------------------------------------ */
+void QuickSortRFREALInteger(double *a1, int *b1, int n) {
+  double *a = a1 - 1;
+  int *b = b1 - 1;
+  int stackl[50], stackr[50];
+  int s = 1;
+  stackl[0] = 1;
+  stackr[0] = n;
+  int l, r, i, j, k;
+  double x, w;
+  int v;
+L10:
+  l = stackl[s - 1];
+  r = stackr[s - 1];
+  s = s - 1;
+L20:
+  i = l;
+  j = r;
+  k = (l + r) / 2;
+  x = a[k];
+  for (;;) {
+    while (a[i] < x) i = i + 1;
+    while (x < a[j]) j = j - 1;
+    if (i <= j) {
+      w = a[i]; a[i] = a[j]; a[j] = w;
+      v = b[i]; b[i] = b[j]; b[j] = v;
+      i = i + 1;
+      j = j - 1;
+      if (i > j) break;
+    } else {
+      break;
+    }
+  }
+  if (j - l >= r - i) {
+    if (l < j) { s = s + 1; stackl[s - 1] = l; stackr[s - 1] = j; }
+    l = i;
+  } else {
+    if (i < r) { s = s + 1; stackl[s - 1] = i; stackr[s - 1] = r; }
+    r = j;
+  }
+  if (l < r) goto L20;
+  if (s != 0) goto L10;
+}
+
+/* Singular values (descending) of a nRows x nCols matrix by one-sided Jacobi.
+ * Stands in for LAPACK dgesdd inside RFLU_InvertMatrixSVD
+ * (libflu/RFLU_InvertMatrixSVD.F90); only the singular values are used by the
+ * stencil builder, through the ratio test below. */
+void singularValues(int nRows, int nCols, std::vector<double> a /* col-major */, double *s) {
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < nCols - 1; ++p)
+      for (int q = p + 1; q < nCols; ++q) {
+        double alpha = 0, beta = 0, gamma = 0;
+        for (int i = 0; i < nRows; ++i) {
+          double ap = a[i + p * nRows], aq = a[i + q * nRows];
+          alpha += ap * ap; beta += aq * aq; gamma += ap * aq;
+        }
+        if (gamma == 0.0) continue;
+        double c = std::fabs(gamma) / std::sqrt(alpha * beta);
+        off = std::max(off, c);
+        if (c < 1e-15) continue;
+        double zeta = (beta - alpha) / (2.0 * gamma);
+        double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+        double cs = 1.0 / std::sqrt(1.0 + t * t), sn = cs * t;
+        for (int i = 0; i < nRows; ++i) {
+          double ap = a[i + p * nRows], aq = a[i + q * nRows];
+          a[i + p * nRows] = cs * ap - sn * aq;
+          a[i + q * nRows] = sn * ap + cs * aq;
+        }
+      }
+    if (off < 1e-15) break;
+  }
+  for (int p = 0; p < nCols; ++p) {
+    double n2 = 0;
+    for (int i = 0; i < nRows; ++i) n2 += a[i + p * nRows] * a[i + p * nRows];
+    s[p] = std::sqrt(n2);
+  }
+  std::sort(s, s + nCols, [](double x, double y) { return x > y; });
+}
+
+/* sCount of RFLU_InvertMatrixSVD (libflu/RFLU_InvertMatrixSVD.F90): number of
+ * singular values treated as zero (first below 100*eps, later ones below 1e-2
+ * of their predecessor, everything after the first drop). */
+int svdSingularCount(int nRows, int nCols, const std::vector<double> &a) {
+  double s[4];
+  singularValues(nRows, nCols, a, s);
+  int sCount = 0;
+  if (!(s[0] > 100.0 * 2.220446049250313e-16)) sCount = 1;
+  for (int i = 1; i < nCols; ++i) {
+    if (!(s[i] > 0.01 * s[i - 1])) {
+      sCount += nCols - i;
+      break;
+    }
+  }
+  return sCount;
+}
+
+struct Patch {
+  int bcType, outflowType, order;
+  double pOut;
+  int n;
+  std::vector<int> bf2v, bf2c;
+  std::vector<double> fn, fc;
+};
+
+} // namespace
+
+struct orc_ctx {
+  /* mesh */
+  int nVert, nCells, nvc;
+  std::vector<double> xyz;
+  std::vector<int> c2v;
+  int nFaces;
+  std::vector<int> f2c, f2v;
+  std::vector<double> fn, fc, vol, cofg;
+  std::vector<Patch> patches;
+  std::vector<int> stOff, stIdx;
+  std::vector<double> moms;
+  std::vector<double> epsq;     /* unused cache slot kept empty: Venkat recomputes vol**(1/3) per face */
+  /* numerics */
+  orc_num_desc num;
+  int nrkSteps;
+  double ark[5], grk[5];
+  double refCp, refGamma, gvMol, gvCp;
+  /* state */
+  std::vector<double> cv, dv, cvOld, rhs, rhsSum, diss, grad, lim;
+  long long posFixCount = 0, negPCount = 0, nanCount = 0;
+  double dtCells;
+};
+
+namespace {
+
+/* ------------------------------------------------------------------------ */
+/* Face list: RFLU_BuildFaceList (modflu/RFLU_ModFaceList.F90:784-1585) with  */
+/* the hash table of RFLU_HashFace (modflu/RFLU_ModHashTable.F90:618-734):    */
+/* faces numbered by first insertion in the cell loop x local-face loop,      */
+/* f2c(1) = inserting cell, f2c(2) = second cell, f2v from the inserting      */
+/* cell's local face; boundary faces (one cell) leave the interior list.      */
+/* Local face tables f2vTet/f2vHex: modflu/RFLU_ModGrid.F90:92-96.            */
+/* ------------------------------------------------------------------------ */
+const int f2vTet[4][3] = {{1, 2, 3}, {2, 4, 3}, {1, 3, 4}, {1, 4, 2}};
+const int f2vHex[6][4] = {{1, 4, 3, 2}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {1, 5, 8, 4}, {5, 6, 7, 8}};
+
+void buildFaceList(orc_ctx *c) {
+  struct Rec { int c1, c2, ifl; };
+  std::map<std::array<int, 3>, int> table;
+  std::vector<Rec> rec;
+  const int nfl = (c->nvc == 4) ? 4 : 6;
+  const int fvs = (c->nvc == 4) ? 3 : 4;
+  for (int icg = 0; icg < c->nCells; ++icg) {
+    for (int ifl = 0; ifl < nfl; ++ifl) {
+      int fv[4];
+      for (int k = 0; k < fvs; ++k)
+        fv[k] = c->c2v[c->nvc * icg + ((fvs == 3) ? f2vTet[ifl][k] : f2vHex[ifl][k]) - 1];
+      std::sort(fv, fv + fvs);
+      std::array<int, 3> key = {fv[0], fv[1], fv[2]};
+      auto it = table.find(key);
+      if (it == table.end()) {
+        table.emplace(key, (int)rec.size());
+        rec.push_back({icg, -1, ifl});
+      } else {
+        rec[it->second].c2 = icg;
+      }
+    }
+  }
+  /* interior (AA) faces keep the first-insertion order */
+  c->f2c.clear(); c->f2v.clear();
+  for (const Rec &r : rec) {
+    if (r.c2 < 0) continue;
+    c->f2c.push_back(r.c1);
+    c->f2c.push_back(r.c2);
+    for (int k = 0; k < 4; ++k) {
+      int v = -1;
+      if (fvs == 3) { if (k < 3) v = c->c2v[c->nvc * r.c1 + f2vTet[r.ifl][k] - 1]; }
+      else v = c->c2v[c->nvc * r.c1 + f2vHex[r.ifl][k] - 1];
+      c->f2v.push_back(v);
+    }
+  }
+  c->nFaces = (int)c->f2c.size() / 2;
+  /* boundary faces: RFLU_UnHashBFace gives the owning cell */
+  for (Patch &p : c->patches) {
+    p.bf2c.assign(p.n, -1);
+    for (int i = 0; i < p.n; ++i) {
+      int fv[4];
+      int n = (p.bf2v[4 * i + 3] < 0) ? 3 : 4;
+      for (int k = 0; k < n; ++k) fv[k] = p.bf2v[4 * i + k];
+      std::sort(fv, fv + n);
+      auto it = table.find({fv[0], fv[1], fv[2]});
+      if (it == table.end() || rec[it->second].c2 >= 0) {
+        std::fprintf(stderr, "oracle: boundary face %d not found as a single-cell face\n", i);
+        std::abort();
+      }
+      p.bf2c[i] = rec[it->second].c1;
+    }
+  }
+}
+
+/* FaceVectorTria / FaceVectorQuad (libfloflu/FaceVector.F90),
+ * FaceCentroidTria / FaceCentroidQuad (libfloflu/FaceCentroid.F90). */
+void faceVectorCentroid(const double *xyz, const int *v, int nv, double &fx, double &fy, double &fz,
+                        double &cx, double &cy, double &cz) {
+  const double *p1 = xyz + 3 * v[0], *p2 = xyz + 3 * v[1], *p3 = xyz + 3 * v[2];
+  if (nv == 3) {
+    double dxa = p1[0] - p2[0], dya = p1[1] - p2[1], dza = p1[2] - p2[2];
+    double dxb = p1[0] - p3[0], dyb = p1[1] - p3[1], dzb = p1[2] - p3[2];
+    fx = 0.5 * (dya * dzb - dyb * dza);
+    fy = -0.5 * (dxa * dzb - dxb * dza);
+    fz = 0.5 * (dxa * dyb - dxb * dya);
+    const double thrd = 1.0 / 3.0;
+    cx = thrd * (p1[0] + p2[0] + p3[0]);
+    cy = thrd * (p1[1] + p2[1] + p3[1]);
+    cz = thrd * (p1[2] + p2[2] + p3[2]);
+  } else {
+    const double *p4 = xyz + 3 * v[3];
+    double dxa = p3[0] - p1[0], dya = p3[1] - p1[1], dza = p3[2] - p1[2];
+    double dxb = p2[0] - p4[0], dyb = p2[1] - p4[1], dzb = p2[2] - p4[2];
+    fx = 0.5 * (dza * dyb - dya * dzb);
+    fy = 0.5 * (dxa * dzb - dza * dxb);
+    fz = 0.5 * (dya * dxb - dxa * dyb);
+    cx = 0.25 * (p1[0] + p2[0] + p3[0] + p4[0]);
+    cy = 0.25 * (p1[1] + p2[1] + p3[1] + p4[1]);
+    cz = 0.25 * (p1[2] + p2[2] + p3[2] + p4[2]);
+  }
+}
+
+/* RFLU_BuildGeometry (modflu/RFLU_ModGeometry.F90:307-700) with approximate
+ * centroids from RFLU_ComputeApproxCentroids (:1277-1497). */
+void buildGeometry(orc_ctx *c) {
+  const int nc = c->nCells;
+  std::vector<double> app(3 * nc);
+  for (int ic = 0; ic < nc; ++ic) {
+    const int *v = &c->c2v[c->nvc * ic];
+    for (int d = 0; d < 3; ++d) {
+      double s = c->xyz[3 * v[0] + d];
+      for (int k = 1; k < c->nvc; ++k) s = s + c->xyz[3 * v[k] + d];
+      app[3 * ic + d] = ((c->nvc == 4) ? (1.0 / 4.0) : (1.0 / 8.0)) * s;
+    }
+  }
+  c->vol.assign(nc, 0.0);
+  c->cofg.assign(3 * nc, 0.0);
+  c->fn.assign(4 * c->nFaces, 0.0);
+  c->fc.assign(3 * c->nFaces, 0.0);
+  auto accum = [&](int cell, double sgn, double fx, double fy, double fz, double cx, double cy, double cz) {
+    double term = (cx - app[3 * cell]) * fx + (cy - app[3 * cell + 1]) * fy + (cz - app[3 * cell + 2]) * fz;
+    if (sgn > 0) c->vol[cell] = c->vol[cell] + term; else c->vol[cell] = c->vol[cell] - term;
+    term = cx * fx + cy * fy + cz * fz;
+    if (sgn > 0) {
+      c->cofg[3 * cell] = c->cofg[3 * cell] + term * cx;
+      c->cofg[3 * cell + 1] = c->cofg[3 * cell + 1] + term * cy;
+      c->cofg[3 * cell + 2] = c->cofg[3 * cell + 2] + term * cz;
+    } else {
+      c->cofg[3 * cell] = c->cofg[3 * cell] - term * cx;
+      c->cofg[3 * cell + 1] = c->cofg[3 * cell + 1] - term * cy;
+      c->cofg[3 * cell + 2] = c->cofg[3 * cell + 2] - term * cz;
+    }
+  };
+  auto store = [](double *fn, double *fc, double fx, double fy, double fz, double cx, double cy, double cz) {
+    double m = std::sqrt(fx * fx + fy * fy + fz * fz);
+    double term = 1.0 / m;
+    fn[0] = fx * term; fn[1] = fy * term; fn[2] = fz * term; fn[3] = m;
+    fc[0] = cx; fc[1] = cy; fc[2] = cz;
+  };
+  for (int f = 0; f < c->nFaces; ++f) {
+    int nv = (c->f2v[4 * f + 3] < 0) ? 3 : 4;
+    double fx, fy, fz, cx, cy, cz;
+    faceVectorCentroid(c->xyz.data(), &c->f2v[4 * f], nv, fx, fy, fz, cx, cy, cz);
+    store(&c->fn[4 * f], &c->fc[3 * f], fx, fy, fz, cx, cy, cz);
+    accum(c->f2c[2 * f], 1.0, fx, fy, fz, cx, cy, cz);
+    accum(c->f2c[2 * f + 1], -1.0, fx, fy, fz, cx, cy, cz);
+  }
+  for (Patch &p : c->patches) {
+    p.fn.assign(4 * p.n, 0.0);
+    p.fc.assign(3 * p.n, 0.0);
+    for (int i = 0; i < p.n; ++i) {
+      int nv = (p.bf2v[4 * i + 3] < 0) ? 3 : 4;
+      double fx, fy, fz, cx, cy, cz;
+      faceVectorCentroid(c->xyz.data(), &p.bf2v[4 * i], nv, fx, fy, fz, cx, cy, cz);
+      store(&p.fn[4 * i], &p.fc[3 * i], fx, fy, fz, cx, cy, cz);
+      accum(p.bf2c[i], 1.0, fx, fy, fz, cx, cy, cz);
+    }
+  }
+  const double THRD = 1.0 / 3.0;
+  for (int ic = 0; ic < nc; ++ic) {
+    c->vol[ic] = THRD * c->vol[ic];
+    double term = 1.0 / (4.0 * c->vol[ic]);
+    c->cofg[3 * ic] = term * c->cofg[3 * ic];
+    c->cofg[3 * ic + 1] = term * c->cofg[3 * ic + 1];
+    c->cofg[3 * ic + 2] = term * c->cofg[3 * ic + 2];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* C2C stencils: RFLU_BuildC2CStencil (modflu/RFLU_ModStencilsCells.F90:    */
+/* 750-1206), RFLU_BuildC2CStencilBasic (:1207-1440), RFLU_AddCellLayer      */
+/* (modflu/RFLU_ModStencilsUtils.F90:696-949), sizes from                    */
+/* RFLU_SetInfoC2CStencil (:2816-2932): nLayersMax 6, min 4, max 40 in 3D.   */
+/* v2c lists hold cells in increasing order (RFLU_BuildVert2CellList).       */
+/* ------------------------------------------------------------------------ */
+void buildStencils(orc_ctx *c) {
+  const int nc = c->nCells, nvc = c->nvc;
+  const int stencilSizeMin = 4, stencilSizeMax = 40, nLayersMax = 6;
+  std::vector<int> v2cOff(c->nVert + 1, 0), v2c;
+  for (int ic = 0; ic < nc; ++ic)
+    for (int k = 0; k < nvc; ++k) v2cOff[c->c2v[nvc * ic + k] + 1]++;
+  for (int v = 0; v < c->nVert; ++v) v2cOff[v + 1] += v2cOff[v];
+  v2c.resize(v2cOff[c->nVert]);
+  {
+    std::vector<int> fill(v2cOff.begin(), v2cOff.end() - 1);
+    for (int ic = 0; ic < nc; ++ic)
+      for (int k = 0; k < nvc; ++k) v2c[fill[c->c2v[nvc * ic + k]]++] = ic;
+  }
+  const double iNVert = 1.0 / (double)nvc;
+  c->stOff.assign(nc + 1, 0);
+  c->stIdx.clear();
+  std::vector<int> c2cs(stencilSizeMax), layerBeg(nLayersMax + 1), layerEnd(nLayersMax + 1);
+  std::vector<int> tmp;
+  std::vector<double> frac;
+  for (int icg = 0; icg < nc; ++icg) {
+    /* --- RFLU_BuildC2CStencilBasic --- */
+    tmp.clear();
+    for (int k = 0; k < nvc; ++k) {
+      int v = c->c2v[nvc * icg + k];
+      for (int j = v2cOff[v]; j < v2cOff[v + 1]; ++j) tmp.push_back(v2c[j]);
+    }
+    std::sort(tmp.begin(), tmp.end());
+    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+    tmp.erase(std::find(tmp.begin(), tmp.end(), icg));
+    int nCells2 = (int)tmp.size();
+    int vT[8];
+    for (int k = 0; k < nvc; ++k) vT[k] = c->c2v[nvc * icg + k];
+    std::sort(vT, vT + nvc);
+    frac.resize(nCells2);
+    for (int i = 0; i < nCells2; ++i) {
+      int vT2[8];
+      for (int k = 0; k < nvc; ++k) vT2[k] = c->c2v[nvc * tmp[i] + k];
+      std::sort(vT2, vT2 + nvc);
+      int nCommon = 0, a = 0, b = 0;
+      while (a < nvc && b < nvc) {
+        if (vT[a] == vT2[b]) { nCommon++; a++; b++; }
+        else if (vT[a] < vT2[b]) a++;
+        else b++;
+      }
+      frac[i] = nCommon * iNVert;
+    }
+    if (nCells2 > 0) QuickSortRFREALInteger(frac.data(), tmp.data(), nCells2);
+    int degr = 0;
+    for (int icl2 = nCells2; icl2 >= std::max(nCells2 - stencilSizeMax + 1, 1); --icl2) c2cs[degr++] = tmp[icl2 - 1];
+    std::sort(c2cs.begin(), c2cs.begin() + degr);
+    layerBeg[1] = 1;
+    layerEnd[1] = degr;
+    int nLayers = 1;
+    for (int iLayer = 2; iLayer <= nLayersMax; ++iLayer) {
+      int sCount = 0;
+      if (degr >= stencilSizeMin) {
+        std::vector<double> a(degr * 4);
+        for (int isl = 0; isl < degr; ++isl) {
+          int j = c2cs[isl];
+          double dx = c->cofg[3 * j] - c->cofg[3 * icg];
+          double dy = c->cofg[3 * j + 1] - c->cofg[3 * icg + 1];
+          double dz = c->cofg[3 * j + 2] - c->cofg[3 * icg + 2];
+          double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+          a[isl] = term; a[isl + degr] = term * dx; a[isl + 2 * degr] = term * dy; a[isl + 3 * degr] = term * dz;
+        }
+        for (int col = 0; col < 4; ++col) {
+          double m = -1.79769313486231571e308;
+          for (int r = 0; r < degr; ++r) m = std::max(m, std::fabs(a[r + col * degr]));
+          for (int r = 0; r < degr; ++r) a[r + col * degr] = a[r + col * degr] / m;
+        }
+        sCount = svdSingularCount(degr, 4, a);
+      }
+      if (sCount != 0 || degr < stencilSizeMin) {
+        /* --- RFLU_AddCellLayer --- */
+        int beg = layerBeg[iLayer - 1], end = layerEnd[iLayer - 1];
+        std::vector<int> sorted(c2cs.begin(), c2cs.begin() + degr);
+        std::sort(sorted.begin(), sorted.end());
+        std::vector<int> help;
+        bool stop = false;
+        for (int isl = beg; isl <= end && !stop; ++isl) {
+          int m = c2cs[isl - 1];
+          for (int k = 0; k < nvc && !stop; ++k) {
+            int v = c->c2v[nvc * m + k];
+            for (int j = v2cOff[v]; j < v2cOff[v + 1]; ++j) {
+              int icg2 = v2c[j];
+              if (icg2 == icg) continue;
+              if (std::binary_search(sorted.begin(), sorted.end(), icg2)) continue;
+              if (std::binary_search(help.begin(), help.end(), icg2)) continue;
+              if ((int)help.size() < stencilSizeMax) {
+                help.push_back(icg2);
+                std::sort(help.begin(), help.end());
+              } else { stop = true; break; }
+            }
+          }
+        }
+        for (int h : help) if (degr < stencilSizeMax) c2cs[degr++] = h;
+        nLayers++;
+        layerBeg[iLayer] = layerEnd[iLayer - 1] + 1;
+        layerEnd[iLayer] = degr;
+      } else {
+        break;
+      }
+    }
+    (void)nLayers;
+    for (int i = 0; i < degr; ++i) c->stIdx.push_back(c2cs[i]);
+    c->stOff[icg + 1] = (int)c->stIdx.size();
+  }
+}
+
+/* RFLU_ComputeWtsC2C + RFLU_ComputeStencilMoments3D1
+ * (modflu/RFLU_ModWeights.F90:1025-1183, 1770-1915). moms[10*ic + k] in the
+ * order r11,r12,r22,r13,r23,r33,r14,r24,r34,r44 (XYZ_MOM_11..XYZ_MOM_44). */
+void buildMoments(orc_ctx *c) {
+  c->moms.assign(10 * c->nCells, 0.0);
+  for (int icg = 0; icg < c->nCells; ++icg) {
+    double *x = &c->moms[10 * icg];
+    for (int k = 0; k < 10; ++k) x[k] = 0.0;
+    for (int s = c->stOff[icg]; s < c->stOff[icg + 1]; ++s) {
+      int j = c->stIdx[s];
+      double dx = c->cofg[3 * j] - c->cofg[3 * icg];
+      double dy = c->cofg[3 * j + 1] - c->cofg[3 * icg + 1];
+      double dz = c->cofg[3 * j + 2] - c->cofg[3 * icg + 2];
+      double wt = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+      dx = wt * dx; dy = wt * dy; dz = wt * dz;
+      x[0] = x[0] + dx * dx; x[1] = x[1] + dx * dy; x[2] = x[2] + dy * dy;
+      x[3] = x[3] + dx * dz; x[4] = x[4] + dy * dz; x[5] = x[5] + dz * dz;
+      x[6] = x[6] + wt * dx; x[7] = x[7] + wt * dy; x[8] = x[8] + wt * dz; x[9] = x[9] + wt * wt;
+    }
+    double r11 = std::sqrt(x[0]);
+    double ir11 = 1.0 / r11;
+    double r12 = ir11 * x[1];
+    double r22 = std::sqrt(x[2] - r12 * r12);
+    double ir22 = 1.0 / r22;
+    double r13 = ir11 * x[3];
+    double r23 = ir22 * (x[4] - r12 * r13);
+    double r33 = std::sqrt(x[5] - (r13 * r13 + r23 * r23));
+    double ir33 = 1.0 / r33;
+    double r14 = ir11 * x[6];
+    double r24 = ir22 * (x[7] - r12 * r14);
+    double r34 = ir33 * (x[8] - (r13 * r14 + r23 * r24));
+    double r44 = std::sqrt(x[9] - (r14 * r14 + r24 * r24 + r34 * r34));
+    x[0] = r11; x[1] = r12; x[2] = r22; x[3] = r13; x[4] = r23; x[5] = r33;
+    x[6] = r14; x[7] = r24; x[8] = r34; x[9] = r44;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Dependent variables: RFLU_SetDependentVars TCPERF branch                  */
+/* (libflu/RFLU_SetDependentVars.F90:234-289) with gv from RFLU_SetGasVars   */
+/* (libflu/RFLU_SetGasVars.F90:173-178): R -> M = 8314.3/R -> R round trip.  */
+/* ------------------------------------------------------------------------ */
+void setDependentVars(orc_ctx *c, int ic) {
+  double gc = MixtPerf_R_M(c->gvMol);
+  double g = MixtPerf_G_CpR(c->gvCp, gc);
+  const double *cv = &c->cv[5 * ic];
+  double r = cv[0];
+  double ir = 1.0 / r;
+  double Eo = ir * cv[4];
+  double Vm2 = ir * ir * (cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3]);
+  double p = MixtPerf_P_DEoGVm2(r, Eo, g, Vm2);
+  double t = MixtPerf_T_DPR(r, p, gc);
+  c->dv[3 * ic] = p;
+  c->dv[3 * ic + 1] = t;
+  c->dv[3 * ic + 2] = MixtPerf_C_GRT(g, gc, t);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Gradients: RFLU_ComputeGradCellsFast_3D                                   */
+/* (modflu/RFLU_ModDifferentiationCells.F90:931-1178).                       */
+/* var = cv in DUVWP state (rho,u,v,w,p).                                    */
+/* ------------------------------------------------------------------------ */
+void computeGradCells(orc_ctx *c, const std::vector<double> &var, std::vector<double> &grad) {
+  for (int icg = 0; icg < c->nCells; ++icg) {
+    const double *m = &c->moms[10 * icg];
+    double r11 = m[0], r12 = m[1], r22 = m[2], r13 = m[3], r23 = m[4], r33 = m[5];
+    double c11 = 1.0 / r11, c22 = 1.0 / r22, c33 = 1.0 / r33;
+    double c12 = -c11 * r12;
+    double c13 = -(c11 * r13 + c12 * c22 * r23);
+    double c23 = -c22 * r23;
+    double c1111 = c11 * c11, c2222 = c22 * c22, c3333 = c33 * c33;
+    double *g = &grad[15 * icg];
+    for (int k = 0; k < 15; ++k) g[k] = 0.0;
+    const double xi = c->cofg[3 * icg], yi = c->cofg[3 * icg + 1], zi = c->cofg[3 * icg + 2];
+    for (int s = c->stOff[icg]; s < c->stOff[icg + 1]; ++s) {
+      int j = c->stIdx[s];
+      double dx = c->cofg[3 * j] - xi, dy = c->cofg[3 * j + 1] - yi, dz = c->cofg[3 * j + 2] - zi;
+      double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+      dx = term * dx; dy = term * dy; dz = term * dz;
+      double term1 = c1111 * (dx);
+      double term2 = c2222 * (dy + c12 * dx);
+      double term3 = c3333 * (dz + c23 * dy + c13 * dx);
+      double wtx = term * (term1 + c12 * term2 + c13 * term3);
+      double wty = term * (term2 + c23 * term3);
+      double wtz = term * (term3);
+      for (int iv = 0; iv < 5; ++iv) {
+        double dVar = var[5 * j + iv] - var[5 * icg + iv];
+        g[3 * iv] = g[3 * iv] + wtx * dVar;
+        g[3 * iv + 1] = g[3 * iv + 1] + wty * dVar;
+        g[3 * iv + 2] = g[3 * iv + 2] + wtz * dVar;
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Limiters: modflu/RFLU_ModLimiters.F90                                      */
+/* ------------------------------------------------------------------------ */
+/* RFLU_ComputeLimiterBarthJesp (:132-322); skipVel excludes vars 2..4. */
+void limiterBarthJesp(orc_ctx *c, const std::vector<double> &var, const std::vector<double> &grad,
+                      std::vector<double> &lim, bool skipVel) {
+  const int nc = c->nCells;
+  std::vector<double> vmin(var), vmax(var);
+  for (int k = 0; k < 5 * nc; ++k) lim[k] = 1.0;
+  auto limitVar = [&](int iv) { return !(skipVel && iv >= 1 && iv <= 3); };
+  for (int f = 0; f < c->nFaces; ++f) {
+    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+    for (int iv = 0; iv < 5; ++iv) {
+      if (!limitVar(iv)) continue;
+      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
+      vmin[5 * c1 + iv] = fmin2(vmin[5 * c1 + iv], v2);
+      vmin[5 * c2 + iv] = fmin2(vmin[5 * c2 + iv], v1);
+      vmax[5 * c1 + iv] = fmax2(vmax[5 * c1 + iv], v2);
+      vmax[5 * c2 + iv] = fmax2(vmax[5 * c2 + iv], v1);
+    }
+  }
+  for (int f = 0; f < c->nFaces; ++f) {
+    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+    double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
+    double dx1 = c->cofg[3 * c1] - xc, dy1 = c->cofg[3 * c1 + 1] - yc, dz1 = c->cofg[3 * c1 + 2] - zc;
+    double dx2 = c->cofg[3 * c2] - xc, dy2 = c->cofg[3 * c2 + 1] - yc, dz2 = c->cofg[3 * c2 + 2] - zc;
+    for (int iv = 0; iv < 5; ++iv) {
+      if (!limitVar(iv)) continue;
+      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
+      double d1min1 = vmin[5 * c1 + iv] - v1, d1max1 = vmax[5 * c1 + iv] - v1;
+      double d1min2 = vmin[5 * c2 + iv] - v2, d1max2 = vmax[5 * c2 + iv] - v2;
+      const double *g1 = &grad[15 * c1 + 3 * iv], *g2 = &grad[15 * c2 + 3 * iv];
+      double d21 = g1[0] * dx1 + g1[1] * dy1 + g1[2] * dz1;
+      double d22 = g2[0] * dx2 + g2[1] * dy2 + g2[2] * dz2;
+      double term;
+      if (d21 > 0.0) { term = fmin2(1.0, d1max1 / d21); lim[5 * c1 + iv] = fmin2(term, lim[5 * c1 + iv]); }
+      else if (d21 < 0.0) { term = fmin2(1.0, d1min1 / d21); lim[5 * c1 + iv] = fmin2(term, lim[5 * c1 + iv]); }
+      if (d22 > 0.0) { term = fmin2(1.0, d1max2 / d22); lim[5 * c2 + iv] = fmin2(term, lim[5 * c2 + iv]); }
+      else if (d22 < 0.0) { term = fmin2(1.0, d1min2 / d22); lim[5 * c2 + iv] = fmin2(term, lim[5 * c2 + iv]); }
+    }
+  }
+}
+
+/* RFLU_ComputeLimiterVenkat (:353-587). */
+void limiterVenkat(orc_ctx *c, const std::vector<double> &var, const std::vector<double> &grad,
+                   std::vector<double> &lim) {
+  const int nc = c->nCells;
+  const double THRD = 1.0 / 3.0, TINY = 1.0e-12, K = 1.0;
+  std::vector<double> vmin(var), vmax(var);
+  for (int k = 0; k < 5 * nc; ++k) lim[k] = 1.0;
+  for (int f = 0; f < c->nFaces; ++f) {
+    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+    for (int iv = 0; iv < 5; ++iv) {
+      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
+      vmin[5 * c1 + iv] = fmin2(vmin[5 * c1 + iv], v2);
+      vmin[5 * c2 + iv] = fmin2(vmin[5 * c2 + iv], v1);
+      vmax[5 * c1 + iv] = fmax2(vmax[5 * c1 + iv], v2);
+      vmax[5 * c2 + iv] = fmax2(vmax[5 * c2 + iv], v1);
+    }
+  }
+  auto venk = [&](double dmm, double d2, double epsq) {
+    double numer = (dmm * dmm + epsq) * d2 + 2 * d2 * d2 * dmm;
+    double denom = d2 * (dmm * dmm + 2 * d2 * d2 + dmm * d2 + epsq);
+    return numer / (denom + TINY);
+  };
+  for (int f = 0; f < c->nFaces; ++f) {
+    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+    double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
+    double dx1 = c->cofg[3 * c1] - xc, dy1 = c->cofg[3 * c1 + 1] - yc, dz1 = c->cofg[3 * c1 + 2] - zc;
+    double dx2 = c->cofg[3 * c2] - xc, dy2 = c->cofg[3 * c2 + 1] - yc, dz2 = c->cofg[3 * c2 + 2] - zc;
+    double ds1 = std::pow(c->vol[c1], THRD), ds2 = std::pow(c->vol[c2], THRD);
+    double epsq1 = (K * ds1) * (K * ds1) * (K * ds1);
+    double epsq2 = (K * ds2) * (K * ds2) * (K * ds2);
+    for (int iv = 0; iv < 5; ++iv) {
+      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
+      double d1min1 = vmin[5 * c1 + iv] - v1, d1max1 = vmax[5 * c1 + iv] - v1;
+      double d1min2 = vmin[5 * c2 + iv] - v2, d1max2 = vmax[5 * c2 + iv] - v2;
+      const double *g1 = &grad[15 * c1 + 3 * iv], *g2 = &grad[15 * c2 + 3 * iv];
+      double d21 = g1[0] * dx1 + g1[1] * dy1 + g1[2] * dz1;
+      double d22 = g2[0] * dx2 + g2[1] * dy2 + g2[2] * dz2;
+      if (d21 > 0.0) lim[5 * c1 + iv] = fmin2(venk(d1max1, d21, epsq1), lim[5 * c1 + iv]);
+      else if (d21 < 0.0) lim[5 * c1 + iv] = fmin2(venk(d1min1, d21, epsq1), lim[5 * c1 + iv]);
+      if (d22 > 0.0) lim[5 * c2 + iv] = fmin2(venk(d1max2, d22, epsq2), lim[5 * c2 + iv]);
+      else if (d22 < 0.0) lim[5 * c2 + iv] = fmin2(venk(d1min2, d22, epsq2), lim[5 * c2 + iv]);
+    }
+  }
+}
+
+/* RFLU_SymmetricEigen3 (:791-912): cyclic Jacobi on a symmetric 3x3,
+ * ascending eigenvalues, eigenvectors as columns.  m and vec column-major. */
+void symmetricEigen3(const double m[9], double vec[9], double val[3]) {
+  const int MAX_SWEEPS = 50;
+  const double EIG_TOL = 1.0e-24;
+  double r[9];
+  for (int k = 0; k < 9; ++k) r[k] = m[k];
+#define R(i, j) r[((i)-1) + 3 * ((j)-1)]
+#define V(i, j) vec[((i)-1) + 3 * ((j)-1)]
+  for (int k = 0; k < 9; ++k) vec[k] = 0.0;
+  for (int i = 1; i <= 3; ++i) V(i, i) = 1.0;
+  double total = 0.0;
+  for (int k = 0; k < 9; ++k) total = total + r[k] * r[k];
+  for (int sweep = 1; sweep <= MAX_SWEEPS; ++sweep) {
+    double offDiag = R(1, 2) * R(1, 2) + R(1, 3) * R(1, 3) + R(2, 3) * R(2, 3);
+    if (offDiag <= EIG_TOL * total) break;
+    for (int ip = 1; ip <= 2; ++ip)
+      for (int iq = ip + 1; iq <= 3; ++iq) {
+        if (R(ip, iq) != 0.0) {
+          double theta = (R(iq, iq) - R(ip, ip)) / (2.0 * R(ip, iq));
+          double tangent;
+          if (std::fabs(theta) > 1.0e150) tangent = 0.5 / theta;
+          else tangent = std::copysign(1.0, theta) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+          double cosine = 1.0 / std::sqrt(tangent * tangent + 1.0);
+          double sine = tangent * cosine;
+          int ir = 6 - ip - iq;
+          double arp = R(ir, ip), arq = R(ir, iq);
+          R(ip, ip) = R(ip, ip) - tangent * R(ip, iq);
+          R(iq, iq) = R(iq, iq) + tangent * R(ip, iq);
+          R(ip, iq) = 0.0;
+          R(iq, ip) = 0.0;
+          R(ir, ip) = cosine * arp - sine * arq;
+          R(ip, ir) = R(ir, ip);
+          R(ir, iq) = sine * arp + cosine * arq;
+          R(iq, ir) = R(ir, iq);
+          for (int i = 1; i <= 3; ++i) {
+            double vp = V(i, ip), vq = V(i, iq);
+            V(i, ip) = cosine * vp - sine * vq;
+            V(i, iq) = sine * vp + cosine * vq;
+          }
+        }
+      }
+  }
+  for (int i = 1; i <= 3; ++i) val[i - 1] = R(i, i);
+  for (int i = 1; i <= 2; ++i) {
+    int iMin = i;
+    for (int k = i + 1; k <= 3; ++k) if (val[k - 1] < val[iMin - 1]) iMin = k;
+    if (iMin != i) {
+      std::swap(val[i - 1], val[iMin - 1]);
+      for (int k = 1; k <= 3; ++k) std::swap(V(k, i), V(k, iMin));
+    }
+  }
+#undef R
+#undef V
+}
+
+/* RFLU_LimitGradVelocityBarthJesp (:588-790). gradVel(iComp,dir) = grad(dir, 2+iComp). */
+void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std::vector<double> &grad,
+                                std::vector<double> &lim) {
+  const int nc = c->nCells;
+  const double EQUAL_EIG_TOL = 1.0e-3;
+  std::vector<double> axes(9 * nc), eig(3 * nc), alpha(3 * nc, 1.0), dmin(3 * nc, 0.0), dmax(3 * nc, 0.0);
+  auto gv = [&](int ic, int i, int j) -> double & { return grad[15 * ic + 3 * (1 + (i - 1)) + (j - 1)]; };
+  for (int ic = 0; ic < nc; ++ic) {
+    double S[9];
+    for (int i = 1; i <= 3; ++i)
+      for (int j = 1; j <= 3; ++j) S[(i - 1) + 3 * (j - 1)] = 0.5 * (gv(ic, i, j) + gv(ic, j, i));
+    symmetricEigen3(S, &axes[9 * ic], &eig[3 * ic]);
+  }
+  for (int f = 0; f < c->nFaces; ++f) {
+    int cc[2] = {c->f2c[2 * f], c->f2c[2 * f + 1]};
+    double du[3];
+    for (int k = 0; k < 3; ++k) du[k] = var[5 * cc[1] + 1 + k] - var[5 * cc[0] + 1 + k];
+    for (int side = 0; side < 2; ++side) {
+      int icl = cc[side];
+      for (int j = 0; j < 3; ++j) {
+        const double *a = &axes[9 * icl + 3 * j];
+        double proj = 0.0;
+        proj = proj + a[0] * du[0]; proj = proj + a[1] * du[1]; proj = proj + a[2] * du[2];
+        if (side == 1) proj = -proj;
+        dmin[3 * icl + j] = fmin2(dmin[3 * icl + j], proj);
+        dmax[3 * icl + j] = fmax2(dmax[3 * icl + j], proj);
+      }
+    }
+  }
+  for (int f = 0; f < c->nFaces; ++f) {
+    for (int side = 0; side < 2; ++side) {
+      int icl = c->f2c[2 * f + side];
+      double off[3];
+      for (int k = 0; k < 3; ++k) off[k] = c->cofg[3 * icl + k] - c->fc[3 * f + k];
+      double shift[3];
+      for (int i = 1; i <= 3; ++i) {
+        double s = 0.0;
+        for (int k = 1; k <= 3; ++k) s = s + gv(icl, i, k) * off[k - 1];
+        shift[i - 1] = s;
+      }
+      for (int j = 0; j < 3; ++j) {
+        const double *a = &axes[9 * icl + 3 * j];
+        double proj = 0.0;
+        proj = proj + a[0] * shift[0]; proj = proj + a[1] * shift[1]; proj = proj + a[2] * shift[2];
+        if (proj > 0.0) alpha[3 * icl + j] = fmin2(alpha[3 * icl + j], dmax[3 * icl + j] / proj);
+        else if (proj < 0.0) alpha[3 * icl + j] = fmin2(alpha[3 * icl + j], dmin[3 * icl + j] / proj);
+      }
+    }
+  }
+  for (int ic = 0; ic < nc; ++ic) {
+    double *e = &eig[3 * ic], *al = &alpha[3 * ic];
+    double mx = std::fabs(e[0]);
+    mx = fmax2(mx, std::fabs(e[1])); mx = fmax2(mx, std::fabs(e[2]));
+    double eigScale = EQUAL_EIG_TOL * mx;
+    bool eq12 = (e[1] - e[0] <= eigScale), eq23 = (e[2] - e[1] <= eigScale);
+    if (eq12 && eq23) {
+      double m = fmin2(fmin2(al[0], al[1]), al[2]);
+      al[0] = al[1] = al[2] = m;
+    } else if (eq12) {
+      double m = fmin2(al[0], al[1]); al[0] = al[1] = m;
+    } else if (eq23) {
+      double m = fmin2(al[1], al[2]); al[1] = al[2] = m;
+    }
+  }
+  for (int ic = 0; ic < nc; ++ic) {
+    const double *A = &axes[9 * ic];
+    double G[3][3], Rm[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) G[i][j] = gv(ic, i + 1, j + 1);
+    /* rotated = MATMUL(TRANSPOSE(axes), gradVel) */
+    for (int j = 0; j < 3; ++j)
+      for (int col = 0; col < 3; ++col) {
+        double s = 0.0;
+        for (int i = 0; i < 3; ++i) s = s + A[i + 3 * j] * G[i][col];
+        Rm[j][col] = s;
+      }
+    for (int j = 0; j < 3; ++j)
+      for (int col = 0; col < 3; ++col) Rm[j][col] = alpha[3 * ic + j] * Rm[j][col];
+    /* gradVel = MATMUL(axes, rotated) */
+    for (int i = 0; i < 3; ++i)
+      for (int col = 0; col < 3; ++col) {
+        double s = 0.0;
+        for (int j = 0; j < 3; ++j) s = s + A[i + 3 * j] * Rm[j][col];
+        gv(ic, i + 1, col + 1) = s;
+      }
+    lim[5 * ic + 1] = lim[5 * ic + 2] = lim[5 * ic + 3] = 1.0;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* CellGradientsMP (libfloflu/CellGradientsMP.F90:160-295).  Works on c->cv  */
+/* in place, as the reference does (cons -> prim -> cons round trip).        */
+/* ------------------------------------------------------------------------ */
+void cellGradients(orc_ctx *c) {
+  if (c->num.spaceOrder <= 1) return;
+  const int nc = c->nCells;
+  /* RFLU_ConvertCvCons2Prim, DUVWP (modflu/RFLU_ModConvertCv.F90:124-397) */
+  for (int ic = 0; ic < nc; ++ic) {
+    double *cv = &c->cv[5 * ic];
+    double ir = 1.0 / cv[0];
+    cv[1] = ir * cv[1];
+    cv[2] = ir * cv[2];
+    cv[3] = ir * cv[3];
+    cv[4] = c->dv[3 * ic];
+  }
+  computeGradCells(c, c->cv, c->grad);
+  switch (c->num.reconst) {
+  case 0: break;
+  case 10:
+    limiterBarthJesp(c, c->cv, c->grad, c->lim, true);
+    limitGradVelocityBarthJesp(c, c->cv, c->grad, c->lim);
+    break;
+  case 100: limiterBarthJesp(c, c->cv, c->grad, c->lim, false); break;
+  case 11: limiterVenkat(c, c->cv, c->grad, c->lim); break;
+  default: std::fprintf(stderr, "oracle: RECONST %d not supported\n", c->num.reconst); std::abort();
+  }
+  if (c->num.reconst != 0) {
+    /* RFLU_LimitGradCells (RFLU_ModLimiters.F90:1061-1146) */
+    for (int ic = 0; ic < nc; ++ic)
+      for (int iv = 0; iv < 5; ++iv) {
+        double l = c->lim[5 * ic + iv];
+        double *g = &c->grad[15 * ic + 3 * iv];
+        g[0] = l * g[0]; g[1] = l * g[1]; g[2] = l * g[2];
+      }
+  }
+  /* RFLU_ConvertCvPrim2Cons (RFLU_ModConvertCv.F90:545-575) */
+  double gc = MixtPerf_R_M(c->gvMol), g = MixtPerf_G_CpR(c->gvCp, gc);
+  for (int ic = 0; ic < nc; ++ic) {
+    double *cv = &c->cv[5 * ic];
+    double r = cv[0], u = cv[1], v = cv[2], w = cv[3], p = c->dv[3 * ic];
+    /* cv(ENER) = r*Eo(r,g,p,u,v,w) on the primitive velocities */
+    cv[1] = r * u;
+    cv[2] = r * v;
+    cv[3] = r * w;
+    /* With PICL compiled in and not used, the energy slot keeps p (:567-571). */
+    if (!c->num.piclBuild) cv[4] = r * MixtPerf_Eo_DGPUVW(r, g, p, u, v, w);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Interior face fluxes                                                      */
+/* ------------------------------------------------------------------------ */
+struct FaceState { double r, u, v, w, p; };
+
+/* 2nd-order reconstruction common to the *_ComputeFlux2_TCP routines:
+ * primitive from cv (ul = mom*irl), p from dv, plus grad . (fc - cofg). */
+FaceState reconstruct(orc_ctx *c, int ic, double xc, double yc, double zc) {
+  const double *cv = &c->cv[5 * ic];
+  FaceState s;
+  s.r = cv[0];
+  double ir = 1.0 / s.r;
+  s.u = cv[1] * ir; s.v = cv[2] * ir; s.w = cv[3] * ir;
+  s.p = c->dv[3 * ic];
+  double dx = xc - c->cofg[3 * ic], dy = yc - c->cofg[3 * ic + 1], dz = zc - c->cofg[3 * ic + 2];
+  const double *g = &c->grad[15 * ic];
+  s.r = s.r + g[0] * dx + g[1] * dy + g[2] * dz;
+  s.u = s.u + g[3] * dx + g[4] * dy + g[5] * dz;
+  s.v = s.v + g[6] * dx + g[7] * dy + g[8] * dz;
+  s.w = s.w + g[9] * dx + g[10] * dy + g[11] * dz;
+  s.p = s.p + g[12] * dx + g[13] * dy + g[14] * dz;
+  return s;
+}
+
+/* Roe flux with the Harten-Hyman entropy fix: RFLU_ROE_ComputeFlux1_TCP
+ * (modflu/RFLU_ModRoeFlux.F90:1683-1942) and ..._Flux2_TCP (:2513-2867).
+ * Returns flx = flxConv - flxDiss. */
+void roeFlux(orc_ctx *c, double nx, double ny, double nz, double nm, double fs, double rl, double ul, double vl,
+             double wl, double pl, double Hl, double rr, double ur, double vr, double wr, double pr, double Hr,
+             double flx[5]) {
+  const double g = c->refGamma, epsentr = c->num.epsEntr, dissFact = c->num.dissFact;
+  double ql = ul * nx + vl * ny + wl * nz - fs;
+  double qr = ur * nx + vr * ny + wr * nz - fs;
+  double rh = std::sqrt(rl * rr);
+  double wt = rl / (rl + rh);
+  double uh = wt * ul + (1.0 - wt) * ur;
+  double vh = wt * vl + (1.0 - wt) * vr;
+  double wh = wt * wl + (1.0 - wt) * wr;
+  double Hh = wt * Hl + (1.0 - wt) * Hr;
+  double qh = uh * nx + vh * ny + wh * nz - fs;
+  double sh = 0.5 * (uh * uh + vh * vh + wh * wh);
+  double ah = MixtPerf_C_GHoVm2(g, Hh, 2.0 * sh);
+  double l1 = std::fabs(qh - ah), l2 = std::fabs(qh), l5 = std::fabs(qh + ah);
+  double efc = epsentr * l5;
+  l1 = EntropyFixHartenHyman(l1, efc);
+  l2 = EntropyFixHartenHyman(l2, efc);
+  l5 = EntropyFixHartenHyman(l5, efc);
+  double dr = rr - rl, du = ur - ul, de = vr - vl, dw = wr - wl, dp = pr - pl;
+  double dq = du * nx + de * ny + dw * nz;
+  double dv1 = (dp - rh * ah * dq) / (2.0 * ah * ah);
+  double dv5 = (dp + rh * ah * dq) / (2.0 * ah * ah);
+  double dv2 = dr - dp / (ah * ah);
+  double t1 = l1 * dv1, t2 = l2 * dv2, t3 = l2 * rh, t5 = l5 * dv5;
+  double fc1 = 0.5 * (ql * rl + qr * rr) * nm;
+  double fc2 = 0.5 * (ql * rl * ul + pl * nx + qr * rr * ur + pr * nx) * nm;
+  double fc3 = 0.5 * (ql * rl * vl + pl * ny + qr * rr * vr + pr * ny) * nm;
+  double fc4 = 0.5 * (ql * rl * wl + pl * nz + qr * rr * wr + pr * nz) * nm;
+  double fc5 = 0.5 * (ql * rl * Hl + pl * fs + qr * rr * Hr + pr * fs) * nm;
+  double fd1 = 0.5 * dissFact * (t1 + t2 + t5) * nm;
+  double fd2 = 0.5 * dissFact * (t1 * (uh - nx * ah) + t2 * uh + t3 * (du - nx * dq) + t5 * (uh + nx * ah)) * nm;
+  double fd3 = 0.5 * dissFact * (t1 * (vh - ny * ah) + t2 * vh + t3 * (de - ny * dq) + t5 * (vh + ny * ah)) * nm;
+  double fd4 = 0.5 * dissFact * (t1 * (wh - nz * ah) + t2 * wh + t3 * (dw - nz * dq) + t5 * (wh + nz * ah)) * nm;
+  double fd5 = 0.5 * dissFact *
+               (t1 * (Hh - qh * ah) + t2 * sh + t3 * (uh * du + vh * de + wh * dw - qh * dq) + t5 * (Hh + qh * ah)) * nm;
+  flx[0] = fc1 - fd1; flx[1] = fc2 - fd2; flx[2] = fc3 - fd3; flx[3] = fc4 - fd4; flx[4] = fc5 - fd5;
+}
+
+/* HLLC: RFLU_HLLC_ComputeFlux1_TCP (modflu/RFLU_ModHLLCFlux.F90:926-1194) and
+ * ..._Flux2_TCP (:2131-2434).  el, al, Hl as computed by the caller. */
+void hllcFlux(orc_ctx *c, double nx, double ny, double nz, double nm, double fs, double rl, double ul, double vl,
+              double wl, double pl, double el, double al, double Hl, double rr, double ur, double vr, double wr,
+              double pr, double er, double ar, double Hr, double flx[5]) {
+  const double g = c->refGamma;
+  double ql = ul * nx + vl * ny + wl * nz - fs;
+  double qr = ur * nx + vr * ny + wr * nz - fs;
+  double wt1 = std::sqrt(rr / rl);
+  double wt2 = 1.0 / (1.0 + wt1);
+  double us = wt2 * (ul + wt1 * ur);
+  double vs = wt2 * (vl + wt1 * vr);
+  double ws = wt2 * (wl + wt1 * wr);
+  double qs = wt2 * (ql + wt1 * qr);
+  double Hs = wt2 * (Hl + wt1 * Hr);
+  double Vms = us * us + vs * vs + ws * ws;
+  double as = MixtPerf_C_GHoVm2(g, Hs, Vms);
+  double sl = fmin2(ql - al, qs - as);
+  double sr = fmax2(qr + ar, qs + as);
+  if (sl > 0.0) {
+    flx[0] = ql * rl * nm;
+    flx[1] = (ql * rl * ul + pl * nx) * nm;
+    flx[2] = (ql * rl * vl + pl * ny) * nm;
+    flx[3] = (ql * rl * wl + pl * nz) * nm;
+    flx[4] = (ql * (rl * el + pl) + pl * fs) * nm;
+  } else if (sr < 0.0) {
+    flx[0] = qr * rr * nm;
+    flx[1] = (qr * rr * ur + pr * nx) * nm;
+    flx[2] = (qr * rr * vr + pr * ny) * nm;
+    flx[3] = (qr * rr * wr + pr * nz) * nm;
+    flx[4] = (qr * (rr * er + pr) + pr * fs) * nm;
+  } else {
+    double sm = (rr * qr * (sr - qr) - rl * ql * (sl - ql) - pr + pl) / (rr * (sr - qr) - rl * (sl - ql));
+    double ps = pl + rl * (ql - sl) * (ql - sm);
+    double rs, rus, rvs, rws, res;
+    if (sm > 0.0) {
+      double term = 1.0 / (sl - sm);
+      rs = term * (sl - ql) * rl;
+      rus = term * ((sl - ql) * rl * ul + (ps - pl) * nx);
+      rvs = term * ((sl - ql) * rl * vl + (ps - pl) * ny);
+      rws = term * ((sl - ql) * rl * wl + (ps - pl) * nz);
+      res = term * ((sl - ql) * rl * el + (ps * sm - pl * ql));
+    } else {
+      double term = 1.0 / (sr - sm);
+      rs = term * (sr - qr) * rr;
+      rus = term * ((sr - qr) * rr * ur + (ps - pr) * nx);
+      rvs = term * ((sr - qr) * rr * vr + (ps - pr) * ny);
+      rws = term * ((sr - qr) * rr * wr + (ps - pr) * nz);
+      res = term * ((sr - qr) * rr * er + (ps * sm - pr * qr));
+    }
+    flx[0] = sm * rs * nm;
+    flx[1] = (sm * rus + ps * nx) * nm;
+    flx[2] = (sm * rvs + ps * ny) * nm;
+    flx[3] = (sm * rws + ps * nz) * nm;
+    flx[4] = (sm * (res + ps) - ps * fs) * nm;
+  }
+}
+
+/* AUSM+: RFLU_AUSM_FluxFunction (modflu/RFLU_ModAUSMFlux.F90:282-416). */
+void ausmFlux(double nx, double ny, double nz, double nm, double fs, double rl, double ul, double vl, double wl,
+              double pl, double Hl, double al, double rr, double ur, double vr, double wr, double pr, double Hr,
+              double ar, double flx[5]) {
+  double ql = ul * nx + vl * ny + wl * nz - fs;
+  double qr = ur * nx + vr * ny + wr * nz - fs;
+  double af = 0.5 * (al + ar);
+  double ml = ql / af, mla = std::fabs(ml);
+  double mr = qr / af, mra = std::fabs(mr);
+  double mlp, wtl, mrm, wtr;
+  if (mla <= 1.0) {
+    mlp = 0.25 * (ml + 1.0) * (ml + 1.0) + 0.125 * (ml * ml - 1.0) * (ml * ml - 1.0);
+    wtl = 0.25 * (ml + 1.0) * (ml + 1.0) * (2.0 - ml) + 0.1875 * ml * (ml * ml - 1.0) * (ml * ml - 1.0);
+  } else {
+    mlp = 0.5 * (ml + mla);
+    wtl = 0.5 * (1.0 + ml / mla);
+  }
+  if (mra <= 1.0) {
+    mrm = -0.25 * (mr - 1.0) * (mr - 1.0) - 0.125 * (mr * mr - 1.0) * (mr * mr - 1.0);
+    wtr = 0.25 * (mr - 1.0) * (mr - 1.0) * (2.0 + mr) - 0.1875 * mr * (mr * mr - 1.0) * (mr * mr - 1.0);
+  } else {
+    mrm = 0.5 * (mr - mra);
+    wtr = 0.5 * (1.0 - mr / mra);
+  }
+  double mf = mlp + mrm, mfa = std::fabs(mf);
+  double mfp = 0.5 * (mf + mfa), mfm = 0.5 * (mf - mfa);
+  double pf = wtl * pl + wtr * pr;
+  flx[0] = (af * (mfp * rl + mfm * rr)) * nm;
+  flx[1] = (af * (mfp * rl * ul + mfm * rr * ur) + pf * nx) * nm;
+  flx[2] = (af * (mfp * rl * vl + mfm * rr * vr) + pf * ny) * nm;
+  flx[3] = (af * (mfp * rl * wl + mfm * rr * wr) + pf * nz) * nm;
+  flx[4] = (af * (mfp * rl * Hl + mfm * rr * Hr) + pf * fs) * nm;
+}
+
+void interiorFlux(orc_ctx *c, int f, double flx[5]) {
+  const int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+  const double nx = c->fn[4 * f], ny = c->fn[4 * f + 1], nz = c->fn[4 * f + 2], nm = c->fn[4 * f + 3];
+  const double fs = 0.0;
+  const double cp = c->refCp, g = c->refGamma;
+  const int disc = c->num.spaceDiscr;
+  if (c->num.spaceOrder == 1) {
+    const double *cl = &c->cv[5 * c1], *cr = &c->cv[5 * c2];
+    double rl = cl[0], irl = 1.0 / rl, ul = cl[1] * irl, vl = cl[2] * irl, wl = cl[3] * irl;
+    double rr = cr[0], irr = 1.0 / rr, ur = cr[1] * irr, vr = cr[2] * irr, wr = cr[3] * irr;
+    double pl = c->dv[3 * c1], pr = c->dv[3 * c2];
+    if (disc == 1) {
+      double tl = c->dv[3 * c1 + 1], tr = c->dv[3 * c2 + 1];
+      double Hl = MixtPerf_Ho_CpTUVW(cp, tl, ul, vl, wl), Hr = MixtPerf_Ho_CpTUVW(cp, tr, ur, vr, wr);
+      roeFlux(c, nx, ny, nz, nm, fs, rl, ul, vl, wl, pl, Hl, rr, ur, vr, wr, pr, Hr, flx);
+    } else if (disc == 3) {
+      double el = cl[4] * irl, er = cr[4] * irr;
+      double al = c->dv[3 * c1 + 2], ar = c->dv[3 * c2 + 2];
+      double Hl = el + irl * pl, Hr = er + irr * pr;
+      hllcFlux(c, nx, ny, nz, nm, fs, rl, ul, vl, wl, pl, el, al, Hl, rr, ur, vr, wr, pr, er, ar, Hr, flx);
+    } else {
+      /* RFLU_AUSM_ComputeFlux1 (RFLU_ModAUSMFlux.F90:550-1027) */
+      double al = c->dv[3 * c1 + 2], ar = c->dv[3 * c2 + 2];
+      double Hl = cl[4] * irl + pl / rl, Hr = cr[4] * irr + pr / rr;
+      ausmFlux(nx, ny, nz, nm, fs, rl, ul, vl, wl, pl, Hl, al, rr, ur, vr, wr, pr, Hr, ar, flx);
+    }
+    return;
+  }
+  const double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
+  FaceState L = reconstruct(c, c1, xc, yc, zc);
+  FaceState Rr = reconstruct(c, c2, xc, yc, zc);
+  if (disc == 1) {
+    double gc = MixtPerf_R_CpG(cp, g);
+    double tl = MixtPerf_T_DPR(L.r, L.p, gc), Hl = MixtPerf_Ho_CpTUVW(cp, tl, L.u, L.v, L.w);
+    double tr = MixtPerf_T_DPR(Rr.r, Rr.p, gc), Hr = MixtPerf_Ho_CpTUVW(cp, tr, Rr.u, Rr.v, Rr.w);
+    roeFlux(c, nx, ny, nz, nm, fs, L.r, L.u, L.v, L.w, L.p, Hl, Rr.r, Rr.u, Rr.v, Rr.w, Rr.p, Hr, flx);
+  } else if (disc == 3) {
+    double irl = 1.0 / c->cv[5 * c1], irr = 1.0 / c->cv[5 * c2];
+    double el = MixtPerf_Eo_DGPUVW(L.r, g, L.p, L.u, L.v, L.w), al = MixtPerf_C_DGP(L.r, g, L.p);
+    double er = MixtPerf_Eo_DGPUVW(Rr.r, g, Rr.p, Rr.u, Rr.v, Rr.w), ar = MixtPerf_C_DGP(Rr.r, g, Rr.p);
+    /* Hl = el + irl*pl with irl the inverse of the cell (unreconstructed) density */
+    double Hl = el + irl * L.p, Hr = er + irr * Rr.p;
+    hllcFlux(c, nx, ny, nz, nm, fs, L.r, L.u, L.v, L.w, L.p, el, al, Hl, Rr.r, Rr.u, Rr.v, Rr.w, Rr.p, er, ar, Hr,
+             flx);
+  } else {
+    double gc = MixtPerf_R_CpG(cp, g);
+    double tl = MixtPerf_T_DPR(L.r, L.p, gc), al = MixtPerf_C_GRT(g, gc, tl);
+    double Hl = MixtPerf_Ho_CpTUVW(cp, tl, L.u, L.v, L.w);
+    double tr = MixtPerf_T_DPR(Rr.r, Rr.p, gc), ar = MixtPerf_C_GRT(g, gc, tr);
+    double Hr = MixtPerf_Ho_CpTUVW(cp, tr, Rr.u, Rr.v, Rr.w);
+    ausmFlux(nx, ny, nz, nm, fs, L.r, L.u, L.v, L.w, L.p, Hl, al, Rr.r, Rr.u, Rr.v, Rr.w, Rr.p, Hr, ar, flx);
+  }
+}
+
+/* BcondOutflowPerf (libfloflu/BcondOutflowPerf.F90:88-159). */
+void bcondOutflowPerf(int bcOpt, double pout, double sxn, double syn, double szn, double cpgas, double mol,
+                      double rho, double rhou, double rhov, double rhow, double rhoe, double press, double &rhob,
+                      double &rhoub, double &rhovb, double &rhowb, double &rhoeb) {
+  double rgas = MixtPerf_R_M(mol);
+  double gamma = MixtPerf_G_CpR(cpgas, rgas);
+  double u = rhou / rho, v = rhov / rho, w = rhow / rho;
+  double csound = MixtPerf_C_DGP(rho, gamma, press);
+  double mach = std::sqrt(u * u + v * v + w * w) / csound;
+  if (mach < 1.0 && (bcOpt == 1 || bcOpt == 2)) {
+    double rrhoc = 1.0 / (rho * csound);
+    double deltp = press - pout;
+    rhob = rho - deltp / (csound * csound);
+    double ub = u + sxn * deltp * rrhoc;
+    double vb = v + syn * deltp * rrhoc;
+    double wb = w + szn * deltp * rrhoc;
+    double vnd = ub * sxn + vb * syn + wb * szn;
+    if (vnd < 0.0) {
+      ub = std::copysign(1.0, u) * fmax2(std::fabs(ub), std::fabs(u));
+      vb = std::copysign(1.0, v) * fmax2(std::fabs(vb), std::fabs(v));
+      wb = std::copysign(1.0, w) * fmax2(std::fabs(wb), std::fabs(w));
+    }
+    rhoub = rhob * ub; rhovb = rhob * vb; rhowb = rhob * wb;
+    rhoeb = rhob * MixtPerf_Eo_DGPUVW(rhob, gamma, pout, ub, vb, wb);
+  } else {
+    rhob = rho; rhoub = rhou; rhovb = rhov; rhowb = rhow; rhoeb = rhoe;
+  }
+}
+
+/* Patch flux of one boundary face: RFLU_CentralFirstPatch
+ * (rocflu/RFLU_CentralFirstPatch.F90:571-911) and RFLU_CentralSecondPatch
+ * (rocflu/RFLU_CentralSecondPatch.F90:634-1029), slip wall and outflow. */
+void patchFlux(orc_ctx *c, const Patch &p, int i, double flx[5]) {
+  const int c1 = p.bf2c[i];
+  const double nx = p.fn[4 * i], ny = p.fn[4 * i + 1], nz = p.fn[4 * i + 2], nm = p.fn[4 * i + 3];
+  const double fs = 0.0;
+  const double *cv = &c->cv[5 * c1];
+  flx[0] = 0.0;
+  if (p.order == 1) {
+    double rl = cv[0], rul = cv[1], rvl = cv[2], rwl = cv[3], rel = cv[4], pl = c->dv[3 * c1];
+    if (p.bcType == ORC_BC_SLIPWALL) {
+      flx[1] = pl * nx * nm; flx[2] = pl * ny * nm; flx[3] = pl * nz * nm; flx[4] = pl * fs * nm;
+      return;
+    }
+    double pr = (p.outflowType != 0) ? p.pOut : pl;
+    double rr, rur, rvr, rwr, rer;
+    bcondOutflowPerf(p.outflowType, pr, nx, ny, nz, c->gvCp, c->gvMol, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr,
+                     rwr, rer);
+    double ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
+    double qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
+    flx[0] = 0.5 * (ql * rl + qr * rr) * nm;
+    flx[1] = 0.5 * (ql * rul + pl * nx + qr * rur + pr * nx) * nm;
+    flx[2] = 0.5 * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
+    flx[3] = 0.5 * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
+    flx[4] = 0.5 * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+    return;
+  }
+  const double xc = p.fc[3 * i], yc = p.fc[3 * i + 1], zc = p.fc[3 * i + 2];
+  FaceState L = reconstruct(c, c1, xc, yc, zc);
+  double rl = L.r, ul = L.u, vl = L.v, wl = L.w, pl = L.p;
+  double rul = rl * ul, rvl = rl * vl, rwl = rl * wl;
+  if (p.bcType == ORC_BC_SLIPWALL) {
+    flx[1] = pl * nx * nm; flx[2] = pl * ny * nm; flx[3] = pl * nz * nm; flx[4] = pl * fs * nm;
+    return;
+  }
+  double pr = (p.outflowType != 0) ? p.pOut : pl;
+  double rgas = MixtPerf_R_M(c->gvMol), g = MixtPerf_G_CpR(c->gvCp, rgas);
+  double rel = rl * MixtPerf_Eo_DGPUVW(rl, g, pl, ul, vl, wl);
+  double rr, rur, rvr, rwr, rer;
+  bcondOutflowPerf(p.outflowType, pr, nx, ny, nz, c->gvCp, c->gvMol, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr,
+                   rer);
+  double ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
+  double qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
+  flx[0] = 0.5 * (ql * rl + qr * rr) * nm;
+  flx[1] = 0.5 * (ql * rul + pl * nx + qr * rur + pr * nx) * nm;
+  flx[2] = 0.5 * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
+  flx[3] = 0.5 * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
+  flx[4] = 0.5 * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+}
+
+/* ConvectiveFluxes (libfloflu/ConvectiveFluxes.F90:120-175): rhs = -diss,
+ * interior face loop with the +/- scatter, then the patch loop. */
+void convectiveFluxes(orc_ctx *c) {
+  const int nc = c->nCells;
+  for (int k = 0; k < 5 * nc; ++k) c->rhs[k] = -c->diss[k];
+  double flx[5];
+  for (int f = 0; f < c->nFaces; ++f) {
+    interiorFlux(c, f, flx);
+    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+    for (int k = 0; k < 5; ++k) c->rhs[5 * c1 + k] = c->rhs[5 * c1 + k] + flx[k];
+    for (int k = 0; k < 5; ++k) c->rhs[5 * c2 + k] = c->rhs[5 * c2 + k] - flx[k];
+  }
+  for (const Patch &p : c->patches) {
+    for (int i = 0; i < p.n; ++i) {
+      patchFlux(c, p, i, flx);
+      int c1 = p.bf2c[i];
+      int k0 = (p.bcType == ORC_BC_SLIPWALL) ? 1 : 0;
+      for (int k = k0; k < 5; ++k) c->rhs[5 * c1 + k] = c->rhs[5 * c1 + k] + flx[k];
+    }
+  }
+}
+
+/* RkInitGeneric (libfloflu/RkInitGeneric.F90:120-170). */
+void rkInit(orc_ctx *c, int iStage) {
+  const int n = 5 * c->nCells;
+  if (c->num.rkScheme == 1 && iStage != 1) {
+    for (int k = 0; k < n; ++k) c->diss[k] = 0.0;
+  } else {
+    for (int k = 0; k < n; ++k) { c->cvOld[k] = c->cv[k]; c->diss[k] = 0.0; }
+  }
+}
+
+/* RkUpdateGeneric, static grid (libfloflu/RkUpdateGeneric.F90:257-322). */
+void rkUpdate(orc_ctx *c, int iStage, double dtMin) {
+  const double fac = c->ark[iStage - 1] * dtMin;
+  const double grk = c->grk[iStage - 1];
+  for (int ic = 0; ic < c->nCells; ++ic) {
+    double adtv = fac / c->vol[ic];
+    for (int iv = 0; iv < 5; ++iv) {
+      int k = 5 * ic + iv;
+      switch (c->num.rkScheme) {
+      case 1:
+        if (iStage == 1) { c->cv[k] = c->cvOld[k] - adtv * c->rhs[k]; c->rhsSum[k] = c->rhs[k]; }
+        else if (iStage == c->nrkSteps) c->cv[k] = c->cvOld[k] - adtv * (c->rhs[k] + c->rhsSum[k]);
+        else { c->cv[k] = c->cvOld[k] - adtv * c->rhs[k]; c->rhsSum[k] = c->rhsSum[k] + grk * c->rhs[k]; }
+        break;
+      case 2:
+        if (iStage == 1) { c->cv[k] = c->cvOld[k] - adtv * c->rhs[k]; c->rhsSum[k] = c->rhs[k]; }
+        else if (iStage == 2) {
+          c->cv[k] = c->cvOld[k] - adtv * (c->rhs[k] - grk * c->rhsSum[k]);
+          c->rhsSum[k] = c->rhs[k];
+        } else c->cv[k] = c->cvOld[k] - adtv * (c->rhs[k] - grk * c->rhsSum[k]);
+        break;
+      default: c->cv[k] = c->cvOld[k] - adtv * c->rhs[k];
+      }
+    }
+  }
+}
+
+/* AfterUpdateMP (libfloflu/AfterUpdateMP.F90:134-136): RFLU_CheckValidity
+ * (libflu/RFLU_CheckValidity.F90:165-214), RFLU_EnforceBounds
+ * (libflu/RFLU_EnforceBounds.F90:165-230), RFLU_CheckPositivity
+ * (libflu/RFLU_CheckPositivity.F90:173-193). */
+void afterUpdate(orc_ctx *c) {
+  const int nc = c->nCells;
+  for (int ic = 0; ic < nc; ++ic) {
+    const double *cv = &c->cv[5 * ic];
+    double rho = cv[0], rrho = 1.0 / rho;
+    double u = rrho * cv[1], v = rrho * cv[2], w = rrho * cv[3];
+    double p = c->dv[3 * ic], t = c->dv[3 * ic + 1];
+    if (std::isnan(rho) || std::isnan(u) || std::isnan(v) || std::isnan(w) || std::isnan(p) || std::isnan(t))
+      c->nanCount++;
+  }
+  const double pTol = 1.0e-12;
+  double rgas = MixtPerf_R_M(c->gvMol), gamma = MixtPerf_G_CpR(c->gvCp, rgas);
+  for (int ic = 0; ic < nc; ++ic) {
+    double *cv = &c->cv[5 * ic];
+    double r = cv[0], ir = 1.0 / r;
+    double u = ir * cv[1], v = ir * cv[2], w = ir * cv[3];
+    double Eo = ir * cv[4];
+    double Vm2 = u * u + v * v + w * w;
+    double p = MixtPerf_P_DEoGVm2(r, Eo, gamma, Vm2);
+    if (p <= 0.0 && std::fabs(p) <= pTol) {
+      c->negPCount++;
+      p = pTol;
+      cv[4] = r * MixtPerf_Eo_DGPUVW(r, gamma, p, u, v, w);
+    }
+  }
+  for (int ic = 0; ic < nc; ++ic) {
+    double *cv = &c->cv[5 * ic];
+    double rho = cv[0], rrho = 1.0 / rho;
+    double u = rrho * cv[1], v = rrho * cv[2], w = rrho * cv[3];
+    double Vm2 = u * u + v * v + w * w;
+    double p = c->dv[3 * ic];
+    if (p <= 0.0) {
+      c->posFixCount++;
+      double Eo = 1.0e4 + 0.5 * Vm2;
+      cv[4] = rho * Eo;
+      setDependentVars(c, ic);
+    }
+  }
+}
+
+void rkStage(orc_ctx *c, int iStage, double dtMin) {
+  rkInit(c, iStage);
+  cellGradients(c);
+  convectiveFluxes(c);
+  rkUpdate(c, iStage, dtMin);
+  for (int ic = 0; ic < c->nCells; ++ic) setDependentVars(c, ic);
+  afterUpdate(c);
+}
+
+/* RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:120-333) and
+ * RFLU_MinimumTimeStep (rocflu/RFLU_MinimumTimeStep.F90:100-245), one region. */
+double timeStep(orc_ctx *c, double currentTime) {
+  const int nc = c->nCells;
+  std::vector<double> dt(nc, 0.0);
+  for (int f = 0; f < c->nFaces; ++f) {
+    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+    double nx = c->fn[4 * f], ny = c->fn[4 * f + 1], nz = c->fn[4 * f + 2], nm = c->fn[4 * f + 3];
+    double fsu = 0.0;
+    double ir1 = 1.0 / c->cv[5 * c1], ir2 = 1.0 / c->cv[5 * c2];
+    double u1 = c->cv[5 * c1 + 1] * ir1, v1 = c->cv[5 * c1 + 2] * ir1, w1 = c->cv[5 * c1 + 3] * ir1;
+    double a1 = c->dv[3 * c1 + 2];
+    double u2 = c->cv[5 * c2 + 1] * ir2, v2 = c->cv[5 * c2 + 2] * ir2, w2 = c->cv[5 * c2 + 3] * ir2;
+    double a2 = c->dv[3 * c2 + 2];
+    double vc = 0.5 * ((u1 + u2) * nx + (v1 + v2) * ny + (w1 + w2) * nz);
+    double as = 0.5 * (a1 + a2);
+    double srad = (std::fabs(vc - fsu) + as) * nm;
+    dt[c1] = dt[c1] + srad;
+    dt[c2] = dt[c2] + srad;
+  }
+  for (const Patch &p : c->patches) {
+    for (int i = 0; i < p.n; ++i) {
+      int c1 = p.bf2c[i];
+      double nx = p.fn[4 * i], ny = p.fn[4 * i + 1], nz = p.fn[4 * i + 2], nm = p.fn[4 * i + 3];
+      double fsu = 0.0;
+      double ir1 = 1.0 / c->cv[5 * c1];
+      double u1 = c->cv[5 * c1 + 1] * ir1, v1 = c->cv[5 * c1 + 2] * ir1, w1 = c->cv[5 * c1 + 3] * ir1;
+      double a1 = c->dv[3 * c1 + 2];
+      double vc = u1 * nx + v1 * ny + w1 * nz;
+      dt[c1] = dt[c1] + (std::fabs(vc - fsu) + a1) * nm;
+    }
+  }
+  double dtMin = 1.79769313486231571e308;
+  for (int ic = 0; ic < nc; ++ic) {
+    dt[ic] = c->vol[ic] / dt[ic];
+    dtMin = fmin2(dtMin, dt[ic]);
+  }
+  /* RFLU_MinimumTimeStep */
+  double cfl = c->num.cfl;
+  if (c->num.rkScheme == 1) cfl = fmin2(cfl, 3.0);
+  else if (c->num.rkScheme == 2) cfl = fmin2(cfl, 2.0);
+  else cfl = fmin2(cfl, 1.0);
+  dtMin = cfl * dtMin;
+  double wtI = 0.0, wtC = 0.0;
+  if (currentTime <= 1.0e-8) wtI = 1.0; else wtC = 1.0;
+  dtMin = wtI / c->num.dtImposed + wtC / dtMin;
+  dtMin = 1.0 / dtMin;
+  if (dtMin <= 0.0) dtMin = 6.0e-12;
+  dtMin = fmax2(dtMin, c->num.dtMinLimit);
+  return dtMin;
+}
+
+} // namespace
+
+extern "C" {
+
+orc_ctx *orc_create(const orc_mesh_desc *m, const orc_num_desc *num) {
+  orc_ctx *c = new orc_ctx();
+  c->nVert = m->nVert;
+  c->nCells = m->nCells;
+  c->nvc = m->nVertPerCell;
+  c->xyz.assign(m->xyz, m->xyz + 3 * m->nVert);
+  c->c2v.assign(m->c2v, m->c2v + c->nvc * m->nCells);
+  for (int ip = 0; ip < m->nPatches; ++ip) {
+    Patch p;
+    p.bcType = m->patchBcType[ip];
+    p.outflowType = m->patchOutflowType[ip];
+    p.pOut = m->patchPout[ip];
+    p.order = m->patchOrder[ip];
+    int b = m->patchFaceOff[ip], e = m->patchFaceOff[ip + 1];
+    p.n = e - b;
+    p.bf2v.assign(m->bf2v + 4 * b, m->bf2v + 4 * e);
+    c->patches.push_back(p);
+  }
+  c->num = *num;
+  buildFaceList(c);
+  buildGeometry(c);
+  if (num->spaceOrder > 1) {
+    buildStencils(c);
+    buildMoments(c);
+  } else {
+    c->stOff.assign(c->nCells + 1, 0);
+  }
+  /* RFLU_DerivedInputValues (libflu/RFLU_DerivedInputValues.F90:309-410) */
+  for (int k = 0; k < 5; ++k) c->ark[k] = c->grk[k] = 0.0;
+  if (num->rkScheme == 1) {
+    c->nrkSteps = 4;
+    c->ark[0] = 0.5; c->ark[1] = 0.5; c->ark[2] = 1.0; c->ark[3] = 1.0 / 6.0;
+    c->grk[0] = 1.0; c->grk[1] = 2.0; c->grk[2] = 2.0; c->grk[3] = 1.0;
+  } else if (num->rkScheme == 2) {
+    c->nrkSteps = 3;
+    c->ark[0] = 8.0 / 15.0; c->ark[1] = 5.0 / 12.0; c->ark[2] = 0.75;
+    c->grk[0] = 0.0; c->grk[1] = 17.0 / 25.0; c->grk[2] = 5.0 / 9.0;
+  } else {
+    c->nrkSteps = 1;
+    c->ark[0] = 1.0; c->grk[0] = 1.0;
+  }
+  c->refCp = num->cp;
+  c->refGamma = num->gamma;
+  c->gvMol = MixtPerf_M_R(MixtPerf_R_CpG(num->cp, num->gamma));
+  c->gvCp = num->cp;
+  const size_t n5 = 5 * (size_t)c->nCells;
+  c->cv.assign(n5, 0.0); c->cvOld.assign(n5, 0.0); c->rhs.assign(n5, 0.0);
+  c->rhsSum.assign(n5, 0.0); c->diss.assign(n5, 0.0); c->lim.assign(n5, 1.0);
+  c->dv.assign(3 * (size_t)c->nCells, 0.0);
+  c->grad.assign(15 * (size_t)c->nCells, 0.0);
+  return c;
+}
+
+void orc_destroy(orc_ctx *c) { delete c; }
+int orc_nfaces(orc_ctx *c) { return c->nFaces; }
+int orc_patch_nfaces(orc_ctx *c, int ip) { return c->patches[ip].n; }
+int orc_stencil_nnz(orc_ctx *c) { return c->stOff[c->nCells]; }
+int orc_nstages(orc_ctx *c) { return c->nrkSteps; }
+
+void orc_get_faces(orc_ctx *c, int *f2c, int *f2v, double *fn, double *fc) {
+  if (f2c) std::memcpy(f2c, c->f2c.data(), sizeof(int) * 2 * c->nFaces);
+  if (f2v) std::memcpy(f2v, c->f2v.data(), sizeof(int) * 4 * c->nFaces);
+  if (fn) std::memcpy(fn, c->fn.data(), sizeof(double) * 4 * c->nFaces);
+  if (fc) std::memcpy(fc, c->fc.data(), sizeof(double) * 3 * c->nFaces);
+}
+void orc_get_cells(orc_ctx *c, double *vol, double *cofg) {
+  if (vol) std::memcpy(vol, c->vol.data(), sizeof(double) * c->nCells);
+  if (cofg) std::memcpy(cofg, c->cofg.data(), sizeof(double) * 3 * c->nCells);
+}
+void orc_get_patch(orc_ctx *c, int ip, int *bf2c, double *fn, double *fc) {
+  const Patch &p = c->patches[ip];
+  if (bf2c) std::memcpy(bf2c, p.bf2c.data(), sizeof(int) * p.n);
+  if (fn) std::memcpy(fn, p.fn.data(), sizeof(double) * 4 * p.n);
+  if (fc) std::memcpy(fc, p.fc.data(), sizeof(double) * 3 * p.n);
+}
+void orc_get_stencil(orc_ctx *c, int *off, int *idx, double *moms) {
+  if (off) std::memcpy(off, c->stOff.data(), sizeof(int) * (c->nCells + 1));
+  if (idx) std::memcpy(idx, c->stIdx.data(), sizeof(int) * c->stIdx.size());
+  if (moms && !c->moms.empty()) std::memcpy(moms, c->moms.data(), sizeof(double) * 10 * c->nCells);
+}
+
+void orc_set_state(orc_ctx *c, const double *cv) {
+  std::memcpy(c->cv.data(), cv, sizeof(double) * 5 * c->nCells);
+  for (int ic = 0; ic < c->nCells; ++ic) setDependentVars(c, ic);
+}
+void orc_get_state(orc_ctx *c, double *cv, double *dv) {
+  if (cv) std::memcpy(cv, c->cv.data(), sizeof(double) * 5 * c->nCells);
+  if (dv) std::memcpy(dv, c->dv.data(), sizeof(double) * 3 * c->nCells);
+}
+void orc_get_rhs(orc_ctx *c, double *rhs) { std::memcpy(rhs, c->rhs.data(), sizeof(double) * 5 * c->nCells); }
+void orc_get_grad(orc_ctx *c, double *grad) { std::memcpy(grad, c->grad.data(), sizeof(double) * 15 * c->nCells); }
+
+void orc_residual(orc_ctx *c, double *rhs, double *grad) {
+  std::vector<double> save = c->cv;
+  for (double &d : c->diss) d = 0.0;
+  cellGradients(c);
+  convectiveFluxes(c);
+  if (rhs) std::memcpy(rhs, c->rhs.data(), sizeof(double) * 5 * c->nCells);
+  if (grad) std::memcpy(grad, c->grad.data(), sizeof(double) * 15 * c->nCells);
+  c->cv = save;
+}
+
+double orc_timestep(orc_ctx *c, double t) { return timeStep(c, t); }
+void orc_rk_stage(orc_ctx *c, int iStage, double dtMin) { rkStage(c, iStage, dtMin); }
+
+int orc_run(orc_ctx *c, int nSteps, double *time, double endTime) {
+  int done = 0;
+  for (int n = 0; n < nSteps; ++n) {
+    double dt = timeStep(c, *time);
+    bool finished = false;
+    if (endTime > 0.0 && *time + dt > endTime) { dt = endTime - *time; finished = true; }
+    for (int s = 1; s <= c->nrkSteps; ++s) rkStage(c, s, dt);
+    *time = *time + dt;
+    ++done;
+    if (finished) break;
+  }
+  return done;
+}
+
+void orc_run_fixed_dt(orc_ctx *c, int nSteps, double dt) {
+  for (int n = 0; n < nSteps; ++n)
+    for (int s = 1; s <= c->nrkSteps; ++s) rkStage(c, s, dt);
+}
+
+void orc_counters(orc_ctx *c, long long *posFix, long long *negP, long long *nan) {
+  if (posFix) *posFix = c->posFixCount;
+  if (negP) *negP = c->negPCount;
+  if (nan) *nan = c->nanCount;
+}
+
+} // extern "C"

@@ -1,0 +1,177 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use
+this module, as the checker and as the timed CPU restatement.  It builds
+oracle/_build/liboracle.so with the committed Makefile on first use.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("nVert", C.c_int), ("nCells", C.c_int), ("nVertPerCell", C.c_int),
+                ("xyz", C.POINTER(C.c_double)), ("c2v", C.POINTER(C.c_int)),
+                ("nPatches", C.c_int), ("patchFaceOff", C.POINTER(C.c_int)),
+                ("bf2v", C.POINTER(C.c_int)), ("patchBcType", C.POINTER(C.c_int)),
+                ("patchOutflowType", C.POINTER(C.c_int)), ("patchPout", C.POINTER(C.c_double)),
+                ("patchOrder", C.POINTER(C.c_int))]
+
+
+class NumDesc(C.Structure):
+    _fields_ = [("spaceOrder", C.c_int), ("spaceDiscr", C.c_int), ("reconst", C.c_int),
+                ("rkScheme", C.c_int), ("piclBuild", C.c_int),
+                ("cp", C.c_double), ("gamma", C.c_double), ("cfl", C.c_double),
+                ("epsEntr", C.c_double), ("dissFact", C.c_double),
+                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "_build", "liboracle.so")
+        src = os.path.join(_HERE, "oracle.cpp")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(NumDesc)]
+        L.orc_destroy.argtypes = [P]
+        for n in ("orc_nfaces", "orc_stencil_nnz", "orc_nstages"):
+            getattr(L, n).restype = C.c_int
+            getattr(L, n).argtypes = [P]
+        L.orc_patch_nfaces.restype = C.c_int
+        L.orc_patch_nfaces.argtypes = [P, C.c_int]
+        L.orc_timestep.restype = C.c_double
+        L.orc_timestep.argtypes = [P, C.c_double]
+        L.orc_rk_stage.argtypes = [P, C.c_int, C.c_double]
+        L.orc_run.restype = C.c_int
+        L.orc_run.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.c_double]
+        L.orc_run_fixed_dt.argtypes = [P, C.c_int, C.c_double]
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def _mesh_arrays(case):
+    xyz = np.ascontiguousarray(case.xyz, dtype=np.float64)
+    c2v = np.ascontiguousarray(case.c2v, dtype=np.int32)
+    off = np.zeros(len(case.patches) + 1, dtype=np.int32)
+    for i, p in enumerate(case.patches):
+        off[i + 1] = off[i] + len(p.bf2v)
+    bf2v = np.ascontiguousarray(np.concatenate([p.bf2v for p in case.patches]).astype(np.int32))
+    bct = np.array([p.bc_type for p in case.patches], dtype=np.int32)
+    oft = np.array([p.outflow_type for p in case.patches], dtype=np.int32)
+    pout = np.array([p.p_out for p in case.patches], dtype=np.float64)
+    order = np.array([p.order for p in case.patches], dtype=np.int32)
+    return xyz, c2v, off, bf2v, bct, oft, pout, order
+
+
+def num_desc(num):
+    return NumDesc(num.space_order, num.space_discr, num.reconst, num.rk_scheme, num.picl_build,
+                   num.cp, num.gamma, num.cfl, num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit)
+
+
+class Oracle:
+    """The reference path on the CPU, one region, reference cell numbering.
+    State arrays are returned as (nCells, 5) views of cv(5,nCells)."""
+
+    def __init__(self, case):
+        self.case = case
+        self._keep = _mesh_arrays(case)
+        xyz, c2v, off, bf2v, bct, oft, pout, order = self._keep
+        md = MeshDesc(xyz.shape[0], c2v.shape[0], c2v.shape[1], _ptr(xyz, C.c_double), _ptr(c2v, C.c_int),
+                      len(case.patches), _ptr(off, C.c_int), _ptr(bf2v, C.c_int), _ptr(bct, C.c_int),
+                      _ptr(oft, C.c_int), _ptr(pout, C.c_double), _ptr(order, C.c_int))
+        self.nd = num_desc(case.num)
+        self.h = lib().orc_create(C.byref(md), C.byref(self.nd))
+        self.n_cells = c2v.shape[0]
+        self.n_faces = lib().orc_nfaces(self.h)
+        if case.cv0 is not None:
+            self.set_state(case.cv0)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    # setup products
+    def faces(self):
+        nf = self.n_faces
+        f2c = np.zeros((nf, 2), np.int32)
+        f2v = np.zeros((nf, 4), np.int32)
+        fn = np.zeros((nf, 4))
+        fc = np.zeros((nf, 3))
+        lib().orc_get_faces(self.h, _ptr(f2c, C.c_int), _ptr(f2v, C.c_int), _ptr(fn, C.c_double), _ptr(fc, C.c_double))
+        return f2c, f2v, fn, fc
+
+    def cells(self):
+        vol = np.zeros(self.n_cells)
+        cofg = np.zeros((self.n_cells, 3))
+        lib().orc_get_cells(self.h, _ptr(vol, C.c_double), _ptr(cofg, C.c_double))
+        return vol, cofg
+
+    def patch(self, ip):
+        n = lib().orc_patch_nfaces(self.h, ip)
+        bf2c = np.zeros(n, np.int32)
+        fn = np.zeros((n, 4))
+        fc = np.zeros((n, 3))
+        lib().orc_get_patch(self.h, ip, _ptr(bf2c, C.c_int), _ptr(fn, C.c_double), _ptr(fc, C.c_double))
+        return bf2c, fn, fc
+
+    def stencil(self):
+        off = np.zeros(self.n_cells + 1, np.int32)
+        nnz = lib().orc_stencil_nnz(self.h)
+        idx = np.zeros(max(nnz, 1), np.int32)
+        moms = np.zeros((self.n_cells, 10))
+        lib().orc_get_stencil(self.h, _ptr(off, C.c_int), _ptr(idx, C.c_int), _ptr(moms, C.c_double))
+        return off, idx[:nnz], moms
+
+    # state
+    def set_state(self, cv):
+        cv = np.ascontiguousarray(cv, dtype=np.float64)
+        lib().orc_set_state(self.h, _ptr(cv, C.c_double))
+
+    def state(self):
+        cv = np.zeros((self.n_cells, 5))
+        dv = np.zeros((self.n_cells, 3))
+        lib().orc_get_state(self.h, _ptr(cv, C.c_double), _ptr(dv, C.c_double))
+        return cv, dv
+
+    def residual(self):
+        rhs = np.zeros((self.n_cells, 5))
+        grad = np.zeros((self.n_cells, 5, 3))
+        lib().orc_residual(self.h, _ptr(rhs, C.c_double), _ptr(grad, C.c_double))
+        return rhs, grad
+
+    def timestep(self, t):
+        return lib().orc_timestep(self.h, t)
+
+    def rk_stage(self, istage, dt):
+        lib().orc_rk_stage(self.h, istage, dt)
+
+    def run(self, n_steps, t=0.0, end_time=0.0):
+        tt = C.c_double(t)
+        done = lib().orc_run(self.h, n_steps, C.byref(tt), end_time)
+        return done, tt.value
+
+    def run_fixed_dt(self, n_steps, dt):
+        lib().orc_run_fixed_dt(self.h, n_steps, dt)
+
+    def counters(self):
+        a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        lib().orc_counters(self.h, C.byref(a), C.byref(b), C.byref(c))
+        return a.value, b.value, c.value

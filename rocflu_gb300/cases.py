@@ -1,0 +1,197 @@
+"""Problem set-ups: mesh, boundary patches, numerics and initial state.
+
+The numeric keys mirror the reference input deck (libfloflu/
+ReadNumericsSection.F90:110-129, ReadTimestepSection.F90:97-121,
+ReadReferenceSection.F90:103-113): DISCR (1 Roe, 3 HLLC, 4 AUSM+), ORDER,
+RECONST (0, 10 Barth-Jespersen with frame-invariant velocity limiting,
+100 componentwise Barth-Jespersen, 11 Venkatakrishnan), RKSCHEME (1 classical
+RK4, 2 Wray RK3, 3 Euler), CFL, ENTROPY, DISSFACT, TIMESTEP (imposed first
+step), DTMINLIMIT, CP, GAMMA.  Boundary types follow modfloflu/
+ModParameters.F90:401,413 (BC_OUTFLOW 20, BC_SLIPWALL 60); outflow TYPE 0 is
+supersonic (extrapolation), 1 subsonic, 2 mixed (ModParameters.F90:501-503).
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from . import meshgen
+
+BC_OUTFLOW = 20
+BC_SLIPWALL = 60
+
+DISCR_ROE, DISCR_HLLC, DISCR_AUSM = 1, 3, 4
+RECONST_NONE, RECONST_BJ, RECONST_VENKAT, RECONST_BJ_COMP = 0, 10, 11, 100
+RK_CLASSICAL4, RK_WRAY3, RK_EULER = 1, 2, 3
+
+
+@dataclass
+class Patch:
+    bf2v: np.ndarray
+    bc_type: int = BC_SLIPWALL
+    outflow_type: int = 0
+    p_out: float = 0.0
+    order: int = 1
+    name: str = ""
+
+
+@dataclass
+class Numerics:
+    space_order: int = 2
+    space_discr: int = DISCR_HLLC
+    reconst: int = RECONST_BJ
+    rk_scheme: int = RK_WRAY3
+    picl_build: int = 1
+    cp: float = 3.5
+    gamma: float = 1.4
+    cfl: float = 0.5
+    eps_entr: float = 0.05
+    diss_fact: float = 1.0
+    dt_imposed: float = 1.0e-5
+    dt_min_limit: float = 1.0e-10
+
+
+@dataclass
+class Case:
+    name: str
+    xyz: np.ndarray
+    c2v: np.ndarray
+    patches: list
+    num: Numerics
+    cv0: np.ndarray = None          # (nCells, 5) conserved state, cell order of c2v
+    end_time: float = 0.0
+    n_steps: int = 0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def n_cells(self):
+        return self.c2v.shape[0]
+
+
+def conserved(rho, u, v, w, p, gamma):
+    """(rho, rho u, rho v, rho w, rho E) from primitive variables."""
+    rho = np.asarray(rho, float)
+    e = p / (rho * (gamma - 1.0)) + 0.5 * (u * u + v * v + w * w)
+    return np.stack([rho, rho * u, rho * v, rho * w, rho * e], axis=1)
+
+
+def _patches(mesh, kinds):
+    out = []
+    for p, k in zip(mesh["patches"], kinds):
+        out.append(Patch(bf2v=p["bf2v"], name=p["name"], **k))
+    return out
+
+
+SLIP = {"bc_type": BC_SLIPWALL}
+
+
+def sod(nx=400, ny=4, nz=4, num=None):
+    """Sod shock tube on [0,1]x[0,0.01]^2 hexes: (1,0,1) for x<0.5 and
+    (0.125,0,0.1) beyond, slip walls in y/z, supersonic (extrapolation)
+    outflow at both x ends, first-order Roe, run to t = 0.2 at CFL 0.5."""
+    mesh = meshgen.hex_box(nx, ny, nz, hi=(1.0, 0.01, 0.01))
+    if num is None:
+        num = Numerics(space_order=1, space_discr=DISCR_ROE, reconst=RECONST_NONE, cfl=0.5)
+    out = {"bc_type": BC_OUTFLOW, "outflow_type": 0, "order": 1}
+    patches = _patches(mesh, [out, out, SLIP, SLIP, SLIP, SLIP])
+    xc = meshgen.cell_centers(mesh)[:, 0]
+    left = xc < 0.5
+    rho = np.where(left, 1.0, 0.125)
+    p = np.where(left, 1.0, 0.1)
+    z = np.zeros_like(rho)
+    cv0 = conserved(rho, z, z, z, p, num.gamma)
+    # imposed first step = the CFL step of the initial state (cubic cells of
+    # side h, still gas, sound speed sqrt(gamma) on the left: dt = h/(6c)),
+    # so the reference's first-step TIMESTEP rule does not change the run
+    h = 1.0 / nx
+    num.dt_imposed = num.cfl * h / (6.0 * math.sqrt(num.gamma))
+    return Case("sod", mesh["xyz"], mesh["c2v"], patches, num, cv0, end_time=0.2)
+
+
+def blast_tets(n=64, num=None, seed=0, p_in=100.0, radius=0.1):
+    """Spherical blast on n^3 hexes split into 6 jittered tetrahedra (+-0.2h,
+    seed 0): rho=1, u=0, p=p_in inside r<radius about the centre, p=1 outside;
+    slip walls on all six sides; 2nd-order LSQ, Venkatakrishnan, HLLC, CFL 0.4."""
+    mesh = meshgen.tet_box(n, jitter=0.2, seed=seed)
+    if num is None:
+        num = Numerics(space_order=2, space_discr=DISCR_HLLC, reconst=RECONST_VENKAT, cfl=0.4)
+    patches = _patches(mesh, [dict(SLIP, order=2)] * 6)
+    c = meshgen.cell_centers(mesh) - 0.5
+    r = np.sqrt((c * c).sum(axis=1))
+    p = np.where(r < radius, p_in, 1.0)
+    rho = np.ones_like(p)
+    z = np.zeros_like(p)
+    cv0 = conserved(rho, z, z, z, p, num.gamma)
+    num.dt_imposed = 1.0  # replaced by the CFL step at t=0 (see first_dt)
+    return Case("blast_tets", mesh["xyz"], mesh["c2v"], patches, num, cv0, n_steps=100)
+
+
+def shock_sphere(n=128, num=None, discr=DISCR_HLLC):
+    """Mach-2 planar shock at x=0.2 moving +x into rho=1, p=1, u=0 (gamma 1.4),
+    Rankine-Hugoniot post-shock state behind it, density-3 sphere of radius
+    0.15 at the centre; n^3 hexes on [0,1]^3; supersonic outflow on the x
+    faces (2nd-order patches), slip walls elsewhere; BJ limiter."""
+    mesh = meshgen.hex_box(n, n, n)
+    if num is None:
+        num = Numerics(space_order=2, space_discr=discr, reconst=RECONST_BJ, cfl=0.4)
+    out = {"bc_type": BC_OUTFLOW, "outflow_type": 0, "order": 2}
+    patches = _patches(mesh, [out, out] + [dict(SLIP, order=2)] * 4)
+    c = meshgen.cell_centers(mesh)
+    g = num.gamma
+    m = 2.0
+    rho2 = (g + 1) * m * m / ((g - 1) * m * m + 2)
+    p2 = 1.0 + 2 * g / (g + 1) * (m * m - 1)
+    u2 = m * math.sqrt(g) * (1.0 - 1.0 / rho2)
+    behind = c[:, 0] < 0.2
+    d = c - 0.5
+    sphere = (d * d).sum(axis=1) < 0.15 ** 2
+    rho = np.where(behind, rho2, np.where(sphere, 3.0, 1.0))
+    p = np.where(behind, p2, 1.0)
+    u = np.where(behind, u2, 0.0)
+    z = np.zeros_like(rho)
+    cv0 = conserved(rho, u, z, z, p, g)
+    num.dt_imposed = 1.0
+    return Case("shock_sphere", mesh["xyz"], mesh["c2v"], patches, num, cv0, n_steps=500,
+                extra={"rho2": rho2, "p2": p2, "u2": u2})
+
+
+def adjoint_tets(n=32, num=None, seed=0, pert_seed=1, limiter=RECONST_VENKAT):
+    """Uniform Mach-0.5 flow along x (rho=1, p=1/gamma, u=0.5) with a seeded
+    +-5% Gaussian perturbation (seed 1) on every conserved variable, on n^3
+    hexes split into 6 jittered tetrahedra; second-order Roe.  x-low:
+    supersonic-type extrapolation outflow, x-high: subsonic outflow at
+    p=1/gamma, slip walls elsewhere, all patches second order."""
+    mesh = meshgen.tet_box(n, jitter=0.2, seed=seed)
+    if num is None:
+        num = Numerics(space_order=2, space_discr=DISCR_ROE, reconst=limiter, cfl=0.4)
+    g = num.gamma
+    patches = _patches(mesh, [{"bc_type": BC_OUTFLOW, "outflow_type": 0, "order": 2},
+                              {"bc_type": BC_OUTFLOW, "outflow_type": 1, "p_out": 1.0 / g, "order": 2}]
+                       + [dict(SLIP, order=2)] * 4)
+    nc = mesh["c2v"].shape[0]
+    one = np.ones(nc)
+    cv0 = conserved(one, 0.5 * one, 0 * one, 0 * one, one / g, g)
+    rng = np.random.Generator(np.random.PCG64(pert_seed))
+    cv0 = cv0 * (1.0 + 0.05 * rng.standard_normal(cv0.shape))
+    # keep the y/z momentum perturbations (their mean is zero) relative to |u|
+    cv0[:, 2] = 0.05 * rng.standard_normal(nc) * 0.5
+    cv0[:, 3] = 0.05 * rng.standard_normal(nc) * 0.5
+    num.dt_imposed = 1.0
+    return Case("adjoint_tets", mesh["xyz"], mesh["c2v"], patches, num, cv0)
+
+
+def blast_hex(n=64, num=None, p_in=10.0, radius=0.15):
+    """Spherical blast on n^3 hexes: rho=1, p=p_in for r<radius, p=1 outside,
+    slip walls, HLLC, BJ limiter (time-unrolled adjoint case)."""
+    mesh = meshgen.hex_box(n, n, n)
+    if num is None:
+        num = Numerics(space_order=2, space_discr=DISCR_HLLC, reconst=RECONST_BJ, cfl=0.4)
+    patches = _patches(mesh, [dict(SLIP, order=2)] * 6)
+    c = meshgen.cell_centers(mesh) - 0.5
+    r = np.sqrt((c * c).sum(axis=1))
+    p = np.where(r < radius, p_in, 1.0)
+    one = np.ones_like(p)
+    z = np.zeros_like(p)
+    cv0 = conserved(one, z, z, z, p, num.gamma)
+    num.dt_imposed = 1.0
+    return Case("blast_hex", mesh["xyz"], mesh["c2v"], patches, num, cv0, n_steps=200)

@@ -1,0 +1,673 @@
+// C ABI of the device path (include/rflu_gpu.h): context creation (cell
+// renumbering, CSR structures, least-squares weights), state transfer and the
+// stage / step / residual drivers.  Kernels live in kernels_*.cu.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rflu_gpu.h"
+#include "ctx.h"
+#include "errors.h"
+#include "ops.h"
+
+namespace rflu {
+
+std::string &lastError() {
+  static thread_local std::string msg;
+  return msg;
+}
+
+namespace {
+
+#define RFLU_CUDA(call)                                                                       \
+  do {                                                                                        \
+    cudaError_t err_ = (call);                                                                \
+    if (err_ != cudaSuccess)                                                                  \
+      return fail(RFLU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_));       \
+  } while (0)
+
+// --- small device helpers of the ABI --------------------------------------
+__global__ void kSetScalars(Scalars *sc, double time, double endTime, int resetCounters) {
+  sc->time = time;
+  sc->endTime = endTime;
+  sc->finished = 0;
+  sc->stepsDone = 0;
+  if (resetCounters) {
+    sc->nanCells = sc->posFixCells = sc->negPCells = 0;
+    sc->firstBadCell = INT_MAX;
+  }
+}
+__global__ void kSetDt(Scalars *sc, double dt) {
+  sc->dtMin = dt;
+  sc->finished = 0;
+}
+// cv(5,nc) in reference order (column-major) -> SoA renumbered
+__global__ void kPermuteIn(const double *src, double *dst, const int *refId, int nc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  int o = refId[i];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) dst[(size_t)k * nc + i] = src[5 * (size_t)o + k];
+}
+// SoA renumbered (ncomp rows of type T) -> reference column-major double
+template <typename T>
+__global__ void kPermuteOut(const T *src, double *dst, const int *refId, int nc, int ncomp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  int o = refId[i];
+  for (int k = 0; k < ncomp; ++k) dst[(size_t)ncomp * o + k] = (double)src[(size_t)k * nc + i];
+}
+
+inline int nblk(long long n) { return (int)((n + 255) / 256); }
+
+// Morton (Z-order) key of a point in the unit box of the mesh, 21 bits/axis.
+inline uint64_t spread3(uint64_t x) {
+  x &= 0x1fffff;
+  x = (x | x << 32) & 0x1f00000000ffffull;
+  x = (x | x << 16) & 0x1f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+
+}  // namespace
+
+// Base of the per-precision contexts; the C ABI calls these.
+struct CtxBase {
+  virtual ~CtxBase() {}
+  virtual int upload(const double *cv) = 0;
+  virtual int download(double *cv, double *dv) = 0;
+  virtual int timestep(double t, double *dt) = 0;
+  virtual int rkStage(int iStage, double dt) = 0;
+  virtual int rungeKutta(double dt) = 0;
+  virtual int step(int nSteps, double *time, double endTime, int *done) = 0;
+  virtual int runFixedDt(int nSteps, double dt) = 0;
+  virtual int residual(const double *cv, double *rhs, double *grad) = 0;
+  virtual int vjp(const double *cv, const double *rhsBar, double *cvBar) = 0;
+  virtual int jvp(const double *cv, const double *cvDot, double *rhsDot) = 0;
+  virtual int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) = 0;
+  virtual int status(rflu_status *s) = 0;
+  cudaStream_t stream = nullptr;
+};
+
+template <typename R>
+struct Ctx : CtxBase {
+  View<R> V{};
+  const Ops<R> *ops = nullptr;
+  std::vector<void *> allocs;
+  double *staging = nullptr;     // (15, nc) doubles: transfers in reference order
+  double *work = nullptr;        // adjoint workspace
+  size_t workBytes = 0;
+  double *cvSave = nullptr;
+  cudaGraphExec_t stepGraph = nullptr, fixedGraph = nullptr;
+  long long lastNan = 0;
+
+  ~Ctx() override {
+    if (stepGraph) cudaGraphExecDestroy(stepGraph);
+    if (fixedGraph) cudaGraphExecDestroy(fixedGraph);
+    for (void *p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  int alloc(T **p, size_t n) {
+    void *q = nullptr;
+    RFLU_CUDA(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+    allocs.push_back(q);
+    *p = (T *)q;
+    return RFLU_OK;
+  }
+  template <typename T, typename S>
+  int put(const T **dst, const std::vector<S> &src) {
+    std::vector<T> tmp(src.begin(), src.end());
+    T *d = nullptr;
+    int rc = alloc(&d, tmp.size());
+    if (rc) return rc;
+    if (!tmp.empty()) RFLU_CUDA(cudaMemcpy(d, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *dst = d;
+    return RFLU_OK;
+  }
+
+  int create(const rflu_grid_desc *g, const rflu_num_desc *num);
+  int checkLaunch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return RFLU_OK;
+  }
+  int syncEvents(bool events) {
+    RFLU_CUDA(cudaStreamSynchronize(stream));
+    if (!events) return RFLU_OK;
+    Scalars s;
+    RFLU_CUDA(cudaMemcpy(&s, V.sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
+    if ((long long)s.nanCells > lastNan) {
+      lastNan = (long long)s.nanCells;
+      return RFLU_EVENT_NAN;
+    }
+    return RFLU_OK;
+  }
+  void stageKernels(int iStage) {
+    ops->gradLimit(V, stream);
+    ops->faceFlux(V, stream);
+    ops->gatherUpdate(V, iStage, &V.sc->dtMin, stream);
+  }
+  int setState(const double *cv) {
+    RFLU_CUDA(cudaMemcpyAsync(staging, cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
+    kPermuteIn<<<nblk(V.nc), 256, 0, stream>>>(staging, V.cv, V.refId, V.nc);
+    ops->initState(V, stream);
+    return checkLaunch("upload");
+  }
+
+  int upload(const double *cv) override {
+    if (!cv) return fail(RFLU_ERR_ARG, "rflu_gpu_upload_state: null cv");
+    int rc = setState(cv);
+    if (rc) return rc;
+    return syncEvents(false);
+  }
+  int download(double *cv, double *dv) override {
+    if (cv) {
+      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.refId, V.nc, 5);
+      RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
+    }
+    if (dv) {
+      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.refId, V.nc, 3);
+      RFLU_CUDA(cudaMemcpyAsync(dv, staging + 5 * (size_t)V.nc, sizeof(double) * 3 * (size_t)V.nc,
+                                cudaMemcpyDeviceToHost, stream));
+    }
+    int rc = checkLaunch("download");
+    if (rc) return rc;
+    return syncEvents(false);
+  }
+  int timestep(double t, double *dt) override {
+    kSetScalars<<<1, 1, 0, stream>>>(V.sc, t, 0.0, 0);
+    ops->timestep(V, stream);
+    int rc = checkLaunch("timestep");
+    if (rc) return rc;
+    Scalars s;
+    RFLU_CUDA(cudaMemcpyAsync(&s, V.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
+    RFLU_CUDA(cudaStreamSynchronize(stream));
+    if (dt) *dt = s.dtMin;
+    return RFLU_OK;
+  }
+  int rkStage(int iStage, double dt) override {
+    if (iStage < 1 || iStage > V.p.nrkSteps) return fail(RFLU_ERR_ARG, "rflu_gpu_rk_stage: stage out of range");
+    kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
+    stageKernels(iStage);
+    int rc = checkLaunch("rk_stage");
+    if (rc) return rc;
+    return syncEvents(true);
+  }
+  int rungeKutta(double dt) override {
+    kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
+    for (int s = 1; s <= V.p.nrkSteps; ++s) stageKernels(s);
+    int rc = checkLaunch("runge_kutta");
+    if (rc) return rc;
+    return syncEvents(true);
+  }
+  // One time step (dt + all stages + time advance) captured once as a graph.
+  int ensureStepGraph() {
+    if (stepGraph) return RFLU_OK;
+    cudaGraph_t graph;
+    RFLU_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    ops->timestep(V, stream);
+    for (int s = 1; s <= V.p.nrkSteps; ++s) stageKernels(s);
+    ops->stepEnd(V, stream);
+    RFLU_CUDA(cudaStreamEndCapture(stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&stepGraph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return RFLU_OK;
+  }
+  int ensureFixedGraph() {
+    if (fixedGraph) return RFLU_OK;
+    cudaGraph_t graph;
+    RFLU_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 1; s <= V.p.nrkSteps; ++s) stageKernels(s);
+    RFLU_CUDA(cudaStreamEndCapture(stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&fixedGraph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return RFLU_OK;
+  }
+  int step(int nSteps, double *time, double endTime, int *done) override {
+    if (!time || nSteps < 0) return fail(RFLU_ERR_ARG, "rflu_gpu_step: bad arguments");
+    int rc = ensureStepGraph();
+    if (rc) return rc;
+    kSetScalars<<<1, 1, 0, stream>>>(V.sc, *time, endTime, 0);
+    Scalars s{};
+    const int chunk = 64;
+    for (int n0 = 0; n0 < nSteps; n0 += chunk) {
+      int m = std::min(chunk, nSteps - n0);
+      for (int k = 0; k < m; ++k) RFLU_CUDA(cudaGraphLaunch(stepGraph, stream));
+      if (endTime > 0.0) {
+        RFLU_CUDA(cudaMemcpyAsync(&s, V.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
+        RFLU_CUDA(cudaStreamSynchronize(stream));
+        if (s.finished != 0) break;
+      }
+    }
+    RFLU_CUDA(cudaMemcpyAsync(&s, V.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
+    rc = syncEvents(true);
+    *time = s.time;
+    if (done) *done = s.stepsDone;
+    return rc;
+  }
+  int runFixedDt(int nSteps, double dt) override {
+    int rc = ensureFixedGraph();
+    if (rc) return rc;
+    kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
+    for (int k = 0; k < nSteps; ++k) RFLU_CUDA(cudaGraphLaunch(fixedGraph, stream));
+    return syncEvents(true);
+  }
+  int residual(const double *cv, double *rhs, double *grad) override {
+    if (!cv || !rhs) return fail(RFLU_ERR_ARG, "rflu_gpu_residual: null argument");
+    const size_t nc = V.nc;
+    RFLU_CUDA(cudaMemcpyAsync(cvSave, V.cv, sizeof(double) * 5 * nc, cudaMemcpyDeviceToDevice, stream));
+    int rc = setState(cv);
+    if (rc) return rc;
+    ops->gradLimit(V, stream);
+    ops->faceFlux(V, stream);
+    ops->gatherRhs(V, stream);
+    kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.rhs, staging, V.refId, V.nc, 5);
+    RFLU_CUDA(cudaMemcpyAsync(rhs, staging, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
+    if (grad) {
+      if (V.p.spaceOrder > 1) {
+        kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.grad, staging, V.refId, V.nc, 15);
+        RFLU_CUDA(cudaMemcpyAsync(grad, staging, sizeof(double) * 15 * nc, cudaMemcpyDeviceToHost, stream));
+      } else {
+        RFLU_CUDA(cudaStreamSynchronize(stream));
+        std::memset(grad, 0, sizeof(double) * 15 * nc);
+      }
+    }
+    RFLU_CUDA(cudaStreamSynchronize(stream));
+    // restore the context state
+    RFLU_CUDA(cudaMemcpyAsync(V.cv, cvSave, sizeof(double) * 5 * nc, cudaMemcpyDeviceToDevice, stream));
+    ops->initState(V, stream);
+    rc = checkLaunch("residual");
+    if (rc) return rc;
+    return syncEvents(false);
+  }
+  int adjointPrep(const double *cv) {
+    if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "adjoint kernels exist for the FP64 modes only");
+    RFLU_CUDA(cudaMemcpyAsync(cvSave, V.cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToDevice, stream));
+    return setState(cv);
+  }
+  int adjointDone() {
+    RFLU_CUDA(cudaMemcpyAsync(V.cv, cvSave, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToDevice, stream));
+    ops->initState(V, stream);
+    int rc = checkLaunch("adjoint");
+    if (rc) return rc;
+    return syncEvents(false);
+  }
+  int vjp(const double *cv, const double *rhsBar, double *cvBar) override {
+    if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
+    int rc = adjointPrep(cv);
+    if (rc) return rc;
+    const size_t nc = V.nc;
+    RFLU_CUDA(cudaMemcpyAsync(staging, rhsBar, sizeof(double) * 5 * nc, cudaMemcpyHostToDevice, stream));
+    ops->vjp(V, staging, staging + 5 * nc, work, stream);
+    RFLU_CUDA(cudaMemcpyAsync(cvBar, staging + 5 * nc, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
+    return adjointDone();
+  }
+  int jvp(const double *cv, const double *cvDot, double *rhsDot) override {
+    if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
+    int rc = adjointPrep(cv);
+    if (rc) return rc;
+    const size_t nc = V.nc;
+    RFLU_CUDA(cudaMemcpyAsync(staging, cvDot, sizeof(double) * 5 * nc, cudaMemcpyHostToDevice, stream));
+    ops->jvp(V, staging, staging + 5 * nc, work, stream);
+    RFLU_CUDA(cudaMemcpyAsync(rhsDot, staging + 5 * nc, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
+    return adjointDone();
+  }
+  int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) override {
+    if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
+    if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
+    int rc = adjointPrep(cv);
+    if (rc) return rc;
+    const size_t nc = V.nc;
+    ops->patchPressure(V, iPatch, staging + 10 * nc, cvBar ? staging + 5 * nc : nullptr, work, stream);
+    RFLU_CUDA(cudaMemcpyAsync(J, staging + 10 * nc, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (cvBar)
+      RFLU_CUDA(cudaMemcpyAsync(cvBar, staging + 5 * nc, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
+    return adjointDone();
+  }
+  int status(rflu_status *st) override {
+    Scalars s;
+    RFLU_CUDA(cudaStreamSynchronize(stream));
+    RFLU_CUDA(cudaMemcpy(&s, V.sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
+    st->nanCells = (long long)s.nanCells;
+    st->posFixCells = (long long)s.posFixCells;
+    st->negPCells = (long long)s.negPCells;
+    st->firstBadCell = (s.firstBadCell == INT_MAX) ? 0 : s.firstBadCell;
+    st->stepsDone = s.stepsDone;
+    st->time = s.time;
+    st->dtMin = s.dtMin;
+    return RFLU_OK;
+  }
+  int nPatches = 0;
+};
+
+template <typename R>
+int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
+  const int nc = g->nCells, nf = g->nFaces, np = g->nPatches;
+  const int nb = np > 0 ? g->patchFaceOff[np] : 0;
+  nPatches = np;
+  RFLU_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+
+  // ---- renumbering: Morton order of the cell centroids --------------------
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int i = 0; i < nc; ++i)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], g->cofg[3 * (size_t)i + d]);
+      hi[d] = std::max(hi[d], g->cofg[3 * (size_t)i + d]);
+    }
+  double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  if (!(ext > 0)) ext = 1.0;
+  std::vector<uint64_t> key(nc);
+  for (int i = 0; i < nc; ++i) {
+    uint64_t q[3];
+    for (int d = 0; d < 3; ++d)
+      q[d] = (uint64_t)std::min(2097151.0, std::floor((g->cofg[3 * (size_t)i + d] - lo[d]) / ext * 2097151.0));
+    key[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+  }
+  std::vector<int> refId(nc), newId(nc);
+  std::iota(refId.begin(), refId.end(), 0);
+  std::stable_sort(refId.begin(), refId.end(), [&](int a, int b) { return key[a] < key[b]; });
+  for (int i = 0; i < nc; ++i) newId[refId[i]] = i;
+
+  // ---- interior faces: stored in order of their renumbered first cell -----
+  std::vector<int> store(nf);
+  std::iota(store.begin(), store.end(), 0);
+  auto c1of = [&](int f) { return newId[g->f2c[2 * (size_t)f] - 1]; };
+  auto c2of = [&](int f) { return newId[g->f2c[2 * (size_t)f + 1] - 1]; };
+  std::stable_sort(store.begin(), store.end(), [&](int a, int b) { return c1of(a) < c1of(b); });
+  std::vector<int> slotOf(nf);
+  for (int s = 0; s < nf; ++s) slotOf[store[s]] = s;
+  std::vector<int> fc1(nf), fc2(nf);
+  std::vector<double> fnx(nf), fny(nf), fnz(nf), fnm(nf), dL(3 * (size_t)nf), dR(3 * (size_t)nf);
+  for (int s = 0; s < nf; ++s) {
+    const int f = store[s];
+    const int o1 = g->f2c[2 * (size_t)f] - 1, o2 = g->f2c[2 * (size_t)f + 1] - 1;
+    if (o1 < 0 || o1 >= nc || o2 < 0 || o2 >= nc) return fail(RFLU_ERR_ARG, "rflu_gpu_create: f2c out of range");
+    fc1[s] = newId[o1];
+    fc2[s] = newId[o2];
+    const double *fn = g->fn + 4 * (size_t)f, *fcp = g->fc + 3 * (size_t)f;
+    fnx[s] = fn[0]; fny[s] = fn[1]; fnz[s] = fn[2]; fnm[s] = fn[3];
+    for (int d = 0; d < 3; ++d) {
+      // dx = xc - pGrid%cofg(XCOORD,c1), as the 2nd-order flux routines form it
+      dL[(size_t)d * nf + s] = fcp[d] - g->cofg[3 * (size_t)o1 + d];
+      dR[(size_t)d * nf + s] = fcp[d] - g->cofg[3 * (size_t)o2 + d];
+    }
+  }
+  // ---- boundary faces --------------------------------------------------------
+  std::vector<int> bcell(nb), bpatch(nb);
+  std::vector<double> bnx(nb), bny(nb), bnz(nb), bnm(nb), bd(3 * (size_t)nb);
+  std::vector<int> pType(std::max(np, 1)), pOut(std::max(np, 1)), pOrder(std::max(np, 1));
+  std::vector<double> pP(std::max(np, 1));
+  for (int ip = 0; ip < np; ++ip) {
+    pType[ip] = g->patchBcType[ip];
+    pOut[ip] = g->patchOutflowType[ip];
+    pOrder[ip] = g->patchOrder[ip];
+    pP[ip] = g->patchPout[ip];
+    if (pType[ip] != RFLU_BC_OUTFLOW && pType[ip] != RFLU_BC_SLIPWALL)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: only slip-wall and outflow patches are on this path");
+    if (pOrder[ip] == 2 && num->spaceOrder < 2)
+      return fail(RFLU_ERR_ARG, "rflu_gpu_create: 2nd-order patch needs ORDER 2");
+    for (int b = g->patchFaceOff[ip]; b < g->patchFaceOff[ip + 1]; ++b) {
+      const int o = g->bf2c[b] - 1;
+      if (o < 0 || o >= nc) return fail(RFLU_ERR_ARG, "rflu_gpu_create: bf2c out of range");
+      bcell[b] = newId[o];
+      bpatch[b] = ip;
+      const double *fn = g->bfn + 4 * (size_t)b, *fcp = g->bfc + 3 * (size_t)b;
+      bnx[b] = fn[0]; bny[b] = fn[1]; bnz[b] = fn[2]; bnm[b] = fn[3];
+      for (int d = 0; d < 3; ++d) bd[(size_t)d * nb + b] = fcp[d] - g->cofg[3 * (size_t)o + d];
+    }
+  }
+  // ---- cell -> face CSR in the reference's summation order ------------------
+  std::vector<int> cnt(nc + 1, 0);
+  for (int f = 0; f < nf; ++f) { cnt[g->f2c[2 * (size_t)f] - 1 + 1]++; cnt[g->f2c[2 * (size_t)f + 1] - 1 + 1]++; }
+  for (int b = 0; b < nb; ++b) cnt[g->bf2c[b] - 1 + 1]++;
+  std::vector<int> offRef(nc + 1, 0);
+  for (int o = 0; o < nc; ++o) offRef[o + 1] = offRef[o] + cnt[o + 1];
+  std::vector<int> entRef(offRef[nc]);
+  {
+    std::vector<int> fill(offRef.begin(), offRef.end() - 1);
+    for (int f = 0; f < nf; ++f) {
+      entRef[fill[g->f2c[2 * (size_t)f] - 1]++] = slotOf[f] << 1;
+      entRef[fill[g->f2c[2 * (size_t)f + 1] - 1]++] = (slotOf[f] << 1) | 1;
+    }
+    for (int b = 0; b < nb; ++b) entRef[fill[g->bf2c[b] - 1]++] = -(b + 1);
+  }
+  std::vector<int> cfOff(nc + 1, 0), cfEnt;
+  cfEnt.reserve(entRef.size());
+  for (int i = 0; i < nc; ++i) {
+    const int o = refId[i];
+    for (int e = offRef[o]; e < offRef[o + 1]; ++e) cfEnt.push_back(entRef[e]);
+    cfOff[i + 1] = (int)cfEnt.size();
+  }
+  // ---- stencils and least-squares weights --------------------------------------
+  // per member: RFLU_ComputeGradCellsFast_3D weights (modflu/
+  // RFLU_ModDifferentiationCells.F90:983-1044) from the R factor and the
+  // unit offset, in FP64 and in the reference's order of operations
+  std::vector<int> stOff(nc + 1, 0), stIdx;
+  std::vector<double> wx, wy, wz, epsq(nc, 0.0);
+  if (num->spaceOrder > 1) {
+    if (!g->c2csOff || !g->c2csMembs || !g->xyzMoms) return fail(RFLU_ERR_ARG, "rflu_gpu_create: ORDER 2 needs stencils");
+    for (int i = 0; i < nc; ++i) {
+      const int o = refId[i];
+      const double *m = g->xyzMoms + 10 * (size_t)o;
+      const double r11 = m[0], r12 = m[1], r22 = m[2], r13 = m[3], r23 = m[4], r33 = m[5];
+      const double c11 = 1.0 / r11, c22 = 1.0 / r22, c33 = 1.0 / r33;
+      const double c12 = -c11 * r12;
+      const double c13 = -(c11 * r13 + c12 * c22 * r23);
+      const double c23 = -c22 * r23;
+      const double c1111 = c11 * c11, c2222 = c22 * c22, c3333 = c33 * c33;
+      const double *xi = g->cofg + 3 * (size_t)o;
+      for (int e = g->c2csOff[o]; e < g->c2csOff[o + 1]; ++e) {
+        const int j = g->c2csMembs[e] - 1;
+        if (j < 0 || j >= nc) return fail(RFLU_ERR_ARG, "rflu_gpu_create: stencil member out of range");
+        double dx = g->cofg[3 * (size_t)j] - xi[0], dy = g->cofg[3 * (size_t)j + 1] - xi[1],
+               dz = g->cofg[3 * (size_t)j + 2] - xi[2];
+        const double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+        dx = term * dx; dy = term * dy; dz = term * dz;
+        const double t1 = c1111 * (dx);
+        const double t2 = c2222 * (dy + c12 * dx);
+        const double t3 = c3333 * (dz + c23 * dy + c13 * dx);
+        wx.push_back(term * (t1 + c12 * t2 + c13 * t3));
+        wy.push_back(term * (t2 + c23 * t3));
+        wz.push_back(term * (t3));
+        stIdx.push_back(newId[j]);
+      }
+      stOff[i + 1] = (int)stIdx.size();
+      // Venkatakrishnan: ds = vol**(1/3), eps^2 = (K ds)^3, K = 1
+      // (modflu/RFLU_ModLimiters.F90:457-460)
+      const double ds = std::pow(g->vol[o], 1.0 / 3.0);
+      epsq[i] = (1.0 * ds) * (1.0 * ds) * (1.0 * ds);
+    }
+  }
+  std::vector<double> vol(nc);
+  for (int i = 0; i < nc; ++i) vol[i] = g->vol[refId[i]];
+
+  // ---- device upload -----------------------------------------------------------
+  V.nc = nc; V.nf = nf; V.nb = nb;
+  int rc = 0;
+#define PUT(dst, src, T) if ((rc = put<T>(&(dst), src))) return rc
+  PUT(V.fc1, fc1, int); PUT(V.fc2, fc2, int);
+  PUT(V.fnx, fnx, R); PUT(V.fny, fny, R); PUT(V.fnz, fnz, R); PUT(V.fnm, fnm, R);
+  PUT(V.dL, dL, R); PUT(V.dR, dR, R);
+  PUT(V.bcell, bcell, int); PUT(V.bpatch, bpatch, int);
+  PUT(V.bnx, bnx, R); PUT(V.bny, bny, R); PUT(V.bnz, bnz, R); PUT(V.bnm, bnm, R);
+  PUT(V.bd, bd, R);
+  PUT(V.patchType, pType, int); PUT(V.patchOutflow, pOut, int); PUT(V.patchOrder, pOrder, int);
+  PUT(V.patchPout, pP, double);
+  PUT(V.cfOff, cfOff, int); PUT(V.cfEnt, cfEnt, int);
+  PUT(V.stOff, stOff, int); PUT(V.stIdx, stIdx, int);
+  PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
+  PUT(V.vol, vol, double); PUT(V.epsq, epsq, R);
+  PUT(V.refId, refId, int);
+#undef PUT
+  if ((rc = alloc(&V.cv, 5 * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.dv, 3 * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.prim, 5 * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.grad, 15 * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.rhsSum, 5 * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.flux, 5 * ((size_t)nf + nb)))) return rc;
+  if ((rc = alloc(&V.rhs, 5 * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.sc, 1))) return rc;
+  if ((rc = alloc(&staging, 15 * (size_t)nc + 16))) return rc;
+  if ((rc = alloc(&cvSave, 5 * (size_t)nc))) return rc;
+  RFLU_CUDA(cudaMemset(V.grad, 0, sizeof(R) * 15 * (size_t)nc));
+  RFLU_CUDA(cudaMemset(V.rhsSum, 0, sizeof(R) * 5 * (size_t)nc));
+  RFLU_CUDA(cudaMemset(V.cv, 0, sizeof(double) * 5 * (size_t)nc));
+  Scalars s0{};
+  s0.dtBits = 0x7fefffffffffffffull;
+  s0.firstBadCell = INT_MAX;
+  RFLU_CUDA(cudaMemcpy(V.sc, &s0, sizeof(Scalars), cudaMemcpyHostToDevice));
+
+  // ---- numerics (libflu/RFLU_DerivedInputValues.F90:309-410) ----------------
+  Params &P = V.p;
+  P.spaceOrder = num->spaceOrder; P.spaceDiscr = num->spaceDiscr; P.reconst = num->reconst;
+  P.rkScheme = num->rkScheme; P.piclBuild = num->piclBuild; P.precision = num->precision;
+  P.refCp = num->cp; P.refGamma = num->gamma;
+  P.gvCp = num->cp;
+  P.gvMol = 8314.3 / (num->cp - num->cp / num->gamma);  // MixtPerf_M_R(MixtPerf_R_CpG(cp,gamma))
+  P.epsEntr = num->epsEntr; P.dissFact = num->dissFact;
+  P.cfl = num->cfl; P.dtImposed = num->dtImposed; P.dtMinLimit = num->dtMinLimit;
+  for (int k = 0; k < 5; ++k) P.ark[k] = P.grk[k] = 0.0;
+  if (num->rkScheme == 1) {
+    P.nrkSteps = 4;
+    P.ark[0] = 0.5; P.ark[1] = 0.5; P.ark[2] = 1.0; P.ark[3] = 1.0 / 6.0;
+    P.grk[0] = 1.0; P.grk[1] = 2.0; P.grk[2] = 2.0; P.grk[3] = 1.0;
+  } else if (num->rkScheme == 2) {
+    P.nrkSteps = 3;
+    P.ark[0] = 8.0 / 15.0; P.ark[1] = 5.0 / 12.0; P.ark[2] = 0.75;
+    P.grk[0] = 0.0; P.grk[1] = 17.0 / 25.0; P.grk[2] = 5.0 / 9.0;
+  } else {
+    P.nrkSteps = 1;
+    P.ark[0] = 1.0; P.grk[0] = 1.0;
+  }
+  // adjoint workspace: gradients/limiter factors/face adjoints of one residual
+  workBytes = sizeof(double) * (size_t)(64 * (size_t)nc + 10 * ((size_t)nf + nb) + 64);
+  if (num->precision != RFLU_PREC_MIXED) {
+    if ((rc = alloc((char **)&work, workBytes))) return rc;
+  }
+  return RFLU_OK;
+}
+
+}  // namespace rflu
+
+struct rflu_gpu_ctx {
+  std::unique_ptr<rflu::CtxBase> impl;
+};
+
+using rflu::fail;
+
+extern "C" {
+
+const char *rflu_gpu_last_error(void) { return rflu::lastError().c_str(); }
+
+int rflu_gpu_create(const rflu_grid_desc *grid, const rflu_num_desc *num, rflu_gpu_ctx **ctx) {
+  if (!grid || !num || !ctx) return fail(RFLU_ERR_ARG, "rflu_gpu_create: null argument");
+  *ctx = nullptr;
+  if (grid->nCells <= 0 || grid->nFaces < 0 || !grid->f2c || !grid->fn || !grid->fc || !grid->vol || !grid->cofg)
+    return fail(RFLU_ERR_ARG, "rflu_gpu_create: incomplete grid description");
+  if (num->spaceOrder != 1 && num->spaceOrder != 2) return fail(RFLU_ERR_ARG, "rflu_gpu_create: ORDER must be 1 or 2");
+  if (num->spaceDiscr != 1 && num->spaceDiscr != 3 && num->spaceDiscr != 4)
+    return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: DISCR must be 1 (Roe), 3 (HLLC) or 4 (AUSM+)");
+  if (num->reconst != 0 && num->reconst != 10 && num->reconst != 11 && num->reconst != 100)
+    return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: RECONST must be 0, 10, 11 or 100");
+  if (num->rkScheme < 1 || num->rkScheme > 3) return fail(RFLU_ERR_ARG, "rflu_gpu_create: RKSCHEME must be 1, 2 or 3");
+  if (num->precision < 0 || num->precision > 2) return fail(RFLU_ERR_ARG, "rflu_gpu_create: bad precision");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(RFLU_ERR_CUDA, "rflu_gpu_create: no CUDA device");
+  rflu_gpu_ctx *c = new (std::nothrow) rflu_gpu_ctx();
+  if (!c) return fail(RFLU_ERR_ARG, "rflu_gpu_create: out of host memory");
+  int rc;
+  if (num->precision == RFLU_PREC_MIXED) {
+    auto *p = new rflu::Ctx<float>();
+    p->ops = rflu::opsMixed();
+    c->impl.reset(p);
+    rc = p->create(grid, num);
+  } else {
+    auto *p = new rflu::Ctx<double>();
+    p->ops = (num->precision == RFLU_PREC_FP64_EXACT) ? rflu::opsFp64Exact() : rflu::opsFp64();
+    c->impl.reset(p);
+    rc = p->create(grid, num);
+  }
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  *ctx = c;
+  return RFLU_OK;
+}
+
+int rflu_gpu_destroy(rflu_gpu_ctx *ctx) {
+  delete ctx;
+  return RFLU_OK;
+}
+
+void *rflu_gpu_stream(rflu_gpu_ctx *ctx) { return ctx ? (void *)ctx->impl->stream : nullptr; }
+
+#define CTX_CHECK(name) \
+  if (!ctx) return fail(RFLU_ERR_ARG, name ": null context")
+
+int rflu_gpu_upload_state(rflu_gpu_ctx *ctx, const double *cv) {
+  CTX_CHECK("rflu_gpu_upload_state");
+  return ctx->impl->upload(cv);
+}
+int rflu_gpu_download_state(rflu_gpu_ctx *ctx, double *cv, double *dv) {
+  CTX_CHECK("rflu_gpu_download_state");
+  return ctx->impl->download(cv, dv);
+}
+int rflu_gpu_timestep(rflu_gpu_ctx *ctx, double currentTime, double *dtMin) {
+  CTX_CHECK("rflu_gpu_timestep");
+  return ctx->impl->timestep(currentTime, dtMin);
+}
+int rflu_gpu_rk_stage(rflu_gpu_ctx *ctx, int iStage, double dtMin) {
+  CTX_CHECK("rflu_gpu_rk_stage");
+  return ctx->impl->rkStage(iStage, dtMin);
+}
+int rflu_gpu_runge_kutta(rflu_gpu_ctx *ctx, double dtMin) {
+  CTX_CHECK("rflu_gpu_runge_kutta");
+  return ctx->impl->rungeKutta(dtMin);
+}
+int rflu_gpu_step(rflu_gpu_ctx *ctx, int nSteps, double *time, double endTime, int *stepsDone) {
+  CTX_CHECK("rflu_gpu_step");
+  return ctx->impl->step(nSteps, time, endTime, stepsDone);
+}
+int rflu_gpu_run_fixed_dt(rflu_gpu_ctx *ctx, int nSteps, double dtMin) {
+  CTX_CHECK("rflu_gpu_run_fixed_dt");
+  return ctx->impl->runFixedDt(nSteps, dtMin);
+}
+int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *grad) {
+  CTX_CHECK("rflu_gpu_residual");
+  return ctx->impl->residual(cv, rhs, grad);
+}
+int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar) {
+  CTX_CHECK("rflu_gpu_vjp");
+  return ctx->impl->vjp(cv, rhsBar, cvBar);
+}
+int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, double *rhsDot) {
+  CTX_CHECK("rflu_gpu_jvp");
+  return ctx->impl->jvp(cv, cvDot, rhsDot);
+}
+int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, double *J, double *cvBar) {
+  CTX_CHECK("rflu_gpu_patch_pressure");
+  return ctx->impl->patchPressure(cv, iPatch, J, cvBar);
+}
+int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status) {
+  CTX_CHECK("rflu_gpu_status");
+  if (!status) return fail(RFLU_ERR_ARG, "rflu_gpu_status: null status");
+  return ctx->impl->status(status);
+}
+
+}  // extern "C"

@@ -1,0 +1,676 @@
+// Kernels of one RK stage and of the time step, templated on the state type
+// R (double or float).  Included by one translation unit per precision mode;
+// RFLU_NS names the namespace of the instantiation.
+//
+// Per stage (RungeKuttaMP, libfloflu/RungeKuttaMP.F90:148-508):
+//   gradLimit   cell-centric: LSQ gradient + limiter  (CellGradientsMP)
+//   faceFlux    face-centric: reconstruction + Riemann flux per face, patch
+//               fluxes per boundary face                (ConvectiveFluxesMP)
+//   gatherUpdate cell-centric: deterministic CSR gather of the face fluxes in
+//               the reference's summation order, RK update, dependent
+//               variables, validity/bounds/positivity   (RKUpdateMP,
+//               RFLU_SetVarsContWrapper, AfterUpdateMP)
+// Per step: cellDt (RFLU_TimeStepInviscid) + dtFinalize (RFLU_MinimumTimeStep).
+#pragma once
+#include <climits>
+#include <cuda_runtime.h>
+
+#include "ctx.h"
+#include "physics.cuh"
+
+namespace rflu {
+namespace RFLU_NS {
+
+constexpr int kBlock = 256;
+inline int blocks(long long n) { return (int)((n + kBlock - 1) / kBlock); }
+
+// Reference arithmetic (the FP64 modes) reproduces the cons -> prim -> cons
+// round trip of CellGradientsMP on the fly; the mixed mode uses the
+// primitive velocity directly.
+template <typename R> struct Ref { static constexpr bool on = false; };
+template <> struct Ref<double> { static constexpr bool on = true; };
+
+// ---------------------------------------------------------------------------
+// Dependent variables of one cell from cv: RFLU_SetDependentVars, TCPERF
+// (libflu/RFLU_SetDependentVars.F90:254-287), always in FP64.
+// ---------------------------------------------------------------------------
+__device__ inline void dependentVars(const Params &p, const double *cv, double &pres, double &temp, double &snd) {
+  double gc = 8314.3 / p.gvMol;
+  double g = p.gvCp / (p.gvCp - gc);
+  double r = cv[0];
+  double ir = 1.0 / r;
+  double Eo = ir * cv[4];
+  double Vm2 = ir * ir * (cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3]);
+  pres = (g - 1.0) * r * (Eo - 0.5 * Vm2);
+  temp = pres / (r * gc);
+  snd = sqrt(g * gc * temp);
+}
+
+template <typename R>
+__device__ inline void loadCv(const View<R> &V, int i, double *cv) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) cv[k] = V.cv[(size_t)k * V.nc + i];
+}
+
+// prim = (rho, u, v, w, p) as RFLU_ConvertCvCons2Prim DUVWP builds it
+// (modflu/RFLU_ModConvertCv.F90:214-224)
+template <typename R>
+__device__ inline void storePrim(const View<R> &V, int i, const double *cv, double pres) {
+  double ir = 1.0 / cv[0];
+  R *q = V.prim;
+  const size_t n = V.nc;
+  q[i] = (R)cv[0];
+  q[n + i] = (R)(ir * cv[1]);
+  q[2 * n + i] = (R)(ir * cv[2]);
+  q[3 * n + i] = (R)(ir * cv[3]);
+  q[4 * n + i] = (R)pres;
+}
+
+// Dependent variables and primitive state of every cell from cv
+// (RFLU_SetVarsContWrapper after upload).
+template <typename R>
+__global__ void kInitState(View<R> V) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  double cv[5], pr, t, c;
+  loadCv(V, i, cv);
+  dependentVars(V.p, cv, pr, t, c);
+  V.dv[i] = pr;
+  V.dv[(size_t)V.nc + i] = t;
+  V.dv[2 * (size_t)V.nc + i] = c;
+  storePrim(V, i, cv, pr);
+}
+
+// ---------------------------------------------------------------------------
+// Gradient + limiter, one thread per cell.
+// LSQ gradient: RFLU_ComputeGradCellsFast_3D (modflu/RFLU_ModDifferentiationCells.F90:
+// 931-1178) with the per-member weights precomputed at set-up.
+// Limiters: RFLU_ComputeLimiterBarthJesp (modflu/RFLU_ModLimiters.F90:132-322),
+// RFLU_ComputeLimiterVenkat (:353-587), RFLU_LimitGradVelocityBarthJesp
+// (:588-790), RFLU_LimitGradCells (:1061-1146).  Each cell's limiter needs
+// only its own gradient and its face neighbours' values, so the reference's
+// two face sweeps become two loops over the cell's own faces.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  const size_t n = V.nc;
+  R q[5], g[15];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) q[k] = V.prim[k * n + i];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) g[k] = R(0);
+  const int sb = V.stOff[i], se = V.stOff[i + 1];
+  for (int s = sb; s < se; ++s) {
+    const int j = V.stIdx[s];
+    const R wx = V.wx[s], wy = V.wy[s], wz = V.wz[s];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      R d = V.prim[k * n + j] - q[k];
+      g[3 * k] = g[3 * k] + wx * d;
+      g[3 * k + 1] = g[3 * k + 1] + wy * d;
+      g[3 * k + 2] = g[3 * k + 2] + wz * d;
+    }
+  }
+  const int rc = V.p.reconst;
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  if (rc == 10 || rc == 100 || rc == 11) {
+    // scalar limiters: min/max over face neighbours, then per face side
+    R vmin[5], vmax[5], lim[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; lim[k] = R(1); }
+    for (int e = cb; e < ce; ++e) {
+      const int code = V.cfEnt[e];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      const int nb = (code & 1) ? V.fc1[f] : V.fc2[f];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        R x = V.prim[k * n + nb];
+        vmin[k] = fmin2(vmin[k], x);
+        vmax[k] = fmax2(vmax[k], x);
+      }
+    }
+    R epsq = (rc == 11) ? V.epsq[i] : R(0);
+    for (int e = cb; e < ce; ++e) {
+      const int code = V.cfEnt[e];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      const R *d = (code & 1) ? V.dR : V.dL;
+      const R dx = d[f], dy = d[(size_t)V.nf + f], dz = d[2 * (size_t)V.nf + f];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        if (rc == 10 && k >= 1 && k <= 3) continue;
+        // d2 = grad . (cofg - fc), the reference's sign
+        R d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
+        R dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
+        if (rc == 11) {
+          const R tiny = R(1.0e-12);
+          if (d2 > R(0)) {
+            R numer = (dmax * dmax + epsq) * d2 + R(2) * d2 * d2 * dmax;
+            R denom = d2 * (dmax * dmax + R(2) * d2 * d2 + dmax * d2 + epsq);
+            lim[k] = fmin2(numer / (denom + tiny), lim[k]);
+          } else if (d2 < R(0)) {
+            R numer = (dmin * dmin + epsq) * d2 + R(2) * d2 * d2 * dmin;
+            R denom = d2 * (dmin * dmin + R(2) * d2 * d2 + dmin * d2 + epsq);
+            lim[k] = fmin2(numer / (denom + tiny), lim[k]);
+          }
+        } else {
+          if (d2 > R(0)) lim[k] = fmin2(fmin2(R(1), dmax / d2), lim[k]);
+          else if (d2 < R(0)) lim[k] = fmin2(fmin2(R(1), dmin / d2), lim[k]);
+        }
+      }
+    }
+    if (rc == 10) {
+      // frame-invariant velocity limiting along the strain-rate eigenvectors
+      R G[9], S[9], A[9], ev[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) G[a + 3 * b] = g[3 * (1 + a) + b];  // G(iComp, dir)
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) S[a + 3 * b] = R(0.5) * (G[a + 3 * b] + G[b + 3 * a]);
+      symmetricEigen3(S, A, ev);
+      R dmn[3] = {R(0), R(0), R(0)}, dmx[3] = {R(0), R(0), R(0)}, al[3] = {R(1), R(1), R(1)};
+      for (int e = cb; e < ce; ++e) {
+        const int code = V.cfEnt[e];
+        if (code < 0) continue;
+        const int f = code >> 1, side = code & 1;
+        const int c1 = V.fc1[f], c2 = V.fc2[f];
+        R du[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) du[k] = V.prim[(1 + k) * n + c2] - V.prim[(1 + k) * n + c1];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          R pr = R(0);
+          pr = pr + A[3 * j] * du[0];
+          pr = pr + A[3 * j + 1] * du[1];
+          pr = pr + A[3 * j + 2] * du[2];
+          if (side) pr = -pr;
+          dmn[j] = fmin2(dmn[j], pr);
+          dmx[j] = fmax2(dmx[j], pr);
+        }
+      }
+      for (int e = cb; e < ce; ++e) {
+        const int code = V.cfEnt[e];
+        if (code < 0) continue;
+        const int f = code >> 1;
+        const R *d = (code & 1) ? V.dR : V.dL;
+        const R off[3] = {-d[f], -d[(size_t)V.nf + f], -d[2 * (size_t)V.nf + f]};
+        R sh[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          R s = R(0);
+          s = s + G[a] * off[0];
+          s = s + G[a + 3] * off[1];
+          s = s + G[a + 6] * off[2];
+          sh[a] = s;
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          R pr = R(0);
+          pr = pr + A[3 * j] * sh[0];
+          pr = pr + A[3 * j + 1] * sh[1];
+          pr = pr + A[3 * j + 2] * sh[2];
+          if (pr > R(0)) al[j] = fmin2(al[j], dmx[j] / pr);
+          else if (pr < R(0)) al[j] = fmin2(al[j], dmn[j] / pr);
+        }
+      }
+      R mx = fabs_(ev[0]);
+      mx = fmax2(mx, fabs_(ev[1]));
+      mx = fmax2(mx, fabs_(ev[2]));
+      const R scale = R(1.0e-3) * mx;
+      const bool e12 = (ev[1] - ev[0] <= scale), e23 = (ev[2] - ev[1] <= scale);
+      if (e12 && e23) {
+        R m = fmin2(fmin2(al[0], al[1]), al[2]);
+        al[0] = al[1] = al[2] = m;
+      } else if (e12) {
+        R m = fmin2(al[0], al[1]);
+        al[0] = al[1] = m;
+      } else if (e23) {
+        R m = fmin2(al[1], al[2]);
+        al[1] = al[2] = m;
+      }
+      // G <- A diag(alpha) A^T G
+      R Rm[9];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          R s = R(0);
+          s = s + A[3 * j] * G[3 * c];
+          s = s + A[3 * j + 1] * G[1 + 3 * c];
+          s = s + A[3 * j + 2] * G[2 + 3 * c];
+          Rm[j + 3 * c] = al[j] * s;
+        }
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          R s = R(0);
+          s = s + A[a] * Rm[3 * c];
+          s = s + A[a + 3] * Rm[1 + 3 * c];
+          s = s + A[a + 6] * Rm[2 + 3 * c];
+          g[3 * (1 + a) + c] = s;
+        }
+      lim[1] = lim[2] = lim[3] = R(1);
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      g[3 * k] = lim[k] * g[3 * k];
+      g[3 * k + 1] = lim[k] * g[3 * k + 1];
+      g[3 * k + 2] = lim[k] * g[3 * k + 2];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
+}
+
+// ---------------------------------------------------------------------------
+// Face state for the 2nd-order routines (*_ComputeFlux2_TCP):
+// cell primitive (with the reference's momentum round trip in the FP64 modes)
+// plus grad . (fc - cofg).
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ inline void faceState(const View<R> &V, int c, R dx, R dy, R dz, R *s, R &irCell) {
+  const size_t n = V.nc;
+  R r = V.prim[c];
+  R ir = R(1) / r;
+  R u = V.prim[n + c], v = V.prim[2 * n + c], w = V.prim[3 * n + c];
+  if (Ref<R>::on) {
+    // ul = pCv(CV_MIXT_XMOM,c1)*irl with pCv(XMOM) = r*u after RFLU_ConvertCvPrim2Cons
+    u = (r * u) * ir;
+    v = (r * v) * ir;
+    w = (r * w) * ir;
+  }
+  R p = V.prim[4 * n + c];
+  const R *g = V.grad;
+  s[0] = r + g[0 * n + c] * dx + g[1 * n + c] * dy + g[2 * n + c] * dz;
+  s[1] = u + g[3 * n + c] * dx + g[4 * n + c] * dy + g[5 * n + c] * dz;
+  s[2] = v + g[6 * n + c] * dx + g[7 * n + c] * dy + g[8 * n + c] * dz;
+  s[3] = w + g[9 * n + c] * dx + g[10 * n + c] * dy + g[11 * n + c] * dz;
+  s[4] = p + g[12 * n + c] * dx + g[13 * n + c] * dy + g[14 * n + c] * dz;
+  irCell = ir;
+}
+
+template <typename R>
+__device__ inline void riemann2(const Params &P, R nx, R ny, R nz, R nm, const R *L, R irl, const R *Rt, R irr, R *flx) {
+  const R cp = (R)P.refCp, g = (R)P.refGamma;
+  if (P.spaceDiscr == 1) {
+    R gc = cp - cp / g;
+    R tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
+    R Hl = perfHo(cp, tl, L[1], L[2], L[3]), Hr = perfHo(cp, tr, Rt[1], Rt[2], Rt[3]);
+    roeFlux(g, (R)P.epsEntr, (R)P.dissFact, nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], Hl, Rt[0], Rt[1], Rt[2],
+            Rt[3], Rt[4], Hr, flx);
+  } else if (P.spaceDiscr == 3) {
+    R el = perfEo(L[0], g, L[4], L[1], L[2], L[3]), al = sqrt_(g * L[4] / L[0]);
+    R er = perfEo(Rt[0], g, Rt[4], Rt[1], Rt[2], Rt[3]), ar = sqrt_(g * Rt[4] / Rt[0]);
+    R Hl = el + irl * L[4], Hr = er + irr * Rt[4];
+    hllcFlux(g, nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], el, al, Hl, Rt[0], Rt[1], Rt[2], Rt[3], Rt[4], er, ar,
+             Hr, flx);
+  } else {
+    R gc = cp - cp / g;
+    R tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
+    R al = sqrt_(g * gc * tl), ar = sqrt_(g * gc * tr);
+    R Hl = perfHo(cp, tl, L[1], L[2], L[3]), Hr = perfHo(cp, tr, Rt[1], Rt[2], Rt[3]);
+    ausmFlux(nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], Hl, al, Rt[0], Rt[1], Rt[2], Rt[3], Rt[4], Hr, ar, flx);
+  }
+}
+
+// First-order interior flux from cv and dv (FP64 throughout; the mixed mode
+// converts the result).
+template <typename R>
+__device__ inline void riemann1(const View<R> &V, int c1, int c2, double nx, double ny, double nz, double nm,
+                                double *flx) {
+  const Params &P = V.p;
+  const size_t n = V.nc;
+  double cl[5], cr[5];
+  loadCv(V, c1, cl);
+  loadCv(V, c2, cr);
+  double rl = cl[0], irl = 1.0 / rl, ul = cl[1] * irl, vl = cl[2] * irl, wl = cl[3] * irl;
+  double rr = cr[0], irr = 1.0 / rr, ur = cr[1] * irr, vr = cr[2] * irr, wr = cr[3] * irr;
+  double pl = V.dv[c1], pr = V.dv[c2];
+  const double cp = P.refCp, g = P.refGamma;
+  if (P.spaceDiscr == 1) {
+    double Hl = perfHo(cp, V.dv[n + c1], ul, vl, wl), Hr = perfHo(cp, V.dv[n + c2], ur, vr, wr);
+    roeFlux(g, P.epsEntr, P.dissFact, nx, ny, nz, nm, rl, ul, vl, wl, pl, Hl, rr, ur, vr, wr, pr, Hr, flx);
+  } else if (P.spaceDiscr == 3) {
+    double el = cl[4] * irl, er = cr[4] * irr;
+    double Hl = el + irl * pl, Hr = er + irr * pr;
+    hllcFlux(g, nx, ny, nz, nm, rl, ul, vl, wl, pl, el, V.dv[2 * n + c1], Hl, rr, ur, vr, wr, pr, er, V.dv[2 * n + c2],
+             Hr, flx);
+  } else {
+    double Hl = cl[4] * irl + pl / rl, Hr = cr[4] * irr + pr / rr;
+    ausmFlux(nx, ny, nz, nm, rl, ul, vl, wl, pl, Hl, V.dv[2 * n + c1], rr, ur, vr, wr, pr, Hr, V.dv[2 * n + c2], flx);
+  }
+}
+
+// One thread per face: interior faces [0,nf), then boundary faces.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kFaceFlux(View<R> V) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nfT = V.nf + V.nb;
+  if (t >= nfT) return;
+  const Params &P = V.p;
+  const size_t n = V.nc;
+  R flx[5];
+  if (t < V.nf) {
+    const int f = t, c1 = V.fc1[f], c2 = V.fc2[f];
+    const R nx = V.fnx[f], ny = V.fny[f], nz = V.fnz[f], nm = V.fnm[f];
+    if (P.spaceOrder == 1) {
+      double fd[5];
+      riemann1(V, c1, c2, (double)nx, (double)ny, (double)nz, (double)nm, fd);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) flx[k] = (R)fd[k];
+    } else {
+      const size_t nf = V.nf;
+      R L[5], Rt[5], irl, irr;
+      faceState(V, c1, V.dL[f], V.dL[nf + f], V.dL[2 * nf + f], L, irl);
+      faceState(V, c2, V.dR[f], V.dR[nf + f], V.dR[2 * nf + f], Rt, irr);
+      riemann2(P, nx, ny, nz, nm, L, irl, Rt, irr, flx);
+    }
+  } else {
+    const int b = t - V.nf, c = V.bcell[b], ip = V.bpatch[b];
+    const int type = V.patchType[ip], order = V.patchOrder[ip];
+    const R nx = V.bnx[b], ny = V.bny[b], nz = V.bnz[b], nm = V.bnm[b];
+    if (order == 1) {
+      // RFLU_CentralFirstPatch reads cv as CellGradientsMP left it: in a
+      // 2nd-order run the momentum went through the prim round trip and,
+      // in the PICL build, the energy slot holds the pressure.
+      double cv[5];
+      loadCv(V, c, cv);
+      const double pl = V.dv[c];
+      if (P.spaceOrder == 2) {
+        const double ir = 1.0 / cv[0];
+        const double up = ir * cv[1], vp = ir * cv[2], wp = ir * cv[3];
+        cv[1] = cv[0] * up;
+        cv[2] = cv[0] * vp;
+        cv[3] = cv[0] * wp;
+        if (P.piclBuild) {
+          cv[4] = pl;
+        } else {
+          const double g = P.gvCp / (P.gvCp - 8314.3 / P.gvMol);
+          cv[4] = cv[0] * perfEo(cv[0], g, pl, up, vp, wp);
+        }
+      }
+      double fd[5];
+      if (type == 60) {
+        fd[0] = 0.0;
+        fd[1] = pl * (double)nx * (double)nm;
+        fd[2] = pl * (double)ny * (double)nm;
+        fd[3] = pl * (double)nz * (double)nm;
+        fd[4] = pl * 0.0 * (double)nm;
+      } else {
+        outflowPatchFlux(V.patchOutflow[ip], V.patchPout[ip], P.gvCp, P.gvMol, (double)nx, (double)ny, (double)nz,
+                         (double)nm, cv[0], cv[1], cv[2], cv[3], cv[4], pl, fd);
+      }
+#pragma unroll
+      for (int k = 0; k < 5; ++k) flx[k] = (R)fd[k];
+    } else {
+      const size_t nb = V.nb;
+      R L[5], irl;
+      faceState(V, c, V.bd[b], V.bd[nb + b], V.bd[2 * nb + b], L, irl);
+      if (type == 60) {
+        flx[0] = R(0);
+        flx[1] = L[4] * nx * nm;
+        flx[2] = L[4] * ny * nm;
+        flx[3] = L[4] * nz * nm;
+        flx[4] = L[4] * R(0) * nm;
+      } else {
+        // RFLU_CentralSecondPatch outflow: rel from the reconstructed state
+        const R cp = (R)P.gvCp, mol = (R)P.gvMol;
+        R rgas = R(8314.3) / mol;
+        R g = cp / (cp - rgas);
+        R rul = L[0] * L[1], rvl = L[0] * L[2], rwl = L[0] * L[3];
+        R rel = L[0] * perfEo(L[0], g, L[4], L[1], L[2], L[3]);
+        outflowPatchFlux(V.patchOutflow[ip], (R)V.patchPout[ip], cp, mol, nx, ny, nz, nm, L[0], rul, rvl, rwl, rel,
+                         L[4], flx);
+      }
+    }
+  }
+  const size_t nT = nfT;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) V.flux[k * nT + t] = flx[k];
+}
+
+// ---------------------------------------------------------------------------
+// Residual gather (ConvectiveFluxes, libfloflu/ConvectiveFluxes.F90:133-175):
+// rhs(c) = -diss(c) + sum over the cell's faces in reference order of +-F.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ inline void gatherRhs(const View<R> &V, int i, R *rhs) {
+  const size_t nT = (size_t)V.nf + V.nb;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) rhs[k] = -R(0);
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  for (int e = cb; e < ce; ++e) {
+    const int code = V.cfEnt[e];
+    if (code >= 0) {
+      const int f = code >> 1;
+      if (code & 1) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] - V.flux[k * nT + f];
+      } else {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] + V.flux[k * nT + f];
+      }
+    } else {
+      const int b = -code - 1;
+      const int k0 = (V.patchType[V.bpatch[b]] == 60) ? 1 : 0;  // slip walls leave rhs(DENS)
+      for (int k = k0; k < 5; ++k) rhs[k] = rhs[k] + V.flux[k * nT + V.nf + b];
+    }
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kGatherRhs(View<R> V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  R rhs[5];
+  gatherRhs(V, i, rhs);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) V.rhs[(size_t)k * V.nc + i] = rhs[k];
+}
+
+// RFLU_CheckValidity / RFLU_EnforceBounds / RFLU_CheckPositivity for one cell
+// (libflu/RFLU_CheckValidity.F90:165-214, RFLU_EnforceBounds.F90:165-230,
+// RFLU_CheckPositivity.F90:173-193); cv and dv updated in place.
+template <typename R>
+__device__ inline void afterUpdate(const View<R> &V, int i, double *cv, double &pr, double &tp, double &cs) {
+  const Params &P = V.p;
+  {
+    double rho = cv[0], rrho = 1.0 / rho;
+    double u = rrho * cv[1], v = rrho * cv[2], w = rrho * cv[3];
+    if (isnan(rho) || isnan(u) || isnan(v) || isnan(w) || isnan(pr) || isnan(tp)) {
+      atomicAdd(&V.sc->nanCells, 1ull);
+      atomicMin(&V.sc->firstBadCell, V.refId[i] + 1);
+    }
+  }
+  const double rgas = 8314.3 / P.gvMol, gamma = P.gvCp / (P.gvCp - rgas);
+  {
+    double r = cv[0], ir = 1.0 / r;
+    double u = ir * cv[1], v = ir * cv[2], w = ir * cv[3];
+    double Eo = ir * cv[4];
+    double Vm2 = u * u + v * v + w * w;
+    double p = (gamma - 1.0) * r * (Eo - 0.5 * Vm2);
+    if (p <= 0.0 && fabs(p) <= 1.0e-12) {
+      atomicAdd(&V.sc->negPCells, 1ull);
+      cv[4] = r * perfEo(r, gamma, 1.0e-12, u, v, w);
+    }
+  }
+  if (pr <= 0.0) {
+    double rho = cv[0], rrho = 1.0 / rho;
+    double u = rrho * cv[1], v = rrho * cv[2], w = rrho * cv[3];
+    double Vm2 = u * u + v * v + w * w;
+    atomicAdd(&V.sc->posFixCells, 1ull);
+    cv[4] = rho * (1.0e4 + 0.5 * Vm2);
+    dependentVars(P, cv, pr, tp, cs);
+  }
+}
+
+// Gather + RKUpdateMP (RkUpdateGeneric, static grid, libfloflu/
+// RkUpdateGeneric.F90:257-322) + RFLU_SetVarsContWrapper + AfterUpdateMP.
+// cvOld of RkInitGeneric is cv itself: nothing writes cv before this kernel.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, const double *dtp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc || V.sc->finished < 0) return;
+  const Params &P = V.p;
+  const size_t n = V.nc;
+  R rhs[5];
+  gatherRhs(V, i, rhs);
+  const double fac = P.ark[iStage - 1] * (*dtp);
+  const double grk = P.grk[iStage - 1];
+  const double adtv = fac / V.vol[i];
+  double cv[5];
+  loadCv(V, i, cv);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double r = (double)rhs[k];
+    R *rs = &V.rhsSum[k * n + i];
+    switch (P.rkScheme) {
+      case 1:
+        if (iStage == 1) { cv[k] = cv[k] - adtv * r; *rs = rhs[k]; }
+        else if (iStage == P.nrkSteps) cv[k] = cv[k] - adtv * (r + (double)*rs);
+        else { cv[k] = cv[k] - adtv * r; *rs = (R)((double)*rs + grk * r); }
+        break;
+      case 2:
+        if (iStage == 1) { cv[k] = cv[k] - adtv * r; *rs = rhs[k]; }
+        else if (iStage == 2) { cv[k] = cv[k] - adtv * (r - grk * (double)*rs); *rs = rhs[k]; }
+        else cv[k] = cv[k] - adtv * (r - grk * (double)*rs);
+        break;
+      default:
+        cv[k] = cv[k] - adtv * r;
+    }
+  }
+  double pr, tp, cs;
+  dependentVars(P, cv, pr, tp, cs);
+  afterUpdate(V, i, cv, pr, tp, cs);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) V.cv[k * n + i] = cv[k];
+  V.dv[i] = pr;
+  V.dv[n + i] = tp;
+  V.dv[2 * n + i] = cs;
+  storePrim(V, i, cv, pr);
+}
+
+// ---------------------------------------------------------------------------
+// Time step: RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:120-333)
+// per cell in face order, then a warp-shuffle + block minimum folded into one
+// atomicMin on the bit pattern of the (positive) dt.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kCellDt(View<R> V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double dt = 1.79769313486231571e308;
+  if (i < V.nc) {
+    const size_t n = V.nc;
+    double sum = 0.0;
+    const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+    for (int e = cb; e < ce; ++e) {
+      const int code = V.cfEnt[e];
+      if (code >= 0) {
+        const int f = code >> 1, c1 = V.fc1[f], c2 = V.fc2[f];
+        const double nx = V.fnx[f], ny = V.fny[f], nz = V.fnz[f], nm = V.fnm[f];
+        const double ir1 = 1.0 / V.cv[c1], ir2 = 1.0 / V.cv[c2];
+        const double u1 = V.cv[n + c1] * ir1, v1 = V.cv[2 * n + c1] * ir1, w1 = V.cv[3 * n + c1] * ir1;
+        const double u2 = V.cv[n + c2] * ir2, v2 = V.cv[2 * n + c2] * ir2, w2 = V.cv[3 * n + c2] * ir2;
+        const double a1 = V.dv[2 * n + c1], a2 = V.dv[2 * n + c2];
+        const double vc = 0.5 * ((u1 + u2) * nx + (v1 + v2) * ny + (w1 + w2) * nz);
+        const double as = 0.5 * (a1 + a2);
+        sum = sum + (fabs(vc - 0.0) + as) * nm;
+      } else {
+        const int b = -code - 1;
+        const double nx = V.bnx[b], ny = V.bny[b], nz = V.bnz[b], nm = V.bnm[b];
+        const double ir1 = 1.0 / V.cv[i];
+        const double u1 = V.cv[n + i] * ir1, v1 = V.cv[2 * n + i] * ir1, w1 = V.cv[3 * n + i] * ir1;
+        const double vc = u1 * nx + v1 * ny + w1 * nz;
+        sum = sum + (fabs(vc - 0.0) + V.dv[2 * n + i]) * nm;
+      }
+    }
+    dt = V.vol[i] / sum;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dt = fmin(dt, __shfl_xor_sync(0xffffffffu, dt, o));
+  __shared__ double wmin[kBlock / 32];
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = dt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = wmin[0];
+    for (int w = 1; w < kBlock / 32; ++w) m = fmin(m, wmin[w]);
+    if (m > 0.0) atomicMin(&V.sc->dtBits, (unsigned long long)__double_as_longlong(m));
+    else atomicMin(&V.sc->dtBits, 0ull);
+  }
+}
+
+// RFLU_MinimumTimeStep (rocflu/RFLU_MinimumTimeStep.F90:100-245) and the
+// endTime clip of RFLU_TimeStepping (rocflu/RFLU_TimeStepping.F90:444-446).
+__device__ inline void finalizeDt(const Params &P, Scalars *sc) {
+  double dtMin = __longlong_as_double((long long)sc->dtBits);
+  double cfl = P.cfl;
+  if (P.rkScheme == 1) cfl = fmin2(cfl, 3.0);
+  else if (P.rkScheme == 2) cfl = fmin2(cfl, 2.0);
+  else cfl = fmin2(cfl, 1.0);
+  dtMin = cfl * dtMin;
+  double wtI = 0.0, wtC = 0.0;
+  if (sc->time <= 1.0e-8) wtI = 1.0; else wtC = 1.0;
+  dtMin = wtI / P.dtImposed + wtC / dtMin;
+  dtMin = 1.0 / dtMin;
+  if (dtMin <= 0.0) dtMin = 6.0e-12;
+  dtMin = fmax2(dtMin, P.dtMinLimit);
+  if (sc->endTime > 0.0 && sc->time + dtMin > sc->endTime) {
+    dtMin = sc->endTime - sc->time;
+    sc->finished = 1;
+  }
+  sc->dtMin = dtMin;
+}
+
+template <typename R>
+__global__ void kStepBegin(View<R> V) {
+  // a step after the clipped last step does nothing (finished < 0)
+  if (V.sc->finished > 0) V.sc->finished = -1;
+  V.sc->dtBits = 0x7fefffffffffffffull;
+}
+
+template <typename R>
+__global__ void kDtFinalize(View<R> V) {
+  if (V.sc->finished < 0) return;
+  finalizeDt(V.p, V.sc);
+}
+
+template <typename R>
+__global__ void kStepEnd(View<R> V) {
+  if (V.sc->finished < 0) return;
+  V.sc->time = V.sc->time + V.sc->dtMin;
+  V.sc->stepsDone += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers of this precision
+// ---------------------------------------------------------------------------
+template <typename R>
+struct Launch {
+  static void initState(const View<R> &V, cudaStream_t s) { kInitState<R><<<blocks(V.nc), kBlock, 0, s>>>(V); }
+  static void gradLimit(const View<R> &V, cudaStream_t s) {
+    if (V.p.spaceOrder > 1) kGradLimit<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+  }
+  static void faceFlux(const View<R> &V, cudaStream_t s) {
+    kFaceFlux<R><<<blocks((long long)V.nf + V.nb), kBlock, 0, s>>>(V);
+  }
+  static void gatherRhs(const View<R> &V, cudaStream_t s) { kGatherRhs<R><<<blocks(V.nc), kBlock, 0, s>>>(V); }
+  static void gatherUpdate(const View<R> &V, int iStage, const double *dtp, cudaStream_t s) {
+    kGatherUpdate<R><<<blocks(V.nc), kBlock, 0, s>>>(V, iStage, dtp);
+  }
+  static void timestep(const View<R> &V, cudaStream_t s) {
+    kStepBegin<R><<<1, 1, 0, s>>>(V);
+    kCellDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+    kDtFinalize<R><<<1, 1, 0, s>>>(V);
+  }
+  static void stepEnd(const View<R> &V, cudaStream_t s) { kStepEnd<R><<<1, 1, 0, s>>>(V); }
+};
+
+}  // namespace RFLU_NS
+}  // namespace rflu

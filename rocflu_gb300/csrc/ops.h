@@ -1,0 +1,30 @@
+// Launcher table of one precision mode.  Each kernel translation unit
+// (kernels_fp64.cu, kernels_fp64x.cu, kernels_mixed.cu) fills one table; the
+// C ABI picks the table from rflu_num_desc::precision.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ctx.h"
+
+namespace rflu {
+
+template <typename R>
+struct Ops {
+  void (*initState)(const View<R> &, cudaStream_t);
+  void (*gradLimit)(const View<R> &, cudaStream_t);
+  void (*faceFlux)(const View<R> &, cudaStream_t);
+  void (*gatherRhs)(const View<R> &, cudaStream_t);
+  void (*gatherUpdate)(const View<R> &, int, const double *, cudaStream_t);
+  void (*timestep)(const View<R> &, cudaStream_t);
+  void (*stepEnd)(const View<R> &, cudaStream_t);
+  // tangent / adjoint of the residual (FP64 modes only; null elsewhere)
+  void (*jvp)(const View<R> &, const double *cvDot, double *rhsDot, double *work, cudaStream_t);
+  void (*vjp)(const View<R> &, const double *rhsBar, double *cvBar, double *work, cudaStream_t);
+  void (*patchPressure)(const View<R> &, int iPatch, double *J, double *cvBar, double *work, cudaStream_t);
+};
+
+const Ops<double> *opsFp64();
+const Ops<double> *opsFp64Exact();
+const Ops<float> *opsMixed();
+
+}  // namespace rflu

@@ -1,0 +1,285 @@
+// Point-wise physics of the path, generic in the scalar type S (double,
+// float, or the dual numbers of the tangent/adjoint kernels).  Each function
+// keeps the operation order of the reference routine it cites, so that the
+// FP64 build without FMA contraction reproduces the reference bit for bit.
+#pragma once
+#include <cmath>
+
+namespace rflu {
+
+__host__ __device__ inline double sqrt_(double x) { return sqrt(x); }
+__host__ __device__ inline float sqrt_(float x) { return sqrtf(x); }
+__host__ __device__ inline double fabs_(double x) { return fabs(x); }
+__host__ __device__ inline float fabs_(float x) { return fabsf(x); }
+__host__ __device__ inline double copysign_(double a, double b) { return copysign(a, b); }
+__host__ __device__ inline float copysign_(float a, float b) { return copysignf(a, b); }
+// Fortran MIN/MAX of two reals (first argument kept on ties)
+template <typename S> __host__ __device__ inline S fmin2(const S &a, const S &b) { return (b < a) ? b : a; }
+template <typename S> __host__ __device__ inline S fmax2(const S &a, const S &b) { return (b > a) ? b : a; }
+
+// libfloflu/MixtPerf_*.F90
+template <typename S> __host__ __device__ inline S perfEo(S d, S g, S p, S u, S v, S w) {  // MixtPerf_E.F90:79
+  return p / (d * (g - S(1))) + S(0.5) * (u * u + v * v + w * w);
+}
+template <typename S> __host__ __device__ inline S perfHo(S cp, S t, S u, S v, S w) {      // MixtPerf_H.F90:78
+  return cp * t + S(0.5) * (u * u + v * v + w * w);
+}
+template <typename S> __host__ __device__ inline S perfCGHoVm2(S g, S ho, S vm2) {          // MixtPerf_C.F90:110
+  return sqrt_((g - S(1)) * (ho - S(0.5) * vm2));
+}
+
+// modflu/RFLU_ModEntropyFixes.F90:95-106
+template <typename S> __host__ __device__ inline S entropyFixHH(S l, S d) {
+  if (l > d) return l;
+  return (l * l + d * d) / (S(2) * d);
+}
+
+// Roe flux with the Harten-Hyman fix, flxConv - flxDiss:
+// RFLU_ROE_ComputeFlux1_TCP / _Flux2_TCP (modflu/RFLU_ModRoeFlux.F90:
+// 1683-1942, 2513-2867).
+template <typename S>
+__host__ __device__ inline void roeFlux(S g, S epsentr, S dissFact, S nx, S ny, S nz, S nm, S rl, S ul, S vl, S wl,
+                                        S pl, S Hl, S rr, S ur, S vr, S wr, S pr, S Hr, S *flx) {
+  const S fs = S(0);
+  S ql = ul * nx + vl * ny + wl * nz - fs;
+  S qr = ur * nx + vr * ny + wr * nz - fs;
+  S rh = sqrt_(rl * rr);
+  S wt = rl / (rl + rh);
+  S uh = wt * ul + (S(1) - wt) * ur;
+  S vh = wt * vl + (S(1) - wt) * vr;
+  S wh = wt * wl + (S(1) - wt) * wr;
+  S Hh = wt * Hl + (S(1) - wt) * Hr;
+  S qh = uh * nx + vh * ny + wh * nz - fs;
+  S sh = S(0.5) * (uh * uh + vh * vh + wh * wh);
+  S ah = perfCGHoVm2(g, Hh, S(2) * sh);
+  S l1 = fabs_(qh - ah), l2 = fabs_(qh), l5 = fabs_(qh + ah);
+  S efc = epsentr * l5;
+  l1 = entropyFixHH(l1, efc);
+  l2 = entropyFixHH(l2, efc);
+  l5 = entropyFixHH(l5, efc);
+  S dr = rr - rl, du = ur - ul, de = vr - vl, dw = wr - wl, dp = pr - pl;
+  S dq = du * nx + de * ny + dw * nz;
+  S dv1 = (dp - rh * ah * dq) / (S(2) * ah * ah);
+  S dv5 = (dp + rh * ah * dq) / (S(2) * ah * ah);
+  S dv2 = dr - dp / (ah * ah);
+  S t1 = l1 * dv1, t2 = l2 * dv2, t3 = l2 * rh, t5 = l5 * dv5;
+  S h = S(0.5), hd = S(0.5) * dissFact;
+  S fc1 = h * (ql * rl + qr * rr) * nm;
+  S fc2 = h * (ql * rl * ul + pl * nx + qr * rr * ur + pr * nx) * nm;
+  S fc3 = h * (ql * rl * vl + pl * ny + qr * rr * vr + pr * ny) * nm;
+  S fc4 = h * (ql * rl * wl + pl * nz + qr * rr * wr + pr * nz) * nm;
+  S fc5 = h * (ql * rl * Hl + pl * fs + qr * rr * Hr + pr * fs) * nm;
+  S fd1 = hd * (t1 + t2 + t5) * nm;
+  S fd2 = hd * (t1 * (uh - nx * ah) + t2 * uh + t3 * (du - nx * dq) + t5 * (uh + nx * ah)) * nm;
+  S fd3 = hd * (t1 * (vh - ny * ah) + t2 * vh + t3 * (de - ny * dq) + t5 * (vh + ny * ah)) * nm;
+  S fd4 = hd * (t1 * (wh - nz * ah) + t2 * wh + t3 * (dw - nz * dq) + t5 * (wh + nz * ah)) * nm;
+  S fd5 = hd * (t1 * (Hh - qh * ah) + t2 * sh + t3 * (uh * du + vh * de + wh * dw - qh * dq) + t5 * (Hh + qh * ah)) * nm;
+  flx[0] = fc1 - fd1; flx[1] = fc2 - fd2; flx[2] = fc3 - fd3; flx[3] = fc4 - fd4; flx[4] = fc5 - fd5;
+}
+
+// HLLC: RFLU_HLLC_ComputeFlux1_TCP / _Flux2_TCP (modflu/RFLU_ModHLLCFlux.F90:
+// 926-1194, 2131-2434).
+template <typename S>
+__host__ __device__ inline void hllcFlux(S g, S nx, S ny, S nz, S nm, S rl, S ul, S vl, S wl, S pl, S el, S al, S Hl,
+                                         S rr, S ur, S vr, S wr, S pr, S er, S ar, S Hr, S *flx) {
+  const S fs = S(0);
+  S ql = ul * nx + vl * ny + wl * nz - fs;
+  S qr = ur * nx + vr * ny + wr * nz - fs;
+  S wt1 = sqrt_(rr / rl);
+  S wt2 = S(1) / (S(1) + wt1);
+  S us = wt2 * (ul + wt1 * ur);
+  S vs = wt2 * (vl + wt1 * vr);
+  S ws = wt2 * (wl + wt1 * wr);
+  S qs = wt2 * (ql + wt1 * qr);
+  S Hs = wt2 * (Hl + wt1 * Hr);
+  S Vms = us * us + vs * vs + ws * ws;
+  S as = perfCGHoVm2(g, Hs, Vms);
+  S sl = fmin2(ql - al, qs - as);
+  S sr = fmax2(qr + ar, qs + as);
+  if (sl > S(0)) {
+    flx[0] = ql * rl * nm;
+    flx[1] = (ql * rl * ul + pl * nx) * nm;
+    flx[2] = (ql * rl * vl + pl * ny) * nm;
+    flx[3] = (ql * rl * wl + pl * nz) * nm;
+    flx[4] = (ql * (rl * el + pl) + pl * fs) * nm;
+  } else if (sr < S(0)) {
+    flx[0] = qr * rr * nm;
+    flx[1] = (qr * rr * ur + pr * nx) * nm;
+    flx[2] = (qr * rr * vr + pr * ny) * nm;
+    flx[3] = (qr * rr * wr + pr * nz) * nm;
+    flx[4] = (qr * (rr * er + pr) + pr * fs) * nm;
+  } else {
+    S sm = (rr * qr * (sr - qr) - rl * ql * (sl - ql) - pr + pl) / (rr * (sr - qr) - rl * (sl - ql));
+    S ps = pl + rl * (ql - sl) * (ql - sm);
+    S rs, rus, rvs, rws, res;
+    if (sm > S(0)) {
+      S term = S(1) / (sl - sm);
+      rs = term * (sl - ql) * rl;
+      rus = term * ((sl - ql) * rl * ul + (ps - pl) * nx);
+      rvs = term * ((sl - ql) * rl * vl + (ps - pl) * ny);
+      rws = term * ((sl - ql) * rl * wl + (ps - pl) * nz);
+      res = term * ((sl - ql) * rl * el + (ps * sm - pl * ql));
+    } else {
+      S term = S(1) / (sr - sm);
+      rs = term * (sr - qr) * rr;
+      rus = term * ((sr - qr) * rr * ur + (ps - pr) * nx);
+      rvs = term * ((sr - qr) * rr * vr + (ps - pr) * ny);
+      rws = term * ((sr - qr) * rr * wr + (ps - pr) * nz);
+      res = term * ((sr - qr) * rr * er + (ps * sm - pr * qr));
+    }
+    flx[0] = sm * rs * nm;
+    flx[1] = (sm * rus + ps * nx) * nm;
+    flx[2] = (sm * rvs + ps * ny) * nm;
+    flx[3] = (sm * rws + ps * nz) * nm;
+    flx[4] = (sm * (res + ps) - ps * fs) * nm;
+  }
+}
+
+// AUSM+: RFLU_AUSM_FluxFunction (modflu/RFLU_ModAUSMFlux.F90:282-416).
+template <typename S>
+__host__ __device__ inline void ausmFlux(S nx, S ny, S nz, S nm, S rl, S ul, S vl, S wl, S pl, S Hl, S al, S rr, S ur,
+                                         S vr, S wr, S pr, S Hr, S ar, S *flx) {
+  const S fs = S(0), one = S(1);
+  S ql = ul * nx + vl * ny + wl * nz - fs;
+  S qr = ur * nx + vr * ny + wr * nz - fs;
+  S af = S(0.5) * (al + ar);
+  S ml = ql / af, mla = fabs_(ml);
+  S mr = qr / af, mra = fabs_(mr);
+  S mlp, wtl, mrm, wtr;
+  if (mla <= one) {
+    mlp = S(0.25) * (ml + one) * (ml + one) + S(0.125) * (ml * ml - one) * (ml * ml - one);
+    wtl = S(0.25) * (ml + one) * (ml + one) * (S(2) - ml) + S(0.1875) * ml * (ml * ml - one) * (ml * ml - one);
+  } else {
+    mlp = S(0.5) * (ml + mla);
+    wtl = S(0.5) * (one + ml / mla);
+  }
+  if (mra <= one) {
+    mrm = -S(0.25) * (mr - one) * (mr - one) - S(0.125) * (mr * mr - one) * (mr * mr - one);
+    wtr = S(0.25) * (mr - one) * (mr - one) * (S(2) + mr) - S(0.1875) * mr * (mr * mr - one) * (mr * mr - one);
+  } else {
+    mrm = S(0.5) * (mr - mra);
+    wtr = S(0.5) * (one - mr / mra);
+  }
+  S mf = mlp + mrm, mfa = fabs_(mf);
+  S mfp = S(0.5) * (mf + mfa), mfm = S(0.5) * (mf - mfa);
+  S pf = wtl * pl + wtr * pr;
+  flx[0] = (af * (mfp * rl + mfm * rr)) * nm;
+  flx[1] = (af * (mfp * rl * ul + mfm * rr * ur) + pf * nx) * nm;
+  flx[2] = (af * (mfp * rl * vl + mfm * rr * vr) + pf * ny) * nm;
+  flx[3] = (af * (mfp * rl * wl + mfm * rr * wr) + pf * nz) * nm;
+  flx[4] = (af * (mfp * rl * Hl + mfm * rr * Hr) + pf * fs) * nm;
+}
+
+// BcondOutflowPerf (libfloflu/BcondOutflowPerf.F90:88-159).
+template <typename S>
+__host__ __device__ inline void bcondOutflowPerf(int bcOpt, S pout, S sxn, S syn, S szn, S cpgas, S mol, S rho, S rhou,
+                                                 S rhov, S rhow, S rhoe, S press, S &rhob, S &rhoub, S &rhovb,
+                                                 S &rhowb, S &rhoeb) {
+  S rgas = S(8314.3) / mol;
+  S gamma = cpgas / (cpgas - rgas);
+  S u = rhou / rho, v = rhov / rho, w = rhow / rho;
+  S csound = sqrt_(gamma * press / rho);
+  S mach = sqrt_(u * u + v * v + w * w) / csound;
+  if (mach < S(1) && (bcOpt == 1 || bcOpt == 2)) {
+    S rrhoc = S(1) / (rho * csound);
+    S deltp = press - pout;
+    rhob = rho - deltp / (csound * csound);
+    S ub = u + sxn * deltp * rrhoc;
+    S vb = v + syn * deltp * rrhoc;
+    S wb = w + szn * deltp * rrhoc;
+    S vnd = ub * sxn + vb * syn + wb * szn;
+    if (vnd < S(0)) {
+      ub = copysign_(S(1), u) * fmax2(fabs_(ub), fabs_(u));
+      vb = copysign_(S(1), v) * fmax2(fabs_(vb), fabs_(v));
+      wb = copysign_(S(1), w) * fmax2(fabs_(wb), fabs_(w));
+    }
+    rhoub = rhob * ub;
+    rhovb = rhob * vb;
+    rhowb = rhob * wb;
+    rhoeb = rhob * perfEo(rhob, gamma, pout, ub, vb, wb);
+  } else {
+    rhob = rho; rhoub = rhou; rhovb = rhov; rhowb = rhow; rhoeb = rhoe;
+  }
+}
+
+// Central patch flux on outflow faces (rocflu/RFLU_CentralFirstPatch.F90:
+// 571-784, RFLU_CentralSecondPatch.F90:634-857).
+template <typename S>
+__host__ __device__ inline void outflowPatchFlux(int bcOpt, S pOut, S cp, S mol, S nx, S ny, S nz, S nm, S rl, S rul,
+                                                 S rvl, S rwl, S rel, S pl, S *flx) {
+  const S fs = S(0);
+  S pr = (bcOpt != 0) ? pOut : pl;
+  S rr, rur, rvr, rwr, rer;
+  bcondOutflowPerf(bcOpt, pr, nx, ny, nz, cp, mol, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr, rer);
+  S ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
+  S qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
+  S h = S(0.5);
+  flx[0] = h * (ql * rl + qr * rr) * nm;
+  flx[1] = h * (ql * rul + pl * nx + qr * rur + pr * nx) * nm;
+  flx[2] = h * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
+  flx[3] = h * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
+  flx[4] = h * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 (RFLU_SymmetricEigen3,
+// modflu/RFLU_ModLimiters.F90:791-912): ascending eigenvalues, eigenvectors
+// as columns.  m, vec are column-major.
+template <typename S>
+__host__ __device__ inline void symmetricEigen3(const S m[9], S vec[9], S val[3]) {
+  S r[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { r[k] = m[k]; vec[k] = S(0); }
+  vec[0] = vec[4] = vec[8] = S(1);
+  S total = S(0);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) total = total + r[k] * r[k];
+  const S tol = S(1.0e-24);
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    S off = r[3] * r[3] + r[6] * r[6] + r[7] * r[7];
+    if (off <= tol * total) break;
+#pragma unroll
+    for (int ip = 0; ip < 2; ++ip)
+#pragma unroll
+      for (int iq = ip + 1; iq < 3; ++iq) {
+        const int pq = ip + 3 * iq, pp = ip + 3 * ip, qq = iq + 3 * iq;
+        if (r[pq] != S(0)) {
+          S theta = (r[qq] - r[pp]) / (S(2) * r[pq]);
+          S t;
+          if (fabs_(theta) > S(1.0e150)) t = S(0.5) / theta;
+          else t = copysign_(S(1), theta) / (fabs_(theta) + sqrt_(theta * theta + S(1)));
+          S c = S(1) / sqrt_(t * t + S(1));
+          S s = t * c;
+          const int ir = 3 - ip - iq;
+          S arp = r[ir + 3 * ip], arq = r[ir + 3 * iq];
+          r[pp] = r[pp] - t * r[pq];
+          r[qq] = r[qq] + t * r[pq];
+          r[pq] = S(0);
+          r[iq + 3 * ip] = S(0);
+          r[ir + 3 * ip] = c * arp - s * arq;
+          r[ip + 3 * ir] = r[ir + 3 * ip];
+          r[ir + 3 * iq] = s * arp + c * arq;
+          r[iq + 3 * ir] = r[ir + 3 * iq];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            S vp = vec[i + 3 * ip], vq = vec[i + 3 * iq];
+            vec[i + 3 * ip] = c * vp - s * vq;
+            vec[i + 3 * iq] = s * vp + c * vq;
+          }
+        }
+      }
+  }
+  val[0] = r[0]; val[1] = r[4]; val[2] = r[8];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    int iMin = i;
+    for (int k = i + 1; k < 3; ++k)
+      if (val[k] < val[iMin]) iMin = k;
+    if (iMin != i) {
+      S t = val[i]; val[i] = val[iMin]; val[iMin] = t;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { S x = vec[k + 3 * i]; vec[k + 3 * i] = vec[k + 3 * iMin]; vec[k + 3 * iMin] = x; }
+    }
+  }
+}
+
+}  // namespace rflu

@@ -1,0 +1,503 @@
+// Host set-up of one region: face list, geometry, C2C stencils and stencil
+// moments, reproducing the numbering and the FP64 values that
+// RFLU_InitFlowSolver (rocflu/RFLU_InitFlowSolver.F90:496-931) leaves in
+// t_grid.  Built with -ffp-contract=off so that every value matches the
+// reference's no-FMA evaluation bit for bit.
+//
+// Face list: the reference hashes each cell face in the cell loop and numbers
+// faces by first insertion (RFLU_BuildFaceList, modflu/RFLU_ModFaceList.F90:
+// 784-1585; RFLU_HashFace, modflu/RFLU_ModHashTable.F90:618-734).  Here every
+// (cell, local face) slot gets a vertex key, slots are bucketed by smallest
+// vertex and sorted, and a matched pair's face id is the rank of its lower
+// slot -- the same order, built without a hash table and in parallel.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "../../include/rflu_gpu.h"
+#include "errors.h"
+
+namespace {
+
+// Local faces (modflu/RFLU_ModGrid.F90:92-96), 0-based.
+const int kTetFace[4][3] = {{0, 1, 2}, {1, 3, 2}, {0, 2, 3}, {0, 3, 1}};
+const int kHexFace[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {0, 4, 7, 3}, {4, 5, 6, 7}};
+
+struct SlotKey {
+  int k1, k2;    // 2nd and 3rd smallest vertex (bucket = smallest)
+  int64_t slot;  // cell*nLocalFaces + localFace, or -(1+boundary face index)
+};
+
+// Face vector and centroid of a triangle or quadrilateral, the formulas of
+// FaceVectorTria/Quad (libfloflu/FaceVector.F90) and FaceCentroidTria/Quad
+// (libfloflu/FaceCentroid.F90).
+void faceGeom(const double *xyz, const int *v, int nv, double *vec, double *cen) {
+  const double *a = xyz + 3 * (size_t)v[0], *b = xyz + 3 * (size_t)v[1], *c = xyz + 3 * (size_t)v[2];
+  if (nv == 3) {
+    double e1x = a[0] - b[0], e1y = a[1] - b[1], e1z = a[2] - b[2];
+    double e2x = a[0] - c[0], e2y = a[1] - c[1], e2z = a[2] - c[2];
+    vec[0] = 0.5 * (e1y * e2z - e2y * e1z);
+    vec[1] = -0.5 * (e1x * e2z - e2x * e1z);
+    vec[2] = 0.5 * (e1x * e2y - e2x * e1y);
+    const double third = 1.0 / 3.0;
+    for (int d = 0; d < 3; ++d) cen[d] = third * (a[d] + b[d] + c[d]);
+  } else {
+    const double *q = xyz + 3 * (size_t)v[3];
+    double dax = c[0] - a[0], day = c[1] - a[1], daz = c[2] - a[2];
+    double dbx = b[0] - q[0], dby = b[1] - q[1], dbz = b[2] - q[2];
+    vec[0] = 0.5 * (daz * dby - day * dbz);
+    vec[1] = 0.5 * (dax * dbz - daz * dbx);
+    vec[2] = 0.5 * (day * dbx - dax * dby);
+    for (int d = 0; d < 3; ++d) cen[d] = 0.25 * (a[d] + b[d] + c[d] + q[d]);
+  }
+}
+
+// Unstable quicksort of (fraction, cell) pairs by fraction.  Equal
+// fractions keep the order this particular partition scheme produces, which
+// decides which equally-shared neighbours survive the 40-member cap; it is
+// the partition of QuickSortRFREALInteger (modfloflu/ModSortSearch.F90:
+// 990-1091), which the stencil must reproduce exactly.
+void sortFractions(double *a, int *b, int n) {
+  if (n <= 0) return;
+  int lo[50], hi[50], top = 0;
+  lo[0] = 0;
+  hi[0] = n - 1;
+  top = 1;
+  while (top > 0) {
+    --top;
+    int l = lo[top], r = hi[top];
+    while (l < r) {
+      int i = l, j = r;
+      const double pivot = a[(l + r + 2) / 2 - 1];
+      for (;;) {
+        while (a[i] < pivot) ++i;
+        while (pivot < a[j]) --j;
+        if (i > j) break;
+        std::swap(a[i], a[j]);
+        std::swap(b[i], b[j]);
+        ++i;
+        --j;
+        if (i > j) break;
+      }
+      if (j - l >= r - i) {
+        if (l < j) { lo[top] = l; hi[top] = j; ++top; }
+        l = i;
+      } else {
+        if (i < r) { lo[top] = i; hi[top] = r; ++top; }
+        r = j;
+      }
+    }
+  }
+}
+
+// Singular-value ratio test of RFLU_InvertMatrixSVD (libflu/
+// RFLU_InvertMatrixSVD.F90): the eigenvalues of the 4x4 normal matrix
+// A^T A (cyclic Jacobi) give the singular values of the column-scaled
+// stencil matrix; returns how many count as zero.
+int singularCount(const std::vector<double> &A, int rows) {
+  double g[4][4] = {};
+  for (int p = 0; p < 4; ++p)
+    for (int q = p; q < 4; ++q) {
+      double s = 0.0;
+      for (int r = 0; r < rows; ++r) s += A[r * 4 + p] * A[r * 4 + q];
+      g[p][q] = g[q][p] = s;
+    }
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int p = 0; p < 4; ++p)
+      for (int q = 0; q < 4; ++q) (p == q ? tot : off) += g[p][q] * g[p][q];
+    if (off <= 1e-30 * tot) break;
+    for (int p = 0; p < 3; ++p)
+      for (int q = p + 1; q < 4; ++q) {
+        if (g[p][q] == 0.0) continue;
+        double th = (g[q][q] - g[p][p]) / (2.0 * g[p][q]);
+        double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 4; ++k) {
+          double gkp = g[k][p], gkq = g[k][q];
+          g[k][p] = c * gkp - s * gkq;
+          g[k][q] = s * gkp + c * gkq;
+        }
+        for (int k = 0; k < 4; ++k) {
+          double gpk = g[p][k], gqk = g[q][k];
+          g[p][k] = c * gpk - s * gqk;
+          g[q][k] = s * gpk + c * gqk;
+        }
+      }
+  }
+  double sv[4];
+  for (int p = 0; p < 4; ++p) sv[p] = std::sqrt(std::max(g[p][p], 0.0));
+  std::sort(sv, sv + 4, [](double x, double y) { return x > y; });
+  int count = (sv[0] > 100.0 * 2.220446049250313e-16) ? 0 : 1;
+  for (int i = 1; i < 4; ++i)
+    if (!(sv[i] > 0.01 * sv[i - 1])) { count += 4 - i; break; }
+  return count;
+}
+
+}  // namespace
+
+struct rflu_setup {
+  int nCells = 0, nFaces = 0, nPatches = 0;
+  std::vector<int> f2c;
+  std::vector<double> fn, fc, vol, cofg;
+  std::vector<int> patchFaceOff, bf2c;
+  std::vector<double> bfn, bfc;
+  std::vector<int> c2csOff, c2csMembs;
+  std::vector<double> xyzMoms;
+};
+
+extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_setup **out) {
+  if (!m || !out || !m->xyz || !m->c2v || m->nCells <= 0 || (m->nVertPerCell != 4 && m->nVertPerCell != 8))
+    return rflu::fail(RFLU_ERR_ARG, "rflu_setup_build: bad mesh description (pure tet or hex meshes only)");
+  rflu_setup *S = new (std::nothrow) rflu_setup();
+  if (!S) return rflu::fail(RFLU_ERR_ARG, "rflu_setup_build: out of host memory");
+  const int nc = m->nCells, nvc = m->nVertPerCell, nv = m->nVert;
+  const int nfl = (nvc == 4) ? 4 : 6, fvs = (nvc == 4) ? 3 : 4;
+  auto vert = [&](int ic, int k) { return m->c2v[(size_t)nvc * ic + k] - 1; };
+  auto localFace = [&](int lf, int k) { return (nvc == 4) ? kTetFace[lf][k] : kHexFace[lf][k]; };
+  S->nCells = nc;
+
+  // ---- slot keys, bucketed by smallest vertex (counting sort) -------------
+  const int64_t nSlots = (int64_t)nc * nfl;
+  const int nb = m->patchFaceOff ? m->patchFaceOff[m->nPatches] : 0;
+  std::vector<int> bucketOff(nv + 1, 0);
+  std::vector<int> smallest(nSlots + nb);
+  std::vector<SlotKey> keys(nSlots + nb);
+#pragma omp parallel for schedule(static)
+  for (int64_t s = 0; s < nSlots; ++s) {
+    int ic = (int)(s / nfl), lf = (int)(s % nfl), fv[4];
+    for (int k = 0; k < fvs; ++k) fv[k] = vert(ic, localFace(lf, k));
+    std::sort(fv, fv + fvs);
+    smallest[s] = fv[0];
+    keys[s] = {fv[1], fv[2], s};
+  }
+  for (int b = 0; b < nb; ++b) {
+    const int *bv = m->bf2v + 4 * (size_t)b;
+    int n = (bv[3] <= 0) ? 3 : 4, fv[4];
+    for (int k = 0; k < n; ++k) fv[k] = bv[k] - 1;
+    std::sort(fv, fv + n);
+    smallest[nSlots + b] = fv[0];
+    keys[nSlots + b] = {fv[1], fv[2], -(int64_t)(b + 1)};
+  }
+  for (int64_t s = 0; s < nSlots + nb; ++s) bucketOff[smallest[s] + 1]++;
+  for (int v = 0; v < nv; ++v) bucketOff[v + 1] += bucketOff[v];
+  std::vector<SlotKey> sorted(nSlots + nb);
+  {
+    std::vector<int> fill(bucketOff.begin(), bucketOff.end() - 1);
+    for (int64_t s = 0; s < nSlots + nb; ++s) sorted[fill[smallest[s]]++] = keys[s];
+  }
+  keys.clear();
+  keys.shrink_to_fit();
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int v = 0; v < nv; ++v)
+    std::sort(sorted.begin() + bucketOff[v], sorted.begin() + bucketOff[v + 1], [](const SlotKey &a, const SlotKey &b) {
+      if (a.k1 != b.k1) return a.k1 < b.k1;
+      if (a.k2 != b.k2) return a.k2 < b.k2;
+      return a.slot > b.slot;  // boundary entries (negative) after cell slots
+    });
+
+  // ---- pair matching: interior faces, boundary owners -----------------------
+  std::vector<int64_t> lowSlot;       // per interior face: lower slot
+  std::vector<int> highCell;
+  std::vector<int> bOwner(nb, -1);
+  std::vector<char> bad(1, 0);
+  lowSlot.reserve(nSlots / 2 + 1);
+  for (int v = 0; v < nv; ++v) {
+    // a group of equal keys never spans two buckets
+    size_t i = bucketOff[v], n = bucketOff[v + 1];
+    while (i < n) {
+      size_t j = i + 1;
+      while (j < n && sorted[j].k1 == sorted[i].k1 && sorted[j].k2 == sorted[i].k2) ++j;
+      // group [i,j): cell slots in descending order, then boundary entries
+      int nCellSlots = 0;
+      for (size_t k = i; k < j; ++k) nCellSlots += (sorted[k].slot >= 0);
+      if (nCellSlots == 2) {
+        int64_t a = sorted[i].slot, b = sorted[i + 1].slot;  // a > b
+        lowSlot.push_back(b);
+        highCell.push_back((int)(a / nfl));
+        if (j - i > 2) bad[0] = 1;  // a boundary face on an interior face
+      } else if (nCellSlots == 1) {
+        for (size_t k = i + 1; k < j; ++k) bOwner[-sorted[k].slot - 1] = (int)(sorted[i].slot / nfl);
+      } else {
+        bad[0] = 1;
+      }
+      i = j;
+    }
+  }
+  sorted.clear();
+  sorted.shrink_to_fit();
+  if (bad[0]) { delete S; return rflu::fail(RFLU_ERR_ARG, "rflu_setup_build: non-conforming mesh"); }
+  for (int b = 0; b < nb; ++b)
+    if (bOwner[b] < 0) { delete S; return rflu::fail(RFLU_ERR_ARG, "rflu_setup_build: boundary face without a cell"); }
+
+  // faces in first-insertion order = ascending lower slot
+  const int nf = (int)lowSlot.size();
+  std::vector<int> order(nf);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return lowSlot[a] < lowSlot[b]; });
+  S->nFaces = nf;
+  S->f2c.resize(2 * (size_t)nf);
+  std::vector<int> f2v(4 * (size_t)nf, -1);
+  for (int f = 0; f < nf; ++f) {
+    int64_t s = lowSlot[order[f]];
+    int ic = (int)(s / nfl), lf = (int)(s % nfl);
+    S->f2c[2 * (size_t)f] = ic;
+    S->f2c[2 * (size_t)f + 1] = highCell[order[f]];
+    for (int k = 0; k < fvs; ++k) f2v[4 * (size_t)f + k] = vert(ic, localFace(lf, k));
+  }
+
+  // ---- geometry (RFLU_BuildGeometry) ----------------------------------------
+  const double *xyz = m->xyz;
+  std::vector<double> app(3 * (size_t)nc);
+  const double w = (nvc == 4) ? 0.25 : 0.125;
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < nc; ++ic)
+    for (int d = 0; d < 3; ++d) {
+      double s = xyz[3 * (size_t)vert(ic, 0) + d];
+      for (int k = 1; k < nvc; ++k) s = s + xyz[3 * (size_t)vert(ic, k) + d];
+      app[3 * (size_t)ic + d] = w * s;
+    }
+  S->fn.resize(4 * (size_t)nf);
+  S->fc.resize(3 * (size_t)nf);
+  std::vector<double> fvec(3 * (size_t)nf);
+#pragma omp parallel for schedule(static)
+  for (int f = 0; f < nf; ++f) {
+    int nvf = (f2v[4 * (size_t)f + 3] < 0) ? 3 : 4;
+    double *v = &fvec[3 * (size_t)f], *cen = &S->fc[3 * (size_t)f];
+    faceGeom(xyz, &f2v[4 * (size_t)f], nvf, v, cen);
+    double mag = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    double inv = 1.0 / mag;
+    double *n = &S->fn[4 * (size_t)f];
+    n[0] = v[0] * inv; n[1] = v[1] * inv; n[2] = v[2] * inv; n[3] = mag;
+  }
+  S->nPatches = m->nPatches;
+  S->patchFaceOff.assign(m->patchFaceOff, m->patchFaceOff + m->nPatches + 1);
+  S->bf2c.resize(nb);
+  S->bfn.resize(4 * (size_t)nb);
+  S->bfc.resize(3 * (size_t)nb);
+  std::vector<double> bvec(3 * (size_t)nb);
+  for (int b = 0; b < nb; ++b) {
+    int v[4];
+    const int *bv = m->bf2v + 4 * (size_t)b;
+    int nvf = (bv[3] <= 0) ? 3 : 4;
+    for (int k = 0; k < nvf; ++k) v[k] = bv[k] - 1;
+    double *vv = &bvec[3 * (size_t)b], *cen = &S->bfc[3 * (size_t)b];
+    faceGeom(xyz, v, nvf, vv, cen);
+    double mag = std::sqrt(vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+    double inv = 1.0 / mag;
+    double *n = &S->bfn[4 * (size_t)b];
+    n[0] = vv[0] * inv; n[1] = vv[1] * inv; n[2] = vv[2] * inv; n[3] = mag;
+    S->bf2c[b] = bOwner[b];
+  }
+  // Volume and centroid sums need the reference's face order per cell: the
+  // interior faces in face order, then the patch faces.  Gather them per cell.
+  std::vector<int> cfOff(nc + 1, 0);
+  for (int f = 0; f < nf; ++f) { cfOff[S->f2c[2 * (size_t)f] + 1]++; cfOff[S->f2c[2 * (size_t)f + 1] + 1]++; }
+  for (int b = 0; b < nb; ++b) cfOff[bOwner[b] + 1]++;
+  for (int ic = 0; ic < nc; ++ic) cfOff[ic + 1] += cfOff[ic];
+  std::vector<int> cfEnt(cfOff[nc]);
+  {
+    std::vector<int> fill(cfOff.begin(), cfOff.end() - 1);
+    for (int f = 0; f < nf; ++f) {
+      cfEnt[fill[S->f2c[2 * (size_t)f]]++] = 2 * f;
+      cfEnt[fill[S->f2c[2 * (size_t)f + 1]]++] = 2 * f + 1;
+    }
+    for (int b = 0; b < nb; ++b) cfEnt[fill[bOwner[b]]++] = 2 * nf + b;
+  }
+  S->vol.assign(nc, 0.0);
+  S->cofg.assign(3 * (size_t)nc, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < nc; ++ic) {
+    double vol = 0.0, cg[3] = {0.0, 0.0, 0.0};
+    const double *a = &app[3 * (size_t)ic];
+    for (int e = cfOff[ic]; e < cfOff[ic + 1]; ++e) {
+      int code = cfEnt[e];
+      const double *vv, *cen;
+      bool minus = false;
+      if (code < 2 * nf) {
+        vv = &fvec[3 * (size_t)(code >> 1)];
+        cen = &S->fc[3 * (size_t)(code >> 1)];
+        minus = code & 1;
+      } else {
+        vv = &bvec[3 * (size_t)(code - 2 * nf)];
+        cen = &S->bfc[3 * (size_t)(code - 2 * nf)];
+      }
+      double t = (cen[0] - a[0]) * vv[0] + (cen[1] - a[1]) * vv[1] + (cen[2] - a[2]) * vv[2];
+      vol = minus ? vol - t : vol + t;
+      t = cen[0] * vv[0] + cen[1] * vv[1] + cen[2] * vv[2];
+      for (int d = 0; d < 3; ++d) cg[d] = minus ? cg[d] - t * cen[d] : cg[d] + t * cen[d];
+    }
+    vol = (1.0 / 3.0) * vol;
+    double t = 1.0 / (4.0 * vol);
+    S->vol[ic] = vol;
+    for (int d = 0; d < 3; ++d) S->cofg[3 * (size_t)ic + d] = t * cg[d];
+  }
+
+  // ---- C2C stencils and moments (ORDER > 1) ---------------------------------
+  S->c2csOff.assign(nc + 1, 0);
+  if (spaceOrder > 1) {
+    const int minSize = 4, maxSize = 40, maxLayers = 6;
+    std::vector<int> v2cOff(nv + 1, 0);
+    for (int ic = 0; ic < nc; ++ic)
+      for (int k = 0; k < nvc; ++k) v2cOff[vert(ic, k) + 1]++;
+    for (int v = 0; v < nv; ++v) v2cOff[v + 1] += v2cOff[v];
+    std::vector<int> v2c(v2cOff[nv]);
+    {
+      std::vector<int> fill(v2cOff.begin(), v2cOff.end() - 1);
+      for (int ic = 0; ic < nc; ++ic)
+        for (int k = 0; k < nvc; ++k) v2c[fill[vert(ic, k)]++] = ic;
+    }
+    std::vector<std::vector<int>> memb(nc);
+    const double invNv = 1.0 / (double)nvc;
+    const double *cg = S->cofg.data();
+#pragma omp parallel
+    {
+      std::vector<int> cand, sv(nvc), sv2(nvc), help;
+      std::vector<double> frac, A;
+#pragma omp for schedule(dynamic, 256)
+      for (int ic = 0; ic < nc; ++ic) {
+        cand.clear();
+        for (int k = 0; k < nvc; ++k) {
+          int v = vert(ic, k);
+          cand.insert(cand.end(), v2c.begin() + v2cOff[v], v2c.begin() + v2cOff[v + 1]);
+        }
+        std::sort(cand.begin(), cand.end());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+        cand.erase(std::lower_bound(cand.begin(), cand.end(), ic));
+        const int nCand = (int)cand.size();
+        for (int k = 0; k < nvc; ++k) sv[k] = vert(ic, k);
+        std::sort(sv.begin(), sv.end());
+        frac.resize(nCand);
+        for (int i = 0; i < nCand; ++i) {
+          for (int k = 0; k < nvc; ++k) sv2[k] = vert(cand[i], k);
+          std::sort(sv2.begin(), sv2.end());
+          int shared = 0;
+          for (int a = 0, b = 0; a < nvc && b < nvc;) {
+            if (sv[a] == sv2[b]) { ++shared; ++a; ++b; }
+            else if (sv[a] < sv2[b]) ++a;
+            else ++b;
+          }
+          frac[i] = shared * invNv;
+        }
+        sortFractions(frac.data(), cand.data(), nCand);
+        std::vector<int> st;
+        for (int i = nCand - 1; i >= std::max(nCand - maxSize, 0); --i) st.push_back(cand[i]);
+        std::sort(st.begin(), st.end());
+        int layerBeg = 0, layerEnd = (int)st.size();
+        for (int layer = 2; layer <= maxLayers; ++layer) {
+          int degr = (int)st.size(), sCount = 0;
+          if (degr >= minSize) {
+            A.assign(4 * (size_t)degr, 0.0);
+            for (int r = 0; r < degr; ++r) {
+              int j = st[r];
+              double dx = cg[3 * (size_t)j] - cg[3 * (size_t)ic];
+              double dy = cg[3 * (size_t)j + 1] - cg[3 * (size_t)ic + 1];
+              double dz = cg[3 * (size_t)j + 2] - cg[3 * (size_t)ic + 2];
+              double t = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+              A[4 * r] = t; A[4 * r + 1] = t * dx; A[4 * r + 2] = t * dy; A[4 * r + 3] = t * dz;
+            }
+            for (int col = 0; col < 4; ++col) {
+              double mx = 0.0;
+              for (int r = 0; r < degr; ++r) mx = std::max(mx, std::fabs(A[4 * r + col]));
+              for (int r = 0; r < degr; ++r) A[4 * r + col] /= mx;
+            }
+            sCount = singularCount(A, degr);
+          }
+          if (sCount == 0 && degr >= minSize) break;
+          // one more vertex-neighbour layer (RFLU_AddCellLayer,
+          // modflu/RFLU_ModStencilsUtils.F90:696-949)
+          std::vector<int> have(st);
+          std::sort(have.begin(), have.end());
+          help.clear();
+          bool full = false;
+          for (int i = layerBeg; i < layerEnd && !full; ++i)
+            for (int k = 0; k < nvc && !full; ++k) {
+              int v = vert(st[i], k);
+              for (int e = v2cOff[v]; e < v2cOff[v + 1]; ++e) {
+                int c2 = v2c[e];
+                if (c2 == ic || std::binary_search(have.begin(), have.end(), c2)) continue;
+                auto it = std::lower_bound(help.begin(), help.end(), c2);
+                if (it != help.end() && *it == c2) continue;
+                if ((int)help.size() >= maxSize) { full = true; break; }
+                help.insert(it, c2);
+              }
+            }
+          layerBeg = layerEnd;
+          for (int h : help)
+            if ((int)st.size() < maxSize) st.push_back(h);
+          layerEnd = (int)st.size();
+        }
+        memb[ic].swap(st);
+      }
+    }
+    for (int ic = 0; ic < nc; ++ic) S->c2csOff[ic + 1] = S->c2csOff[ic] + (int)memb[ic].size();
+    S->c2csMembs.resize(S->c2csOff[nc]);
+    for (int ic = 0; ic < nc; ++ic)
+      for (size_t k = 0; k < memb[ic].size(); ++k) S->c2csMembs[S->c2csOff[ic] + k] = memb[ic][k] + 1;
+    // stencil moments: RFLU_ComputeStencilMoments3D1 (modflu/RFLU_ModWeights.F90:1770-1915)
+    S->xyzMoms.assign(10 * (size_t)nc, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int ic = 0; ic < nc; ++ic) {
+      double mm[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int e = S->c2csOff[ic]; e < S->c2csOff[ic + 1]; ++e) {
+        int j = S->c2csMembs[e] - 1;
+        double dx = cg[3 * (size_t)j] - cg[3 * (size_t)ic];
+        double dy = cg[3 * (size_t)j + 1] - cg[3 * (size_t)ic + 1];
+        double dz = cg[3 * (size_t)j + 2] - cg[3 * (size_t)ic + 2];
+        double wt = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+        dx = wt * dx; dy = wt * dy; dz = wt * dz;
+        mm[0] = mm[0] + dx * dx; mm[1] = mm[1] + dx * dy; mm[2] = mm[2] + dy * dy;
+        mm[3] = mm[3] + dx * dz; mm[4] = mm[4] + dy * dz; mm[5] = mm[5] + dz * dz;
+        mm[6] = mm[6] + wt * dx; mm[7] = mm[7] + wt * dy; mm[8] = mm[8] + wt * dz; mm[9] = mm[9] + wt * wt;
+      }
+      double *r = &S->xyzMoms[10 * (size_t)ic];
+      r[0] = std::sqrt(mm[0]);
+      double i11 = 1.0 / r[0];
+      r[1] = i11 * mm[1];
+      r[2] = std::sqrt(mm[2] - r[1] * r[1]);
+      double i22 = 1.0 / r[2];
+      r[3] = i11 * mm[3];
+      r[4] = i22 * (mm[4] - r[1] * r[3]);
+      r[5] = std::sqrt(mm[5] - (r[3] * r[3] + r[4] * r[4]));
+      double i33 = 1.0 / r[5];
+      r[6] = i11 * mm[6];
+      r[7] = i22 * (mm[7] - r[1] * r[6]);
+      r[8] = i33 * (mm[8] - (r[3] * r[6] + r[4] * r[7]));
+      r[9] = std::sqrt(mm[9] - (r[6] * r[6] + r[7] * r[7] + r[8] * r[8]));
+    }
+  }
+  // 1-based ids in the exported arrays, as the Fortran host holds them
+  for (auto &x : S->f2c) x += 1;
+  for (auto &x : S->bf2c) x += 1;
+  *out = S;
+  return RFLU_OK;
+}
+
+extern "C" int rflu_setup_grid(rflu_setup *S, rflu_grid_desc *g) {
+  if (!S || !g) return rflu::fail(RFLU_ERR_ARG, "rflu_setup_grid: null argument");
+  g->nCells = S->nCells;
+  g->nFaces = S->nFaces;
+  g->f2c = S->f2c.data();
+  g->fn = S->fn.data();
+  g->fc = S->fc.data();
+  g->vol = S->vol.data();
+  g->cofg = S->cofg.data();
+  g->nPatches = S->nPatches;
+  g->patchFaceOff = S->patchFaceOff.data();
+  g->bf2c = S->bf2c.data();
+  g->bfn = S->bfn.data();
+  g->bfc = S->bfc.data();
+  g->c2csOff = S->c2csOff.data();
+  g->c2csMembs = S->c2csMembs.empty() ? nullptr : S->c2csMembs.data();
+  g->xyzMoms = S->xyzMoms.empty() ? nullptr : S->xyzMoms.data();
+  return RFLU_OK;
+}
+
+extern "C" int rflu_setup_destroy(rflu_setup *S) {
+  delete S;
+  return RFLU_OK;
+}

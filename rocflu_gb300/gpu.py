@@ -1,0 +1,318 @@
+"""Host-side mirror of the reference's Fortran interface for this path, over
+the C ABI of librflu_gpu.so (include/rflu_gpu.h).
+
+A Region stands for the Fortran t_region of one grid region: it owns the
+device mirror (rflu_gpu_ctx) and exposes the subroutines the solver driver
+calls, under the reference's names:
+
+  RFLU_TimeStepInviscid + RFLU_MinimumTimeStep -> Region.timestep
+  RungeKuttaMP(regions)                          -> RungeKuttaMP(region, dtMin)
+  RKInitMP/CellGradientsMP/ConvectiveFluxesMP/RKUpdateMP/AfterUpdateMP
+                                                 -> Region.rk_stage(iStage, dtMin)
+  the RFLU_TimeStepping loop                     -> Region.step(nSteps, time, endTime)
+
+Arrays crossing the boundary use the reference layouts as (nCells, k)
+C-order views: cv(5,nCells) column-major is cv[nCells, 5] row-major.
+
+There is no CPU fallback: every call goes to the CUDA library, and loading
+fails with an error when the library or a GPU is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+PREC = {"fp64": 0, "fp64_exact": 1, "mixed": 2}
+EVENT_NAN = 1
+
+_LIB = None
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("nCells", C.c_int), ("nFaces", C.c_int), ("f2c", C.POINTER(C.c_int)),
+                ("fn", C.POINTER(C.c_double)), ("fc", C.POINTER(C.c_double)), ("vol", C.POINTER(C.c_double)),
+                ("cofg", C.POINTER(C.c_double)), ("nPatches", C.c_int), ("patchFaceOff", C.POINTER(C.c_int)),
+                ("bf2c", C.POINTER(C.c_int)), ("bfn", C.POINTER(C.c_double)), ("bfc", C.POINTER(C.c_double)),
+                ("patchBcType", C.POINTER(C.c_int)), ("patchOutflowType", C.POINTER(C.c_int)),
+                ("patchPout", C.POINTER(C.c_double)), ("patchOrder", C.POINTER(C.c_int)),
+                ("c2csOff", C.POINTER(C.c_int)), ("c2csMembs", C.POINTER(C.c_int)),
+                ("xyzMoms", C.POINTER(C.c_double))]
+
+
+class NumDesc(C.Structure):
+    _fields_ = [("spaceOrder", C.c_int), ("spaceDiscr", C.c_int), ("reconst", C.c_int), ("rkScheme", C.c_int),
+                ("piclBuild", C.c_int), ("precision", C.c_int), ("cp", C.c_double), ("gamma", C.c_double),
+                ("cfl", C.c_double), ("epsEntr", C.c_double), ("dissFact", C.c_double),
+                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double)]
+
+
+class Status(C.Structure):
+    _fields_ = [("nanCells", C.c_longlong), ("posFixCells", C.c_longlong), ("negPCells", C.c_longlong),
+                ("firstBadCell", C.c_int), ("stepsDone", C.c_int), ("time", C.c_double), ("dtMin", C.c_double)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("nVert", C.c_int), ("nCells", C.c_int), ("nVertPerCell", C.c_int), ("xyz", C.POINTER(C.c_double)),
+                ("c2v", C.POINTER(C.c_int)), ("nPatches", C.c_int), ("patchFaceOff", C.POINTER(C.c_int)),
+                ("bf2v", C.POINTER(C.c_int))]
+
+
+class RfluError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("rflu error %d: %s" % (code, msg))
+        self.code = code
+
+
+EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_gpu_stream",
+           "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
+           "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_residual", "rflu_gpu_vjp",
+           "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_status", "rflu_setup_build", "rflu_setup_grid",
+           "rflu_setup_destroy")
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=True):
+    """Load librflu_gpu.so (building it first if needed).  Raises if the
+    library cannot be built or loaded; there is no fallback."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError("librflu_gpu.so is missing; run rocflu_gb300.build.build()")
+    L = C.CDLL(_build.LIB)
+    P, D, I = C.c_void_p, C.c_double, C.c_int
+    DP = C.POINTER(C.c_double)
+    L.rflu_gpu_create.argtypes = [C.POINTER(GridDesc), C.POINTER(NumDesc), C.POINTER(P)]
+    L.rflu_gpu_destroy.argtypes = [P]
+    L.rflu_gpu_last_error.restype = C.c_char_p
+    L.rflu_gpu_stream.restype = P
+    L.rflu_gpu_stream.argtypes = [P]
+    L.rflu_gpu_upload_state.argtypes = [P, DP]
+    L.rflu_gpu_download_state.argtypes = [P, DP, DP]
+    L.rflu_gpu_timestep.argtypes = [P, D, DP]
+    L.rflu_gpu_rk_stage.argtypes = [P, I, D]
+    L.rflu_gpu_runge_kutta.argtypes = [P, D]
+    L.rflu_gpu_step.argtypes = [P, I, DP, D, C.POINTER(I)]
+    L.rflu_gpu_run_fixed_dt.argtypes = [P, I, D]
+    L.rflu_gpu_residual.argtypes = [P, DP, DP, DP]
+    L.rflu_gpu_vjp.argtypes = [P, DP, DP, DP]
+    L.rflu_gpu_jvp.argtypes = [P, DP, DP, DP]
+    L.rflu_gpu_patch_pressure.argtypes = [P, DP, I, DP, DP]
+    L.rflu_gpu_status.argtypes = [P, C.POINTER(Status)]
+    L.rflu_setup_build.argtypes = [C.POINTER(MeshDesc), I, C.POINTER(P)]
+    L.rflu_setup_grid.argtypes = [P, C.POINTER(GridDesc)]
+    L.rflu_setup_destroy.argtypes = [P]
+    for name in EXPORTS:
+        if name not in ("rflu_gpu_last_error", "rflu_gpu_stream"):
+            getattr(L, name).restype = C.c_int
+    _LIB = L
+    return L
+
+
+def _check(rc, allow_events=False):
+    if rc < 0 or (rc > 0 and not allow_events):
+        msg = lib().rflu_gpu_last_error().decode() if rc < 0 else "numerical event"
+        raise RfluError(rc, msg)
+    return rc
+
+
+def _p(a, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def num_desc(num, precision):
+    return NumDesc(num.space_order, num.space_discr, num.reconst, num.rk_scheme, num.picl_build,
+                   PREC[precision] if isinstance(precision, str) else int(precision), num.cp, num.gamma, num.cfl,
+                   num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit)
+
+
+class Setup:
+    """Reference setup products built on the host by rflu_setup_build
+    (face list, geometry, C2C stencils, stencil moments)."""
+
+    def __init__(self, case):
+        L = lib()
+        xyz = np.ascontiguousarray(case.xyz, np.float64)
+        c2v = np.ascontiguousarray(case.c2v + 1, np.int32)
+        off = np.zeros(len(case.patches) + 1, np.int32)
+        for i, p in enumerate(case.patches):
+            off[i + 1] = off[i] + len(p.bf2v)
+        bf2v = np.concatenate([p.bf2v for p in case.patches]).astype(np.int32) + 1  # triangles: -1 -> 0
+        bf2v = np.ascontiguousarray(bf2v)
+        self._in = (xyz, c2v, off, bf2v)
+        md = MeshDesc(xyz.shape[0], c2v.shape[0], c2v.shape[1], _p(xyz), _p(c2v, C.c_int), len(case.patches),
+                      _p(off, C.c_int), _p(bf2v, C.c_int))
+        h = C.c_void_p()
+        _check(L.rflu_setup_build(C.byref(md), case.num.space_order, C.byref(h)))
+        self.h = h
+        g = GridDesc()
+        _check(L.rflu_setup_grid(self.h, C.byref(g)))
+        nc, nf = g.nCells, g.nFaces
+        nb = int(off[-1])
+        self.n_cells, self.n_faces = nc, nf
+        self.f2c = np.ctypeslib.as_array(g.f2c, (nf, 2)).copy()
+        self.fn = np.ctypeslib.as_array(g.fn, (nf, 4)).copy()
+        self.fc = np.ctypeslib.as_array(g.fc, (nf, 3)).copy()
+        self.vol = np.ctypeslib.as_array(g.vol, (nc,)).copy()
+        self.cofg = np.ctypeslib.as_array(g.cofg, (nc, 3)).copy()
+        self.patch_off = off
+        self.bf2c = np.ctypeslib.as_array(g.bf2c, (max(nb, 1),))[:nb].copy()
+        self.bfn = np.ctypeslib.as_array(g.bfn, (max(nb, 1), 4))[:nb].copy()
+        self.bfc = np.ctypeslib.as_array(g.bfc, (max(nb, 1), 3))[:nb].copy()
+        self.c2cs_off = np.ctypeslib.as_array(g.c2csOff, (nc + 1,)).copy()
+        nnz = int(self.c2cs_off[-1])
+        if nnz:
+            self.c2cs = np.ctypeslib.as_array(g.c2csMembs, (nnz,)).copy()
+            self.moms = np.ctypeslib.as_array(g.xyzMoms, (nc, 10)).copy()
+        else:
+            self.c2cs = np.zeros(0, np.int32)
+            self.moms = np.zeros((nc, 10))
+        L.rflu_setup_destroy(self.h)
+        self.h = None
+
+
+class Region:
+    """Device mirror of one region (t_region) in the given precision:
+    'fp64', 'fp64_exact' or 'mixed'."""
+
+    def __init__(self, case, precision="fp64", grid=None):
+        """grid: the reference's setup products (an object with f2c (1-based),
+        fn, fc, vol, cofg, bf2c (1-based), bfn, bfc, patch_off, c2cs_off,
+        c2cs (1-based), moms); built by rflu_setup_build when omitted."""
+        L = lib()
+        self.case = case
+        self.precision = precision
+        if grid is None:
+            grid = Setup(case)
+        self.grid = grid
+        nc = int(grid.vol.shape[0])
+        self.n_cells = nc
+        pt = np.array([p.bc_type for p in case.patches], np.int32)
+        po = np.array([p.outflow_type for p in case.patches], np.int32)
+        pp = np.array([p.p_out for p in case.patches], np.float64)
+        pr = np.array([p.order for p in case.patches], np.int32)
+        arrs = dict(
+            f2c=np.ascontiguousarray(grid.f2c, np.int32), fn=np.ascontiguousarray(grid.fn, np.float64),
+            fc=np.ascontiguousarray(grid.fc, np.float64), vol=np.ascontiguousarray(grid.vol, np.float64),
+            cofg=np.ascontiguousarray(grid.cofg, np.float64), off=np.ascontiguousarray(grid.patch_off, np.int32),
+            bf2c=np.ascontiguousarray(grid.bf2c, np.int32), bfn=np.ascontiguousarray(grid.bfn, np.float64),
+            bfc=np.ascontiguousarray(grid.bfc, np.float64), pt=pt, po=po, pp=pp, pr=pr,
+            soff=np.ascontiguousarray(grid.c2cs_off, np.int32),
+            smem=np.ascontiguousarray(grid.c2cs if len(grid.c2cs) else np.zeros(1), np.int32),
+            moms=np.ascontiguousarray(grid.moms, np.float64))
+        a = arrs
+        gd = GridDesc(nc, int(a["f2c"].shape[0]), _p(a["f2c"], C.c_int), _p(a["fn"]), _p(a["fc"]), _p(a["vol"]),
+                      _p(a["cofg"]), len(case.patches), _p(a["off"], C.c_int), _p(a["bf2c"], C.c_int), _p(a["bfn"]),
+                      _p(a["bfc"]), _p(a["pt"], C.c_int), _p(a["po"], C.c_int), _p(a["pp"]), _p(a["pr"], C.c_int),
+                      _p(a["soff"], C.c_int), _p(a["smem"], C.c_int), _p(a["moms"]))
+        self.nd = num_desc(case.num, precision)
+        h = C.c_void_p()
+        _check(L.rflu_gpu_create(C.byref(gd), C.byref(self.nd), C.byref(h)))
+        self.h = h
+        self.n_stages = {1: 4, 2: 3, 3: 1}[case.num.rk_scheme]
+        if case.cv0 is not None:
+            self.upload(case.cv0)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().rflu_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        """The CUDA stream handle (cudaStream_t) the region launches on."""
+        return lib().rflu_gpu_stream(self.h)
+
+    def upload(self, cv):
+        cv = np.ascontiguousarray(cv, np.float64)
+        assert cv.shape == (self.n_cells, 5)
+        _check(lib().rflu_gpu_upload_state(self.h, _p(cv)))
+
+    def download(self, cv_out=None, dv_out=None):
+        cv = np.empty((self.n_cells, 5)) if cv_out is None else cv_out
+        dv = np.empty((self.n_cells, 3)) if dv_out is None else dv_out
+        _check(lib().rflu_gpu_download_state(self.h, _p(cv), _p(dv)))
+        return cv, dv
+
+    def timestep(self, current_time):
+        dt = C.c_double()
+        _check(lib().rflu_gpu_timestep(self.h, current_time, C.byref(dt)))
+        return dt.value
+
+    def rk_stage(self, istage, dt):
+        return _check(lib().rflu_gpu_rk_stage(self.h, istage, dt), allow_events=True)
+
+    def runge_kutta(self, dt):
+        return _check(lib().rflu_gpu_runge_kutta(self.h, dt), allow_events=True)
+
+    def step(self, n_steps, time=0.0, end_time=0.0):
+        t = C.c_double(time)
+        done = C.c_int()
+        rc = _check(lib().rflu_gpu_step(self.h, n_steps, C.byref(t), end_time, C.byref(done)), allow_events=True)
+        return done.value, t.value, rc
+
+    def run_fixed_dt(self, n_steps, dt):
+        return _check(lib().rflu_gpu_run_fixed_dt(self.h, n_steps, dt), allow_events=True)
+
+    def residual(self, cv, with_grad=True):
+        cv = np.ascontiguousarray(cv, np.float64)
+        rhs = np.empty((self.n_cells, 5))
+        grad = np.empty((self.n_cells, 5, 3)) if with_grad else None
+        _check(lib().rflu_gpu_residual(self.h, _p(cv), _p(rhs), _p(grad) if with_grad else None))
+        return rhs, grad
+
+    def vjp(self, cv, rhs_bar):
+        cv = np.ascontiguousarray(cv, np.float64)
+        rb = np.ascontiguousarray(rhs_bar, np.float64)
+        out = np.empty((self.n_cells, 5))
+        _check(lib().rflu_gpu_vjp(self.h, _p(cv), _p(rb), _p(out)))
+        return out
+
+    def jvp(self, cv, cv_dot):
+        cv = np.ascontiguousarray(cv, np.float64)
+        cd = np.ascontiguousarray(cv_dot, np.float64)
+        out = np.empty((self.n_cells, 5))
+        _check(lib().rflu_gpu_jvp(self.h, _p(cv), _p(cd), _p(out)))
+        return out
+
+    def patch_pressure(self, cv, ipatch, with_grad=True):
+        cv = np.ascontiguousarray(cv, np.float64)
+        J = C.c_double()
+        g = np.empty((self.n_cells, 5)) if with_grad else None
+        _check(lib().rflu_gpu_patch_pressure(self.h, _p(cv), ipatch, C.byref(J), _p(g) if with_grad else None))
+        return J.value, g
+
+    def status(self):
+        s = Status()
+        _check(lib().rflu_gpu_status(self.h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in Status._fields_}
+
+
+# --- the reference's subroutine names ---------------------------------------
+def RungeKuttaMP(region, dt_min):
+    """libfloflu/RungeKuttaMP.F90:75 -- all RK stages of one time step."""
+    return region.runge_kutta(dt_min)
+
+
+def RFLU_TimeStep(region, current_time):
+    """rocflu/RFLU_TimeStepInviscid.F90:75 + rocflu/RFLU_MinimumTimeStep.F90:75."""
+    return region.timestep(current_time)
+
+
+def CellGradientsMP_ConvectiveFluxesMP(region, cv):
+    """libfloflu/CellGradientsMP.F90:75 then libfloflu/ConvectiveFluxesMP.F90:73:
+    the residual rhs(5,nCells) and the limited gradCell(3,5,nCells)."""
+    return region.residual(cv)
