@@ -1,0 +1,353 @@
+"""Benchmark of the explicit residual-and-update path on one GB300.
+
+Workload (headline): Mach-2 shock hitting a density-3 sphere on a 128^3
+hexahedral mesh handled as unstructured faces/cells (2,097,152 cells,
+6.24M interior faces), HLLC flux, second-order LSQ reconstruction with the
+Barth-Jespersen limiter (frame-invariant velocity limiting), Wray 3-stage RK,
+CFL 0.4.  A "step" is one time step: the CFL time-step reduction plus three
+RK stages on the device.
+
+  value  Mcell*RK-stage/s of the mixed FP32/FP64 path, state resident in HBM
+  fp64   the same metric for the all-FP64 path, and the mixed-vs-FP64
+         L1/Linf density and pressure differences after the same steps
+  e2e    Mcell*RK-stage/s through the C ABI with host buffers: every step
+         uploads cv from pinned host memory, steps, and downloads cv and dv
+  roofline  dominant kernel of the mixed path against the measured HBM copy
+         bandwidth
+  cpu_baseline  the CPU oracle (FP64 restatement of the reference, one
+         thread) on a bounded sample: the same set-up on a 40^3 mesh
+
+The working set (state, gradients, face fluxes, geometry: > 0.5 GB) is far
+larger than the 126 MB L2, so no L2 flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference path on all host
+cores (one oracle replica per core, each on its own 40^3 sample); the Fortran
+reference cannot be built here.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mcell*RK-stage/s (mixed FP32/FP64 path; FP64 path and L1 rho error reported beside it)"
+UNIT = "Mcell*RK-stage/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=128, help="cells per side of the hex box")
+    p.add_argument("--cpu-n", type=int, default=64, help="cells per side of the CPU sample")
+    p.add_argument("--cpu-steps", type=int, default=6)
+    p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--skip-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return self
+
+        def run():
+            for line in self.proc.stdout:
+                self.samples.append([x.strip() for x in line.split(",")])
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+        return self
+
+    def stop(self):
+        if getattr(self, "proc", None):
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm = [float(s[1]) for s in self.samples if len(s) >= 9 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) >= 9 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            if len(s) >= 9:
+                for k, nm in enumerate(names):
+                    if s[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def algorithmic_bytes(region, precision):
+    """Bytes per launch of the three stage kernels and of the whole stage,
+    counted from the data each kernel must move once (neighbour gathers
+    counted once, ideal reuse), with the per-cell terms of the two-kernel
+    minimum: state, gradients, R-factor weights, stencil ids, face
+    geometry/connectivity."""
+    g = region.grid
+    nc = region.n_cells
+    nf = g.f2c.shape[0]
+    nb = g.bf2c.shape[0]
+    S = len(g.c2cs)
+    r = 4 if precision == "mixed" else 8
+    grad_limit = nc * (5 * r + 15 * r + 4) + S * (4 + 3 * r) + nf * 2 * (8 + 3 * r)
+    face_flux = nc * (5 * r + 15 * r) + (nf + nb) * (4 * r + 3 * r + 5 * r) + nf * 8
+    gather_update = nc * (40 + 40 + 24 + 5 * 2 * r + 5 * r + 8 + 8) + 2 * nf * 5 * r + (2 * nf + nb) * 4
+    return {"gradLimit": grad_limit, "faceFlux": face_flux, "gatherUpdate": gather_update}
+
+
+def run_ours(args):
+    import torch
+
+    from rocflu_gb300 import cases, gpu
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    case = cases.shock_sphere(args.n)
+    t0 = time.time()
+    setup = gpu.Setup(case)
+    setup_s = time.time() - t0
+    # imposed first step = the CFL step of the initial state
+    probe = gpu.Region(case, "fp64", grid=setup)
+    case.num.dt_imposed = probe.timestep(1.0)
+    probe.close()
+    del probe
+
+    results = {}
+    regions = {}
+    for prec in ("mixed", "fp64"):
+        reg = gpu.Region(case, prec, grid=setup)
+        regions[prec] = reg
+        stream = torch.cuda.ExternalStream(reg.stream)
+        t = 0.0
+        n, t, rc = reg.step(args.warmup, t)
+        barrier()
+        clk = ClockSampler(local).start() if prec == "mixed" else None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        n, t, rc = reg.step(args.steps, t)
+        e1.record(stream)
+        e1.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        clocks = clk.stop() if clk else None
+        if ws > 1:
+            import torch.distributed as dist
+
+            tt = torch.tensor([ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        units = region_units = reg.n_cells * reg.n_stages * args.steps
+        results[prec] = {"ms": ms, "value": ws * units / (ms * 1e-3) / 1e6, "clocks": clocks, "rc": rc,
+                         "time": t, "steps": n}
+        ktimes = reg.kernel_times(5)
+        results[prec]["kernel_ms"] = {"gradLimit": ktimes[0], "faceFlux": ktimes[1], "gatherUpdate": ktimes[2],
+                                      "timestep": ktimes[3]}
+        del region_units
+
+    # mixed vs FP64 after the same number of steps from the same state
+    cv_m, dv_m = regions["mixed"].download()
+    cv_d, dv_d = regions["fp64"].download()
+    err = {"L1_rho": float(np.abs(cv_m[:, 0] - cv_d[:, 0]).mean()),
+           "Linf_rho": float(np.abs(cv_m[:, 0] - cv_d[:, 0]).max()),
+           "L1_p": float(np.abs(dv_m[:, 0] - dv_d[:, 0]).mean()),
+           "Linf_p": float(np.abs(dv_m[:, 0] - dv_d[:, 0]).max()),
+           "steps": args.warmup + args.steps}
+
+    # end-to-end through the C ABI with host buffers
+    e2e = None
+    if not args.skip_e2e:
+        reg = regions["mixed"]
+        host_cv = torch.empty((reg.n_cells, 5), dtype=torch.float64).pin_memory()
+        host_dv = torch.empty((reg.n_cells, 3), dtype=torch.float64).pin_memory()
+        cv_np, dv_np = host_cv.numpy(), host_dv.numpy()
+        cv_np[:] = cv_m
+        t = 1.0
+        for _ in range(args.warmup):
+            reg.upload(cv_np)
+            _, t, _ = reg.step(1, t)
+            reg.download(cv_np, dv_np)
+        barrier()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            reg.upload(cv_np)
+            _, t, _ = reg.step(1, t)
+            reg.download(cv_np, dv_np)
+        barrier()
+        wall = time.perf_counter() - w0
+        units = reg.n_cells * reg.n_stages * args.steps
+        e2e = {"value": ws * units / wall / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(host_cv.numel() * 8),
+               "d2h_bytes_per_step": int((host_cv.numel() + host_dv.numel()) * 8)}
+
+    # roofline of the dominant kernel of the mixed path
+    peaks, peak_kind = measured_peaks()
+    ab = algorithmic_bytes(regions["mixed"], "mixed")
+    km = results["mixed"]["kernel_ms"]
+    dom = max(("gradLimit", "faceFlux", "gatherUpdate"), key=lambda k: km[k])
+    achieved = ab[dom] / (km[dom] * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(dom)
+        except Exception:
+            traffic = None
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": ab[dom], "launch_ms": km[dom]}
+
+    fp64 = {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms"] / args.steps,
+            "kernel_ms": results["fp64"]["kernel_ms"], "mixed_over_fp64": results["mixed"]["value"] / results["fp64"]["value"],
+            "mixed_vs_fp64_error": err}
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu = cpu_sample(args.cpu_n, args.cpu_steps)
+
+    if rank == 0:
+        ms = results["mixed"]["ms"]
+        line = {
+            "metric": METRIC, "value": results["mixed"]["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "shock_sphere_hex%d_hllc_bj_wray3" % args.n, "cells": regions["mixed"].n_cells,
+                       "faces": int(setup.f2c.shape[0]), "stages_per_step": 3, "flux": "HLLC", "limiter": "BJ (RECONST 10)",
+                       "parallelism": "replicas" if ws > 1 else "single", "l2": "working set > L2 (no flush)",
+                       "setup_s": setup_s},
+            "gpu_launches": 13 * args.steps,
+            "fp64": fp64,
+            "e2e": e2e,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": results["mixed"]["clocks"],
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def _cpu_worker(n, steps, q=None):
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle
+    from rocflu_gb300 import cases
+
+    case = cases.shock_sphere(n)
+    o = Oracle(case)
+    dt = o.timestep(1.0)
+    t0 = time.perf_counter()
+    o.run_fixed_dt(steps, dt)
+    el = time.perf_counter() - t0
+    res = (case.n_cells * 3 * steps, el)
+    if q is not None:
+        q.put(res)
+    return res
+
+
+def cpu_sample(n, steps):
+    units, el = _cpu_worker(n, steps)
+    return {"value": units / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "shock_sphere %d^3 hex (%d cells), HLLC+BJ, %d Wray steps, one thread, %.1f s" %
+                      (n, n ** 3, steps, el)}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    cores = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    samples = []
+    for step in range(args.steps):
+        q = ctx.Queue()
+        procs = [ctx.Process(target=_cpu_worker, args=(args.cpu_n, args.cpu_steps, q)) for _ in range(cores)]
+        w0 = time.perf_counter()
+        for p in procs:
+            p.start()
+        res = [q.get() for _ in procs]
+        for p in procs:
+            p.join()
+        units = sum(r[0] for r in res)
+        wall = max(r[1] for r in res)
+        samples.append(units / wall / 1e6)
+        vals.append(time.perf_counter() - w0)
+    value = float(np.median(samples))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "shock_sphere_hex%d_hllc_bj_wray3" % args.n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d replicas of the FP64 CPU restatement, each on a %d^3 hex sample, %d Wray steps"
+                                       % (cores, args.cpu_n, args.cpu_steps)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

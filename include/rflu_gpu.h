@@ -149,6 +149,12 @@ int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, dou
 
 int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status);
 
+/* Diagnostics (no reference counterpart): runs nIter RK stages launch by
+ * launch (no graph) with CUDA events between the kernels on the context's
+ * stream and returns the mean duration in ms of [0] gradient+limiter,
+ * [1] face fluxes, [2] gather+update, [3] time-step reduction. */
+int rflu_gpu_kernel_times(rflu_gpu_ctx *ctx, int nIter, double *ms);
+
 /* ------------------------------------------------------------------------ */
 /* Host set-up: builds the reference's setup products from a raw mesh, for   */
 /* hosts that do not run RFLU_InitFlowSolver.  Reproduces RFLU_BuildFaceList */

@@ -97,6 +97,7 @@ struct CtxBase {
   virtual int jvp(const double *cv, const double *cvDot, double *rhsDot) = 0;
   virtual int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) = 0;
   virtual int status(rflu_status *s) = 0;
+  virtual int kernelTimes(int nIter, double *ms) = 0;
   cudaStream_t stream = nullptr;
 };
 
@@ -351,6 +352,34 @@ struct Ctx : CtxBase {
     st->time = s.time;
     st->dtMin = s.dtMin;
     return RFLU_OK;
+  }
+  int kernelTimes(int nIter, double *ms) override {
+    if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_kernel_times: bad arguments");
+    cudaEvent_t ev[5];
+    for (auto &e : ev) RFLU_CUDA(cudaEventCreate(&e));
+    double acc[4] = {0, 0, 0, 0};
+    kSetScalars<<<1, 1, 0, stream>>>(V.sc, 1.0, 0.0, 0);
+    kSetDt<<<1, 1, 0, stream>>>(V.sc, 0.0);  // dt = 0: the state stays put
+    for (int it = 0; it < nIter; ++it) {
+      cudaEventRecord(ev[0], stream);
+      ops->gradLimit(V, stream);
+      cudaEventRecord(ev[1], stream);
+      ops->faceFlux(V, stream);
+      cudaEventRecord(ev[2], stream);
+      ops->gatherUpdate(V, 1 + it % V.p.nrkSteps, &V.sc->dtMin, stream);
+      cudaEventRecord(ev[3], stream);
+      ops->timestep(V, stream);
+      cudaEventRecord(ev[4], stream);
+      RFLU_CUDA(cudaEventSynchronize(ev[4]));
+      for (int k = 0; k < 4; ++k) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+        acc[k] += t;
+      }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 4; ++k) ms[k] = acc[k] / nIter;
+    return checkLaunch("kernel_times");
   }
   int nPatches = 0;
 };
@@ -668,6 +697,11 @@ int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status) {
   CTX_CHECK("rflu_gpu_status");
   if (!status) return fail(RFLU_ERR_ARG, "rflu_gpu_status: null status");
   return ctx->impl->status(status);
+}
+
+int rflu_gpu_kernel_times(rflu_gpu_ctx *ctx, int nIter, double *ms) {
+  CTX_CHECK("rflu_gpu_kernel_times");
+  return ctx->impl->kernelTimes(nIter, ms);
 }
 
 }  // extern "C"

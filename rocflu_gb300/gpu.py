@@ -68,7 +68,7 @@ class RfluError(RuntimeError):
 EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_gpu_stream",
            "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
            "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_residual", "rflu_gpu_vjp",
-           "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_status", "rflu_setup_build", "rflu_setup_grid",
+           "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_setup_build", "rflu_setup_grid",
            "rflu_setup_destroy")
 
 
@@ -106,6 +106,7 @@ def lib(build_if_missing=True):
     L.rflu_gpu_jvp.argtypes = [P, DP, DP, DP]
     L.rflu_gpu_patch_pressure.argtypes = [P, DP, I, DP, DP]
     L.rflu_gpu_status.argtypes = [P, C.POINTER(Status)]
+    L.rflu_gpu_kernel_times.argtypes = [P, I, DP]
     L.rflu_setup_build.argtypes = [C.POINTER(MeshDesc), I, C.POINTER(P)]
     L.rflu_setup_grid.argtypes = [P, C.POINTER(GridDesc)]
     L.rflu_setup_destroy.argtypes = [P]
@@ -294,6 +295,12 @@ class Region:
         g = np.empty((self.n_cells, 5)) if with_grad else None
         _check(lib().rflu_gpu_patch_pressure(self.h, _p(cv), ipatch, C.byref(J), _p(g) if with_grad else None))
         return J.value, g
+
+    def kernel_times(self, n_iter=10):
+        """Mean ms per launch: grad+limiter, face flux, gather+update, dt."""
+        ms = np.zeros(4)
+        _check(lib().rflu_gpu_kernel_times(self.h, n_iter, _p(ms)))
+        return ms
 
     def status(self):
         s = Status()

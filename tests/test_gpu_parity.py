@@ -1,0 +1,259 @@
+"""GPU path (through the C ABI) against the CPU oracle on the same inputs.
+
+fp64_exact: bit-exact (integer-for-integer, bit-for-bit) with the oracle.
+fp64:       FMA contraction allowed; single residual within 1e-12 relative
+            to the field maximum (the reference's regression tolerance is
+            1e-10, tests/rocpicl_tests/checks.py:18).
+mixed:      FP32 state/flux math; density L1 error vs the FP64 run <= 1e-5.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from rocflu_gb300 import cases, gpu
+
+pytestmark = pytest.mark.gpu
+
+FLUXES = [(cases.DISCR_ROE, "roe"), (cases.DISCR_HLLC, "hllc"), (cases.DISCR_AUSM, "ausm")]
+LIMITERS = [cases.RECONST_NONE, cases.RECONST_BJ, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP]
+
+
+def _perturbed(case, seed=3, amp=0.05):
+    rng = np.random.default_rng(seed)
+    cv = case.cv0.copy()
+    cv *= 1.0 + amp * rng.standard_normal(cv.shape)
+    cv[:, 1:4] += amp * rng.standard_normal((cv.shape[0], 3))
+    return cv
+
+
+def _rel(a, b):
+    scale = np.maximum(np.abs(b).max(axis=0), 1e-300)
+    return (np.abs(a - b) / scale).max()
+
+
+def _hex_case(discr, reconst, order=2, patch_order=2, picl=1, n=6):
+    num = cases.Numerics(space_order=order, space_discr=discr, reconst=reconst if order == 2 else 0, picl_build=picl,
+                         cfl=0.4)
+    c = cases.shock_sphere(n, num=num)
+    for p in c.patches:
+        p.order = min(patch_order, order)
+    c.num.dt_imposed = 1e-4
+    return c
+
+
+@pytest.mark.parametrize("discr,name", FLUXES)
+@pytest.mark.parametrize("reconst", LIMITERS)
+def test_residual_bit_exact_hex(gpu_lib, discr, name, reconst):
+    c = _hex_case(discr, reconst)
+    cv = _perturbed(c)
+    o = Oracle(c)
+    o.set_state(cv)
+    rhs_o, grad_o = o.residual()
+    r = gpu.Region(c, "fp64_exact")
+    rhs_g, grad_g = r.residual(cv)
+    np.testing.assert_array_equal(grad_g, grad_o)
+    np.testing.assert_array_equal(rhs_g, rhs_o)
+
+
+@pytest.mark.parametrize("discr,name", FLUXES)
+@pytest.mark.parametrize("reconst", [cases.RECONST_BJ, cases.RECONST_VENKAT])
+def test_residual_bit_exact_tets(gpu_lib, discr, name, reconst):
+    num = cases.Numerics(space_order=2, space_discr=discr, reconst=reconst)
+    c = cases.adjoint_tets(5, num=num)
+    cv = c.cv0
+    o = Oracle(c)
+    o.set_state(cv)
+    rhs_o, grad_o = o.residual()
+    r = gpu.Region(c, "fp64_exact")
+    rhs_g, grad_g = r.residual(cv)
+    np.testing.assert_array_equal(grad_g, grad_o)
+    np.testing.assert_array_equal(rhs_g, rhs_o)
+
+
+@pytest.mark.parametrize("picl", [0, 1])
+@pytest.mark.parametrize("patch_order", [1, 2])
+def test_patch_orders_and_energy_slot(gpu_lib, picl, patch_order):
+    """First-order outflow patches in a second-order run read cv as
+    CellGradientsMP left it (energy slot = p in the PICL build)."""
+    c = _hex_case(cases.DISCR_HLLC, cases.RECONST_BJ, patch_order=patch_order, picl=picl)
+    cv = _perturbed(c)
+    o = Oracle(c)
+    o.set_state(cv)
+    rhs_o, _ = o.residual()
+    r = gpu.Region(c, "fp64_exact")
+    rhs_g, _ = r.residual(cv)
+    np.testing.assert_array_equal(rhs_g, rhs_o)
+
+
+@pytest.mark.parametrize("discr,name", FLUXES)
+def test_residual_first_order(gpu_lib, discr, name):
+    c = _hex_case(discr, 0, order=1, patch_order=1)
+    cv = _perturbed(c)
+    o = Oracle(c)
+    o.set_state(cv)
+    rhs_o, _ = o.residual()
+    rhs_g, _ = gpu.Region(c, "fp64_exact").residual(cv)
+    np.testing.assert_array_equal(rhs_g, rhs_o)
+    rhs_f, _ = gpu.Region(c, "fp64").residual(cv)
+    assert _rel(rhs_f, rhs_o) < 1e-12
+
+
+@pytest.mark.parametrize("discr,name", FLUXES)
+def test_residual_fp64_fma_within_tolerance(gpu_lib, discr, name):
+    c = _hex_case(discr, cases.RECONST_BJ)
+    cv = _perturbed(c)
+    o = Oracle(c)
+    o.set_state(cv)
+    rhs_o, grad_o = o.residual()
+    rhs_g, grad_g = gpu.Region(c, "fp64").residual(cv)
+    assert _rel(rhs_g, rhs_o) < 1e-10
+    assert _rel(grad_g.reshape(-1, 15), grad_o.reshape(-1, 15)) < 1e-10
+
+
+def test_drop_in_with_reference_setup_products(gpu_lib):
+    """rflu_gpu_create fed with the oracle's own setup arrays (as the Fortran
+    host would pass them) gives the same residual as with rflu_setup_build."""
+    c = _hex_case(cases.DISCR_ROE, cases.RECONST_VENKAT)
+    o = Oracle(c)
+    f2c, f2v, fn, fc = o.faces()
+    vol, cofg = o.cells()
+    off, idx, moms = o.stencil()
+    pb = [o.patch(i) for i in range(len(c.patches))]
+    po = np.zeros(len(c.patches) + 1, np.int32)
+    for i, p in enumerate(pb):
+        po[i + 1] = po[i] + len(p[0])
+
+    class G:
+        pass
+
+    g = G()
+    g.f2c, g.fn, g.fc, g.vol, g.cofg = f2c + 1, fn, fc, vol, cofg
+    g.bf2c = np.concatenate([p[0] for p in pb]) + 1
+    g.bfn = np.concatenate([p[1] for p in pb])
+    g.bfc = np.concatenate([p[2] for p in pb])
+    g.patch_off, g.c2cs_off, g.c2cs, g.moms = po, off, idx + 1, moms
+    cv = _perturbed(c)
+    a, _ = gpu.Region(c, "fp64_exact", grid=g).residual(cv)
+    b, _ = gpu.Region(c, "fp64_exact").residual(cv)
+    o.set_state(cv)
+    ref, _ = o.residual()
+    np.testing.assert_array_equal(a, ref)
+    np.testing.assert_array_equal(b, ref)
+
+
+def test_timestep_bit_exact(gpu_lib):
+    c = _hex_case(cases.DISCR_HLLC, cases.RECONST_BJ)
+    cv = _perturbed(c)
+    o = Oracle(c)
+    o.set_state(cv)
+    r = gpu.Region(c, "fp64_exact")
+    r.upload(cv)
+    for t in (0.0, 1.0):  # imposed first step, then the CFL step
+        assert r.timestep(t) == o.timestep(t)
+
+
+def test_sod_full_run_bit_exact(gpu_lib):
+    """Sod tube to t = 0.2 (first-order Roe, Wray RK3, CFL 0.5): every time
+    step and stage on the device; final state identical to the oracle."""
+    c = cases.sod(100, 2, 2)
+    c.num.dt_imposed = c.num.cfl * 0.01 / (6.0 * np.sqrt(1.4))
+    o = Oracle(c)
+    n_o, t_o = o.run(100000, 0.0, 0.2)
+    r = gpu.Region(c, "fp64_exact")
+    n_g, t_g, rc = r.step(100000, 0.0, 0.2)
+    assert rc == 0
+    assert n_g == n_o and t_g == t_o == 0.2
+    cv_o, dv_o = o.state()
+    cv_g, dv_g = r.download()
+    np.testing.assert_array_equal(cv_g, cv_o)
+    np.testing.assert_array_equal(dv_g, dv_o)
+
+
+@pytest.mark.parametrize("discr,name", FLUXES)
+def test_second_order_steps_bit_exact(gpu_lib, discr, name):
+    c = _hex_case(discr, cases.RECONST_BJ)
+    o = Oracle(c)
+    n_o, t_o = o.run(5, 0.0)
+    r = gpu.Region(c, "fp64_exact")
+    n_g, t_g, rc = r.step(5, 0.0)
+    assert n_g == n_o == 5 and t_g == t_o
+    cv_o, _ = o.state()
+    cv_g, _ = r.download()
+    np.testing.assert_array_equal(cv_g, cv_o)
+
+
+def test_rk_stage_entry_matches_step(gpu_lib):
+    c = _hex_case(cases.DISCR_AUSM, cases.RECONST_VENKAT)
+    o = Oracle(c)
+    r = gpu.Region(c, "fp64_exact")
+    dt = 2.0e-4
+    for s in (1, 2, 3):
+        o.rk_stage(s, dt)
+        r.rk_stage(s, dt)
+    np.testing.assert_array_equal(r.download()[0], o.state()[0])
+
+
+def test_mixed_precision_density_error(gpu_lib):
+    """Mixed FP32/FP64 vs the FP64 device run on the shock-sphere set-up."""
+    c = cases.shock_sphere(24)
+    r64 = gpu.Region(c, "fp64")
+    dt = r64.timestep(1.0)
+    r64.run_fixed_dt(20, dt)
+    rmx = gpu.Region(c, "mixed")
+    rmx.run_fixed_dt(20, dt)
+    a, dva = r64.download()
+    b, dvb = rmx.download()
+    l1 = np.abs(a[:, 0] - b[:, 0]).mean()
+    assert l1 <= 1e-5, l1
+    assert np.abs(dva[:, 0] - dvb[:, 0]).mean() / np.abs(dva[:, 0]).mean() < 1e-4
+
+
+def test_conservation_closed_box(gpu_lib):
+    """Mass and gas energy in a slip-wall box stay constant to 1e-10
+    (tests/rocpicl_tests/checks.py:365)."""
+    c = cases.blast_hex(8)
+    vol = gpu.Setup(c).vol
+    for prec in ("fp64", "mixed"):
+        r = gpu.Region(c, prec)
+        m0 = (c.cv0[:, 0] * vol).sum()
+        e0 = (c.cv0[:, 4] * vol).sum()
+        dt = r.timestep(1.0)
+        r.run_fixed_dt(10, dt)
+        cv, _ = r.download()
+        assert abs((cv[:, 0] * vol).sum() - m0) / m0 < 1e-10
+        assert abs((cv[:, 4] * vol).sum() - e0) / e0 < 1e-10
+
+
+def test_positivity_fix_counted(gpu_lib):
+    """Two gas halves flying apart at low pressure: the update drives the
+    pressure negative, RFLU_CheckPositivity floors the energy, and the device
+    counter and state follow the oracle."""
+    c = cases.sod(20, 1, 1)
+    c.num.rk_scheme = cases.RK_EULER
+    x = np.arange(20) + 0.5
+    u = np.where(x < 10, -3.0, 3.0)
+    one = np.ones(20)
+    c.cv0 = cases.conserved(one, u, 0 * one, 0 * one, 0.01 * one, 1.4)
+    r = gpu.Region(c, "fp64_exact")
+    o = Oracle(c)
+    for _ in range(2):
+        r.rk_stage(1, 0.002)
+        o.rk_stage(1, 0.002)
+    pf, neg, nan = o.counters()
+    assert pf > 0
+    assert r.status()["posFixCells"] == pf
+    np.testing.assert_array_equal(r.download()[0], o.state()[0])
+
+
+def test_nan_cells_reported_as_event(gpu_lib):
+    """A NaN cell is reported by the validity check (rc = RFLU_EVENT_NAN and
+    the first bad cell in reference numbering), never trapped on the device."""
+    c = _hex_case(cases.DISCR_HLLC, cases.RECONST_BJ)
+    cv = c.cv0.copy()
+    cv[17, :] = np.nan
+    r = gpu.Region(c, "fp64")
+    r.upload(cv)
+    rc = r.rk_stage(1, 1e-4)
+    assert rc == gpu.EVENT_NAN
+    st = r.status()
+    assert st["nanCells"] > 0 and st["firstBadCell"] >= 1
