@@ -155,6 +155,26 @@ int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status);
  * [1] face fluxes, [2] gather+update, [3] time-step reduction. */
 int rflu_gpu_kernel_times(rflu_gpu_ctx *ctx, int nIter, double *ms);
 
+/* Residual without any allocation (no counterpart in the reference).
+ * Same result as rflu_gpu_residual (rhs only), for callers that cannot
+ * allocate device memory at call time: hosts that reserve all device memory
+ * up front under a fixed budget, and hosts that cannot let cudaMalloc or
+ * cudaFree synchronize the device while their other streams run.
+ *   cvDev  device (or managed) pointer to cv(5,nCells), reference order
+ *   rhsDev device (or managed) pointer to rhs(5,nCells), written
+ * The intermediates live in one file-scope static device array of 64 MiB,
+ * which every GPU that loads the library keeps until the process exits;
+ * meshes whose intermediates do not fit (about 200k hexahedra in FP64) are
+ * rejected with RFLU_ERR_ARG and a message giving the bytes needed.  The
+ * first call on a device looks up the array's device address (with that
+ * device current); make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (other host threads,
+ * other contexts on the same device) race and must be serialised by the
+ * caller.  The call runs on the context's stream and returns after it
+ * finishes; it calls no cudaMalloc, cudaFree or allocating routine and
+ * leaves the context's own state untouched. */
+int rflu_gpu_residual_static(rflu_gpu_ctx *ctx, const double *cvDev, double *rhsDev);
+
 /* ------------------------------------------------------------------------ */
 /* Host set-up: builds the reference's setup products from a raw mesh, for   */
 /* hosts that do not run RFLU_InitFlowSolver.  Reproduces RFLU_BuildFaceList */

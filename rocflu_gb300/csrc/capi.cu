@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <string>
@@ -69,6 +70,40 @@ __global__ void kPermuteOut(const T *src, double *dst, const int *refId, int nc,
 
 inline int nblk(long long n) { return (int)((n + 255) / 256); }
 
+// Scratch of rflu_gpu_residual_static: a fixed device array in this file, so
+// that the call allocates nothing.  Every GPU that loads the library keeps
+// these 64 MiB until the process exits.  All calls share it (see the header).
+constexpr size_t kStaticScratchBytes = size_t(64) << 20;
+__device__ __align__(256) unsigned char gStaticScratch[kStaticScratchBytes];
+
+// Device address of gStaticScratch, looked up once per device with that
+// device current (host code cannot use the symbol itself as an address).
+int staticScratchAddress(void **out) {
+  static std::mutex mu;
+  static void *addr[128] = {};
+  int dev = 0;
+  RFLU_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: device ordinal out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    RFLU_CUDA(cudaGetSymbolAddress(&p, gStaticScratch));
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return RFLU_OK;
+}
+
+// True when p is device (or managed) memory the kernels may read or write.
+bool isDevicePointer(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
 // Morton (Z-order) key of a point in the unit box of the mesh, 21 bits/axis.
 inline uint64_t spread3(uint64_t x) {
   x &= 0x1fffff;
@@ -98,6 +133,7 @@ struct CtxBase {
   virtual int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) = 0;
   virtual int status(rflu_status *s) = 0;
   virtual int kernelTimes(int nIter, double *ms) = 0;
+  virtual int residualStatic(const double *cvDev, double *rhsDev) = 0;
   cudaStream_t stream = nullptr;
 };
 
@@ -380,6 +416,48 @@ struct Ctx : CtxBase {
     for (auto &e : ev) cudaEventDestroy(e);
     for (int k = 0; k < 4; ++k) ms[k] = acc[k] / nIter;
     return checkLaunch("kernel_times");
+  }
+  // The residual of rflu_gpu_residual on device buffers, with every
+  // intermediate (renumbered state, dependent variables, primitive state,
+  // gradients, face fluxes, cell residuals) carved out of gStaticScratch
+  // instead of the context's own buffers.  Nothing in the scratch has to
+  // start at zero: each element a kernel reads was written earlier in the
+  // same call.
+  int residualStatic(const double *cvDev, double *rhsDev) override {
+    if (!cvDev || !rhsDev) return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: null argument");
+    if (!isDevicePointer(cvDev) || !isDevicePointer(rhsDev))
+      return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: cv and rhs must be device (or managed) memory");
+    const size_t nc = V.nc, nT = (size_t)V.nf + V.nb;
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t bCv = up(5 * nc * sizeof(double)), bDv = up(3 * nc * sizeof(double));
+    const size_t bPrim = up(5 * nc * sizeof(R)), bGrad = up(15 * nc * sizeof(R));
+    const size_t bFlux = up(5 * nT * sizeof(R)), bRhs = up(5 * nc * sizeof(R));
+    const size_t need = bCv + bDv + bPrim + bGrad + bFlux + bRhs;
+    if (need > kStaticScratchBytes)
+      return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: this mesh needs " + std::to_string(need) +
+                                    " bytes of scratch; the static scratch holds " +
+                                    std::to_string(kStaticScratchBytes) + " bytes");
+    void *base = nullptr;
+    int rc = staticScratchAddress(&base);
+    if (rc) return rc;
+    unsigned char *p = (unsigned char *)base;
+    View<R> W = V;
+    W.cv = (double *)p;            p += bCv;
+    W.dv = (double *)p;            p += bDv;
+    W.prim = (R *)p;               p += bPrim;
+    W.grad = (R *)p;               p += bGrad;
+    W.flux = (R *)p;               p += bFlux;
+    W.rhs = (R *)p;
+    kPermuteIn<<<nblk(W.nc), 256, 0, stream>>>(cvDev, W.cv, W.refId, W.nc);
+    ops->initState(W, stream);
+    ops->gradLimit(W, stream);
+    ops->faceFlux(W, stream);
+    ops->gatherRhs(W, stream);
+    kPermuteOut<R><<<nblk(W.nc), 256, 0, stream>>>(W.rhs, rhsDev, W.refId, W.nc, 5);
+    rc = checkLaunch("residual_static");
+    if (rc) return rc;
+    RFLU_CUDA(cudaStreamSynchronize(stream));
+    return RFLU_OK;
   }
   int nPatches = 0;
 };
@@ -702,6 +780,11 @@ int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status) {
 int rflu_gpu_kernel_times(rflu_gpu_ctx *ctx, int nIter, double *ms) {
   CTX_CHECK("rflu_gpu_kernel_times");
   return ctx->impl->kernelTimes(nIter, ms);
+}
+
+int rflu_gpu_residual_static(rflu_gpu_ctx *ctx, const double *cvDev, double *rhsDev) {
+  CTX_CHECK("rflu_gpu_residual_static");
+  return ctx->impl->residualStatic(cvDev, rhsDev);
 }
 
 }  // extern "C"
