@@ -346,6 +346,8 @@ struct Ctx : CtxBase {
   }
   int vjp(const double *cv, const double *rhsBar, double *cvBar) override {
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
+    if (V.p.reconst == 10)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: the eigen-frame velocity limiter (RECONST 10) has a tangent only");
     int rc = adjointPrep(cv);
     if (rc) return rc;
     const size_t nc = V.nc;
@@ -367,6 +369,8 @@ struct Ctx : CtxBase {
   int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) override {
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
+    if (cvBar && V.p.reconst == 10)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through RECONST 10");
     int rc = adjointPrep(cv);
     if (rc) return rc;
     const size_t nc = V.nc;
@@ -602,6 +606,19 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   }
   std::vector<double> vol(nc);
   for (int i = 0; i < nc; ++i) vol[i] = g->vol[refId[i]];
+  // transposed stencil for the adjoint of the LSQ gradient (FP64 modes)
+  std::vector<int> tsOff(nc + 1, 0), tsCell(stIdx.size()), tsEnt(stIdx.size());
+  for (size_t s = 0; s < stIdx.size(); ++s) tsOff[stIdx[s] + 1]++;
+  for (int j = 0; j < nc; ++j) tsOff[j + 1] += tsOff[j];
+  {
+    std::vector<int> fill(tsOff.begin(), tsOff.end() - 1);
+    for (int i = 0; i < nc; ++i)
+      for (int s = stOff[i]; s < stOff[i + 1]; ++s) {
+        const int e = fill[stIdx[s]]++;
+        tsCell[e] = i;
+        tsEnt[e] = s;
+      }
+  }
 
   // ---- device upload -----------------------------------------------------------
   V.nc = nc; V.nf = nf; V.nb = nb;
@@ -620,6 +637,9 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
   PUT(V.vol, vol, double); PUT(V.epsq, epsq, R);
   PUT(V.refId, refId, int);
+  if (num->precision != RFLU_PREC_MIXED) {
+    PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
+  }
 #undef PUT
   if ((rc = alloc(&V.cv, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.dv, 3 * (size_t)nc))) return rc;
@@ -662,7 +682,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     P.ark[0] = 1.0; P.grk[0] = 1.0;
   }
   // adjoint workspace: gradients/limiter factors/face adjoints of one residual
-  workBytes = sizeof(double) * (size_t)(64 * (size_t)nc + 10 * ((size_t)nf + nb) + 64);
+  workBytes = sizeof(double) * (size_t)(96 * (size_t)nc + 24 * ((size_t)nf + nb) + 64);
   if (num->precision != RFLU_PREC_MIXED) {
     if ((rc = alloc((char **)&work, workBytes))) return rc;
   }

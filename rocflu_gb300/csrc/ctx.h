@@ -55,6 +55,9 @@ struct View {
   const double *vol;
   const R *epsq;                    // Venkatakrishnan eps^2 = (vol^(1/3))^3 per cell
   const int *refId;                 // renumbered -> reference (0-based) cell id
+  // transposed stencil (FP64 modes): for cell j, the (cell i, entry s) pairs
+  // of the stencils that contain j, for the adjoint of the LSQ gradient
+  const int *tsOff, *tsCell, *tsEnt;
   // state
   double *cv;                       // (5, nc)
   double *dv;                       // (3, nc): p, T, c

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "ctx.h"
+#include "dual.cuh"
 #include "physics.cuh"
 
 namespace rflu {
@@ -82,7 +83,24 @@ __global__ void kInitState(View<R> V) {
 }
 
 // ---------------------------------------------------------------------------
-// Gradient + limiter, one thread per cell.
+// Cell data as the stage code reads it.  PlainLoad reads the primal arrays
+// (S = R, the state type; H = double, the type of the first-order paths,
+// FP64 in every mode); the tangent kernels use a loader whose S and H are
+// dual numbers carrying the directional derivatives.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct PlainLoad {
+  using S = R;
+  using H = double;
+  const View<R> &V;
+  __device__ S prim(int k, int c) const { return V.prim[(size_t)k * V.nc + c]; }
+  __device__ S grad(int k, int c) const { return V.grad[(size_t)k * V.nc + c]; }
+  __device__ H cv(int k, int c) const { return V.cv[(size_t)k * V.nc + c]; }
+  __device__ H dv(int k, int c) const { return V.dv[(size_t)k * V.nc + c]; }
+};
+
+// ---------------------------------------------------------------------------
+// Gradient + limiter of one cell.
 // LSQ gradient: RFLU_ComputeGradCellsFast_3D (modflu/RFLU_ModDifferentiationCells.F90:
 // 931-1178) with the per-member weights precomputed at set-up.
 // Limiters: RFLU_ComputeLimiterBarthJesp (modflu/RFLU_ModLimiters.F90:132-322),
@@ -91,23 +109,21 @@ __global__ void kInitState(View<R> V) {
 // only its own gradient and its face neighbours' values, so the reference's
 // two face sweeps become two loops over the cell's own faces.
 // ---------------------------------------------------------------------------
-template <typename R>
-__global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= V.nc) return;
-  const size_t n = V.nc;
-  R q[5], g[15];
+template <typename R, typename L>
+__device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typename L::S *g) {
+  using S = typename L::S;
+  S q[5];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) q[k] = V.prim[k * n + i];
+  for (int k = 0; k < 5; ++k) q[k] = ld.prim(k, i);
 #pragma unroll
-  for (int k = 0; k < 15; ++k) g[k] = R(0);
+  for (int k = 0; k < 15; ++k) g[k] = S(0);
   const int sb = V.stOff[i], se = V.stOff[i + 1];
   for (int s = sb; s < se; ++s) {
     const int j = V.stIdx[s];
-    const R wx = V.wx[s], wy = V.wy[s], wz = V.wz[s];
+    const S wx = S(V.wx[s]), wy = S(V.wy[s]), wz = S(V.wz[s]);
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      R d = V.prim[k * n + j] - q[k];
+      S d = ld.prim(k, j) - q[k];
       g[3 * k] = g[3 * k] + wx * d;
       g[3 * k + 1] = g[3 * k + 1] + wy * d;
       g[3 * k + 2] = g[3 * k + 2] + wz * d;
@@ -117,9 +133,9 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
   if (rc == 10 || rc == 100 || rc == 11) {
     // scalar limiters: min/max over face neighbours, then per face side
-    R vmin[5], vmax[5], lim[5];
+    S vmin[5], vmax[5], lim[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; lim[k] = R(1); }
+    for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; lim[k] = S(1); }
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
       if (code < 0) continue;
@@ -127,44 +143,44 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
       const int nb = (code & 1) ? V.fc1[f] : V.fc2[f];
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        R x = V.prim[k * n + nb];
+        S x = ld.prim(k, nb);
         vmin[k] = fmin2(vmin[k], x);
         vmax[k] = fmax2(vmax[k], x);
       }
     }
-    R epsq = (rc == 11) ? V.epsq[i] : R(0);
+    S epsq = (rc == 11) ? S(V.epsq[i]) : S(0);
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
       const R *d = (code & 1) ? V.dR : V.dL;
-      const R dx = d[f], dy = d[(size_t)V.nf + f], dz = d[2 * (size_t)V.nf + f];
+      const S dx = S(d[f]), dy = S(d[(size_t)V.nf + f]), dz = S(d[2 * (size_t)V.nf + f]);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         if (rc == 10 && k >= 1 && k <= 3) continue;
         // d2 = grad . (cofg - fc), the reference's sign
-        R d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
-        R dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
+        S d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
+        S dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
         if (rc == 11) {
-          const R tiny = R(1.0e-12);
-          if (d2 > R(0)) {
-            R numer = (dmax * dmax + epsq) * d2 + R(2) * d2 * d2 * dmax;
-            R denom = d2 * (dmax * dmax + R(2) * d2 * d2 + dmax * d2 + epsq);
+          const S tiny = S(1.0e-12);
+          if (d2 > S(0)) {
+            S numer = (dmax * dmax + epsq) * d2 + S(2) * d2 * d2 * dmax;
+            S denom = d2 * (dmax * dmax + S(2) * d2 * d2 + dmax * d2 + epsq);
             lim[k] = fmin2(numer / (denom + tiny), lim[k]);
-          } else if (d2 < R(0)) {
-            R numer = (dmin * dmin + epsq) * d2 + R(2) * d2 * d2 * dmin;
-            R denom = d2 * (dmin * dmin + R(2) * d2 * d2 + dmin * d2 + epsq);
+          } else if (d2 < S(0)) {
+            S numer = (dmin * dmin + epsq) * d2 + S(2) * d2 * d2 * dmin;
+            S denom = d2 * (dmin * dmin + S(2) * d2 * d2 + dmin * d2 + epsq);
             lim[k] = fmin2(numer / (denom + tiny), lim[k]);
           }
         } else {
-          if (d2 > R(0)) lim[k] = fmin2(fmin2(R(1), dmax / d2), lim[k]);
-          else if (d2 < R(0)) lim[k] = fmin2(fmin2(R(1), dmin / d2), lim[k]);
+          if (d2 > S(0)) lim[k] = fmin2(fmin2(S(1), dmax / d2), lim[k]);
+          else if (d2 < S(0)) lim[k] = fmin2(fmin2(S(1), dmin / d2), lim[k]);
         }
       }
     }
     if (rc == 10) {
       // frame-invariant velocity limiting along the strain-rate eigenvectors
-      R G[9], S[9], A[9], ev[3];
+      S G[9], Sy[9], A[9], ev[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -172,20 +188,20 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) S[a + 3 * b] = R(0.5) * (G[a + 3 * b] + G[b + 3 * a]);
-      symmetricEigen3(S, A, ev);
-      R dmn[3] = {R(0), R(0), R(0)}, dmx[3] = {R(0), R(0), R(0)}, al[3] = {R(1), R(1), R(1)};
+        for (int b = 0; b < 3; ++b) Sy[a + 3 * b] = S(0.5) * (G[a + 3 * b] + G[b + 3 * a]);
+      symmetricEigen3(Sy, A, ev);
+      S dmn[3] = {S(0), S(0), S(0)}, dmx[3] = {S(0), S(0), S(0)}, al[3] = {S(1), S(1), S(1)};
       for (int e = cb; e < ce; ++e) {
         const int code = V.cfEnt[e];
         if (code < 0) continue;
         const int f = code >> 1, side = code & 1;
         const int c1 = V.fc1[f], c2 = V.fc2[f];
-        R du[3];
+        S du[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) du[k] = V.prim[(1 + k) * n + c2] - V.prim[(1 + k) * n + c1];
+        for (int k = 0; k < 3; ++k) du[k] = ld.prim(1 + k, c2) - ld.prim(1 + k, c1);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          R pr = R(0);
+          S pr = S(0);
           pr = pr + A[3 * j] * du[0];
           pr = pr + A[3 * j + 1] * du[1];
           pr = pr + A[3 * j + 2] * du[2];
@@ -199,11 +215,11 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
         if (code < 0) continue;
         const int f = code >> 1;
         const R *d = (code & 1) ? V.dR : V.dL;
-        const R off[3] = {-d[f], -d[(size_t)V.nf + f], -d[2 * (size_t)V.nf + f]};
-        R sh[3];
+        const S off[3] = {-S(d[f]), -S(d[(size_t)V.nf + f]), -S(d[2 * (size_t)V.nf + f])};
+        S sh[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          R s = R(0);
+          S s = S(0);
           s = s + G[a] * off[0];
           s = s + G[a + 3] * off[1];
           s = s + G[a + 6] * off[2];
@@ -211,36 +227,36 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          R pr = R(0);
+          S pr = S(0);
           pr = pr + A[3 * j] * sh[0];
           pr = pr + A[3 * j + 1] * sh[1];
           pr = pr + A[3 * j + 2] * sh[2];
-          if (pr > R(0)) al[j] = fmin2(al[j], dmx[j] / pr);
-          else if (pr < R(0)) al[j] = fmin2(al[j], dmn[j] / pr);
+          if (pr > S(0)) al[j] = fmin2(al[j], dmx[j] / pr);
+          else if (pr < S(0)) al[j] = fmin2(al[j], dmn[j] / pr);
         }
       }
-      R mx = fabs_(ev[0]);
+      S mx = fabs_(ev[0]);
       mx = fmax2(mx, fabs_(ev[1]));
       mx = fmax2(mx, fabs_(ev[2]));
-      const R scale = R(1.0e-3) * mx;
+      const S scale = S(1.0e-3) * mx;
       const bool e12 = (ev[1] - ev[0] <= scale), e23 = (ev[2] - ev[1] <= scale);
       if (e12 && e23) {
-        R m = fmin2(fmin2(al[0], al[1]), al[2]);
+        S m = fmin2(fmin2(al[0], al[1]), al[2]);
         al[0] = al[1] = al[2] = m;
       } else if (e12) {
-        R m = fmin2(al[0], al[1]);
+        S m = fmin2(al[0], al[1]);
         al[0] = al[1] = m;
       } else if (e23) {
-        R m = fmin2(al[1], al[2]);
+        S m = fmin2(al[1], al[2]);
         al[1] = al[2] = m;
       }
       // G <- A diag(alpha) A^T G
-      R Rm[9];
+      S Rm[9];
 #pragma unroll
       for (int j = 0; j < 3; ++j)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          R s = R(0);
+          S s = S(0);
           s = s + A[3 * j] * G[3 * c];
           s = s + A[3 * j + 1] * G[1 + 3 * c];
           s = s + A[3 * j + 2] * G[2 + 3 * c];
@@ -250,13 +266,13 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
       for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          R s = R(0);
+          S s = S(0);
           s = s + A[a] * Rm[3 * c];
           s = s + A[a + 3] * Rm[1 + 3 * c];
           s = s + A[a + 6] * Rm[2 + 3 * c];
           g[3 * (1 + a) + c] = s;
         }
-      lim[1] = lim[2] = lim[3] = R(1);
+      lim[1] = lim[2] = lim[3] = S(1);
     }
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
@@ -265,6 +281,15 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
       g[3 * k + 2] = lim[k] * g[3 * k + 2];
     }
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  R g[15];
+  gradLimitCell(V, PlainLoad<R>{V}, i, g);
+  const size_t n = V.nc;
 #pragma unroll
   for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
 }
@@ -274,77 +299,175 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
 // cell primitive (with the reference's momentum round trip in the FP64 modes)
 // plus grad . (fc - cofg).
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ inline void faceState(const View<R> &V, int c, R dx, R dy, R dz, R *s, R &irCell) {
-  const size_t n = V.nc;
-  R r = V.prim[c];
-  R ir = R(1) / r;
-  R u = V.prim[n + c], v = V.prim[2 * n + c], w = V.prim[3 * n + c];
+template <typename R, typename L>
+__device__ inline void faceState(const View<R> &V, const L &ld, int c, typename L::S dx, typename L::S dy,
+                                 typename L::S dz, typename L::S *s, typename L::S &irCell) {
+  using S = typename L::S;
+  S r = ld.prim(0, c);
+  S ir = S(1) / r;
+  S u = ld.prim(1, c), v = ld.prim(2, c), w = ld.prim(3, c);
   if (Ref<R>::on) {
     // ul = pCv(CV_MIXT_XMOM,c1)*irl with pCv(XMOM) = r*u after RFLU_ConvertCvPrim2Cons
     u = (r * u) * ir;
     v = (r * v) * ir;
     w = (r * w) * ir;
   }
-  R p = V.prim[4 * n + c];
-  const R *g = V.grad;
-  s[0] = r + g[0 * n + c] * dx + g[1 * n + c] * dy + g[2 * n + c] * dz;
-  s[1] = u + g[3 * n + c] * dx + g[4 * n + c] * dy + g[5 * n + c] * dz;
-  s[2] = v + g[6 * n + c] * dx + g[7 * n + c] * dy + g[8 * n + c] * dz;
-  s[3] = w + g[9 * n + c] * dx + g[10 * n + c] * dy + g[11 * n + c] * dz;
-  s[4] = p + g[12 * n + c] * dx + g[13 * n + c] * dy + g[14 * n + c] * dz;
+  S p = ld.prim(4, c);
+  s[0] = r + ld.grad(0, c) * dx + ld.grad(1, c) * dy + ld.grad(2, c) * dz;
+  s[1] = u + ld.grad(3, c) * dx + ld.grad(4, c) * dy + ld.grad(5, c) * dz;
+  s[2] = v + ld.grad(6, c) * dx + ld.grad(7, c) * dy + ld.grad(8, c) * dz;
+  s[3] = w + ld.grad(9, c) * dx + ld.grad(10, c) * dy + ld.grad(11, c) * dz;
+  s[4] = p + ld.grad(12, c) * dx + ld.grad(13, c) * dy + ld.grad(14, c) * dz;
   irCell = ir;
 }
 
-template <typename R>
-__device__ inline void riemann2(const Params &P, R nx, R ny, R nz, R nm, const R *L, R irl, const R *Rt, R irr, R *flx) {
-  const R cp = (R)P.refCp, g = (R)P.refGamma;
+template <typename S>
+__device__ inline void riemann2(const Params &P, S nx, S ny, S nz, S nm, const S *L, S irl, const S *Rt, S irr, S *flx) {
+  const S cp = S(P.refCp), g = S(P.refGamma);
   if (P.spaceDiscr == 1) {
-    R gc = cp - cp / g;
-    R tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
-    R Hl = perfHo(cp, tl, L[1], L[2], L[3]), Hr = perfHo(cp, tr, Rt[1], Rt[2], Rt[3]);
-    roeFlux(g, (R)P.epsEntr, (R)P.dissFact, nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], Hl, Rt[0], Rt[1], Rt[2],
+    S gc = cp - cp / g;
+    S tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
+    S Hl = perfHo(cp, tl, L[1], L[2], L[3]), Hr = perfHo(cp, tr, Rt[1], Rt[2], Rt[3]);
+    roeFlux(g, S(P.epsEntr), S(P.dissFact), nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], Hl, Rt[0], Rt[1], Rt[2],
             Rt[3], Rt[4], Hr, flx);
   } else if (P.spaceDiscr == 3) {
-    R el = perfEo(L[0], g, L[4], L[1], L[2], L[3]), al = sqrt_(g * L[4] / L[0]);
-    R er = perfEo(Rt[0], g, Rt[4], Rt[1], Rt[2], Rt[3]), ar = sqrt_(g * Rt[4] / Rt[0]);
-    R Hl = el + irl * L[4], Hr = er + irr * Rt[4];
+    S el = perfEo(L[0], g, L[4], L[1], L[2], L[3]), al = sqrt_(g * L[4] / L[0]);
+    S er = perfEo(Rt[0], g, Rt[4], Rt[1], Rt[2], Rt[3]), ar = sqrt_(g * Rt[4] / Rt[0]);
+    S Hl = el + irl * L[4], Hr = er + irr * Rt[4];
     hllcFlux(g, nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], el, al, Hl, Rt[0], Rt[1], Rt[2], Rt[3], Rt[4], er, ar,
              Hr, flx);
   } else {
-    R gc = cp - cp / g;
-    R tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
-    R al = sqrt_(g * gc * tl), ar = sqrt_(g * gc * tr);
-    R Hl = perfHo(cp, tl, L[1], L[2], L[3]), Hr = perfHo(cp, tr, Rt[1], Rt[2], Rt[3]);
+    S gc = cp - cp / g;
+    S tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
+    S al = sqrt_(g * gc * tl), ar = sqrt_(g * gc * tr);
+    S Hl = perfHo(cp, tl, L[1], L[2], L[3]), Hr = perfHo(cp, tr, Rt[1], Rt[2], Rt[3]);
     ausmFlux(nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], Hl, al, Rt[0], Rt[1], Rt[2], Rt[3], Rt[4], Hr, ar, flx);
   }
 }
 
-// First-order interior flux from cv and dv (FP64 throughout; the mixed mode
-// converts the result).
-template <typename R>
-__device__ inline void riemann1(const View<R> &V, int c1, int c2, double nx, double ny, double nz, double nm,
-                                double *flx) {
-  const Params &P = V.p;
-  const size_t n = V.nc;
-  double cl[5], cr[5];
-  loadCv(V, c1, cl);
-  loadCv(V, c2, cr);
-  double rl = cl[0], irl = 1.0 / rl, ul = cl[1] * irl, vl = cl[2] * irl, wl = cl[3] * irl;
-  double rr = cr[0], irr = 1.0 / rr, ur = cr[1] * irr, vr = cr[2] * irr, wr = cr[3] * irr;
-  double pl = V.dv[c1], pr = V.dv[c2];
-  const double cp = P.refCp, g = P.refGamma;
+// First-order interior flux from cv and dv (type H: FP64 in every mode).
+template <typename H>
+__device__ inline void riemann1(const Params &P, const H *cl, const H *dvl, const H *cr, const H *dvr, H nx, H ny,
+                                H nz, H nm, H *flx) {
+  H rl = cl[0], irl = H(1) / rl, ul = cl[1] * irl, vl = cl[2] * irl, wl = cl[3] * irl;
+  H rr = cr[0], irr = H(1) / rr, ur = cr[1] * irr, vr = cr[2] * irr, wr = cr[3] * irr;
+  H pl = dvl[0], pr = dvr[0];
+  const H cp = H(P.refCp), g = H(P.refGamma);
   if (P.spaceDiscr == 1) {
-    double Hl = perfHo(cp, V.dv[n + c1], ul, vl, wl), Hr = perfHo(cp, V.dv[n + c2], ur, vr, wr);
-    roeFlux(g, P.epsEntr, P.dissFact, nx, ny, nz, nm, rl, ul, vl, wl, pl, Hl, rr, ur, vr, wr, pr, Hr, flx);
+    H Hl = perfHo(cp, dvl[1], ul, vl, wl), Hr = perfHo(cp, dvr[1], ur, vr, wr);
+    roeFlux(g, H(P.epsEntr), H(P.dissFact), nx, ny, nz, nm, rl, ul, vl, wl, pl, Hl, rr, ur, vr, wr, pr, Hr, flx);
   } else if (P.spaceDiscr == 3) {
-    double el = cl[4] * irl, er = cr[4] * irr;
-    double Hl = el + irl * pl, Hr = er + irr * pr;
-    hllcFlux(g, nx, ny, nz, nm, rl, ul, vl, wl, pl, el, V.dv[2 * n + c1], Hl, rr, ur, vr, wr, pr, er, V.dv[2 * n + c2],
-             Hr, flx);
+    H el = cl[4] * irl, er = cr[4] * irr;
+    H Hl = el + irl * pl, Hr = er + irr * pr;
+    hllcFlux(g, nx, ny, nz, nm, rl, ul, vl, wl, pl, el, dvl[2], Hl, rr, ur, vr, wr, pr, er, dvr[2], Hr, flx);
   } else {
-    double Hl = cl[4] * irl + pl / rl, Hr = cr[4] * irr + pr / rr;
-    ausmFlux(nx, ny, nz, nm, rl, ul, vl, wl, pl, Hl, V.dv[2 * n + c1], rr, ur, vr, wr, pr, Hr, V.dv[2 * n + c2], flx);
+    H Hl = cl[4] * irl + pl / rl, Hr = cr[4] * irr + pr / rr;
+    ausmFlux(nx, ny, nz, nm, rl, ul, vl, wl, pl, Hl, dvl[2], rr, ur, vr, wr, pr, Hr, dvr[2], flx);
+  }
+}
+
+// First-order patch flux (RFLU_CentralFirstPatch, slip wall :785-911 and
+// outflow :571-784) from the cell's cv and p.  RFLU_CentralFirstPatch reads
+// cv as CellGradientsMP left it: in a 2nd-order run the momentum went
+// through the prim round trip and, in the PICL build, the energy slot holds
+// the pressure.
+template <typename H>
+__device__ inline void patch1(const Params &P, int type, int outflowType, double pOut, const H *cvIn, H pl, H nx, H ny,
+                              H nz, H nm, H *fd) {
+  H cv[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) cv[k] = cvIn[k];
+  if (P.spaceOrder == 2) {
+    const H ir = H(1) / cv[0];
+    const H up = ir * cv[1], vp = ir * cv[2], wp = ir * cv[3];
+    cv[1] = cv[0] * up;
+    cv[2] = cv[0] * vp;
+    cv[3] = cv[0] * wp;
+    if (P.piclBuild) {
+      cv[4] = pl;
+    } else {
+      const H g = H(P.gvCp) / (H(P.gvCp) - H(8314.3) / H(P.gvMol));
+      cv[4] = cv[0] * perfEo(cv[0], g, pl, up, vp, wp);
+    }
+  }
+  if (type == 60) {
+    fd[0] = H(0);
+    fd[1] = pl * nx * nm;
+    fd[2] = pl * ny * nm;
+    fd[3] = pl * nz * nm;
+    fd[4] = pl * H(0) * nm;
+  } else {
+    outflowPatchFlux(outflowType, H(pOut), H(P.gvCp), H(P.gvMol), nx, ny, nz, nm, cv[0], cv[1], cv[2], cv[3], cv[4],
+                     pl, fd);
+  }
+}
+
+// Second-order patch flux (RFLU_CentralSecondPatch, slip wall :858-1029,
+// outflow :634-857) from the reconstructed face state L.
+template <typename S>
+__device__ inline void patch2(const Params &P, int type, int outflowType, double pOut, const S *L, S nx, S ny, S nz,
+                              S nm, S *flx) {
+  if (type == 60) {
+    flx[0] = S(0);
+    flx[1] = L[4] * nx * nm;
+    flx[2] = L[4] * ny * nm;
+    flx[3] = L[4] * nz * nm;
+    flx[4] = L[4] * S(0) * nm;
+  } else {
+    const S cp = S(P.gvCp), mol = S(P.gvMol);
+    S rgas = S(8314.3) / mol;
+    S g = cp / (cp - rgas);
+    S rul = L[0] * L[1], rvl = L[0] * L[2], rwl = L[0] * L[3];
+    S rel = L[0] * perfEo(L[0], g, L[4], L[1], L[2], L[3]);
+    outflowPatchFlux(outflowType, S(pOut), cp, mol, nx, ny, nz, nm, L[0], rul, rvl, rwl, rel, L[4], flx);
+  }
+}
+
+template <typename To, typename From> __device__ inline To cvt(const From &x) { return To(x); }
+
+// Flux of face t (interior faces [0,nf), then boundary faces).
+template <typename R, typename L>
+__device__ inline void faceFluxEval(const View<R> &V, const L &ld, int t, typename L::S *flx) {
+  using S = typename L::S;
+  using H = typename L::H;
+  const Params &P = V.p;
+  if (t < V.nf) {
+    const int f = t, c1 = V.fc1[f], c2 = V.fc2[f];
+    if (P.spaceOrder == 1) {
+      H cl[5], cr[5], dl[3], dr[3], fd[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) { cl[k] = ld.cv(k, c1); cr[k] = ld.cv(k, c2); }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { dl[k] = ld.dv(k, c1); dr[k] = ld.dv(k, c2); }
+      riemann1(P, cl, dl, cr, dr, H((double)V.fnx[f]), H((double)V.fny[f]), H((double)V.fnz[f]), H((double)V.fnm[f]),
+               fd);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) flx[k] = cvt<S>(fd[k]);
+    } else {
+      const size_t nf = V.nf;
+      S Lf[5], Rt[5], irl, irr;
+      faceState(V, ld, c1, S(V.dL[f]), S(V.dL[nf + f]), S(V.dL[2 * nf + f]), Lf, irl);
+      faceState(V, ld, c2, S(V.dR[f]), S(V.dR[nf + f]), S(V.dR[2 * nf + f]), Rt, irr);
+      riemann2(P, S(V.fnx[f]), S(V.fny[f]), S(V.fnz[f]), S(V.fnm[f]), Lf, irl, Rt, irr, flx);
+    }
+  } else {
+    const int b = t - V.nf, c = V.bcell[b], ip = V.bpatch[b];
+    const int type = V.patchType[ip], order = V.patchOrder[ip];
+    if (order == 1) {
+      H cv[5], fd[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) cv[k] = ld.cv(k, c);
+      patch1(P, type, V.patchOutflow[ip], V.patchPout[ip], cv, ld.dv(0, c), H((double)V.bnx[b]),
+             H((double)V.bny[b]), H((double)V.bnz[b]), H((double)V.bnm[b]), fd);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) flx[k] = cvt<S>(fd[k]);
+    } else {
+      const size_t nb = V.nb;
+      S Lf[5], irl;
+      faceState(V, ld, c, S(V.bd[b]), S(V.bd[nb + b]), S(V.bd[2 * nb + b]), Lf, irl);
+      patch2(P, type, V.patchOutflow[ip], V.patchPout[ip], Lf, S(V.bnx[b]), S(V.bny[b]), S(V.bnz[b]), S(V.bnm[b]),
+             flx);
+    }
   }
 }
 
@@ -354,83 +477,8 @@ __global__ void __launch_bounds__(kBlock) kFaceFlux(View<R> V) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nfT = V.nf + V.nb;
   if (t >= nfT) return;
-  const Params &P = V.p;
-  const size_t n = V.nc;
   R flx[5];
-  if (t < V.nf) {
-    const int f = t, c1 = V.fc1[f], c2 = V.fc2[f];
-    const R nx = V.fnx[f], ny = V.fny[f], nz = V.fnz[f], nm = V.fnm[f];
-    if (P.spaceOrder == 1) {
-      double fd[5];
-      riemann1(V, c1, c2, (double)nx, (double)ny, (double)nz, (double)nm, fd);
-#pragma unroll
-      for (int k = 0; k < 5; ++k) flx[k] = (R)fd[k];
-    } else {
-      const size_t nf = V.nf;
-      R L[5], Rt[5], irl, irr;
-      faceState(V, c1, V.dL[f], V.dL[nf + f], V.dL[2 * nf + f], L, irl);
-      faceState(V, c2, V.dR[f], V.dR[nf + f], V.dR[2 * nf + f], Rt, irr);
-      riemann2(P, nx, ny, nz, nm, L, irl, Rt, irr, flx);
-    }
-  } else {
-    const int b = t - V.nf, c = V.bcell[b], ip = V.bpatch[b];
-    const int type = V.patchType[ip], order = V.patchOrder[ip];
-    const R nx = V.bnx[b], ny = V.bny[b], nz = V.bnz[b], nm = V.bnm[b];
-    if (order == 1) {
-      // RFLU_CentralFirstPatch reads cv as CellGradientsMP left it: in a
-      // 2nd-order run the momentum went through the prim round trip and,
-      // in the PICL build, the energy slot holds the pressure.
-      double cv[5];
-      loadCv(V, c, cv);
-      const double pl = V.dv[c];
-      if (P.spaceOrder == 2) {
-        const double ir = 1.0 / cv[0];
-        const double up = ir * cv[1], vp = ir * cv[2], wp = ir * cv[3];
-        cv[1] = cv[0] * up;
-        cv[2] = cv[0] * vp;
-        cv[3] = cv[0] * wp;
-        if (P.piclBuild) {
-          cv[4] = pl;
-        } else {
-          const double g = P.gvCp / (P.gvCp - 8314.3 / P.gvMol);
-          cv[4] = cv[0] * perfEo(cv[0], g, pl, up, vp, wp);
-        }
-      }
-      double fd[5];
-      if (type == 60) {
-        fd[0] = 0.0;
-        fd[1] = pl * (double)nx * (double)nm;
-        fd[2] = pl * (double)ny * (double)nm;
-        fd[3] = pl * (double)nz * (double)nm;
-        fd[4] = pl * 0.0 * (double)nm;
-      } else {
-        outflowPatchFlux(V.patchOutflow[ip], V.patchPout[ip], P.gvCp, P.gvMol, (double)nx, (double)ny, (double)nz,
-                         (double)nm, cv[0], cv[1], cv[2], cv[3], cv[4], pl, fd);
-      }
-#pragma unroll
-      for (int k = 0; k < 5; ++k) flx[k] = (R)fd[k];
-    } else {
-      const size_t nb = V.nb;
-      R L[5], irl;
-      faceState(V, c, V.bd[b], V.bd[nb + b], V.bd[2 * nb + b], L, irl);
-      if (type == 60) {
-        flx[0] = R(0);
-        flx[1] = L[4] * nx * nm;
-        flx[2] = L[4] * ny * nm;
-        flx[3] = L[4] * nz * nm;
-        flx[4] = L[4] * R(0) * nm;
-      } else {
-        // RFLU_CentralSecondPatch outflow: rel from the reconstructed state
-        const R cp = (R)P.gvCp, mol = (R)P.gvMol;
-        R rgas = R(8314.3) / mol;
-        R g = cp / (cp - rgas);
-        R rul = L[0] * L[1], rvl = L[0] * L[2], rwl = L[0] * L[3];
-        R rel = L[0] * perfEo(L[0], g, L[4], L[1], L[2], L[3]);
-        outflowPatchFlux(V.patchOutflow[ip], (R)V.patchPout[ip], cp, mol, nx, ny, nz, nm, L[0], rul, rvl, rwl, rel,
-                         L[4], flx);
-      }
-    }
-  }
+  faceFluxEval(V, PlainLoad<R>{V}, t, flx);
   const size_t nT = nfT;
 #pragma unroll
   for (int k = 0; k < 5; ++k) V.flux[k * nT + t] = flx[k];
@@ -440,11 +488,11 @@ __global__ void __launch_bounds__(kBlock) kFaceFlux(View<R> V) {
 // Residual gather (ConvectiveFluxes, libfloflu/ConvectiveFluxes.F90:133-175):
 // rhs(c) = -diss(c) + sum over the cell's faces in reference order of +-F.
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ inline void gatherRhs(const View<R> &V, int i, R *rhs) {
+template <typename R, typename T>
+__device__ inline void gatherRhs(const View<R> &V, const T *flux, int i, T *rhs) {
   const size_t nT = (size_t)V.nf + V.nb;
 #pragma unroll
-  for (int k = 0; k < 5; ++k) rhs[k] = -R(0);
+  for (int k = 0; k < 5; ++k) rhs[k] = -T(0);
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
   for (int e = cb; e < ce; ++e) {
     const int code = V.cfEnt[e];
@@ -452,15 +500,15 @@ __device__ inline void gatherRhs(const View<R> &V, int i, R *rhs) {
       const int f = code >> 1;
       if (code & 1) {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] - V.flux[k * nT + f];
+        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] - flux[k * nT + f];
       } else {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] + V.flux[k * nT + f];
+        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] + flux[k * nT + f];
       }
     } else {
       const int b = -code - 1;
       const int k0 = (V.patchType[V.bpatch[b]] == 60) ? 1 : 0;  // slip walls leave rhs(DENS)
-      for (int k = k0; k < 5; ++k) rhs[k] = rhs[k] + V.flux[k * nT + V.nf + b];
+      for (int k = k0; k < 5; ++k) rhs[k] = rhs[k] + flux[k * nT + V.nf + b];
     }
   }
 }
@@ -470,7 +518,7 @@ __global__ void __launch_bounds__(kBlock) kGatherRhs(View<R> V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   R rhs[5];
-  gatherRhs(V, i, rhs);
+  gatherRhs(V, (const R *)V.flux, i, rhs);
 #pragma unroll
   for (int k = 0; k < 5; ++k) V.rhs[(size_t)k * V.nc + i] = rhs[k];
 }
@@ -521,7 +569,7 @@ __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, c
   const Params &P = V.p;
   const size_t n = V.nc;
   R rhs[5];
-  gatherRhs(V, i, rhs);
+  gatherRhs(V, (const R *)V.flux, i, rhs);
   const double fac = P.ark[iStage - 1] * (*dtp);
   const double grk = P.grk[iStage - 1];
   const double adtv = fac / V.vol[i];
