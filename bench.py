@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--precisions", default="mixed,fp64", help="device paths to time (profiling runs time one)")
+    p.add_argument("--skip-adjoint", action="store_true")
+    p.add_argument("--adj-n", type=int, default=32, help="hexes per side of the tet adjoint case")
     return p.parse_args()
 
 
@@ -122,6 +124,22 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
+def dram_traffic(kernel, n_cells):
+    """DRAM bytes (read + write) per launch of `kernel`, from the committed ncu
+    summary (profiles/dram_traffic_per_cell.txt: one 'kernel bytes_per_cell'
+    line per kernel, measured on a smaller case of the same workload and
+    scaled here by the cells one launch processes); None when absent."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_per_cell.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == kernel:
+                return float(parts[1]) * n_cells
+    except OSError:
+        pass
+    return None
+
+
 def algorithmic_bytes(region, precision):
     """Bytes per launch of the three stage kernels and of the whole stage,
     counted from the data each kernel must move once (neighbour gathers
@@ -173,6 +191,7 @@ def run_ours(args):
     results = {}
     regions = {}
     precs = [x for x in args.precisions.split(",") if x]
+    clk = ClockSampler(local).start()
     for prec in precs:
         reg = gpu.Region(case, prec, grid=setup)
         regions[prec] = reg
@@ -180,7 +199,6 @@ def run_ours(args):
         t = 0.0
         n, t, rc = reg.step(args.warmup, t)
         barrier()
-        clk = ClockSampler(local).start() if prec == "mixed" else None
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -189,7 +207,7 @@ def run_ours(args):
         e1.synchronize()
         barrier()
         ms = e0.elapsed_time(e1)
-        clocks = clk.stop() if clk else None
+        clocks = None
         if ws > 1:
             import torch.distributed as dist
 
@@ -241,6 +259,7 @@ def run_ours(args):
         units = reg.n_cells * reg.n_stages * args.steps
         e2e = {"value": ws * units / wall / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(host_cv.numel() * 8),
                "d2h_bytes_per_step": int((host_cv.numel() + host_dv.numel()) * 8)}
+    clocks = clk.stop()
 
     # roofline of the dominant kernel of the mixed path
     peaks, peak_kind = measured_peaks()
@@ -248,20 +267,27 @@ def run_ours(args):
     km = results["mixed"]["kernel_ms"]
     dom = max(("gradLimit", "faceFlux", "gatherUpdate"), key=lambda k: km[k])
     achieved = ab[dom] / (km[dom] * 1e-3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get(dom)
-        except Exception:
-            traffic = None
+    traffic = dram_traffic(dom, regions["mixed"].n_cells)
     roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": ab[dom], "launch_ms": km[dom]}
 
+    fp64_tflops = gpu.fp64_rate()
     fp64 = {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms"] / args.steps,
             "kernel_ms": results["fp64"]["kernel_ms"], "mixed_over_fp64": results["mixed"]["value"] / results["fp64"]["value"],
-            "mixed_vs_fp64_error": err}
+            "mixed_vs_fp64_error": err,
+            "roofline": {"bound": "fp64", "peak_fp64_tflops_measured": fp64_tflops,
+                         "note": "FP64 kernels run the FP64 pipe at ~90% (ncu, profiles/); HBM is not their bound"}}
+
+    # single-residual adjoint: 32^3 x 6 jittered tets, 2nd-order Roe, Venkatakrishnan
+    adjoint = None
+    if not args.skip_adjoint:
+        ac = cases.adjoint_tets(args.adj_n)
+        areg = gpu.Region(ac, "fp64")
+        at = areg.adjoint_times(5)
+        adjoint = {"workload": "adjoint_tets%d_roe_venkat" % args.adj_n, "cells": areg.n_cells,
+                   "primal_residual_ms": at[0], "vjp_ms": at[1], "vjp_over_primal": at[1] / at[0]}
+        areg.close()
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -279,10 +305,11 @@ def run_ours(args):
                        "setup_s": setup_s},
             "gpu_launches": 13 * args.steps,
             "fp64": fp64,
+            "adjoint": adjoint,
             "e2e": e2e,
             "roofline": roof,
             "cpu_baseline": cpu,
-            "clocks": results["mixed"]["clocks"],
+            "clocks": clocks,
         }
         print(json.dumps(line))
     if ws > 1:

@@ -154,6 +154,13 @@ int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status);
  * stream and returns the mean duration in ms of [0] gradient+limiter,
  * [1] face fluxes, [2] gather+update, [3] time-step reduction. */
 int rflu_gpu_kernel_times(rflu_gpu_ctx *ctx, int nIter, double *ms);
+/* Diagnostics (no reference counterpart): mean device time in ms of [0] one
+ * primal residual (gradient+limiter, face fluxes, gather) and [1] one
+ * adjoint (rflu_gpu_vjp's kernels) on the current device state, FP64 modes. */
+int rflu_gpu_adjoint_times(rflu_gpu_ctx *ctx, int nIter, double *ms);
+/* Diagnostics: FP64 fused multiply-add rate of the current device in
+ * TFLOP/s (independent FMA chains on every SM), the roof of FP64 kernels. */
+int rflu_gpu_fp64_rate(double *tflops);
 
 /* Residual without any allocation (no counterpart in the reference).
  * Same result as rflu_gpu_residual (rhs only), for callers that cannot

@@ -29,6 +29,7 @@
 namespace rflu {
 namespace RFLU_NS {
 
+#ifdef RFLU_WITH_ADJOINT
 struct AdjWork {
   double *cvd, *primd, *dvd, *gradd, *fluxd;          // tangent state / lambda in cvd
   double *G, *lim, *faceAdj, *Gbar, *qbar, *nbBar, *cvbarD, *dvbar;
@@ -594,13 +595,15 @@ struct AdjointOps {
   }
 };
 
-template <>
-struct AdjointOps<float> {
-  static constexpr void (*jvp)(const View<float> &, const double *, double *, double *, cudaStream_t) = nullptr;
-  static constexpr void (*vjp)(const View<float> &, const double *, double *, double *, cudaStream_t) = nullptr;
-  static constexpr void (*patchPressure)(const View<float> &, int, double *, double *, double *,
-                                         cudaStream_t) = nullptr;
+#else
+// Translation units without the adjoint (the mixed mode): no entries.
+template <typename R>
+struct AdjointOps {
+  static constexpr void (*jvp)(const View<R> &, const double *, double *, double *, cudaStream_t) = nullptr;
+  static constexpr void (*vjp)(const View<R> &, const double *, double *, double *, cudaStream_t) = nullptr;
+  static constexpr void (*patchPressure)(const View<R> &, int, double *, double *, double *, cudaStream_t) = nullptr;
 };
+#endif
 
 }  // namespace RFLU_NS
 }  // namespace rflu

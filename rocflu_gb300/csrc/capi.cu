@@ -104,6 +104,23 @@ bool isDevicePointer(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// FP64 FMA throughput probe: 8 independent chains per thread.
+__device__ double gFmaSink;
+__global__ void kFp64Fma(int iters, double seed) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed * (threadIdx.x + k);
+  const double b = 0.9999999999, c = 1.0e-12;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == 12345.678) gFmaSink = s;  // keeps the chains alive
+}
+
 // Morton (Z-order) key of a point in the unit box of the mesh, 21 bits/axis.
 inline uint64_t spread3(uint64_t x) {
   x &= 0x1fffff;
@@ -134,6 +151,7 @@ struct CtxBase {
   virtual int status(rflu_status *s) = 0;
   virtual int kernelTimes(int nIter, double *ms) = 0;
   virtual int residualStatic(const double *cvDev, double *rhsDev) = 0;
+  virtual int adjointTimes(int nIter, double *ms) = 0;
   cudaStream_t stream = nullptr;
 };
 
@@ -255,8 +273,10 @@ struct Ctx : CtxBase {
     if (stepGraph) return RFLU_OK;
     cudaGraph_t graph;
     RFLU_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    ops->timestep(V, stream);
-    for (int s = 1; s <= V.p.nrkSteps; ++s) stageKernels(s);
+    ops->stepStart(V, stream);  // dt reduction + gradients of stage 1
+    ops->faceFlux(V, stream);
+    ops->gatherUpdate(V, 1, &V.sc->dtMin, stream);
+    for (int s = 2; s <= V.p.nrkSteps; ++s) stageKernels(s);
     ops->stepEnd(V, stream);
     RFLU_CUDA(cudaStreamEndCapture(stream, &graph));
     cudaError_t e = cudaGraphInstantiate(&stepGraph, graph, 0);
@@ -463,6 +483,34 @@ struct Ctx : CtxBase {
     RFLU_CUDA(cudaStreamSynchronize(stream));
     return RFLU_OK;
   }
+  int adjointTimes(int nIter, double *ms) override {
+    if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
+    if (!ops->vjp || V.p.reconst == 10) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
+    const size_t nc = V.nc;
+    RFLU_CUDA(cudaMemsetAsync(staging, 0, sizeof(double) * 5 * nc, stream));
+    cudaEvent_t ev[3];
+    for (auto &e : ev) RFLU_CUDA(cudaEventCreate(&e));
+    double acc[2] = {0, 0};
+    for (int it = 0; it < nIter; ++it) {
+      cudaEventRecord(ev[0], stream);
+      ops->gradLimit(V, stream);
+      ops->faceFlux(V, stream);
+      ops->gatherRhs(V, stream);
+      cudaEventRecord(ev[1], stream);
+      ops->vjp(V, staging, staging + 5 * nc, work, stream);
+      cudaEventRecord(ev[2], stream);
+      RFLU_CUDA(cudaEventSynchronize(ev[2]));
+      for (int k = 0; k < 2; ++k) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+        acc[k] += t;
+      }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    ms[0] = acc[0] / nIter;
+    ms[1] = acc[1] / nIter;
+    return checkLaunch("adjoint_times");
+  }
   int nPatches = 0;
 };
 
@@ -666,6 +714,11 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   P.refCp = num->cp; P.refGamma = num->gamma;
   P.gvCp = num->cp;
   P.gvMol = 8314.3 / (num->cp - num->cp / num->gamma);  // MixtPerf_M_R(MixtPerf_R_CpG(cp,gamma))
+  P.gcR = 8314.3 / P.gvMol;                             // MixtPerf_R_M(M), the round trip
+  P.gRT = P.gvCp / (P.gvCp - P.gcR);                    // MixtPerf_G_CpR(cp,R)
+  P.igcR = 1.0 / P.gcR;
+  P.refCpF = (float)P.refCp; P.refGammaF = (float)P.refGamma; P.epsEntrF = (float)num->epsEntr;
+  P.dissFactF = (float)num->dissFact; P.gvCpF = (float)P.gvCp; P.gvMolF = (float)P.gvMol;
   P.epsEntr = num->epsEntr; P.dissFact = num->dissFact;
   P.cfl = num->cfl; P.dtImposed = num->dtImposed; P.dtMinLimit = num->dtMinLimit;
   for (int k = 0; k < 5; ++k) P.ark[k] = P.grk[k] = 0.0;
@@ -800,6 +853,38 @@ int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status) {
 int rflu_gpu_kernel_times(rflu_gpu_ctx *ctx, int nIter, double *ms) {
   CTX_CHECK("rflu_gpu_kernel_times");
   return ctx->impl->kernelTimes(nIter, ms);
+}
+
+int rflu_gpu_adjoint_times(rflu_gpu_ctx *ctx, int nIter, double *ms) {
+  CTX_CHECK("rflu_gpu_adjoint_times");
+  return ctx->impl->adjointTimes(nIter, ms);
+}
+
+int rflu_gpu_fp64_rate(double *tflops) {
+  if (!tflops) return fail(RFLU_ERR_ARG, "rflu_gpu_fp64_rate: null argument");
+  int dev = 0, sms = 0;
+  RFLU_CUDA(cudaGetDevice(&dev));
+  RFLU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  cudaStream_t s;
+  RFLU_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int iters = 8192, threads = 256, blocksPerSm = 8;
+  rflu::kFp64Fma<<<sms * blocksPerSm, threads, 0, s>>>(iters / 8, 1e-3);  // warm-up
+  cudaEventRecord(e0, s);
+  rflu::kFp64Fma<<<sms * blocksPerSm, threads, 0, s>>>(iters, 1e-3);
+  cudaEventRecord(e1, s);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  if (err != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("rflu_gpu_fp64_rate: ") + cudaGetErrorString(err));
+  const double flops = 2.0 * 8.0 * iters * (double)threads * sms * blocksPerSm;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return RFLU_OK;
 }
 
 int rflu_gpu_residual_static(rflu_gpu_ctx *ctx, const double *cvDev, double *rhsDev) {

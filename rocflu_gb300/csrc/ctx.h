@@ -26,6 +26,9 @@ struct Params {
   int spaceOrder, spaceDiscr, reconst, rkScheme, piclBuild, precision;
   double refCp, refGamma;     // global%refCp, global%refGamma (flux routines)
   double gvCp, gvMol;         // gv(GV_MIXT_CP), gv(GV_MIXT_MOL) = 8314.3/R
+  double gcR, gRT, igcR;      // 8314.3/gvMol, gvCp/(gvCp-gcR), 1/gcR (computed once on the host)
+  // FP32 copies for the mixed-mode flux arithmetic (no per-face conversions)
+  float refCpF, refGammaF, epsEntrF, dissFactF, gvCpF, gvMolF;
   double epsEntr, dissFact;
   double cfl, dtImposed, dtMinLimit;
   int nrkSteps;

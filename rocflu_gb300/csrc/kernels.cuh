@@ -30,14 +30,21 @@ inline int blocks(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 // primitive velocity directly.
 template <typename R> struct Ref { static constexpr bool on = false; };
 template <> struct Ref<double> { static constexpr bool on = true; };
+// Resident blocks requested from the register allocator: the FP32 gather
+// kernels are latency-bound and need the occupancy; the FP64 ones are
+// FP64-pipe-bound and keep their registers.
+template <typename R> struct MinBlocks { static constexpr int v = 1; };
+template <> struct MinBlocks<float> { static constexpr int v = 4; };
+template <typename R> struct MinBlocksFlux { static constexpr int v = 1; };
+template <> struct MinBlocksFlux<float> { static constexpr int v = 3; };
 
 // ---------------------------------------------------------------------------
 // Dependent variables of one cell from cv: RFLU_SetDependentVars, TCPERF
 // (libflu/RFLU_SetDependentVars.F90:254-287), always in FP64.
 // ---------------------------------------------------------------------------
 __device__ inline void dependentVars(const Params &p, const double *cv, double &pres, double &temp, double &snd) {
-  double gc = 8314.3 / p.gvMol;
-  double g = p.gvCp / (p.gvCp - gc);
+  const double gc = p.gcR;  // MixtPerf_R_M(gv(GV_MIXT_MOL)), computed once
+  const double g = p.gRT;   // MixtPerf_G_CpR(gv(GV_MIXT_CP), gc)
   double r = cv[0];
   double ir = 1.0 / r;
   double Eo = ir * cv[4];
@@ -118,6 +125,7 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = S(0);
   const int sb = V.stOff[i], se = V.stOff[i + 1];
+#pragma unroll 2
   for (int s = sb; s < se; ++s) {
     const int j = V.stIdx[s];
     const S wx = S(V.wx[s]), wy = S(V.wy[s]), wz = S(V.wz[s]);
@@ -284,7 +292,7 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
 }
 
 template <typename R>
-__global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
+__global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimit(View<R> V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   R g[15];
@@ -292,6 +300,71 @@ __global__ void __launch_bounds__(kBlock) kGradLimit(View<R> V) {
   const size_t n = V.nc;
 #pragma unroll
   for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
+}
+
+// Block minimum of a per-thread dt (warp shuffles, then one warp over the
+// warp minima) folded into one atomicMin on the bit pattern of the positive
+// double (IEEE order of positive doubles = order of their bit patterns).
+__device__ inline void blockMinDt(Scalars *sc, double dt) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dt = fmin(dt, __shfl_xor_sync(0xffffffffu, dt, o));
+  __shared__ double wmin[kBlock / 32];
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = dt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = wmin[0];
+    for (int w = 1; w < kBlock / 32; ++w) m = fmin(m, wmin[w]);
+    if (m > 0.0) atomicMin(&sc->dtBits, (unsigned long long)__double_as_longlong(m));
+    else atomicMin(&sc->dtBits, 0ull);
+  }
+}
+
+// RFLU_TimeStepInviscid's per-cell spectral-radius sum in FP32 from the
+// primitive state (mixed mode; the sound speed from the FP64-recovered p).
+template <typename R>
+__device__ inline double cellDtPrim(const View<R> &V, int i) {
+  const size_t n = V.nc;
+  const float g = (float)V.p.refGamma;
+  const float ri = (float)V.prim[i];
+  const float ui = (float)V.prim[n + i], vi = (float)V.prim[2 * n + i], wi = (float)V.prim[3 * n + i];
+  const float ai = sqrtf(g * (float)V.prim[4 * n + i] / ri);
+  float sum = 0.f;
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  for (int e = cb; e < ce; ++e) {
+    const int code = V.cfEnt[e];
+    if (code >= 0) {
+      const int f = code >> 1, nb = (code & 1) ? V.fc1[f] : V.fc2[f];
+      const float rj = (float)V.prim[nb];
+      const float uj = (float)V.prim[n + nb], vj = (float)V.prim[2 * n + nb], wj = (float)V.prim[3 * n + nb];
+      const float aj = sqrtf(g * (float)V.prim[4 * n + nb] / rj);
+      const float vc = 0.5f * ((ui + uj) * (float)V.fnx[f] + (vi + vj) * (float)V.fny[f] + (wi + wj) * (float)V.fnz[f]);
+      sum += (fabsf(vc) + 0.5f * (ai + aj)) * (float)V.fnm[f];
+    } else {
+      const int b = -code - 1;
+      const float vc = ui * (float)V.bnx[b] + vi * (float)V.bny[b] + wi * (float)V.bnz[b];
+      sum += (fabsf(vc) + ai) * (float)V.bnm[b];
+    }
+  }
+  return V.vol[i] / (double)sum;
+}
+
+// First stage of a mixed-mode step: gradient + limiter and the time-step
+// reduction in one pass over the cell's neighbours.
+template <typename R>
+__global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double dt = 1.79769313486231571e308;
+  if (i < V.nc && V.sc->finished >= 0) {
+    if (V.p.spaceOrder > 1) {
+      R g[15];
+      gradLimitCell(V, PlainLoad<R>{V}, i, g);
+      const size_t n = V.nc;
+#pragma unroll
+      for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
+    }
+    dt = cellDtPrim(V, i);
+  }
+  blockMinDt(V.sc, dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -321,15 +394,19 @@ __device__ inline void faceState(const View<R> &V, const L &ld, int c, typename 
   irCell = ir;
 }
 
+// A numerics parameter in the arithmetic type S (the FP32 copy in the mixed mode).
+template <typename S> __device__ inline S prm(double d, float) { return S(d); }
+template <> __device__ inline float prm<float>(double, float f) { return f; }
+
 template <typename S>
 __device__ inline void riemann2(const Params &P, S nx, S ny, S nz, S nm, const S *L, S irl, const S *Rt, S irr, S *flx) {
-  const S cp = S(P.refCp), g = S(P.refGamma);
+  const S cp = prm<S>(P.refCp, P.refCpF), g = prm<S>(P.refGamma, P.refGammaF);
   if (P.spaceDiscr == 1) {
     S gc = cp - cp / g;
     S tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
     S Hl = perfHo(cp, tl, L[1], L[2], L[3]), Hr = perfHo(cp, tr, Rt[1], Rt[2], Rt[3]);
-    roeFlux(g, S(P.epsEntr), S(P.dissFact), nx, ny, nz, nm, L[0], L[1], L[2], L[3], L[4], Hl, Rt[0], Rt[1], Rt[2],
-            Rt[3], Rt[4], Hr, flx);
+    roeFlux(g, prm<S>(P.epsEntr, P.epsEntrF), prm<S>(P.dissFact, P.dissFactF), nx, ny, nz, nm, L[0], L[1], L[2], L[3],
+            L[4], Hl, Rt[0], Rt[1], Rt[2], Rt[3], Rt[4], Hr, flx);
   } else if (P.spaceDiscr == 3) {
     S el = perfEo(L[0], g, L[4], L[1], L[2], L[3]), al = sqrt_(g * L[4] / L[0]);
     S er = perfEo(Rt[0], g, Rt[4], Rt[1], Rt[2], Rt[3]), ar = sqrt_(g * Rt[4] / Rt[0]);
@@ -414,7 +491,7 @@ __device__ inline void patch2(const Params &P, int type, int outflowType, double
     flx[3] = L[4] * nz * nm;
     flx[4] = L[4] * S(0) * nm;
   } else {
-    const S cp = S(P.gvCp), mol = S(P.gvMol);
+    const S cp = prm<S>(P.gvCp, P.gvCpF), mol = prm<S>(P.gvMol, P.gvMolF);
     S rgas = S(8314.3) / mol;
     S g = cp / (cp - rgas);
     S rul = L[0] * L[1], rvl = L[0] * L[2], rwl = L[0] * L[3];
@@ -473,7 +550,7 @@ __device__ inline void faceFluxEval(const View<R> &V, const L &ld, int t, typena
 
 // One thread per face: interior faces [0,nf), then boundary faces.
 template <typename R>
-__global__ void __launch_bounds__(kBlock) kFaceFlux(View<R> V) {
+__global__ void __launch_bounds__(kBlock, MinBlocksFlux<R>::v) kFaceFlux(View<R> V) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nfT = V.nf + V.nb;
   if (t >= nfT) return;
@@ -537,7 +614,7 @@ __device__ inline void afterUpdate(const View<R> &V, int i, double *cv, double &
       atomicMin(&V.sc->firstBadCell, V.refId[i] + 1);
     }
   }
-  const double rgas = 8314.3 / P.gvMol, gamma = P.gvCp / (P.gvCp - rgas);
+  const double gamma = P.gRT;
   {
     double r = cv[0], ir = 1.0 / r;
     double u = ir * cv[1], v = ir * cv[2], w = ir * cv[3];
@@ -595,6 +672,39 @@ __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, c
     }
   }
   double pr, tp, cs;
+  if (!Ref<R>::on) {
+    // Mixed mode: RFLU_SetDependentVars and AfterUpdateMP with one
+    // reciprocal and one square root per cell, all in FP64.  A cell with
+    // p <= 0 gets the energy floor of RFLU_CheckPositivity (which also
+    // overrides the tiny-pressure clamp of RFLU_EnforceBounds).
+    const double ir = 1.0 / cv[0];
+    const double u = ir * cv[1], v = ir * cv[2], w = ir * cv[3];
+    const double ke = 0.5 * (cv[1] * u + cv[2] * v + cv[3] * w);
+    pr = (P.gRT - 1.0) * (cv[4] - ke);
+    if (isnan(cv[0]) || isnan(u) || isnan(v) || isnan(w) || isnan(pr)) {
+      atomicAdd(&V.sc->nanCells, 1ull);
+      atomicMin(&V.sc->firstBadCell, V.refId[i] + 1);
+    }
+    if (pr <= 0.0) {
+      if (fabs(pr) <= 1.0e-12) atomicAdd(&V.sc->negPCells, 1ull);
+      atomicAdd(&V.sc->posFixCells, 1ull);
+      cv[4] = 1.0e4 * cv[0] + ke;
+      pr = (P.gRT - 1.0) * (cv[4] - ke);
+    }
+    tp = pr * ir * P.igcR;
+    cs = sqrt(P.gRT * pr * ir);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) V.cv[k * n + i] = cv[k];
+    V.dv[i] = pr;
+    V.dv[n + i] = tp;
+    V.dv[2 * n + i] = cs;
+    V.prim[i] = (R)cv[0];
+    V.prim[n + i] = (R)u;
+    V.prim[2 * n + i] = (R)v;
+    V.prim[3 * n + i] = (R)w;
+    V.prim[4 * n + i] = (R)pr;
+    return;
+  }
   dependentVars(P, cv, pr, tp, cs);
   afterUpdate(V, i, cv, pr, tp, cs);
 #pragma unroll
@@ -641,17 +751,7 @@ __global__ void __launch_bounds__(kBlock) kCellDt(View<R> V) {
     }
     dt = V.vol[i] / sum;
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) dt = fmin(dt, __shfl_xor_sync(0xffffffffu, dt, o));
-  __shared__ double wmin[kBlock / 32];
-  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = dt;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double m = wmin[0];
-    for (int w = 1; w < kBlock / 32; ++w) m = fmin(m, wmin[w]);
-    if (m > 0.0) atomicMin(&V.sc->dtBits, (unsigned long long)__double_as_longlong(m));
-    else atomicMin(&V.sc->dtBits, 0ull);
-  }
+  blockMinDt(V.sc, dt);
 }
 
 // RFLU_MinimumTimeStep (rocflu/RFLU_MinimumTimeStep.F90:100-245) and the
@@ -716,6 +816,20 @@ struct Launch {
     kStepBegin<R><<<1, 1, 0, s>>>(V);
     kCellDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
     kDtFinalize<R><<<1, 1, 0, s>>>(V);
+  }
+  // Time-step reduction + gradients of the first stage of a step.  The FP64
+  // modes keep the reference's separate FP64 sweep (bit-exact dt); the mixed
+  // mode folds an FP32 sweep into the gradient kernel, which gathers the
+  // same neighbours.
+  static void stepStart(const View<R> &V, cudaStream_t s) {
+    if (Ref<R>::on) {
+      timestep(V, s);
+      gradLimit(V, s);
+    } else {
+      kStepBegin<R><<<1, 1, 0, s>>>(V);
+      kGradLimitDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+      kDtFinalize<R><<<1, 1, 0, s>>>(V);
+    }
   }
   static void stepEnd(const View<R> &V, cudaStream_t s) { kStepEnd<R><<<1, 1, 0, s>>>(V); }
 };

@@ -1,5 +1,6 @@
 // Kernel instantiation of the fp64 mode: FP64, fused multiply-add allowed (-fmad=true).
 #define RFLU_NS fp64
+#define RFLU_WITH_ADJOINT 1
 #include "kernels.cuh"
 #include "adjoint.cuh"
 #include "ops.h"
@@ -8,7 +9,7 @@ namespace rflu {
 const Ops<double> *opsFp64() {
   using L = fp64::Launch<double>;
   static const Ops<double> ops = {L::initState, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
-                                 L::timestep,  L::stepEnd,   fp64::AdjointOps<double>::jvp, fp64::AdjointOps<double>::vjp,
+                                 L::timestep,  L::stepEnd,   L::stepStart, fp64::AdjointOps<double>::jvp, fp64::AdjointOps<double>::vjp,
                                  fp64::AdjointOps<double>::patchPressure};
   return &ops;
 }

@@ -1,5 +1,6 @@
 // Kernel instantiation of the fp64x mode: FP64 in the reference's evaluation order without FMA contraction (-fmad=false): bit-exact with the CPU restatement.
 #define RFLU_NS fp64x
+#define RFLU_WITH_ADJOINT 1
 #include "kernels.cuh"
 #include "adjoint.cuh"
 #include "ops.h"
@@ -8,7 +9,7 @@ namespace rflu {
 const Ops<double> *opsFp64Exact() {
   using L = fp64x::Launch<double>;
   static const Ops<double> ops = {L::initState, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
-                                 L::timestep,  L::stepEnd,   fp64x::AdjointOps<double>::jvp, fp64x::AdjointOps<double>::vjp,
+                                 L::timestep,  L::stepEnd,   L::stepStart, fp64x::AdjointOps<double>::jvp, fp64x::AdjointOps<double>::vjp,
                                  fp64x::AdjointOps<double>::patchPressure};
   return &ops;
 }

@@ -68,7 +68,8 @@ class RfluError(RuntimeError):
 EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_gpu_stream",
            "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
            "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_residual", "rflu_gpu_vjp",
-           "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static", "rflu_setup_build", "rflu_setup_grid",
+           "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
+           "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_setup_build", "rflu_setup_grid",
            "rflu_setup_destroy")
 
 
@@ -108,6 +109,8 @@ def lib(build_if_missing=True):
     L.rflu_gpu_status.argtypes = [P, C.POINTER(Status)]
     L.rflu_gpu_kernel_times.argtypes = [P, I, DP]
     L.rflu_gpu_residual_static.argtypes = [P, P, P]
+    L.rflu_gpu_adjoint_times.argtypes = [P, I, DP]
+    L.rflu_gpu_fp64_rate.argtypes = [DP]
     L.rflu_setup_build.argtypes = [C.POINTER(MeshDesc), I, C.POINTER(P)]
     L.rflu_setup_grid.argtypes = [P, C.POINTER(GridDesc)]
     L.rflu_setup_destroy.argtypes = [P]
@@ -303,6 +306,12 @@ class Region:
         _check(lib().rflu_gpu_kernel_times(self.h, n_iter, _p(ms)))
         return ms
 
+    def adjoint_times(self, n_iter=5):
+        """Mean ms of one primal residual and of one VJP on the device state."""
+        ms = np.zeros(2)
+        _check(lib().rflu_gpu_adjoint_times(self.h, n_iter, _p(ms)))
+        return ms
+
     def residual_static(self, cv_dev_ptr, rhs_dev_ptr):
         """rflu_gpu_residual_static on device buffers (integer device
         addresses of cv(5,nCells) and rhs(5,nCells) in reference order)."""
@@ -312,6 +321,13 @@ class Region:
         s = Status()
         _check(lib().rflu_gpu_status(self.h, C.byref(s)))
         return {f: getattr(s, f) for f, _ in Status._fields_}
+
+
+def fp64_rate():
+    """Measured FP64 FMA rate of the current GPU in TFLOP/s."""
+    t = C.c_double()
+    _check(lib().rflu_gpu_fp64_rate(C.byref(t)))
+    return t.value
 
 
 # --- the reference's subroutine names ---------------------------------------
