@@ -56,7 +56,10 @@ def build(verbose=False, force=False):
                                             os.path.join(OUT, "kernels_fp64.o")],
         "kernels_fp64x.o": [nvcc] + common + ["-fmad=false", "-c", os.path.join(SRC, "kernels_fp64x.cu"), "-o",
                                              os.path.join(OUT, "kernels_fp64x.o")],
-        "kernels_mixed.o": [nvcc] + common + ["-fmad=true", "-c", os.path.join(SRC, "kernels_mixed.cu"), "-o",
+        # FP32 division and square root at full throughput (within 2 ulp)
+        # in the mixed mode; its FP64 parts are IEEE regardless
+        "kernels_mixed.o": [nvcc] + common + ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-c",
+                                             os.path.join(SRC, "kernels_mixed.cu"), "-o",
                                              os.path.join(OUT, "kernels_mixed.o")],
     }
     if verbose:
