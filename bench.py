@@ -56,6 +56,7 @@ def parse():
     p.add_argument("--precisions", default="mixed,fp64", help="device paths to time (profiling runs time one)")
     p.add_argument("--skip-adjoint", action="store_true")
     p.add_argument("--adj-n", type=int, default=32, help="hexes per side of the tet adjoint case")
+    p.add_argument("--only-adjoint", action="store_true", help="time the adjoint case only")
     return p.parse_args()
 
 
@@ -177,6 +178,16 @@ def run_ours(args):
 
             dist.barrier()
         torch.cuda.synchronize()
+
+    if args.only_adjoint:
+        # the adjoint section alone (profiling runs of the adjoint kernels)
+        ac = cases.adjoint_tets(args.adj_n)
+        areg = gpu.Region(ac, "fp64")
+        at = areg.adjoint_times(3)
+        if rank == 0:
+            print(json.dumps({"partial": True, "adjoint": {"primal_residual_ms": at[0], "vjp_ms": at[1],
+                                                           "vjp_over_primal": at[1] / at[0]}}))
+        return
 
     case = cases.shock_sphere(args.n)
     t0 = time.time()

@@ -65,6 +65,22 @@ def lib():
         L.orc_run.restype = C.c_int
         L.orc_run.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.c_double]
         L.orc_run_fixed_dt.argtypes = [P, C.c_int, C.c_double]
+        # every handle and array crosses as a full 64-bit pointer
+        DP, IP, LLP = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_longlong)
+        L.orc_get_faces.argtypes = [P, IP, IP, DP, DP]
+        L.orc_get_cells.argtypes = [P, DP, DP]
+        L.orc_get_patch.argtypes = [P, C.c_int, IP, DP, DP]
+        L.orc_get_stencil.argtypes = [P, IP, IP, DP]
+        L.orc_set_state.argtypes = [P, DP]
+        L.orc_get_state.argtypes = [P, DP, DP]
+        L.orc_get_rhs.argtypes = [P, DP]
+        L.orc_get_grad.argtypes = [P, DP]
+        L.orc_residual.argtypes = [P, DP, DP]
+        L.orc_counters.argtypes = [P, LLP, LLP, LLP]
+        for name in ("orc_get_faces", "orc_get_cells", "orc_get_patch", "orc_get_stencil", "orc_set_state",
+                     "orc_get_state", "orc_get_rhs", "orc_get_grad", "orc_residual", "orc_counters",
+                     "orc_rk_stage", "orc_run_fixed_dt", "orc_destroy"):
+            getattr(L, name).restype = None
         _LIB = L
     return _LIB
 

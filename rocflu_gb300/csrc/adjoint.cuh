@@ -25,6 +25,7 @@
 // eigen-frame velocity limiter of RECONST 10 is covered by the tangent only.
 #pragma once
 #include "dual.cuh"
+#include "roe_adjoint.cuh"
 
 namespace rflu {
 namespace RFLU_NS {
@@ -316,6 +317,14 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<double> V, AdjWork W) {
       double L[5], Rt[5], irl, irr;
       faceState(V, ld, c1, V.dL[f], V.dL[nf + f], V.dL[2 * nf + f], L, irl);
       faceState(V, ld, c2, V.dR[f], V.dR[nf + f], V.dR[2 * nf + f], Rt, irr);
+      if (P.spaceDiscr == 1) {
+        // Roe: hand-written reverse sweep (no dependence on the cell 1/rho)
+        roe2Adjoint(P.refGamma, P.refCp, P.epsEntr, P.dissFact, V.fnx[f], V.fny[f], V.fnz[f], V.fnm[f], L, Rt, fbar,
+                    out, out + 6);
+        out[5] = 0.0;
+        out[11] = 0.0;
+        return;
+      }
       D6 a[5], b[5], ia, ib, flx[5];
       for (int side = 0; side < 2; ++side) {
 #pragma unroll

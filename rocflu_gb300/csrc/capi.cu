@@ -654,24 +654,6 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   }
   std::vector<double> vol(nc);
   for (int i = 0; i < nc; ++i) vol[i] = g->vol[refId[i]];
-  // member-major (ELL) copies of the stencils and of the cell -> face lists
-  int stMax = 0, cfMax = 0;
-  for (int i = 0; i < nc; ++i) {
-    stMax = std::max(stMax, stOff[i + 1] - stOff[i]);
-    cfMax = std::max(cfMax, cfOff[i + 1] - cfOff[i]);
-  }
-  std::vector<int> stIdxE((size_t)stMax * nc, -1), cfEntE((size_t)cfMax * nc, INT_MIN);
-  std::vector<double> wxE((size_t)stMax * nc, 0.0), wyE((size_t)stMax * nc, 0.0), wzE((size_t)stMax * nc, 0.0);
-  for (int i = 0; i < nc; ++i) {
-    for (int s = 0; s < stOff[i + 1] - stOff[i]; ++s) {
-      const size_t o = (size_t)s * nc + i;
-      stIdxE[o] = stIdx[stOff[i] + s];
-      wxE[o] = wx[stOff[i] + s];
-      wyE[o] = wy[stOff[i] + s];
-      wzE[o] = wz[stOff[i] + s];
-    }
-    for (int e = 0; e < cfOff[i + 1] - cfOff[i]; ++e) cfEntE[(size_t)e * nc + i] = cfEnt[cfOff[i] + e];
-  }
   // transposed stencil for the adjoint of the LSQ gradient (FP64 modes)
   std::vector<int> tsOff(nc + 1, 0), tsCell(stIdx.size()), tsEnt(stIdx.size());
   for (size_t s = 0; s < stIdx.size(); ++s) tsOff[stIdx[s] + 1]++;
@@ -703,10 +685,6 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
   PUT(V.vol, vol, double); PUT(V.epsq, epsq, R);
   PUT(V.refId, refId, int);
-  V.stMax = stMax;
-  V.cfMax = cfMax;
-  PUT(V.stIdxE, stIdxE, int); PUT(V.cfEntE, cfEntE, int);
-  PUT(V.wxE, wxE, R); PUT(V.wyE, wyE, R); PUT(V.wzE, wzE, R);
   if (num->precision != RFLU_PREC_MIXED) {
     PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
   }

@@ -55,15 +55,6 @@ struct View {
   // C2C stencil CSR and per-member least-squares weights
   const int *stOff, *stIdx;
   const R *wx, *wy, *wz;
-  // the same stencils member-major (ELL): member s of cell i at [s*nc + i],
-  // padded with -1 / zero weights up to stMax, so that a warp's loads of one
-  // member slot are one coalesced line
-  int stMax;
-  const int *stIdxE;
-  const R *wxE, *wyE, *wzE;
-  // cell -> face entries member-major as well (cfMax slots, INT_MIN padding)
-  int cfMax;
-  const int *cfEntE;
   const double *vol;
   const R *epsq;                    // Venkatakrishnan eps^2 = (vol^(1/3))^3 per cell
   const int *refId;                 // renumbered -> reference (0-based) cell id

@@ -124,13 +124,11 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
   for (int k = 0; k < 5; ++k) q[k] = ld.prim(k, i);
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = S(0);
-  const size_t nc = V.nc;
+  const int sb = V.stOff[i], se = V.stOff[i + 1];
 #pragma unroll 2
-  for (int s = 0; s < V.stMax; ++s) {
-    const size_t o = s * nc + i;
-    const int j = V.stIdxE[o];
-    if (j < 0) break;  // past the cell's last member
-    const S wx = S(V.wxE[o]), wy = S(V.wyE[o]), wz = S(V.wzE[o]);
+  for (int s = sb; s < se; ++s) {
+    const int j = V.stIdx[s];
+    const S wx = S(V.wx[s]), wy = S(V.wy[s]), wz = S(V.wz[s]);
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       S d = ld.prim(k, j) - q[k];
@@ -140,14 +138,14 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
     }
   }
   const int rc = V.p.reconst;
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
   if (rc == 10 || rc == 100 || rc == 11) {
     // scalar limiters: min/max over face neighbours, then per face side
     S vmin[5], vmax[5], lim[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; lim[k] = S(1); }
-    for (int e = 0; e < V.cfMax; ++e) {
-      const int code = V.cfEntE[(size_t)e * V.nc + i];
-      if (code == INT_MIN) break;  // past the cell's last entry
+    for (int e = cb; e < ce; ++e) {
+      const int code = V.cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
       const int nb = (code & 1) ? V.fc1[f] : V.fc2[f];
@@ -159,9 +157,8 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       }
     }
     S epsq = (rc == 11) ? S(V.epsq[i]) : S(0);
-    for (int e = 0; e < V.cfMax; ++e) {
-      const int code = V.cfEntE[(size_t)e * V.nc + i];
-      if (code == INT_MIN) break;  // past the cell's last entry
+    for (int e = cb; e < ce; ++e) {
+      const int code = V.cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
       const R *d = (code & 1) ? V.dR : V.dL;
@@ -202,9 +199,8 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         for (int b = 0; b < 3; ++b) Sy[a + 3 * b] = S(0.5) * (G[a + 3 * b] + G[b + 3 * a]);
       symmetricEigen3(Sy, A, ev);
       S dmn[3] = {S(0), S(0), S(0)}, dmx[3] = {S(0), S(0), S(0)}, al[3] = {S(1), S(1), S(1)};
-      for (int e = 0; e < V.cfMax; ++e) {
-        const int code = V.cfEntE[(size_t)e * V.nc + i];
-      if (code == INT_MIN) break;  // past the cell's last entry
+      for (int e = cb; e < ce; ++e) {
+        const int code = V.cfEnt[e];
         if (code < 0) continue;
         const int f = code >> 1, side = code & 1;
         const int c1 = V.fc1[f], c2 = V.fc2[f];
@@ -222,9 +218,8 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
           dmx[j] = fmax2(dmx[j], pr);
         }
       }
-      for (int e = 0; e < V.cfMax; ++e) {
-        const int code = V.cfEntE[(size_t)e * V.nc + i];
-      if (code == INT_MIN) break;  // past the cell's last entry
+      for (int e = cb; e < ce; ++e) {
+        const int code = V.cfEnt[e];
         if (code < 0) continue;
         const int f = code >> 1;
         const R *d = (code & 1) ? V.dR : V.dL;
@@ -334,9 +329,9 @@ __device__ inline double cellDtPrim(const View<R> &V, int i) {
   const float ui = (float)V.prim[n + i], vi = (float)V.prim[2 * n + i], wi = (float)V.prim[3 * n + i];
   const float ai = sqrtf(g * (float)V.prim[4 * n + i] / ri);
   float sum = 0.f;
-  for (int e = 0; e < V.cfMax; ++e) {
-    const int code = V.cfEntE[(size_t)e * V.nc + i];
-      if (code == INT_MIN) break;  // past the cell's last entry
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  for (int e = cb; e < ce; ++e) {
+    const int code = V.cfEnt[e];
     if (code >= 0) {
       const int f = code >> 1, nb = (code & 1) ? V.fc1[f] : V.fc2[f];
       const float rj = (float)V.prim[nb];
@@ -575,9 +570,9 @@ __device__ inline void gatherRhs(const View<R> &V, const T *flux, int i, T *rhs)
   const size_t nT = (size_t)V.nf + V.nb;
 #pragma unroll
   for (int k = 0; k < 5; ++k) rhs[k] = -T(0);
-  for (int e = 0; e < V.cfMax; ++e) {
-    const int code = V.cfEntE[(size_t)e * V.nc + i];
-      if (code == INT_MIN) break;  // past the cell's last entry
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  for (int e = cb; e < ce; ++e) {
+    const int code = V.cfEnt[e];
     if (code >= 0) {
       const int f = code >> 1;
       if (code & 1) {
@@ -732,9 +727,9 @@ __global__ void __launch_bounds__(kBlock) kCellDt(View<R> V) {
   if (i < V.nc) {
     const size_t n = V.nc;
     double sum = 0.0;
-      for (int e = 0; e < V.cfMax; ++e) {
-      const int code = V.cfEntE[(size_t)e * V.nc + i];
-      if (code == INT_MIN) break;  // past the cell's last entry
+    const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+    for (int e = cb; e < ce; ++e) {
+      const int code = V.cfEnt[e];
       if (code >= 0) {
         const int f = code >> 1, c1 = V.fc1[f], c2 = V.fc2[f];
         const double nx = V.fnx[f], ny = V.fny[f], nz = V.fnz[f], nm = V.fnm[f];
