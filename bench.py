@@ -145,7 +145,8 @@ def algorithmic_bytes(region, precision):
     """Bytes per launch of the three stage kernels and of the whole stage,
     counted from the data each kernel must move once (neighbour gathers
     counted once, ideal reuse), with the per-cell terms of the two-kernel
-    minimum: state, gradients, R-factor weights, stencil ids, face
+    minimum: state, gradients, LSQ weights (FP64) or R-factor coefficients
+    and centroids (mixed), stencil ids, face
     geometry/connectivity."""
     g = region.grid
     nc = region.n_cells
@@ -153,7 +154,11 @@ def algorithmic_bytes(region, precision):
     nb = g.bf2c.shape[0]
     S = len(g.c2cs)
     r = 4 if precision == "mixed" else 8
-    grad_limit = nc * (5 * r + 15 * r + 4) + S * (4 + 3 * r) + nf * 2 * (8 + 3 * r)
+    if precision == "mixed":
+        # weights formed on the fly: R-factor coefficients and centroids per cell
+        grad_limit = nc * (5 * r + 15 * r + 4 + 6 * r + 3 * r) + S * 4 + nf * 2 * (8 + 3 * r)
+    else:
+        grad_limit = nc * (5 * r + 15 * r + 4) + S * (4 + 3 * r) + nf * 2 * (8 + 3 * r)
     face_flux = nc * (5 * r + 15 * r) + (nf + nb) * (4 * r + 3 * r + 5 * r) + nf * 8
     gather_update = nc * (40 + 40 + 24 + 5 * 2 * r + 5 * r + 8 + 8) + 2 * nf * 5 * r + (2 * nf + nb) * 4
     return {"gradLimit": grad_limit, "faceFlux": face_flux, "gatherUpdate": gather_update}
@@ -314,7 +319,10 @@ def run_ours(args):
                        "faces": int(setup.f2c.shape[0]), "stages_per_step": 3, "flux": "HLLC", "limiter": "BJ (RECONST 10)",
                        "parallelism": "replicas" if ws > 1 else "single", "l2": "working set > L2 (no flush)",
                        "setup_s": setup_s},
-            "gpu_launches": 13 * args.steps,
+            # mixed step graph: step begin, gradient+dt, dt finalize, face flux and
+            # gather-update of stage 1, three kernels per later stage, step end;
+            # plus the one scalar-setting kernel of the step call
+            "gpu_launches": 12 * args.steps + 1,
             "fp64": fp64,
             "adjoint": adjoint,
             "e2e": e2e,

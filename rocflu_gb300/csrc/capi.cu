@@ -617,7 +617,9 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   // RFLU_ModDifferentiationCells.F90:983-1044) from the R factor and the
   // unit offset, in FP64 and in the reference's order of operations
   std::vector<int> stOff(nc + 1, 0), stIdx;
-  std::vector<double> wx, wy, wz, epsq(nc, 0.0);
+  std::vector<double> wx, wy, wz, epsq(nc, 0.0), rcf;
+  const bool mixed = num->precision == RFLU_PREC_MIXED;
+  if (mixed && num->spaceOrder > 1) rcf.resize(6 * (size_t)nc);
   if (num->spaceOrder > 1) {
     if (!g->c2csOff || !g->c2csMembs || !g->xyzMoms) return fail(RFLU_ERR_ARG, "rflu_gpu_create: ORDER 2 needs stencils");
     for (int i = 0; i < nc; ++i) {
@@ -629,6 +631,10 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
       const double c13 = -(c11 * r13 + c12 * c22 * r23);
       const double c23 = -c22 * r23;
       const double c1111 = c11 * c11, c2222 = c22 * c22, c3333 = c33 * c33;
+      if (mixed) {
+        rcf[i] = c1111; rcf[(size_t)nc + i] = c2222; rcf[2 * (size_t)nc + i] = c3333;
+        rcf[3 * (size_t)nc + i] = c12; rcf[4 * (size_t)nc + i] = c13; rcf[5 * (size_t)nc + i] = c23;
+      }
       const double *xi = g->cofg + 3 * (size_t)o;
       for (int e = g->c2csOff[o]; e < g->c2csOff[o + 1]; ++e) {
         const int j = g->c2csMembs[e] - 1;
@@ -640,9 +646,11 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
         const double t1 = c1111 * (dx);
         const double t2 = c2222 * (dy + c12 * dx);
         const double t3 = c3333 * (dz + c23 * dy + c13 * dx);
-        wx.push_back(term * (t1 + c12 * t2 + c13 * t3));
-        wy.push_back(term * (t2 + c23 * t3));
-        wz.push_back(term * (t3));
+        if (!mixed) {
+          wx.push_back(term * (t1 + c12 * t2 + c13 * t3));
+          wy.push_back(term * (t2 + c23 * t3));
+          wz.push_back(term * (t3));
+        }
         stIdx.push_back(newId[j]);
       }
       stOff[i + 1] = (int)stIdx.size();
@@ -652,8 +660,14 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
       epsq[i] = (1.0 * ds) * (1.0 * ds) * (1.0 * ds);
     }
   }
-  std::vector<double> vol(nc);
-  for (int i = 0; i < nc; ++i) vol[i] = g->vol[refId[i]];
+  std::vector<double> vol(nc), ivol(nc), cgx(nc), cgy(nc), cgz(nc);
+  for (int i = 0; i < nc; ++i) {
+    vol[i] = g->vol[refId[i]];
+    ivol[i] = 1.0 / vol[i];
+    cgx[i] = g->cofg[3 * (size_t)refId[i]];
+    cgy[i] = g->cofg[3 * (size_t)refId[i] + 1];
+    cgz[i] = g->cofg[3 * (size_t)refId[i] + 2];
+  }
   // transposed stencil for the adjoint of the LSQ gradient (FP64 modes)
   std::vector<int> tsOff(nc + 1, 0), tsCell(stIdx.size()), tsEnt(stIdx.size());
   for (size_t s = 0; s < stIdx.size(); ++s) tsOff[stIdx[s] + 1]++;
@@ -682,10 +696,14 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   PUT(V.patchPout, pP, double);
   PUT(V.cfOff, cfOff, int); PUT(V.cfEnt, cfEnt, int);
   PUT(V.stOff, stOff, int); PUT(V.stIdx, stIdx, int);
-  PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
   PUT(V.vol, vol, double); PUT(V.epsq, epsq, R);
   PUT(V.refId, refId, int);
-  if (num->precision != RFLU_PREC_MIXED) {
+  if (mixed) {
+    // weights formed in the gradient kernel from the R factor and centroids
+    PUT(V.cgx, cgx, R); PUT(V.cgy, cgy, R); PUT(V.cgz, cgz, R);
+    PUT(V.rcf, rcf, R); PUT(V.ivol, ivol, R);
+  } else {
+    PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
     PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
   }
 #undef PUT

@@ -57,6 +57,12 @@ struct View {
   const R *wx, *wy, *wz;
   const double *vol;
   const R *epsq;                    // Venkatakrishnan eps^2 = (vol^(1/3))^3 per cell
+  // mixed mode: LSQ weights are formed on the fly from the cell's R-factor
+  // coefficients (c1111, c2222, c3333, c12, c13, c23) and the members'
+  // centroids, instead of streaming three weights per stencil member
+  const R *cgx, *cgy, *cgz;         // cell centroids (FP32)
+  const R *rcf;                     // (6, nc) R-factor coefficients
+  const R *ivol;                    // 1/vol (FP32), for the FP32 RK increment
   const int *refId;                 // renumbered -> reference (0-based) cell id
   // transposed stencil (FP64 modes): for cell j, the (cell i, entry s) pairs
   // of the stencils that contain j, for the adjoint of the LSQ gradient

@@ -125,16 +125,47 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = S(0);
   const int sb = V.stOff[i], se = V.stOff[i + 1];
+  if constexpr (Ref<R>::on) {
 #pragma unroll 2
-  for (int s = sb; s < se; ++s) {
-    const int j = V.stIdx[s];
-    const S wx = S(V.wx[s]), wy = S(V.wy[s]), wz = S(V.wz[s]);
+    for (int s = sb; s < se; ++s) {
+      const int j = V.stIdx[s];
+      const S wx = S(V.wx[s]), wy = S(V.wy[s]), wz = S(V.wz[s]);
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      S d = ld.prim(k, j) - q[k];
-      g[3 * k] = g[3 * k] + wx * d;
-      g[3 * k + 1] = g[3 * k + 1] + wy * d;
-      g[3 * k + 2] = g[3 * k + 2] + wz * d;
+      for (int k = 0; k < 5; ++k) {
+        S d = ld.prim(k, j) - q[k];
+        g[3 * k] = g[3 * k] + wx * d;
+        g[3 * k + 1] = g[3 * k + 1] + wy * d;
+        g[3 * k + 2] = g[3 * k + 2] + wz * d;
+      }
+    }
+  } else {
+    // the same weights (RFLU_ComputeGradCellsFast_3D, :983-1044) formed here
+    // in FP32 from the R-factor coefficients and the member's centroid
+    const size_t n = V.nc;
+    const S c1111 = S(V.rcf[i]), c2222 = S(V.rcf[n + i]), c3333 = S(V.rcf[2 * n + i]);
+    const S c12 = S(V.rcf[3 * n + i]), c13 = S(V.rcf[4 * n + i]), c23 = S(V.rcf[5 * n + i]);
+    const S xi = S(V.cgx[i]), yi = S(V.cgy[i]), zi = S(V.cgz[i]);
+#pragma unroll 2
+    for (int s = sb; s < se; ++s) {
+      const int j = V.stIdx[s];
+      S dx = S(V.cgx[j]) - xi, dy = S(V.cgy[j]) - yi, dz = S(V.cgz[j]) - zi;
+      const S term = S(1) / sqrt_(dx * dx + dy * dy + dz * dz);
+      dx = term * dx;
+      dy = term * dy;
+      dz = term * dz;
+      const S t1 = c1111 * dx;
+      const S t2 = c2222 * (dy + c12 * dx);
+      const S t3 = c3333 * (dz + c23 * dy + c13 * dx);
+      const S wx = term * (t1 + c12 * t2 + c13 * t3);
+      const S wy = term * (t2 + c23 * t3);
+      const S wz = term * t3;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        S d = ld.prim(k, j) - q[k];
+        g[3 * k] = g[3 * k] + wx * d;
+        g[3 * k + 1] = g[3 * k + 1] + wy * d;
+        g[3 * k + 2] = g[3 * k + 2] + wz * d;
+      }
     }
   }
   const int rc = V.p.reconst;
@@ -636,6 +667,79 @@ __device__ inline void afterUpdate(const View<R> &V, int i, double *cv, double &
   }
 }
 
+// Mixed-mode RKUpdateMP + RFLU_SetVarsContWrapper + AfterUpdateMP of one cell.
+// The increment adtv*(rhs - grk*rhsSum) is formed in FP32 (the rhs is FP32)
+// and added to the FP64 master cv; p is recovered in FP64 (it is a difference
+// of two nearly equal energies at high Mach numbers).  The FP64 reciprocal of
+// rho and the sound speed start from FP32 seeds refined by one Newton-Raphson
+// step (quadratic convergence: a 2^-22 seed ends near 2^-44), so the cell
+// costs a few dozen FP64 instructions instead of two IEEE divisions and a
+// square root.  A cell with p <= 0 gets the energy floor of
+// RFLU_CheckPositivity (libflu/RFLU_CheckPositivity.F90:173-193), which also
+// overrides the tiny-pressure clamp of RFLU_EnforceBounds.
+template <typename R>
+__device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fac, float grk, const R *rhs,
+                                   double *cv) {
+  const Params &P = V.p;
+  const size_t n = V.nc;
+  const float adtv = fac * (float)V.ivol[i];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const float r = (float)rhs[k];
+    R *rs = &V.rhsSum[k * n + i];
+    float inc;
+    switch (P.rkScheme) {
+      case 1:
+        if (iStage == 1) { inc = adtv * r; *rs = r; }
+        else if (iStage == P.nrkSteps) inc = adtv * (r + (float)*rs);
+        else { inc = adtv * r; *rs = (float)*rs + grk * r; }
+        break;
+      case 2:
+        if (iStage == 1) { inc = adtv * r; *rs = r; }
+        else if (iStage == 2) { inc = adtv * (r - grk * (float)*rs); *rs = r; }
+        else inc = adtv * (r - grk * (float)*rs);
+        break;
+      default:
+        inc = adtv * r;
+    }
+    cv[k] = cv[k] - (double)inc;
+  }
+  // 1/rho: FP32 seed y, then y + y*(1 - rho*y)
+  double ir = (double)(1.0f / (float)cv[0]);
+  ir = fma(ir, fma(-cv[0], ir, 1.0), ir);
+  const double msq = cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3];
+  double ke = 0.5 * msq * ir;
+  double pr = (P.gRT - 1.0) * (cv[4] - ke);
+  const float irf = (float)ir;
+  const float rf = (float)cv[0];
+  const float uf = (float)cv[1] * irf, vf = (float)cv[2] * irf, wf = (float)cv[3] * irf;
+  if (isnan(rf) || isnan(uf) || isnan(vf) || isnan(wf) || isnan((float)pr)) {
+    atomicAdd(&V.sc->nanCells, 1ull);
+    atomicMin(&V.sc->firstBadCell, V.refId[i] + 1);
+  }
+  if (pr <= 0.0) {
+    if (fabs(pr) <= 1.0e-12) atomicAdd(&V.sc->negPCells, 1ull);
+    atomicAdd(&V.sc->posFixCells, 1ull);
+    cv[4] = 1.0e4 * cv[0] + ke;
+    pr = (P.gRT - 1.0) * (cv[4] - ke);
+  }
+  const double c2 = P.gRT * pr * ir;
+  // sqrt(c2): FP32 seed y ~ 1/sqrt(c2), h = c2*y, then h + h*(1 - h*y)/2
+  const double y = (double)rsqrtf((float)c2);
+  const double h = c2 * y;
+  const double cs = fma(0.5 * h, fma(-h, y, 1.0), h);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) V.cv[k * n + i] = cv[k];
+  V.dv[i] = pr;
+  V.dv[n + i] = pr * ir * P.igcR;
+  V.dv[2 * n + i] = cs;
+  V.prim[i] = rf;
+  V.prim[n + i] = uf;
+  V.prim[2 * n + i] = vf;
+  V.prim[3 * n + i] = wf;
+  V.prim[4 * n + i] = (float)pr;
+}
+
 // Gather + RKUpdateMP (RkUpdateGeneric, static grid, libfloflu/
 // RkUpdateGeneric.F90:257-322) + RFLU_SetVarsContWrapper + AfterUpdateMP.
 // cvOld of RkInitGeneric is cv itself: nothing writes cv before this kernel.
@@ -649,9 +753,13 @@ __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, c
   gatherRhs(V, (const R *)V.flux, i, rhs);
   const double fac = P.ark[iStage - 1] * (*dtp);
   const double grk = P.grk[iStage - 1];
-  const double adtv = fac / V.vol[i];
   double cv[5];
   loadCv(V, i, cv);
+  if constexpr (!Ref<R>::on) {
+    mixedUpdate(V, i, iStage, (float)fac, (float)grk, rhs, cv);
+    return;
+  }
+  const double adtv = fac / V.vol[i];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const double r = (double)rhs[k];
@@ -672,39 +780,6 @@ __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, c
     }
   }
   double pr, tp, cs;
-  if (!Ref<R>::on) {
-    // Mixed mode: RFLU_SetDependentVars and AfterUpdateMP with one
-    // reciprocal and one square root per cell, all in FP64.  A cell with
-    // p <= 0 gets the energy floor of RFLU_CheckPositivity (which also
-    // overrides the tiny-pressure clamp of RFLU_EnforceBounds).
-    const double ir = 1.0 / cv[0];
-    const double u = ir * cv[1], v = ir * cv[2], w = ir * cv[3];
-    const double ke = 0.5 * (cv[1] * u + cv[2] * v + cv[3] * w);
-    pr = (P.gRT - 1.0) * (cv[4] - ke);
-    if (isnan(cv[0]) || isnan(u) || isnan(v) || isnan(w) || isnan(pr)) {
-      atomicAdd(&V.sc->nanCells, 1ull);
-      atomicMin(&V.sc->firstBadCell, V.refId[i] + 1);
-    }
-    if (pr <= 0.0) {
-      if (fabs(pr) <= 1.0e-12) atomicAdd(&V.sc->negPCells, 1ull);
-      atomicAdd(&V.sc->posFixCells, 1ull);
-      cv[4] = 1.0e4 * cv[0] + ke;
-      pr = (P.gRT - 1.0) * (cv[4] - ke);
-    }
-    tp = pr * ir * P.igcR;
-    cs = sqrt(P.gRT * pr * ir);
-#pragma unroll
-    for (int k = 0; k < 5; ++k) V.cv[k * n + i] = cv[k];
-    V.dv[i] = pr;
-    V.dv[n + i] = tp;
-    V.dv[2 * n + i] = cs;
-    V.prim[i] = (R)cv[0];
-    V.prim[n + i] = (R)u;
-    V.prim[2 * n + i] = (R)v;
-    V.prim[3 * n + i] = (R)w;
-    V.prim[4 * n + i] = (R)pr;
-    return;
-  }
   dependentVars(P, cv, pr, tp, cs);
   afterUpdate(V, i, cv, pr, tp, cs);
 #pragma unroll
