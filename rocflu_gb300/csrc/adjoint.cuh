@@ -101,6 +101,15 @@ struct TanLoad {
     size_t o = (size_t)k * V.nc + c;
     return mk(V.grad[o], W.gradd[o]);
   }
+  __device__ void prim4(int c, S *q) const {
+    for (int k = 0; k < 4; ++k) q[k] = prim(k, c);
+  }
+  __device__ void prim5(int c, S *q) const {
+    for (int k = 0; k < 5; ++k) q[k] = prim(k, c);
+  }
+  __device__ void grad15(int c, S *g) const {
+    for (int k = 0; k < 15; ++k) g[k] = grad(k, c);
+  }
   __device__ H cv(int k, int c) const {
     size_t o = (size_t)k * V.nc + c;
     return mk(V.cv[o], W.cvd[o]);

@@ -59,13 +59,15 @@ __global__ void kPermuteIn(const double *src, double *dst, const int *refId, int
 #pragma unroll
   for (int k = 0; k < 5; ++k) dst[(size_t)k * nc + i] = src[5 * (size_t)o + k];
 }
-// SoA renumbered (ncomp rows of type T) -> reference column-major double
+// Renumbered per-cell data (component k of cell i at src[k*kStride +
+// i*iStride]) -> reference column-major double
 template <typename T>
-__global__ void kPermuteOut(const T *src, double *dst, const int *refId, int nc, int ncomp) {
+__global__ void kPermuteOut(const T *src, double *dst, const int *refId, int nc, int ncomp, size_t kStride,
+                            size_t iStride) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   int o = refId[i];
-  for (int k = 0; k < ncomp; ++k) dst[(size_t)ncomp * o + k] = (double)src[(size_t)k * nc + i];
+  for (int k = 0; k < ncomp; ++k) dst[(size_t)ncomp * o + k] = (double)src[k * kStride + i * iStride];
 }
 
 inline int nblk(long long n) { return (int)((n + 255) / 256); }
@@ -230,11 +232,12 @@ struct Ctx : CtxBase {
   }
   int download(double *cv, double *dv) override {
     if (cv) {
-      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.refId, V.nc, 5);
+      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.refId, V.nc, 5, V.nc, 1);
       RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
     }
     if (dv) {
-      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.refId, V.nc, 3);
+      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.refId, V.nc, 3, V.nc,
+                                                          1);
       RFLU_CUDA(cudaMemcpyAsync(dv, staging + 5 * (size_t)V.nc, sizeof(double) * 3 * (size_t)V.nc,
                                 cudaMemcpyDeviceToHost, stream));
     }
@@ -333,11 +336,14 @@ struct Ctx : CtxBase {
     ops->gradLimit(V, stream);
     ops->faceFlux(V, stream);
     ops->gatherRhs(V, stream);
-    kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.rhs, staging, V.refId, V.nc, 5);
+    kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.rhs, staging, V.refId, V.nc, 5, V.nc, 1);
     RFLU_CUDA(cudaMemcpyAsync(rhs, staging, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
     if (grad) {
       if (V.p.spaceOrder > 1) {
-        kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.grad, staging, V.refId, V.nc, 15);
+        if (Layout<R>::packed)
+          kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.grad, staging, V.refId, V.nc, 15, 1, 16);
+        else
+          kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.grad, staging, V.refId, V.nc, 15, V.nc, 1);
         RFLU_CUDA(cudaMemcpyAsync(grad, staging, sizeof(double) * 15 * nc, cudaMemcpyDeviceToHost, stream));
       } else {
         RFLU_CUDA(cudaStreamSynchronize(stream));
@@ -454,7 +460,7 @@ struct Ctx : CtxBase {
     const size_t nc = V.nc, nT = (size_t)V.nf + V.nb;
     auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t bCv = up(5 * nc * sizeof(double)), bDv = up(3 * nc * sizeof(double));
-    const size_t bPrim = up(5 * nc * sizeof(R)), bGrad = up(15 * nc * sizeof(R));
+    const size_t bPrim = up(Layout<R>::prim * nc * sizeof(R)), bGrad = up(Layout<R>::grad * nc * sizeof(R));
     const size_t bFlux = up(5 * nT * sizeof(R)), bRhs = up(5 * nc * sizeof(R));
     const size_t need = bCv + bDv + bPrim + bGrad + bFlux + bRhs;
     if (need > kStaticScratchBytes)
@@ -477,7 +483,7 @@ struct Ctx : CtxBase {
     ops->gradLimit(W, stream);
     ops->faceFlux(W, stream);
     ops->gatherRhs(W, stream);
-    kPermuteOut<R><<<nblk(W.nc), 256, 0, stream>>>(W.rhs, rhsDev, W.refId, W.nc, 5);
+    kPermuteOut<R><<<nblk(W.nc), 256, 0, stream>>>(W.rhs, rhsDev, W.refId, W.nc, 5, W.nc, 1);
     rc = checkLaunch("residual_static");
     if (rc) return rc;
     RFLU_CUDA(cudaStreamSynchronize(stream));
@@ -709,15 +715,15 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
 #undef PUT
   if ((rc = alloc(&V.cv, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.dv, 3 * (size_t)nc))) return rc;
-  if ((rc = alloc(&V.prim, 5 * (size_t)nc))) return rc;
-  if ((rc = alloc(&V.grad, 15 * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.prim, Layout<R>::prim * (size_t)nc))) return rc;
+  if ((rc = alloc(&V.grad, Layout<R>::grad * (size_t)nc))) return rc;
   if ((rc = alloc(&V.rhsSum, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.flux, 5 * ((size_t)nf + nb)))) return rc;
   if ((rc = alloc(&V.rhs, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.sc, 1))) return rc;
   if ((rc = alloc(&staging, 15 * (size_t)nc + 16))) return rc;
   if ((rc = alloc(&cvSave, 5 * (size_t)nc))) return rc;
-  RFLU_CUDA(cudaMemset(V.grad, 0, sizeof(R) * 15 * (size_t)nc));
+  RFLU_CUDA(cudaMemset(V.grad, 0, sizeof(R) * Layout<R>::grad * (size_t)nc));
   RFLU_CUDA(cudaMemset(V.rhsSum, 0, sizeof(R) * 5 * (size_t)nc));
   RFLU_CUDA(cudaMemset(V.cv, 0, sizeof(double) * 5 * (size_t)nc));
   Scalars s0{};

@@ -35,6 +35,23 @@ struct Params {
   double ark[5], grk[5];
 };
 
+// Per-cell record layout of prim, grad and flux.  The FP64 modes keep them as
+// structure-of-arrays (component k of cell i at a[k*n + i]).  The mixed mode
+// packs each cell's record into float4s so that a neighbour gather is two or
+// four 16-byte loads: prim (8 floats per cell) = (rho, u, v, w | p, xc, yc, zc)
+// with the cell centroid riding along for the least-squares weights; grad (16
+// floats per cell) = the 15 components in the order 3*var + dir and one pad;
+// flux = one float4 (mass and momentum) per face followed by the nT energy
+// fluxes.
+template <typename R> struct Layout {
+  static constexpr bool packed = false;
+  static constexpr int prim = 5, grad = 15;
+};
+template <> struct Layout<float> {
+  static constexpr bool packed = true;
+  static constexpr int prim = 8, grad = 16;
+};
+
 template <typename R>
 struct View {
   int nc, nf, nb;             // cells, interior faces, boundary faces
@@ -59,8 +76,9 @@ struct View {
   const R *epsq;                    // Venkatakrishnan eps^2 = (vol^(1/3))^3 per cell
   // mixed mode: LSQ weights are formed on the fly from the cell's R-factor
   // coefficients (c1111, c2222, c3333, c12, c13, c23) and the members'
-  // centroids, instead of streaming three weights per stencil member
-  const R *cgx, *cgy, *cgz;         // cell centroids (FP32)
+  // centroids (read from the packed prim records), instead of streaming three
+  // weights per stencil member
+  const R *cgx, *cgy, *cgz;         // cell centroids (FP32), written into prim
   const R *rcf;                     // (6, nc) R-factor coefficients
   const R *ivol;                    // 1/vol (FP32), for the FP32 RK increment
   const int *refId;                 // renumbered -> reference (0-based) cell id
@@ -70,10 +88,10 @@ struct View {
   // state
   double *cv;                       // (5, nc)
   double *dv;                       // (3, nc): p, T, c
-  R *prim;                          // (5, nc): rho, u, v, w, p
-  R *grad;                          // (15, nc): component (3*var + dir)
+  R *prim;                          // rho, u, v, w, p (Layout<R>)
+  R *grad;                          // component (3*var + dir) (Layout<R>)
   R *rhsSum;                        // (5, nc)
-  R *flux;                          // (5, nf + nb)
+  R *flux;                          // 5 per face, nf + nb faces (Layout<R>)
   R *rhs;                           // (5, nc), residual output only
   Scalars *sc;
   Params p;

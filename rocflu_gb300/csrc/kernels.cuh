@@ -60,18 +60,136 @@ __device__ inline void loadCv(const View<R> &V, int i, double *cv) {
   for (int k = 0; k < 5; ++k) cv[k] = V.cv[(size_t)k * V.nc + i];
 }
 
+// ---------------------------------------------------------------------------
+// Cell data as the stage code reads it.  PlainLoad reads the primal arrays
+// (S = R, the state type; H = double, the type of the first-order paths,
+// FP64 in every mode); the tangent kernels use a loader whose S and H are
+// dual numbers carrying the directional derivatives.
+// ---------------------------------------------------------------------------
+__device__ inline float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ inline void st4(float *p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+
+template <typename R>
+struct PlainLoad {
+  using S = R;
+  using H = double;
+  const View<R> &V;
+  __device__ S prim(int k, int c) const {
+    if constexpr (Layout<R>::packed) return V.prim[8 * (size_t)c + k];
+    else return V.prim[(size_t)k * V.nc + c];
+  }
+  __device__ S grad(int k, int c) const {
+    if constexpr (Layout<R>::packed) return V.grad[16 * (size_t)c + k];
+    else return V.grad[(size_t)k * V.nc + c];
+  }
+  // rho, u, v, w
+  __device__ void prim4(int c, S *q) const {
+    if constexpr (Layout<R>::packed) {
+      const float4 a = ld4(V.prim + 8 * (size_t)c);
+      q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) q[k] = prim(k, c);
+    }
+  }
+  // rho, u, v, w, p
+  __device__ void prim5(int c, S *q) const {
+    if constexpr (Layout<R>::packed) {
+      const float4 a = ld4(V.prim + 8 * (size_t)c), b = ld4(V.prim + 8 * (size_t)c + 4);
+      q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) q[k] = prim(k, c);
+    }
+  }
+  // rho, u, v, w, p and the centroid (packed layout only)
+  __device__ void primCg(int c, S *q, S *x) const {
+    const float4 a = ld4(V.prim + 8 * (size_t)c), b = ld4(V.prim + 8 * (size_t)c + 4);
+    q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x;
+    x[0] = b.y; x[1] = b.z; x[2] = b.w;
+  }
+  __device__ void grad15(int c, S *g) const {
+    if constexpr (Layout<R>::packed) {
+      const float *p = V.grad + 16 * (size_t)c;
+      const float4 a = ld4(p), b = ld4(p + 4), d = ld4(p + 8), e = ld4(p + 12);
+      g[0] = a.x; g[1] = a.y; g[2] = a.z; g[3] = a.w;
+      g[4] = b.x; g[5] = b.y; g[6] = b.z; g[7] = b.w;
+      g[8] = d.x; g[9] = d.y; g[10] = d.z; g[11] = d.w;
+      g[12] = e.x; g[13] = e.y; g[14] = e.z;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) g[k] = grad(k, c);
+    }
+  }
+  __device__ H cv(int k, int c) const { return V.cv[(size_t)k * V.nc + c]; }
+  __device__ H dv(int k, int c) const { return V.dv[(size_t)k * V.nc + c]; }
+};
+
+// Store of one cell's gradient record.
+template <typename R>
+__device__ inline void storeGrad(const View<R> &V, int i, const R *g) {
+  if constexpr (Layout<R>::packed) {
+    float *p = V.grad + 16 * (size_t)i;
+    st4(p, g[0], g[1], g[2], g[3]);
+    st4(p + 4, g[4], g[5], g[6], g[7]);
+    st4(p + 8, g[8], g[9], g[10], g[11]);
+    st4(p + 12, g[12], g[13], g[14], 0.f);
+  } else {
+    const size_t n = V.nc;
+#pragma unroll
+    for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
+  }
+}
+
+// Store of one cell's primitive record (the packed layout carries the centroid).
+template <typename R>
+__device__ inline void storePrimRec(const View<R> &V, int i, R r, R u, R v, R w, R p) {
+  if constexpr (Layout<R>::packed) {
+    float *q = V.prim + 8 * (size_t)i;
+    st4(q, r, u, v, w);
+    st4(q + 4, p, V.cgx[i], V.cgy[i], V.cgz[i]);
+  } else {
+    const size_t n = V.nc;
+    V.prim[i] = r;
+    V.prim[n + i] = u;
+    V.prim[2 * n + i] = v;
+    V.prim[3 * n + i] = w;
+    V.prim[4 * n + i] = p;
+  }
+}
+
+// Flux of face t: SoA in the FP64 modes; in the packed layout one float4
+// (mass, momentum) per face followed by the nT energy fluxes.
+template <typename R>
+__device__ inline void storeFlux(const View<R> &V, size_t nT, int t, const R *f) {
+  if constexpr (Layout<R>::packed) {
+    st4(V.flux + 4 * (size_t)t, f[0], f[1], f[2], f[3]);
+    V.flux[4 * nT + t] = f[4];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) V.flux[k * nT + t] = f[k];
+  }
+}
+template <typename R, typename T>
+__device__ inline void loadFlux(const T *flux, size_t nT, int t, T *f) {
+  if constexpr (Layout<R>::packed) {
+    const float4 a = ld4(flux + 4 * (size_t)t);
+    f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w;
+    f[4] = flux[4 * nT + t];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) f[k] = flux[k * nT + t];
+  }
+}
+
 // prim = (rho, u, v, w, p) as RFLU_ConvertCvCons2Prim DUVWP builds it
 // (modflu/RFLU_ModConvertCv.F90:214-224)
 template <typename R>
 __device__ inline void storePrim(const View<R> &V, int i, const double *cv, double pres) {
   double ir = 1.0 / cv[0];
-  R *q = V.prim;
-  const size_t n = V.nc;
-  q[i] = (R)cv[0];
-  q[n + i] = (R)(ir * cv[1]);
-  q[2 * n + i] = (R)(ir * cv[2]);
-  q[3 * n + i] = (R)(ir * cv[3]);
-  q[4 * n + i] = (R)pres;
+  storePrimRec(V, i, (R)cv[0], (R)(ir * cv[1]), (R)(ir * cv[2]), (R)(ir * cv[3]), (R)pres);
 }
 
 // Dependent variables and primitive state of every cell from cv
@@ -90,23 +208,6 @@ __global__ void kInitState(View<R> V) {
 }
 
 // ---------------------------------------------------------------------------
-// Cell data as the stage code reads it.  PlainLoad reads the primal arrays
-// (S = R, the state type; H = double, the type of the first-order paths,
-// FP64 in every mode); the tangent kernels use a loader whose S and H are
-// dual numbers carrying the directional derivatives.
-// ---------------------------------------------------------------------------
-template <typename R>
-struct PlainLoad {
-  using S = R;
-  using H = double;
-  const View<R> &V;
-  __device__ S prim(int k, int c) const { return V.prim[(size_t)k * V.nc + c]; }
-  __device__ S grad(int k, int c) const { return V.grad[(size_t)k * V.nc + c]; }
-  __device__ H cv(int k, int c) const { return V.cv[(size_t)k * V.nc + c]; }
-  __device__ H dv(int k, int c) const { return V.dv[(size_t)k * V.nc + c]; }
-};
-
-// ---------------------------------------------------------------------------
 // Gradient + limiter of one cell.
 // LSQ gradient: RFLU_ComputeGradCellsFast_3D (modflu/RFLU_ModDifferentiationCells.F90:
 // 931-1178) with the per-member weights precomputed at set-up.
@@ -120,8 +221,7 @@ template <typename R, typename L>
 __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typename L::S *g) {
   using S = typename L::S;
   S q[5];
-#pragma unroll
-  for (int k = 0; k < 5; ++k) q[k] = ld.prim(k, i);
+  ld.prim5(i, q);
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = S(0);
   const int sb = V.stOff[i], se = V.stOff[i + 1];
@@ -148,7 +248,9 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
 #pragma unroll 2
     for (int s = sb; s < se; ++s) {
       const int j = V.stIdx[s];
-      S dx = S(V.cgx[j]) - xi, dy = S(V.cgy[j]) - yi, dz = S(V.cgz[j]) - zi;
+      S qj[5], xj[3];
+      ld.primCg(j, qj, xj);
+      S dx = xj[0] - xi, dy = xj[1] - yi, dz = xj[2] - zi;
       const S term = S(1) / sqrt_(dx * dx + dy * dy + dz * dz);
       dx = term * dx;
       dy = term * dy;
@@ -161,7 +263,7 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       const S wz = term * t3;
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        S d = ld.prim(k, j) - q[k];
+        S d = qj[k] - q[k];
         g[3 * k] = g[3 * k] + wx * d;
         g[3 * k + 1] = g[3 * k + 1] + wy * d;
         g[3 * k + 2] = g[3 * k + 2] + wz * d;
@@ -180,11 +282,12 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       if (code < 0) continue;
       const int f = code >> 1;
       const int nb = (code & 1) ? V.fc1[f] : V.fc2[f];
+      S x[5];
+      ld.prim5(nb, x);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        S x = ld.prim(k, nb);
-        vmin[k] = fmin2(vmin[k], x);
-        vmax[k] = fmax2(vmax[k], x);
+        vmin[k] = fmin2(vmin[k], x[k]);
+        vmax[k] = fmax2(vmax[k], x[k]);
       }
     }
     S epsq = (rc == 11) ? S(V.epsq[i]) : S(0);
@@ -235,9 +338,11 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         if (code < 0) continue;
         const int f = code >> 1, side = code & 1;
         const int c1 = V.fc1[f], c2 = V.fc2[f];
-        S du[3];
+        S du[3], a1[4], a2[4];
+        ld.prim4(c1, a1);
+        ld.prim4(c2, a2);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) du[k] = ld.prim(1 + k, c2) - ld.prim(1 + k, c1);
+        for (int k = 0; k < 3; ++k) du[k] = a2[1 + k] - a1[1 + k];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           S pr = S(0);
@@ -328,9 +433,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimit(View<R> V)
   if (i >= V.nc) return;
   R g[15];
   gradLimitCell(V, PlainLoad<R>{V}, i, g);
-  const size_t n = V.nc;
-#pragma unroll
-  for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
+  storeGrad(V, i, g);
 }
 
 // Block minimum of a per-thread dt (warp shuffles, then one warp over the
@@ -354,20 +457,24 @@ __device__ inline void blockMinDt(Scalars *sc, double dt) {
 // primitive state (mixed mode; the sound speed from the FP64-recovered p).
 template <typename R>
 __device__ inline double cellDtPrim(const View<R> &V, int i) {
-  const size_t n = V.nc;
+  const PlainLoad<R> ld{V};
   const float g = (float)V.p.refGamma;
-  const float ri = (float)V.prim[i];
-  const float ui = (float)V.prim[n + i], vi = (float)V.prim[2 * n + i], wi = (float)V.prim[3 * n + i];
-  const float ai = sqrtf(g * (float)V.prim[4 * n + i] / ri);
+  R qi[5];
+  ld.prim5(i, qi);
+  const float ri = (float)qi[0];
+  const float ui = (float)qi[1], vi = (float)qi[2], wi = (float)qi[3];
+  const float ai = sqrtf(g * (float)qi[4] / ri);
   float sum = 0.f;
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
   for (int e = cb; e < ce; ++e) {
     const int code = V.cfEnt[e];
     if (code >= 0) {
       const int f = code >> 1, nb = (code & 1) ? V.fc1[f] : V.fc2[f];
-      const float rj = (float)V.prim[nb];
-      const float uj = (float)V.prim[n + nb], vj = (float)V.prim[2 * n + nb], wj = (float)V.prim[3 * n + nb];
-      const float aj = sqrtf(g * (float)V.prim[4 * n + nb] / rj);
+      R qj[5];
+      ld.prim5(nb, qj);
+      const float rj = (float)qj[0];
+      const float uj = (float)qj[1], vj = (float)qj[2], wj = (float)qj[3];
+      const float aj = sqrtf(g * (float)qj[4] / rj);
       const float vc = 0.5f * ((ui + uj) * (float)V.fnx[f] + (vi + vj) * (float)V.fny[f] + (wi + wj) * (float)V.fnz[f]);
       sum += (fabsf(vc) + 0.5f * (ai + aj)) * (float)V.fnm[f];
     } else {
@@ -389,9 +496,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> 
     if (V.p.spaceOrder > 1) {
       R g[15];
       gradLimitCell(V, PlainLoad<R>{V}, i, g);
-      const size_t n = V.nc;
-#pragma unroll
-      for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
+      storeGrad(V, i, g);
     }
     dt = cellDtPrim(V, i);
   }
@@ -407,21 +512,24 @@ template <typename R, typename L>
 __device__ inline void faceState(const View<R> &V, const L &ld, int c, typename L::S dx, typename L::S dy,
                                  typename L::S dz, typename L::S *s, typename L::S &irCell) {
   using S = typename L::S;
-  S r = ld.prim(0, c);
+  S q[5], gr[15];
+  ld.prim5(c, q);
+  ld.grad15(c, gr);
+  S r = q[0];
   S ir = S(1) / r;
-  S u = ld.prim(1, c), v = ld.prim(2, c), w = ld.prim(3, c);
+  S u = q[1], v = q[2], w = q[3];
   if (Ref<R>::on) {
     // ul = pCv(CV_MIXT_XMOM,c1)*irl with pCv(XMOM) = r*u after RFLU_ConvertCvPrim2Cons
     u = (r * u) * ir;
     v = (r * v) * ir;
     w = (r * w) * ir;
   }
-  S p = ld.prim(4, c);
-  s[0] = r + ld.grad(0, c) * dx + ld.grad(1, c) * dy + ld.grad(2, c) * dz;
-  s[1] = u + ld.grad(3, c) * dx + ld.grad(4, c) * dy + ld.grad(5, c) * dz;
-  s[2] = v + ld.grad(6, c) * dx + ld.grad(7, c) * dy + ld.grad(8, c) * dz;
-  s[3] = w + ld.grad(9, c) * dx + ld.grad(10, c) * dy + ld.grad(11, c) * dz;
-  s[4] = p + ld.grad(12, c) * dx + ld.grad(13, c) * dy + ld.grad(14, c) * dz;
+  S p = q[4];
+  s[0] = r + gr[0] * dx + gr[1] * dy + gr[2] * dz;
+  s[1] = u + gr[3] * dx + gr[4] * dy + gr[5] * dz;
+  s[2] = v + gr[6] * dx + gr[7] * dy + gr[8] * dz;
+  s[3] = w + gr[9] * dx + gr[10] * dy + gr[11] * dz;
+  s[4] = p + gr[12] * dx + gr[13] * dy + gr[14] * dz;
   irCell = ir;
 }
 
@@ -587,9 +695,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocksFlux<R>::v) kFaceFlux(View<R>
   if (t >= nfT) return;
   R flx[5];
   faceFluxEval(V, PlainLoad<R>{V}, t, flx);
-  const size_t nT = nfT;
-#pragma unroll
-  for (int k = 0; k < 5; ++k) V.flux[k * nT + t] = flx[k];
+  storeFlux(V, (size_t)nfT, t, flx);
 }
 
 // ---------------------------------------------------------------------------
@@ -606,17 +712,23 @@ __device__ inline void gatherRhs(const View<R> &V, const T *flux, int i, T *rhs)
     const int code = V.cfEnt[e];
     if (code >= 0) {
       const int f = code >> 1;
+      T fl[5];
+      loadFlux<R>(flux, nT, f, fl);
       if (code & 1) {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] - flux[k * nT + f];
+        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] - fl[k];
       } else {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] + flux[k * nT + f];
+        for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] + fl[k];
       }
     } else {
       const int b = -code - 1;
       const int k0 = (V.patchType[V.bpatch[b]] == 60) ? 1 : 0;  // slip walls leave rhs(DENS)
-      for (int k = k0; k < 5; ++k) rhs[k] = rhs[k] + flux[k * nT + V.nf + b];
+      T fl[5];
+      loadFlux<R>(flux, nT, V.nf + b, fl);
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        if (k >= k0) rhs[k] = rhs[k] + fl[k];
     }
   }
 }
@@ -733,11 +845,7 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
   V.dv[i] = pr;
   V.dv[n + i] = pr * ir * P.igcR;
   V.dv[2 * n + i] = cs;
-  V.prim[i] = rf;
-  V.prim[n + i] = uf;
-  V.prim[2 * n + i] = vf;
-  V.prim[3 * n + i] = wf;
-  V.prim[4 * n + i] = (float)pr;
+  storePrimRec(V, i, (R)rf, (R)uf, (R)vf, (R)wf, (R)pr);
 }
 
 // Gather + RKUpdateMP (RkUpdateGeneric, static grid, libfloflu/
