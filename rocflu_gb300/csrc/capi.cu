@@ -72,6 +72,17 @@ __global__ void kPermuteOut(const T *src, double *dst, const int *refId, int nc,
 
 inline int nblk(long long n) { return (int)((n + 255) / 256); }
 
+// T and c of RFLU_SetDependentVars (TCPERF) from cv and p, for a mixed-mode
+// context whose steps store p only.
+__global__ void kDvFill(const double *cv, double *dv, int nc, double gcR, double gRT) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const double r = cv[i], p = dv[i];
+  const double t = p / (r * gcR);
+  dv[(size_t)nc + i] = t;
+  dv[2 * (size_t)nc + i] = sqrt(gRT * gcR * t);
+}
+
 // Scratch of rflu_gpu_residual_static: a fixed device array in this file, so
 // that the call allocates nothing.  Every GPU that loads the library keeps
 // these 64 MiB until the process exits.  All calls share it (see the header).
@@ -231,6 +242,7 @@ struct Ctx : CtxBase {
     return syncEvents(false);
   }
   int download(double *cv, double *dv) override {
+    if (dv && V.p.dvPOnly) kDvFill<<<nblk(V.nc), 256, 0, stream>>>(V.cv, V.dv, V.nc, V.p.gcR, V.p.gRT);
     if (cv) {
       kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.refId, V.nc, 5, V.nc, 1);
       RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
@@ -692,9 +704,26 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   V.nc = nc; V.nf = nf; V.nb = nb;
   int rc = 0;
 #define PUT(dst, src, T) if ((rc = put<T>(&(dst), src))) return rc
-  PUT(V.fc1, fc1, int); PUT(V.fc2, fc2, int);
-  PUT(V.fnx, fnx, R); PUT(V.fny, fny, R); PUT(V.fnz, fnz, R); PUT(V.fnm, fnm, R);
-  PUT(V.dL, dL, R); PUT(V.dR, dR, R);
+  if (mixed) {
+    // one 48-byte record per interior face (ctx.h)
+    for (int i = 0; i < nc; ++i)
+      if (cfOff[i + 1] - cfOff[i] > 6)
+        return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: the mixed mode takes cells of at most 6 faces");
+    std::vector<float> fpk(12 * (size_t)nf);
+    for (int s = 0; s < nf; ++s) {
+      float *r = &fpk[12 * (size_t)s];
+      r[0] = (float)fnx[s]; r[1] = (float)fny[s]; r[2] = (float)fnz[s]; r[3] = (float)fnm[s];
+      r[4] = (float)dL[s]; r[5] = (float)dL[(size_t)nf + s]; r[6] = (float)dL[2 * (size_t)nf + s];
+      r[7] = (float)dR[s]; r[8] = (float)dR[(size_t)nf + s]; r[9] = (float)dR[2 * (size_t)nf + s];
+      std::memcpy(&r[10], &fc1[s], sizeof(int));
+      std::memcpy(&r[11], &fc2[s], sizeof(int));
+    }
+    PUT(V.fpk, fpk, float);
+  } else {
+    PUT(V.fc1, fc1, int); PUT(V.fc2, fc2, int);
+    PUT(V.fnx, fnx, R); PUT(V.fny, fny, R); PUT(V.fnz, fnz, R); PUT(V.fnm, fnm, R);
+    PUT(V.dL, dL, R); PUT(V.dR, dR, R);
+  }
   PUT(V.bcell, bcell, int); PUT(V.bpatch, bpatch, int);
   PUT(V.bnx, bnx, R); PUT(V.bny, bny, R); PUT(V.bnz, bnz, R); PUT(V.bnm, bnm, R);
   PUT(V.bd, bd, R);
@@ -758,6 +787,8 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     P.nrkSteps = 1;
     P.ark[0] = 1.0; P.grk[0] = 1.0;
   }
+  for (int k = 0; k < 5; ++k) { P.arkF[k] = (float)P.ark[k]; P.grkF[k] = (float)P.grk[k]; }
+  P.dvPOnly = (num->precision == RFLU_PREC_MIXED && num->spaceOrder > 1) ? 1 : 0;
   // adjoint workspace: gradients/limiter factors/face adjoints of one residual
   workBytes = sizeof(double) * (size_t)(96 * (size_t)nc + 24 * ((size_t)nf + nb) + 64);
   if (num->precision != RFLU_PREC_MIXED) {

@@ -33,6 +33,10 @@ struct Params {
   double cfl, dtImposed, dtMinLimit;
   int nrkSteps;
   double ark[5], grk[5];
+  float arkF[5], grkF[5];     // FP32 copies for the mixed-mode update
+  // mixed mode at 2nd order: no kernel of the step reads T or c, so the stage
+  // update stores p only and T, c are formed from cv when dv is read out
+  int dvPOnly;
 };
 
 // Per-cell record layout of prim, grad and flux.  The FP64 modes keep them as
@@ -55,10 +59,14 @@ template <> struct Layout<float> {
 template <typename R>
 struct View {
   int nc, nf, nb;             // cells, interior faces, boundary faces
-  // interior faces (storage order), renumbered cells
+  // interior faces (storage order), renumbered cells; FP64 modes
   const int *fc1, *fc2;
   const R *fnx, *fny, *fnz, *fnm;   // unit normal and area
   const R *dL, *dR;                 // (3, nf): fc - cofg(c1), fc - cofg(c2)
+  // the same interior face data in the mixed mode, one 48-byte record per
+  // face: (nx, ny, nz, nm), (dLx, dLy, dLz, dRx), (dRy, dRz, c1, c2) with the
+  // cell ids stored as int bit patterns
+  const float *fpk;
   // boundary faces
   const int *bcell;                 // owning cell
   const int *bpatch;                // patch index

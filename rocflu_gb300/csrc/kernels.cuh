@@ -70,6 +70,53 @@ __device__ inline float4 ld4(const float *p) { return *reinterpret_cast<const fl
 __device__ inline void st4(float *p, float a, float b, float c, float d) {
   *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
 }
+// One 32-byte record in a single 256-bit load (sm_100 and later; the address
+// is 32-byte aligned: records are 8 floats from a 256-byte aligned base).
+// Only for data no thread of the running kernel writes.
+__device__ inline void ld8(const float *p, float *v) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+      : "l"(p));
+}
+
+// Interior face f in either layout: cells, unit normal and area, and the
+// offset fc - cofg of side 0 (c1) or side 1 (c2).
+template <typename R>
+__device__ inline void faceCells(const View<R> &V, int f, int &c1, int &c2) {
+  if constexpr (Layout<R>::packed) {
+    const float4 F2 = ld4(V.fpk + 12 * (size_t)f + 8);
+    c1 = __float_as_int(F2.z);
+    c2 = __float_as_int(F2.w);
+  } else {
+    c1 = V.fc1[f];
+    c2 = V.fc2[f];
+  }
+}
+template <typename R>
+__device__ inline void faceNormal(const View<R> &V, int f, R &nx, R &ny, R &nz, R &nm) {
+  if constexpr (Layout<R>::packed) {
+    const float4 F0 = ld4(V.fpk + 12 * (size_t)f);
+    nx = F0.x; ny = F0.y; nz = F0.z; nm = F0.w;
+  } else {
+    nx = V.fnx[f]; ny = V.fny[f]; nz = V.fnz[f]; nm = V.fnm[f];
+  }
+}
+template <typename R>
+__device__ inline void faceOffset(const View<R> &V, int f, int side, R *d) {
+  if constexpr (Layout<R>::packed) {
+    const float4 F1 = ld4(V.fpk + 12 * (size_t)f + 4);
+    if (side) {
+      const float4 F2 = ld4(V.fpk + 12 * (size_t)f + 8);
+      d[0] = F1.w; d[1] = F2.x; d[2] = F2.y;
+    } else {
+      d[0] = F1.x; d[1] = F1.y; d[2] = F1.z;
+    }
+  } else {
+    const R *a = side ? V.dR : V.dL;
+    const size_t nf = V.nf;
+    d[0] = a[f]; d[1] = a[nf + f]; d[2] = a[2 * nf + f];
+  }
+}
 
 template <typename R>
 struct PlainLoad {
@@ -97,8 +144,10 @@ struct PlainLoad {
   // rho, u, v, w, p
   __device__ void prim5(int c, S *q) const {
     if constexpr (Layout<R>::packed) {
-      const float4 a = ld4(V.prim + 8 * (size_t)c), b = ld4(V.prim + 8 * (size_t)c + 4);
-      q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x;
+      float r[8];
+      ld8(V.prim + 8 * (size_t)c, r);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) q[k] = r[k];
     } else {
 #pragma unroll
       for (int k = 0; k < 5; ++k) q[k] = prim(k, c);
@@ -106,18 +155,19 @@ struct PlainLoad {
   }
   // rho, u, v, w, p and the centroid (packed layout only)
   __device__ void primCg(int c, S *q, S *x) const {
-    const float4 a = ld4(V.prim + 8 * (size_t)c), b = ld4(V.prim + 8 * (size_t)c + 4);
-    q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w; q[4] = b.x;
-    x[0] = b.y; x[1] = b.z; x[2] = b.w;
+    float r[8];
+    ld8(V.prim + 8 * (size_t)c, r);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = r[k];
+    x[0] = r[5]; x[1] = r[6]; x[2] = r[7];
   }
   __device__ void grad15(int c, S *g) const {
     if constexpr (Layout<R>::packed) {
-      const float *p = V.grad + 16 * (size_t)c;
-      const float4 a = ld4(p), b = ld4(p + 4), d = ld4(p + 8), e = ld4(p + 12);
-      g[0] = a.x; g[1] = a.y; g[2] = a.z; g[3] = a.w;
-      g[4] = b.x; g[5] = b.y; g[6] = b.z; g[7] = b.w;
-      g[8] = d.x; g[9] = d.y; g[10] = d.z; g[11] = d.w;
-      g[12] = e.x; g[13] = e.y; g[14] = e.z;
+      float r[16];
+      ld8(V.grad + 16 * (size_t)c, r);
+      ld8(V.grad + 16 * (size_t)c + 8, r + 8);
+#pragma unroll
+      for (int k = 0; k < 15; ++k) g[k] = r[k];
     } else {
 #pragma unroll
       for (int k = 0; k < 15; ++k) g[k] = grad(k, c);
@@ -281,7 +331,9 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       const int code = V.cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
-      const int nb = (code & 1) ? V.fc1[f] : V.fc2[f];
+      int c1, c2;
+      faceCells(V, f, c1, c2);
+      const int nb = (code & 1) ? c1 : c2;
       S x[5];
       ld.prim5(nb, x);
 #pragma unroll
@@ -295,8 +347,9 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       const int code = V.cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
-      const R *d = (code & 1) ? V.dR : V.dL;
-      const S dx = S(d[f]), dy = S(d[(size_t)V.nf + f]), dz = S(d[2 * (size_t)V.nf + f]);
+      R d[3];
+      faceOffset(V, f, code & 1, d);
+      const S dx = S(d[0]), dy = S(d[1]), dz = S(d[2]);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         if (rc == 10 && k >= 1 && k <= 3) continue;
@@ -337,7 +390,8 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         const int code = V.cfEnt[e];
         if (code < 0) continue;
         const int f = code >> 1, side = code & 1;
-        const int c1 = V.fc1[f], c2 = V.fc2[f];
+        int c1, c2;
+        faceCells(V, f, c1, c2);
         S du[3], a1[4], a2[4];
         ld.prim4(c1, a1);
         ld.prim4(c2, a2);
@@ -358,8 +412,9 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         const int code = V.cfEnt[e];
         if (code < 0) continue;
         const int f = code >> 1;
-        const R *d = (code & 1) ? V.dR : V.dL;
-        const S off[3] = {-S(d[f]), -S(d[(size_t)V.nf + f]), -S(d[2 * (size_t)V.nf + f])};
+        R d[3];
+        faceOffset(V, f, code & 1, d);
+        const S off[3] = {-S(d[0]), -S(d[1]), -S(d[2])};
         S sh[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -427,12 +482,237 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
   }
 }
 
+// The mixed-mode cell kernel: the same gradient and limiter as gradLimitCell
+// (and, with kDt, the spectral-radius sum of RFLU_TimeStepInviscid) in one
+// pass over the cell's faces instead of five.  The strain-rate eigenframe
+// needs only the unlimited gradient, so the velocity projections are taken in
+// the same pass as the neighbour min/max; each face's offset fc - cofg is kept
+// in shared memory (dc, stride kBlock) for the limiter pass.  At most
+// kMaxCellFaces faces per cell (tetrahedra 4, prisms and pyramids 5,
+// hexahedra 6).  Returns the spectral-radius sum (kDt) or 0.
+constexpr int kMaxCellFaces = 6;
+
+template <bool kDt>
+__device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, float *dc) {
+  const Params &P = V.p;
+  float rec[8];
+  ld8(V.prim + 8 * (size_t)i, rec);
+  const float q[5] = {rec[0], rec[1], rec[2], rec[3], rec[4]};
+#pragma unroll
+  for (int k = 0; k < 15; ++k) g[k] = 0.f;
+  const bool second = P.spaceOrder > 1;
+  if (second) {
+    // LSQ weights of RFLU_ComputeGradCellsFast_3D (:983-1044) in FP32 from
+    // the R-factor coefficients and the member's centroid
+    const size_t n = V.nc;
+    const float c1111 = V.rcf[i], c2222 = V.rcf[n + i], c3333 = V.rcf[2 * n + i];
+    const float c12 = V.rcf[3 * n + i], c13 = V.rcf[4 * n + i], c23 = V.rcf[5 * n + i];
+    const int sb = V.stOff[i], se = V.stOff[i + 1];
+#pragma unroll 2
+    for (int s = sb; s < se; ++s) {
+      float r[8];
+      ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
+      float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+      const float term = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
+      dx = term * dx;
+      dy = term * dy;
+      dz = term * dz;
+      const float t1 = c1111 * dx;
+      const float t2 = c2222 * (dy + c12 * dx);
+      const float t3 = c3333 * (dz + c23 * dy + c13 * dx);
+      const float wx = term * (t1 + c12 * t2 + c13 * t3);
+      const float wy = term * (t2 + c23 * t3);
+      const float wz = term * t3;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const float d = r[k] - q[k];
+        g[3 * k] = g[3 * k] + wx * d;
+        g[3 * k + 1] = g[3 * k + 1] + wy * d;
+        g[3 * k + 2] = g[3 * k + 2] + wz * d;
+      }
+    }
+  }
+  const int rc = P.reconst;
+  const bool lim = second && (rc == 10 || rc == 100 || rc == 11);
+  const bool velo = lim && rc == 10;
+  float G[9], A[9], ev[3];
+  if (velo) {
+    float Sy[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) G[a + 3 * b] = g[3 * (1 + a) + b];  // G(iComp, dir)
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) Sy[a + 3 * b] = 0.5f * (G[a + 3 * b] + G[b + 3 * a]);
+    symmetricEigen3(Sy, A, ev);
+  }
+  float vmin[5], vmax[5], dmn[3] = {0.f, 0.f, 0.f}, dmx[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; }
+  const float gam = P.refGammaF;
+  const float ai = kDt ? sqrtf(gam * q[4] / q[0]) : 0.f;
+  float sum = 0.f;
+  int nfc = 0;
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  for (int e = cb; e < ce; ++e) {
+    const int code = V.cfEnt[e];
+    if (code >= 0) {
+      if (!lim && !kDt) continue;
+      const int f = code >> 1, side = code & 1;
+      const float *fr = V.fpk + 12 * (size_t)f;
+      const float4 F1 = ld4(fr + 4), F2 = ld4(fr + 8);
+      const int nb = side ? __float_as_int(F2.z) : __float_as_int(F2.w);
+      float x[8];
+      ld8(V.prim + 8 * (size_t)nb, x);
+      if (lim) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          vmin[k] = fmin2(vmin[k], x[k]);
+          vmax[k] = fmax2(vmax[k], x[k]);
+        }
+        if (velo) {
+          // A^T (u(c2) - u(c1)) seen from this cell = A^T (u(nb) - u(i))
+          const float du0 = x[1] - q[1], du1 = x[2] - q[2], du2 = x[3] - q[3];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            float pr = 0.f;
+            pr = pr + A[3 * j] * du0;
+            pr = pr + A[3 * j + 1] * du1;
+            pr = pr + A[3 * j + 2] * du2;
+            dmn[j] = fmin2(dmn[j], pr);
+            dmx[j] = fmax2(dmx[j], pr);
+          }
+        }
+        float *slot = dc + 3 * nfc * kBlock;
+        slot[0] = side ? F1.w : F1.x;
+        slot[kBlock] = side ? F2.x : F1.y;
+        slot[2 * kBlock] = side ? F2.y : F1.z;
+        ++nfc;
+      }
+      if (kDt) {
+        const float4 F0 = ld4(fr);
+        const float aj = sqrtf(gam * x[4] / x[0]);
+        const float vc = 0.5f * ((q[1] + x[1]) * F0.x + (q[2] + x[2]) * F0.y + (q[3] + x[3]) * F0.z);
+        sum += (fabsf(vc) + 0.5f * (ai + aj)) * F0.w;
+      }
+    } else if (kDt) {
+      const int b = -code - 1;
+      const float vc = q[1] * V.bnx[b] + q[2] * V.bny[b] + q[3] * V.bnz[b];
+      sum += (fabsf(vc) + ai) * V.bnm[b];
+    }
+  }
+  if (!lim) return sum;
+  float lm[5] = {1.f, 1.f, 1.f, 1.f, 1.f}, al[3] = {1.f, 1.f, 1.f};
+  const float epsq = (rc == 11) ? V.epsq[i] : 0.f;
+  for (int c = 0; c < nfc; ++c) {
+    const float *slot = dc + 3 * c * kBlock;
+    const float dx = slot[0], dy = slot[kBlock], dz = slot[2 * kBlock];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      if (velo && k >= 1 && k <= 3) continue;
+      // d2 = grad . (cofg - fc), the reference's sign
+      const float d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
+      const float dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
+      if (rc == 11) {
+        const float tiny = 1.0e-12f;
+        if (d2 > 0.f) {
+          const float numer = (dmax * dmax + epsq) * d2 + 2.f * d2 * d2 * dmax;
+          const float denom = d2 * (dmax * dmax + 2.f * d2 * d2 + dmax * d2 + epsq);
+          lm[k] = fmin2(numer / (denom + tiny), lm[k]);
+        } else if (d2 < 0.f) {
+          const float numer = (dmin * dmin + epsq) * d2 + 2.f * d2 * d2 * dmin;
+          const float denom = d2 * (dmin * dmin + 2.f * d2 * d2 + dmin * d2 + epsq);
+          lm[k] = fmin2(numer / (denom + tiny), lm[k]);
+        }
+      } else {
+        if (d2 > 0.f) lm[k] = fmin2(fmin2(1.f, dmax / d2), lm[k]);
+        else if (d2 < 0.f) lm[k] = fmin2(fmin2(1.f, dmin / d2), lm[k]);
+      }
+    }
+    if (velo) {
+      const float off[3] = {-dx, -dy, -dz};
+      float sh[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        float s = 0.f;
+        s = s + G[a] * off[0];
+        s = s + G[a + 3] * off[1];
+        s = s + G[a + 6] * off[2];
+        sh[a] = s;
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        float pr = 0.f;
+        pr = pr + A[3 * j] * sh[0];
+        pr = pr + A[3 * j + 1] * sh[1];
+        pr = pr + A[3 * j + 2] * sh[2];
+        if (pr > 0.f) al[j] = fmin2(al[j], dmx[j] / pr);
+        else if (pr < 0.f) al[j] = fmin2(al[j], dmn[j] / pr);
+      }
+    }
+  }
+  if (velo) {
+    float mx = fabsf(ev[0]);
+    mx = fmax2(mx, fabsf(ev[1]));
+    mx = fmax2(mx, fabsf(ev[2]));
+    const float scale = 1.0e-3f * mx;
+    const bool e12 = (ev[1] - ev[0] <= scale), e23 = (ev[2] - ev[1] <= scale);
+    if (e12 && e23) {
+      const float m = fmin2(fmin2(al[0], al[1]), al[2]);
+      al[0] = al[1] = al[2] = m;
+    } else if (e12) {
+      const float m = fmin2(al[0], al[1]);
+      al[0] = al[1] = m;
+    } else if (e23) {
+      const float m = fmin2(al[1], al[2]);
+      al[1] = al[2] = m;
+    }
+    // G <- A diag(alpha) A^T G
+    float Rm[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float s = 0.f;
+        s = s + A[3 * j] * G[3 * c];
+        s = s + A[3 * j + 1] * G[1 + 3 * c];
+        s = s + A[3 * j + 2] * G[2 + 3 * c];
+        Rm[j + 3 * c] = al[j] * s;
+      }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float s = 0.f;
+        s = s + A[a] * Rm[3 * c];
+        s = s + A[a + 3] * Rm[1 + 3 * c];
+        s = s + A[a + 6] * Rm[2 + 3 * c];
+        g[3 * (1 + a) + c] = s;
+      }
+    lm[1] = lm[2] = lm[3] = 1.f;
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    g[3 * k] = lm[k] * g[3 * k];
+    g[3 * k + 1] = lm[k] * g[3 * k + 1];
+    g[3 * k + 2] = lm[k] * g[3 * k + 2];
+  }
+  return sum;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimit(View<R> V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   R g[15];
-  gradLimitCell(V, PlainLoad<R>{V}, i, g);
+  if constexpr (Layout<R>::packed) {
+    __shared__ float dc[3 * kMaxCellFaces * kBlock];
+    gradLimitPacked<false>(V, i, g, dc + threadIdx.x);
+  } else {
+    gradLimitCell(V, PlainLoad<R>{V}, i, g);
+  }
   storeGrad(V, i, g);
 }
 
@@ -469,14 +749,19 @@ __device__ inline double cellDtPrim(const View<R> &V, int i) {
   for (int e = cb; e < ce; ++e) {
     const int code = V.cfEnt[e];
     if (code >= 0) {
-      const int f = code >> 1, nb = (code & 1) ? V.fc1[f] : V.fc2[f];
+      const int f = code >> 1;
+      int c1, c2;
+      faceCells(V, f, c1, c2);
+      const int nb = (code & 1) ? c1 : c2;
       R qj[5];
       ld.prim5(nb, qj);
       const float rj = (float)qj[0];
       const float uj = (float)qj[1], vj = (float)qj[2], wj = (float)qj[3];
       const float aj = sqrtf(g * (float)qj[4] / rj);
-      const float vc = 0.5f * ((ui + uj) * (float)V.fnx[f] + (vi + vj) * (float)V.fny[f] + (wi + wj) * (float)V.fnz[f]);
-      sum += (fabsf(vc) + 0.5f * (ai + aj)) * (float)V.fnm[f];
+      R nx, ny, nz, nm;
+      faceNormal(V, f, nx, ny, nz, nm);
+      const float vc = 0.5f * ((ui + uj) * (float)nx + (vi + vj) * (float)ny + (wi + wj) * (float)nz);
+      sum += (fabsf(vc) + 0.5f * (ai + aj)) * (float)nm;
     } else {
       const int b = -code - 1;
       const float vc = ui * (float)V.bnx[b] + vi * (float)V.bny[b] + wi * (float)V.bnz[b];
@@ -492,14 +777,33 @@ template <typename R>
 __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> V) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double dt = 1.79769313486231571e308;
-  if (i < V.nc && V.sc->finished >= 0) {
-    if (V.p.spaceOrder > 1) {
+  if constexpr (Layout<R>::packed) {
+    __shared__ float dc[3 * kMaxCellFaces * kBlock];
+    if (i < V.nc && V.sc->finished >= 0) {
       R g[15];
-      gradLimitCell(V, PlainLoad<R>{V}, i, g);
-      storeGrad(V, i, g);
+      const float sum = gradLimitPacked<true>(V, i, g, dc + threadIdx.x);
+      if (V.p.spaceOrder > 1) storeGrad(V, i, g);
+      dt = V.vol[i] / (double)sum;
     }
-    dt = cellDtPrim(V, i);
+  } else {
+    if (i < V.nc && V.sc->finished >= 0) {
+      if (V.p.spaceOrder > 1) {
+        R g[15];
+        gradLimitCell(V, PlainLoad<R>{V}, i, g);
+        storeGrad(V, i, g);
+      }
+      dt = cellDtPrim(V, i);
+    }
   }
+  blockMinDt(V.sc, dt);
+}
+
+// Time step alone from the primitive state (mixed mode).
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kCellDtPrim(View<R> V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double dt = 1.79769313486231571e308;
+  if (i < V.nc) dt = cellDtPrim(V, i);
   blockMinDt(V.sc, dt);
 }
 
@@ -648,23 +952,28 @@ __device__ inline void faceFluxEval(const View<R> &V, const L &ld, int t, typena
   using H = typename L::H;
   const Params &P = V.p;
   if (t < V.nf) {
-    const int f = t, c1 = V.fc1[f], c2 = V.fc2[f];
+    const int f = t;
+    int c1, c2;
+    faceCells(V, f, c1, c2);
+    R nx, ny, nz, nm;
+    faceNormal(V, f, nx, ny, nz, nm);
     if (P.spaceOrder == 1) {
       H cl[5], cr[5], dl[3], dr[3], fd[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) { cl[k] = ld.cv(k, c1); cr[k] = ld.cv(k, c2); }
 #pragma unroll
       for (int k = 0; k < 3; ++k) { dl[k] = ld.dv(k, c1); dr[k] = ld.dv(k, c2); }
-      riemann1(P, cl, dl, cr, dr, H((double)V.fnx[f]), H((double)V.fny[f]), H((double)V.fnz[f]), H((double)V.fnm[f]),
-               fd);
+      riemann1(P, cl, dl, cr, dr, H((double)nx), H((double)ny), H((double)nz), H((double)nm), fd);
 #pragma unroll
       for (int k = 0; k < 5; ++k) flx[k] = cvt<S>(fd[k]);
     } else {
-      const size_t nf = V.nf;
       S Lf[5], Rt[5], irl, irr;
-      faceState(V, ld, c1, S(V.dL[f]), S(V.dL[nf + f]), S(V.dL[2 * nf + f]), Lf, irl);
-      faceState(V, ld, c2, S(V.dR[f]), S(V.dR[nf + f]), S(V.dR[2 * nf + f]), Rt, irr);
-      riemann2(P, S(V.fnx[f]), S(V.fny[f]), S(V.fnz[f]), S(V.fnm[f]), Lf, irl, Rt, irr, flx);
+      R dl[3], dr[3];
+      faceOffset(V, f, 0, dl);
+      faceOffset(V, f, 1, dr);
+      faceState(V, ld, c1, S(dl[0]), S(dl[1]), S(dl[2]), Lf, irl);
+      faceState(V, ld, c2, S(dr[0]), S(dr[1]), S(dr[2]), Rt, irr);
+      riemann2(P, S(nx), S(ny), S(nz), S(nm), Lf, irl, Rt, irr, flx);
     }
   } else {
     const int b = t - V.nf, c = V.bcell[b], ip = V.bpatch[b];
@@ -694,6 +1003,21 @@ __global__ void __launch_bounds__(kBlock, MinBlocksFlux<R>::v) kFaceFlux(View<R>
   const int nfT = V.nf + V.nb;
   if (t >= nfT) return;
   R flx[5];
+  if constexpr (Layout<R>::packed) {
+    if (t < V.nf && V.p.spaceOrder > 1) {
+      // one 48-byte face record, one 32-byte prim and one 64-byte gradient
+      // record per side
+      const float *fr = V.fpk + 12 * (size_t)t;
+      const float4 F0 = ld4(fr), F1 = ld4(fr + 4), F2 = ld4(fr + 8);
+      const PlainLoad<R> ld{V};
+      float Lf[5], Rt[5], irl, irr;
+      faceState(V, ld, __float_as_int(F2.z), F1.x, F1.y, F1.z, Lf, irl);
+      faceState(V, ld, __float_as_int(F2.w), F1.w, F2.x, F2.y, Rt, irr);
+      riemann2(V.p, F0.x, F0.y, F0.z, F0.w, Lf, irl, Rt, irr, flx);
+      storeFlux(V, (size_t)nfT, t, flx);
+      return;
+    }
+  }
   faceFluxEval(V, PlainLoad<R>{V}, t, flx);
   storeFlux(V, (size_t)nfT, t, flx);
 }
@@ -779,7 +1103,8 @@ __device__ inline void afterUpdate(const View<R> &V, int i, double *cv, double &
   }
 }
 
-// Mixed-mode RKUpdateMP + RFLU_SetVarsContWrapper + AfterUpdateMP of one cell.
+// Mixed-mode RKUpdateMP + RFLU_SetVarsContWrapper + AfterUpdateMP of one cell
+// (T and c only when a kernel of the step reads them, P.dvPOnly == 0).
 // The increment adtv*(rhs - grk*rhsSum) is formed in FP32 (the rhs is FP32)
 // and added to the FP64 master cv; p is recovered in FP64 (it is a difference
 // of two nearly equal energies at high Mach numbers).  The FP64 reciprocal of
@@ -816,14 +1141,15 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
     }
     cv[k] = cv[k] - (double)inc;
   }
-  // 1/rho: FP32 seed y, then y + y*(1 - rho*y)
-  double ir = (double)(1.0f / (float)cv[0]);
+  // 1/rho: FP32 seed y (also the FP32 velocities' reciprocal), then
+  // y + y*(1 - rho*y) in FP64
+  const float rf = (float)cv[0];
+  const float irf = 1.0f / rf;
+  double ir = (double)irf;
   ir = fma(ir, fma(-cv[0], ir, 1.0), ir);
   const double msq = cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3];
   double ke = 0.5 * msq * ir;
   double pr = (P.gRT - 1.0) * (cv[4] - ke);
-  const float irf = (float)ir;
-  const float rf = (float)cv[0];
   const float uf = (float)cv[1] * irf, vf = (float)cv[2] * irf, wf = (float)cv[3] * irf;
   if (isnan(rf) || isnan(uf) || isnan(vf) || isnan(wf) || isnan((float)pr)) {
     atomicAdd(&V.sc->nanCells, 1ull);
@@ -835,16 +1161,17 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
     cv[4] = 1.0e4 * cv[0] + ke;
     pr = (P.gRT - 1.0) * (cv[4] - ke);
   }
-  const double c2 = P.gRT * pr * ir;
-  // sqrt(c2): FP32 seed y ~ 1/sqrt(c2), h = c2*y, then h + h*(1 - h*y)/2
-  const double y = (double)rsqrtf((float)c2);
-  const double h = c2 * y;
-  const double cs = fma(0.5 * h, fma(-h, y, 1.0), h);
 #pragma unroll
   for (int k = 0; k < 5; ++k) V.cv[k * n + i] = cv[k];
   V.dv[i] = pr;
-  V.dv[n + i] = pr * ir * P.igcR;
-  V.dv[2 * n + i] = cs;
+  if (!P.dvPOnly) {
+    const double c2 = P.gRT * pr * ir;
+    // sqrt(c2): FP32 seed y ~ 1/sqrt(c2), h = c2*y, then h + h*(1 - h*y)/2
+    const double y = (double)rsqrtf((float)c2);
+    const double h = c2 * y;
+    V.dv[n + i] = pr * ir * P.igcR;
+    V.dv[2 * n + i] = fma(0.5 * h, fma(-h, y, 1.0), h);
+  }
   storePrimRec(V, i, (R)rf, (R)uf, (R)vf, (R)wf, (R)pr);
 }
 
@@ -859,14 +1186,14 @@ __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, c
   const size_t n = V.nc;
   R rhs[5];
   gatherRhs(V, (const R *)V.flux, i, rhs);
-  const double fac = P.ark[iStage - 1] * (*dtp);
-  const double grk = P.grk[iStage - 1];
   double cv[5];
   loadCv(V, i, cv);
   if constexpr (!Ref<R>::on) {
-    mixedUpdate(V, i, iStage, (float)fac, (float)grk, rhs, cv);
+    mixedUpdate(V, i, iStage, P.arkF[iStage - 1] * (float)(*dtp), P.grkF[iStage - 1], rhs, cv);
     return;
   }
+  const double fac = P.ark[iStage - 1] * (*dtp);
+  const double grk = P.grk[iStage - 1];
   const double adtv = fac / V.vol[i];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
@@ -995,9 +1322,12 @@ struct Launch {
   static void gatherUpdate(const View<R> &V, int iStage, const double *dtp, cudaStream_t s) {
     kGatherUpdate<R><<<blocks(V.nc), kBlock, 0, s>>>(V, iStage, dtp);
   }
+  // The FP64 modes: RFLU_TimeStepInviscid in FP64 from cv and dv; the mixed
+  // mode: the FP32 sum from the primitive state, as its steps take it.
   static void timestep(const View<R> &V, cudaStream_t s) {
     kStepBegin<R><<<1, 1, 0, s>>>(V);
-    kCellDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+    if (Ref<R>::on) kCellDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+    else kCellDtPrim<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
     kDtFinalize<R><<<1, 1, 0, s>>>(V);
   }
   // Time-step reduction + gradients of the first stage of a step.  The FP64
