@@ -207,6 +207,12 @@ struct Ctx : CtxBase {
   }
 
   int create(const rflu_grid_desc *g, const rflu_num_desc *num);
+  int buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cfEnt, const std::vector<int> &stOff,
+                 const std::vector<int> &stIdx, const std::vector<int> &fc1, const std::vector<int> &fc2,
+                 const std::vector<double> &fnx, const std::vector<double> &fny, const std::vector<double> &fnz,
+                 const std::vector<double> &fnm, const std::vector<double> &dL, const std::vector<double> &dR,
+                 const std::vector<double> &bnx, const std::vector<double> &bny, const std::vector<double> &bnz,
+                 const std::vector<double> &bnm);
   int checkLaunch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -532,6 +538,103 @@ struct Ctx : CtxBase {
   int nPatches = 0;
 };
 
+// Tiles of the mixed-mode gradient kernel (ctx.h): per tile of kTile
+// consecutive cells, the sorted list of halo cells its stencils and faces
+// reach; the local id of every stencil member; and the entry-major face
+// arrays feD/feN with the neighbour's local id as the tag.  Left untiled
+// (V.tiled = 0) when a tile would stage more records than shared memory or a
+// 16-bit id holds.
+template <typename R>
+int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cfEnt, const std::vector<int> &stOff,
+                       const std::vector<int> &stIdx, const std::vector<int> &fc1, const std::vector<int> &fc2,
+                       const std::vector<double> &fnx, const std::vector<double> &fny,
+                       const std::vector<double> &fnz, const std::vector<double> &fnm,
+                       const std::vector<double> &dL, const std::vector<double> &dR,
+                       const std::vector<double> &bnx, const std::vector<double> &bny,
+                       const std::vector<double> &bnz, const std::vector<double> &bnm) {
+  const int nc = V.nc, nf = V.nf, nb = V.nb;
+  const int nTiles = (nc + kTile - 1) / kTile;
+  std::vector<int> haloOff(nTiles + 1, 0), haloIdx;
+  std::vector<unsigned short> stLoc(stIdx.size());
+  std::vector<int> entLoc(cfEnt.size(), -1);
+  std::vector<int> mark(nc, -1);
+  int maxRecs = 0, cfW = 0;
+  for (int i = 0; i < nc; ++i) cfW = std::max(cfW, cfOff[i + 1] - cfOff[i]);
+  auto other = [&](int e) {  // neighbour of a cell's interior face entry
+    const int f = cfEnt[e] >> 1;
+    return (cfEnt[e] & 1) ? fc1[f] : fc2[f];
+  };
+  for (int t = 0; t < nTiles; ++t) {
+    const int b0 = t * kTile, b1 = std::min(nc, b0 + kTile);
+    std::vector<int> halo;
+    auto visit = [&](int j) {
+      if ((j < b0 || j >= b1) && mark[j] != t) {
+        mark[j] = t;
+        halo.push_back(j);
+      }
+    };
+    for (int i = b0; i < b1; ++i) {
+      for (int s = stOff[i]; s < stOff[i + 1]; ++s) visit(stIdx[s]);
+      for (int e = cfOff[i]; e < cfOff[i + 1]; ++e)
+        if (cfEnt[e] >= 0) visit(other(e));
+    }
+    std::sort(halo.begin(), halo.end());
+    const int recs = kTile + (int)halo.size();
+    if (recs > 65535) return RFLU_OK;  // stays untiled
+    maxRecs = std::max(maxRecs, recs);
+    auto local = [&](int j) {
+      if (j >= b0 && j < b1) return j - b0;
+      return kTile + (int)(std::lower_bound(halo.begin(), halo.end(), j) - halo.begin());
+    };
+    for (int i = b0; i < b1; ++i) {
+      for (int s = stOff[i]; s < stOff[i + 1]; ++s) stLoc[s] = (unsigned short)local(stIdx[s]);
+      for (int e = cfOff[i]; e < cfOff[i + 1]; ++e)
+        if (cfEnt[e] >= 0) entLoc[e] = local(other(e));
+    }
+    haloIdx.insert(haloIdx.end(), halo.begin(), halo.end());
+    haloOff[t + 1] = (int)haloIdx.size();
+  }
+  // shared memory: 8 floats per record plus the face-offset cache
+  const size_t smem = sizeof(float) * (8 * (size_t)maxRecs + 3 * 6 * kTile);
+  int dev = 0, optin = 0;
+  RFLU_CUDA(cudaGetDevice(&dev));
+  RFLU_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem > (size_t)optin) return RFLU_OK;  // stays untiled
+  std::vector<float> feD(4 * (size_t)cfW * nc, 0.f), feN(4 * (size_t)cfW * nc, 0.f);
+  for (int i = 0; i < nc; ++i)
+    for (int k = 0; k < cfW; ++k) {
+      float *d = &feD[4 * ((size_t)k * nc + i)], *nn = &feN[4 * ((size_t)k * nc + i)];
+      int tag = INT_MIN;
+      const int e = cfOff[i] + k;
+      if (e < cfOff[i + 1]) {
+        const int code = cfEnt[e];
+        if (code >= 0) {
+          const int f = code >> 1;
+          const std::vector<double> &dd = (code & 1) ? dR : dL;
+          d[0] = (float)dd[f]; d[1] = (float)dd[(size_t)nf + f]; d[2] = (float)dd[2 * (size_t)nf + f];
+          nn[0] = (float)fnx[f]; nn[1] = (float)fny[f]; nn[2] = (float)fnz[f]; nn[3] = (float)fnm[f];
+          tag = entLoc[e];
+        } else {
+          const int b = -code - 1;
+          nn[0] = (float)bnx[b]; nn[1] = (float)bny[b]; nn[2] = (float)bnz[b]; nn[3] = (float)bnm[b];
+          tag = code;
+        }
+      }
+      std::memcpy(&d[3], &tag, sizeof(int));
+    }
+  (void)nb;
+  int rc = 0;
+  if ((rc = put<int>(&V.haloOff, haloOff))) return rc;
+  if ((rc = put<int>(&V.haloIdx, haloIdx))) return rc;
+  if ((rc = put<unsigned short>(&V.stLoc, stLoc))) return rc;
+  if ((rc = put<float>(&V.feD, feD))) return rc;
+  if ((rc = put<float>(&V.feN, feN))) return rc;
+  V.maxRecs = maxRecs;
+  V.cfW = cfW;
+  V.tiled = 1;
+  return RFLU_OK;
+}
+
 template <typename R>
 int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   const int nc = g->nCells, nf = g->nFaces, np = g->nPatches;
@@ -635,9 +738,9 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   // RFLU_ModDifferentiationCells.F90:983-1044) from the R factor and the
   // unit offset, in FP64 and in the reference's order of operations
   std::vector<int> stOff(nc + 1, 0), stIdx;
-  std::vector<double> wx, wy, wz, epsq(nc, 0.0), rcf;
+  std::vector<double> wx, wy, wz, epsq(nc, 0.0), lsq;
   const bool mixed = num->precision == RFLU_PREC_MIXED;
-  if (mixed && num->spaceOrder > 1) rcf.resize(6 * (size_t)nc);
+  if (mixed && num->spaceOrder > 1) lsq.resize(6 * (size_t)nc);
   if (num->spaceOrder > 1) {
     if (!g->c2csOff || !g->c2csMembs || !g->xyzMoms) return fail(RFLU_ERR_ARG, "rflu_gpu_create: ORDER 2 needs stencils");
     for (int i = 0; i < nc; ++i) {
@@ -650,8 +753,13 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
       const double c23 = -c22 * r23;
       const double c1111 = c11 * c11, c2222 = c22 * c22, c3333 = c33 * c33;
       if (mixed) {
-        rcf[i] = c1111; rcf[(size_t)nc + i] = c2222; rcf[2 * (size_t)nc + i] = c3333;
-        rcf[3 * (size_t)nc + i] = c12; rcf[4 * (size_t)nc + i] = c13; rcf[5 * (size_t)nc + i] = c23;
+        // w = L d / |d|^2 with the symmetric L of the weights' linear map
+        lsq[i] = c1111 + c12 * c12 * c2222 + c13 * c13 * c3333;
+        lsq[(size_t)nc + i] = c12 * c2222 + c13 * c23 * c3333;
+        lsq[2 * (size_t)nc + i] = c13 * c3333;
+        lsq[3 * (size_t)nc + i] = c2222 + c23 * c23 * c3333;
+        lsq[4 * (size_t)nc + i] = c23 * c3333;
+        lsq[5 * (size_t)nc + i] = c3333;
       }
       const double *xi = g->cofg + 3 * (size_t)o;
       for (int e = g->c2csOff[o]; e < g->c2csOff[o + 1]; ++e) {
@@ -736,7 +844,11 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   if (mixed) {
     // weights formed in the gradient kernel from the R factor and centroids
     PUT(V.cgx, cgx, R); PUT(V.cgy, cgy, R); PUT(V.cgz, cgz, R);
-    PUT(V.rcf, rcf, R); PUT(V.ivol, ivol, R);
+    PUT(V.lsq, lsq, R); PUT(V.ivol, ivol, R);
+    if (num->spaceOrder > 1) {
+      if ((rc = buildTiles(cfOff, cfEnt, stOff, stIdx, fc1, fc2, fnx, fny, fnz, fnm, dL, dR, bnx, bny, bnz, bnm)))
+        return rc;
+    }
   } else {
     PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
     PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
@@ -794,7 +906,8 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   if (num->precision != RFLU_PREC_MIXED) {
     if ((rc = alloc((char **)&work, workBytes))) return rc;
   }
-  return RFLU_OK;
+  ops->configure(V);
+  return checkLaunch("rflu_gpu_create");
 }
 
 }  // namespace rflu

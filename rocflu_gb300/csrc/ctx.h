@@ -47,6 +47,8 @@ struct Params {
 // floats per cell) = the 15 components in the order 3*var + dir and one pad;
 // flux = one float4 (mass and momentum) per face followed by the nT energy
 // fluxes.
+constexpr int kTile = 256;
+
 template <typename R> struct Layout {
   static constexpr bool packed = false;
   static constexpr int prim = 5, grad = 15;
@@ -82,13 +84,27 @@ struct View {
   const R *wx, *wy, *wz;
   const double *vol;
   const R *epsq;                    // Venkatakrishnan eps^2 = (vol^(1/3))^3 per cell
-  // mixed mode: LSQ weights are formed on the fly from the cell's R-factor
-  // coefficients (c1111, c2222, c3333, c12, c13, c23) and the members'
-  // centroids (read from the packed prim records), instead of streaming three
-  // weights per stencil member
+  // mixed mode: the LSQ weights w_j = L d_j / |d_j|^2 of a cell share one
+  // symmetric 3x3 matrix L (the product of the R-factor coefficients), so the
+  // gradient is L * sum_j (q_j - q_i) d_j / |d_j|^2 with d_j the centroid
+  // offset (centroids ride in the packed prim records)
   const R *cgx, *cgy, *cgz;         // cell centroids (FP32), written into prim
-  const R *rcf;                     // (6, nc) R-factor coefficients
+  const R *lsq;                     // (6, nc): Lxx, Lxy, Lxz, Lyy, Lyz, Lzz
   const R *ivol;                    // 1/vol (FP32), for the FP32 RK increment
+  // mixed mode, tiled gradient kernel: cells in tiles of kTile consecutive
+  // (Morton) cells; a tile's CTA stages the prim records of its cells and of
+  // the halo (the other cells its stencils and faces reach) in shared memory
+  // and addresses them by 16-bit local ids (own cells 0..kTile-1, halo after)
+  int tiled;                        // 0: the gather kernel instead
+  int maxRecs;                      // max staged records over the tiles
+  int cfW;                          // max faces per cell (entries of feD/feN)
+  const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids
+  const unsigned short *stLoc;      // local id of each stencil member (stIdx order)
+  // per cell-face entry, entry-major (entry k of cell i at [k*nc + i]), in
+  // the reference's face order: (dx, dy, dz, tag) with d = fc - cofg(i) and
+  // tag = local id of the neighbour (interior), -(b+1) (boundary face b) or
+  // INT_MIN (no entry); and the face's (nx, ny, nz, nm)
+  const float *feD, *feN;           // 4 floats per entry
   const int *refId;                 // renumbered -> reference (0-based) cell id
   // transposed stencil (FP64 modes): for cell j, the (cell i, entry s) pairs
   // of the stencils that contain j, for the adjoint of the LSQ gradient

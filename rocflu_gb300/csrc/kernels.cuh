@@ -489,47 +489,62 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
 // the same pass as the neighbour min/max; each face's offset fc - cofg is kept
 // in shared memory (dc, stride kBlock) for the limiter pass.  At most
 // kMaxCellFaces faces per cell (tetrahedra 4, prisms and pyramids 5,
-// hexahedra 6).  Returns the spectral-radius sum (kDt) or 0.
+// hexahedra 6).  With kTiled the cell's, its stencil members' and its face
+// neighbours' prim records come from the CTA's staged tile (recs, local ids)
+// and its faces from the entry-major arrays feD/feN; otherwise they are
+// gathered from global memory.  Returns the spectral-radius sum (kDt) or 0.
+//
+// LSQ gradient (RFLU_ComputeGradCellsFast_3D, modflu/
+// RFLU_ModDifferentiationCells.F90:983-1044): the reference's per-member
+// weights are w_j = L d_j / |d_j|^2 with L the cell's symmetric matrix of
+// R-factor products, so G = L * sum_j (q_j - q_i) d_j / |d_j|^2.
 constexpr int kMaxCellFaces = 6;
 
-template <bool kDt>
-__device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, float *dc) {
+__device__ inline void ldRec(const float *recs, int l, float *v) {
+  const float4 a = *reinterpret_cast<const float4 *>(recs + 8 * l);
+  const float4 b = *reinterpret_cast<const float4 *>(recs + 8 * l + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+template <bool kDt, bool kTiled>
+__device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, float *dc, const float *recs,
+                                        int li) {
   const Params &P = V.p;
   float rec[8];
-  ld8(V.prim + 8 * (size_t)i, rec);
+  if (kTiled) ldRec(recs, li, rec);
+  else ld8(V.prim + 8 * (size_t)i, rec);
   const float q[5] = {rec[0], rec[1], rec[2], rec[3], rec[4]};
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = 0.f;
   const bool second = P.spaceOrder > 1;
   if (second) {
-    // LSQ weights of RFLU_ComputeGradCellsFast_3D (:983-1044) in FP32 from
-    // the R-factor coefficients and the member's centroid
-    const size_t n = V.nc;
-    const float c1111 = V.rcf[i], c2222 = V.rcf[n + i], c3333 = V.rcf[2 * n + i];
-    const float c12 = V.rcf[3 * n + i], c13 = V.rcf[4 * n + i], c23 = V.rcf[5 * n + i];
     const int sb = V.stOff[i], se = V.stOff[i + 1];
 #pragma unroll 2
     for (int s = sb; s < se; ++s) {
       float r[8];
-      ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
-      float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
-      const float term = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
-      dx = term * dx;
-      dy = term * dy;
-      dz = term * dz;
-      const float t1 = c1111 * dx;
-      const float t2 = c2222 * (dy + c12 * dx);
-      const float t3 = c3333 * (dz + c23 * dy + c13 * dx);
-      const float wx = term * (t1 + c12 * t2 + c13 * t3);
-      const float wy = term * (t2 + c23 * t3);
-      const float wz = term * t3;
+      if (kTiled) ldRec(recs, V.stLoc[s], r);
+      else ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
+      const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+      const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+      const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         const float d = r[k] - q[k];
-        g[3 * k] = g[3 * k] + wx * d;
-        g[3 * k + 1] = g[3 * k + 1] + wy * d;
-        g[3 * k + 2] = g[3 * k + 2] + wz * d;
+        g[3 * k] = g[3 * k] + sx * d;
+        g[3 * k + 1] = g[3 * k + 1] + sy * d;
+        g[3 * k + 2] = g[3 * k + 2] + sz * d;
       }
+    }
+    const size_t n = V.nc;
+    const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
+    const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const float x = g[3 * k], y = g[3 * k + 1], z = g[3 * k + 2];
+      g[3 * k] = lxx * x + lxy * y + lxz * z;
+      g[3 * k + 1] = lxy * x + lyy * y + lyz * z;
+      g[3 * k + 2] = lxz * x + lyz * y + lzz * z;
     }
   }
   const int rc = P.reconst;
@@ -556,51 +571,77 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
   float sum = 0.f;
   int nfc = 0;
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
-  for (int e = cb; e < ce; ++e) {
-    const int code = V.cfEnt[e];
-    if (code >= 0) {
-      if (!lim && !kDt) continue;
-      const int f = code >> 1, side = code & 1;
-      const float *fr = V.fpk + 12 * (size_t)f;
-      const float4 F1 = ld4(fr + 4), F2 = ld4(fr + 8);
-      const int nb = side ? __float_as_int(F2.z) : __float_as_int(F2.w);
-      float x[8];
-      ld8(V.prim + 8 * (size_t)nb, x);
-      if (lim) {
+  // one face of the pass: neighbour record x, offset d of this cell's side
+  auto face = [&](const float *x, float d0, float d1, float d2) {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          vmin[k] = fmin2(vmin[k], x[k]);
-          vmax[k] = fmax2(vmax[k], x[k]);
-        }
-        if (velo) {
-          // A^T (u(c2) - u(c1)) seen from this cell = A^T (u(nb) - u(i))
-          const float du0 = x[1] - q[1], du1 = x[2] - q[2], du2 = x[3] - q[3];
+    for (int k = 0; k < 5; ++k) {
+      vmin[k] = fmin2(vmin[k], x[k]);
+      vmax[k] = fmax2(vmax[k], x[k]);
+    }
+    if (velo) {
+      // A^T (u(c2) - u(c1)) seen from this cell = A^T (u(nb) - u(i))
+      const float du0 = x[1] - q[1], du1 = x[2] - q[2], du2 = x[3] - q[3];
 #pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            float pr = 0.f;
-            pr = pr + A[3 * j] * du0;
-            pr = pr + A[3 * j + 1] * du1;
-            pr = pr + A[3 * j + 2] * du2;
-            dmn[j] = fmin2(dmn[j], pr);
-            dmx[j] = fmax2(dmx[j], pr);
-          }
+      for (int j = 0; j < 3; ++j) {
+        float pr = 0.f;
+        pr = pr + A[3 * j] * du0;
+        pr = pr + A[3 * j + 1] * du1;
+        pr = pr + A[3 * j + 2] * du2;
+        dmn[j] = fmin2(dmn[j], pr);
+        dmx[j] = fmax2(dmx[j], pr);
+      }
+    }
+    float *slot = dc + 3 * nfc * kBlock;
+    slot[0] = d0;
+    slot[kBlock] = d1;
+    slot[2 * kBlock] = d2;
+    ++nfc;
+  };
+  if (kTiled) {
+    const size_t n = V.nc;
+    for (int k = 0; k < ce - cb; ++k) {
+      const float4 D = ld4(V.feD + 4 * (k * n + i));
+      const int tag = __float_as_int(D.w);
+      if (tag >= 0) {
+        if (!lim && !kDt) continue;
+        float x[8];
+        ldRec(recs, tag, x);
+        if (lim) face(x, D.x, D.y, D.z);
+        if (kDt) {
+          const float4 N = ld4(V.feN + 4 * (k * n + i));
+          const float aj = sqrtf(gam * x[4] / x[0]);
+          const float vc = 0.5f * ((q[1] + x[1]) * N.x + (q[2] + x[2]) * N.y + (q[3] + x[3]) * N.z);
+          sum += (fabsf(vc) + 0.5f * (ai + aj)) * N.w;
         }
-        float *slot = dc + 3 * nfc * kBlock;
-        slot[0] = side ? F1.w : F1.x;
-        slot[kBlock] = side ? F2.x : F1.y;
-        slot[2 * kBlock] = side ? F2.y : F1.z;
-        ++nfc;
+      } else if (kDt) {
+        const float4 N = ld4(V.feN + 4 * (k * n + i));
+        const float vc = q[1] * N.x + q[2] * N.y + q[3] * N.z;
+        sum += (fabsf(vc) + ai) * N.w;
       }
-      if (kDt) {
-        const float4 F0 = ld4(fr);
-        const float aj = sqrtf(gam * x[4] / x[0]);
-        const float vc = 0.5f * ((q[1] + x[1]) * F0.x + (q[2] + x[2]) * F0.y + (q[3] + x[3]) * F0.z);
-        sum += (fabsf(vc) + 0.5f * (ai + aj)) * F0.w;
+    }
+  } else {
+    for (int e = cb; e < ce; ++e) {
+      const int code = V.cfEnt[e];
+      if (code >= 0) {
+        if (!lim && !kDt) continue;
+        const int f = code >> 1, side = code & 1;
+        const float *fr = V.fpk + 12 * (size_t)f;
+        const float4 F1 = ld4(fr + 4), F2 = ld4(fr + 8);
+        const int nb = side ? __float_as_int(F2.z) : __float_as_int(F2.w);
+        float x[8];
+        ld8(V.prim + 8 * (size_t)nb, x);
+        if (lim) face(x, side ? F1.w : F1.x, side ? F2.x : F1.y, side ? F2.y : F1.z);
+        if (kDt) {
+          const float4 F0 = ld4(fr);
+          const float aj = sqrtf(gam * x[4] / x[0]);
+          const float vc = 0.5f * ((q[1] + x[1]) * F0.x + (q[2] + x[2]) * F0.y + (q[3] + x[3]) * F0.z);
+          sum += (fabsf(vc) + 0.5f * (ai + aj)) * F0.w;
+        }
+      } else if (kDt) {
+        const int b = -code - 1;
+        const float vc = q[1] * V.bnx[b] + q[2] * V.bny[b] + q[3] * V.bnz[b];
+        sum += (fabsf(vc) + ai) * V.bnm[b];
       }
-    } else if (kDt) {
-      const int b = -code - 1;
-      const float vc = q[1] * V.bnx[b] + q[2] * V.bny[b] + q[3] * V.bnz[b];
-      sum += (fabsf(vc) + ai) * V.bnm[b];
     }
   }
   if (!lim) return sum;
@@ -709,7 +750,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimit(View<R> V)
   R g[15];
   if constexpr (Layout<R>::packed) {
     __shared__ float dc[3 * kMaxCellFaces * kBlock];
-    gradLimitPacked<false>(V, i, g, dc + threadIdx.x);
+    gradLimitPacked<false, false>(V, i, g, dc + threadIdx.x, nullptr, 0);
   } else {
     gradLimitCell(V, PlainLoad<R>{V}, i, g);
   }
@@ -730,6 +771,48 @@ __device__ inline void blockMinDt(Scalars *sc, double dt) {
     for (int w = 1; w < kBlock / 32; ++w) m = fmin(m, wmin[w]);
     if (m > 0.0) atomicMin(&sc->dtBits, (unsigned long long)__double_as_longlong(m));
     else atomicMin(&sc->dtBits, 0ull);
+  }
+}
+
+// Tiled mixed-mode gradient + limiter (+ time step with kDt): one CTA per
+// tile of kTile consecutive cells.  The CTA first copies the prim records of
+// its cells (contiguous) and of its halo into shared memory, so each record
+// leaves L2 once per tile instead of once per stencil reference.
+static_assert(kTile == kBlock, "one thread per cell of a tile");
+
+template <typename R>
+inline size_t tileSmemBytes(const View<R> &V) {
+  return sizeof(float) * (8 * (size_t)V.maxRecs + 3 * kMaxCellFaces * kBlock);
+}
+
+template <typename R, bool kDt>
+__global__ void __launch_bounds__(kBlock, 4) kGradTile(View<R> V) {
+  if constexpr (Layout<R>::packed) {
+    extern __shared__ float4 tileSmem[];
+    float *recs = reinterpret_cast<float *>(tileSmem);
+    float *dc = recs + 8 * (size_t)V.maxRecs;
+    const int base = blockIdx.x * kTile;
+    const int nIn = min(kTile, V.nc - base);
+    const int hb = V.haloOff[blockIdx.x], nh = V.haloOff[blockIdx.x + 1] - hb;
+    for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
+      const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
+      const int dst = r < nIn ? r : kTile + (r - nIn);
+      float v[8];
+      ld8(V.prim + 8 * (size_t)src, v);
+      float4 *d4 = reinterpret_cast<float4 *>(recs + 8 * (size_t)dst);
+      d4[0] = make_float4(v[0], v[1], v[2], v[3]);
+      d4[1] = make_float4(v[4], v[5], v[6], v[7]);
+    }
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    double dt = 1.79769313486231571e308;
+    if (i < V.nc && (!kDt || V.sc->finished >= 0)) {
+      float g[15];
+      const float sum = gradLimitPacked<kDt, true>(V, i, g, dc + threadIdx.x, recs, threadIdx.x);
+      storeGrad(V, i, g);
+      if (kDt) dt = V.vol[i] / (double)sum;
+    }
+    if (kDt) blockMinDt(V.sc, dt);
   }
 }
 
@@ -781,7 +864,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> 
     __shared__ float dc[3 * kMaxCellFaces * kBlock];
     if (i < V.nc && V.sc->finished >= 0) {
       R g[15];
-      const float sum = gradLimitPacked<true>(V, i, g, dc + threadIdx.x);
+      const float sum = gradLimitPacked<true, false>(V, i, g, dc + threadIdx.x, nullptr, 0);
       if (V.p.spaceOrder > 1) storeGrad(V, i, g);
       dt = V.vol[i] / (double)sum;
     }
@@ -1313,7 +1396,18 @@ template <typename R>
 struct Launch {
   static void initState(const View<R> &V, cudaStream_t s) { kInitState<R><<<blocks(V.nc), kBlock, 0, s>>>(V); }
   static void gradLimit(const View<R> &V, cudaStream_t s) {
-    if (V.p.spaceOrder > 1) kGradLimit<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+    if (V.p.spaceOrder < 2) return;
+    if (V.tiled) kGradTile<R, false><<<blocks(V.nc), kBlock, tileSmemBytes(V), s>>>(V);
+    else kGradLimit<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+  }
+  // Kernel attributes that depend on the mesh (shared memory of the tiled
+  // kernels); called once at set-up, outside any stream capture.
+  static void configure(const View<R> &V) {
+    if (V.tiled) {
+      const int b = (int)tileSmemBytes(V);
+      cudaFuncSetAttribute(kGradTile<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+      cudaFuncSetAttribute(kGradTile<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    }
   }
   static void faceFlux(const View<R> &V, cudaStream_t s) {
     kFaceFlux<R><<<blocks((long long)V.nf + V.nb), kBlock, 0, s>>>(V);
@@ -1340,7 +1434,8 @@ struct Launch {
       gradLimit(V, s);
     } else {
       kStepBegin<R><<<1, 1, 0, s>>>(V);
-      kGradLimitDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+      if (V.tiled) kGradTile<R, true><<<blocks(V.nc), kBlock, tileSmemBytes(V), s>>>(V);
+      else kGradLimitDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
       kDtFinalize<R><<<1, 1, 0, s>>>(V);
     }
   }
