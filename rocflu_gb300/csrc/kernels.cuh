@@ -1186,6 +1186,19 @@ __device__ inline void afterUpdate(const View<R> &V, int i, double *cv, double &
   }
 }
 
+// Which stages read and which write the accumulated residual rhsSum
+// (RkUpdateGeneric: classical RK4 sums the stage residuals, Wray's scheme
+// keeps the previous one).  All five components are loaded before any is
+// stored, so the loads are not ordered behind the stores.
+struct RkAccess {
+  bool rd, wr;
+  __device__ RkAccess(const Params &P, int iStage) {
+    if (P.rkScheme == 1) { rd = iStage > 1; wr = iStage < P.nrkSteps; }
+    else if (P.rkScheme == 2) { rd = iStage > 1; wr = iStage < 3; }
+    else { rd = false; wr = false; }
+  }
+};
+
 // Mixed-mode RKUpdateMP + RFLU_SetVarsContWrapper + AfterUpdateMP of one cell
 // (T and c only when a kernel of the step reads them, P.dvPOnly == 0).
 // The increment adtv*(rhs - grk*rhsSum) is formed in FP32 (the rhs is FP32)
@@ -1203,26 +1216,35 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
   const Params &P = V.p;
   const size_t n = V.nc;
   const float adtv = fac * (float)V.ivol[i];
+  RkAccess ra(P, iStage);
+  float rs[5];
+  if (ra.rd) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) rs[k] = (float)V.rhsSum[k * n + i];
+  }
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const float r = (float)rhs[k];
-    R *rs = &V.rhsSum[k * n + i];
     float inc;
     switch (P.rkScheme) {
       case 1:
-        if (iStage == 1) { inc = adtv * r; *rs = r; }
-        else if (iStage == P.nrkSteps) inc = adtv * (r + (float)*rs);
-        else { inc = adtv * r; *rs = (float)*rs + grk * r; }
+        if (iStage == 1) { inc = adtv * r; rs[k] = r; }
+        else if (iStage == P.nrkSteps) inc = adtv * (r + rs[k]);
+        else { inc = adtv * r; rs[k] = rs[k] + grk * r; }
         break;
       case 2:
-        if (iStage == 1) { inc = adtv * r; *rs = r; }
-        else if (iStage == 2) { inc = adtv * (r - grk * (float)*rs); *rs = r; }
-        else inc = adtv * (r - grk * (float)*rs);
+        if (iStage == 1) { inc = adtv * r; rs[k] = r; }
+        else if (iStage == 2) { inc = adtv * (r - grk * rs[k]); rs[k] = r; }
+        else inc = adtv * (r - grk * rs[k]);
         break;
       default:
         inc = adtv * r;
     }
     cv[k] = cv[k] - (double)inc;
+  }
+  if (ra.wr) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) V.rhsSum[k * n + i] = (R)rs[k];
   }
   // 1/rho: FP32 seed y (also the FP32 velocities' reciprocal), then
   // y + y*(1 - rho*y) in FP64
@@ -1278,24 +1300,33 @@ __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, c
   const double fac = P.ark[iStage - 1] * (*dtp);
   const double grk = P.grk[iStage - 1];
   const double adtv = fac / V.vol[i];
+  RkAccess ra(P, iStage);
+  R rs[5];
+  if (ra.rd) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) rs[k] = V.rhsSum[k * n + i];
+  }
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const double r = (double)rhs[k];
-    R *rs = &V.rhsSum[k * n + i];
     switch (P.rkScheme) {
       case 1:
-        if (iStage == 1) { cv[k] = cv[k] - adtv * r; *rs = rhs[k]; }
-        else if (iStage == P.nrkSteps) cv[k] = cv[k] - adtv * (r + (double)*rs);
-        else { cv[k] = cv[k] - adtv * r; *rs = (R)((double)*rs + grk * r); }
+        if (iStage == 1) { cv[k] = cv[k] - adtv * r; rs[k] = rhs[k]; }
+        else if (iStage == P.nrkSteps) cv[k] = cv[k] - adtv * (r + (double)rs[k]);
+        else { cv[k] = cv[k] - adtv * r; rs[k] = (R)((double)rs[k] + grk * r); }
         break;
       case 2:
-        if (iStage == 1) { cv[k] = cv[k] - adtv * r; *rs = rhs[k]; }
-        else if (iStage == 2) { cv[k] = cv[k] - adtv * (r - grk * (double)*rs); *rs = rhs[k]; }
-        else cv[k] = cv[k] - adtv * (r - grk * (double)*rs);
+        if (iStage == 1) { cv[k] = cv[k] - adtv * r; rs[k] = rhs[k]; }
+        else if (iStage == 2) { cv[k] = cv[k] - adtv * (r - grk * (double)rs[k]); rs[k] = rhs[k]; }
+        else cv[k] = cv[k] - adtv * (r - grk * (double)rs[k]);
         break;
       default:
         cv[k] = cv[k] - adtv * r;
     }
+  }
+  if (ra.wr) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) V.rhsSum[k * n + i] = rs[k];
   }
   double pr, tp, cs;
   dependentVars(P, cv, pr, tp, cs);
