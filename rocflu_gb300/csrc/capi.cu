@@ -594,8 +594,14 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
     haloIdx.insert(haloIdx.end(), halo.begin(), halo.end());
     haloOff[t + 1] = (int)haloIdx.size();
   }
-  // shared memory: 8 floats per record plus the face-offset cache
-  const size_t smem = sizeof(float) * (8 * (size_t)maxRecs + 3 * 6 * kTile);
+  int maxTileSt = 0;
+  for (int t = 0; t < nTiles; ++t) {
+    const int b0 = t * kTile, b1 = std::min(nc, b0 + kTile);
+    maxTileSt = std::max(maxTileSt, stOff[b1] - stOff[b0]);
+  }
+  stLoc.resize(stLoc.size() + 16, 0);  // whole 16-byte words past the last tile
+  // shared memory: 8 floats per record, the face-offset cache and the ids
+  const size_t smem = sizeof(float) * (8 * (size_t)maxRecs + 3 * 6 * kTile) + 16 * (((size_t)maxTileSt + 7) / 8 + 1);
   int dev = 0, optin = 0;
   RFLU_CUDA(cudaGetDevice(&dev));
   RFLU_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -630,6 +636,7 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
   if ((rc = put<float>(&V.feD, feD))) return rc;
   if ((rc = put<float>(&V.feN, feN))) return rc;
   V.maxRecs = maxRecs;
+  V.maxTileSt = maxTileSt;
   V.cfW = cfW;
   V.tiled = 1;
   return RFLU_OK;

@@ -97,9 +97,11 @@ struct View {
   // and addresses them by 16-bit local ids (own cells 0..kTile-1, halo after)
   int tiled;                        // 0: the gather kernel instead
   int maxRecs;                      // max staged records over the tiles
+  int maxTileSt;                    // max stencil entries of a tile's cells
   int cfW;                          // max faces per cell (entries of feD/feN)
   const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids
-  const unsigned short *stLoc;      // local id of each stencil member (stIdx order)
+  const unsigned short *stLoc;      // local id of each stencil member (stIdx order),
+                                    // 16-byte aligned and padded by 8 ids
   // per cell-face entry, entry-major (entry k of cell i at [k*nc + i]), in
   // the reference's face order: (dx, dy, dz, tag) with d = fc - cofg(i) and
   // tag = local id of the neighbour (interior), -(b+1) (boundary face b) or

@@ -36,7 +36,7 @@ template <> struct Ref<double> { static constexpr bool on = true; };
 template <typename R> struct MinBlocks { static constexpr int v = 1; };
 template <> struct MinBlocks<float> { static constexpr int v = 4; };
 template <typename R> struct MinBlocksFlux { static constexpr int v = 1; };
-template <> struct MinBlocksFlux<float> { static constexpr int v = 3; };
+template <> struct MinBlocksFlux<float> { static constexpr int v = 4; };
 
 // ---------------------------------------------------------------------------
 // Dependent variables of one cell from cv: RFLU_SetDependentVars, TCPERF
@@ -509,7 +509,7 @@ __device__ inline void ldRec(const float *recs, int l, float *v) {
 
 template <bool kDt, bool kTiled>
 __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, float *dc, const float *recs,
-                                        int li) {
+                                        int li, const unsigned short *stSm = nullptr, int stBase = 0) {
   const Params &P = V.p;
   float rec[8];
   if (kTiled) ldRec(recs, li, rec);
@@ -523,7 +523,7 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
 #pragma unroll 2
     for (int s = sb; s < se; ++s) {
       float r[8];
-      if (kTiled) ldRec(recs, V.stLoc[s], r);
+      if (kTiled) ldRec(recs, stSm[s - stBase], r);
       else ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
       const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
       const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
@@ -780,9 +780,13 @@ __device__ inline void blockMinDt(Scalars *sc, double dt) {
 // leaves L2 once per tile instead of once per stencil reference.
 static_assert(kTile == kBlock, "one thread per cell of a tile");
 
+// Shared memory of a tile: the staged records, the face-offset cache, and
+// the tile's stencil ids copied in 16-byte words (maxTileSt ids plus the
+// misalignment of the first word).
 template <typename R>
 inline size_t tileSmemBytes(const View<R> &V) {
-  return sizeof(float) * (8 * (size_t)V.maxRecs + 3 * kMaxCellFaces * kBlock);
+  return sizeof(float) * (8 * (size_t)V.maxRecs + 3 * kMaxCellFaces * kBlock) +
+         16 * (((size_t)V.maxTileSt + 7) / 8 + 1);
 }
 
 template <typename R, bool kDt>
@@ -791,9 +795,14 @@ __global__ void __launch_bounds__(kBlock, 4) kGradTile(View<R> V) {
     extern __shared__ float4 tileSmem[];
     float *recs = reinterpret_cast<float *>(tileSmem);
     float *dc = recs + 8 * (size_t)V.maxRecs;
+    uint4 *stWords = reinterpret_cast<uint4 *>(dc + 3 * kMaxCellFaces * kBlock);
     const int base = blockIdx.x * kTile;
     const int nIn = min(kTile, V.nc - base);
     const int hb = V.haloOff[blockIdx.x], nh = V.haloOff[blockIdx.x + 1] - hb;
+    // the tile's stencil ids, whole 16-byte words of stLoc (padded at the end)
+    const int w0 = V.stOff[base] >> 3, w1 = (V.stOff[base + nIn] + 7) >> 3;
+    const uint4 *src4 = reinterpret_cast<const uint4 *>(V.stLoc);
+    for (int w = w0 + (int)threadIdx.x; w < w1; w += kBlock) stWords[w - w0] = src4[w];
     for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
       const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
       const int dst = r < nIn ? r : kTile + (r - nIn);
@@ -808,7 +817,8 @@ __global__ void __launch_bounds__(kBlock, 4) kGradTile(View<R> V) {
     double dt = 1.79769313486231571e308;
     if (i < V.nc && (!kDt || V.sc->finished >= 0)) {
       float g[15];
-      const float sum = gradLimitPacked<kDt, true>(V, i, g, dc + threadIdx.x, recs, threadIdx.x);
+      const float sum = gradLimitPacked<kDt, true>(V, i, g, dc + threadIdx.x, recs, threadIdx.x,
+                                                   reinterpret_cast<const unsigned short *>(stWords), 8 * w0);
       storeGrad(V, i, g);
       if (kDt) dt = V.vol[i] / (double)sum;
     }
