@@ -486,13 +486,15 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
 // (and, with kDt, the spectral-radius sum of RFLU_TimeStepInviscid) in one
 // pass over the cell's faces instead of five.  The strain-rate eigenframe
 // needs only the unlimited gradient, so the velocity projections are taken in
-// the same pass as the neighbour min/max; each face's offset fc - cofg is kept
-// in shared memory (dc, stride kBlock) for the limiter pass.  At most
-// kMaxCellFaces faces per cell (tetrahedra 4, prisms and pyramids 5,
+// the same pass as the neighbour min/max.  Venkatakrishnan keeps each face's
+// offset fc - cofg in shared memory (dc, stride kBlock) for its second pass;
+// at most kMaxCellFaces faces per cell (tetrahedra 4, prisms and pyramids 5,
 // hexahedra 6).  With kTiled the cell's, its stencil members' and its face
 // neighbours' prim records come from the CTA's staged tile (recs, local ids)
 // and its faces from the entry-major arrays feD/feN; otherwise they are
-// gathered from global memory.  Returns the spectral-radius sum (kDt) or 0.
+// gathered from global memory.  kRc is the limiter (RECONST) when fixed at
+// compile time, -1 to read it from the parameters.  Returns the
+// spectral-radius sum (kDt) or 0.
 //
 // LSQ gradient (RFLU_ComputeGradCellsFast_3D, modflu/
 // RFLU_ModDifferentiationCells.F90:983-1044): the reference's per-member
@@ -507,7 +509,7 @@ __device__ inline void ldRec(const float *recs, int l, float *v) {
   v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
 
-template <bool kDt, bool kTiled>
+template <bool kDt, bool kTiled, int kRc>
 __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, float *dc, const float *recs,
                                         int li, const unsigned short *stSm = nullptr, int stBase = 0) {
   const Params &P = V.p;
@@ -547,12 +549,16 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
       g[3 * k + 2] = lxz * x + lyz * y + lzz * z;
     }
   }
-  const int rc = P.reconst;
+  const int rc = kRc >= 0 ? kRc : P.reconst;
   const bool lim = second && (rc == 10 || rc == 100 || rc == 11);
   const bool velo = lim && rc == 10;
-  float G[9], A[9], ev[3];
+  const bool venkat = lim && rc == 11;
+  // velocity limiter frame: eigenvectors A(:, j) = A[3j..3j+2] of the
+  // strain rate, and B = A^T G with G(comp, dir) the velocity gradient
+  float A[9], B[9];
+  bool e12 = false, e23 = false;  // eigenvalues merged (within 1e-3 of the largest magnitude)
   if (velo) {
-    float Sy[9];
+    float G[9], Sy[9], ev[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -562,21 +568,46 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
 #pragma unroll
       for (int b = 0; b < 3; ++b) Sy[a + 3 * b] = 0.5f * (G[a + 3 * b] + G[b + 3 * a]);
     symmetricEigen3(Sy, A, ev);
-  }
-  float vmin[5], vmax[5], dmn[3] = {0.f, 0.f, 0.f}, dmx[3] = {0.f, 0.f, 0.f};
+    float mx = fabsf(ev[0]);
+    mx = fmax2(mx, fabsf(ev[1]));
+    mx = fmax2(mx, fabsf(ev[2]));
+    const float scale = 1.0e-3f * mx;
+    e12 = (ev[1] - ev[0] <= scale);
+    e23 = (ev[2] - ev[1] <= scale);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; }
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) B[3 * j + c] = A[3 * j] * G[3 * c] + A[3 * j + 1] * G[1 + 3 * c] + A[3 * j + 2] * G[2 + 3 * c];
+  }
+  // Barth-Jespersen in one pass: min over faces of dmax/d2 (d2 > 0) is
+  // dmax / (largest positive d2), and likewise dmin / (most negative d2), so
+  // the pass keeps the extreme d2 per component (pmx, nmn) next to the
+  // neighbour extremes; the velocity limiter keeps the extreme projections of
+  // the face increments (smx, smn) next to those of the neighbour differences
+  // (dmx, dmn).  Venkatakrishnan needs the final extremes per face and takes
+  // a second pass over the offsets kept in dc.
+  float vmin[5], vmax[5], pmx[5], nmn[5];
+  float dmn[3] = {0.f, 0.f, 0.f}, dmx[3] = {0.f, 0.f, 0.f}, smn[3] = {0.f, 0.f, 0.f}, smx[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; pmx[k] = 0.f; nmn[k] = 0.f; }
   const float gam = P.refGammaF;
   const float ai = kDt ? sqrtf(gam * q[4] / q[0]) : 0.f;
   float sum = 0.f;
   int nfc = 0;
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
-  // one face of the pass: neighbour record x, offset d of this cell's side
+  // one face of the pass: neighbour record x, offset d = fc - cofg of this side
   auto face = [&](const float *x, float d0, float d1, float d2) {
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
+      if (velo && k >= 1 && k <= 3) continue;
       vmin[k] = fmin2(vmin[k], x[k]);
       vmax[k] = fmax2(vmax[k], x[k]);
+      if (!venkat) {
+        // grad . (cofg - fc), the reference's sign
+        const float dd = -(g[3 * k] * d0 + g[3 * k + 1] * d1 + g[3 * k + 2] * d2);
+        if (dd > 0.f) pmx[k] = fmax2(pmx[k], dd);
+        else if (dd < 0.f) nmn[k] = fmin2(nmn[k], dd);
+      }
     }
     if (velo) {
       // A^T (u(c2) - u(c1)) seen from this cell = A^T (u(nb) - u(i))
@@ -589,13 +620,19 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
         pr = pr + A[3 * j + 2] * du2;
         dmn[j] = fmin2(dmn[j], pr);
         dmx[j] = fmax2(dmx[j], pr);
+        // A^T G (cofg - fc)
+        const float ps = -(B[3 * j] * d0 + B[3 * j + 1] * d1 + B[3 * j + 2] * d2);
+        if (ps > 0.f) smx[j] = fmax2(smx[j], ps);
+        else if (ps < 0.f) smn[j] = fmin2(smn[j], ps);
       }
     }
-    float *slot = dc + 3 * nfc * kBlock;
-    slot[0] = d0;
-    slot[kBlock] = d1;
-    slot[2 * kBlock] = d2;
-    ++nfc;
+    if (venkat) {
+      float *slot = dc + 3 * nfc * kBlock;
+      slot[0] = d0;
+      slot[kBlock] = d1;
+      slot[2 * kBlock] = d2;
+      ++nfc;
+    }
   };
   if (kTiled) {
     const size_t n = V.nc;
@@ -645,19 +682,17 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
     }
   }
   if (!lim) return sum;
-  float lm[5] = {1.f, 1.f, 1.f, 1.f, 1.f}, al[3] = {1.f, 1.f, 1.f};
-  const float epsq = (rc == 11) ? V.epsq[i] : 0.f;
-  for (int c = 0; c < nfc; ++c) {
-    const float *slot = dc + 3 * c * kBlock;
-    const float dx = slot[0], dy = slot[kBlock], dz = slot[2 * kBlock];
+  float lm[5] = {1.f, 1.f, 1.f, 1.f, 1.f};
+  if (venkat) {
+    const float epsq = V.epsq[i];
+    const float tiny = 1.0e-12f;
+    for (int c = 0; c < nfc; ++c) {
+      const float *slot = dc + 3 * c * kBlock;
+      const float dx = slot[0], dy = slot[kBlock], dz = slot[2 * kBlock];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      if (velo && k >= 1 && k <= 3) continue;
-      // d2 = grad . (cofg - fc), the reference's sign
-      const float d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
-      const float dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
-      if (rc == 11) {
-        const float tiny = 1.0e-12f;
+      for (int k = 0; k < 5; ++k) {
+        const float d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
+        const float dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
         if (d2 > 0.f) {
           const float numer = (dmax * dmax + epsq) * d2 + 2.f * d2 * d2 * dmax;
           const float denom = d2 * (dmax * dmax + 2.f * d2 * d2 + dmax * d2 + epsq);
@@ -667,39 +702,24 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
           const float denom = d2 * (dmin * dmin + 2.f * d2 * d2 + dmin * d2 + epsq);
           lm[k] = fmin2(numer / (denom + tiny), lm[k]);
         }
-      } else {
-        if (d2 > 0.f) lm[k] = fmin2(fmin2(1.f, dmax / d2), lm[k]);
-        else if (d2 < 0.f) lm[k] = fmin2(fmin2(1.f, dmin / d2), lm[k]);
       }
     }
-    if (velo) {
-      const float off[3] = {-dx, -dy, -dz};
-      float sh[3];
+  } else {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        float s = 0.f;
-        s = s + G[a] * off[0];
-        s = s + G[a + 3] * off[1];
-        s = s + G[a + 6] * off[2];
-        sh[a] = s;
-      }
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        float pr = 0.f;
-        pr = pr + A[3 * j] * sh[0];
-        pr = pr + A[3 * j + 1] * sh[1];
-        pr = pr + A[3 * j + 2] * sh[2];
-        if (pr > 0.f) al[j] = fmin2(al[j], dmx[j] / pr);
-        else if (pr < 0.f) al[j] = fmin2(al[j], dmn[j] / pr);
-      }
+    for (int k = 0; k < 5; ++k) {
+      if (velo && k >= 1 && k <= 3) continue;
+      if (pmx[k] > 0.f) lm[k] = fmin2(fmin2(1.f, (vmax[k] - q[k]) / pmx[k]), lm[k]);
+      if (nmn[k] < 0.f) lm[k] = fmin2(fmin2(1.f, (vmin[k] - q[k]) / nmn[k]), lm[k]);
     }
   }
   if (velo) {
-    float mx = fabsf(ev[0]);
-    mx = fmax2(mx, fabsf(ev[1]));
-    mx = fmax2(mx, fabsf(ev[2]));
-    const float scale = 1.0e-3f * mx;
-    const bool e12 = (ev[1] - ev[0] <= scale), e23 = (ev[2] - ev[1] <= scale);
+    float al[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      al[j] = 1.f;
+      if (smx[j] > 0.f) al[j] = fmin2(al[j], dmx[j] / smx[j]);
+      if (smn[j] < 0.f) al[j] = fmin2(al[j], dmn[j] / smn[j]);
+    }
     if (e12 && e23) {
       const float m = fmin2(fmin2(al[0], al[1]), al[2]);
       al[0] = al[1] = al[2] = m;
@@ -710,28 +730,12 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
       const float m = fmin2(al[1], al[2]);
       al[1] = al[2] = m;
     }
-    // G <- A diag(alpha) A^T G
-    float Rm[9];
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float s = 0.f;
-        s = s + A[3 * j] * G[3 * c];
-        s = s + A[3 * j + 1] * G[1 + 3 * c];
-        s = s + A[3 * j + 2] * G[2 + 3 * c];
-        Rm[j + 3 * c] = al[j] * s;
-      }
+    // G <- A diag(alpha) A^T G = A diag(alpha) B
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float s = 0.f;
-        s = s + A[a] * Rm[3 * c];
-        s = s + A[a + 3] * Rm[1 + 3 * c];
-        s = s + A[a + 6] * Rm[2 + 3 * c];
-        g[3 * (1 + a) + c] = s;
-      }
+      for (int c = 0; c < 3; ++c)
+        g[3 * (1 + a) + c] = A[a] * (al[0] * B[c]) + A[a + 3] * (al[1] * B[3 + c]) + A[a + 6] * (al[2] * B[6 + c]);
     lm[1] = lm[2] = lm[3] = 1.f;
   }
 #pragma unroll
@@ -750,7 +754,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimit(View<R> V)
   R g[15];
   if constexpr (Layout<R>::packed) {
     __shared__ float dc[3 * kMaxCellFaces * kBlock];
-    gradLimitPacked<false, false>(V, i, g, dc + threadIdx.x, nullptr, 0);
+    gradLimitPacked<false, false, -1>(V, i, g, dc + threadIdx.x, nullptr, 0);
   } else {
     gradLimitCell(V, PlainLoad<R>{V}, i, g);
   }
@@ -784,18 +788,18 @@ static_assert(kTile == kBlock, "one thread per cell of a tile");
 // the tile's stencil ids copied in 16-byte words (maxTileSt ids plus the
 // misalignment of the first word).
 template <typename R>
-inline size_t tileSmemBytes(const View<R> &V) {
-  return sizeof(float) * (8 * (size_t)V.maxRecs + 3 * kMaxCellFaces * kBlock) +
+inline size_t tileSmemBytes(const View<R> &V, bool venkat) {
+  return sizeof(float) * (8 * (size_t)V.maxRecs + (venkat ? 3 * kMaxCellFaces * kBlock : 0)) +
          16 * (((size_t)V.maxTileSt + 7) / 8 + 1);
 }
 
-template <typename R, bool kDt>
+template <typename R, bool kDt, int kRc>
 __global__ void __launch_bounds__(kBlock, 4) kGradTile(View<R> V) {
   if constexpr (Layout<R>::packed) {
     extern __shared__ float4 tileSmem[];
     float *recs = reinterpret_cast<float *>(tileSmem);
     float *dc = recs + 8 * (size_t)V.maxRecs;
-    uint4 *stWords = reinterpret_cast<uint4 *>(dc + 3 * kMaxCellFaces * kBlock);
+    uint4 *stWords = reinterpret_cast<uint4 *>(dc + (kRc == 11 ? 3 * kMaxCellFaces * kBlock : 0));
     const int base = blockIdx.x * kTile;
     const int nIn = min(kTile, V.nc - base);
     const int hb = V.haloOff[blockIdx.x], nh = V.haloOff[blockIdx.x + 1] - hb;
@@ -817,7 +821,7 @@ __global__ void __launch_bounds__(kBlock, 4) kGradTile(View<R> V) {
     double dt = 1.79769313486231571e308;
     if (i < V.nc && (!kDt || V.sc->finished >= 0)) {
       float g[15];
-      const float sum = gradLimitPacked<kDt, true>(V, i, g, dc + threadIdx.x, recs, threadIdx.x,
+      const float sum = gradLimitPacked<kDt, true, kRc>(V, i, g, dc + threadIdx.x, recs, threadIdx.x,
                                                    reinterpret_cast<const unsigned short *>(stWords), 8 * w0);
       storeGrad(V, i, g);
       if (kDt) dt = V.vol[i] / (double)sum;
@@ -874,7 +878,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> 
     __shared__ float dc[3 * kMaxCellFaces * kBlock];
     if (i < V.nc && V.sc->finished >= 0) {
       R g[15];
-      const float sum = gradLimitPacked<true, false>(V, i, g, dc + threadIdx.x, nullptr, 0);
+      const float sum = gradLimitPacked<true, false, -1>(V, i, g, dc + threadIdx.x, nullptr, 0);
       if (V.p.spaceOrder > 1) storeGrad(V, i, g);
       dt = V.vol[i] / (double)sum;
     }
@@ -1438,16 +1442,31 @@ struct Launch {
   static void initState(const View<R> &V, cudaStream_t s) { kInitState<R><<<blocks(V.nc), kBlock, 0, s>>>(V); }
   static void gradLimit(const View<R> &V, cudaStream_t s) {
     if (V.p.spaceOrder < 2) return;
-    if (V.tiled) kGradTile<R, false><<<blocks(V.nc), kBlock, tileSmemBytes(V), s>>>(V);
+    if (V.tiled) launchTile<false>(V, s);
     else kGradLimit<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+  }
+  // the tiled kernel specialised for the limiter (RECONST 10, 100, 11; other
+  // values: unlimited)
+  template <bool kDt>
+  static void launchTile(const View<R> &V, cudaStream_t s) {
+    const int rc = V.p.reconst;
+    const size_t b = tileSmemBytes(V, rc == 11);
+    if (rc == 10) kGradTile<R, kDt, 10><<<blocks(V.nc), kBlock, b, s>>>(V);
+    else if (rc == 100) kGradTile<R, kDt, 100><<<blocks(V.nc), kBlock, b, s>>>(V);
+    else if (rc == 11) kGradTile<R, kDt, 11><<<blocks(V.nc), kBlock, b, s>>>(V);
+    else kGradTile<R, kDt, 0><<<blocks(V.nc), kBlock, b, s>>>(V);
+  }
+  template <bool kDt, int kRc>
+  static void setTileSmem(const View<R> &V) {
+    cudaFuncSetAttribute(kGradTile<R, kDt, kRc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tileSmemBytes(V, kRc == 11));
   }
   // Kernel attributes that depend on the mesh (shared memory of the tiled
   // kernels); called once at set-up, outside any stream capture.
   static void configure(const View<R> &V) {
     if (V.tiled) {
-      const int b = (int)tileSmemBytes(V);
-      cudaFuncSetAttribute(kGradTile<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-      cudaFuncSetAttribute(kGradTile<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+      setTileSmem<false, 0>(V); setTileSmem<false, 10>(V); setTileSmem<false, 100>(V); setTileSmem<false, 11>(V);
+      setTileSmem<true, 0>(V); setTileSmem<true, 10>(V); setTileSmem<true, 100>(V); setTileSmem<true, 11>(V);
     }
   }
   static void faceFlux(const View<R> &V, cudaStream_t s) {
@@ -1475,7 +1494,7 @@ struct Launch {
       gradLimit(V, s);
     } else {
       kStepBegin<R><<<1, 1, 0, s>>>(V);
-      if (V.tiled) kGradTile<R, true><<<blocks(V.nc), kBlock, tileSmemBytes(V), s>>>(V);
+      if (V.tiled) launchTile<true>(V, s);
       else kGradLimitDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
       kDtFinalize<R><<<1, 1, 0, s>>>(V);
     }
