@@ -146,6 +146,20 @@ int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, doubl
  * (0-based) of p_f*|A_f|, p_f the limited second-order face pressure of the
  * owning cell, and its gradient dJ/dcv(5,nCells) (no reference counterpart). */
 int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, double *J, double *cvBar);
+/* Time-unrolled discrete adjoint (no reference counterpart): from the host
+ * state cv0(5,nCells), nSteps RungeKuttaMP steps with the fixed dtMin, and
+ * the functional J = sum over n = 1..nSteps of dtMin * (the patch-pressure
+ * functional of rflu_gpu_patch_pressure at the state after step n).  The
+ * reverse sweep applies each stage's residual VJP with the RK combination
+ * transposed; the state is checkpointed on the device every `every` steps
+ * and each segment is recomputed from its checkpoint (the segment's stage
+ * states only are held).  cvBar0(5,nCells) receives dJ/dcv0; with cvBar0
+ * NULL only the forward sweep runs and J alone is returned.  stats[4] (may
+ * be NULL): forward-sweep ms, reverse-sweep ms (recompute + adjoint), device
+ * bytes held by the context and the call, number of checkpoints.  FP64
+ * modes; RECONST 10 has no adjoint.  Leaves the context state untouched. */
+int rflu_gpu_unrolled_adjoint(rflu_gpu_ctx *ctx, const double *cv0, int nSteps, double dtMin, int every, int iPatch,
+                              double *J, double *cvBar0, double *stats);
 
 int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status);
 

@@ -72,6 +72,36 @@ __global__ void kPermuteOut(const T *src, double *dst, const int *refId, int nc,
 
 inline int nblk(long long n) { return (int)((n + 255) / 256); }
 
+// Reverse sweep of the RK combination (time-unrolled adjoint): the seed of
+// stage s's residual VJP, sigma = sum_t coef_t / vol * lambda_t, per cell in
+// the reference layout (5 per cell); coef_t = ark_t * dt * W[t][s].
+struct SeedTerms {
+  const double *lam[5];
+  double coef[5];
+  int n;
+};
+__global__ void kStageSeed(double *sigma, SeedTerms T, const double *vol, const int *refId, int nc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const size_t o = (size_t)refId[i];
+  const double iv = 1.0 / vol[i];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    double s = 0.0;
+    for (int t = 0; t < T.n; ++t) s += T.coef[t] * T.lam[t][5 * o + k];
+    sigma[5 * o + k] = s * iv;
+  }
+}
+__global__ void kSubInto(double *out, const double *a, const double *b, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] - b[i];
+}
+__global__ void kAxpyInPlace(double *y, double a, const double *x, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+__global__ void kAccumJ(double *acc, const double *j, double dt) { *acc += dt * *j; }
+
 // T and c of RFLU_SetDependentVars (TCPERF) from cv and p, for a mixed-mode
 // context whose steps store p only.
 __global__ void kDvFill(const double *cv, double *dv, int nc, double gcR, double gRT) {
@@ -165,6 +195,8 @@ struct CtxBase {
   virtual int kernelTimes(int nIter, double *ms) = 0;
   virtual int residualStatic(const double *cvDev, double *rhsDev) = 0;
   virtual int adjointTimes(int nIter, double *ms) = 0;
+  virtual int unrolledAdjoint(const double *cv0, int nSteps, double dt, int every, int iPatch, double *J,
+                              double *cvBar0, double *stats) = 0;
   cudaStream_t stream = nullptr;
 };
 
@@ -187,10 +219,13 @@ struct Ctx : CtxBase {
     if (stream) cudaStreamDestroy(stream);
   }
 
+  size_t bytesHeld = 0;          // device bytes of the context's own arrays
+
   template <typename T>
   int alloc(T **p, size_t n) {
     void *q = nullptr;
     RFLU_CUDA(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+    bytesHeld += std::max<size_t>(n, 1) * sizeof(T);
     allocs.push_back(q);
     *p = (T *)q;
     return RFLU_OK;
@@ -506,6 +541,143 @@ struct Ctx : CtxBase {
     if (rc) return rc;
     RFLU_CUDA(cudaStreamSynchronize(stream));
     return RFLU_OK;
+  }
+  // rflu_gpu_unrolled_adjoint.  Stage map of every scheme:
+  //   cv(s) = cv(s-1) - (ark_s dt / vol) sum_{m<=s} W[s][m] R(cv(m-1))
+  // (Wray: W[s][s] = 1, W[s][s-1] = -grk_s; the reference's RK4: W[s][s] = 1,
+  // last stage also W[4][1] = 1, W[4][m] = grk_m; Euler: W[1][1] = 1), so
+  //   lambda(s-1) = lambda(s) - R'(cv(s-1))^T sum_{t>=s} (ark_t dt W[t][s]/vol) lambda(t).
+  int unrolledAdjoint(const double *cv0, int nSteps, double dt, int every, int iPatch, double *Jout, double *cvBar0,
+                      double *stats) override {
+    if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
+      return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
+    if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: adjoint kernels exist for the FP64 modes only");
+    if (V.p.reconst == 10) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: RECONST 10 has no adjoint");
+    if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
+    const int nrk = V.p.nrkSteps;
+    double W[6][6] = {};
+    for (int t = 1; t <= nrk; ++t) W[t][t] = 1.0;
+    if (V.p.rkScheme == 2) {
+      W[2][1] = -V.p.grk[1];
+      W[3][2] = -V.p.grk[2];
+    } else if (V.p.rkScheme == 1) {
+      W[nrk][1] = 1.0;
+      for (int m = 2; m < nrk; ++m) W[nrk][m] = V.p.grk[m - 1];
+    }
+    const size_t nc = V.nc, n5 = 5 * nc, b5 = n5 * sizeof(double);
+    const int nCk = (nSteps + every - 1) / every;
+    const bool grad = cvBar0 != nullptr;
+    const size_t nSeg = grad ? (size_t)every * nrk + 1 : 0;
+    // device buffers of the call: checkpoints, segment stage states, the
+    // stage adjoints lambda(0..nrk), seed, VJP result, functional gradient
+    const size_t nVec = (size_t)nCk + nSeg + (grad ? (size_t)nrk + 1 + 3 : 0);
+    double *buf = nullptr, *jd = nullptr;
+    RFLU_CUDA(cudaMalloc(&buf, std::max<size_t>(nVec, 1) * b5));
+    if (cudaMalloc(&jd, 3 * sizeof(double)) != cudaSuccess) {
+      cudaFree(buf);
+      return fail(RFLU_ERR_CUDA, "rflu_gpu_unrolled_adjoint: cudaMalloc");
+    }
+    auto vec = [&](size_t k) { return buf + k * n5; };
+    cudaError_t err = cudaSuccess;  // first failed copy; checked before returning
+    auto cp = [&](void *d, const void *src, size_t bytes, cudaMemcpyKind kind) {
+      const cudaError_t e = cudaMemcpyAsync(d, src, bytes, kind, stream);
+      if (e != cudaSuccess && err == cudaSuccess) err = e;
+    };
+    auto zero = [&](void *d, size_t bytes) {
+      const cudaError_t e = cudaMemsetAsync(d, 0, bytes, stream);
+      if (e != cudaSuccess && err == cudaSuccess) err = e;
+    };
+    double *ck = vec(0), *seg = vec(nCk);
+    double *lam = grad ? vec(nCk + nSeg) : nullptr;
+    double *sigma = grad ? vec(nCk + nSeg + nrk + 1) : nullptr;
+    double *wv = grad ? sigma + n5 : nullptr, *pg = grad ? sigma + 2 * n5 : nullptr;
+    double *jStep = jd, *jAcc = jd + 1;
+    cudaEvent_t ev[3];
+    for (auto &e : ev) cudaEventCreate(&e);
+    int rc = RFLU_OK;
+    auto finish = [&](int r) {
+      for (auto &e : ev) cudaEventDestroy(e);
+      cudaFree(buf);
+      cudaFree(jd);
+      return r;
+    };
+    const int nb = nblk((long long)n5);
+    cp(cvSave, V.cv, b5, cudaMemcpyDeviceToDevice);
+    if ((rc = setState(cv0))) return finish(rc);
+    zero(jd, 3 * sizeof(double));
+    kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
+    // forward sweep: checkpoints (and J when no gradient is asked for)
+    cudaEventRecord(ev[0], stream);
+    for (int n = 0; n < nSteps; ++n) {
+      if (n % every == 0)
+        cp(ck + (size_t)(n / every) * n5, V.cv, b5, cudaMemcpyDeviceToDevice);
+      for (int st = 1; st <= nrk; ++st) stageKernels(st);
+      if (!grad) {
+        ops->patchPressure(V, iPatch, jStep, nullptr, work, stream);
+        kAccumJ<<<1, 1, 0, stream>>>(jAcc, jStep, dt);
+      }
+    }
+    cudaEventRecord(ev[1], stream);
+    if (grad) {
+      double *lamTop = lam + (size_t)nrk * n5;  // lambda at the end of the current step
+      zero(lamTop, b5);
+      auto loadState = [&](const double *src) {
+        cp(V.cv, src, b5, cudaMemcpyDeviceToDevice);
+        ops->initState(V, stream);
+      };
+      for (int sg = nCk - 1; sg >= 0; --sg) {
+        const int n0 = sg * every, n1 = std::min(nSteps, n0 + every);
+        loadState(ck + (size_t)sg * n5);
+        for (int n = n0; n < n1; ++n)
+          for (int st = 1; st <= nrk; ++st) {
+            cp(seg + ((size_t)(n - n0) * nrk + st - 1) * n5, V.cv, b5, cudaMemcpyDeviceToDevice);
+            stageKernels(st);
+          }
+        cp(seg + (size_t)(n1 - n0) * nrk * n5, V.cv, b5, cudaMemcpyDeviceToDevice);
+        for (int n = n1 - 1; n >= n0; --n) {
+          // the functional's term at the state after step n
+          loadState(seg + (size_t)(n + 1 - n0) * nrk * n5);
+          ops->patchPressure(V, iPatch, jStep, pg, work, stream);
+          kAccumJ<<<1, 1, 0, stream>>>(jAcc, jStep, dt);
+          kAxpyInPlace<<<nb, 256, 0, stream>>>(lamTop, dt, pg, n5);
+          for (int st = nrk; st >= 1; --st) {
+            SeedTerms T{};
+            for (int t = st; t <= nrk; ++t)
+              if (W[t][st] != 0.0) {
+                T.lam[T.n] = lam + (size_t)t * n5;
+                T.coef[T.n] = V.p.ark[t - 1] * dt * W[t][st];
+                ++T.n;
+              }
+            kStageSeed<<<nblk(V.nc), 256, 0, stream>>>(sigma, T, V.vol, V.refId, V.nc);
+            loadState(seg + ((size_t)(n - n0) * nrk + st - 1) * n5);
+            ops->vjp(V, sigma, wv, work, stream);
+            kSubInto<<<nb, 256, 0, stream>>>(lam + (size_t)(st - 1) * n5, lam + (size_t)st * n5, wv, n5);
+          }
+          cp(lamTop, lam, b5, cudaMemcpyDeviceToDevice);
+        }
+      }
+      cp(cvBar0, lamTop, b5, cudaMemcpyDeviceToHost);
+    }
+    cudaEventRecord(ev[2], stream);
+    cp(Jout, jAcc, sizeof(double), cudaMemcpyDeviceToHost);
+    // the context state as it was
+    cp(V.cv, cvSave, b5, cudaMemcpyDeviceToDevice);
+    ops->initState(V, stream);
+    if ((rc = checkLaunch("rflu_gpu_unrolled_adjoint"))) return finish(rc);
+    const cudaError_t es = cudaStreamSynchronize(stream);
+    if (err == cudaSuccess) err = es;
+    if (err != cudaSuccess)
+      return finish(fail(RFLU_ERR_CUDA, std::string("rflu_gpu_unrolled_adjoint: ") + cudaGetErrorString(err)));
+    if (stats) {
+      float f = 0.f, b = 0.f;
+      cudaEventElapsedTime(&f, ev[0], ev[1]);
+      cudaEventElapsedTime(&b, ev[1], ev[2]);
+      stats[0] = f;
+      stats[1] = grad ? b : 0.0;
+      stats[2] = (double)(bytesHeld + std::max<size_t>(nVec, 1) * b5 + 3 * sizeof(double));
+      stats[3] = nCk;
+    }
+    return finish(syncEvents(false));
   }
   int adjointTimes(int nIter, double *ms) override {
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
@@ -1018,6 +1190,11 @@ int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, doubl
 int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, double *J, double *cvBar) {
   CTX_CHECK("rflu_gpu_patch_pressure");
   return ctx->impl->patchPressure(cv, iPatch, J, cvBar);
+}
+int rflu_gpu_unrolled_adjoint(rflu_gpu_ctx *ctx, const double *cv0, int nSteps, double dtMin, int every, int iPatch,
+                              double *J, double *cvBar0, double *stats) {
+  CTX_CHECK("rflu_gpu_unrolled_adjoint");
+  return ctx->impl->unrolledAdjoint(cv0, nSteps, dtMin, every, iPatch, J, cvBar0, stats);
 }
 int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status) {
   CTX_CHECK("rflu_gpu_status");

@@ -68,7 +68,7 @@ class RfluError(RuntimeError):
 EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_gpu_stream",
            "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
            "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_residual", "rflu_gpu_vjp",
-           "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
+           "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_unrolled_adjoint", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
            "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_setup_build", "rflu_setup_grid",
            "rflu_setup_destroy")
 
@@ -106,6 +106,7 @@ def lib(build_if_missing=True):
     L.rflu_gpu_vjp.argtypes = [P, DP, DP, DP]
     L.rflu_gpu_jvp.argtypes = [P, DP, DP, DP]
     L.rflu_gpu_patch_pressure.argtypes = [P, DP, I, DP, DP]
+    L.rflu_gpu_unrolled_adjoint.argtypes = [P, DP, I, D, I, I, DP, DP, DP]
     L.rflu_gpu_status.argtypes = [P, C.POINTER(Status)]
     L.rflu_gpu_kernel_times.argtypes = [P, I, DP]
     L.rflu_gpu_residual_static.argtypes = [P, P, P]
@@ -299,6 +300,20 @@ class Region:
         g = np.empty((self.n_cells, 5)) if with_grad else None
         _check(lib().rflu_gpu_patch_pressure(self.h, _p(cv), ipatch, C.byref(J), _p(g) if with_grad else None))
         return J.value, g
+
+    def unrolled_adjoint(self, cv0, n_steps, dt, every, ipatch, with_grad=True):
+        """J = sum over the n_steps fixed-dt steps of dt * (patch-pressure
+        functional after the step) and dJ/dcv0 by the checkpointed reverse
+        sweep (rflu_gpu_unrolled_adjoint).  Returns (J, cv_bar0 or None,
+        stats dict)."""
+        cv0 = np.ascontiguousarray(cv0, np.float64)
+        J = C.c_double()
+        g = np.empty((self.n_cells, 5)) if with_grad else None
+        st = np.zeros(4)
+        _check(lib().rflu_gpu_unrolled_adjoint(self.h, _p(cv0), n_steps, dt, every, ipatch, C.byref(J),
+                                               _p(g) if with_grad else None, _p(st)))
+        return J.value, g, {"forward_ms": st[0], "reverse_ms": st[1], "device_bytes": int(st[2]),
+                            "checkpoints": int(st[3])}
 
     def kernel_times(self, n_iter=10):
         """Mean ms per launch: grad+limiter, face flux, gather+update, dt."""
