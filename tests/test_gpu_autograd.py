@@ -143,12 +143,16 @@ def test_unrolled_adjoint_finite_differences(gpu_lib, reconst):
     J, g, _ = r.unrolled_adjoint(cv0, n, dt, every, 1)
     assert J > 0
     eps = 1e-6
+    fd, ad = [], []
     for d in _density_blobs(c, 4, 21):
         jp, _, _ = r.unrolled_adjoint(cv0 + eps * d, n, dt, every, 1, with_grad=False)
         jm, _, _ = r.unrolled_adjoint(cv0 - eps * d, n, dt, every, 1, with_grad=False)
-        fd = (jp - jm) / (2 * eps)
-        ad = float((g * d).sum())
-        assert abs(fd - ad) <= 1e-5 * abs(ad), (fd, ad)
+        fd.append((jp - jm) / (2 * eps))
+        ad.append(float((g * d).sum()))
+    fd, ad = np.array(fd), np.array(ad)
+    # relative to the gradient's scale over the directions: a direction with
+    # a small derivative is dominated by the differences' round-off (~1e-12)
+    assert (np.abs(fd - ad) <= 1e-5 * np.abs(ad).max()).all(), (fd, ad)
 
 
 def test_unrolled_adjoint_rejections(gpu_lib):
