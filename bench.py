@@ -348,31 +348,35 @@ def run_ours(args):
 
 def unrolled_adjoint(args, cases, gpu):
     """Time-unrolled adjoint: spherical blast on n^3 hexes (p=10 inside
-    r=0.15, p=1 outside, rho=1), HLLC, second order with the
-    Venkatakrishnan limiter (the eigen-frame BJ limiter has a tangent only),
-    Wray RK3, dt fixed from the initial CFL 0.4, the functional the
-    time-integrated pressure on the x=1 patch.  Gradient w.r.t. the initial
+    r=0.15, p=1 outside, rho=1), HLLC, second order with the componentwise
+    Barth-Jespersen limiter (RECONST 100: the eigen-frame BJ limiter has a
+    tangent only, and the reference's Venkatakrishnan limiter, whose face
+    offsets are taken as cofg - fc, lets face pressures of this blast go
+    negative within the first step), Wray RK3, dt fixed from the initial
+    CFL 0.4, the functional the time-integrated pressure on the x=1 patch.  Gradient w.r.t. the initial
     density by the checkpointed reverse sweep; central differences on seeded
     density blobs, on the case as stated (exactly uniform outside the blast,
     where the limiters' d2 = 0 branch is not differentiable) and on the same
     case with a smooth 2% background variation."""
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_VENKAT, cfl=0.4)
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ_COMP, cfl=0.4)
     c = cases.blast_hex(args.unrolled_n, num=num, p_in=10.0, radius=0.15)
     x = gpu.Setup(c).cofg
     reg = gpu.Region(c, "fp64")
     dt = reg.timestep(1.0)
     n, every = args.unrolled_steps, args.unrolled_every
-    out = {"workload": "blast_hex%d_hllc_venkat_wray3" % args.unrolled_n, "cells": reg.n_cells, "steps": n,
+    out = {"workload": "blast_hex%d_hllc_bjcomp_wray3" % args.unrolled_n, "cells": reg.n_cells, "steps": n,
            "checkpoint_every": every, "dt": dt, "functional": "sum_n dt * sum_{x=1 patch} p_f |A_f|"}
     bg = np.sin(2 * np.pi * x[:, 0] + 0.3) * np.sin(2 * np.pi * x[:, 1] + 0.7) * np.sin(2 * np.pi * x[:, 2] + 1.1)
     smooth = c.cv0.copy()
     smooth[:, 0] *= 1 + 0.02 * bg
     smooth[:, 4] *= 1 + 0.02 * np.roll(bg, 7)
     smooth[:, 1] += 0.01 * bg
+    # density blobs (sigma 0.1) between the blast and the x=1 wall, where the
+    # functional has a sensitivity well above the differences' round-off
     rng = np.random.default_rng(2024)
     dirs = []
     for _ in range(args.unrolled_fd):
-        c0 = rng.uniform(0.25, 0.75, 3)
+        c0 = np.array([rng.uniform(0.55, 0.85), rng.uniform(0.3, 0.7), rng.uniform(0.3, 0.7)])
         d = np.zeros_like(c.cv0)
         d[:, 0] = np.exp(-((x - c0) ** 2).sum(axis=1) / (2 * 0.1 ** 2)) * rng.choice([-1.0, 1.0])
         dirs.append(d)
@@ -380,18 +384,21 @@ def unrolled_adjoint(args, cases, gpu):
         reg.upload(cv0)
         J, g, st = reg.unrolled_adjoint(cv0, n, dt, every, 1)
         errs = []
-        eps = 1e-6
+        eps = 1e-4  # relative density change at a blob's centre
         for d in dirs:
             jp, _, _ = reg.unrolled_adjoint(cv0 + eps * d, n, dt, every, 1, with_grad=False)
             jm, _, _ = reg.unrolled_adjoint(cv0 - eps * d, n, dt, every, 1, with_grad=False)
             ad = float((g * d).sum())
             errs.append(abs((jp - jm) / (2 * eps) - ad) / max(abs(ad), 1e-300))
         errs = np.array(errs)
+        ok = np.isfinite(errs)
         out[name] = {"J": J, "forward_ms": st["forward_ms"], "reverse_ms": st["reverse_ms"],
                      "adjoint_over_primal": st["reverse_ms"] / st["forward_ms"],
                      "device_bytes": st["device_bytes"], "checkpoints": st["checkpoints"],
-                     "fd_eps": eps, "fd_rel_err_median": float(np.median(errs)), "fd_rel_err_max": float(errs.max()),
+                     "fd_eps": eps, "fd_rel_err_median": float(np.median(errs[ok])) if ok.any() else None,
+                     "fd_rel_err_max": float(errs[ok].max()) if ok.any() else None,
                      "fd_dirs_below_1e-6": int((errs < 1e-6).sum()), "fd_dirs_below_1e-5": int((errs < 1e-5).sum()),
+                     "fd_dirs_below_1e-4": int((errs < 1e-4).sum()), "fd_dirs_not_finite": int((~ok).sum()),
                      "fd_dirs": len(errs)}
     reg.close()
     return out
