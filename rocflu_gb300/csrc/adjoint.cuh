@@ -462,17 +462,21 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
       const int js = W.jstar[k * n + i];
       const double qi = V.prim[k * n + i];
       const double dext = (js >= 0 ? V.prim[k * n + js] : qi) - qi;
-      double pDext, pD2;
+      double db, d2b;
       if (rc == 11) {
         using D2 = Dual<2>;
         D2 phi = venkat(D2::seed(dext, 0), D2::seed(d2, 1), D2(V.epsq[i]));
-        pDext = phi.d[0];
-        pD2 = phi.d[1];
+        db = lb * phi.d[0];
+        d2b = lb * phi.d[1];
       } else {
-        pDext = 1.0 / d2;
-        pD2 = -dext / (d2 * d2);
+        // lim = dext/d2: d lim/d dext = 1/d2, d lim/d d2 = -(dext/d2)/d2, taken
+        // as (lb/d2) and -(lb/d2)*(dext/d2) so that a tiny d2 (differences of
+        // ~1e-200 ahead of a wave) neither squares into 0 nor makes 0/0 at a
+        // local extreme (dext = 0)
+        const double r = lb / d2;
+        db = r;
+        d2b = -r * (dext / d2);
       }
-      const double db = lb * pDext, d2b = lb * pD2;
 #pragma unroll
       for (int c = 0; c < 3; ++c) gb[3 * k + c] += d2b * (-dxyz[c]);
       if (js >= 0) {

@@ -103,3 +103,19 @@ def test_adjoint_rejects_mixed_and_eigen_frame(gpu_lib):
     c2 = _case(cases.DISCR_ROE, cases.RECONST_BJ)
     with pytest.raises(gpu.RfluError):
         gpu.Region(c2, "fp64").vjp(c2.cv0, c2.cv0)
+
+
+@pytest.mark.parametrize("reconst", [cases.RECONST_BJ_COMP, cases.RECONST_VENKAT])
+def test_adjoint_finite_with_tiny_differences(gpu_lib, reconst):
+    """A state whose neighbour differences are ~1e-200 (the far field ahead
+    of a wave): the limiter's active branch has d2 ~ 1e-200 and, at a local
+    extreme, dext = 0; the VJP and the functional's gradient stay finite."""
+    c = _case(cases.DISCR_HLLC, reconst)
+    rng = np.random.default_rng(4)
+    cv = np.tile(c.cv0.mean(axis=0), (c.cv0.shape[0], 1))
+    cv[:, 1:4] += 1e-200 * rng.standard_normal((cv.shape[0], 3))
+    r = gpu.Region(c, "fp64")
+    g = r.vjp(cv, rng.standard_normal(cv.shape))
+    assert np.isfinite(g).all()
+    _, gp = r.patch_pressure(cv, 1)
+    assert np.isfinite(gp).all()
