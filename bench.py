@@ -133,8 +133,9 @@ def measured_peaks():
 def dram_traffic(kernel, n_cells):
     """DRAM bytes (read + write) per launch of `kernel`, from the committed ncu
     summary (profiles/dram_traffic_per_cell.txt: one 'kernel bytes_per_cell'
-    line per kernel, measured on a smaller case of the same workload and
-    scaled here by the cells one launch processes); None when absent."""
+    line per kernel, dram__bytes_read.sum + dram__bytes_write.sum of one
+    launch on this workload divided by its cells, scaled here by the cells one
+    launch processes); None when absent."""
     path = os.path.join(ROOT, "profiles", "dram_traffic_per_cell.txt")
     try:
         for line in open(path):
@@ -147,25 +148,38 @@ def dram_traffic(kernel, n_cells):
 
 
 def algorithmic_bytes(region, precision):
-    """Bytes per launch of the three stage kernels and of the whole stage,
-    counted from the data each kernel must move once (neighbour gathers
-    counted once, ideal reuse), with the per-cell terms of the two-kernel
-    minimum: state, gradients, LSQ weights (FP64) or R-factor coefficients
-    and centroids (mixed), stencil ids, face
-    geometry/connectivity."""
+    """Bytes per launch of the three stage kernels, counted from the data each
+    kernel must move once (every cell or face record read once, neighbour
+    re-reads and tile halos excluded).
+
+    mixed (packed records, tiled gradient kernel):
+      gradient+limiter  per cell: prim record 32, stencil offset 4, L matrix
+                        24, face-entry offset 4, gradient record 64; per
+                        stencil member: 2-byte local id; per cell-face entry
+                        (2 nf + nb): 16-byte offset/neighbour entry
+      face flux         per interior face: 48-byte record; per cell: prim 32 +
+                        gradient 64; per face: 20 bytes of flux written; per
+                        boundary face: 36 bytes of SoA geometry
+      gather+update     per cell: cv read+write 80, p 8, prim record 32, 1/vol
+                        4, centroid 12, CSR offset 4, rhsSum 80/3 (written in
+                        stage 1, read+written in 2, read in 3); per face: flux
+                        20; per cell-face entry: 4
+    fp64 (structure of arrays, per-member LSQ weights)."""
     g = region.grid
     nc = region.n_cells
     nf = g.f2c.shape[0]
     nb = g.bf2c.shape[0]
     S = len(g.c2cs)
-    r = 4 if precision == "mixed" else 8
+    ent = 2 * nf + nb
     if precision == "mixed":
-        # weights formed on the fly: R-factor coefficients and centroids per cell
-        grad_limit = nc * (5 * r + 15 * r + 4 + 6 * r + 3 * r) + S * 4 + nf * 2 * (8 + 3 * r)
+        grad_limit = nc * (32 + 4 + 24 + 4 + 64) + S * 2 + ent * 16
+        face_flux = nf * 48 + nc * 96 + (nf + nb) * 20 + nb * 36
+        gather_update = nc * (80 + 8 + 32 + 4 + 12 + 4 + 80.0 / 3) + (nf + nb) * 20 + ent * 4
     else:
+        r = 8
         grad_limit = nc * (5 * r + 15 * r + 4) + S * (4 + 3 * r) + nf * 2 * (8 + 3 * r)
-    face_flux = nc * (5 * r + 15 * r) + (nf + nb) * (4 * r + 3 * r + 5 * r) + nf * 8
-    gather_update = nc * (40 + 40 + 24 + 5 * 2 * r + 5 * r + 8 + 8) + 2 * nf * 5 * r + (2 * nf + nb) * 4
+        face_flux = nc * (5 * r + 15 * r) + (nf + nb) * (4 * r + 3 * r + 5 * r) + nf * 8
+        gather_update = nc * (40 + 40 + 24 + 5 * 2 * r + 5 * r + 8 + 8) + 2 * nf * 5 * r + (2 * nf + nb) * 4
     return {"gradLimit": grad_limit, "faceFlux": face_flux, "gatherUpdate": gather_update}
 
 
