@@ -773,7 +773,7 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
   }
   stLoc.resize(stLoc.size() + 16, 0);  // whole 16-byte words past the last tile
   // shared memory: 8 floats per record, the face-offset cache and the ids
-  const size_t smem = sizeof(float) * (8 * (size_t)maxRecs + 3 * 6 * kTile) + 16 * (((size_t)maxTileSt + 7) / 8 + 1);
+  const size_t smem = sizeof(float) * (2 * (8 * (size_t)maxRecs + 4 * (((size_t)maxTileSt + 7) / 8 + 1)) + 3 * 6 * kTile);
   int dev = 0, optin = 0;
   RFLU_CUDA(cudaGetDevice(&dev));
   RFLU_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1086,6 +1086,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     if ((rc = alloc((char **)&work, workBytes))) return rc;
   }
   ops->configure(V);
+  V.tileGrid = ops->tileGrid(V);
   return checkLaunch("rflu_gpu_create");
 }
 

@@ -98,6 +98,7 @@ struct View {
   int tiled;                        // 0: the gather kernel instead
   int maxRecs;                      // max staged records over the tiles
   int maxTileSt;                    // max stencil entries of a tile's cells
+  int tileGrid;                     // CTAs of the persistent tiled kernels
   int cfW;                          // max faces per cell (entries of feD/feN)
   const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids
   const unsigned short *stLoc;      // local id of each stencil member (stIdx order),

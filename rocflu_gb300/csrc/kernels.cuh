@@ -12,6 +12,7 @@
 //               RFLU_SetVarsContWrapper, AfterUpdateMP)
 // Per step: cellDt (RFLU_TimeStepInviscid) + dtFinalize (RFLU_MinimumTimeStep).
 #pragma once
+#include <algorithm>
 #include <climits>
 #include <cuda_runtime.h>
 
@@ -778,54 +779,95 @@ __device__ inline void blockMinDt(Scalars *sc, double dt) {
   }
 }
 
-// Tiled mixed-mode gradient + limiter (+ time step with kDt): one CTA per
-// tile of kTile consecutive cells.  The CTA first copies the prim records of
-// its cells (contiguous) and of its halo into shared memory, so each record
-// leaves L2 once per tile instead of once per stencil reference.
+// Tiled mixed-mode gradient + limiter (+ time step with kDt), persistent:
+// each CTA walks the tiles t = blockIdx.x, + gridDim.x, ... of kTile
+// consecutive cells.  A tile's prim records (its own cells, contiguous, and
+// its halo) and its stencil ids are copied into shared memory with cp.async,
+// double-buffered: the copies of the next tile are in flight while the CTA
+// computes the current one.  Each record leaves L2 once per tile instead of
+// once per stencil reference.
 static_assert(kTile == kBlock, "one thread per cell of a tile");
 
-// Shared memory of a tile: the staged records, the face-offset cache, and
-// the tile's stencil ids copied in 16-byte words (maxTileSt ids plus the
-// misalignment of the first word).
+__device__ inline void cpAsync16(void *smemDst, const void *gSrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smemDst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gSrc) : "memory");
+}
+__device__ inline void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ inline void cpAsyncWait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// One tile buffer: 8 floats per staged record, then the tile's stencil ids
+// as whole 16-byte words of stLoc (maxTileSt ids plus the misalignment of
+// the first word).  Two buffers per CTA, then the Venkatakrishnan face-offset
+// cache.
+template <typename R>
+__host__ __device__ inline size_t tileIdWords(const View<R> &V) {
+  return ((size_t)V.maxTileSt + 7) / 8 + 1;
+}
+template <typename R>
+__host__ __device__ inline size_t tileBufFloats(const View<R> &V) {
+  return 8 * (size_t)V.maxRecs + 4 * tileIdWords(V);
+}
 template <typename R>
 inline size_t tileSmemBytes(const View<R> &V, bool venkat) {
-  return sizeof(float) * (8 * (size_t)V.maxRecs + (venkat ? 3 * kMaxCellFaces * kBlock : 0)) +
-         16 * (((size_t)V.maxTileSt + 7) / 8 + 1);
+  return sizeof(float) * (2 * tileBufFloats(V) + (venkat ? 3 * kMaxCellFaces * kBlock : 0));
+}
+
+// Issue the copies of tile t into buf (this thread's share).
+template <typename R>
+__device__ inline void stageTile(const View<R> &V, int t, float *buf) {
+  const int base = t * kTile, nIn = min(kTile, V.nc - base);
+  const int hb = V.haloOff[t], nh = V.haloOff[t + 1] - hb;
+  uint4 *ids = reinterpret_cast<uint4 *>(buf + 8 * (size_t)V.maxRecs);
+  const int w0 = V.stOff[base] >> 3, w1 = (V.stOff[base + nIn] + 7) >> 3;
+  const uint4 *src4 = reinterpret_cast<const uint4 *>(V.stLoc);
+  for (int w = w0 + (int)threadIdx.x; w < w1; w += kBlock) cpAsync16(ids + (w - w0), src4 + w);
+  for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
+    const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
+    const int dst = r < nIn ? r : kTile + (r - nIn);
+    const float *g = V.prim + 8 * (size_t)src;
+    float *d = buf + 8 * (size_t)dst;
+    cpAsync16(d, g);
+    cpAsync16(d + 4, g + 4);
+  }
 }
 
 template <typename R, bool kDt, int kRc>
-__global__ void __launch_bounds__(kBlock, 4) kGradTile(View<R> V) {
+__global__ void __launch_bounds__(kBlock, 3) kGradTile(View<R> V) {
   if constexpr (Layout<R>::packed) {
     extern __shared__ float4 tileSmem[];
-    float *recs = reinterpret_cast<float *>(tileSmem);
-    float *dc = recs + 8 * (size_t)V.maxRecs;
-    uint4 *stWords = reinterpret_cast<uint4 *>(dc + (kRc == 11 ? 3 * kMaxCellFaces * kBlock : 0));
-    const int base = blockIdx.x * kTile;
-    const int nIn = min(kTile, V.nc - base);
-    const int hb = V.haloOff[blockIdx.x], nh = V.haloOff[blockIdx.x + 1] - hb;
-    // the tile's stencil ids, whole 16-byte words of stLoc (padded at the end)
-    const int w0 = V.stOff[base] >> 3, w1 = (V.stOff[base + nIn] + 7) >> 3;
-    const uint4 *src4 = reinterpret_cast<const uint4 *>(V.stLoc);
-    for (int w = w0 + (int)threadIdx.x; w < w1; w += kBlock) stWords[w - w0] = src4[w];
-    for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
-      const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
-      const int dst = r < nIn ? r : kTile + (r - nIn);
-      float v[8];
-      ld8(V.prim + 8 * (size_t)src, v);
-      float4 *d4 = reinterpret_cast<float4 *>(recs + 8 * (size_t)dst);
-      d4[0] = make_float4(v[0], v[1], v[2], v[3]);
-      d4[1] = make_float4(v[4], v[5], v[6], v[7]);
-    }
-    __syncthreads();
-    const int i = base + threadIdx.x;
+    const size_t bufFloats = tileBufFloats(V);
+    float *const smem = reinterpret_cast<float *>(tileSmem);
+    float *dc = smem + 2 * bufFloats;
+    const int nTiles = (V.nc + kTile - 1) / kTile;
+    // a step after the clipped last step does nothing (uniform over the CTA)
+    const bool live = !kDt || V.sc->finished >= 0;
     double dt = 1.79769313486231571e308;
-    if (i < V.nc && (!kDt || V.sc->finished >= 0)) {
-      float g[15];
-      const float sum = gradLimitPacked<kDt, true, kRc>(V, i, g, dc + threadIdx.x, recs, threadIdx.x,
-                                                   reinterpret_cast<const unsigned short *>(stWords), 8 * w0);
-      storeGrad(V, i, g);
-      if (kDt) dt = V.vol[i] / (double)sum;
+    int t = blockIdx.x, b = 0;
+    if (live && t < nTiles) stageTile(V, t, smem);
+    cpAsyncCommit();
+    for (; live && t < nTiles; t += gridDim.x, b ^= 1) {
+      const int tn = t + gridDim.x;
+      if (tn < nTiles) stageTile(V, tn, smem + (b ^ 1) * bufFloats);
+      cpAsyncCommit();
+      cpAsyncWait<1>();  // this thread's copies of tile t have landed
+      __syncthreads();   // and everyone else's
+      float *buf = smem + b * bufFloats;
+      const int base = t * kTile;
+      const int i = base + threadIdx.x;
+      if (i < V.nc) {
+        float g[15];
+        const float sum = gradLimitPacked<kDt, true, kRc>(
+            V, i, g, dc + threadIdx.x, buf, threadIdx.x,
+            reinterpret_cast<const unsigned short *>(buf + 8 * (size_t)V.maxRecs), 8 * (V.stOff[base] >> 3));
+        storeGrad(V, i, g);
+        if (kDt) dt = fmin(dt, V.vol[i] / (double)sum);
+      }
+      __syncthreads();  // buffer b is free for the tile after next
     }
+    cpAsyncWait<0>();
     if (kDt) blockMinDt(V.sc, dt);
   }
 }
@@ -1451,10 +1493,30 @@ struct Launch {
   static void launchTile(const View<R> &V, cudaStream_t s) {
     const int rc = V.p.reconst;
     const size_t b = tileSmemBytes(V, rc == 11);
-    if (rc == 10) kGradTile<R, kDt, 10><<<blocks(V.nc), kBlock, b, s>>>(V);
-    else if (rc == 100) kGradTile<R, kDt, 100><<<blocks(V.nc), kBlock, b, s>>>(V);
-    else if (rc == 11) kGradTile<R, kDt, 11><<<blocks(V.nc), kBlock, b, s>>>(V);
-    else kGradTile<R, kDt, 0><<<blocks(V.nc), kBlock, b, s>>>(V);
+    const int nTiles = (V.nc + kTile - 1) / kTile;
+    const int grid = V.tileGrid > 0 ? std::min(nTiles, V.tileGrid) : nTiles;
+    if (rc == 10) kGradTile<R, kDt, 10><<<grid, kBlock, b, s>>>(V);
+    else if (rc == 100) kGradTile<R, kDt, 100><<<grid, kBlock, b, s>>>(V);
+    else if (rc == 11) kGradTile<R, kDt, 11><<<grid, kBlock, b, s>>>(V);
+    else kGradTile<R, kDt, 0><<<grid, kBlock, b, s>>>(V);
+  }
+  // CTAs of the persistent tiled kernels: the resident CTAs per SM of the
+  // variant the mesh's limiter selects, times the SMs (0 when untiled)
+  template <bool kDt, int kRc>
+  static int residentTiles(const View<R> &V) {
+    int per = 0, dev = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kGradTile<R, kDt, kRc>, kBlock, tileSmemBytes(V, kRc == 11));
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(per, 1) * sms;
+  }
+  static int tileGrid(const View<R> &V) {
+    if (!V.tiled) return 0;
+    const int rc = V.p.reconst;
+    if (rc == 10) return std::min(residentTiles<false, 10>(V), residentTiles<true, 10>(V));
+    if (rc == 100) return std::min(residentTiles<false, 100>(V), residentTiles<true, 100>(V));
+    if (rc == 11) return std::min(residentTiles<false, 11>(V), residentTiles<true, 11>(V));
+    return std::min(residentTiles<false, 0>(V), residentTiles<true, 0>(V));
   }
   template <bool kDt, int kRc>
   static void setTileSmem(const View<R> &V) {
