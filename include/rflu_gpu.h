@@ -138,7 +138,9 @@ int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *
 
 /* Discrete adjoint of the same residual (no reference counterpart; it
  * differentiates rflu_gpu_residual): cvBar = (dR/dcv)^T rhsBar, through the
- * limiter's active branch.  Arrays (5,nCells). */
+ * limiter's active branch.  Arrays (5,nCells).  In the mixed mode the flux,
+ * reconstruction and limiter Jacobians are FP32, the cons -> prim Jacobian
+ * FP64 (the arithmetic of the mixed residual). */
 int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar);
 /* Tangent of the same residual: rhsDot = (dR/dcv) cvDot. */
 int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, double *rhsDot);
@@ -156,8 +158,9 @@ int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, dou
  * states only are held).  cvBar0(5,nCells) receives dJ/dcv0; with cvBar0
  * NULL only the forward sweep runs and J alone is returned.  stats[4] (may
  * be NULL): forward-sweep ms, reverse-sweep ms (recompute + adjoint), device
- * bytes held by the context and the call, number of checkpoints.  FP64
- * modes; RECONST 10 has no adjoint.  Leaves the context state untouched. */
+ * bytes held by the context and the call, number of checkpoints.  Every
+ * precision mode (the mixed mode runs its own primal and FP32-Jacobian
+ * adjoint); RECONST 10 has no adjoint.  Leaves the context state untouched. */
 int rflu_gpu_unrolled_adjoint(rflu_gpu_ctx *ctx, const double *cv0, int nSteps, double dtMin, int every, int iPatch,
                               double *J, double *cvBar0, double *stats);
 

@@ -1,5 +1,9 @@
 // Tangent (JVP) and discrete adjoint (VJP) of the residual of one region,
-// R(cv) = CellGradientsMP + ConvectiveFluxesMP, in the FP64 modes.
+// R(cv) = CellGradientsMP + ConvectiveFluxesMP, for every precision mode:
+// templated on the state type R of the View (double: FP64 modes, float: the
+// mixed mode).  In the mixed mode the flux, reconstruction and limiter
+// Jacobians are evaluated in FP32 (the arithmetic of the mixed primal), the
+// prim/dv -> cv Jacobian (pressure recovery) in FP64.
 //
 // Tangent: the primal cell/face code of kernels.cuh evaluated on Dual<1>
 // (value + one directional derivative), so every branch the primal takes
@@ -13,13 +17,14 @@
 //   2. face adjoint (one thread per face): Fbar = lambda(c1) - lambda(c2)
 //      (boundary: lambda(c)); the transposed flux Jacobian applied to Fbar
 //      from the face's local Jacobian (Dual<6>/Dual<8> seeds on the
-//      reconstructed left/right states), stored per face side;
+//      reconstructed left/right states; the FP64 modes' Roe flux has a
+//      hand-written reverse sweep), stored per face side;
 //   3. cell adjoint (one thread per cell, gather over the same CSR): side
 //      adjoints -> primitive and limited-gradient adjoints; limiter reverse
 //      through its active branch; own-term of the gradient transpose;
 //   4. cell adjoint (gather over the transposed stencil and the face
 //      neighbours): neighbour terms of the gradient and limiter transposes,
-//      then prim/dv -> cv through the local Jacobian (Dual<5>).
+//      then prim/dv -> cv through the local Jacobian (Dual<5>, FP64).
 // No atomics: every sum is a gather in a fixed order.  The adjoint covers
 // RECONST 0, 11 (Venkatakrishnan) and 100 (componentwise BJ); the
 // eigen-frame velocity limiter of RECONST 10 is covered by the tangent only.
@@ -30,32 +35,41 @@
 namespace rflu {
 namespace RFLU_NS {
 
-#ifdef RFLU_WITH_ADJOINT
+template <typename R>
 struct AdjWork {
-  double *cvd, *primd, *dvd, *gradd, *fluxd;          // tangent state / lambda in cvd
-  double *G, *lim, *faceAdj, *Gbar, *qbar, *nbBar, *cvbarD, *dvbar;
-  int *estar, *jstar;
+  R *cvd, *primd, *dvd, *gradd, *fluxd;  // tangent state / lambda in cvd
+  R *G, *lim, *faceAdj, *Gbar, *qbar, *nbBar, *cvbarD, *dvbar;
+  int *estar, *jstar;                    // 5 per cell each
 };
 
-inline size_t adjWorkDoubles(size_t nc, size_t nT) { return 96 * nc + 24 * nT + 64; }
-
-inline AdjWork carveAdjWork(double *w, size_t nc, size_t nT) {
-  AdjWork a;
-  a.cvd = w; w += 5 * nc;
-  a.primd = w; w += 5 * nc;
-  a.dvd = w; w += 3 * nc;
-  a.gradd = w; w += 15 * nc;
-  a.fluxd = w; w += 5 * nT;
-  a.G = w; w += 15 * nc;
-  a.lim = w; w += 5 * nc;
-  a.faceAdj = w; w += 16 * nT;
-  a.Gbar = w; w += 15 * nc;
-  a.qbar = w; w += 5 * nc;
-  a.nbBar = w; w += 5 * nc;
-  a.cvbarD = w; w += 5 * nc;
-  a.dvbar = w; w += 3 * nc;
-  a.estar = (int *)w; w += 3 * nc;  // 5 ints per cell
-  a.jstar = (int *)w; w += 3 * nc;
+// The workspace carved from the context's adjoint buffer: 81 Nc + 21 (Nf+Nb)
+// values of R and 10 Nc ints (the context allocates
+// sizeof(R)*(96 Nc + 24 (Nf+Nb) + 64) + 4*10 Nc + 256 bytes).
+template <typename R>
+inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
+  char *p = reinterpret_cast<char *>(work);
+  auto take = [&](size_t count) {
+    R *r = reinterpret_cast<R *>(p);
+    p += count * sizeof(R);
+    return r;
+  };
+  AdjWork<R> a;
+  a.cvd = take(5 * nc);
+  a.primd = take(5 * nc);
+  a.dvd = take(3 * nc);
+  a.gradd = take(15 * nc);
+  a.fluxd = take(5 * nT);
+  a.G = take(15 * nc);
+  a.lim = take(5 * nc);
+  a.faceAdj = take(16 * nT);
+  a.Gbar = take(15 * nc);
+  a.qbar = take(5 * nc);
+  a.nbBar = take(5 * nc);
+  a.cvbarD = take(5 * nc);
+  a.dvbar = take(3 * nc);
+  a.estar = reinterpret_cast<int *>(p);
+  p += sizeof(int) * 5 * nc;
+  a.jstar = reinterpret_cast<int *>(p);
   return a;
 }
 
@@ -81,25 +95,23 @@ __device__ inline void primFromCv(const Params &P, const S *cv, S *q, S *dv) {
   q[4] = p;
 }
 
-using D1 = Dual<1>;
-
+// Cell data of the tangent: primal values (layout of the mode) with the
+// directional derivatives of the workspace (structure of arrays).
+template <typename R>
 struct TanLoad {
-  using S = D1;
-  using H = D1;
-  const View<double> &V;
-  const AdjWork &W;
-  __device__ S mk(double v, double d) const {
-    S x(v);
-    x.d[0] = d;
+  using S = Dual<1, R>;
+  using H = Dual<1, double>;
+  const View<R> &V;
+  const AdjWork<R> &W;
+  __device__ S prim(int k, int c) const {
+    S x(PlainLoad<R>{V}.prim(k, c));
+    x.d[0] = W.primd[(size_t)k * V.nc + c];
     return x;
   }
-  __device__ S prim(int k, int c) const {
-    size_t o = (size_t)k * V.nc + c;
-    return mk(V.prim[o], W.primd[o]);
-  }
   __device__ S grad(int k, int c) const {
-    size_t o = (size_t)k * V.nc + c;
-    return mk(V.grad[o], W.gradd[o]);
+    S x(PlainLoad<R>{V}.grad(k, c));
+    x.d[0] = W.gradd[(size_t)k * V.nc + c];
+    return x;
   }
   __device__ void prim4(int c, S *q) const {
     for (int k = 0; k < 4; ++k) q[k] = prim(k, c);
@@ -107,83 +119,102 @@ struct TanLoad {
   __device__ void prim5(int c, S *q) const {
     for (int k = 0; k < 5; ++k) q[k] = prim(k, c);
   }
+  // packed layout only: prim and the centroid (no derivative)
+  __device__ void primCg(int c, S *q, S *x) const {
+    prim5(c, q);
+    for (int k = 0; k < 3; ++k) x[k] = S(V.prim[8 * (size_t)c + 5 + k]);
+  }
   __device__ void grad15(int c, S *g) const {
     for (int k = 0; k < 15; ++k) g[k] = grad(k, c);
   }
   __device__ H cv(int k, int c) const {
     size_t o = (size_t)k * V.nc + c;
-    return mk(V.cv[o], W.cvd[o]);
+    H x(V.cv[o]);
+    x.d[0] = W.cvd[o];
+    return x;
   }
   __device__ H dv(int k, int c) const {
     size_t o = (size_t)k * V.nc + c;
-    return mk(V.dv[o], W.dvd[o]);
+    H x(V.dv[o]);
+    x.d[0] = W.dvd[o];
+    return x;
   }
 };
 
 // ---------------------------------------------------------------------------
 // Tangent kernels
 // ---------------------------------------------------------------------------
-__global__ void kTanInit(View<double> V, AdjWork W, const double *cvDotRef) {
+template <typename R>
+__global__ void kTanInit(View<R> V, AdjWork<R> W, const double *cvDotRef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   const size_t n = V.nc;
   const int o = V.refId[i];
+  using D1 = Dual<1>;
   D1 cv[5], q[5], dv[3];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     cv[k] = D1(V.cv[k * n + i]);
     cv[k].d[0] = cvDotRef[5 * (size_t)o + k];
-    W.cvd[k * n + i] = cv[k].d[0];
+    W.cvd[k * n + i] = (R)cv[k].d[0];
   }
   primFromCv(V.p, cv, q, dv);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) W.primd[k * n + i] = q[k].d[0];
+  for (int k = 0; k < 5; ++k) W.primd[k * n + i] = (R)q[k].d[0];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) W.dvd[k * n + i] = dv[k].d[0];
+  for (int k = 0; k < 3; ++k) W.dvd[k * n + i] = (R)dv[k].d[0];
 }
 
-__global__ void __launch_bounds__(kBlock) kTanGrad(View<double> V, AdjWork W) {
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kTanGrad(View<R> V, AdjWork<R> W) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
-  D1 g[15];
-  gradLimitCell(V, TanLoad{V, W}, i, g);
+  Dual<1, R> g[15];
+  gradLimitCell(V, TanLoad<R>{V, W}, i, g);
   const size_t n = V.nc;
+  R gv[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) {
-    V.grad[k * n + i] = g[k].v;
+    gv[k] = g[k].v;
     W.gradd[k * n + i] = g[k].d[0];
   }
+  storeGrad(V, i, gv);
 }
 
-__global__ void __launch_bounds__(kBlock) kTanFlux(View<double> V, AdjWork W) {
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kTanFlux(View<R> V, AdjWork<R> W) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nT = V.nf + V.nb;
   if (t >= nT) return;
-  D1 flx[5];
-  faceFluxEval(V, TanLoad{V, W}, t, flx);
+  Dual<1, R> flx[5];
+  faceFluxEval(V, TanLoad<R>{V, W}, t, flx);
+  R fd[5];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) W.fluxd[(size_t)k * nT + t] = flx[k].d[0];
+  for (int k = 0; k < 5; ++k) fd[k] = flx[k].d[0];
+  storeFluxAt(W.fluxd, (size_t)nT, t, fd);
 }
 
-__global__ void kTanGather(View<double> V, AdjWork W, double *outRef) {
+template <typename R>
+__global__ void kTanGather(View<R> V, AdjWork<R> W, double *outRef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
-  double r[5];
-  gatherRhs(V, (const double *)W.fluxd, i, r);
+  R r[5];
+  gatherRhs(V, (const R *)W.fluxd, i, r);
   const int o = V.refId[i];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) outRef[5 * (size_t)o + k] = r[k];
+  for (int k = 0; k < 5; ++k) outRef[5 * (size_t)o + k] = (double)r[k];
 }
 
 // ---------------------------------------------------------------------------
 // Adjoint kernels
 // ---------------------------------------------------------------------------
-__global__ void kAdjLambda(View<double> V, AdjWork W, const double *lamRef) {
+template <typename R>
+__global__ void kAdjLambda(View<R> V, AdjWork<R> W, const double *lamRef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   const int o = V.refId[i];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) W.cvd[(size_t)k * V.nc + i] = lamRef[5 * (size_t)o + k];
+  for (int k = 0; k < 5; ++k) W.cvd[(size_t)k * V.nc + i] = (R)lamRef[5 * (size_t)o + k];
 }
 
 // Venkatakrishnan factor (RFLU_ModLimiters.F90:494-516) of one face side.
@@ -195,21 +226,25 @@ __device__ inline S venkat(S dext, S d2, S epsq) {
 }
 
 // Forward pass of the limited gradient with the limiter's active branch.
-__global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<double> V, AdjWork W) {
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   const size_t n = V.nc;
-  double q[5], g[15];
+  const PlainLoad<R> ld{V};
+  R q[5], g[15];
+  ld.prim5(i, q);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) q[k] = V.prim[k * n + i];
-#pragma unroll
-  for (int k = 0; k < 15; ++k) g[k] = 0.0;
+  for (int k = 0; k < 15; ++k) g[k] = R(0);
   for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
     const int j = V.stIdx[s];
-    const double wx = V.wx[s], wy = V.wy[s], wz = V.wz[s];
+    R wx, wy, wz;
+    lsqWeight(V, i, s, wx, wy, wz);
+    R qj[5];
+    ld.prim5(j, qj);
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      double d = V.prim[k * n + j] - q[k];
+      R d = qj[k] - q[k];
       g[3 * k] = g[3 * k] + wx * d;
       g[3 * k + 1] = g[3 * k + 1] + wy * d;
       g[3 * k + 2] = g[3 * k + 2] + wz * d;
@@ -218,10 +253,10 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<double> V, AdjWork W)
 #pragma unroll
   for (int k = 0; k < 15; ++k) W.G[k * n + i] = g[k];
   const int rc = V.p.reconst;
-  double lim[5] = {1, 1, 1, 1, 1};
+  R lim[5] = {R(1), R(1), R(1), R(1), R(1)};
   int es[5] = {-1, -1, -1, -1, -1}, js[5] = {-1, -1, -1, -1, -1};
   if (rc == 11 || rc == 100) {
-    double vmin[5], vmax[5];
+    R vmin[5], vmax[5];
     int jmin[5], jmax[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) { vmin[k] = vmax[k] = q[k]; jmin[k] = jmax[k] = -1; }
@@ -229,36 +264,38 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<double> V, AdjWork W)
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
       if (code < 0) continue;
-      const int f = code >> 1, nb = (code & 1) ? V.fc1[f] : V.fc2[f];
+      int c1, c2;
+      faceCells(V, code >> 1, c1, c2);
+      const int nb = (code & 1) ? c1 : c2;
+      R x[5];
+      ld.prim5(nb, x);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        double x = V.prim[k * n + nb];
-        if (x < vmin[k]) { vmin[k] = x; jmin[k] = nb; }
-        if (x > vmax[k]) { vmax[k] = x; jmax[k] = nb; }
+        if (x[k] < vmin[k]) { vmin[k] = x[k]; jmin[k] = nb; }
+        if (x[k] > vmax[k]) { vmax[k] = x[k]; jmax[k] = nb; }
       }
     }
-    const double epsq = V.epsq[i];
+    const R epsq = V.epsq[i];
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
       if (code < 0) continue;
-      const int f = code >> 1;
-      const double *d = (code & 1) ? V.dR : V.dL;
-      const double dx = d[f], dy = d[(size_t)V.nf + f], dz = d[2 * (size_t)V.nf + f];
+      R d[3];
+      faceOffset(V, code >> 1, code & 1, d);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        const double d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
-        if (!(d2 > 0.0) && !(d2 < 0.0)) continue;
-        const bool up = d2 > 0.0;
-        const double dext = up ? vmax[k] - q[k] : vmin[k] - q[k];
-        double t;
+        const R d2 = -(g[3 * k] * d[0] + g[3 * k + 1] * d[1] + g[3 * k + 2] * d[2]);
+        if (!(d2 > R(0)) && !(d2 < R(0))) continue;
+        const bool up = d2 > R(0);
+        const R dext = up ? vmax[k] - q[k] : vmin[k] - q[k];
+        R t;
         bool active;
         if (rc == 11) {
           t = venkat(dext, d2, epsq);
           active = true;
         } else {
-          const double x = dext / d2;
-          t = fmin2(1.0, x);
-          active = x < 1.0;
+          const R x = dext / d2;
+          t = fmin2(R(1), x);
+          active = x < R(1);
         }
         if (t < lim[k]) {
           lim[k] = t;
@@ -268,44 +305,55 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<double> V, AdjWork W)
       }
     }
   }
+  R gl[15];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     W.lim[k * n + i] = lim[k];
     W.estar[k * n + i] = es[k];
     W.jstar[k * n + i] = js[k];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) V.grad[(3 * k + c) * n + i] = lim[k] * g[3 * k + c];
+    for (int c = 0; c < 3; ++c) gl[3 * k + c] = lim[k] * g[3 * k + c];
   }
+  storeGrad(V, i, gl);
 }
 
 // Transposed flux Jacobian of one face applied to Fbar.
-template <int N>
-__device__ inline void contract(const Dual<N> *flx, const double *fbar, double *out) {
+template <int N, typename T>
+__device__ inline void contract(const Dual<N, T> *flx, const T *fbar, T *out) {
 #pragma unroll
   for (int m = 0; m < N; ++m) {
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int k = 0; k < 5; ++k) s += fbar[k] * flx[k].d[m];
     out[m] = s;
   }
 }
 
-__global__ void __launch_bounds__(kBlock) kAdjFace(View<double> V, AdjWork W) {
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nT = V.nf + V.nb;
   if (t >= nT) return;
   const Params &P = V.p;
   const size_t n = V.nc;
-  const PlainLoad<double> ld{V};
-  double *out = W.faceAdj + 16 * (size_t)t;
-  double fbar[5];
+  const PlainLoad<R> ld{V};
+  R *out = W.faceAdj + 16 * (size_t)t;
+  R fbar[5];
   if (t < V.nf) {
-    const int f = t, c1 = V.fc1[f], c2 = V.fc2[f];
+    const int f = t;
+    int c1, c2;
+    faceCells(V, f, c1, c2);
+    R nx, ny, nz, nm;
+    faceNormal(V, f, nx, ny, nz, nm);
 #pragma unroll
     for (int k = 0; k < 5; ++k) fbar[k] = W.cvd[k * n + c1] - W.cvd[k * n + c2];
     if (P.spaceOrder == 1) {
+      // first order: FP64 from cv and dv in every mode (as the primal)
       using D8 = Dual<8>;
       D8 cl[5], dl[3], cr[5], dr[3], flx[5];
+      double fb[5], o8[8];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) fb[k] = (double)fbar[k];
       for (int side = 0; side < 2; ++side) {
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
@@ -317,23 +365,27 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<double> V, AdjWork W) {
           dl[k] = side ? D8(V.dv[k * n + c1]) : D8::seed(V.dv[k * n + c1], 5 + k);
           dr[k] = side ? D8::seed(V.dv[k * n + c2], 5 + k) : D8(V.dv[k * n + c2]);
         }
-        riemann1(P, cl, dl, cr, dr, D8(V.fnx[f]), D8(V.fny[f]), D8(V.fnz[f]), D8(V.fnm[f]), flx);
-        contract(flx, fbar, out + 8 * side);
+        riemann1(P, cl, dl, cr, dr, D8((double)nx), D8((double)ny), D8((double)nz), D8((double)nm), flx);
+        contract(flx, fb, o8);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) out[8 * side + m] = (R)o8[m];
       }
     } else {
-      using D6 = Dual<6>;
-      const size_t nf = V.nf;
-      double L[5], Rt[5], irl, irr;
-      faceState(V, ld, c1, V.dL[f], V.dL[nf + f], V.dL[2 * nf + f], L, irl);
-      faceState(V, ld, c2, V.dR[f], V.dR[nf + f], V.dR[2 * nf + f], Rt, irr);
-      if (P.spaceDiscr == 1) {
-        // Roe: hand-written reverse sweep (no dependence on the cell 1/rho)
-        roe2Adjoint(P.refGamma, P.refCp, P.epsEntr, P.dissFact, V.fnx[f], V.fny[f], V.fnz[f], V.fnm[f], L, Rt, fbar,
-                    out, out + 6);
-        out[5] = 0.0;
-        out[11] = 0.0;
-        return;
+      R L[5], Rt[5], irl, irr, dl[3], dr[3];
+      faceOffset(V, f, 0, dl);
+      faceOffset(V, f, 1, dr);
+      faceState(V, ld, c1, dl[0], dl[1], dl[2], L, irl);
+      faceState(V, ld, c2, dr[0], dr[1], dr[2], Rt, irr);
+      if constexpr (Ref<R>::on) {
+        if (P.spaceDiscr == 1) {
+          // Roe: hand-written reverse sweep (no dependence on the cell 1/rho)
+          roe2Adjoint(P.refGamma, P.refCp, P.epsEntr, P.dissFact, nx, ny, nz, nm, L, Rt, fbar, out, out + 6);
+          out[5] = 0.0;
+          out[11] = 0.0;
+          return;
+        }
       }
+      using D6 = Dual<6, R>;
       D6 a[5], b[5], ia, ib, flx[5];
       for (int side = 0; side < 2; ++side) {
 #pragma unroll
@@ -343,7 +395,7 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<double> V, AdjWork W) {
         }
         ia = side ? D6(irl) : D6::seed(irl, 5);
         ib = side ? D6::seed(irr, 5) : D6(irr);
-        riemann2(P, D6(V.fnx[f]), D6(V.fny[f]), D6(V.fnz[f]), D6(V.fnm[f]), a, ia, b, ib, flx);
+        riemann2(P, D6(nx), D6(ny), D6(nz), D6(nm), a, ia, b, ib, flx);
         contract(flx, fbar, out + 6 * side);
       }
     }
@@ -352,20 +404,26 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<double> V, AdjWork W) {
     const int type = V.patchType[ip], order = V.patchOrder[ip];
 #pragma unroll
     for (int k = 0; k < 5; ++k) fbar[k] = W.cvd[k * n + c];
-    if (type == 60) fbar[0] = 0.0;  // slip walls leave rhs(DENS)
+    if (type == 60) fbar[0] = R(0);  // slip walls leave rhs(DENS)
     if (order == 1) {
       using D6 = Dual<6>;
       D6 cv[5], flx[5];
+      double fb[5], o6[6];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) cv[k] = D6::seed(V.cv[k * n + c], k);
+      for (int k = 0; k < 5; ++k) {
+        cv[k] = D6::seed(V.cv[k * n + c], k);
+        fb[k] = (double)fbar[k];
+      }
       D6 pl = D6::seed(V.dv[c], 5);
-      patch1(P, type, V.patchOutflow[ip], V.patchPout[ip], cv, pl, D6(V.bnx[b]), D6(V.bny[b]), D6(V.bnz[b]),
-             D6(V.bnm[b]), flx);
-      contract(flx, fbar, out);
+      patch1(P, type, V.patchOutflow[ip], V.patchPout[ip], cv, pl, D6((double)V.bnx[b]), D6((double)V.bny[b]),
+             D6((double)V.bnz[b]), D6((double)V.bnm[b]), flx);
+      contract(flx, fb, o6);
+#pragma unroll
+      for (int m = 0; m < 6; ++m) out[m] = (R)o6[m];
     } else {
-      using D5 = Dual<5>;
+      using D5 = Dual<5, R>;
       const size_t nb = V.nb;
-      double L[5], irl;
+      R L[5], irl;
       faceState(V, ld, c, V.bd[b], V.bd[nb + b], V.bd[2 * nb + b], L, irl);
       D5 a[5], flx[5];
 #pragma unroll
@@ -379,22 +437,24 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<double> V, AdjWork W) {
 
 // Side adjoints -> primitive / gradient adjoints of the cell, limiter reverse,
 // gradient own-term.
-__global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   const Params &P = V.p;
-  const size_t n = V.nc, nf = V.nf, nb = V.nb;
-  double qb[5] = {0, 0, 0, 0, 0}, gtb[15], cvb[5] = {0, 0, 0, 0, 0}, dvb[3] = {0, 0, 0};
+  const size_t n = V.nc, nb = V.nb;
+  const PlainLoad<R> ld{V};
+  R qb[5] = {0, 0, 0, 0, 0}, gtb[15], cvb[5] = {0, 0, 0, 0, 0}, dvb[3] = {0, 0, 0};
 #pragma unroll
-  for (int k = 0; k < 15; ++k) gtb[k] = 0.0;
-  double rbar = 0.0;
-  const double rho = V.prim[i];
+  for (int k = 0; k < 15; ++k) gtb[k] = R(0);
+  R rbar = R(0);
+  const R rho = ld.prim(0, i);
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
   for (int e = cb; e < ce; ++e) {
     const int code = V.cfEnt[e];
     if (code >= 0) {
       const int f = code >> 1, side = code & 1;
-      const double *a = W.faceAdj + 16 * (size_t)f;
+      const R *a = W.faceAdj + 16 * (size_t)f;
       if (P.spaceOrder == 1) {
         a += 8 * side;
 #pragma unroll
@@ -403,26 +463,26 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
         for (int k = 0; k < 3; ++k) dvb[k] += a[5 + k];
       } else {
         a += 6 * side;
-        const double *d = side ? V.dR : V.dL;
-        const double dx = d[f], dy = d[nf + f], dz = d[2 * nf + f];
+        R d[3];
+        faceOffset(V, f, side, d);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
           qb[k] += a[k];
-          gtb[3 * k] += a[k] * dx;
-          gtb[3 * k + 1] += a[k] * dy;
-          gtb[3 * k + 2] += a[k] * dz;
+          gtb[3 * k] += a[k] * d[0];
+          gtb[3 * k + 1] += a[k] * d[1];
+          gtb[3 * k + 2] += a[k] * d[2];
         }
         rbar += a[5];
       }
     } else {
       const int b = -code - 1;
-      const double *a = W.faceAdj + 16 * (size_t)(nf + b);
+      const R *a = W.faceAdj + 16 * (size_t)(V.nf + b);
       if (V.patchOrder[V.bpatch[b]] == 1) {
 #pragma unroll
         for (int k = 0; k < 5; ++k) cvb[k] += a[k];
         dvb[0] += a[5];
       } else {
-        const double dx = V.bd[b], dy = V.bd[nb + b], dz = V.bd[2 * nb + b];
+        const R dx = V.bd[b], dy = V.bd[nb + b], dz = V.bd[2 * nb + b];
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
           qb[k] += a[k];
@@ -434,16 +494,16 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
     }
   }
   // irl = 1/rho of the cell (HLLC: Hl = el + irl*pl)
-  qb[0] += rbar * (-1.0 / (rho * rho));
-  double gb[15], nbb[5] = {0, 0, 0, 0, 0};
+  qb[0] += rbar * (R(-1) / (rho * rho));
+  R gb[15], nbb[5] = {0, 0, 0, 0, 0};
 #pragma unroll
-  for (int k = 0; k < 15; ++k) gb[k] = 0.0;
+  for (int k = 0; k < 15; ++k) gb[k] = R(0);
   const int rc = P.reconst;
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     if (P.spaceOrder < 2) break;
-    const double l = W.lim[k * n + i];
-    double lb = 0.0;
+    const R l = W.lim[k * n + i];
+    R lb = R(0);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       gb[3 * k + c] = l * gtb[3 * k + c];
@@ -452,19 +512,18 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
     const int es = W.estar[k * n + i];
     if ((rc == 11 || rc == 100) && es >= 0) {
       const int code = V.cfEnt[es];
-      const int f = code >> 1;
-      const double *d = (code & 1) ? V.dR : V.dL;
-      const double dxyz[3] = {d[f], d[nf + f], d[2 * nf + f]};
-      double g3[3];
+      R dxyz[3];
+      faceOffset(V, code >> 1, code & 1, dxyz);
+      R g3[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) g3[c] = W.G[(3 * k + c) * n + i];
-      const double d2 = -(g3[0] * dxyz[0] + g3[1] * dxyz[1] + g3[2] * dxyz[2]);
+      const R d2 = -(g3[0] * dxyz[0] + g3[1] * dxyz[1] + g3[2] * dxyz[2]);
       const int js = W.jstar[k * n + i];
-      const double qi = V.prim[k * n + i];
-      const double dext = (js >= 0 ? V.prim[k * n + js] : qi) - qi;
-      double db, d2b;
+      const R qi = ld.prim(k, i);
+      const R dext = (js >= 0 ? ld.prim(k, js) : qi) - qi;
+      R db, d2b;
       if (rc == 11) {
-        using D2 = Dual<2>;
+        using D2 = Dual<2, R>;
         D2 phi = venkat(D2::seed(dext, 0), D2::seed(d2, 1), D2(V.epsq[i]));
         db = lb * phi.d[0];
         d2b = lb * phi.d[1];
@@ -473,7 +532,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
         // as (lb/d2) and -(lb/d2)*(dext/d2) so that a tiny d2 (differences of
         // ~1e-200 ahead of a wave) neither squares into 0 nor makes 0/0 at a
         // local extreme (dext = 0)
-        const double r = lb / d2;
+        const R r = lb / d2;
         db = r;
         d2b = -r * (dext / d2);
       }
@@ -487,7 +546,8 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
   }
   // gradient own-term: G_i = sum_s w_s (q_{m_s} - q_i)
   for (int s = V.stOff[i]; s < V.stOff[i + 1] && P.spaceOrder > 1; ++s) {
-    const double wx = V.wx[s], wy = V.wy[s], wz = V.wz[s];
+    R wx, wy, wz;
+    lsqWeight(V, i, s, wx, wy, wz);
 #pragma unroll
     for (int k = 0; k < 5; ++k) qb[k] -= wx * gb[3 * k] + wy * gb[3 * k + 1] + wz * gb[3 * k + 2];
   }
@@ -504,17 +564,19 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<double> V, AdjWork W) {
 }
 
 // Neighbour terms, then (prim, dv) -> cv; output in reference order.
-__global__ void __launch_bounds__(kBlock) kAdjCell2(View<double> V, AdjWork W, double *outRef) {
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, double *outRef) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= V.nc) return;
   const size_t n = V.nc;
-  double qb[5];
+  R qb[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) qb[k] = W.qbar[k * n + j];
   if (V.tsOff && V.p.spaceOrder > 1) {
     for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
       const int i = V.tsCell[e], s = V.tsEnt[e];
-      const double wx = V.wx[s], wy = V.wy[s], wz = V.wz[s];
+      R wx, wy, wz;
+      lsqWeight(V, i, s, wx, wy, wz);
 #pragma unroll
       for (int k = 0; k < 5; ++k)
         qb[k] += wx * W.Gbar[(3 * k) * n + i] + wy * W.Gbar[(3 * k + 1) * n + i] + wz * W.Gbar[(3 * k + 2) * n + i];
@@ -524,7 +586,9 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<double> V, AdjWork W, d
   for (int e = cb; e < ce; ++e) {
     const int code = V.cfEnt[e];
     if (code < 0) continue;
-    const int f = code >> 1, i = (code & 1) ? V.fc1[f] : V.fc2[f];
+    int c1, c2;
+    faceCells(V, code >> 1, c1, c2);
+    const int i = (code & 1) ? c1 : c2;
 #pragma unroll
     for (int k = 0; k < 5; ++k)
       if (W.jstar[k * n + i] == j && W.estar[k * n + i] >= 0) qb[k] += W.nbBar[k * n + i];
@@ -542,7 +606,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<double> V, AdjWork W, d
   for (int m = 0; m < 5; ++m) {
     double s = W.cvbarD[m * n + j];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) s += qb[k] * q[k].d[m];
+    for (int k = 0; k < 5; ++k) s += (double)qb[k] * q[k].d[m];
 #pragma unroll
     for (int k = 0; k < 3; ++k) s += dvb[k] * dv[k].d[m];
     outRef[5 * (size_t)o + m] = s;
@@ -552,29 +616,29 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<double> V, AdjWork W, d
 // Boundary-pressure functional: per-face p_f |A_f| on patch ip and the seed
 // of the face adjoint (dJ/dp_f = |A_f|); the sum is a fixed-order block
 // reduction.
-__global__ void kPatchSeed(View<double> V, AdjWork W, int ip, double *Jout) {
+template <typename R>
+__global__ void kPatchSeed(View<R> V, AdjWork<R> W, int ip, double *Jout) {
   __shared__ double part[kBlock];
-  const size_t n = V.nc, nb = V.nb;
-  const PlainLoad<double> ld{V};
+  const size_t nb = V.nb;
+  const PlainLoad<R> ld{V};
   double acc = 0.0;
   for (int b = threadIdx.x; b < V.nb; b += blockDim.x) {
     if (V.bpatch[b] != ip) continue;
     const int c = V.bcell[b];
-    const double nm = V.bnm[b];
-    double *a = W.faceAdj + 16 * (size_t)(V.nf + b);
+    const R nm = V.bnm[b];
+    R *a = W.faceAdj + 16 * (size_t)(V.nf + b);
     double pf;
     if (V.patchOrder[ip] == 1) {
       pf = V.dv[c];
       a[5] = nm;
     } else {
-      double L[5], irl;
+      R L[5], irl;
       faceState(V, ld, c, V.bd[b], V.bd[nb + b], V.bd[2 * nb + b], L, irl);
-      pf = L[4];
+      pf = (double)L[4];
       a[4] = nm;
     }
-    acc += pf * nm;
+    acc += pf * (double)nm;
   }
-  (void)n;
   part[threadIdx.x] = acc;
   __syncthreads();
   for (int s = kBlock / 2; s > 0; s >>= 1) {
@@ -588,44 +652,34 @@ template <typename R>
 struct AdjointOps {
   static void jvp(const View<R> &V, const double *cvDotRef, double *rhsDotRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
-    AdjWork W = carveAdjWork(work, V.nc, nT);
-    kTanInit<<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvDotRef);
-    if (V.p.spaceOrder > 1) kTanGrad<<<blocks(V.nc), kBlock, 0, s>>>(V, W);
-    kTanFlux<<<blocks((long long)nT), kBlock, 0, s>>>(V, W);
-    kTanGather<<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsDotRef);
+    AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
+    kTanInit<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvDotRef);
+    if (V.p.spaceOrder > 1) kTanGrad<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    kTanFlux<R><<<blocks((long long)nT), kBlock, 0, s>>>(V, W);
+    kTanGather<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsDotRef);
   }
-  static void cellAdjoint(const View<R> &V, AdjWork &W, double *cvBarRef, cudaStream_t s) {
-    kAdjCell1<<<blocks(V.nc), kBlock, 0, s>>>(V, W);
-    kAdjCell2<<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvBarRef);
+  static void cellAdjoint(const View<R> &V, AdjWork<R> &W, double *cvBarRef, cudaStream_t s) {
+    kAdjCell1<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    kAdjCell2<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvBarRef);
   }
   static void vjp(const View<R> &V, const double *rhsBarRef, double *cvBarRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
-    AdjWork W = carveAdjWork(work, V.nc, nT);
-    kAdjLambda<<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
-    if (V.p.spaceOrder > 1) kAdjGradFwd<<<blocks(V.nc), kBlock, 0, s>>>(V, W);
-    cudaMemsetAsync(W.faceAdj, 0, sizeof(double) * 16 * nT, s);
-    kAdjFace<<<blocks((long long)nT), kBlock, 0, s>>>(V, W);
+    AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
+    kAdjLambda<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
+    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    cudaMemsetAsync(W.faceAdj, 0, sizeof(R) * 16 * nT, s);
+    kAdjFace<R><<<blocks((long long)nT), kBlock, 0, s>>>(V, W);
     cellAdjoint(V, W, cvBarRef, s);
   }
   static void patchPressure(const View<R> &V, int ip, double *J, double *cvBarRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
-    AdjWork W = carveAdjWork(work, V.nc, nT);
-    if (V.p.spaceOrder > 1) kAdjGradFwd<<<blocks(V.nc), kBlock, 0, s>>>(V, W);
-    cudaMemsetAsync(W.faceAdj, 0, sizeof(double) * 16 * nT, s);
-    kPatchSeed<<<1, kBlock, 0, s>>>(V, W, ip, J);
+    AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
+    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    cudaMemsetAsync(W.faceAdj, 0, sizeof(R) * 16 * nT, s);
+    kPatchSeed<R><<<1, kBlock, 0, s>>>(V, W, ip, J);
     if (cvBarRef) cellAdjoint(V, W, cvBarRef, s);
   }
 };
-
-#else
-// Translation units without the adjoint (the mixed mode): no entries.
-template <typename R>
-struct AdjointOps {
-  static constexpr void (*jvp)(const View<R> &, const double *, double *, double *, cudaStream_t) = nullptr;
-  static constexpr void (*vjp)(const View<R> &, const double *, double *, double *, cudaStream_t) = nullptr;
-  static constexpr void (*patchPressure)(const View<R> &, int, double *, double *, double *, cudaStream_t) = nullptr;
-};
-#endif
 
 }  // namespace RFLU_NS
 }  // namespace rflu

@@ -412,7 +412,7 @@ struct Ctx : CtxBase {
     return syncEvents(false);
   }
   int adjointPrep(const double *cv) {
-    if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "adjoint kernels exist for the FP64 modes only");
+    if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "no adjoint kernels in this precision mode");
     RFLU_CUDA(cudaMemcpyAsync(cvSave, V.cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToDevice, stream));
     return setState(cv);
   }
@@ -551,7 +551,7 @@ struct Ctx : CtxBase {
                       double *stats) override {
     if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
       return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
-    if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: adjoint kernels exist for the FP64 modes only");
+    if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
     if (V.p.reconst == 10) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: RECONST 10 has no adjoint");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     const int nrk = V.p.nrkSteps;
@@ -1030,8 +1030,9 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     }
   } else {
     PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
-    PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
   }
+  // transposed stencil (adjoint of the LSQ gradient, every mode)
+  PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
 #undef PUT
   if ((rc = alloc(&V.cv, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.dv, 3 * (size_t)nc))) return rc;
@@ -1080,11 +1081,10 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   }
   for (int k = 0; k < 5; ++k) { P.arkF[k] = (float)P.ark[k]; P.grkF[k] = (float)P.grk[k]; }
   P.dvPOnly = (num->precision == RFLU_PREC_MIXED && num->spaceOrder > 1) ? 1 : 0;
-  // adjoint workspace: gradients/limiter factors/face adjoints of one residual
-  workBytes = sizeof(double) * (size_t)(96 * (size_t)nc + 24 * ((size_t)nf + nb) + 64);
-  if (num->precision != RFLU_PREC_MIXED) {
-    if ((rc = alloc((char **)&work, workBytes))) return rc;
-  }
+  // adjoint workspace (adjoint.cuh: carveAdjWork): gradients, limiter
+  // factors and branches, face adjoints of one residual, in the mode's type
+  workBytes = sizeof(R) * (size_t)(96 * (size_t)nc + 24 * ((size_t)nf + nb) + 64) + sizeof(int) * 10 * (size_t)nc + 256;
+  if ((rc = alloc((char **)&work, workBytes))) return rc;
   ops->configure(V);
   V.tileGrid = ops->tileGrid(V);
   return checkLaunch("rflu_gpu_create");

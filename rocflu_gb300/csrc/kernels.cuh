@@ -178,6 +178,32 @@ struct PlainLoad {
   __device__ H dv(int k, int c) const { return V.dv[(size_t)k * V.nc + c]; }
 };
 
+// Least-squares weight of stencil member s (cell j) of cell i
+// (RFLU_ComputeGradCellsFast_3D, :983-1044): the FP64 modes read the
+// precomputed weights; the mixed mode forms w = L d / |d|^2 from the cell's
+// matrix L and the centroid offset d = x_j - x_i of the packed records.
+template <typename R>
+__device__ inline void lsqWeight(const View<R> &V, int i, int s, R &wx, R &wy, R &wz) {
+  if constexpr (Layout<R>::packed) {
+    const int j = V.stIdx[s];
+    const size_t n = V.nc;
+    const float dx = V.prim[8 * (size_t)j + 5] - V.prim[8 * (size_t)i + 5];
+    const float dy = V.prim[8 * (size_t)j + 6] - V.prim[8 * (size_t)i + 6];
+    const float dz = V.prim[8 * (size_t)j + 7] - V.prim[8 * (size_t)i + 7];
+    const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+    const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
+    const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
+    const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
+    wx = lxx * sx + lxy * sy + lxz * sz;
+    wy = lxy * sx + lyy * sy + lyz * sz;
+    wz = lxz * sx + lyz * sy + lzz * sz;
+  } else {
+    wx = V.wx[s];
+    wy = V.wy[s];
+    wz = V.wz[s];
+  }
+}
+
 // Store of one cell's gradient record.
 template <typename R>
 __device__ inline void storeGrad(const View<R> &V, int i, const R *g) {
@@ -214,14 +240,18 @@ __device__ inline void storePrimRec(const View<R> &V, int i, R r, R u, R v, R w,
 // Flux of face t: SoA in the FP64 modes; in the packed layout one float4
 // (mass, momentum) per face followed by the nT energy fluxes.
 template <typename R>
-__device__ inline void storeFlux(const View<R> &V, size_t nT, int t, const R *f) {
+__device__ inline void storeFluxAt(R *flux, size_t nT, int t, const R *f) {
   if constexpr (Layout<R>::packed) {
-    st4(V.flux + 4 * (size_t)t, f[0], f[1], f[2], f[3]);
-    V.flux[4 * nT + t] = f[4];
+    st4(flux + 4 * (size_t)t, f[0], f[1], f[2], f[3]);
+    flux[4 * nT + t] = f[4];
   } else {
 #pragma unroll
-    for (int k = 0; k < 5; ++k) V.flux[k * nT + t] = f[k];
+    for (int k = 0; k < 5; ++k) flux[k * nT + t] = f[k];
   }
+}
+template <typename R>
+__device__ inline void storeFlux(const View<R> &V, size_t nT, int t, const R *f) {
+  storeFluxAt(V.flux, nT, t, f);
 }
 template <typename R, typename T>
 __device__ inline void loadFlux(const T *flux, size_t nT, int t, T *f) {
@@ -290,35 +320,34 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       }
     }
   } else {
-    // the same weights (RFLU_ComputeGradCellsFast_3D, :983-1044) formed here
-    // in FP32 from the R-factor coefficients and the member's centroid
-    const size_t n = V.nc;
-    const S c1111 = S(V.rcf[i]), c2222 = S(V.rcf[n + i]), c3333 = S(V.rcf[2 * n + i]);
-    const S c12 = S(V.rcf[3 * n + i]), c13 = S(V.rcf[4 * n + i]), c23 = S(V.rcf[5 * n + i]);
-    const S xi = S(V.cgx[i]), yi = S(V.cgy[i]), zi = S(V.cgz[i]);
+    // mixed mode (the tangent kernels): G = L sum_j (q_j - q_i) d_j/|d_j|^2,
+    // the formulation of gradLimitPacked; centroids carry no derivative
+    S qi[5], xi[3];
+    ld.primCg(i, qi, xi);
 #pragma unroll 2
     for (int s = sb; s < se; ++s) {
-      const int j = V.stIdx[s];
       S qj[5], xj[3];
-      ld.primCg(j, qj, xj);
-      S dx = xj[0] - xi, dy = xj[1] - yi, dz = xj[2] - zi;
-      const S term = S(1) / sqrt_(dx * dx + dy * dy + dz * dz);
-      dx = term * dx;
-      dy = term * dy;
-      dz = term * dz;
-      const S t1 = c1111 * dx;
-      const S t2 = c2222 * (dy + c12 * dx);
-      const S t3 = c3333 * (dz + c23 * dy + c13 * dx);
-      const S wx = term * (t1 + c12 * t2 + c13 * t3);
-      const S wy = term * (t2 + c23 * t3);
-      const S wz = term * t3;
+      ld.primCg(V.stIdx[s], qj, xj);
+      const S dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = xj[2] - xi[2];
+      const S inv = S(1) / (dx * dx + dy * dy + dz * dz);
+      const S sx = inv * dx, sy = inv * dy, sz = inv * dz;
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        S d = qj[k] - q[k];
-        g[3 * k] = g[3 * k] + wx * d;
-        g[3 * k + 1] = g[3 * k + 1] + wy * d;
-        g[3 * k + 2] = g[3 * k + 2] + wz * d;
+        const S d = qj[k] - q[k];
+        g[3 * k] = g[3 * k] + sx * d;
+        g[3 * k + 1] = g[3 * k + 1] + sy * d;
+        g[3 * k + 2] = g[3 * k + 2] + sz * d;
       }
+    }
+    const size_t n = V.nc;
+    const S lxx = S(V.lsq[i]), lxy = S(V.lsq[n + i]), lxz = S(V.lsq[2 * n + i]);
+    const S lyy = S(V.lsq[3 * n + i]), lyz = S(V.lsq[4 * n + i]), lzz = S(V.lsq[5 * n + i]);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const S x = g[3 * k], y = g[3 * k + 1], z = g[3 * k + 2];
+      g[3 * k] = lxx * x + lxy * y + lxz * z;
+      g[3 * k + 1] = lxy * x + lyy * y + lyz * z;
+      g[3 * k + 2] = lxz * x + lyz * y + lzz * z;
     }
   }
   const int rc = V.p.reconst;
@@ -815,6 +844,39 @@ inline size_t tileSmemBytes(const View<R> &V, bool venkat) {
   return sizeof(float) * (2 * tileBufFloats(V) + (venkat ? 3 * kMaxCellFaces * kBlock : 0));
 }
 
+// L2 prefetch of the 128-byte lines of [p, p + bytes), spread over the CTA;
+// every prefetched address lies inside the range (the first is p itself).
+__device__ inline void prefetchL2(const void *p, size_t bytes, int &lane) {
+  if (bytes == 0) return;
+  const size_t b = reinterpret_cast<size_t>(p), line0 = b >> 7;
+  const int lines = (int)(((b + bytes - 1) >> 7) - line0 + 1);
+  // line j of the range goes to thread (lane + j) mod kBlock
+  for (int j = ((int)threadIdx.x - lane) & (kBlock - 1); j < lines; j += kBlock) {
+    const size_t a = j == 0 ? b : (line0 + j) << 7;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+  }
+  lane = (lane + lines) & (kBlock - 1);
+}
+
+// The per-cell arrays the compute phase of tile t reads from global memory
+// (face entries, LSQ matrix, CSR offsets, volumes): pulled into L2 while the
+// CTA computes the tile before it.
+template <typename R, bool kDt, int kRc>
+__device__ inline void prefetchTile(const View<R> &V, int t) {
+  const size_t n = V.nc;
+  const int base = t * kTile, nIn = min(kTile, V.nc - base);
+  int lane = 0;
+  for (int k = 0; k < V.cfW; ++k) {
+    prefetchL2(V.feD + 4 * (k * n + base), 16 * (size_t)nIn, lane);
+    if (kDt) prefetchL2(V.feN + 4 * (k * n + base), 16 * (size_t)nIn, lane);
+  }
+  for (int c = 0; c < 6; ++c) prefetchL2(V.lsq + c * n + base, 4 * (size_t)nIn, lane);
+  prefetchL2(V.stOff + base, 4 * (size_t)(nIn + 1), lane);
+  prefetchL2(V.cfOff + base, 4 * (size_t)(nIn + 1), lane);
+  if (kDt) prefetchL2(V.vol + base, 8 * (size_t)nIn, lane);
+  if (kRc == 11) prefetchL2(V.epsq + base, 4 * (size_t)nIn, lane);
+}
+
 // Issue the copies of tile t into buf (this thread's share).
 template <typename R>
 __device__ inline void stageTile(const View<R> &V, int t, float *buf) {
@@ -848,9 +910,13 @@ __global__ void __launch_bounds__(kBlock, 3) kGradTile(View<R> V) {
     int t = blockIdx.x, b = 0;
     if (live && t < nTiles) stageTile(V, t, smem);
     cpAsyncCommit();
+    if (live && t < nTiles) prefetchTile<R, kDt, kRc>(V, t);
     for (; live && t < nTiles; t += gridDim.x, b ^= 1) {
       const int tn = t + gridDim.x;
-      if (tn < nTiles) stageTile(V, tn, smem + (b ^ 1) * bufFloats);
+      if (tn < nTiles) {
+        stageTile(V, tn, smem + (b ^ 1) * bufFloats);
+        prefetchTile<R, kDt, kRc>(V, tn);
+      }
       cpAsyncCommit();
       cpAsyncWait<1>();  // this thread's copies of tile t have landed
       __syncthreads();   // and everyone else's

@@ -1,6 +1,5 @@
 // Kernel instantiation of the fp64 mode: FP64, fused multiply-add allowed (-fmad=true).
 #define RFLU_NS fp64
-#define RFLU_WITH_ADJOINT 1
 #include "kernels.cuh"
 #include "adjoint.cuh"
 #include "ops.h"

@@ -1,6 +1,5 @@
 // Kernel instantiation of the fp64x mode: FP64 in the reference's evaluation order without FMA contraction (-fmad=false): bit-exact with the CPU restatement.
 #define RFLU_NS fp64x
-#define RFLU_WITH_ADJOINT 1
 #include "kernels.cuh"
 #include "adjoint.cuh"
 #include "ops.h"

@@ -96,13 +96,63 @@ def test_patch_pressure_gradient(gpu_lib):
         assert abs(fd - ad) <= 1e-6 * abs(ad) + 1e-12, (fd, ad)
 
 
-def test_adjoint_rejects_mixed_and_eigen_frame(gpu_lib):
-    c = _case(cases.DISCR_ROE, cases.RECONST_VENKAT)
-    with pytest.raises(gpu.RfluError):
-        gpu.Region(c, "mixed").vjp(c.cv0, c.cv0)
+def test_adjoint_rejects_eigen_frame(gpu_lib):
     c2 = _case(cases.DISCR_ROE, cases.RECONST_BJ)
-    with pytest.raises(gpu.RfluError):
-        gpu.Region(c2, "fp64").vjp(c2.cv0, c2.cv0)
+    for prec in ("fp64", "mixed"):
+        with pytest.raises(gpu.RfluError):
+            gpu.Region(c2, prec).vjp(c2.cv0, c2.cv0)
+
+
+# Mixed precision: the adjoint and tangent kernels evaluate the flux,
+# reconstruction and limiter Jacobians in FP32 (the mixed primal's
+# arithmetic) and the cons -> prim Jacobian in FP64.
+
+
+@pytest.mark.parametrize("discr,name", FLUXES)
+@pytest.mark.parametrize("reconst", [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP])
+def test_mixed_dot_product(gpu_lib, discr, name, reconst):
+    """<lambda, J v> = <J^T lambda, v> for the mixed tangent and adjoint, to
+    FP32 accumulation (1e-5 relative)."""
+    c = _case(discr, reconst)
+    r = gpu.Region(c, "mixed")
+    rng = np.random.default_rng(7)
+    for v in _dirs(c, 3, 1):
+        lam = rng.standard_normal(c.cv0.shape)
+        a = (lam * r.jvp(c.cv0, v)).sum()
+        b = (r.vjp(c.cv0, lam) * v).sum()
+        assert abs(a - b) <= 1e-5 * max(abs(a), abs(b)), (a, b)
+
+
+@pytest.mark.parametrize("discr,name", FLUXES)
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP])
+def test_mixed_vjp_against_fp64(gpu_lib, discr, name, reconst):
+    """The mixed VJP against the FP64 VJP and against FP64 central
+    differences (eps = 1e-6) of the FP64 residual on 16 directions: the
+    mixed Jacobian is the FP64 one to FP32 rounding (median relative
+    disagreement below 1e-4)."""
+    c = _case(discr, reconst)
+    rm, r64 = gpu.Region(c, "mixed"), gpu.Region(c, "fp64")
+    rng = np.random.default_rng(11)
+    lam = rng.standard_normal(c.cv0.shape)
+    gm, g64 = rm.vjp(c.cv0, lam), r64.vjp(c.cv0, lam)
+    assert np.isfinite(gm).all()
+    assert np.abs(gm - g64).max() <= 2e-3 * np.abs(g64).max()
+    errs = []
+    eps = 1e-6
+    for v in _dirs(c, 16, 3):
+        rp, _ = r64.residual(c.cv0 + eps * v, with_grad=False)
+        rmn, _ = r64.residual(c.cv0 - eps * v, with_grad=False)
+        fd = (lam * (rp - rmn)).sum() / (2 * eps)
+        errs.append(abs(fd - (gm * v).sum()) / abs(fd))
+    assert np.median(errs) < 1e-4, errs
+
+
+def test_mixed_patch_pressure_gradient(gpu_lib):
+    c = _case(cases.DISCR_HLLC, cases.RECONST_VENKAT)
+    Jm, gm = gpu.Region(c, "mixed").patch_pressure(c.cv0, 1)
+    J64, g64 = gpu.Region(c, "fp64").patch_pressure(c.cv0, 1)
+    assert abs(Jm - J64) <= 1e-6 * abs(J64)
+    assert np.abs(gm - g64).max() <= 1e-4 * np.abs(g64).max()
 
 
 @pytest.mark.parametrize("reconst", [cases.RECONST_BJ_COMP, cases.RECONST_VENKAT])
