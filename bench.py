@@ -322,6 +322,16 @@ def run_ours(args):
         at = areg.adjoint_times(5)
         adjoint = {"workload": "adjoint_tets%d_roe_venkat" % args.adj_n, "cells": areg.n_cells,
                    "primal_residual_ms": at[0], "vjp_ms": at[1], "vjp_over_primal": at[1] / at[0]}
+        # the mixed-precision VJP (FP32 flux/limiter Jacobians) on the same
+        # case, and its agreement with the FP64 VJP for one seeded lambda
+        mreg = gpu.Region(ac, "mixed")
+        mt = mreg.adjoint_times(5)
+        lam = np.random.default_rng(2).standard_normal(ac.cv0.shape)
+        g64, gm = areg.vjp(ac.cv0, lam), mreg.vjp(ac.cv0, lam)
+        adjoint["mixed"] = {"primal_residual_ms": mt[0], "vjp_ms": mt[1], "vjp_over_primal": mt[1] / mt[0],
+                            "vjp_over_fp64_primal": mt[1] / at[0],
+                            "rel_diff_vs_fp64_vjp": float(np.abs(gm - g64).max() / np.abs(g64).max())}
+        mreg.close()
         areg.close()
 
     unrolled = None if args.skip_unrolled else unrolled_adjoint(args, cases, gpu)
@@ -421,6 +431,16 @@ def unrolled_adjoint(args, cases, gpu):
                               "below_1e-6": int((errs < 1e-6).sum()), "below_1e-5": int((errs < 1e-5).sum()),
                               "below_1e-4": int((errs < 1e-4).sum()), "not_finite": int((~ok).sum()),
                               "ad_abs_median": float(np.median(absd))})
+        if name == "smooth_background":
+            # the same gradient with the mixed primal and mixed stage VJPs
+            mreg = gpu.Region(c, "mixed")
+            Jm, gm, stm = mreg.unrolled_adjoint(cv0, n, dt, every, 1)
+            res["mixed"] = {"J": Jm, "forward_ms": stm["forward_ms"], "reverse_ms": stm["reverse_ms"],
+                            "adjoint_over_primal": stm["reverse_ms"] / stm["forward_ms"],
+                            "reverse_speedup_vs_fp64": st["reverse_ms"] / stm["reverse_ms"],
+                            "device_bytes": stm["device_bytes"],
+                            "grad_rel_diff_vs_fp64": float(np.abs(gm - g).max() / np.abs(g).max())}
+            mreg.close()
         out[name] = res
     reg.close()
     return out

@@ -265,6 +265,27 @@ __device__ inline void loadFlux(const T *flux, size_t nT, int t, T *f) {
   }
 }
 
+// Mixed mode: primitive state from the FP64 master cv.  1/rho from an FP32
+// seed y (also the FP32 velocities' reciprocal) refined once in FP64,
+// y + y*(1 - rho*y) (quadratic convergence: ~2^-44), and the pressure in FP64
+// from the kinetic energy (the cancellation at strong shocks).
+struct MixedPrim {
+  float rf, irf, uf, vf, wf;
+  double ir, ke, pr;
+  __device__ MixedPrim(const Params &P, const double *cv) {
+    rf = (float)cv[0];
+    irf = 1.0f / rf;
+    ir = (double)irf;
+    ir = fma(ir, fma(-cv[0], ir, 1.0), ir);
+    const double msq = cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3];
+    ke = 0.5 * msq * ir;
+    pr = (P.gRT - 1.0) * (cv[4] - ke);
+    uf = (float)cv[1] * irf;
+    vf = (float)cv[2] * irf;
+    wf = (float)cv[3] * irf;
+  }
+};
+
 // prim = (rho, u, v, w, p) as RFLU_ConvertCvCons2Prim DUVWP builds it
 // (modflu/RFLU_ModConvertCv.F90:214-224)
 template <typename R>
@@ -282,10 +303,20 @@ __global__ void kInitState(View<R> V) {
   double cv[5], pr, t, c;
   loadCv(V, i, cv);
   dependentVars(V.p, cv, pr, t, c);
-  V.dv[i] = pr;
-  V.dv[(size_t)V.nc + i] = t;
-  V.dv[2 * (size_t)V.nc + i] = c;
-  storePrim(V, i, cv, pr);
+  if constexpr (Layout<R>::packed) {
+    // the primitive record exactly as the mixed update forms it, so that a
+    // state restarted from cv continues bit for bit
+    MixedPrim m(V.p, cv);
+    V.dv[i] = m.pr;
+    V.dv[(size_t)V.nc + i] = t;
+    V.dv[2 * (size_t)V.nc + i] = c;
+    storePrimRec(V, i, m.rf, m.uf, m.vf, m.wf, (float)m.pr);
+  } else {
+    V.dv[i] = pr;
+    V.dv[(size_t)V.nc + i] = t;
+    V.dv[2 * (size_t)V.nc + i] = c;
+    storePrim(V, i, cv, pr);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1368,16 +1399,10 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
 #pragma unroll
     for (int k = 0; k < 5; ++k) V.rhsSum[k * n + i] = (R)rs[k];
   }
-  // 1/rho: FP32 seed y (also the FP32 velocities' reciprocal), then
-  // y + y*(1 - rho*y) in FP64
-  const float rf = (float)cv[0];
-  const float irf = 1.0f / rf;
-  double ir = (double)irf;
-  ir = fma(ir, fma(-cv[0], ir, 1.0), ir);
-  const double msq = cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3];
-  double ke = 0.5 * msq * ir;
-  double pr = (P.gRT - 1.0) * (cv[4] - ke);
-  const float uf = (float)cv[1] * irf, vf = (float)cv[2] * irf, wf = (float)cv[3] * irf;
+  const MixedPrim m(P, cv);
+  const float rf = m.rf, uf = m.uf, vf = m.vf, wf = m.wf;
+  const double ir = m.ir, ke = m.ke;
+  double pr = m.pr;
   if (isnan(rf) || isnan(uf) || isnan(vf) || isnan(wf) || isnan((float)pr)) {
     atomicAdd(&V.sc->nanCells, 1ull);
     atomicMin(&V.sc->firstBadCell, V.refId[i] + 1);
