@@ -330,7 +330,10 @@ def run_ours(args):
         g64, gm = areg.vjp(ac.cv0, lam), mreg.vjp(ac.cv0, lam)
         adjoint["mixed"] = {"primal_residual_ms": mt[0], "vjp_ms": mt[1], "vjp_over_primal": mt[1] / mt[0],
                             "vjp_over_fp64_primal": mt[1] / at[0],
-                            "rel_diff_vs_fp64_vjp": float(np.abs(gm - g64).max() / np.abs(g64).max())}
+                            # norm-wise, and the worst cell (limiter branches
+                            # near a tie can resolve differently in FP32)
+                            "rel_l2_diff_vs_fp64_vjp": float(np.linalg.norm(gm - g64) / np.linalg.norm(g64)),
+                            "rel_max_diff_vs_fp64_vjp": float(np.abs(gm - g64).max() / np.abs(g64).max())}
         mreg.close()
         areg.close()
 
@@ -439,7 +442,8 @@ def unrolled_adjoint(args, cases, gpu):
                             "adjoint_over_primal": stm["reverse_ms"] / stm["forward_ms"],
                             "reverse_speedup_vs_fp64": st["reverse_ms"] / stm["reverse_ms"],
                             "device_bytes": stm["device_bytes"],
-                            "grad_rel_diff_vs_fp64": float(np.abs(gm - g).max() / np.abs(g).max())}
+                            "grad_rel_l2_diff_vs_fp64": float(np.linalg.norm(gm - g) / np.linalg.norm(g)),
+                            "grad_rel_max_diff_vs_fp64": float(np.abs(gm - g).max() / np.abs(g).max())}
             mreg.close()
         out[name] = res
     reg.close()

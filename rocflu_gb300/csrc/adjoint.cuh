@@ -17,8 +17,8 @@
 //   2. face adjoint (one thread per face): Fbar = lambda(c1) - lambda(c2)
 //      (boundary: lambda(c)); the transposed flux Jacobian applied to Fbar
 //      from the face's local Jacobian (Dual<6>/Dual<8> seeds on the
-//      reconstructed left/right states; the FP64 modes' Roe flux has a
-//      hand-written reverse sweep), stored per face side;
+//      reconstructed left/right states; the Roe flux has a hand-written
+//      reverse sweep), stored per face side;
 //   3. cell adjoint (one thread per cell, gather over the same CSR): side
 //      adjoints -> primitive and limited-gradient adjoints; limiter reverse
 //      through its active branch; own-term of the gradient transpose;
@@ -376,14 +376,13 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W) {
       faceOffset(V, f, 1, dr);
       faceState(V, ld, c1, dl[0], dl[1], dl[2], L, irl);
       faceState(V, ld, c2, dr[0], dr[1], dr[2], Rt, irr);
-      if constexpr (Ref<R>::on) {
-        if (P.spaceDiscr == 1) {
-          // Roe: hand-written reverse sweep (no dependence on the cell 1/rho)
-          roe2Adjoint(P.refGamma, P.refCp, P.epsEntr, P.dissFact, nx, ny, nz, nm, L, Rt, fbar, out, out + 6);
-          out[5] = 0.0;
-          out[11] = 0.0;
-          return;
-        }
+      if (P.spaceDiscr == 1) {
+        // Roe: hand-written reverse sweep in the mode's arithmetic (no
+        // dependence on the cell 1/rho)
+        roe2Adjoint(P.refGamma, P.refCp, P.epsEntr, P.dissFact, nx, ny, nz, nm, L, Rt, fbar, out, out + 6);
+        out[5] = R(0);
+        out[11] = R(0);
+        return;
       }
       using D6 = Dual<6, R>;
       D6 a[5], b[5], ia, ib, flx[5];
