@@ -40,11 +40,17 @@ struct AdjWork {
   R *cvd, *primd, *dvd, *gradd, *fluxd;  // tangent state / lambda in cvd
   R *G, *lim, *faceAdj, *Gbar, *qbar, *nbBar, *cvbarD, *dvbar;
   int *estar, *jstar;                    // 5 per cell each
+  // packed layout: per cell i a 24-float record (L_i Gbar_i for the five
+  // variables, 15 floats; the centroid x_i; pad), so that a transposed
+  // stencil entry of cell j costs three 256-bit loads:
+  // w_s . Gbar_i = (d/|d|^2) . (L_i Gbar_i), d = x_j - x_i (L symmetric)
+  R *adjRec;
 };
 
 // The workspace carved from the context's adjoint buffer: 81 Nc + 21 (Nf+Nb)
-// values of R and 10 Nc ints (the context allocates
-// sizeof(R)*(96 Nc + 24 (Nf+Nb) + 64) + 4*10 Nc + 256 bytes).
+// values of R, 10 Nc ints and (packed layout) 24 Nc floats on a 32-byte
+// boundary (the context allocates sizeof(R)*(120 Nc + 24 (Nf+Nb) + 64) +
+// 4*10 Nc + 256 bytes).
 template <typename R>
 inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
   char *p = reinterpret_cast<char *>(work);
@@ -70,6 +76,9 @@ inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
   a.estar = reinterpret_cast<int *>(p);
   p += sizeof(int) * 5 * nc;
   a.jstar = reinterpret_cast<int *>(p);
+  p += sizeof(int) * 5 * nc;
+  p = reinterpret_cast<char *>((reinterpret_cast<size_t>(p) + 31) & ~size_t(31));
+  a.adjRec = reinterpret_cast<R *>(p);
   return a;
 }
 
@@ -552,6 +561,26 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   }
 #pragma unroll
   for (int k = 0; k < 15; ++k) W.Gbar[k * n + i] = gb[k];
+  if constexpr (Layout<R>::packed) {
+    const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
+    const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
+    float h[24];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const float x = gb[3 * k], y = gb[3 * k + 1], z = gb[3 * k + 2];
+      h[3 * k] = lxx * x + lxy * y + lxz * z;
+      h[3 * k + 1] = lxy * x + lyy * y + lyz * z;
+      h[3 * k + 2] = lxz * x + lyz * y + lzz * z;
+    }
+    h[15] = V.prim[8 * (size_t)i + 5];
+    h[16] = V.prim[8 * (size_t)i + 6];
+    h[17] = V.prim[8 * (size_t)i + 7];
+#pragma unroll
+    for (int k = 18; k < 24; ++k) h[k] = 0.f;
+    float *rec = W.adjRec + 24 * (size_t)i;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) st4(rec + 4 * q, h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+  }
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     W.qbar[k * n + i] = qb[k];
@@ -572,13 +601,29 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
 #pragma unroll
   for (int k = 0; k < 5; ++k) qb[k] = W.qbar[k * n + j];
   if (V.tsOff && V.p.spaceOrder > 1) {
-    for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
-      const int i = V.tsCell[e], s = V.tsEnt[e];
-      R wx, wy, wz;
-      lsqWeight(V, i, s, wx, wy, wz);
+    if constexpr (Layout<R>::packed) {
+      const float xj = V.prim[8 * (size_t)j + 5], yj = V.prim[8 * (size_t)j + 6], zj = V.prim[8 * (size_t)j + 7];
+      for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
+        float h[24];
+        const float *rec = W.adjRec + 24 * (size_t)V.tsCell[e];
+        ld8(rec, h);
+        ld8(rec + 8, h + 8);
+        ld8(rec + 16, h + 16);
+        const float dx = xj - h[15], dy = yj - h[16], dz = zj - h[17];
+        const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+        const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
 #pragma unroll
-      for (int k = 0; k < 5; ++k)
-        qb[k] += wx * W.Gbar[(3 * k) * n + i] + wy * W.Gbar[(3 * k + 1) * n + i] + wz * W.Gbar[(3 * k + 2) * n + i];
+        for (int k = 0; k < 5; ++k) qb[k] += sx * h[3 * k] + sy * h[3 * k + 1] + sz * h[3 * k + 2];
+      }
+    } else {
+      for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
+        const int i = V.tsCell[e], s = V.tsEnt[e];
+        R wx, wy, wz;
+        lsqWeight(V, i, s, wx, wy, wz);
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+          qb[k] += wx * W.Gbar[(3 * k) * n + i] + wy * W.Gbar[(3 * k + 1) * n + i] + wz * W.Gbar[(3 * k + 2) * n + i];
+      }
     }
   }
   const int cb = V.cfOff[j], ce = (V.p.spaceOrder > 1) ? V.cfOff[j + 1] : cb;

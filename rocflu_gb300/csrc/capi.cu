@@ -1083,7 +1083,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   P.dvPOnly = (num->precision == RFLU_PREC_MIXED && num->spaceOrder > 1) ? 1 : 0;
   // adjoint workspace (adjoint.cuh: carveAdjWork): gradients, limiter
   // factors and branches, face adjoints of one residual, in the mode's type
-  workBytes = sizeof(R) * (size_t)(96 * (size_t)nc + 24 * ((size_t)nf + nb) + 64) + sizeof(int) * 10 * (size_t)nc + 256;
+  workBytes = sizeof(R) * (size_t)(120 * (size_t)nc + 24 * ((size_t)nf + nb) + 64) + sizeof(int) * 10 * (size_t)nc + 256;
   if ((rc = alloc((char **)&work, workBytes))) return rc;
   ops->configure(V);
   V.tileGrid = ops->tileGrid(V);
