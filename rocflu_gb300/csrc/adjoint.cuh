@@ -1,9 +1,10 @@
 // Tangent (JVP) and discrete adjoint (VJP) of the residual of one region,
 // R(cv) = CellGradientsMP + ConvectiveFluxesMP, for every precision mode:
 // templated on the state type R of the View (double: FP64 modes, float: the
-// mixed mode).  In the mixed mode the flux, reconstruction and limiter
-// Jacobians are evaluated in FP32 (the arithmetic of the mixed primal), the
-// prim/dv -> cv Jacobian (pressure recovery) in FP64.
+// mixed mode).  In the mixed mode the flux, reconstruction, limiter and
+// prim/dv -> cv Jacobians are evaluated in FP32 (the arithmetic of the mixed
+// primal's fluxes; the Jacobian of the pressure recovery has no cancellation,
+// unlike the recovery itself).
 //
 // Tangent: the primal cell/face code of kernels.cuh evaluated on Dual<1>
 // (value + one directional derivative), so every branch the primal takes
@@ -24,7 +25,8 @@
 //      through its active branch; own-term of the gradient transpose;
 //   4. cell adjoint (gather over the transposed stencil and the face
 //      neighbours): neighbour terms of the gradient and limiter transposes,
-//      then prim/dv -> cv through the local Jacobian (Dual<5>, FP64).
+//      then prim/dv -> cv through the local Jacobian (Dual<5> in FP64; the
+//      mixed mode's closed form in FP32).
 // No atomics: every sum is a gather in a fixed order.  The adjoint covers
 // RECONST 0, 11 (Venkatakrishnan) and 100 (componentwise BJ); the
 // eigen-frame velocity limiter of RECONST 10 is covered by the tangent only.
@@ -637,23 +639,54 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
     for (int k = 0; k < 5; ++k)
       if (W.jstar[k * n + i] == j && W.estar[k * n + i] >= 0) qb[k] += W.nbBar[k * n + i];
   }
-  using D5 = Dual<5>;
-  D5 cv[5], q[5], dv[3];
-#pragma unroll
-  for (int k = 0; k < 5; ++k) cv[k] = D5::seed(V.cv[k * n + j], k);
-  primFromCv(V.p, cv, q, dv);
-  double dvb[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) dvb[k] = W.dvbar[k * n + j];
   const int o = V.refId[j];
+  if constexpr (Layout<R>::packed) {
+    // (prim, dv) -> cv in FP32 from the primitive record: the Jacobian has no
+    // cancellation (dp/dcv = (g-1)(|u|^2/2, -u, -v, -w, 1)); only the
+    // primal's recovery of p itself needs FP64
+    const float *rec = V.prim + 8 * (size_t)j;
+    const float r = rec[0], u = rec[1], v = rec[2], w = rec[3], pr = rec[4];
+    const float g = V.p.refGammaF, gc = (float)V.p.gcR;
+    const float ir = 1.f / r;
+    const float dp[5] = {(g - 1.f) * 0.5f * (u * u + v * v + w * w), -(g - 1.f) * u, -(g - 1.f) * v, -(g - 1.f) * w,
+                         g - 1.f};
+    float out[5];
 #pragma unroll
-  for (int m = 0; m < 5; ++m) {
-    double s = W.cvbarD[m * n + j];
+    for (int m = 0; m < 5; ++m) out[m] = W.cvbarD[m * n + j] + qb[4] * dp[m];
+    out[0] += qb[0] - ir * (qb[1] * u + qb[2] * v + qb[3] * w);
+    out[1] += ir * qb[1];
+    out[2] += ir * qb[2];
+    out[3] += ir * qb[3];
+    // dv = (p, T, c): T = p/(r gc), c = sqrt(g gc T)
+    const float b0 = W.dvbar[j], b1 = W.dvbar[n + j], b2 = W.dvbar[2 * n + j];
+    if (b0 != 0.f || b1 != 0.f || b2 != 0.f) {
+      const float t = pr * ir / gc, c = sqrtf(g * gc * t);
+      const float tb = b1 + b2 * 0.5f * g * gc / c;  // adjoint of T
+      const float pb = b0 + tb * ir / gc;            // of p through T
 #pragma unroll
-    for (int k = 0; k < 5; ++k) s += (double)qb[k] * q[k].d[m];
+      for (int m = 0; m < 5; ++m) out[m] += pb * dp[m];
+      out[0] += -tb * t * ir;                        // dT/drho at fixed p
+    }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s += dvb[k] * dv[k].d[m];
-    outRef[5 * (size_t)o + m] = s;
+    for (int m = 0; m < 5; ++m) outRef[5 * (size_t)o + m] = (double)out[m];
+  } else {
+    using D5 = Dual<5>;
+    D5 cv[5], q[5], dv[3];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) cv[k] = D5::seed(V.cv[k * n + j], k);
+    primFromCv(V.p, cv, q, dv);
+    double dvb[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dvb[k] = W.dvbar[k * n + j];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      double s = W.cvbarD[m * n + j];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) s += (double)qb[k] * q[k].d[m];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) s += dvb[k] * dv[k].d[m];
+      outRef[5 * (size_t)o + m] = s;
+    }
   }
 }
 
