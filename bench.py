@@ -275,25 +275,26 @@ def run_ours(args):
     if not args.skip_e2e:
         reg = regions["mixed"]
         host_cv = torch.empty((reg.n_cells, 5), dtype=torch.float64).pin_memory()
-        host_dv = torch.empty((reg.n_cells, 3), dtype=torch.float64).pin_memory()
-        cv_np, dv_np = host_cv.numpy(), host_dv.numpy()
+        cv_np = host_cv.numpy()
         cv_np[:] = cv_m
         t = 1.0
+        # each step: cv host -> device (upload_state), one RungeKuttaMP step,
+        # the new cv device -> host (download_state; dv is derived from cv)
         for _ in range(args.warmup):
             reg.upload(cv_np)
             _, t, _ = reg.step(1, t)
-            reg.download(cv_np, dv_np)
+            reg.download(cv_np, with_dv=False)
         barrier()
         w0 = time.perf_counter()
         for _ in range(args.steps):
             reg.upload(cv_np)
             _, t, _ = reg.step(1, t)
-            reg.download(cv_np, dv_np)
+            reg.download(cv_np, with_dv=False)
         barrier()
         wall = time.perf_counter() - w0
         units = reg.n_cells * reg.n_stages * args.steps
         e2e = {"value": ws * units / wall / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(host_cv.numel() * 8),
-               "d2h_bytes_per_step": int((host_cv.numel() + host_dv.numel()) * 8)}
+               "d2h_bytes_per_step": int(host_cv.numel() * 8)}
     clocks = clk.stop()
 
     # roofline of the dominant kernel of the mixed path

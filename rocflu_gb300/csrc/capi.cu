@@ -271,8 +271,7 @@ struct Ctx : CtxBase {
   }
   int setState(const double *cv) {
     RFLU_CUDA(cudaMemcpyAsync(staging, cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
-    kPermuteIn<<<nblk(V.nc), 256, 0, stream>>>(staging, V.cv, V.refId, V.nc);
-    ops->initState(V, stream);
+    ops->initFromRef(V, staging, stream);
     return checkLaunch("upload");
   }
 

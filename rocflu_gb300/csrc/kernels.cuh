@@ -297,26 +297,54 @@ __device__ inline void storePrim(const View<R> &V, int i, const double *cv, doub
 // Dependent variables and primitive state of every cell from cv
 // (RFLU_SetVarsContWrapper after upload).
 template <typename R>
-__global__ void kInitState(View<R> V) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= V.nc) return;
-  double cv[5], pr, t, c;
-  loadCv(V, i, cv);
-  dependentVars(V.p, cv, pr, t, c);
+__device__ inline void initCell(const View<R> &V, int i, const double *cv) {
   if constexpr (Layout<R>::packed) {
     // the primitive record exactly as the mixed update forms it, so that a
-    // state restarted from cv continues bit for bit
-    MixedPrim m(V.p, cv);
+    // state restarted from cv continues bit for bit; T and c only when a
+    // kernel of the step reads them (else formed at read-out)
+    const MixedPrim m(V.p, cv);
     V.dv[i] = m.pr;
-    V.dv[(size_t)V.nc + i] = t;
-    V.dv[2 * (size_t)V.nc + i] = c;
+    if (!V.p.dvPOnly) {
+      double pr, t, c;
+      dependentVars(V.p, cv, pr, t, c);
+      V.dv[(size_t)V.nc + i] = t;
+      V.dv[2 * (size_t)V.nc + i] = c;
+    }
     storePrimRec(V, i, m.rf, m.uf, m.vf, m.wf, (float)m.pr);
   } else {
+    double pr, t, c;
+    dependentVars(V.p, cv, pr, t, c);
     V.dv[i] = pr;
     V.dv[(size_t)V.nc + i] = t;
     V.dv[2 * (size_t)V.nc + i] = c;
     storePrim(V, i, cv, pr);
   }
+}
+
+template <typename R>
+__global__ void kInitState(View<R> V) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  double cv[5];
+  loadCv(V, i, cv);
+  initCell(V, i, cv);
+}
+
+// Upload in one pass: cv(5,nCells) in the reference's order and layout
+// (staged on the device) -> the renumbered master cv, primitive state and
+// dependent variables.
+template <typename R>
+__global__ void kInitFromRef(View<R> V, const double *ref) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  const size_t o = (size_t)V.refId[i];
+  double cv[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    cv[k] = ref[5 * o + k];
+    V.cv[(size_t)k * V.nc + i] = cv[k];
+  }
+  initCell(V, i, cv);
 }
 
 // ---------------------------------------------------------------------------
@@ -1573,6 +1601,9 @@ __global__ void kStepEnd(View<R> V) {
 template <typename R>
 struct Launch {
   static void initState(const View<R> &V, cudaStream_t s) { kInitState<R><<<blocks(V.nc), kBlock, 0, s>>>(V); }
+  static void initFromRef(const View<R> &V, const double *ref, cudaStream_t s) {
+    kInitFromRef<R><<<blocks(V.nc), kBlock, 0, s>>>(V, ref);
+  }
   static void gradLimit(const View<R> &V, cudaStream_t s) {
     if (V.p.spaceOrder < 2) return;
     if (V.tiled) launchTile<false>(V, s);

@@ -7,7 +7,7 @@
 namespace rflu {
 const Ops<float> *opsMixed() {
   using L = mixed::Launch<float>;
-  static const Ops<float> ops = {L::initState, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
+  static const Ops<float> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, mixed::AdjointOps<float>::jvp, mixed::AdjointOps<float>::vjp,
                                  mixed::AdjointOps<float>::patchPressure};
   return &ops;

@@ -11,6 +11,7 @@ namespace rflu {
 template <typename R>
 struct Ops {
   void (*initState)(const View<R> &, cudaStream_t);
+  void (*initFromRef)(const View<R> &, const double *cvRef, cudaStream_t);  // permute-in + initState
   void (*gradLimit)(const View<R> &, cudaStream_t);
   void (*faceFlux)(const View<R> &, cudaStream_t);
   void (*gatherRhs)(const View<R> &, cudaStream_t);

@@ -247,10 +247,14 @@ class Region:
         assert cv.shape == (self.n_cells, 5)
         _check(lib().rflu_gpu_upload_state(self.h, _p(cv)))
 
-    def download(self, cv_out=None, dv_out=None):
+    def download(self, cv_out=None, dv_out=None, with_dv=True):
+        """cv (and dv unless with_dv is False: rflu_gpu_download_state with a
+        NULL dv) in reference order."""
         cv = np.empty((self.n_cells, 5)) if cv_out is None else cv_out
-        dv = np.empty((self.n_cells, 3)) if dv_out is None else dv_out
-        _check(lib().rflu_gpu_download_state(self.h, _p(cv), _p(dv)))
+        dv = None
+        if with_dv:
+            dv = np.empty((self.n_cells, 3)) if dv_out is None else dv_out
+        _check(lib().rflu_gpu_download_state(self.h, _p(cv), _p(dv) if dv is not None else None))
         return cv, dv
 
     def timestep(self, current_time):
