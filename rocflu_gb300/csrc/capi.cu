@@ -102,6 +102,27 @@ __global__ void kAxpyInPlace(double *y, double a, const double *x, size_t n) {
 }
 __global__ void kAccumJ(double *acc, const double *j, double dt) { *acc += dt * *j; }
 
+// Download in one pass: renumbered SoA (ncomp rows) -> reference order and
+// layout, one thread per reference cell so that the writes to `dst` are
+// contiguous (dst may be the caller's pinned host buffer).
+__global__ void kGatherOut(const double *src, double *dst, const int *newId, int nc, int ncomp) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= nc) return;
+  const int i = newId[o];
+  for (int k = 0; k < ncomp; ++k) dst[(size_t)ncomp * o + k] = src[(size_t)k * nc + i];
+}
+
+// The device address of a host buffer the kernels can access directly
+// (pinned, mapped memory), or null for pageable memory.
+inline const void *mappedHostPtr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
+
 // T and c of RFLU_SetDependentVars (TCPERF) from cv and p, for a mixed-mode
 // context whose steps store p only.
 __global__ void kDvFill(const double *cv, double *dv, int nc, double gcR, double gRT) {
@@ -269,9 +290,15 @@ struct Ctx : CtxBase {
     ops->faceFlux(V, stream);
     ops->gatherUpdate(V, iStage, &V.sc->dtMin, stream);
   }
+  // cv(5,nCells) of the host: read by the upload kernel straight from a
+  // pinned buffer, else staged with one copy
   int setState(const double *cv) {
-    RFLU_CUDA(cudaMemcpyAsync(staging, cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
-    ops->initFromRef(V, staging, stream);
+    const double *src = static_cast<const double *>(mappedHostPtr(cv));
+    if (!src) {
+      RFLU_CUDA(cudaMemcpyAsync(staging, cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
+      src = staging;
+    }
+    ops->initFromRef(V, src, stream);
     return checkLaunch("upload");
   }
 
@@ -283,15 +310,23 @@ struct Ctx : CtxBase {
   }
   int download(double *cv, double *dv) override {
     if (dv && V.p.dvPOnly) kDvFill<<<nblk(V.nc), 256, 0, stream>>>(V.cv, V.dv, V.nc, V.p.gcR, V.p.gRT);
+    // pinned host buffers are written by the gather kernel directly
     if (cv) {
-      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.refId, V.nc, 5, V.nc, 1);
-      RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
+      if (double *dst = static_cast<double *>(const_cast<void *>(mappedHostPtr(cv)))) {
+        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.cv, dst, V.newId, V.nc, 5);
+      } else {
+        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.newId, V.nc, 5);
+        RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
+      }
     }
     if (dv) {
-      kPermuteOut<double><<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.refId, V.nc, 3, V.nc,
-                                                          1);
-      RFLU_CUDA(cudaMemcpyAsync(dv, staging + 5 * (size_t)V.nc, sizeof(double) * 3 * (size_t)V.nc,
-                                cudaMemcpyDeviceToHost, stream));
+      if (double *dst = static_cast<double *>(const_cast<void *>(mappedHostPtr(dv)))) {
+        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.dv, dst, V.newId, V.nc, 3);
+      } else {
+        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.newId, V.nc, 3);
+        RFLU_CUDA(cudaMemcpyAsync(dv, staging + 5 * (size_t)V.nc, sizeof(double) * 3 * (size_t)V.nc,
+                                  cudaMemcpyDeviceToHost, stream));
+      }
     }
     int rc = checkLaunch("download");
     if (rc) return rc;
@@ -1018,7 +1053,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   PUT(V.cfOff, cfOff, int); PUT(V.cfEnt, cfEnt, int);
   PUT(V.stOff, stOff, int); PUT(V.stIdx, stIdx, int);
   PUT(V.vol, vol, double); PUT(V.epsq, epsq, R);
-  PUT(V.refId, refId, int);
+  PUT(V.refId, refId, int); PUT(V.newId, newId, int);
   if (mixed) {
     // weights formed in the gradient kernel from the R factor and centroids
     PUT(V.cgx, cgx, R); PUT(V.cgy, cgy, R); PUT(V.cgz, cgz, R);

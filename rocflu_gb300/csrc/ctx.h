@@ -109,6 +109,7 @@ struct View {
   // INT_MIN (no entry); and the face's (nx, ny, nz, nm)
   const float *feD, *feN;           // 4 floats per entry
   const int *refId;                 // renumbered -> reference (0-based) cell id
+  const int *newId;                 // reference (0-based) -> renumbered cell id
   // transposed stencil (FP64 modes): for cell j, the (cell i, entry s) pairs
   // of the stencils that contain j, for the adjoint of the LSQ gradient
   const int *tsOff, *tsCell, *tsEnt;

@@ -330,18 +330,19 @@ __global__ void kInitState(View<R> V) {
   initCell(V, i, cv);
 }
 
-// Upload in one pass: cv(5,nCells) in the reference's order and layout
-// (staged on the device) -> the renumbered master cv, primitive state and
-// dependent variables.
+// Upload in one pass: cv(5,nCells) in the reference's order and layout ->
+// the renumbered master cv, primitive state and dependent variables.  One
+// thread per reference cell, so that the reads of `ref` are contiguous: it
+// may be the caller's pinned host buffer, read over the host link.
 template <typename R>
 __global__ void kInitFromRef(View<R> V, const double *ref) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= V.nc) return;
-  const size_t o = (size_t)V.refId[i];
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= V.nc) return;
+  const int i = V.newId[o];
   double cv[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
-    cv[k] = ref[5 * o + k];
+    cv[k] = ref[5 * (size_t)o + k];
     V.cv[(size_t)k * V.nc + i] = cv[k];
   }
   initCell(V, i, cv);

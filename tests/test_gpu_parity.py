@@ -295,3 +295,25 @@ def test_nan_cells_reported_as_event(gpu_lib):
     assert rc == gpu.EVENT_NAN
     st = r.status()
     assert st["nanCells"] > 0 and st["firstBadCell"] >= 1
+
+
+@pytest.mark.parametrize("prec", ["fp64_exact", "mixed"])
+def test_pinned_host_buffers_match_pageable(gpu_lib, prec):
+    """Upload and download through pinned host buffers (read and written by
+    the kernels over the host link) give the same bits as pageable buffers
+    (staged copies)."""
+    torch = pytest.importorskip("torch")
+    c = cases.shock_sphere(8)
+    cv0 = _perturbed(c)
+    a = gpu.Region(c, prec)
+    a.upload(cv0)
+    a.step(2, 0.0)
+    cv_a, dv_a = a.download()
+    pin_cv = torch.from_numpy(cv0.copy()).pin_memory()
+    pin_dv = torch.empty((cv0.shape[0], 3), dtype=torch.float64).pin_memory()
+    b = gpu.Region(c, prec)
+    b.upload(pin_cv.numpy())
+    b.step(2, 0.0)
+    b.download(pin_cv.numpy(), pin_dv.numpy())
+    np.testing.assert_array_equal(pin_cv.numpy(), cv_a)
+    np.testing.assert_array_equal(pin_dv.numpy(), dv_a)
