@@ -102,25 +102,13 @@ __global__ void kAxpyInPlace(double *y, double a, const double *x, size_t n) {
 }
 __global__ void kAccumJ(double *acc, const double *j, double dt) { *acc += dt * *j; }
 
-// Download in one pass: renumbered SoA (ncomp rows) -> reference order and
-// layout, one thread per reference cell so that the writes to `dst` are
-// contiguous (dst may be the caller's pinned host buffer).
+// Download: renumbered SoA (ncomp rows) -> reference order and layout, one
+// thread per reference cell so that the writes to `dst` are contiguous.
 __global__ void kGatherOut(const double *src, double *dst, const int *newId, int nc, int ncomp) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= nc) return;
   const int i = newId[o];
   for (int k = 0; k < ncomp; ++k) dst[(size_t)ncomp * o + k] = src[(size_t)k * nc + i];
-}
-
-// The device address of a host buffer the kernels can access directly
-// (pinned, mapped memory), or null for pageable memory.
-inline const void *mappedHostPtr(const void *p) {
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
 }
 
 // T and c of RFLU_SetDependentVars (TCPERF) from cv and p, for a mixed-mode
@@ -290,15 +278,12 @@ struct Ctx : CtxBase {
     ops->faceFlux(V, stream);
     ops->gatherUpdate(V, iStage, &V.sc->dtMin, stream);
   }
-  // cv(5,nCells) of the host: read by the upload kernel straight from a
-  // pinned buffer, else staged with one copy
+  // cv(5,nCells) of the host: one copy into the staging buffer (the copy
+  // engines move pinned buffers at ~200 GB/s; kernels reading the host
+  // buffer directly measured 2x slower), then one upload kernel
   int setState(const double *cv) {
-    const double *src = static_cast<const double *>(mappedHostPtr(cv));
-    if (!src) {
-      RFLU_CUDA(cudaMemcpyAsync(staging, cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
-      src = staging;
-    }
-    ops->initFromRef(V, src, stream);
+    RFLU_CUDA(cudaMemcpyAsync(staging, cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
+    ops->initFromRef(V, staging, stream);
     return checkLaunch("upload");
   }
 
@@ -310,23 +295,14 @@ struct Ctx : CtxBase {
   }
   int download(double *cv, double *dv) override {
     if (dv && V.p.dvPOnly) kDvFill<<<nblk(V.nc), 256, 0, stream>>>(V.cv, V.dv, V.nc, V.p.gcR, V.p.gRT);
-    // pinned host buffers are written by the gather kernel directly
     if (cv) {
-      if (double *dst = static_cast<double *>(const_cast<void *>(mappedHostPtr(cv)))) {
-        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.cv, dst, V.newId, V.nc, 5);
-      } else {
-        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.newId, V.nc, 5);
-        RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
-      }
+      kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.newId, V.nc, 5);
+      RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
     }
     if (dv) {
-      if (double *dst = static_cast<double *>(const_cast<void *>(mappedHostPtr(dv)))) {
-        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.dv, dst, V.newId, V.nc, 3);
-      } else {
-        kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.newId, V.nc, 3);
-        RFLU_CUDA(cudaMemcpyAsync(dv, staging + 5 * (size_t)V.nc, sizeof(double) * 3 * (size_t)V.nc,
-                                  cudaMemcpyDeviceToHost, stream));
-      }
+      kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.newId, V.nc, 3);
+      RFLU_CUDA(cudaMemcpyAsync(dv, staging + 5 * (size_t)V.nc, sizeof(double) * 3 * (size_t)V.nc,
+                                cudaMemcpyDeviceToHost, stream));
     }
     int rc = checkLaunch("download");
     if (rc) return rc;

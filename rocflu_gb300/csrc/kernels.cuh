@@ -330,10 +330,9 @@ __global__ void kInitState(View<R> V) {
   initCell(V, i, cv);
 }
 
-// Upload in one pass: cv(5,nCells) in the reference's order and layout ->
-// the renumbered master cv, primitive state and dependent variables.  One
-// thread per reference cell, so that the reads of `ref` are contiguous: it
-// may be the caller's pinned host buffer, read over the host link.
+// Upload in one pass: cv(5,nCells) in the reference's order and layout
+// (staged on the device) -> the renumbered master cv, primitive state and
+// dependent variables; one thread per reference cell (contiguous reads).
 template <typename R>
 __global__ void kInitFromRef(View<R> V, const double *ref) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;

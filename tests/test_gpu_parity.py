@@ -299,9 +299,8 @@ def test_nan_cells_reported_as_event(gpu_lib):
 
 @pytest.mark.parametrize("prec", ["fp64_exact", "mixed"])
 def test_pinned_host_buffers_match_pageable(gpu_lib, prec):
-    """Upload and download through pinned host buffers (read and written by
-    the kernels over the host link) give the same bits as pageable buffers
-    (staged copies)."""
+    """Upload and download through pinned host buffers give the same bits
+    as through pageable buffers."""
     torch = pytest.importorskip("torch")
     c = cases.shock_sphere(8)
     cv0 = _perturbed(c)
