@@ -782,8 +782,8 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
     maxTileSt = std::max(maxTileSt, stOff[b1] - stOff[b0]);
   }
   stLoc.resize(stLoc.size() + 16, 0);  // whole 16-byte words past the last tile
-  // shared memory: 8 floats per record, the face-offset cache and the ids
-  const size_t smem = sizeof(float) * (2 * (8 * (size_t)maxRecs + 4 * (((size_t)maxTileSt + 7) / 8 + 1)) + 3 * 6 * kTile);
+  // shared memory: two tile buffers and the face-offset cache
+  const size_t smem = sizeof(float) * (2 * tileBufFloatsFor(maxRecs, maxTileSt) + 3 * 6 * kTile);
   int dev = 0, optin = 0;
   RFLU_CUDA(cudaGetDevice(&dev));
   RFLU_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));

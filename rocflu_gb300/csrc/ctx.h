@@ -48,6 +48,14 @@ struct Params {
 // flux = one float4 (mass and momentum) per face followed by the nT energy
 // fluxes.
 constexpr int kTile = 256;
+// Shared-memory footprint of one staged tile of the mixed-mode gradient
+// kernel: 8 floats per record, the stencil ids as whole 16-byte words (plus
+// one for the misalignment of the first), kTileOffInts stencil offsets.
+constexpr int kTileOffInts = kTile + 4;
+__host__ __device__ inline size_t tileIdWordsFor(int maxTileSt) { return ((size_t)maxTileSt + 7) / 8 + 1; }
+__host__ __device__ inline size_t tileBufFloatsFor(int maxRecs, int maxTileSt) {
+  return 8 * (size_t)maxRecs + 4 * tileIdWordsFor(maxTileSt) + kTileOffInts;
+}
 
 template <typename R> struct Layout {
   static constexpr bool packed = false;

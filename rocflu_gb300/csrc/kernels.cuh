@@ -265,6 +265,34 @@ __device__ inline void loadFlux(const T *flux, size_t nT, int t, T *f) {
   }
 }
 
+// Conversions between float and double with integer and FP32 instructions,
+// bit-identical to the hardware conversions (round to nearest even): in the
+// mixed update they would otherwise occupy half of the FP64 pipe, the
+// kernel's bound on this part.
+__device__ inline double f2d(float f) {
+  // denormals are scaled into the normal range first (exact: a power of 2)
+  const bool den = (__float_as_uint(f) & 0x7F800000u) == 0u && f != 0.f;
+  const unsigned u = __float_as_uint(den ? f * 18446744073709551616.f : f);
+  const unsigned ex = (u >> 23) & 0xFFu;
+  unsigned long long dex = ex == 0u ? 0ull : (ex == 255u ? 2047ull : (unsigned long long)(ex + 896u));
+  if (den) dex -= 64ull;
+  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) | (dex << 52) |
+                                  ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+__device__ inline float d2f(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int fex = (int)((b >> 52) & 0x7FFull) - 896;
+  if (fex <= 0 || fex >= 255) return (float)d;  // zero, float denormals, overflow, inf, nan
+  const unsigned long long man = b & 0xFFFFFFFFFFFFFull;
+  const unsigned m = (unsigned)(man >> 29);
+  const unsigned rem = (unsigned)(man & 0x1FFFFFFFull);
+  // the mantissa carry of the rounding increments the exponent, as it must
+  const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  const unsigned bits = ((unsigned)(b >> 32) & 0x80000000u) | (((unsigned)fex << 23) | m) + up;
+  return __uint_as_float(bits);
+}
+
 // Mixed mode: primitive state from the FP64 master cv.  1/rho from an FP32
 // seed y (also the FP32 velocities' reciprocal) refined once in FP64,
 // y + y*(1 - rho*y) (quadratic convergence: ~2^-44), and the pressure in FP64
@@ -273,16 +301,16 @@ struct MixedPrim {
   float rf, irf, uf, vf, wf;
   double ir, ke, pr;
   __device__ MixedPrim(const Params &P, const double *cv) {
-    rf = (float)cv[0];
+    rf = d2f(cv[0]);
     irf = 1.0f / rf;
-    ir = (double)irf;
+    ir = f2d(irf);
     ir = fma(ir, fma(-cv[0], ir, 1.0), ir);
     const double msq = cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3];
     ke = 0.5 * msq * ir;
     pr = (P.gRT - 1.0) * (cv[4] - ke);
-    uf = (float)cv[1] * irf;
-    vf = (float)cv[2] * irf;
-    wf = (float)cv[3] * irf;
+    uf = d2f(cv[1]) * irf;
+    vf = d2f(cv[2]) * irf;
+    wf = d2f(cv[3]) * irf;
   }
 };
 
@@ -591,30 +619,58 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
 // R-factor products, so G = L * sum_j (q_j - q_i) d_j / |d_j|^2.
 constexpr int kMaxCellFaces = 6;
 
+// A staged record's two 16-byte halves are swapped when bit 2 of its local id
+// is set: the first halves of 8 consecutive records then cover all eight
+// 16-byte bank groups of a 128-byte row instead of four, and a quarter-warp's
+// 16-byte loads of neighbouring records do not conflict.
+__device__ inline int recHalf0(int l) { return 8 * l + (l & 4); }
+
 __device__ inline void ldRec(const float *recs, int l, float *v) {
-  const float4 a = *reinterpret_cast<const float4 *>(recs + 8 * l);
-  const float4 b = *reinterpret_cast<const float4 *>(recs + 8 * l + 4);
+  const int o = recHalf0(l);
+  const float4 a = *reinterpret_cast<const float4 *>(recs + o);
+  const float4 b = *reinterpret_cast<const float4 *>(recs + (o ^ 4));
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
   v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
 
 template <bool kDt, bool kTiled, int kRc>
 __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, float *dc, const float *recs,
-                                        int li, const unsigned short *stSm = nullptr, int stBase = 0) {
+                                        int li, const unsigned short *stSm = nullptr,
+                                        const int *stOffSm = nullptr) {
   const Params &P = V.p;
+  const size_t n = V.nc;
+  const int rc = kRc >= 0 ? kRc : P.reconst;
+  const bool second = P.spaceOrder > 1;
+  const bool lim = second && (rc == 10 || rc == 100 || rc == 11);
+  // The tiled path issues its per-cell global loads (LSQ matrix,
+  // Venkatakrishnan epsilon) before the stencil loop, which runs from shared
+  // memory and hides their latency, and all of its face entries at once after
+  // it.  Every cell has V.cfW entries in feD/feN; the unused ones carry the
+  // tag INT_MIN.
+  float4 De[kMaxCellFaces];
+  float lq[6];
+  float epsq = 0.f;
+  if (kTiled) {
+    if (second) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) lq[c] = V.lsq[c * n + i];
+    }
+    if (lim && rc == 11) epsq = V.epsq[i];
+  }
   float rec[8];
   if (kTiled) ldRec(recs, li, rec);
   else ld8(V.prim + 8 * (size_t)i, rec);
   const float q[5] = {rec[0], rec[1], rec[2], rec[3], rec[4]};
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = 0.f;
-  const bool second = P.spaceOrder > 1;
   if (second) {
-    const int sb = V.stOff[i], se = V.stOff[i + 1];
+    // tiled: s counts from the first staged 16-byte word of stencil ids
+    const int s0 = kTiled ? 8 * (stOffSm[0] >> 3) : 0;
+    const int sb = (kTiled ? stOffSm[li] : V.stOff[i]) - s0, se = (kTiled ? stOffSm[li + 1] : V.stOff[i + 1]) - s0;
 #pragma unroll 2
     for (int s = sb; s < se; ++s) {
       float r[8];
-      if (kTiled) ldRec(recs, stSm[s - stBase], r);
+      if (kTiled) ldRec(recs, stSm[s], r);
       else ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
       const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
       const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
@@ -627,9 +683,13 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
         g[3 * k + 2] = g[3 * k + 2] + sz * d;
       }
     }
-    const size_t n = V.nc;
-    const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
-    const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
+  }
+  if (second) {
+    if (!kTiled) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) lq[c] = V.lsq[c * n + i];
+    }
+    const float lxx = lq[0], lxy = lq[1], lxz = lq[2], lyy = lq[3], lyz = lq[4], lzz = lq[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const float x = g[3 * k], y = g[3 * k + 1], z = g[3 * k + 2];
@@ -638,8 +698,6 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
       g[3 * k + 2] = lxz * x + lyz * y + lzz * z;
     }
   }
-  const int rc = kRc >= 0 ? kRc : P.reconst;
-  const bool lim = second && (rc == 10 || rc == 100 || rc == 11);
   const bool velo = lim && rc == 10;
   const bool venkat = lim && rc == 11;
   // velocity limiter frame: eigenvectors A(:, j) = A[3j..3j+2] of the
@@ -668,6 +726,13 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
 #pragma unroll
       for (int c = 0; c < 3; ++c) B[3 * j + c] = A[3 * j] * G[3 * c] + A[3 * j + 1] * G[1 + 3 * c] + A[3 * j + 2] * G[2 + 3 * c];
   }
+  if (kTiled) {
+#pragma unroll
+    for (int k = 0; k < kMaxCellFaces; ++k) {
+      if ((lim || kDt) && k < V.cfW) De[k] = ld4(V.feD + 4 * (k * n + i));
+      else De[k] = make_float4(0.f, 0.f, 0.f, __int_as_float(INT_MIN));
+    }
+  }
   // Barth-Jespersen in one pass: min over faces of dmax/d2 (d2 > 0) is
   // dmax / (largest positive d2), and likewise dmin / (most negative d2), so
   // the pass keeps the extreme d2 per component (pmx, nmn) next to the
@@ -683,7 +748,6 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
   const float ai = kDt ? sqrtf(gam * q[4] / q[0]) : 0.f;
   float sum = 0.f;
   int nfc = 0;
-  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
   // one face of the pass: neighbour record x, offset d = fc - cofg of this side
   auto face = [&](const float *x, float d0, float d1, float d2) {
 #pragma unroll
@@ -724,28 +788,37 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
     }
   };
   if (kTiled) {
-    const size_t n = V.nc;
-    for (int k = 0; k < ce - cb; ++k) {
-      const float4 D = ld4(V.feD + 4 * (k * n + i));
-      const int tag = __float_as_int(D.w);
-      if (tag >= 0) {
-        if (!lim && !kDt) continue;
-        float x[8];
-        ldRec(recs, tag, x);
-        if (lim) face(x, D.x, D.y, D.z);
-        if (kDt) {
-          const float4 N = ld4(V.feN + 4 * (k * n + i));
-          const float aj = sqrtf(gam * x[4] / x[0]);
-          const float vc = 0.5f * ((q[1] + x[1]) * N.x + (q[2] + x[2]) * N.y + (q[3] + x[3]) * N.z);
-          sum += (fabsf(vc) + 0.5f * (ai + aj)) * N.w;
+    if (lim) {
+#pragma unroll
+      for (int k = 0; k < kMaxCellFaces; ++k) {
+        const int tag = __float_as_int(De[k].w);
+        if (tag >= 0) {
+          float x[8];
+          ldRec(recs, tag, x);
+          face(x, De[k].x, De[k].y, De[k].z);
         }
-      } else if (kDt) {
-        const float4 N = ld4(V.feN + 4 * (k * n + i));
-        const float vc = q[1] * N.x + q[2] * N.y + q[3] * N.z;
-        sum += (fabsf(vc) + ai) * N.w;
+      }
+    }
+    if (kDt) {
+#pragma unroll
+      for (int k = 0; k < kMaxCellFaces; ++k) {
+        const int tag = __float_as_int(De[k].w);
+        if (tag == INT_MIN) continue;
+        const float4 Nk = ld4(V.feN + 4 * (k * n + i));
+        if (tag >= 0) {
+          float x[8];
+          ldRec(recs, tag, x);
+          const float aj = sqrtf(gam * x[4] / x[0]);
+          const float vc = 0.5f * ((q[1] + x[1]) * Nk.x + (q[2] + x[2]) * Nk.y + (q[3] + x[3]) * Nk.z);
+          sum += (fabsf(vc) + 0.5f * (ai + aj)) * Nk.w;
+        } else {
+          const float vc = q[1] * Nk.x + q[2] * Nk.y + q[3] * Nk.z;
+          sum += (fabsf(vc) + ai) * Nk.w;
+        }
       }
     }
   } else {
+    const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
       if (code >= 0) {
@@ -773,7 +846,7 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
   if (!lim) return sum;
   float lm[5] = {1.f, 1.f, 1.f, 1.f, 1.f};
   if (venkat) {
-    const float epsq = V.epsq[i];
+    if (!kTiled) epsq = V.epsq[i];
     const float tiny = 1.0e-12f;
     for (int c = 0; c < nfc; ++c) {
       const float *slot = dc + 3 * c * kBlock;
@@ -880,6 +953,10 @@ __device__ inline void cpAsync16(void *smemDst, const void *gSrc) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smemDst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gSrc) : "memory");
 }
+__device__ inline void cpAsync4(void *smemDst, const void *gSrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smemDst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gSrc) : "memory");
+}
 __device__ inline void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ inline void cpAsyncWait() {
@@ -888,15 +965,16 @@ __device__ inline void cpAsyncWait() {
 
 // One tile buffer: 8 floats per staged record, then the tile's stencil ids
 // as whole 16-byte words of stLoc (maxTileSt ids plus the misalignment of
-// the first word).  Two buffers per CTA, then the Venkatakrishnan face-offset
+// the first word), then the tile's kTile + 1 stencil offsets stOff (padded to
+// kTileOffInts).  Two buffers per CTA, then the Venkatakrishnan face-offset
 // cache.
 template <typename R>
 __host__ __device__ inline size_t tileIdWords(const View<R> &V) {
-  return ((size_t)V.maxTileSt + 7) / 8 + 1;
+  return tileIdWordsFor(V.maxTileSt);
 }
 template <typename R>
 __host__ __device__ inline size_t tileBufFloats(const View<R> &V) {
-  return 8 * (size_t)V.maxRecs + 4 * tileIdWords(V);
+  return tileBufFloatsFor(V.maxRecs, V.maxTileSt);
 }
 template <typename R>
 inline size_t tileSmemBytes(const View<R> &V, bool venkat) {
@@ -945,13 +1023,15 @@ __device__ inline void stageTile(const View<R> &V, int t, float *buf) {
   const int w0 = V.stOff[base] >> 3, w1 = (V.stOff[base + nIn] + 7) >> 3;
   const uint4 *src4 = reinterpret_cast<const uint4 *>(V.stLoc);
   for (int w = w0 + (int)threadIdx.x; w < w1; w += kBlock) cpAsync16(ids + (w - w0), src4 + w);
+  int *offs = reinterpret_cast<int *>(ids + tileIdWords(V));
+  for (int r = threadIdx.x; r <= nIn; r += kBlock) cpAsync4(offs + r, V.stOff + base + r);
   for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
     const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
     const int dst = r < nIn ? r : kTile + (r - nIn);
     const float *g = V.prim + 8 * (size_t)src;
-    float *d = buf + 8 * (size_t)dst;
-    cpAsync16(d, g);
-    cpAsync16(d + 4, g + 4);
+    const int o = recHalf0(dst);
+    cpAsync16(buf + o, g);
+    cpAsync16(buf + (o ^ 4), g + 4);
   }
 }
 
@@ -983,10 +1063,11 @@ __global__ void __launch_bounds__(kBlock, 3) kGradTile(View<R> V) {
       const int base = t * kTile;
       const int i = base + threadIdx.x;
       if (i < V.nc) {
+        const float *ids = buf + 8 * (size_t)V.maxRecs;
         float g[15];
         const float sum = gradLimitPacked<kDt, true, kRc>(
-            V, i, g, dc + threadIdx.x, buf, threadIdx.x,
-            reinterpret_cast<const unsigned short *>(buf + 8 * (size_t)V.maxRecs), 8 * (V.stOff[base] >> 3));
+            V, i, g, dc + threadIdx.x, buf, threadIdx.x, reinterpret_cast<const unsigned short *>(ids),
+            reinterpret_cast<const int *>(ids + 4 * tileIdWords(V)));
         storeGrad(V, i, g);
         if (kDt) dt = fmin(dt, V.vol[i] / (double)sum);
       }
@@ -1421,7 +1502,7 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
       default:
         inc = adtv * r;
     }
-    cv[k] = cv[k] - (double)inc;
+    cv[k] = cv[k] - f2d(inc);
   }
   if (ra.wr) {
 #pragma unroll
@@ -1431,7 +1512,8 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
   const float rf = m.rf, uf = m.uf, vf = m.vf, wf = m.wf;
   const double ir = m.ir, ke = m.ke;
   double pr = m.pr;
-  if (isnan(rf) || isnan(uf) || isnan(vf) || isnan(wf) || isnan((float)pr)) {
+  const float prf = d2f(pr);
+  if (isnan(rf) || isnan(uf) || isnan(vf) || isnan(wf) || isnan(prf)) {
     atomicAdd(&V.sc->nanCells, 1ull);
     atomicMin(&V.sc->firstBadCell, V.refId[i] + 1);
   }
@@ -1447,12 +1529,12 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
   if (!P.dvPOnly) {
     const double c2 = P.gRT * pr * ir;
     // sqrt(c2): FP32 seed y ~ 1/sqrt(c2), h = c2*y, then h + h*(1 - h*y)/2
-    const double y = (double)rsqrtf((float)c2);
+    const double y = f2d(rsqrtf(d2f(c2)));
     const double h = c2 * y;
     V.dv[n + i] = pr * ir * P.igcR;
     V.dv[2 * n + i] = fma(0.5 * h, fma(-h, y, 1.0), h);
   }
-  storePrimRec(V, i, (R)rf, (R)uf, (R)vf, (R)wf, (R)pr);
+  storePrimRec(V, i, (R)rf, (R)uf, (R)vf, (R)wf, (R)d2f(pr));
 }
 
 // Gather + RKUpdateMP (RkUpdateGeneric, static grid, libfloflu/
@@ -1469,7 +1551,7 @@ __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, c
   double cv[5];
   loadCv(V, i, cv);
   if constexpr (!Ref<R>::on) {
-    mixedUpdate(V, i, iStage, P.arkF[iStage - 1] * (float)(*dtp), P.grkF[iStage - 1], rhs, cv);
+    mixedUpdate(V, i, iStage, P.arkF[iStage - 1] * d2f(*dtp), P.grkF[iStage - 1], rhs, cv);
     return;
   }
   const double fac = P.ark[iStage - 1] * (*dtp);

@@ -269,17 +269,18 @@ __host__ __device__ inline void symmetricEigen3(const S m[9], S vec[9], S val[3]
       }
   }
   val[0] = r[0]; val[1] = r[4]; val[2] = r[8];
+  // selection sort (first strict minimum, swapped into place), written with
+  // fixed indices so that val and vec stay in registers
+  auto swapCols = [&](int a, int b) {
+    S t = val[a]; val[a] = val[b]; val[b] = t;
 #pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    int iMin = i;
-    for (int k = i + 1; k < 3; ++k)
-      if (val[k] < val[iMin]) iMin = k;
-    if (iMin != i) {
-      S t = val[i]; val[i] = val[iMin]; val[iMin] = t;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) { S x = vec[k + 3 * i]; vec[k + 3 * i] = vec[k + 3 * iMin]; vec[k + 3 * iMin] = x; }
-    }
-  }
+    for (int k = 0; k < 3; ++k) { S x = vec[k + 3 * a]; vec[k + 3 * a] = vec[k + 3 * b]; vec[k + 3 * b] = x; }
+  };
+  const bool m1 = val[1] < val[0];
+  const bool m2 = val[2] < (m1 ? val[1] : val[0]);
+  if (m2) swapCols(0, 2);
+  else if (m1) swapCols(0, 1);
+  if (val[2] < val[1]) swapCols(1, 2);
 }
 
 }  // namespace rflu
