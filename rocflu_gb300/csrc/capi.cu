@@ -1096,7 +1096,8 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   workBytes = sizeof(R) * (size_t)(120 * (size_t)nc + 24 * ((size_t)nf + nb) + 64) + sizeof(int) * 10 * (size_t)nc + 256;
   if ((rc = alloc((char **)&work, workBytes))) return rc;
   ops->configure(V);
-  V.tileGrid = ops->tileGrid(V);
+  V.tileGrid = ops->tileGrid(V, 0);
+  V.tileGridDt = ops->tileGrid(V, 1);
   return checkLaunch("rflu_gpu_create");
 }
 

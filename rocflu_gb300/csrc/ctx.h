@@ -107,6 +107,7 @@ struct View {
   int maxRecs;                      // max staged records over the tiles
   int maxTileSt;                    // max stencil entries of a tile's cells
   int tileGrid;                     // CTAs of the persistent tiled kernels
+  int tileGridDt;                   // ... of the variant with the time-step sum
   int cfW;                          // max faces per cell (entries of feD/feN)
   const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids
   const unsigned short *stLoc;      // local id of each stencil member (stIdx order),

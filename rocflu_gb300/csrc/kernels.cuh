@@ -661,6 +661,37 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
   if (kTiled) ldRec(recs, li, rec);
   else ld8(V.prim + 8 * (size_t)i, rec);
   const float q[5] = {rec[0], rec[1], rec[2], rec[3], rec[4]};
+  const float gam = P.refGammaF;
+  const float ai = kDt ? sqrtf(gam * q[4] / q[0]) : 0.f;
+  float sum = 0.f;
+  if (kTiled && kDt) {
+    // the spectral-radius sum of the time step first, while no gradient
+    // state is live: its face entries and normals are all in flight at once
+    float4 Dt[kMaxCellFaces], Nt[kMaxCellFaces];
+#pragma unroll
+    for (int k = 0; k < kMaxCellFaces; ++k) {
+      if (k < V.cfW) {
+        Dt[k] = ld4(V.feD + 4 * (k * n + i));
+        Nt[k] = ld4(V.feN + 4 * (k * n + i));
+      } else {
+        Dt[k].w = __int_as_float(INT_MIN);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxCellFaces; ++k) {
+      const int tag = __float_as_int(Dt[k].w);
+      if (tag >= 0) {
+        float x[8];
+        ldRec(recs, tag, x);
+        const float aj = sqrtf(gam * x[4] / x[0]);
+        const float vc = 0.5f * ((q[1] + x[1]) * Nt[k].x + (q[2] + x[2]) * Nt[k].y + (q[3] + x[3]) * Nt[k].z);
+        sum += (fabsf(vc) + 0.5f * (ai + aj)) * Nt[k].w;
+      } else if (tag != INT_MIN) {
+        const float vc = q[1] * Nt[k].x + q[2] * Nt[k].y + q[3] * Nt[k].z;
+        sum += (fabsf(vc) + ai) * Nt[k].w;
+      }
+    }
+  }
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = 0.f;
   if (second) {
@@ -729,7 +760,7 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
   if (kTiled) {
 #pragma unroll
     for (int k = 0; k < kMaxCellFaces; ++k) {
-      if ((lim || kDt) && k < V.cfW) De[k] = ld4(V.feD + 4 * (k * n + i));
+      if (lim && k < V.cfW) De[k] = ld4(V.feD + 4 * (k * n + i));
       else De[k] = make_float4(0.f, 0.f, 0.f, __int_as_float(INT_MIN));
     }
   }
@@ -744,9 +775,6 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
   float dmn[3] = {0.f, 0.f, 0.f}, dmx[3] = {0.f, 0.f, 0.f}, smn[3] = {0.f, 0.f, 0.f}, smx[3] = {0.f, 0.f, 0.f};
 #pragma unroll
   for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; pmx[k] = 0.f; nmn[k] = 0.f; }
-  const float gam = P.refGammaF;
-  const float ai = kDt ? sqrtf(gam * q[4] / q[0]) : 0.f;
-  float sum = 0.f;
   int nfc = 0;
   // one face of the pass: neighbour record x, offset d = fc - cofg of this side
   auto face = [&](const float *x, float d0, float d1, float d2) {
@@ -796,24 +824,6 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
           float x[8];
           ldRec(recs, tag, x);
           face(x, De[k].x, De[k].y, De[k].z);
-        }
-      }
-    }
-    if (kDt) {
-#pragma unroll
-      for (int k = 0; k < kMaxCellFaces; ++k) {
-        const int tag = __float_as_int(De[k].w);
-        if (tag == INT_MIN) continue;
-        const float4 Nk = ld4(V.feN + 4 * (k * n + i));
-        if (tag >= 0) {
-          float x[8];
-          ldRec(recs, tag, x);
-          const float aj = sqrtf(gam * x[4] / x[0]);
-          const float vc = 0.5f * ((q[1] + x[1]) * Nk.x + (q[2] + x[2]) * Nk.y + (q[3] + x[3]) * Nk.z);
-          sum += (fabsf(vc) + 0.5f * (ai + aj)) * Nk.w;
-        } else {
-          const float vc = q[1] * Nk.x + q[2] * Nk.y + q[3] * Nk.z;
-          sum += (fabsf(vc) + ai) * Nk.w;
         }
       }
     }
@@ -946,7 +956,9 @@ __device__ inline void blockMinDt(Scalars *sc, double dt) {
 // its halo) and its stencil ids are copied into shared memory with cp.async,
 // double-buffered: the copies of the next tile are in flight while the CTA
 // computes the current one.  Each record leaves L2 once per tile instead of
-// once per stencil reference.
+// once per stencil reference.  Three CTAs fit per SM by shared memory; the
+// variant with the time-step sum holds more per-cell state and runs at two
+// (up to 128 registers) instead of spilling at three.
 static_assert(kTile == kBlock, "one thread per cell of a tile");
 
 __device__ inline void cpAsync16(void *smemDst, const void *gSrc) {
@@ -981,37 +993,37 @@ inline size_t tileSmemBytes(const View<R> &V, bool venkat) {
   return sizeof(float) * (2 * tileBufFloats(V) + (venkat ? 3 * kMaxCellFaces * kBlock : 0));
 }
 
-// L2 prefetch of the 128-byte lines of [p, p + bytes), spread over the CTA;
-// every prefetched address lies inside the range (the first is p itself).
-__device__ inline void prefetchL2(const void *p, size_t bytes, int &lane) {
-  if (bytes == 0) return;
-  const size_t b = reinterpret_cast<size_t>(p), line0 = b >> 7;
-  const int lines = (int)(((b + bytes - 1) >> 7) - line0 + 1);
-  // line j of the range goes to thread (lane + j) mod kBlock
-  for (int j = ((int)threadIdx.x - lane) & (kBlock - 1); j < lines; j += kBlock) {
-    const size_t a = j == 0 ? b : (line0 + j) << 7;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
-  }
-  lane = (lane + lines) & (kBlock - 1);
-}
-
-// The per-cell arrays the compute phase of tile t reads from global memory
-// (face entries, LSQ matrix, CSR offsets, volumes): pulled into L2 while the
-// CTA computes the tile before it.
+// L2 prefetch of the per-cell arrays the compute phase of tile t reads from
+// global memory (face entries, LSQ matrix, volumes, Venkatakrishnan epsilon),
+// issued for the next tile while the CTA computes the current one.  Each
+// array is read per tile as chunks of kTile consecutive elements (feD/feN: one
+// chunk per face slot, lsq: one per matrix entry) of at most 4 KB: warp w
+// takes chunks w, w + 8, ... and its lanes one 128-byte line each.
 template <typename R, bool kDt, int kRc>
 __device__ inline void prefetchTile(const View<R> &V, int t) {
   const size_t n = V.nc;
-  const int base = t * kTile, nIn = min(kTile, V.nc - base);
-  int lane = 0;
-  for (int k = 0; k < V.cfW; ++k) {
-    prefetchL2(V.feD + 4 * (k * n + base), 16 * (size_t)nIn, lane);
-    if (kDt) prefetchL2(V.feN + 4 * (k * n + base), 16 * (size_t)nIn, lane);
+  const int lane = threadIdx.x & 31;
+  const int nFe = V.cfW, nN = kDt ? V.cfW : 0;
+  const int nChunks = nFe + nN + 6 + (kDt ? 1 : 0) + (kRc == 11 ? 1 : 0);
+  for (int c = threadIdx.x >> 5; c < nChunks; c += kBlock / 32) {
+    const char *arr;
+    unsigned esz;
+    size_t off = 0;
+    if (c < nFe) { arr = reinterpret_cast<const char *>(V.feD); esz = 16; off = (size_t)c * n; }
+    else if (c < nFe + nN) { arr = reinterpret_cast<const char *>(V.feN); esz = 16; off = (size_t)(c - nFe) * n; }
+    else if (c < nFe + nN + 6) { arr = reinterpret_cast<const char *>(V.lsq); esz = 4; off = (size_t)(c - nFe - nN) * n; }
+    else if (kDt && c == nFe + nN + 6) { arr = reinterpret_cast<const char *>(V.vol); esz = 8; }
+    else { arr = reinterpret_cast<const char *>(V.epsq); esz = 4; }
+    // bytes of this chunk's part of the array from the tile's first element
+    const size_t first = (size_t)t * kTile;
+    const size_t avail = esz * (n - first);
+    const unsigned bytes = esz * kTile;
+    const unsigned at = 128u * lane;
+    if (at < bytes && at < avail) {
+      const char *a = arr + esz * (off + first) + at;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+    }
   }
-  for (int c = 0; c < 6; ++c) prefetchL2(V.lsq + c * n + base, 4 * (size_t)nIn, lane);
-  prefetchL2(V.stOff + base, 4 * (size_t)(nIn + 1), lane);
-  prefetchL2(V.cfOff + base, 4 * (size_t)(nIn + 1), lane);
-  if (kDt) prefetchL2(V.vol + base, 8 * (size_t)nIn, lane);
-  if (kRc == 11) prefetchL2(V.epsq + base, 4 * (size_t)nIn, lane);
 }
 
 // Issue the copies of tile t into buf (this thread's share).
@@ -1036,7 +1048,7 @@ __device__ inline void stageTile(const View<R> &V, int t, float *buf) {
 }
 
 template <typename R, bool kDt, int kRc>
-__global__ void __launch_bounds__(kBlock, 3) kGradTile(View<R> V) {
+__global__ void __launch_bounds__(kBlock, kDt ? 2 : 3) kGradTile(View<R> V) {
   if constexpr (Layout<R>::packed) {
     extern __shared__ float4 tileSmem[];
     const size_t bufFloats = tileBufFloats(V);
@@ -1698,14 +1710,16 @@ struct Launch {
     const int rc = V.p.reconst;
     const size_t b = tileSmemBytes(V, rc == 11);
     const int nTiles = (V.nc + kTile - 1) / kTile;
-    const int grid = V.tileGrid > 0 ? std::min(nTiles, V.tileGrid) : nTiles;
+    const int g = kDt ? V.tileGridDt : V.tileGrid;
+    const int grid = g > 0 ? std::min(nTiles, g) : nTiles;
     if (rc == 10) kGradTile<R, kDt, 10><<<grid, kBlock, b, s>>>(V);
     else if (rc == 100) kGradTile<R, kDt, 100><<<grid, kBlock, b, s>>>(V);
     else if (rc == 11) kGradTile<R, kDt, 11><<<grid, kBlock, b, s>>>(V);
     else kGradTile<R, kDt, 0><<<grid, kBlock, b, s>>>(V);
   }
   // CTAs of the persistent tiled kernels: the resident CTAs per SM of the
-  // variant the mesh's limiter selects, times the SMs (0 when untiled)
+  // variant the mesh's limiter selects (with the time-step sum when withDt),
+  // times the SMs (0 when untiled)
   template <bool kDt, int kRc>
   static int residentTiles(const View<R> &V) {
     int per = 0, dev = 0, sms = 0;
@@ -1714,13 +1728,13 @@ struct Launch {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return std::max(per, 1) * sms;
   }
-  static int tileGrid(const View<R> &V) {
+  static int tileGrid(const View<R> &V, int withDt) {
     if (!V.tiled) return 0;
     const int rc = V.p.reconst;
-    if (rc == 10) return std::min(residentTiles<false, 10>(V), residentTiles<true, 10>(V));
-    if (rc == 100) return std::min(residentTiles<false, 100>(V), residentTiles<true, 100>(V));
-    if (rc == 11) return std::min(residentTiles<false, 11>(V), residentTiles<true, 11>(V));
-    return std::min(residentTiles<false, 0>(V), residentTiles<true, 0>(V));
+    if (rc == 10) return withDt ? residentTiles<true, 10>(V) : residentTiles<false, 10>(V);
+    if (rc == 100) return withDt ? residentTiles<true, 100>(V) : residentTiles<false, 100>(V);
+    if (rc == 11) return withDt ? residentTiles<true, 11>(V) : residentTiles<false, 11>(V);
+    return withDt ? residentTiles<true, 0>(V) : residentTiles<false, 0>(V);
   }
   template <bool kDt, int kRc>
   static void setTileSmem(const View<R> &V) {

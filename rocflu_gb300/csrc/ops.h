@@ -20,7 +20,7 @@ struct Ops {
   void (*stepEnd)(const View<R> &, cudaStream_t);
   void (*stepStart)(const View<R> &, cudaStream_t);  // dt reduction + first-stage gradients
   void (*configure)(const View<R> &);                  // mesh-dependent kernel attributes
-  int (*tileGrid)(const View<R> &);                    // CTAs of the persistent tiled kernels
+  int (*tileGrid)(const View<R> &, int withDt);        // CTAs of the persistent tiled kernels
   // tangent / adjoint of the residual (FP64 modes only; null elsewhere)
   void (*jvp)(const View<R> &, const double *cvDot, double *rhsDot, double *work, cudaStream_t);
   void (*vjp)(const View<R> &, const double *rhsBar, double *cvBar, double *work, cudaStream_t);
