@@ -698,20 +698,58 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
     // tiled: s counts from the first staged 16-byte word of stencil ids
     const int s0 = kTiled ? 8 * (stOffSm[0] >> 3) : 0;
     const int sb = (kTiled ? stOffSm[li] : V.stOff[i]) - s0, se = (kTiled ? stOffSm[li + 1] : V.stOff[i + 1]) - s0;
+    if (kTiled) {
+      // Packed FP32 pairs (f32x2): the record's register pairs (rho, u),
+      // (v, w), (p, xc), (yc, zc) give the eight differences in four adds,
+      // and the sums of (rho, u) and (v, w) advance in pairs per direction.
+      // Each lane rounds as the scalar loop below does.
+      const float2 n01 = make_float2(-rec[0], -rec[1]), n23 = make_float2(-rec[2], -rec[3]);
+      const float2 n4x = make_float2(-rec[4], -rec[5]), nyz = make_float2(-rec[6], -rec[7]);
+      float2 gx01 = make_float2(0.f, 0.f), gx23 = gx01, gy01 = gx01, gy23 = gx01, gz01 = gx01, gz23 = gx01;
+      float gx4 = 0.f, gy4 = 0.f, gz4 = 0.f;
 #pragma unroll 2
-    for (int s = sb; s < se; ++s) {
-      float r[8];
-      if (kTiled) ldRec(recs, stSm[s], r);
-      else ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
-      const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
-      const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
-      const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
+      for (int s = sb; s < se; ++s) {
+        const int o = recHalf0(stSm[s]);
+        const float4 a = *reinterpret_cast<const float4 *>(recs + o);
+        const float4 b = *reinterpret_cast<const float4 *>(recs + (o ^ 4));
+        const float2 d01 = __fadd2_rn(make_float2(a.x, a.y), n01);
+        const float2 d23 = __fadd2_rn(make_float2(a.z, a.w), n23);
+        const float2 d4x = __fadd2_rn(make_float2(b.x, b.y), n4x);
+        const float2 dyz = __fadd2_rn(make_float2(b.z, b.w), nyz);
+        const float dx = d4x.y, dy = dyz.x, dz = dyz.y;
+        const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+        const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
+        const float2 sx2 = make_float2(sx, sx), sy2 = make_float2(sy, sy), sz2 = make_float2(sz, sz);
+        gx01 = __ffma2_rn(sx2, d01, gx01);
+        gx23 = __ffma2_rn(sx2, d23, gx23);
+        gy01 = __ffma2_rn(sy2, d01, gy01);
+        gy23 = __ffma2_rn(sy2, d23, gy23);
+        gz01 = __ffma2_rn(sz2, d01, gz01);
+        gz23 = __ffma2_rn(sz2, d23, gz23);
+        gx4 = fmaf(sx, d4x.x, gx4);
+        gy4 = fmaf(sy, d4x.x, gy4);
+        gz4 = fmaf(sz, d4x.x, gz4);
+      }
+      g[0] = gx01.x; g[1] = gy01.x; g[2] = gz01.x;
+      g[3] = gx01.y; g[4] = gy01.y; g[5] = gz01.y;
+      g[6] = gx23.x; g[7] = gy23.x; g[8] = gz23.x;
+      g[9] = gx23.y; g[10] = gy23.y; g[11] = gz23.y;
+      g[12] = gx4; g[13] = gy4; g[14] = gz4;
+    } else {
+#pragma unroll 2
+      for (int s = sb; s < se; ++s) {
+        float r[8];
+        ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
+        const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+        const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+        const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        const float d = r[k] - q[k];
-        g[3 * k] = g[3 * k] + sx * d;
-        g[3 * k + 1] = g[3 * k + 1] + sy * d;
-        g[3 * k + 2] = g[3 * k + 2] + sz * d;
+        for (int k = 0; k < 5; ++k) {
+          const float d = r[k] - q[k];
+          g[3 * k] = g[3 * k] + sx * d;
+          g[3 * k + 1] = g[3 * k + 1] + sy * d;
+          g[3 * k + 2] = g[3 * k + 2] + sz * d;
+        }
       }
     }
   }
