@@ -178,6 +178,11 @@ int rflu_gpu_adjoint_times(rflu_gpu_ctx *ctx, int nIter, double *ms);
 /* Diagnostics: FP64 fused multiply-add rate of the current device in
  * TFLOP/s (independent FMA chains on every SM), the roof of FP64 kernels. */
 int rflu_gpu_fp64_rate(double *tflops);
+/* Diagnostics: compares the mixed mode's integer-pipe float<->double
+ * conversions with the hardware conversions on n generated values (random
+ * doubles, doubles near the float range, rounding ties, widened floats and
+ * float midpoints) and returns the number of differing results. */
+int rflu_gpu_check_conversions(long long n, unsigned long long seed, unsigned long long *mismatches);
 
 /* Residual without any allocation (no counterpart in the reference).
  * Same result as rflu_gpu_residual (rhs only), for callers that cannot

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/rflu_gpu.h"
+#include "convert.cuh"
 #include "ctx.h"
 #include "errors.h"
 #include "ops.h"
@@ -158,6 +159,50 @@ bool isDevicePointer(const void *p) {
 
 // FP64 FMA throughput probe: 8 independent chains per thread.
 __device__ double gFmaSink;
+// Self-check of f2d/d2f against the hardware conversions.  Value k of the
+// sample: a 64-bit hash of (seed, k); by k mod 4 its bits as a double, a
+// double with an exponent near the float range (normal, denormal and
+// overflowing results), the same with the 29 bits dropped by the rounding set
+// to a tie, or a float (its hash bits) widened, plus the midpoint between it
+// and the next float up.
+__device__ inline unsigned long long mix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+__device__ inline bool sameFloat(float a, float b) {
+  return __float_as_uint(a) == __float_as_uint(b) || (isnan(a) && isnan(b));
+}
+__global__ void kCvtCheck(long long n, unsigned long long seed, unsigned long long *bad) {
+  unsigned long long miss = 0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long h = mix64(seed ^ mix64((unsigned long long)k));
+    const int mode = (int)(k & 3);
+    if (mode < 3) {
+      unsigned long long bits = h;
+      if (mode >= 1) {
+        const unsigned long long e = (h >> 40) % 340 + (1023 - 190);
+        bits = (h & 0x800FFFFFFFFFFFFFull) | (e << 52);
+        if (mode == 2) bits = (bits & ~0x1FFFFFFFull) | 0x10000000ull;
+      }
+      const double d = __longlong_as_double((long long)bits);
+      if (!sameFloat(d2f(d), __double2float_rn(d))) ++miss;
+    } else {
+      const float f = __uint_as_float((unsigned)(h >> 32));
+      const double w = f2d(f);
+      if (__double_as_longlong(w) != __double_as_longlong((double)f) && !(isnan(f) && isnan(w))) ++miss;
+      if (isfinite(f) && fabsf(f) < 3.0e38f) {
+        const double up = (double)__uint_as_float(__float_as_uint(f) + (f >= 0.f ? 1u : 0u) - (f < 0.f ? 1u : 0u));
+        const double mid = (double)f + (up - (double)f) * 0.5;
+        if (!sameFloat(d2f(mid), __double2float_rn(mid))) ++miss;
+        if (!sameFloat(d2f(w), f)) ++miss;
+      }
+    }
+  }
+  if (miss) atomicAdd(bad, miss);
+}
+
 __global__ void kFp64Fma(int iters, double seed) {
   double a[8];
 #pragma unroll
@@ -1248,6 +1293,24 @@ int rflu_gpu_fp64_rate(double *tflops) {
   if (err != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("rflu_gpu_fp64_rate: ") + cudaGetErrorString(err));
   const double flops = 2.0 * 8.0 * iters * (double)threads * sms * blocksPerSm;
   *tflops = flops / (ms * 1e-3) / 1e12;
+  return RFLU_OK;
+}
+
+int rflu_gpu_check_conversions(long long n, unsigned long long seed, unsigned long long *mismatches) {
+  if (!mismatches || n < 0) return fail(RFLU_ERR_ARG, "rflu_gpu_check_conversions: bad argument");
+  unsigned long long *bad = nullptr;
+  RFLU_CUDA(cudaMalloc(&bad, sizeof(unsigned long long)));
+  cudaError_t err = cudaMemset(bad, 0, sizeof(unsigned long long));
+  if (err == cudaSuccess) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    rflu::kCvtCheck<<<sms * 8, 256>>>(n, seed, bad);
+    err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaMemcpy(mismatches, bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(bad);
+  if (err != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("rflu_gpu_check_conversions: ") + cudaGetErrorString(err));
   return RFLU_OK;
 }
 

@@ -16,6 +16,7 @@
 #include <climits>
 #include <cuda_runtime.h>
 
+#include "convert.cuh"
 #include "ctx.h"
 #include "dual.cuh"
 #include "physics.cuh"
@@ -265,33 +266,6 @@ __device__ inline void loadFlux(const T *flux, size_t nT, int t, T *f) {
   }
 }
 
-// Conversions between float and double with integer and FP32 instructions,
-// bit-identical to the hardware conversions (round to nearest even): in the
-// mixed update they would otherwise occupy half of the FP64 pipe, the
-// kernel's bound on this part.
-__device__ inline double f2d(float f) {
-  // denormals are scaled into the normal range first (exact: a power of 2)
-  const bool den = (__float_as_uint(f) & 0x7F800000u) == 0u && f != 0.f;
-  const unsigned u = __float_as_uint(den ? f * 18446744073709551616.f : f);
-  const unsigned ex = (u >> 23) & 0xFFu;
-  unsigned long long dex = ex == 0u ? 0ull : (ex == 255u ? 2047ull : (unsigned long long)(ex + 896u));
-  if (den) dex -= 64ull;
-  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) | (dex << 52) |
-                                  ((unsigned long long)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)bits);
-}
-__device__ inline float d2f(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const int fex = (int)((b >> 52) & 0x7FFull) - 896;
-  if (fex <= 0 || fex >= 255) return (float)d;  // zero, float denormals, overflow, inf, nan
-  const unsigned long long man = b & 0xFFFFFFFFFFFFFull;
-  const unsigned m = (unsigned)(man >> 29);
-  const unsigned rem = (unsigned)(man & 0x1FFFFFFFull);
-  // the mantissa carry of the rounding increments the exponent, as it must
-  const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
-  const unsigned bits = ((unsigned)(b >> 32) & 0x80000000u) | (((unsigned)fex << 23) | m) + up;
-  return __uint_as_float(bits);
-}
 
 // Mixed mode: primitive state from the FP64 master cv.  1/rho from an FP32
 // seed y (also the FP32 velocities' reciprocal) refined once in FP64,

@@ -69,7 +69,7 @@ EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_g
            "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
            "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_residual", "rflu_gpu_vjp",
            "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_unrolled_adjoint", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
-           "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_setup_build", "rflu_setup_grid",
+           "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_gpu_check_conversions", "rflu_setup_build", "rflu_setup_grid",
            "rflu_setup_destroy")
 
 
@@ -112,6 +112,7 @@ def lib(build_if_missing=True):
     L.rflu_gpu_residual_static.argtypes = [P, P, P]
     L.rflu_gpu_adjoint_times.argtypes = [P, I, DP]
     L.rflu_gpu_fp64_rate.argtypes = [DP]
+    L.rflu_gpu_check_conversions.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]
     L.rflu_setup_build.argtypes = [C.POINTER(MeshDesc), I, C.POINTER(P)]
     L.rflu_setup_grid.argtypes = [P, C.POINTER(GridDesc)]
     L.rflu_setup_destroy.argtypes = [P]
@@ -347,6 +348,14 @@ def fp64_rate():
     t = C.c_double()
     _check(lib().rflu_gpu_fp64_rate(C.byref(t)))
     return t.value
+
+
+def check_conversions(n, seed=1):
+    """Mismatches of the mixed mode's float<->double conversions against the
+    hardware's over n generated values (0 expected)."""
+    m = C.c_ulonglong()
+    _check(lib().rflu_gpu_check_conversions(n, seed, C.byref(m)))
+    return m.value
 
 
 # --- the reference's subroutine names ---------------------------------------

@@ -316,3 +316,12 @@ def test_pinned_host_buffers_match_pageable(gpu_lib, prec):
     b.download(pin_cv.numpy(), pin_dv.numpy())
     np.testing.assert_array_equal(pin_cv.numpy(), cv_a)
     np.testing.assert_array_equal(pin_dv.numpy(), dv_a)
+
+
+def test_mixed_conversions_match_hardware(gpu_lib):
+    """The mixed update's integer-pipe float<->double conversions give the
+    hardware conversions' bits on 2^26 generated values per seed (random
+    doubles, the float exponent range with denormal and overflowing results,
+    rounding ties, widened floats and float midpoints)."""
+    for seed in (1, 2):
+        assert gpu.check_conversions(1 << 26, seed) == 0
