@@ -47,10 +47,13 @@ struct AdjWork {
   // stencil entry of cell j costs three 256-bit loads:
   // w_s . Gbar_i = (d/|d|^2) . (L_i Gbar_i), d = x_j - x_i (L symmetric)
   R *adjRec;
+  // packed layout: per cell the sum over its stencil of d/|d|^2 (3 Nc, SoA),
+  // so that the gradient's own term in the adjoint is one dot product
+  R *ssum;
 };
 
 // The workspace carved from the context's adjoint buffer: 81 Nc + 21 (Nf+Nb)
-// values of R, 10 Nc ints and (packed layout) 24 Nc floats on a 32-byte
+// values of R, 10 Nc ints and (packed layout) 24 + 3 Nc floats on a 32-byte
 // boundary (the context allocates sizeof(R)*(120 Nc + 24 (Nf+Nb) + 64) +
 // 4*10 Nc + 256 bytes).
 template <typename R>
@@ -81,6 +84,7 @@ inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
   p += sizeof(int) * 5 * nc;
   p = reinterpret_cast<char *>((reinterpret_cast<size_t>(p) + 31) & ~size_t(31));
   a.adjRec = reinterpret_cast<R *>(p);
+  a.ssum = a.adjRec + 24 * nc;
   return a;
 }
 
@@ -247,18 +251,57 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W) {
   ld.prim5(i, q);
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = R(0);
-  for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
-    const int j = V.stIdx[s];
-    R wx, wy, wz;
-    lsqWeight(V, i, s, wx, wy, wz);
-    R qj[5];
-    ld.prim5(j, qj);
+  if constexpr (Layout<R>::packed) {
+    // the primal's formulation (one record per member, L applied to the
+    // sums), so G is the primal's gradient; with it the sum of the members'
+    // d/|d|^2 for the own term of the reverse pass
+    float rec[8];
+    ld8(V.prim + 8 * (size_t)i, rec);
+    float sx0 = 0.f, sy0 = 0.f, sz0 = 0.f;
+#pragma unroll 2
+    for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
+      float r[8];
+      ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
+      const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+      const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+      const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
+      sx0 += sx;
+      sy0 += sy;
+      sz0 += sz;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const float d = r[k] - q[k];
+        g[3 * k] = g[3 * k] + sx * d;
+        g[3 * k + 1] = g[3 * k + 1] + sy * d;
+        g[3 * k + 2] = g[3 * k + 2] + sz * d;
+      }
+    }
+    const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
+    const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      R d = qj[k] - q[k];
-      g[3 * k] = g[3 * k] + wx * d;
-      g[3 * k + 1] = g[3 * k + 1] + wy * d;
-      g[3 * k + 2] = g[3 * k + 2] + wz * d;
+      const float x = g[3 * k], y = g[3 * k + 1], z = g[3 * k + 2];
+      g[3 * k] = lxx * x + lxy * y + lxz * z;
+      g[3 * k + 1] = lxy * x + lyy * y + lyz * z;
+      g[3 * k + 2] = lxz * x + lyz * y + lzz * z;
+    }
+    W.ssum[i] = sx0;
+    W.ssum[n + i] = sy0;
+    W.ssum[2 * n + i] = sz0;
+  } else {
+    for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
+      const int j = V.stIdx[s];
+      R wx, wy, wz;
+      lsqWeight(V, i, s, wx, wy, wz);
+      R qj[5];
+      ld.prim5(j, qj);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        R d = qj[k] - q[k];
+        g[3 * k] = g[3 * k] + wx * d;
+        g[3 * k + 1] = g[3 * k + 1] + wy * d;
+        g[3 * k + 2] = g[3 * k + 2] + wz * d;
+      }
     }
   }
 #pragma unroll
@@ -340,11 +383,15 @@ __device__ inline void contract(const Dual<N, T> *flx, const T *fbar, T *out) {
   }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nT = V.nf + V.nb;
-  if (t >= nT) return;
+// Face adjoints of faces t0 .. t1-1 (interior faces first, then boundary
+// faces).  kRoe2 compiles only the second-order Roe interior path (its
+// hand-written reverse sweep), so that the common case is not held to the
+// register allocation of the dual-number paths; the launcher gives it the
+// interior faces of such runs and the generic kernel the rest.
+template <typename R, bool kRoe2>
+__global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int t0, int t1) {
+  const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= t1) return;
   const Params &P = V.p;
   const size_t n = V.nc;
   const PlainLoad<R> ld{V};
@@ -358,7 +405,7 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W) {
     faceNormal(V, f, nx, ny, nz, nm);
 #pragma unroll
     for (int k = 0; k < 5; ++k) fbar[k] = W.cvd[k * n + c1] - W.cvd[k * n + c2];
-    if (P.spaceOrder == 1) {
+    if (!kRoe2 && P.spaceOrder == 1) {
       // first order: FP64 from cv and dv in every mode (as the primal)
       using D8 = Dual<8>;
       D8 cl[5], dl[3], cr[5], dr[3], flx[5];
@@ -387,7 +434,7 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W) {
       faceOffset(V, f, 1, dr);
       faceState(V, ld, c1, dl[0], dl[1], dl[2], L, irl);
       faceState(V, ld, c2, dr[0], dr[1], dr[2], Rt, irr);
-      if (P.spaceDiscr == 1) {
+      if (kRoe2 || P.spaceDiscr == 1) {
         // Roe: hand-written reverse sweep in the mode's arithmetic (no
         // dependence on the cell 1/rho)
         roe2Adjoint(P.refGamma, P.refCp, P.epsEntr, P.dissFact, nx, ny, nz, nm, L, Rt, fbar, out, out + 6);
@@ -405,11 +452,13 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W) {
         }
         ia = side ? D6(irl) : D6::seed(irl, 5);
         ib = side ? D6::seed(irr, 5) : D6(irr);
-        riemann2(P, D6(nx), D6(ny), D6(nz), D6(nm), a, ia, b, ib, flx);
-        contract(flx, fbar, out + 6 * side);
+        if constexpr (!kRoe2) {
+          riemann2(P, D6(nx), D6(ny), D6(nz), D6(nm), a, ia, b, ib, flx);
+          contract(flx, fbar, out + 6 * side);
+        }
       }
     }
-  } else {
+  } else if constexpr (!kRoe2) {
     const int b = t - V.nf, c = V.bcell[b], ip = V.bpatch[b];
     const int type = V.patchType[ip], order = V.patchOrder[ip];
 #pragma unroll
@@ -555,11 +604,13 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     }
   }
   // gradient own-term: G_i = sum_s w_s (q_{m_s} - q_i)
-  for (int s = V.stOff[i]; s < V.stOff[i + 1] && P.spaceOrder > 1; ++s) {
-    R wx, wy, wz;
-    lsqWeight(V, i, s, wx, wy, wz);
+  if constexpr (!Layout<R>::packed) {
+    for (int s = V.stOff[i]; s < V.stOff[i + 1] && P.spaceOrder > 1; ++s) {
+      R wx, wy, wz;
+      lsqWeight(V, i, s, wx, wy, wz);
 #pragma unroll
-    for (int k = 0; k < 5; ++k) qb[k] -= wx * gb[3 * k] + wy * gb[3 * k + 1] + wz * gb[3 * k + 2];
+      for (int k = 0; k < 5; ++k) qb[k] -= wx * gb[3 * k] + wy * gb[3 * k + 1] + wz * gb[3 * k + 2];
+    }
   }
 #pragma unroll
   for (int k = 0; k < 15; ++k) W.Gbar[k * n + i] = gb[k];
@@ -573,6 +624,13 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
       h[3 * k] = lxx * x + lxy * y + lxz * z;
       h[3 * k + 1] = lxy * x + lyy * y + lyz * z;
       h[3 * k + 2] = lxz * x + lyz * y + lzz * z;
+    }
+    // w_s = L_i d_s/|d_s|^2 with L_i symmetric: sum_s w_s . Gbar_k =
+    // (sum_s d_s/|d_s|^2) . (L_i Gbar_k)
+    if (P.spaceOrder > 1) {
+      const float sx = W.ssum[i], sy = W.ssum[n + i], sz = W.ssum[2 * n + i];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) qb[k] -= sx * h[3 * k] + sy * h[3 * k + 1] + sz * h[3 * k + 2];
     }
     h[15] = V.prim[8 * (size_t)i + 5];
     h[16] = V.prim[8 * (size_t)i + 6];
@@ -605,6 +663,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
   if (V.tsOff && V.p.spaceOrder > 1) {
     if constexpr (Layout<R>::packed) {
       const float xj = V.prim[8 * (size_t)j + 5], yj = V.prim[8 * (size_t)j + 6], zj = V.prim[8 * (size_t)j + 7];
+#pragma unroll 2
       for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
         float h[24];
         const float *rec = W.adjRec + 24 * (size_t)V.tsCell[e];
@@ -739,13 +798,22 @@ struct AdjointOps {
     kAdjCell1<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     kAdjCell2<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvBarRef);
   }
+  static void faceAdjoint(const View<R> &V, const AdjWork<R> &W, cudaStream_t s) {
+    const int nT = V.nf + V.nb;
+    if (V.p.spaceOrder > 1 && V.p.spaceDiscr == 1) {
+      if (V.nf > 0) kAdjFace<R, true><<<blocks((long long)V.nf), kBlock, 0, s>>>(V, W, 0, V.nf);
+      if (V.nb > 0) kAdjFace<R, false><<<blocks((long long)V.nb), kBlock, 0, s>>>(V, W, V.nf, nT);
+    } else if (nT > 0) {
+      kAdjFace<R, false><<<blocks((long long)nT), kBlock, 0, s>>>(V, W, 0, nT);
+    }
+  }
   static void vjp(const View<R> &V, const double *rhsBarRef, double *cvBarRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
     AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
     kAdjLambda<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
     if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     cudaMemsetAsync(W.faceAdj, 0, sizeof(R) * 16 * nT, s);
-    kAdjFace<R><<<blocks((long long)nT), kBlock, 0, s>>>(V, W);
+    faceAdjoint(V, W, s);
     cellAdjoint(V, W, cvBarRef, s);
   }
   static void patchPressure(const View<R> &V, int ip, double *J, double *cvBarRef, double *work, cudaStream_t s) {
