@@ -167,13 +167,15 @@ int rflu_gpu_unrolled_adjoint(rflu_gpu_ctx *ctx, const double *cv0, int nSteps, 
 int rflu_gpu_status(rflu_gpu_ctx *ctx, rflu_status *status);
 
 /* Diagnostics (no reference counterpart): runs nIter RK stages launch by
- * launch (no graph) with CUDA events between the kernels on the context's
- * stream and returns the mean duration in ms of [0] gradient+limiter,
- * [1] face fluxes, [2] gather+update, [3] time-step reduction. */
+ * launch (no graph, after one untimed stage) with CUDA events between the
+ * kernels on the context's stream and returns the mean duration in ms of
+ * [0] gradient+limiter, [1] face fluxes, [2] gather+update, [3] time-step
+ * reduction. */
 int rflu_gpu_kernel_times(rflu_gpu_ctx *ctx, int nIter, double *ms);
-/* Diagnostics (no reference counterpart): mean device time in ms of [0] one
- * primal residual (gradient+limiter, face fluxes, gather) and [1] one
- * adjoint (rflu_gpu_vjp's kernels) on the current device state, FP64 modes. */
+/* Diagnostics (no reference counterpart): mean device time in ms, over nIter
+ * repetitions after one untimed, of [0] one primal residual
+ * (gradient+limiter, face fluxes, gather) and [1] one adjoint (rflu_gpu_vjp's
+ * kernels) on the current device state. */
 int rflu_gpu_adjoint_times(rflu_gpu_ctx *ctx, int nIter, double *ms);
 /* Diagnostics: FP64 fused multiply-add rate of the current device in
  * TFLOP/s (independent FMA chains on every SM), the roof of FP64 kernels. */

@@ -42,18 +42,22 @@ struct AdjWork {
   R *cvd, *primd, *dvd, *gradd, *fluxd;  // tangent state / lambda in cvd
   R *G, *lim, *faceAdj, *Gbar, *qbar, *nbBar, *cvbarD, *dvbar;
   int *estar, *jstar;                    // 5 per cell each
-  // packed layout: per cell i a 24-float record (L_i Gbar_i for the five
-  // variables, 15 floats; the centroid x_i; pad), so that a transposed
-  // stencil entry of cell j costs three 256-bit loads:
+  // packed layout: per cell i a 16-float record (L_i Gbar_i for the five
+  // variables, 15 floats; pad), so that a transposed stencil entry of cell j
+  // costs two 256-bit loads next to its weights from View::tsW:
   // w_s . Gbar_i = (d/|d|^2) . (L_i Gbar_i), d = x_j - x_i (L symmetric)
   R *adjRec;
+  // packed layout: per cell a 12-word record of the limiter's extreme-
+  // neighbour terms: for each variable the neighbour that receives one (-1:
+  // none; int bits), then its value, then pad
+  R *nbRec;
   // packed layout: per cell the sum over its stencil of d/|d|^2 (3 Nc, SoA),
   // so that the gradient's own term in the adjoint is one dot product
   R *ssum;
 };
 
 // The workspace carved from the context's adjoint buffer: 81 Nc + 21 (Nf+Nb)
-// values of R, 10 Nc ints and (packed layout) 24 + 3 Nc floats on a 32-byte
+// values of R, 10 Nc ints and (packed layout) 16 + 12 + 3 Nc floats on a 32-byte
 // boundary (the context allocates sizeof(R)*(120 Nc + 24 (Nf+Nb) + 64) +
 // 4*10 Nc + 256 bytes).
 template <typename R>
@@ -84,7 +88,8 @@ inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
   p += sizeof(int) * 5 * nc;
   p = reinterpret_cast<char *>((reinterpret_cast<size_t>(p) + 31) & ~size_t(31));
   a.adjRec = reinterpret_cast<R *>(p);
-  a.ssum = a.adjRec + 24 * nc;
+  a.nbRec = a.adjRec + 16 * nc;
+  a.ssum = a.nbRec + 12 * nc;
   return a;
 }
 
@@ -240,12 +245,18 @@ __device__ inline S venkat(S dext, S d2, S epsq) {
   return numer / (denom + S(1.0e-12));
 }
 
-// Forward pass of the limited gradient with the limiter's active branch.
+// Forward pass of the limited gradient with the limiter's active branch;
+// with lamRef, also kAdjLambda's copy of the cell's adjoint seed.
 template <typename R>
-__global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W) {
+__global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, const double *lamRef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
   const size_t n = V.nc;
+  if (lamRef) {
+    const int o = V.refId[i];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) W.cvd[(size_t)k * n + i] = (R)lamRef[5 * (size_t)o + k];
+  }
   const PlainLoad<R> ld{V};
   R q[5], g[15];
   ld.prim5(i, q);
@@ -258,7 +269,7 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W) {
     float rec[8];
     ld8(V.prim + 8 * (size_t)i, rec);
     float sx0 = 0.f, sy0 = 0.f, sz0 = 0.f;
-#pragma unroll 2
+#pragma unroll 4
     for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
       float r[8];
       ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
@@ -555,6 +566,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   // irl = 1/rho of the cell (HLLC: Hl = el + irl*pl)
   qb[0] += rbar * (R(-1) / (rho * rho));
   R gb[15], nbb[5] = {0, 0, 0, 0, 0};
+  int nbt[5] = {-1, -1, -1, -1, -1};  // the neighbour receiving nbb[k]
 #pragma unroll
   for (int k = 0; k < 15; ++k) gb[k] = R(0);
   const int rc = P.reconst;
@@ -600,6 +612,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
       if (js >= 0) {
         qb[k] -= db;
         nbb[k] = db;
+        nbt[k] = js;
       }
     }
   }
@@ -617,7 +630,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   if constexpr (Layout<R>::packed) {
     const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
     const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
-    float h[24];
+    float h[16];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const float x = gb[3 * k], y = gb[3 * k + 1], z = gb[3 * k + 2];
@@ -632,20 +645,24 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
 #pragma unroll
       for (int k = 0; k < 5; ++k) qb[k] -= sx * h[3 * k] + sy * h[3 * k + 1] + sz * h[3 * k + 2];
     }
-    h[15] = V.prim[8 * (size_t)i + 5];
-    h[16] = V.prim[8 * (size_t)i + 6];
-    h[17] = V.prim[8 * (size_t)i + 7];
+    h[15] = 0.f;
+    float *rec = W.adjRec + 16 * (size_t)i;
 #pragma unroll
-    for (int k = 18; k < 24; ++k) h[k] = 0.f;
-    float *rec = W.adjRec + 24 * (size_t)i;
-#pragma unroll
-    for (int q = 0; q < 6; ++q) st4(rec + 4 * q, h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+    for (int q = 0; q < 4; ++q) st4(rec + 4 * q, h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
   }
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     W.qbar[k * n + i] = qb[k];
-    W.nbBar[k * n + i] = nbb[k];
     W.cvbarD[k * n + i] = cvb[k];
+  }
+  if constexpr (Layout<R>::packed) {
+    float *nr = W.nbRec + 12 * (size_t)i;
+    st4(nr, __int_as_float(nbt[0]), __int_as_float(nbt[1]), __int_as_float(nbt[2]), __int_as_float(nbt[3]));
+    st4(nr + 4, __int_as_float(nbt[4]), nbb[0], nbb[1], nbb[2]);
+    st4(nr + 8, nbb[3], nbb[4], 0.f, 0.f);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) W.nbBar[k * n + i] = nbb[k];
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) W.dvbar[k * n + i] = dvb[k];
@@ -662,19 +679,17 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
   for (int k = 0; k < 5; ++k) qb[k] = W.qbar[k * n + j];
   if (V.tsOff && V.p.spaceOrder > 1) {
     if constexpr (Layout<R>::packed) {
-      const float xj = V.prim[8 * (size_t)j + 5], yj = V.prim[8 * (size_t)j + 6], zj = V.prim[8 * (size_t)j + 7];
 #pragma unroll 2
-      for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
-        float h[24];
-        const float *rec = W.adjRec + 24 * (size_t)V.tsCell[e];
+      for (int k = 0; k < V.tsWidth; ++k) {
+        const float4 w = ld4(V.tsW + 4 * (k * n + j));
+        const int i = __float_as_int(w.w);
+        if (i < 0) break;
+        float h[16];
+        const float *rec = W.adjRec + 16 * (size_t)i;
         ld8(rec, h);
         ld8(rec + 8, h + 8);
-        ld8(rec + 16, h + 16);
-        const float dx = xj - h[15], dy = yj - h[16], dz = zj - h[17];
-        const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
-        const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
 #pragma unroll
-        for (int k = 0; k < 5; ++k) qb[k] += sx * h[3 * k] + sy * h[3 * k + 1] + sz * h[3 * k + 2];
+        for (int c = 0; c < 5; ++c) qb[c] += w.x * h[3 * c] + w.y * h[3 * c + 1] + w.z * h[3 * c + 2];
       }
     } else {
       for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
@@ -694,9 +709,20 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
     int c1, c2;
     faceCells(V, code >> 1, c1, c2);
     const int i = (code & 1) ? c1 : c2;
+    if constexpr (Layout<R>::packed) {
+      const float *nr = W.nbRec + 12 * (size_t)i;
+      const float4 a = ld4(nr), b = ld4(nr + 4), c = ld4(nr + 8);
+      const int t[5] = {__float_as_int(a.x), __float_as_int(a.y), __float_as_int(a.z), __float_as_int(a.w),
+                        __float_as_int(b.x)};
+      const float v[5] = {b.y, b.z, b.w, c.x, c.y};
 #pragma unroll
-    for (int k = 0; k < 5; ++k)
-      if (W.jstar[k * n + i] == j && W.estar[k * n + i] >= 0) qb[k] += W.nbBar[k * n + i];
+      for (int k = 0; k < 5; ++k)
+        if (t[k] == j) qb[k] += v[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        if (W.jstar[k * n + i] == j && W.estar[k * n + i] >= 0) qb[k] += W.nbBar[k * n + i];
+    }
   }
   const int o = V.refId[j];
   if constexpr (Layout<R>::packed) {
@@ -810,16 +836,18 @@ struct AdjointOps {
   static void vjp(const View<R> &V, const double *rhsBarRef, double *cvBarRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
     AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
-    kAdjLambda<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
-    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
-    cudaMemsetAsync(W.faceAdj, 0, sizeof(R) * 16 * nT, s);
+    // every face-adjoint entry the cell kernels read is written by the face
+    // kernels: no clearing of faceAdj here
+    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
+    else kAdjLambda<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
+    (void)nT;
     faceAdjoint(V, W, s);
     cellAdjoint(V, W, cvBarRef, s);
   }
   static void patchPressure(const View<R> &V, int ip, double *J, double *cvBarRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
     AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
-    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, nullptr);
     cudaMemsetAsync(W.faceAdj, 0, sizeof(R) * 16 * nT, s);
     kPatchSeed<R><<<1, kBlock, 0, s>>>(V, W, ip, J);
     if (cvBarRef) cellAdjoint(V, W, cvBarRef, s);

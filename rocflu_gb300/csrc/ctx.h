@@ -106,6 +106,11 @@ struct View {
   int tiled;                        // 0: the gather kernel instead
   int maxRecs;                      // max staged records over the tiles
   int maxTileSt;                    // max stencil entries of a tile's cells
+  // mixed mode, adjoint of the LSQ gradient: the transposed stencil entry-
+  // major (entry k of cell j at k*nc + j): d/|d|^2 with d = x_j - x_i for
+  // the cell i whose stencil holds j, and i as int bits (-1 past the end)
+  float *tsW;
+  int tsWidth;                      // entries per cell of tsW
   int tileGrid;                     // CTAs of the persistent tiled kernels
   int tileGridDt;                   // ... of the variant with the time-step sum
   int cfW;                          // max faces per cell (entries of feD/feN)

@@ -1167,6 +1167,29 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> 
   blockMinDt(V.sc, dt);
 }
 
+// The transposed-stencil weights of the mixed adjoint (View::tsW), formed
+// with the expression the gradient kernels use for the same pair of cells.
+template <typename R>
+__global__ void kTsWeights(View<R> V) {
+  if constexpr (Layout<R>::packed) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= V.nc) return;
+    const size_t n = V.nc;
+    const float xj = V.cgx[j], yj = V.cgy[j], zj = V.cgz[j];
+    const int b = V.tsOff[j], c = V.tsOff[j + 1] - b;
+    for (int k = 0; k < V.tsWidth; ++k) {
+      float4 w = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+      if (k < c) {
+        const int i = V.tsCell[b + k];
+        const float dx = xj - V.cgx[i], dy = yj - V.cgy[i], dz = zj - V.cgz[i];
+        const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+        w = make_float4(inv * dx, inv * dy, inv * dz, __int_as_float(i));
+      }
+      *reinterpret_cast<float4 *>(V.tsW + 4 * (k * n + j)) = w;
+    }
+  }
+}
+
 // Time step alone from the primitive state (mixed mode).
 template <typename R>
 __global__ void __launch_bounds__(kBlock) kCellDtPrim(View<R> V) {
@@ -1760,6 +1783,7 @@ struct Launch {
       setTileSmem<false, 0>(V); setTileSmem<false, 10>(V); setTileSmem<false, 100>(V); setTileSmem<false, 11>(V);
       setTileSmem<true, 0>(V); setTileSmem<true, 10>(V); setTileSmem<true, 100>(V); setTileSmem<true, 11>(V);
     }
+    if (V.tsW) kTsWeights<R><<<blocks(V.nc), kBlock>>>(V);
   }
   static void faceFlux(const View<R> &V, cudaStream_t s) {
     kFaceFlux<R><<<blocks((long long)V.nf + V.nb), kBlock, 0, s>>>(V);
