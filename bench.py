@@ -147,6 +147,24 @@ def dram_traffic(kernel, n_cells):
     return None
 
 
+def stage_bytes_per_cell(n_cells, n_faces, n_members):
+    """The fixed two-kernel-minimum byte count per cell and RK stage of the
+    whole stage (gradient + limiter kernel; flux + residual + update kernel),
+    neighbour gathers counted once, boundary faces ignored, with the mesh's
+    measured S (stencil members per cell) and Nf/Nc:
+      FP64:  cv r/w 80 + rhsSum r/w 80 + gradients w/r 240 + vol 8 + cofg 24
+             + R factor 48 + stencil ids 4 S + (fn 32 + fc 24 + f2c 8) Nf/Nc
+      mixed: the same terms with FP32 gradients (120) and FP32 geometry
+             (vol 4, cofg 12, R factor 24, face 16 + 12 + 8), the master cv
+             and rhsSum counted in FP64 (80 + 80).
+    At 128^3 hexes (S = 25.6, Nf/Nc = 2.98): 773 and 530 bytes."""
+    s = n_members / n_cells
+    r = n_faces / n_cells
+    fp64 = 80 + 80 + 240 + 8 + 24 + 48 + 4 * s + 64 * r
+    mixed = 80 + 80 + 120 + 4 + 12 + 24 + 4 * s + 36 * r
+    return {"fp64": fp64, "mixed": mixed, "S": s, "nf_per_nc": r}
+
+
 def algorithmic_bytes(region, precision):
     """Bytes per launch of the three stage kernels, counted from the data each
     kernel must move once (every cell or face record read once, neighbour
@@ -204,13 +222,18 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     if args.only_adjoint:
-        # the adjoint section alone (profiling runs of the adjoint kernels)
-        ac = cases.adjoint_tets(args.adj_n)
-        areg = gpu.Region(ac, "fp64")
-        at = areg.adjoint_times(3)
+        # the adjoint timing alone, on the single-VJP workload (profiling runs
+        # of the adjoint kernels), for each precision in --precisions
+        num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=cases.RECONST_BJ_COMP)
+        ac = cases.adjoint_tets(args.adj_n, num=num)
+        out = {}
+        for prec in [x for x in args.precisions.split(",") if x]:
+            areg = gpu.Region(ac, prec)
+            at = areg.adjoint_times(3)
+            out[prec] = {"primal_residual_ms": at[0], "vjp_ms": at[1], "vjp_over_primal": at[1] / at[0]}
+            areg.close()
         if rank == 0:
-            print(json.dumps({"partial": True, "adjoint": {"primal_residual_ms": at[0], "vjp_ms": at[1],
-                                                           "vjp_over_primal": at[1] / at[0]}}))
+            print(json.dumps({"partial": True, "adjoint": out}))
         return
 
     case = cases.shock_sphere(args.n)
@@ -308,6 +331,16 @@ def run_ours(args):
             "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": ab[dom], "launch_ms": km[dom]}
 
+    # whole-stage roofline of both paths (fixed per-cell-stage formula)
+    sb = stage_bytes_per_cell(regions["mixed"].n_cells, int(setup.f2c.shape[0]), int(setup.c2cs.shape[0]))
+    stage_roof = {"formula": "stage_bytes_per_cell (bench.py)", "S": sb["S"], "nf_per_nc": sb["nf_per_nc"],
+                  "peak_gbs": peaks["hbm_gbs"], "peak_source": peak_kind}
+    for prec in ("mixed", "fp64"):
+        stage_ms = results[prec]["ms"] / (args.steps * regions[prec].n_stages)
+        ach = sb[prec] * regions[prec].n_cells / (stage_ms * 1e-3) / 1e9
+        stage_roof[prec] = {"bytes_per_cell_stage": sb[prec], "stage_ms": stage_ms, "achieved_gbs": ach,
+                            "frac": ach / peaks["hbm_gbs"]}
+
     fp64_tflops = gpu.fp64_rate()
     fp64 = {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms"] / args.steps,
             "kernel_ms": results["fp64"]["kernel_ms"], "mixed_over_fp64": results["mixed"]["value"] / results["fp64"]["value"],
@@ -349,6 +382,7 @@ def run_ours(args):
             "unrolled_adjoint": unrolled,
             "e2e": e2e,
             "roofline": roof,
+            "stage_roofline": stage_roof,
             "cpu_baseline": cpu,
             "clocks": clocks,
         }
