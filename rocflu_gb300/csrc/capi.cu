@@ -104,10 +104,11 @@ __global__ void kAxpyInPlace(double *y, double a, const double *x, size_t n) {
 __global__ void kAccumJ(double *acc, const double *j, double dt) { *acc += dt * *j; }
 
 // Download: renumbered SoA (ncomp rows) -> reference order and layout, one
-// thread per reference cell so that the writes to `dst` are contiguous.
-__global__ void kGatherOut(const double *src, double *dst, const int *newId, int nc, int ncomp) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= nc) return;
+// thread per reference cell o0 .. o1-1 so that the writes to `dst` are
+// contiguous.
+__global__ void kGatherOut(const double *src, double *dst, const int *newId, int nc, int ncomp, int o0, int o1) {
+  const int o = o0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= o1) return;
   const int i = newId[o];
   for (int k = 0; k < ncomp; ++k) dst[(size_t)ncomp * o + k] = src[(size_t)k * nc + i];
 }
@@ -252,6 +253,10 @@ struct CtxBase {
   virtual int unrolledAdjoint(const double *cv0, int nSteps, double dt, int every, int iPatch, double *J,
                               double *cvBar0, double *stats) = 0;
   cudaStream_t stream = nullptr;
+  // host transfers: the copy stream and one event per chunk (+ one)
+  static constexpr int kMaxChunks = 8;
+  cudaStream_t copyStream = nullptr;
+  cudaEvent_t chunkEv[kMaxChunks + 1] = {};
 };
 
 template <typename R>
@@ -270,6 +275,9 @@ struct Ctx : CtxBase {
     if (stepGraph) cudaGraphExecDestroy(stepGraph);
     if (fixedGraph) cudaGraphExecDestroy(fixedGraph);
     for (void *p : allocs) cudaFree(p);
+    for (auto &e : chunkEv)
+      if (e) cudaEventDestroy(e);
+    if (copyStream) cudaStreamDestroy(copyStream);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -323,13 +331,46 @@ struct Ctx : CtxBase {
     ops->faceFlux(V, stream);
     ops->gatherUpdate(V, iStage, &V.sc->dtMin, stream);
   }
-  // cv(5,nCells) of the host: one copy into the staging buffer (the copy
-  // engines move pinned buffers at ~200 GB/s; kernels reading the host
-  // buffer directly measured 2x slower), then one upload kernel
+  // Host <-> device transfers in reference order go through the staging
+  // buffer in chunks of reference cells: chunk c's copy runs on copyStream
+  // while the kernel of chunk c-1 (permute + state set-up, or the reference-
+  // order gather) runs on the stream, so that only one chunk's kernel is
+  // not hidden behind the copies (the copy engines move pinned buffers at
+  // ~200 GB/s; kernels reading the host buffer directly measured 2x slower).
+  int nChunks() const { return V.nc >= (1 << 18) ? kMaxChunks : 1; }
+  int chunkBegin(int c) const { return (int)(((long long)V.nc * c) / nChunks()); }
   int setState(const double *cv) {
-    RFLU_CUDA(cudaMemcpyAsync(staging, cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
-    ops->initFromRef(V, staging, stream);
+    const int K = nChunks();
+    // staging is free once the work queued on the stream so far is done
+    RFLU_CUDA(cudaEventRecord(chunkEv[kMaxChunks], stream));
+    RFLU_CUDA(cudaStreamWaitEvent(copyStream, chunkEv[kMaxChunks], 0));
+    for (int c = 0; c < K; ++c) {
+      const int o0 = chunkBegin(c), o1 = chunkBegin(c + 1);
+      RFLU_CUDA(cudaMemcpyAsync(staging + 5 * (size_t)o0, cv + 5 * (size_t)o0, sizeof(double) * 5 * (size_t)(o1 - o0),
+                                cudaMemcpyHostToDevice, copyStream));
+      RFLU_CUDA(cudaEventRecord(chunkEv[c], copyStream));
+      RFLU_CUDA(cudaStreamWaitEvent(stream, chunkEv[c], 0));
+      ops->initFromRef(V, staging, o0, o1, stream);
+    }
     return checkLaunch("upload");
+  }
+  // the reference-order gather of ncomp rows of src into staging + off and
+  // the copy to the host, chunk by chunk
+  int gatherToHost(const double *src, int ncomp, size_t off, double *host) {
+    const int K = nChunks();
+    for (int c = 0; c < K; ++c) {
+      const int o0 = chunkBegin(c), o1 = chunkBegin(c + 1);
+      if (o1 <= o0) continue;
+      kGatherOut<<<nblk(o1 - o0), 256, 0, stream>>>(src, staging + off, V.newId, V.nc, ncomp, o0, o1);
+      RFLU_CUDA(cudaEventRecord(chunkEv[c], stream));
+      RFLU_CUDA(cudaStreamWaitEvent(copyStream, chunkEv[c], 0));
+      RFLU_CUDA(cudaMemcpyAsync(host + (size_t)ncomp * o0, staging + off + (size_t)ncomp * o0,
+                                sizeof(double) * ncomp * (size_t)(o1 - o0), cudaMemcpyDeviceToHost, copyStream));
+    }
+    // later work on the stream may overwrite staging: it waits for the copies
+    RFLU_CUDA(cudaEventRecord(chunkEv[kMaxChunks], copyStream));
+    RFLU_CUDA(cudaStreamWaitEvent(stream, chunkEv[kMaxChunks], 0));
+    return RFLU_OK;
   }
 
   int upload(const double *cv) override {
@@ -340,15 +381,9 @@ struct Ctx : CtxBase {
   }
   int download(double *cv, double *dv) override {
     if (dv && V.p.dvPOnly) kDvFill<<<nblk(V.nc), 256, 0, stream>>>(V.cv, V.dv, V.nc, V.p.gcR, V.p.gRT);
-    if (cv) {
-      kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.cv, staging, V.newId, V.nc, 5);
-      RFLU_CUDA(cudaMemcpyAsync(cv, staging, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
-    }
-    if (dv) {
-      kGatherOut<<<nblk(V.nc), 256, 0, stream>>>(V.dv, staging + 5 * (size_t)V.nc, V.newId, V.nc, 3);
-      RFLU_CUDA(cudaMemcpyAsync(dv, staging + 5 * (size_t)V.nc, sizeof(double) * 3 * (size_t)V.nc,
-                                cudaMemcpyDeviceToHost, stream));
-    }
+    int rcg = RFLU_OK;
+    if (cv && (rcg = gatherToHost(V.cv, 5, 0, cv))) return rcg;
+    if (dv && (rcg = gatherToHost(V.dv, 3, 5 * (size_t)V.nc, dv))) return rcg;
     int rc = checkLaunch("download");
     if (rc) return rc;
     return syncEvents(false);
@@ -877,6 +912,8 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   const int nb = np > 0 ? g->patchFaceOff[np] : 0;
   nPatches = np;
   RFLU_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  RFLU_CUDA(cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking));
+  for (auto &e : chunkEv) RFLU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 
   // ---- renumbering: Morton order of the cell centroids --------------------
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};

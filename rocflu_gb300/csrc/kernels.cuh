@@ -334,11 +334,12 @@ __global__ void kInitState(View<R> V) {
 
 // Upload in one pass: cv(5,nCells) in the reference's order and layout
 // (staged on the device) -> the renumbered master cv, primitive state and
-// dependent variables; one thread per reference cell (contiguous reads).
+// dependent variables; one thread per reference cell o0 .. o1-1 (contiguous
+// reads).
 template <typename R>
-__global__ void kInitFromRef(View<R> V, const double *ref) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= V.nc) return;
+__global__ void kInitFromRef(View<R> V, const double *ref, int o0, int o1) {
+  const int o = o0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= o1) return;
   const int i = V.newId[o];
   double cv[5];
 #pragma unroll
@@ -1730,8 +1731,8 @@ __global__ void kStepEnd(View<R> V) {
 template <typename R>
 struct Launch {
   static void initState(const View<R> &V, cudaStream_t s) { kInitState<R><<<blocks(V.nc), kBlock, 0, s>>>(V); }
-  static void initFromRef(const View<R> &V, const double *ref, cudaStream_t s) {
-    kInitFromRef<R><<<blocks(V.nc), kBlock, 0, s>>>(V, ref);
+  static void initFromRef(const View<R> &V, const double *ref, int o0, int o1, cudaStream_t s) {
+    if (o1 > o0) kInitFromRef<R><<<blocks(o1 - o0), kBlock, 0, s>>>(V, ref, o0, o1);
   }
   static void gradLimit(const View<R> &V, cudaStream_t s) {
     if (V.p.spaceOrder < 2) return;

@@ -11,7 +11,8 @@ namespace rflu {
 template <typename R>
 struct Ops {
   void (*initState)(const View<R> &, cudaStream_t);
-  void (*initFromRef)(const View<R> &, const double *cvRef, cudaStream_t);  // permute-in + initState
+  // permute-in + initState of the reference cells o0 .. o1-1
+  void (*initFromRef)(const View<R> &, const double *cvRef, int o0, int o1, cudaStream_t);
   void (*gradLimit)(const View<R> &, cudaStream_t);
   void (*faceFlux)(const View<R> &, cudaStream_t);
   void (*gatherRhs)(const View<R> &, cudaStream_t);

@@ -325,3 +325,30 @@ def test_mixed_conversions_match_hardware(gpu_lib):
     rounding ties, widened floats and float midpoints)."""
     for seed in (1, 2):
         assert gpu.check_conversions(1 << 26, seed) == 0
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_chunked_transfers_round_trip(gpu_lib, prec):
+    """Meshes of 2^18 cells and more move cv and dv in chunks, each chunk's
+    copy overlapped with the permutation kernel of the one before: an upload
+    followed by a download returns the uploaded cv bit for bit, through
+    pageable and through pinned buffers, with the same dv both ways and p
+    the pressure of cv."""
+    torch = pytest.importorskip("torch")
+    c = cases.shock_sphere(64)
+    assert c.cv0.shape[0] >= 1 << 18
+    cv0 = _perturbed(c)
+    r = gpu.Region(c, prec)
+    r.upload(cv0)
+    cv1, dv1 = r.download()
+    np.testing.assert_array_equal(cv1, cv0)
+    pin_in = torch.from_numpy(cv0.copy()).pin_memory()
+    pin_cv = torch.empty(cv0.shape, dtype=torch.float64).pin_memory()
+    pin_dv = torch.empty((cv0.shape[0], 3), dtype=torch.float64).pin_memory()
+    r.upload(pin_in.numpy())
+    r.download(pin_cv.numpy(), pin_dv.numpy())
+    np.testing.assert_array_equal(pin_cv.numpy(), cv0)
+    np.testing.assert_array_equal(pin_dv.numpy(), dv1)
+    g = c.num.gamma
+    p = (g - 1.0) * (cv0[:, 4] - 0.5 * (cv0[:, 1:4] ** 2).sum(axis=1) / cv0[:, 0])
+    np.testing.assert_allclose(dv1[:, 0], p, rtol=1e-12)
