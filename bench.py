@@ -65,6 +65,25 @@ def parse():
     return p.parse_args()
 
 
+def max_over_ranks(x, device=None):
+    """The maximum of x over the ranks of the default process group (x itself
+    when the job is not distributed): the slowest rank's time."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(units_per_rank, world_size, ms):
+    """Mcell*RK-stage/s of the whole job: the cell-stages all ranks processed
+    (each rank runs its own region: replicas) over the slowest rank's ms."""
+    return world_size * units_per_rank / (ms * 1e-3) / 1e6
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -264,16 +283,10 @@ def run_ours(args):
         e1.record(stream)
         e1.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
+        ms = max_over_ranks(e0.elapsed_time(e1), dev)
         clocks = None
-        if ws > 1:
-            import torch.distributed as dist
-
-            tt = torch.tensor([ms], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            ms = float(tt.item())
         units = region_units = reg.n_cells * reg.n_stages * args.steps
-        results[prec] = {"ms": ms, "value": ws * units / (ms * 1e-3) / 1e6, "clocks": clocks, "rc": rc,
+        results[prec] = {"ms": ms, "value": whole_job_value(units, ws, ms), "clocks": clocks, "rc": rc,
                          "time": t, "steps": n}
         ktimes = reg.kernel_times(5)
         results[prec]["kernel_ms"] = {"gradLimit": ktimes[0], "faceFlux": ktimes[1], "gatherUpdate": ktimes[2],
@@ -314,9 +327,9 @@ def run_ours(args):
             _, t, _ = reg.step(1, t)
             reg.download(cv_np, with_dv=False)
         barrier()
-        wall = time.perf_counter() - w0
+        wall = max_over_ranks(time.perf_counter() - w0, dev)
         units = reg.n_cells * reg.n_stages * args.steps
-        e2e = {"value": ws * units / wall / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(host_cv.numel() * 8),
+        e2e = {"value": whole_job_value(units, ws, wall * 1e3), "unit": UNIT, "h2d_bytes_per_step": int(host_cv.numel() * 8),
                "d2h_bytes_per_step": int(host_cv.numel() * 8)}
     clocks = clk.stop()
 
@@ -546,10 +559,9 @@ def run_reference(args):
     ctx = mp.get_context("spawn")
     cores = os.cpu_count() or 1
     vals = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
     samples = []
-    for step in range(args.steps):
+    # W untimed samples, then K timed ones
+    for step in range(-args.warmup, args.steps):
         q = ctx.Queue()
         procs = [ctx.Process(target=_cpu_worker, args=(args.cpu_n, args.cpu_steps, q)) for _ in range(cores)]
         w0 = time.perf_counter()
@@ -558,6 +570,8 @@ def run_reference(args):
         res = [q.get() for _ in procs]
         for p in procs:
             p.join()
+        if step < 0:
+            continue
         units = sum(r[0] for r in res)
         wall = max(r[1] for r in res)
         samples.append(units / wall / 1e6)

@@ -1,0 +1,47 @@
+"""bench.py's host logic for more than one rank, on CPU (gloo, world size
+2): each rank times its own region (replicas), the job's time is the
+slowest rank's and its value counts every rank's cell-stages; the reference
+arm runs on rank 0 alone and the other ranks exit 0 without output."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..")
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def test_max_over_ranks_and_whole_job_value():
+    ws, port = 2, _free_port()
+    procs = []
+    for rank in range(ws):
+        env = dict(os.environ, RANK=str(rank), WORLD_SIZE=str(ws), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.join(ROOT, "tests", "dist_rank.py")], env=env,
+                                      stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
+    outs = []
+    for p in procs:
+        out, err = p.communicate(timeout=300)
+        assert p.returncode == 0, err
+        outs.append(json.loads(out.strip().splitlines()[-1]))
+    for o in outs:
+        assert o["ms"] == 15.0  # the slowest rank
+        assert o["value"] == pytest.approx(2 * 1_000_000 / 15e-3 / 1e6)
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    env = dict(os.environ, WORLD_SIZE="2", RANK="1", LOCAL_RANK="1")
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference"], env=env,
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert p.stdout.strip() == ""
