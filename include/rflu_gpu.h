@@ -76,7 +76,9 @@ typedef struct {
 typedef struct {
   int spaceOrder;   /* ORDER: 1 or 2 */
   int spaceDiscr;   /* DISCR: 1 Roe, 3 HLLC, 4 AUSM+ */
-  int reconst;      /* RECONST: 0 none, 10 Barth-Jespersen (frame-invariant velocity), 11 Venkatakrishnan, 100 componentwise BJ */
+  int reconst;      /* RECONST: 0 none, 1 WENO (simple) and 2 WENO-XYZ gradient smoothing with the simple
+                       positivity limiter, 10 Barth-Jespersen (frame-invariant velocity), 11 Venkatakrishnan,
+                       100 componentwise BJ */
   int rkScheme;     /* RKSCHEME: 1 classical RK4, 2 Wray RK3, 3 Euler */
   int piclBuild;    /* 1 when reproducing the reference built with PICL (its CMake default) */
   int precision;    /* RFLU_PREC_* */
@@ -139,10 +141,13 @@ int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *
 /* Discrete adjoint of the same residual (no reference counterpart; it
  * differentiates rflu_gpu_residual): cvBar = (dR/dcv)^T rhsBar, through the
  * limiter's active branch.  Arrays (5,nCells).  In the mixed mode the flux,
- * reconstruction and limiter Jacobians are FP32, the cons -> prim Jacobian
- * FP64 (the arithmetic of the mixed residual). */
+ * reconstruction, limiter and cons -> prim Jacobians are FP32 (the last in
+ * closed form: unlike the pressure recovery it differentiates, it has no
+ * cancellation).  RECONST 10 (eigenframe limiter), 1 and 2 (WENO
+ * smoothing): RFLU_ERR_UNSUPPORTED. */
 int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar);
-/* Tangent of the same residual: rhsDot = (dR/dcv) cvDot. */
+/* Tangent of the same residual: rhsDot = (dR/dcv) cvDot (every limiter but
+ * the WENO smoothing, RECONST 1 and 2: RFLU_ERR_UNSUPPORTED). */
 int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, double *rhsDot);
 /* Boundary-pressure functional J = sum over the faces of patch iPatch
  * (0-based) of p_f*|A_f|, p_f the limited second-order face pressure of the
@@ -160,7 +165,7 @@ int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, dou
  * be NULL): forward-sweep ms, reverse-sweep ms (recompute + adjoint), device
  * bytes held by the context and the call, number of checkpoints.  Every
  * precision mode (the mixed mode runs its own primal and FP32-Jacobian
- * adjoint); RECONST 10 has no adjoint.  Leaves the context state untouched. */
+ * adjoint); RECONST 10, 1 and 2 have no adjoint.  Leaves the context state untouched. */
 int rflu_gpu_unrolled_adjoint(rflu_gpu_ctx *ctx, const double *cv0, int nSteps, double dtMin, int every, int iPatch,
                               double *J, double *cvBar0, double *stats);
 

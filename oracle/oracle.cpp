@@ -702,6 +702,92 @@ void symmetricEigen3(const double m[9], double vec[9], double val[3]) {
 #undef V
 }
 
+/* WENO smoothing of the cell gradients (modflu/RFLU_ModWENO.F90), 3-D
+   stencils: every gradient becomes an average over the cell and its stencil
+   members (the cell first, then the members in stencil order), weighted by
+   an inverse squared magnitude + 1e-15, from the unsmoothed gradients of
+   all cells.
+   xyz = true:  RFLU_WENOGradCellsXYZFast_3D (:1366-1572, RECONST 2): each
+                direction by its own component, sum of w*g over sum of w;
+   xyz = false: RFLU_WENOGradCells_3D (:298-452, RECONST 1): one weight per
+                cell from |gx|+|gy|+|gz|, normalised weights applied. */
+void wenoGradCells(orc_ctx *c, std::vector<double> &grad, bool xyz) {
+  const int nc = c->nCells;
+  std::vector<double> out(grad.size());
+  for (int icg = 0; icg < nc; ++icg) {
+    const int sb = c->stOff[icg], se = c->stOff[icg + 1];
+    for (int iv = 0; iv < 5; ++iv) {
+      const double *g0 = &grad[15 * icg + 3 * iv];
+      double *o = &out[15 * icg + 3 * iv];
+      if (xyz) {
+        for (int d = 0; d < 3; ++d) {
+          double term = g0[d];
+          double sum = 1.0 / (term * term + 1.0e-15);
+          double gl = sum * term;
+          for (int s = sb; s < se; ++s) {
+            term = grad[15 * c->stIdx[s] + 3 * iv + d];
+            double w = 1.0 / (term * term + 1.0e-15);
+            sum = sum + w;
+            gl = gl + w * term;
+          }
+          o[d] = gl / sum;
+        }
+      } else {
+        double term = std::fabs(g0[0]) + std::fabs(g0[1]) + std::fabs(g0[2]);
+        const double w0 = 1.0 / (term * term + 1.0e-15);
+        double sum = w0;
+        for (int s = sb; s < se; ++s) {
+          const double *gj = &grad[15 * c->stIdx[s] + 3 * iv];
+          term = std::fabs(gj[0]) + std::fabs(gj[1]) + std::fabs(gj[2]);
+          sum = sum + 1.0 / (term * term + 1.0e-15);
+        }
+        term = w0 / sum;
+        o[0] = term * g0[0];
+        o[1] = term * g0[1];
+        o[2] = term * g0[2];
+        for (int s = sb; s < se; ++s) {
+          const double *gj = &grad[15 * c->stIdx[s] + 3 * iv];
+          double t = std::fabs(gj[0]) + std::fabs(gj[1]) + std::fabs(gj[2]);
+          term = (1.0 / (t * t + 1.0e-15)) / sum;
+          o[0] = o[0] + term * gj[0];
+          o[1] = o[1] + term * gj[1];
+          o[2] = o[2] + term * gj[2];
+        }
+      }
+    }
+  }
+  grad.swap(out);
+}
+
+/* RFLU_LimitGradCellsSimple (:1147-1300): the gradient of a positive
+   variable (density and pressure, libflu/RFLU_SetVarInfo.F90:140-144) is
+   zeroed when its reconstruction at a face of the cell,
+   ((var + gx*dx) + gy*dy) + gz*dz with d = fc - cofg, is <= 0.  The
+   reference's face loop stops at the first such face; whether any face
+   does is independent of the order, so the faces are visited face by face
+   here (interior, then the patches) and the gradients zeroed afterwards. */
+void limitGradCellsSimple(orc_ctx *c, const std::vector<double> &var, std::vector<double> &grad) {
+  const int nc = c->nCells;
+  std::vector<char> zero(5 * (size_t)nc, 0);
+  auto check = [&](int ic, const double *fcp) {
+    const double dx = fcp[0] - c->cofg[3 * ic], dy = fcp[1] - c->cofg[3 * ic + 1], dz = fcp[2] - c->cofg[3 * ic + 2];
+    for (int iv = 0; iv < 5; iv += 4) {
+      const double *g = &grad[15 * ic + 3 * iv];
+      const double varf = var[5 * ic + iv] + g[0] * dx + g[1] * dy + g[2] * dz;
+      if (varf <= 0.0) zero[5 * ic + iv] = 1;
+    }
+  };
+  for (int f = 0; f < c->nFaces; ++f) {
+    check(c->f2c[2 * f], &c->fc[3 * f]);
+    check(c->f2c[2 * f + 1], &c->fc[3 * f]);
+  }
+  for (const Patch &p : c->patches)
+    for (size_t b = 0; b < p.bf2c.size(); ++b) check(p.bf2c[b], &p.fc[3 * b]);
+  for (int ic = 0; ic < nc; ++ic)
+    for (int iv = 0; iv < 5; ++iv)
+      if (zero[5 * ic + iv]) grad[15 * ic + 3 * iv] = grad[15 * ic + 3 * iv + 1] = grad[15 * ic + 3 * iv + 2] = 0.0;
+}
+
 /* RFLU_LimitGradVelocityBarthJesp (:588-790). gradVel(iComp,dir) = grad(dir, 2+iComp). */
 void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std::vector<double> &grad,
                                 std::vector<double> &lim) {
@@ -810,6 +896,11 @@ void cellGradients(orc_ctx *c) {
   computeGradCells(c, c->cv, c->grad);
   switch (c->num.reconst) {
   case 0: break;
+  case 1:
+  case 2:
+    wenoGradCells(c, c->grad, c->num.reconst == 2);
+    limitGradCellsSimple(c, c->cv, c->grad);
+    break;
   case 10:
     limiterBarthJesp(c, c->cv, c->grad, c->lim, true);
     limitGradVelocityBarthJesp(c, c->cv, c->grad, c->lim);
@@ -818,7 +909,7 @@ void cellGradients(orc_ctx *c) {
   case 11: limiterVenkat(c, c->cv, c->grad, c->lim); break;
   default: std::fprintf(stderr, "oracle: RECONST %d not supported\n", c->num.reconst); std::abort();
   }
-  if (c->num.reconst != 0) {
+  if (c->num.reconst == 10 || c->num.reconst == 100 || c->num.reconst == 11) {
     /* RFLU_LimitGradCells (RFLU_ModLimiters.F90:1061-1146) */
     for (int ic = 0; ic < nc; ++ic)
       for (int iv = 0; iv < 5; ++iv) {

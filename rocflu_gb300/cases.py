@@ -22,6 +22,7 @@ BC_SLIPWALL = 60
 
 DISCR_ROE, DISCR_HLLC, DISCR_AUSM = 1, 3, 4
 RECONST_NONE, RECONST_BJ, RECONST_VENKAT, RECONST_BJ_COMP = 0, 10, 11, 100
+RECONST_WENO_SIMPLE, RECONST_WENO_XYZ = 1, 2
 RK_CLASSICAL4, RK_WRAY3, RK_EULER = 1, 2, 3
 
 

@@ -517,6 +517,8 @@ struct Ctx : CtxBase {
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
     if (V.p.reconst == 10)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: the eigen-frame velocity limiter (RECONST 10) has a tangent only");
+    if (V.p.reconst == 1 || V.p.reconst == 2)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through WENO smoothing (RECONST 1, 2)");
     int rc = adjointPrep(cv);
     if (rc) return rc;
     const size_t nc = V.nc;
@@ -527,6 +529,8 @@ struct Ctx : CtxBase {
   }
   int jvp(const double *cv, const double *cvDot, double *rhsDot) override {
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
+    if (V.p.reconst == 1 || V.p.reconst == 2)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through WENO smoothing (RECONST 1, 2)");
     int rc = adjointPrep(cv);
     if (rc) return rc;
     const size_t nc = V.nc;
@@ -538,8 +542,8 @@ struct Ctx : CtxBase {
   int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) override {
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
-    if (cvBar && V.p.reconst == 10)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through RECONST 10");
+    if (cvBar && (V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2))
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through RECONST 10, 1 or 2");
     int rc = adjointPrep(cv);
     if (rc) return rc;
     const size_t nc = V.nc;
@@ -607,7 +611,8 @@ struct Ctx : CtxBase {
     const size_t bCv = up(5 * nc * sizeof(double)), bDv = up(3 * nc * sizeof(double));
     const size_t bPrim = up(Layout<R>::prim * nc * sizeof(R)), bGrad = up(Layout<R>::grad * nc * sizeof(R));
     const size_t bFlux = up(5 * nT * sizeof(R)), bRhs = up(5 * nc * sizeof(R));
-    const size_t need = bCv + bDv + bPrim + bGrad + bFlux + bRhs;
+    const size_t bRaw = V.gradRaw ? bGrad : 0;
+    const size_t need = bCv + bDv + bPrim + bGrad + bRaw + bFlux + bRhs;
     if (need > kStaticScratchBytes)
       return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: this mesh needs " + std::to_string(need) +
                                     " bytes of scratch; the static scratch holds " +
@@ -621,6 +626,7 @@ struct Ctx : CtxBase {
     W.dv = (double *)p;            p += bDv;
     W.prim = (R *)p;               p += bPrim;
     W.grad = (R *)p;               p += bGrad;
+    if (V.gradRaw) { W.gradRaw = (R *)p; p += bRaw; }
     W.flux = (R *)p;               p += bFlux;
     W.rhs = (R *)p;
     kPermuteIn<<<nblk(W.nc), 256, 0, stream>>>(cvDev, W.cv, W.refId, W.nc);
@@ -644,7 +650,8 @@ struct Ctx : CtxBase {
     if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
       return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
-    if (V.p.reconst == 10) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: RECONST 10 has no adjoint");
+    if (V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: RECONST 10, 1 and 2 have no adjoint");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     const int nrk = V.p.nrkSteps;
     double W[6][6] = {};
@@ -773,7 +780,8 @@ struct Ctx : CtxBase {
   }
   int adjointTimes(int nIter, double *ms) override {
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
-    if (!ops->vjp || V.p.reconst == 10) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
+    if (!ops->vjp || V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
     const size_t nc = V.nc;
     RFLU_CUDA(cudaMemsetAsync(staging, 0, sizeof(double) * 5 * nc, stream));
     cudaEvent_t ev[3];
@@ -1137,6 +1145,9 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   if ((rc = alloc(&V.dv, 3 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.prim, Layout<R>::prim * (size_t)nc))) return rc;
   if ((rc = alloc(&V.grad, Layout<R>::grad * (size_t)nc))) return rc;
+  if ((num->reconst == 1 || num->reconst == 2) && num->spaceOrder > 1 &&
+      (rc = alloc(&V.gradRaw, Layout<R>::grad * (size_t)nc)))
+    return rc;
   if ((rc = alloc(&V.rhsSum, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.flux, 5 * ((size_t)nf + nb)))) return rc;
   if ((rc = alloc(&V.rhs, 5 * (size_t)nc))) return rc;
@@ -1211,8 +1222,9 @@ int rflu_gpu_create(const rflu_grid_desc *grid, const rflu_num_desc *num, rflu_g
   if (num->spaceOrder != 1 && num->spaceOrder != 2) return fail(RFLU_ERR_ARG, "rflu_gpu_create: ORDER must be 1 or 2");
   if (num->spaceDiscr != 1 && num->spaceDiscr != 3 && num->spaceDiscr != 4)
     return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: DISCR must be 1 (Roe), 3 (HLLC) or 4 (AUSM+)");
-  if (num->reconst != 0 && num->reconst != 10 && num->reconst != 11 && num->reconst != 100)
-    return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: RECONST must be 0, 10, 11 or 100");
+  if (num->reconst != 0 && num->reconst != 1 && num->reconst != 2 && num->reconst != 10 && num->reconst != 11 &&
+      num->reconst != 100)
+    return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: RECONST must be 0, 1, 2, 10, 11 or 100");
   if (num->rkScheme < 1 || num->rkScheme > 3) return fail(RFLU_ERR_ARG, "rflu_gpu_create: RKSCHEME must be 1, 2 or 3");
   if (num->precision < 0 || num->precision > 2) return fail(RFLU_ERR_ARG, "rflu_gpu_create: bad precision");
   int dev = 0;

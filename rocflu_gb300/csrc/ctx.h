@@ -106,6 +106,9 @@ struct View {
   int tiled;                        // 0: the gather kernel instead
   int maxRecs;                      // max staged records over the tiles
   int maxTileSt;                    // max stencil entries of a tile's cells
+  // WENO smoothing (RECONST 1, 2): the unsmoothed gradients the gradient
+  // kernels write, in the layout of grad, read by kWenoSmooth
+  R *gradRaw;
   // mixed mode, adjoint of the LSQ gradient: the transposed stencil entry-
   // major (entry k of cell j at k*nc + j): d/|d|^2 with d = x_j - x_i for
   // the cell i whose stencil holds j, and i as int bits (-1 past the end)

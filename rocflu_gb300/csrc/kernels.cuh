@@ -1168,6 +1168,118 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> 
   blockMinDt(V.sc, dt);
 }
 
+// WENO smoothing of the cell gradients and the simple limiter, one thread
+// per cell (CellGradientsMP, libfloflu/CellGradientsMP.F90:184-200):
+// RECONST 2 = RFLU_WENOGradCellsXYZFast_3D (modflu/RFLU_ModWENO.F90:
+// 1366-1572), RECONST 1 = RFLU_WENOGradCells_3D (:298-452), then
+// RFLU_LimitGradCellsSimple (modflu/RFLU_ModLimiters.F90:1147-1300).  The
+// unsmoothed gradients (raw, written by the gradient kernels) of the cell and
+// its stencil members are averaged, the cell first and the members in
+// stencil order, with weights 1/(t^2 + 1e-15): XYZ per component, sum(w g) /
+// sum(w); the simple form one weight per variable from |gx|+|gy|+|gz|,
+// normalised before it is applied.  Then the density and pressure gradients
+// (the positive variables, libflu/RFLU_SetVarInfo.F90:140-144) are zeroed
+// where the cell's value reconstructed at one of its faces,
+// ((q + gx dx) + gy dy) + gz dz with d = fc - cofg, is <= 0; that any face
+// does is independent of the reference's face order.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kWenoSmooth(View<R> V, const R *raw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  const size_t n = V.nc, nb = V.nb;
+  const bool xyz = V.p.reconst == 2;
+  const R eps = R(1.0e-15);
+  auto rawRow = [&](int c, R *t) {
+    if constexpr (Layout<R>::packed) {
+      float r[16];
+      ld8(raw + 16 * (size_t)c, r);
+      ld8(raw + 16 * (size_t)c + 8, r + 8);
+#pragma unroll
+      for (int k = 0; k < 15; ++k) t[k] = r[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) t[k] = raw[k * n + c];
+    }
+  };
+  const int sb = V.stOff[i], se = V.stOff[i + 1];
+  R g[15], own[15];
+  rawRow(i, own);
+  if (xyz) {
+    R sum[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) {
+      sum[k] = R(1) / (own[k] * own[k] + eps);
+      g[k] = sum[k] * own[k];
+    }
+    for (int s = sb; s < se; ++s) {
+      R t[15];
+      rawRow(V.stIdx[s], t);
+#pragma unroll
+      for (int k = 0; k < 15; ++k) {
+        const R w = R(1) / (t[k] * t[k] + eps);
+        sum[k] = sum[k] + w;
+        g[k] = g[k] + w * t[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 15; ++k) g[k] = g[k] / sum[k];
+  } else {
+    R w0[5], sum[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const R t = fabs(own[3 * v]) + fabs(own[3 * v + 1]) + fabs(own[3 * v + 2]);
+      w0[v] = R(1) / (t * t + eps);
+      sum[v] = w0[v];
+    }
+    for (int s = sb; s < se; ++s) {
+      R t[15];
+      rawRow(V.stIdx[s], t);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
+        sum[v] = sum[v] + R(1) / (m * m + eps);
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const R term = w0[v] / sum[v];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) g[3 * v + d] = term * own[3 * v + d];
+    }
+    for (int s = sb; s < se; ++s) {
+      R t[15];
+      rawRow(V.stIdx[s], t);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
+        const R term = (R(1) / (m * m + eps)) / sum[v];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g[3 * v + d] = g[3 * v + d] + term * t[3 * v + d];
+      }
+    }
+  }
+  const PlainLoad<R> ld{V};
+  const R q0 = ld.prim(0, i), q4 = ld.prim(4, i);
+  bool z0 = false, z4 = false;
+  for (int e = V.cfOff[i]; e < V.cfOff[i + 1]; ++e) {
+    const int code = V.cfEnt[e];
+    R d[3];
+    if (code >= 0) {
+      faceOffset(V, code >> 1, code & 1, d);
+    } else {
+      const int b = -code - 1;
+      d[0] = V.bd[b];
+      d[1] = V.bd[nb + b];
+      d[2] = V.bd[2 * nb + b];
+    }
+    if (q0 + g[0] * d[0] + g[1] * d[1] + g[2] * d[2] <= R(0)) z0 = true;
+    if (q4 + g[12] * d[0] + g[13] * d[1] + g[14] * d[2] <= R(0)) z4 = true;
+  }
+  if (z0) g[0] = g[1] = g[2] = R(0);
+  if (z4) g[12] = g[13] = g[14] = R(0);
+  storeGrad(V, i, g);
+}
+
 // The transposed-stencil weights of the mixed adjoint (View::tsW), formed
 // with the expression the gradient kernels use for the same pair of cells.
 template <typename R>
@@ -1734,10 +1846,21 @@ struct Launch {
   static void initFromRef(const View<R> &V, const double *ref, int o0, int o1, cudaStream_t s) {
     if (o1 > o0) kInitFromRef<R><<<blocks(o1 - o0), kBlock, 0, s>>>(V, ref, o0, o1);
   }
+  // WENO smoothing (RECONST 1, 2): the gradient kernels write the
+  // unsmoothed gradients into gradRaw (a copy of the view), kWenoSmooth the
+  // final ones into grad
+  static bool weno(const View<R> &V) { return V.p.reconst == 1 || V.p.reconst == 2; }
+  static View<R> rawView(const View<R> &V) {
+    View<R> W = V;
+    if (weno(V)) W.grad = V.gradRaw;
+    return W;
+  }
   static void gradLimit(const View<R> &V, cudaStream_t s) {
     if (V.p.spaceOrder < 2) return;
-    if (V.tiled) launchTile<false>(V, s);
-    else kGradLimit<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+    const View<R> W = rawView(V);
+    if (V.tiled) launchTile<false>(W, s);
+    else kGradLimit<R><<<blocks(V.nc), kBlock, 0, s>>>(W);
+    if (weno(V)) kWenoSmooth<R><<<blocks(V.nc), kBlock, 0, s>>>(V, V.gradRaw);
   }
   // the tiled kernel specialised for the limiter (RECONST 10, 100, 11; other
   // values: unlimited)
@@ -1811,8 +1934,10 @@ struct Launch {
       gradLimit(V, s);
     } else {
       kStepBegin<R><<<1, 1, 0, s>>>(V);
-      if (V.tiled) launchTile<true>(V, s);
-      else kGradLimitDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+      const View<R> W = rawView(V);
+      if (V.tiled) launchTile<true>(W, s);
+      else kGradLimitDt<R><<<blocks(V.nc), kBlock, 0, s>>>(W);
+      if (weno(V) && V.p.spaceOrder > 1) kWenoSmooth<R><<<blocks(V.nc), kBlock, 0, s>>>(V, V.gradRaw);
       kDtFinalize<R><<<1, 1, 0, s>>>(V);
     }
   }

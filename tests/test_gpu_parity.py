@@ -15,7 +15,8 @@ from rocflu_gb300 import cases, gpu
 pytestmark = pytest.mark.gpu
 
 FLUXES = [(cases.DISCR_ROE, "roe"), (cases.DISCR_HLLC, "hllc"), (cases.DISCR_AUSM, "ausm")]
-LIMITERS = [cases.RECONST_NONE, cases.RECONST_BJ, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP]
+LIMITERS = [cases.RECONST_NONE, cases.RECONST_BJ, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP,
+            cases.RECONST_WENO_SIMPLE, cases.RECONST_WENO_XYZ]
 
 
 def _perturbed(case, seed=3, amp=0.05):
@@ -56,7 +57,7 @@ def test_residual_bit_exact_hex(gpu_lib, discr, name, reconst):
 
 
 @pytest.mark.parametrize("discr,name", FLUXES)
-@pytest.mark.parametrize("reconst", [cases.RECONST_BJ, cases.RECONST_VENKAT])
+@pytest.mark.parametrize("reconst", [cases.RECONST_BJ, cases.RECONST_VENKAT, cases.RECONST_WENO_XYZ])
 def test_residual_bit_exact_tets(gpu_lib, discr, name, reconst):
     num = cases.Numerics(space_order=2, space_discr=discr, reconst=reconst)
     c = cases.adjoint_tets(5, num=num)
@@ -68,6 +69,35 @@ def test_residual_bit_exact_tets(gpu_lib, discr, name, reconst):
     rhs_g, grad_g = r.residual(cv)
     np.testing.assert_array_equal(grad_g, grad_o)
     np.testing.assert_array_equal(rhs_g, rhs_o)
+
+
+@pytest.mark.parametrize("reconst", [cases.RECONST_WENO_SIMPLE, cases.RECONST_WENO_XYZ])
+@pytest.mark.parametrize("prec", ["fp64_exact", "mixed"])
+def test_simple_limiter_zeroes_nonpositive_face_values(gpu_lib, reconst, prec):
+    """RFLU_LimitGradCellsSimple after the WENO smoothing: a pressure
+    p = x - 0.05 (perturbed by 1%) is positive at every cell centre but not at
+    the x = 0 faces, so the first layer's pressure gradients are zeroed; the
+    residual and gradients follow the oracle bit for bit (FP64_EXACT), and
+    the mixed path zeroes the same gradients."""
+    c = _hex_case(cases.DISCR_HLLC, reconst)
+    x = gpu.Setup(c).cofg[:, 0]
+    one = np.ones_like(x)
+    rng = np.random.default_rng(5)
+    p = (x - 0.05) * (1 + 0.01 * rng.standard_normal(x.shape))
+    cv = cases.conserved(1.0 + 0.1 * x, 0.1 * one, 0 * one, 0 * one, p, 1.4)
+    o = Oracle(c)
+    o.set_state(cv)
+    rhs_o, grad_o = o.residual()
+    first = x < 1.0 / 6
+    assert np.all(grad_o[first, 4] == 0.0) and np.all(grad_o[~first, 4, 0] > 0.5)
+    r = gpu.Region(c, prec)
+    rhs_g, grad_g = r.residual(cv)
+    if prec == "fp64_exact":
+        np.testing.assert_array_equal(grad_g, grad_o)
+        np.testing.assert_array_equal(rhs_g, rhs_o)
+    else:
+        np.testing.assert_array_equal(grad_g[:, 4] == 0.0, grad_o[:, 4] == 0.0)
+        assert np.abs(grad_g - grad_o).max() <= 1e-4 * np.abs(grad_o).max()
 
 
 @pytest.mark.parametrize("picl", [0, 1])

@@ -112,6 +112,47 @@ def test_lsq_gradient_exact_for_linear_fields(make):
     assert np.abs(grad - expect[None]).max() < 1e-9
 
 
+@pytest.mark.parametrize("reconst", [cases.RECONST_WENO_SIMPLE, cases.RECONST_WENO_XYZ])
+@pytest.mark.parametrize("make", [lambda: cases.shock_sphere(6), lambda: cases.blast_tets(4)])
+def test_weno_keeps_linear_gradients(make, reconst):
+    """WENO smoothing (RFLU_ModWENO.F90) averages the gradients of a cell and
+    its stencil members with normalised weights; for a linear field all of
+    them are the exact gradient, so the average is too, and the simple
+    limiter leaves the positive density and pressure alone."""
+    c = make()
+    c.num.reconst = reconst
+    o = Oracle(c)
+    _, cofg = o.cells()
+    x, y, z = cofg.T
+    rho = 1.0 + 0.1 * x - 0.2 * y + 0.05 * z
+    u, v, w = 0.3 * x + 0.1, -0.2 * y + 0.05 * z, 0.1 * x + 0.2 * y
+    p = 2.0 + 0.5 * x + 0.25 * y - 0.125 * z
+    o.set_state(cases.conserved(rho, u, v, w, p, 1.4))
+    _, grad = o.residual()
+    expect = np.array([[0.1, -0.2, 0.05], [0.3, 0, 0], [0, -0.2, 0.05], [0.1, 0.2, 0], [0.5, 0.25, -0.125]])
+    assert np.abs(grad - expect[None]).max() < 1e-9
+
+
+@pytest.mark.parametrize("reconst", [cases.RECONST_WENO_SIMPLE, cases.RECONST_WENO_XYZ])
+def test_simple_limiter_zeroes_nonpositive_face_values(reconst):
+    """RFLU_LimitGradCellsSimple (RFLU_ModLimiters.F90:1147-1300): a pressure
+    p = x - 0.05 is positive at every cell centre of the 6^3 box but not at
+    the x = 0 faces, so the first layer's pressure gradient is zeroed; the
+    other layers and the (positive) density keep theirs."""
+    c = cases.shock_sphere(6)
+    c.num.reconst = reconst
+    o = Oracle(c)
+    _, cofg = o.cells()
+    x = cofg[:, 0]
+    one = np.ones_like(x)
+    o.set_state(cases.conserved(1.0 + 0.1 * x, 0 * one, 0 * one, 0 * one, x - 0.05, 1.4))
+    _, grad = o.residual()
+    first = x < 1.0 / 6
+    assert np.all(grad[first, 4] == 0.0)
+    assert np.abs(grad[~first, 4] - np.array([1.0, 0, 0])).max() < 1e-9
+    assert np.abs(grad[:, 0] - np.array([0.1, 0, 0])).max() < 1e-9
+
+
 @pytest.mark.parametrize("discr", [cases.DISCR_ROE, cases.DISCR_HLLC, cases.DISCR_AUSM])
 @pytest.mark.parametrize("order", [1, 2])
 def test_free_stream_preserved(discr, order):
