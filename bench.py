@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--adj-n", type=int, default=32, help="hexes per side of the tet adjoint case")
     p.add_argument("--only-adjoint", action="store_true", help="time the adjoint case only")
     p.add_argument("--skip-unrolled", action="store_true", help="skip the time-unrolled adjoint case")
+    p.add_argument("--skip-weno", action="store_true", help="skip the WENO-XYZ (RECONST 2) variant")
     p.add_argument("--unrolled-n", type=int, default=64, help="hexes per side of the unrolled-adjoint blast")
     p.add_argument("--unrolled-steps", type=int, default=200)
     p.add_argument("--unrolled-every", type=int, default=20, help="checkpoint interval (steps)")
@@ -370,6 +371,7 @@ def run_ours(args):
     if not args.skip_adjoint:
         adjoint = single_adjoint(args, cases, gpu)
     unrolled = None if args.skip_unrolled else unrolled_adjoint(args, cases, gpu)
+    weno = None if args.skip_weno else weno_variant(args, cases, gpu, setup, case.num.dt_imposed)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -393,6 +395,7 @@ def run_ours(args):
             "fp64": fp64,
             "adjoint": adjoint,
             "unrolled_adjoint": unrolled,
+            "weno": weno,
             "e2e": e2e,
             "roofline": roof,
             "stage_roofline": stage_roof,
@@ -446,6 +449,41 @@ def single_adjoint(args, cases, gpu):
             out["mixed"] = res
     areg.close()
     mreg.close()
+    return out
+
+
+def weno_variant(args, cases, gpu, setup, dt_imposed):
+    """The headline workload with the solver's default reconstruction instead
+    of the BJ limiter: WENO-XYZ gradient smoothing + the simple positivity
+    limiter (RECONST 2), HLLC, Wray RK3, mixed and FP64: step rate, the
+    gradient phase (raw gradients + smoothing) per stage, and the mixed
+    path's density error against the FP64 one after the same steps."""
+    import torch
+
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_WENO_XYZ, cfl=0.4)
+    c = cases.shock_sphere(args.n, num=num)
+    c.num.dt_imposed = dt_imposed
+    steps, warm = 10, 3
+    out = {"workload": "shock_sphere_hex%d_hllc_wenoxyz_wray3" % args.n, "steps": steps, "warmup": warm}
+    cvs = {}
+    for prec in ("mixed", "fp64"):
+        reg = gpu.Region(c, prec, grid=setup)
+        stream = torch.cuda.ExternalStream(reg.stream)
+        _, t, _ = reg.step(warm, 0.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, t, rc = reg.step(steps, t)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        kt = reg.kernel_times(5)
+        out[prec] = {"value": reg.n_cells * reg.n_stages * steps / (ms * 1e-3) / 1e6, "unit": UNIT,
+                     "ms_per_step": ms / steps, "gradient_ms": kt[0], "face_flux_ms": kt[1], "update_ms": kt[2],
+                     "rc": rc}
+        cvs[prec] = reg.download()[0]
+        reg.close()
+    out["mixed_vs_fp64_L1_rho"] = float(np.abs(cvs["mixed"][:, 0] - cvs["fp64"][:, 0]).mean())
     return out
 
 

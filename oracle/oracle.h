@@ -9,11 +9,16 @@
  * -ffp-contract=off, matching the reference release flags (no FMA contraction).
  *
  * Parity status: the reference itself cannot be compiled here (no Fortran
- * compiler, no MPI) and its stored goldens exercise periodic/NSCBC patches
- * that are outside this path, so parity is pinned by the reference's own
- * property checks (conservation to 1e-10, frame invariance of the BJ limiter
- * to 1e-7) and known-answer tests, not by golden vectors ("parity unpinned"
- * against golden vectors).
+ * compiler, no MPI).  One of its stored goldens lies on this path: the closed
+ * gas-jump box (its tests/goldens/box/gas-jump/closed-creconst0/np2; HLLC,
+ * second order, WENO-XYZ + the simple limiter, first-order slip walls, Wray
+ * RK3, 569 steps), which this restatement reproduces to 6e-15 of each
+ * field's maximum (the reference harness allows 1e-10).  Its other goldens
+ * need periodic/symmetry patches, constrained gradients or particles, outside
+ * this path; the Barth-Jespersen, Venkatakrishnan, Roe, AUSM+ and
+ * outflow branches are pinned by the reference's property checks
+ * (conservation to 1e-10, frame invariance of the BJ limiter to 1e-7) and
+ * known-answer tests only.
  *
  * Indexing: all arrays use 0-based indices; layouts follow the reference
  * (column-major Fortran):  cv(5,nCells) -> cv[iv + 5*ic],

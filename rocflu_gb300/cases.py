@@ -86,6 +86,35 @@ def _patches(mesh, kinds):
 SLIP = {"bc_type": BC_SLIPWALL}
 
 
+def gas_jump_closed(n=8, length=0.008, x_jump=0.0043, left=(1.2, 0.0, 101325.0), right=(0.97, 82700.0)):
+    """The reference test suite's closed gas-jump box (tests/goldens/box/
+    gas-jump/closed-creconst0; deck tests/templates/rectshktb.inp with its
+    overrides): n^3 hexes on [0, length]^3, the hard-coded rectshktb state
+    (utilities/init/RFLU_InitFlowHardCode.F90:839-910: rho, u, p = left for
+    centroid x < x_jump, rho, p = right at rest beyond), slip walls on all six
+    sides without an ORDER key, hence first order (spaceOrderBFaces,
+    libflu/RFLU_InitInputValues.F90:195); HLLC, second order, WENO-XYZ
+    (RECONST 2), no constrained gradients, Wray RK3, CFL 0.4, TIMESTEP 1e-9,
+    DTMINLIMIT 2e-10, gamma 1.4, cp 1004.64, run to t = 1.05e-4."""
+    mesh = meshgen.hex_box(n, n, n, hi=(length, length, length))
+    num = Numerics(space_order=2, space_discr=DISCR_HLLC, reconst=RECONST_WENO_XYZ, rk_scheme=RK_WRAY3, cfl=0.4,
+                   cp=1004.64, gamma=1.4, dt_imposed=1.0e-9, dt_min_limit=2.0e-10)
+    patches = _patches(mesh, [dict(SLIP, order=1)] * 6)
+    x = meshgen.cell_centers(mesh)[:, 0]
+    inside = x < x_jump
+    d = np.where(inside, left[0], right[0])
+    u = np.where(inside, left[1], 0.0)
+    p = np.where(inside, left[2], right[1])
+    # the state as the hard-coded initialisation forms it: gamma from the gas
+    # constant's round trip (MixtPerf_R_M / MixtPerf_G_CpR) and
+    # d * MixtPerf_Eo_DGPUVW(d, g, p, u, v, w)
+    gc = 8314.3 / (8314.3 / (num.cp - num.cp / num.gamma))
+    g = num.cp / (num.cp - gc)
+    z = np.zeros_like(d)
+    cv0 = np.stack([d, d * u, z, z, d * (p / (d * (g - 1.0)) + 0.5 * (u * u))], axis=1)
+    return Case("gas_jump_closed", mesh["xyz"], mesh["c2v"], patches, num, cv0, end_time=1.05e-4)
+
+
 def sod(nx=400, ny=4, nz=4, num=None):
     """Sod shock tube on [0,1]x[0,0.01]^2 hexes: (1,0,1) for x<0.5 and
     (0.125,0,0.1) beyond, slip walls in y/z, supersonic (extrapolation)

@@ -382,3 +382,29 @@ def test_chunked_transfers_round_trip(gpu_lib, prec):
     g = c.num.gamma
     p = (g - 1.0) * (cv0[:, 4] - 0.5 * (cv0[:, 1:4] ** 2).sum(axis=1) / cv0[:, 0])
     np.testing.assert_allclose(dv1[:, 0], p, rtol=1e-12)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64_exact", 1e-10), ("fp64", 1e-10), ("mixed", 1e-5)])
+def test_gas_jump_closed_box_matches_reference_golden(gpu_lib, prec, tol):
+    """The device through the C ABI against the reference's own result of its
+    closed gas-jump box (tests/golden/gas_jump_closed_creconst0_np2.json:
+    HLLC, second order, WENO-XYZ + simple limiter, first-order slip walls,
+    Wray RK3 from the imposed 1e-9 steps to t = 1.05e-4): the FP64 modes
+    within the reference harness's 1e-10 of each field's maximum
+    (tests/rocpicl_tests/checks.py:18), FP64_EXACT also bit for bit equal to
+    the oracle, the mixed mode within 1e-5."""
+    from golden import gas_jump
+
+    golden, layers, scales = gas_jump.load()
+    c = cases.gas_jump_closed()
+    r = gpu.Region(c, prec)
+    steps, t, rc = r.step(100000, 0.0, c.end_time)
+    assert rc == 0 and abs(t - golden["time"]) <= 1e-9 * golden["time"]
+    cv, _ = r.download()
+    err = np.abs(cv - layers[gas_jump.layer_of_cells(c)]) / scales
+    assert err.max() <= tol, err.max(axis=0)
+    if prec == "fp64_exact":
+        o = Oracle(c)
+        n_o, _ = o.run(100000, 0.0, c.end_time)
+        assert n_o == steps
+        np.testing.assert_array_equal(cv, o.state()[0])

@@ -241,3 +241,23 @@ def test_energy_slot_of_picl_build_on_first_order_outflow():
         out_cells |= set(o.patch(ip)[0].tolist())
     assert diff.any()
     assert set(np.nonzero(diff)[0].tolist()) <= out_cells
+
+
+def test_gas_jump_closed_box_matches_reference_golden():
+    """The oracle against the reference's own result (its test suite's
+    tests/goldens/box/gas-jump/closed-creconst0/np2, extracted by
+    tests/golden/make_gas_jump_closed.py): HLLC, second order, WENO-XYZ with
+    the simple limiter, first-order slip walls, Wray RK3 from the imposed
+    1e-9 steps to t = 1.05e-4 at CFL 0.4.  Every cell within 1e-10 of the
+    field's maximum, the reference harness's tolerance (checks.py:18)."""
+    from golden import gas_jump
+
+    golden, layers, scales = gas_jump.load()
+    c = cases.gas_jump_closed()
+    o = Oracle(c)
+    _, t = o.run(100000, 0.0, c.end_time)
+    assert abs(t - golden["time"]) <= 1e-9 * golden["time"]
+    cv, _ = o.state()
+    ix = gas_jump.layer_of_cells(c)
+    err = np.abs(cv - layers[ix]) / scales
+    assert err.max() <= 1e-10, err.max(axis=0)
