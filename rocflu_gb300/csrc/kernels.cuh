@@ -1204,7 +1204,48 @@ __global__ void __launch_bounds__(kBlock) kWenoSmooth(View<R> V, const R *raw) {
   const int sb = V.stOff[i], se = V.stOff[i + 1];
   R g[15], own[15];
   rawRow(i, own);
-  if (xyz) {
+  if constexpr (Layout<R>::packed) {
+    if (xyz) {
+      // mixed mode: the same sums in packed f32x2 pairs of components; the
+      // weight's reciprocal as one approximate reciprocal (its argument
+      // t^2 + 1e-15 is a normal float, its result at most 1e15)
+      auto rcp = [](float x) {
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        return r;
+      };
+      const float2 e2 = make_float2(1.0e-15f, 1.0e-15f);
+      float2 sum[8], gl[8];
+      auto add = [&](const float *t, bool first) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float2 tq = make_float2(t[2 * q], q < 7 ? t[2 * q + 1] : 0.f);
+          const float2 a = __ffma2_rn(tq, tq, e2);
+          const float2 w = make_float2(rcp(a.x), rcp(a.y));
+          if (first) {
+            sum[q] = w;
+            gl[q] = __fmul2_rn(w, tq);
+          } else {
+            sum[q] = __fadd2_rn(sum[q], w);
+            gl[q] = __ffma2_rn(w, tq, gl[q]);
+          }
+        }
+      };
+      add(own, true);
+      for (int s = sb; s < se; ++s) {
+        float r[16];
+        ld8(raw + 16 * (size_t)V.stIdx[s], r);
+        ld8(raw + 16 * (size_t)V.stIdx[s] + 8, r + 8);
+        add(r, false);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        g[2 * q] = gl[q].x * rcp(sum[q].x);
+        if (q < 7) g[2 * q + 1] = gl[q].y * rcp(sum[q].y);
+      }
+    }
+  }
+  if (xyz && !Layout<R>::packed) {
     R sum[15];
 #pragma unroll
     for (int k = 0; k < 15; ++k) {
@@ -1223,7 +1264,7 @@ __global__ void __launch_bounds__(kBlock) kWenoSmooth(View<R> V, const R *raw) {
     }
 #pragma unroll
     for (int k = 0; k < 15; ++k) g[k] = g[k] / sum[k];
-  } else {
+  } else if (!xyz) {
     R w0[5], sum[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
