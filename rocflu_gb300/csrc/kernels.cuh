@@ -600,6 +600,16 @@ constexpr int kMaxCellFaces = 6;
 // 16-byte loads of neighbouring records do not conflict.
 __device__ inline int recHalf0(int l) { return 8 * l + (l & 4); }
 
+// One approximate reciprocal (rcp.approx.ftz.f32) where the argument is a
+// squared distance between cell centroids: a normal float for any mesh whose
+// cells are wider than ~1e-19 in its length unit, so the flush of denormals
+// never acts and the compiler's general reciprocal sequence is not needed.
+__device__ inline float rcpDist2(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 __device__ inline void ldRec(const float *recs, int l, float *v) {
   const int o = recHalf0(l);
   const float4 a = *reinterpret_cast<const float4 *>(recs + o);
@@ -692,7 +702,7 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
         const float2 d4x = __fadd2_rn(make_float2(b.x, b.y), n4x);
         const float2 dyz = __fadd2_rn(make_float2(b.z, b.w), nyz);
         const float dx = d4x.y, dy = dyz.x, dz = dyz.y;
-        const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
+        const float inv = rcpDist2(dx * dx + dy * dy + dz * dz);
         const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
         const float2 sx2 = make_float2(sx, sx), sy2 = make_float2(sy, sy), sz2 = make_float2(sz, sz);
         gx01 = __ffma2_rn(sx2, d01, gx01);
