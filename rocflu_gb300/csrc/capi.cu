@@ -309,7 +309,7 @@ struct Ctx : CtxBase {
                  const std::vector<double> &fnx, const std::vector<double> &fny, const std::vector<double> &fnz,
                  const std::vector<double> &fnm, const std::vector<double> &dL, const std::vector<double> &dR,
                  const std::vector<double> &bnx, const std::vector<double> &bny, const std::vector<double> &bnz,
-                 const std::vector<double> &bnm);
+                 const std::vector<double> &bnm, const std::vector<double> &bd);
   int checkLaunch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -823,7 +823,8 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
                        const std::vector<double> &fnz, const std::vector<double> &fnm,
                        const std::vector<double> &dL, const std::vector<double> &dR,
                        const std::vector<double> &bnx, const std::vector<double> &bny,
-                       const std::vector<double> &bnz, const std::vector<double> &bnm) {
+                       const std::vector<double> &bnz, const std::vector<double> &bnm,
+                       const std::vector<double> &bd) {
   const int nc = V.nc, nf = V.nf, nb = V.nb;
   const int nTiles = (nc + kTile - 1) / kTile;
   std::vector<int> haloOff(nTiles + 1, 0), haloIdx;
@@ -894,6 +895,9 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
           tag = entLoc[e];
         } else {
           const int b = -code - 1;
+          // the boundary face's offset fc - cofg (the WENO pass's positivity
+          // check reads it; the gradient kernel reads interior entries only)
+          d[0] = (float)bd[b]; d[1] = (float)bd[(size_t)nb + b]; d[2] = (float)bd[2 * (size_t)nb + b];
           nn[0] = (float)bnx[b]; nn[1] = (float)bny[b]; nn[2] = (float)bnz[b]; nn[3] = (float)bnm[b];
           tag = code;
         }
@@ -1127,7 +1131,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     PUT(V.cgx, cgx, R); PUT(V.cgy, cgy, R); PUT(V.cgz, cgz, R);
     PUT(V.lsq, lsq, R); PUT(V.ivol, ivol, R);
     if (num->spaceOrder > 1) {
-      if ((rc = buildTiles(cfOff, cfEnt, stOff, stIdx, fc1, fc2, fnx, fny, fnz, fnm, dL, dR, bnx, bny, bnz, bnm)))
+      if ((rc = buildTiles(cfOff, cfEnt, stOff, stIdx, fc1, fc2, fnx, fny, fnz, fnm, dL, dR, bnx, bny, bnz, bnm, bd)))
         return rc;
       // the adjoint's transposed-stencil weights (filled by ops->configure)
       int w = 0;

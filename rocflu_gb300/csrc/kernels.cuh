@@ -1192,143 +1192,238 @@ __global__ void __launch_bounds__(kBlock, MinBlocks<R>::v) kGradLimitDt(View<R> 
 // where the cell's value reconstructed at one of its faces,
 // ((q + gx dx) + gy dy) + gz dz with d = fc - cofg, is <= 0; that any face
 // does is independent of the reference's face order.
-template <typename R>
-__global__ void __launch_bounds__(kBlock) kWenoSmooth(View<R> V, const R *raw) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= V.nc) return;
-  const size_t n = V.nc, nb = V.nb;
-  const bool xyz = V.p.reconst == 2;
-  const R eps = R(1.0e-15);
-  auto rawRow = [&](int c, R *t) {
-    if constexpr (Layout<R>::packed) {
-      float r[16];
-      ld8(raw + 16 * (size_t)c, r);
-      ld8(raw + 16 * (size_t)c + 8, r + 8);
+// The WENO averages of one cell from its own unsmoothed gradient and its
+// stencil members' (fetch(s, t) fills member s's 15 components into t).
+// Mixed mode, XYZ: packed f32x2 pairs of components, one approximate
+// reciprocal per weight (its argument t^2 + 1e-15 is a normal float, its
+// result at most 1e15).
+template <typename Fetch>
+__device__ inline void wenoXyzPacked(const float *own, int sb, int se, Fetch fetch, float *g) {
+  auto rcp = [](float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  };
+  const float2 e2 = make_float2(1.0e-15f, 1.0e-15f);
+  float2 sum[8], gl[8];
+  auto add = [&](const float *t, bool first) {
 #pragma unroll
-      for (int k = 0; k < 15; ++k) t[k] = r[k];
-    } else {
-#pragma unroll
-      for (int k = 0; k < 15; ++k) t[k] = raw[k * n + c];
+    for (int q = 0; q < 8; ++q) {
+      const float2 tq = make_float2(t[2 * q], q < 7 ? t[2 * q + 1] : 0.f);
+      const float2 a = __ffma2_rn(tq, tq, e2);
+      const float2 w = make_float2(rcp(a.x), rcp(a.y));
+      if (first) {
+        sum[q] = w;
+        gl[q] = __fmul2_rn(w, tq);
+      } else {
+        sum[q] = __fadd2_rn(sum[q], w);
+        gl[q] = __ffma2_rn(w, tq, gl[q]);
+      }
     }
   };
-  const int sb = V.stOff[i], se = V.stOff[i + 1];
-  R g[15], own[15];
-  rawRow(i, own);
-  if constexpr (Layout<R>::packed) {
-    if (xyz) {
-      // mixed mode: the same sums in packed f32x2 pairs of components; the
-      // weight's reciprocal as one approximate reciprocal (its argument
-      // t^2 + 1e-15 is a normal float, its result at most 1e15)
-      auto rcp = [](float x) {
-        float r;
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-        return r;
-      };
-      const float2 e2 = make_float2(1.0e-15f, 1.0e-15f);
-      float2 sum[8], gl[8];
-      auto add = [&](const float *t, bool first) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float2 tq = make_float2(t[2 * q], q < 7 ? t[2 * q + 1] : 0.f);
-          const float2 a = __ffma2_rn(tq, tq, e2);
-          const float2 w = make_float2(rcp(a.x), rcp(a.y));
-          if (first) {
-            sum[q] = w;
-            gl[q] = __fmul2_rn(w, tq);
-          } else {
-            sum[q] = __fadd2_rn(sum[q], w);
-            gl[q] = __ffma2_rn(w, tq, gl[q]);
-          }
-        }
-      };
-      add(own, true);
-      for (int s = sb; s < se; ++s) {
-        float r[16];
-        ld8(raw + 16 * (size_t)V.stIdx[s], r);
-        ld8(raw + 16 * (size_t)V.stIdx[s] + 8, r + 8);
-        add(r, false);
-      }
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        g[2 * q] = gl[q].x * rcp(sum[q].x);
-        if (q < 7) g[2 * q + 1] = gl[q].y * rcp(sum[q].y);
-      }
-    }
+  add(own, true);
+  for (int s = sb; s < se; ++s) {
+    float r[16];
+    fetch(s, r);
+    add(r, false);
   }
-  if (xyz && !Layout<R>::packed) {
-    R sum[15];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    g[2 * q] = gl[q].x * rcp(sum[q].x);
+    if (q < 7) g[2 * q + 1] = gl[q].y * rcp(sum[q].y);
+  }
+}
+// Every mode, XYZ in the reference's operation order.
+template <typename R, typename Fetch>
+__device__ inline void wenoXyz(const R *own, int sb, int se, Fetch fetch, R *g) {
+  const R eps = R(1.0e-15);
+  R sum[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) {
+    sum[k] = R(1) / (own[k] * own[k] + eps);
+    g[k] = sum[k] * own[k];
+  }
+  for (int s = sb; s < se; ++s) {
+    R t[16];
+    fetch(s, t);
 #pragma unroll
     for (int k = 0; k < 15; ++k) {
-      sum[k] = R(1) / (own[k] * own[k] + eps);
-      g[k] = sum[k] * own[k];
-    }
-    for (int s = sb; s < se; ++s) {
-      R t[15];
-      rawRow(V.stIdx[s], t);
-#pragma unroll
-      for (int k = 0; k < 15; ++k) {
-        const R w = R(1) / (t[k] * t[k] + eps);
-        sum[k] = sum[k] + w;
-        g[k] = g[k] + w * t[k];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 15; ++k) g[k] = g[k] / sum[k];
-  } else if (!xyz) {
-    R w0[5], sum[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      const R t = fabs(own[3 * v]) + fabs(own[3 * v + 1]) + fabs(own[3 * v + 2]);
-      w0[v] = R(1) / (t * t + eps);
-      sum[v] = w0[v];
-    }
-    for (int s = sb; s < se; ++s) {
-      R t[15];
-      rawRow(V.stIdx[s], t);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
-        sum[v] = sum[v] + R(1) / (m * m + eps);
-      }
-    }
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      const R term = w0[v] / sum[v];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) g[3 * v + d] = term * own[3 * v + d];
-    }
-    for (int s = sb; s < se; ++s) {
-      R t[15];
-      rawRow(V.stIdx[s], t);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
-        const R term = (R(1) / (m * m + eps)) / sum[v];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) g[3 * v + d] = g[3 * v + d] + term * t[3 * v + d];
-      }
+      const R w = R(1) / (t[k] * t[k] + eps);
+      sum[k] = sum[k] + w;
+      g[k] = g[k] + w * t[k];
     }
   }
-  const PlainLoad<R> ld{V};
-  const R q0 = ld.prim(0, i), q4 = ld.prim(4, i);
-  bool z0 = false, z4 = false;
-  for (int e = V.cfOff[i]; e < V.cfOff[i + 1]; ++e) {
-    const int code = V.cfEnt[e];
-    R d[3];
-    if (code >= 0) {
-      faceOffset(V, code >> 1, code & 1, d);
-    } else {
-      const int b = -code - 1;
-      d[0] = V.bd[b];
-      d[1] = V.bd[nb + b];
-      d[2] = V.bd[2 * nb + b];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) g[k] = g[k] / sum[k];
+}
+// Every mode, the simple form (one weight per variable from |gx|+|gy|+|gz|,
+// normalised before it is applied) in the reference's operation order.
+template <typename R, typename Fetch>
+__device__ inline void wenoSimple(const R *own, int sb, int se, Fetch fetch, R *g) {
+  const R eps = R(1.0e-15);
+  R w0[5], sum[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const R t = fabs(own[3 * v]) + fabs(own[3 * v + 1]) + fabs(own[3 * v + 2]);
+    w0[v] = R(1) / (t * t + eps);
+    sum[v] = w0[v];
+  }
+  for (int s = sb; s < se; ++s) {
+    R t[16];
+    fetch(s, t);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
+      sum[v] = sum[v] + R(1) / (m * m + eps);
     }
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const R term = w0[v] / sum[v];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[3 * v + d] = term * own[3 * v + d];
+  }
+  for (int s = sb; s < se; ++s) {
+    R t[16];
+    fetch(s, t);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
+      const R term = (R(1) / (m * m + eps)) / sum[v];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) g[3 * v + d] = g[3 * v + d] + term * t[3 * v + d];
+    }
+  }
+}
+// RFLU_LimitGradCellsSimple on one cell: face(k, d) gives the cell's k-th
+// face offset d = fc - cofg and returns false past its last face.
+template <typename R, typename Face>
+__device__ inline void simplePositivity(R q0, R q4, int nFaces, Face face, R *g) {
+  bool z0 = false, z4 = false;
+  for (int k = 0; k < nFaces; ++k) {
+    R d[3];
+    if (!face(k, d)) continue;
     if (q0 + g[0] * d[0] + g[1] * d[1] + g[2] * d[2] <= R(0)) z0 = true;
     if (q4 + g[12] * d[0] + g[13] * d[1] + g[14] * d[2] <= R(0)) z4 = true;
   }
   if (z0) g[0] = g[1] = g[2] = R(0);
   if (z4) g[12] = g[13] = g[14] = R(0);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kWenoSmooth(View<R> V, const R *raw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  const size_t n = V.nc, nb = V.nb;
+  auto rawRow = [&](int c, R *t) {
+    if constexpr (Layout<R>::packed) {
+      ld8(raw + 16 * (size_t)c, t);
+      ld8(raw + 16 * (size_t)c + 8, t + 8);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) t[k] = raw[k * n + c];
+    }
+  };
+  auto fetch = [&](int s, R *t) { rawRow(V.stIdx[s], t); };
+  const int sb = V.stOff[i], se = V.stOff[i + 1];
+  R g[15], own[16];
+  rawRow(i, own);
+  if (V.p.reconst == 2) {
+    if constexpr (Layout<R>::packed) wenoXyzPacked(own, sb, se, fetch, g);
+    else wenoXyz(own, sb, se, fetch, g);
+  } else {
+    wenoSimple(own, sb, se, fetch, g);
+  }
+  const PlainLoad<R> ld{V};
+  const int cb = V.cfOff[i];
+  simplePositivity(ld.prim(0, i), ld.prim(4, i), V.cfOff[i + 1] - cb,
+                   [&](int k, R *d) {
+                     const int code = V.cfEnt[cb + k];
+                     if (code >= 0) {
+                       faceOffset(V, code >> 1, code & 1, d);
+                     } else {
+                       const int b = -code - 1;
+                       d[0] = V.bd[b];
+                       d[1] = V.bd[nb + b];
+                       d[2] = V.bd[2 * nb + b];
+                     }
+                     return true;
+                   },
+                   g);
   storeGrad(V, i, g);
+}
+
+// Tiled WENO smoothing for the mixed mode: one tile of kTile Morton cells per
+// CTA.  The unsmoothed 64-byte gradient records of the tile's cells and of
+// its halo, its stencil ids and its stencil offsets are staged in shared
+// memory (the gradient kernel's tiles and 16-bit local ids), so the members'
+// records are read from shared memory instead of gathered through L2; the
+// positivity check reads the entry-major face offsets feD.  The four 16-byte
+// quarters of record l are stored rotated by (l >> 1) & 3, so that the same
+// quarter of eight consecutive records lies in eight different bank groups.
+__device__ inline int wenoQuad(int l, int q) { return 16 * l + 4 * (q ^ ((l >> 1) & 3)); }
+
+template <typename R>
+inline size_t wenoTileSmemBytes(const View<R> &V) {
+  return sizeof(float) * (16 * (size_t)V.maxRecs + 4 * tileIdWords(V) + kTileOffInts);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kWenoTile(View<R> V, const R *raw) {
+  if constexpr (Layout<R>::packed) {
+    extern __shared__ float4 wenoSmem[];
+    float *recs = reinterpret_cast<float *>(wenoSmem);
+    uint4 *ids = reinterpret_cast<uint4 *>(recs + 16 * (size_t)V.maxRecs);
+    int *offs = reinterpret_cast<int *>(ids + tileIdWords(V));
+    const size_t n = V.nc;
+    const int t = blockIdx.x, base = t * kTile, nIn = min(kTile, V.nc - base);
+    const int hb = V.haloOff[t], nh = V.haloOff[t + 1] - hb;
+    const int w0 = V.stOff[base] >> 3, w1 = (V.stOff[base + nIn] + 7) >> 3;
+    const uint4 *src4 = reinterpret_cast<const uint4 *>(V.stLoc);
+    for (int w = w0 + (int)threadIdx.x; w < w1; w += kBlock) cpAsync16(ids + (w - w0), src4 + w);
+    for (int r = threadIdx.x; r <= nIn; r += kBlock) cpAsync4(offs + r, V.stOff + base + r);
+    for (int x = threadIdx.x; x < 4 * (nIn + nh); x += kBlock) {
+      const int r = x >> 2, q = x & 3;
+      const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
+      const int dst = r < nIn ? r : kTile + (r - nIn);
+      cpAsync16(recs + wenoQuad(dst, q), raw + 16 * (size_t)src + 4 * q);
+    }
+    cpAsyncCommit();
+    cpAsyncWait<0>();
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    if (i >= V.nc) return;
+    const unsigned short *st = reinterpret_cast<const unsigned short *>(ids);
+    const int s0 = 8 * (offs[0] >> 3);
+    const int sb = offs[threadIdx.x] - s0, se = offs[threadIdx.x + 1] - s0;
+    auto rec = [&](int l, float *v) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 a = *reinterpret_cast<const float4 *>(recs + wenoQuad(l, q));
+        v[4 * q] = a.x;
+        v[4 * q + 1] = a.y;
+        v[4 * q + 2] = a.z;
+        v[4 * q + 3] = a.w;
+      }
+    };
+    auto fetch = [&](int s, float *v) { rec(st[s], v); };
+    float own[16], g[15];
+    rec(threadIdx.x, own);
+    if (V.p.reconst == 2) wenoXyzPacked(own, sb, se, fetch, g);
+    else wenoSimple(own, sb, se, fetch, g);
+    float pr[8];
+    ld8(V.prim + 8 * (size_t)i, pr);
+    simplePositivity(pr[0], pr[4], V.cfW,
+                     [&](int k, float *d) {
+                       const float4 D = ld4(V.feD + 4 * (k * n + i));
+                       d[0] = D.x;
+                       d[1] = D.y;
+                       d[2] = D.z;
+                       return __float_as_int(D.w) != INT_MIN;
+                     },
+                     g);
+    storeGrad(V, i, g);
+  }
 }
 
 // The transposed-stencil weights of the mixed adjoint (View::tsW), formed
@@ -1911,7 +2006,13 @@ struct Launch {
     const View<R> W = rawView(V);
     if (V.tiled) launchTile<false>(W, s);
     else kGradLimit<R><<<blocks(V.nc), kBlock, 0, s>>>(W);
-    if (weno(V)) kWenoSmooth<R><<<blocks(V.nc), kBlock, 0, s>>>(V, V.gradRaw);
+    if (weno(V)) smooth(V, s);
+  }
+  static void smooth(const View<R> &V, cudaStream_t s) {
+    if (Layout<R>::packed && V.tiled)
+      kWenoTile<R><<<(V.nc + kTile - 1) / kTile, kBlock, wenoTileSmemBytes(V), s>>>(V, V.gradRaw);
+    else
+      kWenoSmooth<R><<<blocks(V.nc), kBlock, 0, s>>>(V, V.gradRaw);
   }
   // the tiled kernel specialised for the limiter (RECONST 10, 100, 11; other
   // values: unlimited)
@@ -1959,6 +2060,8 @@ struct Launch {
       setTileSmem<true, 0>(V); setTileSmem<true, 10>(V); setTileSmem<true, 100>(V); setTileSmem<true, 11>(V);
     }
     if (V.tsW) kTsWeights<R><<<blocks(V.nc), kBlock>>>(V);
+    if (Layout<R>::packed && V.tiled && V.gradRaw)
+      cudaFuncSetAttribute(kWenoTile<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wenoTileSmemBytes(V));
   }
   static void faceFlux(const View<R> &V, cudaStream_t s) {
     kFaceFlux<R><<<blocks((long long)V.nf + V.nb), kBlock, 0, s>>>(V);
@@ -1988,7 +2091,7 @@ struct Launch {
       const View<R> W = rawView(V);
       if (V.tiled) launchTile<true>(W, s);
       else kGradLimitDt<R><<<blocks(V.nc), kBlock, 0, s>>>(W);
-      if (weno(V) && V.p.spaceOrder > 1) kWenoSmooth<R><<<blocks(V.nc), kBlock, 0, s>>>(V, V.gradRaw);
+      if (weno(V) && V.p.spaceOrder > 1) smooth(V, s);
       kDtFinalize<R><<<1, 1, 0, s>>>(V);
     }
   }
