@@ -265,7 +265,8 @@ struct Ctx : CtxBase {
   const Ops<R> *ops = nullptr;
   std::vector<void *> allocs;
   double *staging = nullptr;     // (15, nc) doubles: transfers in reference order
-  double *work = nullptr;        // adjoint workspace
+  double *work = nullptr;        // adjoint workspace (allocated by the first adjoint call)
+  int tsWidthLazy = 0;           // ... and the width of its transposed-stencil weights
   size_t workBytes = 0;
   double *cvSave = nullptr;
   cudaGraphExec_t stepGraph = nullptr, fixedGraph = nullptr;
@@ -501,8 +502,24 @@ struct Ctx : CtxBase {
     if (rc) return rc;
     return syncEvents(false);
   }
+  // The adjoint's device memory (workspace; mixed mode: the transposed-
+  // stencil weights) is allocated on the first adjoint call, so that a
+  // context that only steps does not hold it.
+  int ensureAdjoint() {
+    if (work) return RFLU_OK;
+    int rc = alloc((char **)&work, workBytes);
+    if (rc) return rc;
+    if (tsWidthLazy > 0) {
+      if ((rc = alloc(&V.tsW, 4 * (size_t)tsWidthLazy * V.nc))) return rc;
+      V.tsWidth = tsWidthLazy;
+      ops->adjointSetup(V, stream);
+    }
+    return checkLaunch("adjoint set-up");
+  }
   int adjointPrep(const double *cv) {
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "no adjoint kernels in this precision mode");
+    int rc = ensureAdjoint();
+    if (rc) return rc;
     RFLU_CUDA(cudaMemcpyAsync(cvSave, V.cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToDevice, stream));
     return setState(cv);
   }
@@ -653,6 +670,7 @@ struct Ctx : CtxBase {
     if (V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: RECONST 10, 1 and 2 have no adjoint");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
+    if (int rc0 = ensureAdjoint()) return rc0;
     const int nrk = V.p.nrkSteps;
     double W[6][6] = {};
     for (int t = 1; t <= nrk; ++t) W[t][t] = 1.0;
@@ -782,6 +800,7 @@ struct Ctx : CtxBase {
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
     if (!ops->vjp || V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
+    if (int rc0 = ensureAdjoint()) return rc0;
     const size_t nc = V.nc;
     RFLU_CUDA(cudaMemsetAsync(staging, 0, sizeof(double) * 5 * nc, stream));
     cudaEvent_t ev[3];
@@ -1133,11 +1152,11 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     if (num->spaceOrder > 1) {
       if ((rc = buildTiles(cfOff, cfEnt, stOff, stIdx, fc1, fc2, fnx, fny, fnz, fnm, dL, dR, bnx, bny, bnz, bnm, bd)))
         return rc;
-      // the adjoint's transposed-stencil weights (filled by ops->configure)
+      // the width of the adjoint's transposed-stencil weights, allocated and
+      // filled with the adjoint workspace on the first adjoint call
       int w = 0;
       for (int j = 0; j < nc; ++j) w = std::max(w, tsOff[j + 1] - tsOff[j]);
-      V.tsWidth = w;
-      if (w > 0 && (rc = alloc(&V.tsW, 4 * (size_t)w * nc))) return rc;
+      tsWidthLazy = w;
     }
   } else {
     PUT(V.wx, wx, R); PUT(V.wy, wy, R); PUT(V.wz, wz, R);
@@ -1198,7 +1217,6 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   // adjoint workspace (adjoint.cuh: carveAdjWork): gradients, limiter
   // factors and branches, face adjoints of one residual, in the mode's type
   workBytes = sizeof(R) * (size_t)(120 * (size_t)nc + 24 * ((size_t)nf + nb) + 64) + sizeof(int) * 10 * (size_t)nc + 256;
-  if ((rc = alloc((char **)&work, workBytes))) return rc;
   ops->configure(V);
   RFLU_CUDA(cudaDeviceSynchronize());
   V.tileGrid = ops->tileGrid(V, 0);

@@ -2054,12 +2054,14 @@ struct Launch {
   }
   // Kernel attributes that depend on the mesh (shared memory of the tiled
   // kernels); called once at set-up, outside any stream capture.
+  static void adjointSetup(const View<R> &V, cudaStream_t s) {
+    if (V.tsW) kTsWeights<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+  }
   static void configure(const View<R> &V) {
     if (V.tiled) {
       setTileSmem<false, 0>(V); setTileSmem<false, 10>(V); setTileSmem<false, 100>(V); setTileSmem<false, 11>(V);
       setTileSmem<true, 0>(V); setTileSmem<true, 10>(V); setTileSmem<true, 100>(V); setTileSmem<true, 11>(V);
     }
-    if (V.tsW) kTsWeights<R><<<blocks(V.nc), kBlock>>>(V);
     if (Layout<R>::packed && V.tiled && V.gradRaw)
       cudaFuncSetAttribute(kWenoTile<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wenoTileSmemBytes(V));
   }

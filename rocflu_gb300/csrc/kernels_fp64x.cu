@@ -9,7 +9,7 @@ const Ops<double> *opsFp64Exact() {
   using L = fp64x::Launch<double>;
   static const Ops<double> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, fp64x::AdjointOps<double>::jvp, fp64x::AdjointOps<double>::vjp,
-                                 fp64x::AdjointOps<double>::patchPressure};
+                                 fp64x::AdjointOps<double>::patchPressure, L::adjointSetup};
   return &ops;
 }
 }  // namespace rflu

@@ -9,7 +9,7 @@ const Ops<float> *opsMixed() {
   using L = mixed::Launch<float>;
   static const Ops<float> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, mixed::AdjointOps<float>::jvp, mixed::AdjointOps<float>::vjp,
-                                 mixed::AdjointOps<float>::patchPressure};
+                                 mixed::AdjointOps<float>::patchPressure, L::adjointSetup};
   return &ops;
 }
 }  // namespace rflu

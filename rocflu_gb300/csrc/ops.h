@@ -26,6 +26,8 @@ struct Ops {
   void (*jvp)(const View<R> &, const double *cvDot, double *rhsDot, double *work, cudaStream_t);
   void (*vjp)(const View<R> &, const double *rhsBar, double *cvBar, double *work, cudaStream_t);
   void (*patchPressure)(const View<R> &, int iPatch, double *J, double *cvBar, double *work, cudaStream_t);
+  // fills the adjoint's mesh-dependent arrays (View::tsW) once they exist
+  void (*adjointSetup)(const View<R> &, cudaStream_t);
 };
 
 const Ops<double> *opsFp64();
