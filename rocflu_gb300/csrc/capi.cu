@@ -849,7 +849,7 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
   std::vector<int> haloOff(nTiles + 1, 0), haloIdx;
   std::vector<unsigned short> stLoc(stIdx.size());
   std::vector<int> entLoc(cfEnt.size(), -1);
-  std::vector<int> mark(nc, -1);
+  std::vector<int> mark(nc, -1), slot(nc, -1);
   int maxRecs = 0, cfW = 0;
   for (int i = 0; i < nc; ++i) cfW = std::max(cfW, cfOff[i + 1] - cfOff[i]);
   auto other = [&](int e) {  // neighbour of a cell's interior face entry
@@ -871,19 +871,31 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
         if (cfEnt[e] >= 0) visit(other(e));
     }
     std::sort(halo.begin(), halo.end());
-    const int recs = kTile + (int)halo.size();
+    // A halo cell j takes slot 8 r + (j & 7), r counting the halo cells of
+    // its residue, so every staged record's local id keeps the low three bits
+    // of its cell id (own cells too: tiles start at multiples of 8).  On a
+    // Morton-ordered structured mesh the k-th stencil members (and k-th face
+    // neighbours) of 8 consecutive cells then differ in those bits, and with
+    // the record swizzle their 16-byte loads hit 8 different bank groups.
+    // Unused slots hold -1 and are not staged.
+    int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j : halo) slot[j] = 8 * cnt[j & 7]++ + (j & 7);
+    const int rows = *std::max_element(cnt, cnt + 8);
+    const int recs = kTile + 8 * rows;
     if (recs > 65535) return RFLU_OK;  // stays untiled
     maxRecs = std::max(maxRecs, recs);
     auto local = [&](int j) {
       if (j >= b0 && j < b1) return j - b0;
-      return kTile + (int)(std::lower_bound(halo.begin(), halo.end(), j) - halo.begin());
+      return kTile + slot[j];
     };
     for (int i = b0; i < b1; ++i) {
       for (int s = stOff[i]; s < stOff[i + 1]; ++s) stLoc[s] = (unsigned short)local(stIdx[s]);
       for (int e = cfOff[i]; e < cfOff[i + 1]; ++e)
         if (cfEnt[e] >= 0) entLoc[e] = local(other(e));
     }
-    haloIdx.insert(haloIdx.end(), halo.begin(), halo.end());
+    const size_t h0 = haloIdx.size();
+    haloIdx.resize(h0 + 8 * (size_t)rows, -1);
+    for (int j : halo) haloIdx[h0 + slot[j]] = j;
     haloOff[t + 1] = (int)haloIdx.size();
   }
   int maxTileSt = 0;

@@ -117,7 +117,7 @@ struct View {
   int tileGrid;                     // CTAs of the persistent tiled kernels
   int tileGridDt;                   // ... of the variant with the time-step sum
   int cfW;                          // max faces per cell (entries of feD/feN)
-  const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids
+  const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids by slot (-1: unused)
   const unsigned short *stLoc;      // local id of each stencil member (stIdx order),
                                     // 16-byte aligned and padded by 8 ids
   // per cell-face entry, entry-major (entry k of cell i at [k*nc + i]), in

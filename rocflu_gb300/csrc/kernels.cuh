@@ -1062,6 +1062,7 @@ __device__ inline void stageTile(const View<R> &V, int t, float *buf) {
   for (int r = threadIdx.x; r <= nIn; r += kBlock) cpAsync4(offs + r, V.stOff + base + r);
   for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
     const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
+    if (src < 0) continue;  // an unused halo slot
     const int dst = r < nIn ? r : kTile + (r - nIn);
     const float *g = V.prim + 8 * (size_t)src;
     const int o = recHalf0(dst);
@@ -1385,6 +1386,7 @@ __global__ void __launch_bounds__(kBlock) kWenoTile(View<R> V, const R *raw) {
     for (int x = threadIdx.x; x < 4 * (nIn + nh); x += kBlock) {
       const int r = x >> 2, q = x & 3;
       const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
+      if (src < 0) continue;  // an unused halo slot
       const int dst = r < nIn ? r : kTile + (r - nIn);
       cpAsync16(recs + wenoQuad(dst, q), raw + 16 * (size_t)src + 4 * q);
     }
