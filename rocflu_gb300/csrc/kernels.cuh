@@ -692,7 +692,7 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
       const float2 n4x = make_float2(-rec[4], -rec[5]), nyz = make_float2(-rec[6], -rec[7]);
       float2 gx01 = make_float2(0.f, 0.f), gx23 = gx01, gy01 = gx01, gy23 = gx01, gz01 = gx01, gz23 = gx01;
       float gx4 = 0.f, gy4 = 0.f, gz4 = 0.f;
-#pragma unroll 2
+#pragma unroll 4
       for (int s = sb; s < se; ++s) {
         const int o = recHalf0(stSm[s]);
         const float4 a = *reinterpret_cast<const float4 *>(recs + o);
@@ -738,6 +738,13 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
       }
     }
   }
+  if (kTiled) {
+#pragma unroll
+    for (int k = 0; k < kMaxCellFaces; ++k) {
+      if (lim && k < V.cfW) De[k] = ld4(V.feD + 4 * (k * n + i));
+      else De[k] = make_float4(0.f, 0.f, 0.f, __int_as_float(INT_MIN));
+    }
+  }
   if (second) {
     if (!kTiled) {
 #pragma unroll
@@ -779,13 +786,6 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
     for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int c = 0; c < 3; ++c) B[3 * j + c] = A[3 * j] * G[3 * c] + A[3 * j + 1] * G[1 + 3 * c] + A[3 * j + 2] * G[2 + 3 * c];
-  }
-  if (kTiled) {
-#pragma unroll
-    for (int k = 0; k < kMaxCellFaces; ++k) {
-      if (lim && k < V.cfW) De[k] = ld4(V.feD + 4 * (k * n + i));
-      else De[k] = make_float4(0.f, 0.f, 0.f, __int_as_float(INT_MIN));
-    }
   }
   // Barth-Jespersen in one pass: min over faces of dmax/d2 (d2 > 0) is
   // dmax / (largest positive d2), and likewise dmin / (most negative d2), so
