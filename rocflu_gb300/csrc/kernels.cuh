@@ -14,6 +14,7 @@
 #pragma once
 #include <algorithm>
 #include <climits>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "convert.cuh"
@@ -435,6 +436,16 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       }
     }
     S epsq = (rc == 11) ? S(V.epsq[i]) : S(0);
+    // Barth-Jespersen on plain floating-point types: the minimum over faces
+    // of dmax/d2 (d2 > 0) is dmax over the largest d2, because correctly
+    // rounded division is monotone and dmax >= 0, and likewise dmin over the
+    // most negative d2: one division per variable and sign instead of one
+    // per face, with the same values (signed zeros aside).  The tangent
+    // types keep the per-face form, whose ties pick the first face.
+    constexpr bool kOnePass = std::is_floating_point<S>::value;
+    S pmx[5], nmn[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { pmx[k] = S(0); nmn[k] = S(0); }
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
       if (code < 0) continue;
@@ -448,7 +459,10 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         // d2 = grad . (cofg - fc), the reference's sign
         S d2 = -(g[3 * k] * dx + g[3 * k + 1] * dy + g[3 * k + 2] * dz);
         S dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
-        if (rc == 11) {
+        if (kOnePass && rc != 11) {
+          if (d2 > S(0)) pmx[k] = fmax2(pmx[k], d2);
+          else if (d2 < S(0)) nmn[k] = fmin2(nmn[k], d2);
+        } else if (rc == 11) {
           const S tiny = S(1.0e-12);
           if (d2 > S(0)) {
             S numer = (dmax * dmax + epsq) * d2 + S(2) * d2 * d2 * dmax;
@@ -465,6 +479,15 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         }
       }
     }
+    if (kOnePass && rc != 11) {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        if (rc == 10 && k >= 1 && k <= 3) continue;
+        const S dmax = vmax[k] - q[k], dmin = vmin[k] - q[k];
+        if (pmx[k] > S(0)) lim[k] = fmin2(fmin2(S(1), dmax / pmx[k]), lim[k]);
+        if (nmn[k] < S(0)) lim[k] = fmin2(fmin2(S(1), dmin / nmn[k]), lim[k]);
+      }
+    }
     if (rc == 10) {
       // frame-invariant velocity limiting along the strain-rate eigenvectors
       S G[9], Sy[9], A[9], ev[3];
@@ -478,6 +501,7 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         for (int b = 0; b < 3; ++b) Sy[a + 3 * b] = S(0.5) * (G[a + 3 * b] + G[b + 3 * a]);
       symmetricEigen3(Sy, A, ev);
       S dmn[3] = {S(0), S(0), S(0)}, dmx[3] = {S(0), S(0), S(0)}, al[3] = {S(1), S(1), S(1)};
+      S spx[3] = {S(0), S(0), S(0)}, snx[3] = {S(0), S(0), S(0)};  // extreme projections (one pass)
       for (int e = cb; e < ce; ++e) {
         const int code = V.cfEnt[e];
         if (code < 0) continue;
@@ -522,8 +546,20 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
           pr = pr + A[3 * j] * sh[0];
           pr = pr + A[3 * j + 1] * sh[1];
           pr = pr + A[3 * j + 2] * sh[2];
-          if (pr > S(0)) al[j] = fmin2(al[j], dmx[j] / pr);
-          else if (pr < S(0)) al[j] = fmin2(al[j], dmn[j] / pr);
+          if (kOnePass) {
+            if (pr > S(0)) spx[j] = fmax2(spx[j], pr);
+            else if (pr < S(0)) snx[j] = fmin2(snx[j], pr);
+          } else {
+            if (pr > S(0)) al[j] = fmin2(al[j], dmx[j] / pr);
+            else if (pr < S(0)) al[j] = fmin2(al[j], dmn[j] / pr);
+          }
+        }
+      }
+      if (kOnePass) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (spx[j] > S(0)) al[j] = fmin2(al[j], dmx[j] / spx[j]);
+          if (snx[j] < S(0)) al[j] = fmin2(al[j], dmn[j] / snx[j]);
         }
       }
       S mx = fabs_(ev[0]);
