@@ -182,11 +182,13 @@ def test_timestep_bit_exact(gpu_lib):
         assert r.timestep(t) == o.timestep(t)
 
 
-def test_sod_full_run_bit_exact(gpu_lib):
-    """Sod tube to t = 0.2 (first-order Roe, Wray RK3, CFL 0.5): every time
-    step and stage on the device; final state identical to the oracle."""
-    c = cases.sod(100, 2, 2)
-    c.num.dt_imposed = c.num.cfl * 0.01 / (6.0 * np.sqrt(1.4))
+@pytest.mark.parametrize("nx,nyz", [(100, 2), (400, 4)])
+def test_sod_full_run_bit_exact(gpu_lib, nx, nyz):
+    """Sod tube to t = 0.2 (first-order Roe, Wray RK3, CFL 0.5), also at the
+    full 400 x 4 x 4 size: every time step and stage on the device; final
+    state identical to the oracle."""
+    c = cases.sod(nx, nyz, nyz)
+    c.num.dt_imposed = c.num.cfl * (1.0 / nx) / (6.0 * np.sqrt(1.4))
     o = Oracle(c)
     n_o, t_o = o.run(100000, 0.0, 0.2)
     r = gpu.Region(c, "fp64_exact")
