@@ -654,6 +654,42 @@ __device__ inline void ldRec(const float *recs, int l, float *v) {
   v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
 
+// Spectral-radius sum of RFLU_TimeStepInviscid (rocflu/
+// RFLU_TimeStepInviscid.F90:165-293) for cell i of a tile staged in shared
+// memory, in FP32: its face entries and normals are all loaded first, then
+// the neighbours' records are read from the tile.  q, ai: the cell's
+// primitive state and sound speed.
+__device__ inline float tileDtSum(const View<float> &V, int i, const float *recs, const float *q, float ai) {
+  const size_t n = V.nc;
+  const float gam = V.p.refGammaF;
+  float sum = 0.f;
+  float4 Dt[kMaxCellFaces], Nt[kMaxCellFaces];
+#pragma unroll
+  for (int k = 0; k < kMaxCellFaces; ++k) {
+    if (k < V.cfW) {
+      Dt[k] = ld4(V.feD + 4 * (k * n + i));
+      Nt[k] = ld4(V.feN + 4 * (k * n + i));
+    } else {
+      Dt[k].w = __int_as_float(INT_MIN);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kMaxCellFaces; ++k) {
+    const int tag = __float_as_int(Dt[k].w);
+    if (tag >= 0) {
+      float x[8];
+      ldRec(recs, tag, x);
+      const float aj = sqrtf(gam * x[4] / x[0]);
+      const float vc = 0.5f * ((q[1] + x[1]) * Nt[k].x + (q[2] + x[2]) * Nt[k].y + (q[3] + x[3]) * Nt[k].z);
+      sum += (fabsf(vc) + 0.5f * (ai + aj)) * Nt[k].w;
+    } else if (tag != INT_MIN) {
+      const float vc = q[1] * Nt[k].x + q[2] * Nt[k].y + q[3] * Nt[k].z;
+      sum += (fabsf(vc) + ai) * Nt[k].w;
+    }
+  }
+  return sum;
+}
+
 template <bool kDt, bool kTiled, int kRc>
 __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, float *dc, const float *recs,
                                         int li, const unsigned short *stSm = nullptr,
@@ -685,34 +721,9 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
   const float gam = P.refGammaF;
   const float ai = kDt ? sqrtf(gam * q[4] / q[0]) : 0.f;
   float sum = 0.f;
-  if (kTiled && kDt) {
-    // the spectral-radius sum of the time step first, while no gradient
-    // state is live: its face entries and normals are all in flight at once
-    float4 Dt[kMaxCellFaces], Nt[kMaxCellFaces];
-#pragma unroll
-    for (int k = 0; k < kMaxCellFaces; ++k) {
-      if (k < V.cfW) {
-        Dt[k] = ld4(V.feD + 4 * (k * n + i));
-        Nt[k] = ld4(V.feN + 4 * (k * n + i));
-      } else {
-        Dt[k].w = __int_as_float(INT_MIN);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kMaxCellFaces; ++k) {
-      const int tag = __float_as_int(Dt[k].w);
-      if (tag >= 0) {
-        float x[8];
-        ldRec(recs, tag, x);
-        const float aj = sqrtf(gam * x[4] / x[0]);
-        const float vc = 0.5f * ((q[1] + x[1]) * Nt[k].x + (q[2] + x[2]) * Nt[k].y + (q[3] + x[3]) * Nt[k].z);
-        sum += (fabsf(vc) + 0.5f * (ai + aj)) * Nt[k].w;
-      } else if (tag != INT_MIN) {
-        const float vc = q[1] * Nt[k].x + q[2] * Nt[k].y + q[3] * Nt[k].z;
-        sum += (fabsf(vc) + ai) * Nt[k].w;
-      }
-    }
-  }
+  // the spectral-radius sum of the time step first, while no gradient state
+  // is live
+  if (kTiled && kDt) sum = tileDtSum(V, i, recs, q, ai);
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = 0.f;
   if (second) {
@@ -1050,6 +1061,11 @@ __host__ __device__ inline size_t tileBufFloats(const View<R> &V) {
 template <typename R>
 inline size_t tileSmemBytes(const View<R> &V, bool venkat) {
   return sizeof(float) * (2 * tileBufFloats(V) + (venkat ? 3 * kMaxCellFaces * kBlock : 0));
+}
+// The standalone time-step kernel stages the records only.
+template <typename R>
+inline size_t dtTileSmemBytes(const View<R> &V) {
+  return sizeof(float) * 8 * (size_t)V.maxRecs;
 }
 
 // L2 prefetch of the per-cell arrays the compute phase of tile t reads from
@@ -1494,6 +1510,42 @@ __global__ void __launch_bounds__(kBlock) kCellDtPrim(View<R> V) {
   double dt = 1.79769313486231571e308;
   if (i < V.nc) dt = cellDtPrim(V, i);
   blockMinDt(V.sc, dt);
+}
+
+// Time step alone on a tiled mesh (mixed mode), one CTA per tile: the tile's
+// and halo's prim records are staged in shared memory and each cell takes
+// the spectral-radius sum of the first stage of a step (tileDtSum), so this
+// entry and the step's own time step agree.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kCellDtTile(View<R> V) {
+  if constexpr (Layout<R>::packed) {
+    extern __shared__ float4 dtSmem[];
+    float *recs = reinterpret_cast<float *>(dtSmem);
+    const int t = blockIdx.x, base = t * kTile, nIn = min(kTile, V.nc - base);
+    const int hb = V.haloOff[t], nh = V.haloOff[t + 1] - hb;
+    for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
+      const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
+      if (src < 0) continue;  // an unused halo slot
+      const int dst = r < nIn ? r : kTile + (r - nIn);
+      const float *g = V.prim + 8 * (size_t)src;
+      const int o = recHalf0(dst);
+      cpAsync16(recs + o, g);
+      cpAsync16(recs + (o ^ 4), g + 4);
+    }
+    cpAsyncCommit();
+    cpAsyncWait<0>();
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    double dt = 1.79769313486231571e308;
+    if (i < V.nc) {
+      float rec[8];
+      ldRec(recs, threadIdx.x, rec);
+      const float q[5] = {rec[0], rec[1], rec[2], rec[3], rec[4]};
+      const float ai = sqrtf(V.p.refGammaF * q[4] / q[0]);
+      dt = V.vol[i] / (double)tileDtSum(V, i, recs, q, ai);
+    }
+    blockMinDt(V.sc, dt);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2102,6 +2154,8 @@ struct Launch {
     }
     if (Layout<R>::packed && V.tiled && V.gradRaw)
       cudaFuncSetAttribute(kWenoTile<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wenoTileSmemBytes(V));
+    if (Layout<R>::packed && V.tiled)
+      cudaFuncSetAttribute(kCellDtTile<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dtTileSmemBytes(V));
   }
   static void faceFlux(const View<R> &V, cudaStream_t s) {
     kFaceFlux<R><<<blocks((long long)V.nf + V.nb), kBlock, 0, s>>>(V);
@@ -2115,6 +2169,8 @@ struct Launch {
   static void timestep(const View<R> &V, cudaStream_t s) {
     kStepBegin<R><<<1, 1, 0, s>>>(V);
     if (Ref<R>::on) kCellDt<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
+    else if (Layout<R>::packed && V.tiled)
+      kCellDtTile<R><<<(V.nc + kTile - 1) / kTile, kBlock, dtTileSmemBytes(V), s>>>(V);
     else kCellDtPrim<R><<<blocks(V.nc), kBlock, 0, s>>>(V);
     kDtFinalize<R><<<1, 1, 0, s>>>(V);
   }

@@ -214,6 +214,18 @@ def test_second_order_steps_bit_exact(gpu_lib, discr, name):
     np.testing.assert_array_equal(cv_g, cv_o)
 
 
+@pytest.mark.parametrize("mesh", ["hex", "tets"])
+def test_mixed_timestep_entry_matches_step(gpu_lib, mesh):
+    """The time-step entry (RFLU_MinimumTimeStep's place) and the time step
+    that a mixed step takes from the same state are the same number."""
+    c = cases.shock_sphere(24) if mesh == "hex" else cases.blast_tets(8)
+    r = gpu.Region(c, "mixed")
+    dt = r.timestep(1.0)
+    n, t, rc = r.step(1, 1.0)
+    assert rc == 0 and n == 1
+    assert r.status()["dtMin"] == dt
+
+
 def test_rk_stage_entry_matches_step(gpu_lib):
     c = _hex_case(cases.DISCR_AUSM, cases.RECONST_VENKAT)
     o = Oracle(c)
