@@ -20,6 +20,7 @@
 #include "ctx.h"
 #include "errors.h"
 #include "ops.h"
+#include "tiles.h"
 
 namespace rflu {
 
@@ -845,102 +846,27 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
                        const std::vector<double> &bnz, const std::vector<double> &bnm,
                        const std::vector<double> &bd) {
   const int nc = V.nc, nf = V.nf, nb = V.nb;
-  const int nTiles = (nc + kTile - 1) / kTile;
-  std::vector<int> haloOff(nTiles + 1, 0), haloIdx;
-  std::vector<unsigned short> stLoc(stIdx.size());
-  std::vector<int> entLoc(cfEnt.size(), -1);
-  std::vector<int> mark(nc, -1), slot(nc, -1);
   int cfW = 0;
   for (int i = 0; i < nc; ++i) cfW = std::max(cfW, cfOff[i + 1] - cfOff[i]);
-  auto other = [&](int e) {  // neighbour of a cell's interior face entry
-    const int f = cfEnt[e] >> 1;
-    return (cfEnt[e] & 1) ? fc1[f] : fc2[f];
-  };
-  // pass 1: each tile's halo (sorted global ids of the cells outside the
-  // tile that its stencils and interior faces reach)
-  std::vector<std::vector<int>> halos(nTiles);
-  for (int t = 0; t < nTiles; ++t) {
-    const int b0 = t * kTile, b1 = std::min(nc, b0 + kTile);
-    std::vector<int> &halo = halos[t];
-    auto visit = [&](int j) {
-      if ((j < b0 || j >= b1) && mark[j] != t) {
-        mark[j] = t;
-        halo.push_back(j);
-      }
-    };
-    for (int i = b0; i < b1; ++i) {
-      for (int s = stOff[i]; s < stOff[i + 1]; ++s) visit(stIdx[s]);
-      for (int e = cfOff[i]; e < cfOff[i + 1]; ++e)
-        if (cfEnt[e] >= 0) visit(other(e));
-    }
-    std::sort(halo.begin(), halo.end());
-  }
-  int maxTileSt = 0;
-  for (int t = 0; t < nTiles; ++t) {
-    const int b0 = t * kTile, b1 = std::min(nc, b0 + kTile);
-    maxTileSt = std::max(maxTileSt, stOff[b1] - stOff[b0]);
-  }
-  // Halo slots.  Compact: the halo cells in order after the tile's own
-  // cells.  Bank-aligned: a halo cell j takes slot 8 r + (j & 7), r counting
-  // the halo cells of its residue, so every staged record's local id keeps
-  // the low three bits of its cell id (own cells too: tiles start at
-  // multiples of 8), and unused slots hold -1 and are not staged.  On a
-  // Morton-ordered structured mesh the k-th stencil members (and k-th face
-  // neighbours) of 8 consecutive cells then differ in those bits, and with
-  // the record swizzle their 16-byte loads hit 8 different bank groups.  The
-  // aligned slots are taken unless their larger buffers would fit fewer
-  // CTAs per SM into shared memory (unstructured meshes, whose residues are
-  // uneven).
-  int compactRecs = 0, alignedRecs = 0;
-  for (int t = 0; t < nTiles; ++t) {
-    int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int j : halos[t]) cnt[j & 7]++;
-    compactRecs = std::max(compactRecs, kTile + (int)halos[t].size());
-    alignedRecs = std::max(alignedRecs, kTile + 8 * *std::max_element(cnt, cnt + 8));
-  }
   int dev = 0, optin = 0, perSm = 0, reserved = 0;
   RFLU_CUDA(cudaGetDevice(&dev));
   RFLU_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   RFLU_CUDA(cudaDeviceGetAttribute(&perSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
   RFLU_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
-  // shared memory of a CTA: two tile buffers, and the face-offset cache of
-  // the Venkatakrishnan variant
-  auto smemOf = [&](int recs, bool venkat) {
+  // shared memory of a CTA of the gradient kernel: two tile buffers, and the
+  // face-offset cache of the Venkatakrishnan variant
+  auto smemOf = [&](int recs, int maxTileSt, bool venkat) {
     return sizeof(float) * (2 * tileBufFloatsFor(recs, maxTileSt) + (venkat ? 3 * 6 * kTile : 0));
   };
-  auto ctas = [&](int recs, bool venkat) { return (size_t)perSm / (smemOf(recs, venkat) + (size_t)reserved); };
-  const bool aligned = alignedRecs <= 65535 && ctas(alignedRecs, false) >= ctas(compactRecs, false) &&
-                       ctas(alignedRecs, true) >= ctas(compactRecs, true);
-  const int maxRecs = aligned ? alignedRecs : compactRecs;
-  if (maxRecs > 65535) return RFLU_OK;  // stays untiled
-  if (smemOf(maxRecs, true) > (size_t)optin) return RFLU_OK;
-  // pass 2: slots, the tiles' local ids of stencil members and face
-  // neighbours, and the slot-ordered halo lists
-  for (int t = 0; t < nTiles; ++t) {
-    const int b0 = t * kTile, b1 = std::min(nc, b0 + kTile);
-    const std::vector<int> &halo = halos[t];
-    int rows = 0;
-    if (aligned) {
-      int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      for (int j : halo) slot[j] = 8 * cnt[j & 7]++ + (j & 7);
-      rows = *std::max_element(cnt, cnt + 8);
-    } else {
-      for (size_t k = 0; k < halo.size(); ++k) slot[halo[k]] = (int)k;
-    }
-    auto local = [&](int j) {
-      if (j >= b0 && j < b1) return j - b0;
-      return kTile + slot[j];
-    };
-    for (int i = b0; i < b1; ++i) {
-      for (int s = stOff[i]; s < stOff[i + 1]; ++s) stLoc[s] = (unsigned short)local(stIdx[s]);
-      for (int e = cfOff[i]; e < cfOff[i + 1]; ++e)
-        if (cfEnt[e] >= 0) entLoc[e] = local(other(e));
-    }
-    const size_t h0 = haloIdx.size();
-    haloIdx.resize(h0 + (aligned ? 8 * (size_t)rows : halo.size()), -1);
-    for (int j : halo) haloIdx[h0 + slot[j]] = j;
-    haloOff[t + 1] = (int)haloIdx.size();
-  }
+  auto ctasPerSm = [&](int recs, int maxTileSt, bool venkat) {
+    return (size_t)perSm / (smemOf(recs, maxTileSt, venkat) + (size_t)reserved);
+  };
+  TilePlan plan;
+  if (!planTiles(nc, kTile, cfOff, cfEnt, stOff, stIdx, fc1, fc2, ctasPerSm, plan)) return RFLU_OK;  // stays untiled
+  if (smemOf(plan.maxRecs, plan.maxTileSt, true) > (size_t)optin) return RFLU_OK;
+  const int maxRecs = plan.maxRecs, maxTileSt = plan.maxTileSt;
+  const std::vector<int> &haloOff = plan.haloOff, &haloIdx = plan.haloIdx, &entLoc = plan.entLoc;
+  std::vector<unsigned short> &stLoc = plan.stLoc;
   stLoc.resize(stLoc.size() + 16, 0);  // whole 16-byte words past the last tile
   std::vector<float> feD(4 * (size_t)cfW * nc, 0.f), feN(4 * (size_t)cfW * nc, 0.f);
   for (int i = 0; i < nc; ++i)
