@@ -831,11 +831,11 @@ struct Ctx : CtxBase {
 };
 
 // Tiles of the mixed-mode gradient kernel (ctx.h): per tile of kTile
-// consecutive cells, the sorted list of halo cells its stencils and faces
-// reach; the local id of every stencil member; and the entry-major face
-// arrays feD/feN with the neighbour's local id as the tag.  Left untiled
-// (V.tiled = 0) when a tile would stage more records than shared memory or a
-// 16-bit id holds.
+// consecutive cells, its halo cells in slots (planTiles, tiles.h: aligned to
+// the shared-memory banks where that costs no occupancy); the local id of
+// every stencil member; and the entry-major face arrays feD/feN with the
+// neighbour's local id as the tag.  Left untiled (V.tiled = 0) when a tile
+// would stage more records than shared memory or a 16-bit id holds.
 template <typename R>
 int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cfEnt, const std::vector<int> &stOff,
                        const std::vector<int> &stIdx, const std::vector<int> &fc1, const std::vector<int> &fc2,

@@ -102,7 +102,8 @@ struct View {
   // mixed mode, tiled gradient kernel: cells in tiles of kTile consecutive
   // (Morton) cells; a tile's CTA stages the prim records of its cells and of
   // the halo (the other cells its stencils and faces reach) in shared memory
-  // and addresses them by 16-bit local ids (own cells 0..kTile-1, halo after)
+  // and addresses them by 16-bit local ids (own cells 0..kTile-1, halo slots
+  // after; the plan is tiles.h's planTiles)
   int tiled;                        // 0: the gather kernel instead
   int maxRecs;                      // max staged records over the tiles
   int maxTileSt;                    // max stencil entries of a tile's cells
