@@ -941,7 +941,6 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   std::vector<int> store(nf);
   std::iota(store.begin(), store.end(), 0);
   auto c1of = [&](int f) { return newId[g->f2c[2 * (size_t)f] - 1]; };
-  auto c2of = [&](int f) { return newId[g->f2c[2 * (size_t)f + 1] - 1]; };
   std::stable_sort(store.begin(), store.end(), [&](int a, int b) { return c1of(a) < c1of(b); });
   std::vector<int> slotOf(nf);
   for (int s = 0; s < nf; ++s) slotOf[store[s]] = s;
