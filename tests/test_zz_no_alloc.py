@@ -2,10 +2,14 @@
 static scratch, for callers that cannot allocate device memory per call,
 against the allocating rflu_gpu_residual on two calls in a row.
 
+The scratch layout depends on the reconstruction: WENO smoothing (RECONST 1
+and 2) carves a second gradient array for the unsmoothed gradients, first
+order carves gradients it never writes, and the mixed mode packs its records
+differently; every combination is compared with the allocating entry in all
+three precision modes.
+
 Collected last (file name) so that a run stopping at the first failure has
 already run every other test."""
-import ctypes as C
-
 import numpy as np
 import pytest
 
@@ -13,10 +17,18 @@ from rocflu_gb300 import cases, gpu
 
 pytestmark = pytest.mark.gpu
 
+# (space order, RECONST, create options): the BJ eigenframe limiter (tiled
+# and gather-based gradient kernels in the mixed mode), WENO-XYZ and simple
+# WENO smoothing (second gradient array), and first order (no gradients)
+VARIANTS = [(2, cases.RECONST_BJ, 0), (2, cases.RECONST_BJ, gpu.OPT_UNTILED), (2, cases.RECONST_WENO_XYZ, 0),
+            (2, cases.RECONST_WENO_SIMPLE, 0), (1, cases.RECONST_NONE, 0)]
 
-def _case(discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ, n=6):
-    num = cases.Numerics(space_order=2, space_discr=discr, reconst=reconst, cfl=0.4)
+
+def _case(discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ, n=6, order=2):
+    num = cases.Numerics(space_order=order, space_discr=discr, reconst=reconst, cfl=0.4)
     c = cases.shock_sphere(n, num=num)
+    for p in c.patches:
+        p.order = min(p.order, order)
     c.num.dt_imposed = 1e-4
     return c
 
@@ -28,12 +40,16 @@ def _state(case, seed):
     return cv
 
 
+@pytest.mark.parametrize("order,reconst,options", VARIANTS)
 @pytest.mark.parametrize("precision", ["fp64_exact", "fp64", "mixed"])
-def test_residual_static_matches_allocating_entry(gpu_lib, precision):
+def test_residual_static_matches_allocating_entry(gpu_lib, precision, order, reconst, options):
     import torch
 
-    c = _case()
-    r = gpu.Region(c, precision)
+    c = _case(reconst=reconst, order=order)
+    r = gpu.Region(c, precision, options=options)
+    r.step(1, 0.0)  # a context state that differs from the inputs below
+    cv_before, dv_before = r.download()
+    status_before = r.status()
     for call in range(2):
         cv = _state(c, seed=10 + call)
         ref, _ = r.residual(cv, with_grad=False)      # the allocating entry point
@@ -41,13 +57,14 @@ def test_residual_static_matches_allocating_entry(gpu_lib, precision):
         rhs_dev = torch.full_like(cv_dev, float("nan"))
         torch.cuda.synchronize()
         r.residual_static(cv_dev.data_ptr(), rhs_dev.data_ptr())
-        torch.cuda.synchronize()
-        got = rhs_dev.cpu().numpy()
+        got = rhs_dev.cpu().numpy()                   # complete on return
         # same kernels on the same inputs: identical in every precision mode
         np.testing.assert_array_equal(got, ref)
-    # the context's own device state is untouched by the static call
-    cv_ctx, _ = r.download()
-    np.testing.assert_array_equal(cv_ctx, c.cv0)
+    # the context's own state and counters are untouched by the static call
+    cv_after, dv_after = r.download()
+    np.testing.assert_array_equal(cv_after, cv_before)
+    np.testing.assert_array_equal(dv_after, dv_before)
+    assert r.status() == status_before
 
 
 def test_residual_static_rejects_oversized_mesh(gpu_lib):
@@ -63,10 +80,17 @@ def test_residual_static_rejects_oversized_mesh(gpu_lib):
 
 
 def test_residual_static_rejects_host_pointers(gpu_lib):
+    import torch
+
     c = _case()
     r = gpu.Region(c, "fp64")
     cv = np.ascontiguousarray(c.cv0)
     rhs = np.empty_like(cv)
     with pytest.raises(gpu.RfluError) as e:
         r.residual_static(cv.ctypes.data, rhs.ctypes.data)
+    assert "device" in str(e.value)
+    # pinned host memory is refused as well (a kernel could reach it, slowly)
+    pinned = torch.from_numpy(cv).pin_memory()
+    with pytest.raises(gpu.RfluError) as e:
+        r.residual_static(pinned.data_ptr(), pinned.data_ptr())
     assert "device" in str(e.value)
