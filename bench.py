@@ -9,20 +9,26 @@ RK stages on the device.
 
   value  Mcell*RK-stage/s of the mixed FP32/FP64 path, state resident in HBM
   fp64   the same metric for the all-FP64 path, and the mixed-vs-FP64
-         L1/Linf density and pressure differences after the same steps
+         L1/Linf density and pressure differences after the configured 500
+         steps from the same initial state (and after 100 and 250)
   e2e    Mcell*RK-stage/s through the C ABI with host buffers: every step
-         uploads cv from pinned host memory, steps, and downloads cv and dv
+         uploads cv from pinned host memory, steps, and downloads cv
   roofline  dominant kernel of the mixed path against the measured HBM copy
          bandwidth
-  cpu_baseline  the CPU oracle (FP64 restatement of the reference, one
-         thread) on a bounded sample: the same set-up on a 40^3 mesh
+  tets   the same metric on the 64^3 x 6 jittered-tetrahedron blast mesh
+         (1,572,864 cells), HLLC + Venkatakrishnan, mixed and FP64, with
+         its whole-stage roofline at the mesh's measured S and Nf/Nc
+  cpu_baseline  the CPU oracle (the FP64 restatement of the reference,
+         OpenMP over all host cores) on a bounded sample of the same 128^3
+         workload: a few whole steps, plus one step on one thread
 
 The working set (state, gradients, face fluxes, geometry: > 0.5 GB) is far
 larger than the 126 MB L2, so no L2 flush is needed between steps.
 
---impl reference times the CPU restatement of the reference path on all host
-cores (one oracle replica per core, each on its own 40^3 sample); the Fortran
-reference cannot be built here.
+--impl reference times the CPU restatement of the reference path on the same
+128^3 workload with all host cores (OpenMP; per cell the same sums in the
+reference's order, so results do not depend on the thread count), one whole
+time step per bench step; the Fortran reference cannot be built here.
 """
 import argparse
 import json
@@ -49,8 +55,10 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=128, help="cells per side of the hex box")
-    p.add_argument("--cpu-n", type=int, default=64, help="cells per side of the CPU sample")
-    p.add_argument("--cpu-steps", type=int, default=6)
+    p.add_argument("--cpu-steps", type=int, default=3, help="whole steps of the all-core CPU sample")
+    p.add_argument("--accuracy-steps", type=int, default=500, help="steps of the mixed-vs-FP64 comparison")
+    p.add_argument("--skip-tets", action="store_true", help="skip the tetrahedral-mesh throughput block")
+    p.add_argument("--tet-n", type=int, default=64, help="hexes per side of the tet blast mesh (x6 tets)")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--precisions", default="mixed,fp64", help="device paths to time (profiling runs time one)")
@@ -298,14 +306,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"partial": True, "results": results}))
         return
-    # mixed vs FP64 after the same number of steps from the same state
-    cv_m, dv_m = regions["mixed"].download()
-    cv_d, dv_d = regions["fp64"].download()
-    err = {"L1_rho": float(np.abs(cv_m[:, 0] - cv_d[:, 0]).mean()),
-           "Linf_rho": float(np.abs(cv_m[:, 0] - cv_d[:, 0]).max()),
-           "L1_p": float(np.abs(dv_m[:, 0] - dv_d[:, 0]).mean()),
-           "Linf_p": float(np.abs(dv_m[:, 0] - dv_d[:, 0]).max()),
-           "steps": args.warmup + args.steps}
+    cv_m, _ = regions["mixed"].download(with_dv=False)
 
     # end-to-end through the C ABI with host buffers
     e2e = None
@@ -333,6 +334,9 @@ def run_ours(args):
         e2e = {"value": whole_job_value(units, ws, wall * 1e3), "unit": UNIT, "h2d_bytes_per_step": int(host_cv.numel() * 8),
                "d2h_bytes_per_step": int(host_cv.numel() * 8)}
     clocks = clk.stop()
+
+    # mixed vs FP64 from the same initial state after the configured steps
+    err = accuracy_run(regions, case, args.accuracy_steps)
 
     # roofline of the dominant kernel of the mixed path
     peaks, peak_kind = measured_peaks()
@@ -372,10 +376,16 @@ def run_ours(args):
         adjoint = single_adjoint(args, cases, gpu)
     unrolled = None if args.skip_unrolled else unrolled_adjoint(args, cases, gpu)
     weno = None if args.skip_weno else weno_variant(args, cases, gpu, setup, case.num.dt_imposed)
+    tets = None if args.skip_tets else tet_block(args, cases, gpu)
+    for reg in regions.values():
+        reg.close()
+    regions_cells = int(setup.n_cells)
 
     cpu = None
-    if rank == 0 and not args.skip_cpu:
-        cpu = cpu_sample(args.cpu_n, args.cpu_steps)
+    if rank == 0 and not args.skip_cpu and ws == 1:
+        cpu = cpu_sample(case, args.cpu_steps)
+        cpu["gpu_over_cpu"] = {"mixed": results["mixed"]["value"] / cpu["value"],
+                               "fp64": results["fp64"]["value"] / cpu["value"]}
 
     if rank == 0:
         ms = results["mixed"]["ms"]
@@ -383,10 +393,8 @@ def run_ours(args):
             "metric": METRIC, "value": results["mixed"]["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": "shock_sphere_hex%d_hllc_bj_wray3" % args.n, "cells": regions["mixed"].n_cells,
-                       "faces": int(setup.f2c.shape[0]), "stages_per_step": 3, "flux": "HLLC", "limiter": "BJ (RECONST 10)",
-                       "parallelism": "replicas" if ws > 1 else "single", "l2": "working set > L2 (no flush)",
-                       "setup_s": setup_s},
+            "config": workload_config(args.n, regions_cells, int(setup.f2c.shape[0]), ws),
+            "setup_s": setup_s,
             # mixed step graph: step begin, gradient+dt, dt finalize, face flux and
             # gather-update of stage 1, three kernels per later stage, step end;
             # plus the one scalar-setting kernel of the step call
@@ -396,6 +404,7 @@ def run_ours(args):
             "adjoint": adjoint,
             "unrolled_adjoint": unrolled,
             "weno": weno,
+            "tets": tets,
             "e2e": e2e,
             "roofline": roof,
             "stage_roofline": stage_roof,
@@ -564,63 +573,170 @@ def unrolled_adjoint(args, cases, gpu):
     return out
 
 
-def _cpu_worker(n, steps, q=None):
-    sys.path.insert(0, ROOT)
-    from oracle.oracle import Oracle
+def workload_config(n, cells, faces, ws):
+    """The config block both arms print for the headline workload."""
+    return {"workload": "shock_sphere_hex%d_hllc_bj_wray3" % n, "cells": int(cells), "faces": int(faces),
+            "stages_per_step": 3, "flux": "HLLC", "limiter": "BJ (RECONST 10)",
+            "parallelism": "replicas" if ws > 1 else "single", "l2": "working set > L2 (no flush)"}
+
+
+def accuracy_run(regions, case, n_steps, marks=(100, 250)):
+    """The mixed path against the FP64 path from the same initial state:
+    L1/Linf of density and pressure after each mark and after n_steps whole
+    steps (CFL time step each step; the imposed first step is the CFL step
+    of the initial state)."""
+    for r in regions.values():
+        r.upload(case.cv0)
+    t = {k: 0.0 for k in regions}
+    rcs = {k: 0 for k in regions}
+    done = 0
+    hist = []
+    for m in sorted({x for x in marks if x < n_steps} | {n_steps}):
+        for k, r in regions.items():
+            n, t[k], rc = r.step(m - done, t[k])
+            rcs[k] |= rc
+        cvm, dvm = regions["mixed"].download()
+        cvd, dvd = regions["fp64"].download()
+        hist.append({"steps": m, "L1_rho": float(np.abs(cvm[:, 0] - cvd[:, 0]).mean()),
+                     "Linf_rho": float(np.abs(cvm[:, 0] - cvd[:, 0]).max()),
+                     "L1_p": float(np.abs(dvm[:, 0] - dvd[:, 0]).mean()),
+                     "Linf_p": float(np.abs(dvm[:, 0] - dvd[:, 0]).max()),
+                     "time_mixed": t["mixed"], "time_fp64": t["fp64"]})
+        done = m
+    out = dict(hist[-1])
+    out["history"] = hist
+    out["event_codes"] = rcs
+    out["status"] = {k: r.status() for k, r in regions.items()}
+    return out
+
+
+def tet_block(args, cases, gpu):
+    """Throughput on the tetrahedral blast mesh of the 3-D blast
+    configuration: 64^3 hexes split into 6 jittered tetrahedra (1,572,864
+    cells, seed 0), HLLC, second order with the Venkatakrishnan limiter,
+    Wray RK3, CFL 0.4, slip walls, at p = 4 inside r < 0.1 (the p = 100 of
+    the configuration drives the reference scheme's face pressures negative
+    within a few steps, the CPU oracle and the device alike).  Mixed and
+    FP64 step rates and each one's whole-stage roofline with this mesh's
+    measured S (stencil members per cell) and Nf/Nc."""
+    import torch
+
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_VENKAT, cfl=0.4)
+    c = cases.blast_tets(args.tet_n, num=num, p_in=4.0)
+    t0 = time.time()
+    setup = gpu.Setup(c)
+    setup_s = time.time() - t0
+    probe = gpu.Region(c, "fp64", grid=setup)
+    c.num.dt_imposed = probe.timestep(1.0)
+    probe.close()
+    nc, nf, nnz = int(setup.n_cells), int(setup.f2c.shape[0]), int(setup.c2cs.shape[0])
+    sb = stage_bytes_per_cell(nc, nf, nnz)
+    peaks, peak_kind = measured_peaks()
+    steps, warm = 10, 3
+    out = {"workload": "blast_tets%dx6_hllc_venkat_wray3_p4" % args.tet_n, "cells": nc, "faces": nf,
+           "boundary_faces": int(setup.bf2c.shape[0]), "S": sb["S"], "nf_per_nc": sb["nf_per_nc"],
+           "steps": steps, "warmup": warm, "setup_s": setup_s, "peak_gbs": peaks["hbm_gbs"], "peak_source": peak_kind}
+    for prec in ("mixed", "fp64"):
+        reg = gpu.Region(c, prec, grid=setup)
+        stream = torch.cuda.ExternalStream(reg.stream)
+        _, t, _ = reg.step(warm, 0.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, t, rc = reg.step(steps, t)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        kt = reg.kernel_times(5)
+        stage_ms = ms / (steps * reg.n_stages)
+        ach = sb[prec] * nc / (stage_ms * 1e-3) / 1e9
+        st = reg.status()
+        out[prec] = {"value": nc * reg.n_stages * steps / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": ms / steps,
+                     "kernel_ms": {"gradLimit": kt[0], "faceFlux": kt[1], "gatherUpdate": kt[2], "timestep": kt[3]},
+                     "stage_roofline": {"bytes_per_cell_stage": sb[prec], "stage_ms": stage_ms, "achieved_gbs": ach,
+                                        "frac": ach / peaks["hbm_gbs"]},
+                     "rc": rc, "nanCells": st["nanCells"], "posFixCells": st["posFixCells"], "time": t}
+        reg.close()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def _oracle_case(n):
+    """The headline workload for the CPU oracle, with the imposed first step
+    set, as on the device, to the CFL step of the initial state."""
+    from oracle import oracle as orc
     from rocflu_gb300 import cases
 
     case = cases.shock_sphere(n)
-    o = Oracle(case)
-    dt = o.timestep(1.0)
+    o = orc.Oracle(case)
+    o.set_dt_imposed(o.timestep(1.0))
+    return case, o
+
+
+def cpu_sample(case, n_steps):
+    """The CPU oracle (FP64 restatement of the reference path, OpenMP over
+    every host core) on the same 128^3 workload: one untimed step (the
+    imposed first step), n_steps timed whole steps on all cores, then one
+    step on one thread."""
+    from oracle import oracle as orc
+
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
     t0 = time.perf_counter()
-    o.run_fixed_dt(steps, dt)
+    o = orc.Oracle(case)
+    o.set_dt_imposed(case.num.dt_imposed)
+    setup_s = time.perf_counter() - t0
+    _, t = o.run(1, 0.0)
+    t0 = time.perf_counter()
+    _, t = o.run(n_steps, t)
     el = time.perf_counter() - t0
-    res = (case.n_cells * 3 * steps, el)
-    if q is not None:
-        q.put(res)
-    return res
-
-
-def cpu_sample(n, steps):
-    units, el = _cpu_worker(n, steps)
-    return {"value": units / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "shock_sphere %d^3 hex (%d cells), HLLC+BJ, %d Wray steps, one thread, %.1f s" %
-                      (n, n ** 3, steps, el)}
+    units = o.n_cells * o.n_stages() * n_steps
+    orc.set_threads(1)
+    t0 = time.perf_counter()
+    _, t = o.run(1, t)
+    el1 = time.perf_counter() - t0
+    orc.set_threads(cores)
+    return {"value": units / el / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "the same %d-cell mesh and set-up, %d whole Wray steps after one untimed step, %d threads, "
+                      "%.1f s (oracle set-up %.1f s untimed)" % (o.n_cells, n_steps, cores, el, setup_s),
+            "single_thread": {"value": o.n_cells * o.n_stages() / el1 / 1e6, "unit": UNIT, "cores": 1,
+                              "sample": "one whole step of the same workload, %.1f s" % el1}}
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference path (the
+    Fortran reference cannot be built here or on the GPU machine) on the same
+    128^3 workload with every host core; each bench step is one whole time
+    step (CFL time step + three Wray stages), W untimed, K timed."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
-    import multiprocessing as mp
+    from oracle import oracle as orc
 
-    ctx = mp.get_context("spawn")
     cores = os.cpu_count() or 1
-    vals = []
-    samples = []
-    # W untimed samples, then K timed ones
-    for step in range(-args.warmup, args.steps):
-        q = ctx.Queue()
-        procs = [ctx.Process(target=_cpu_worker, args=(args.cpu_n, args.cpu_steps, q)) for _ in range(cores)]
-        w0 = time.perf_counter()
-        for p in procs:
-            p.start()
-        res = [q.get() for _ in procs]
-        for p in procs:
-            p.join()
-        if step < 0:
-            continue
-        units = sum(r[0] for r in res)
-        wall = max(r[1] for r in res)
-        samples.append(units / wall / 1e6)
-        vals.append(time.perf_counter() - w0)
-    value = float(np.median(samples))
+    orc.set_threads(cores)
+    t0 = time.perf_counter()
+    case, o = _oracle_case(args.n)
+    setup_s = time.perf_counter() - t0
+    t = 0.0
+    for _ in range(args.warmup):
+        _, t = o.run(1, t)
+    els = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, t = o.run(1, t)
+        els.append(time.perf_counter() - t0)
+    total = sum(els)
+    value = o.n_cells * o.n_stages() * args.steps / total / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "shock_sphere_hex%d_hllc_bj_wray3" % args.n},
+            "warmup": args.warmup, "ms_per_step": total * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args.n, o.n_cells, o.n_faces, ws),
+            "setup_s": setup_s,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d replicas of the FP64 CPU restatement, each on a %d^3 hex sample, %d Wray steps"
-                                       % (cores, args.cpu_n, args.cpu_steps)},
+                             "sample": "the FP64 CPU restatement of the reference path (OpenMP, %d threads) on the "
+                                       "same %d-cell mesh: %d whole Wray steps after %d untimed"
+                                       % (cores, o.n_cells, args.steps, args.warmup)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

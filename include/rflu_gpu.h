@@ -85,7 +85,12 @@ typedef struct {
   double cp, gamma; /* CP, GAMMA */
   double cfl, epsEntr, dissFact; /* CFL, ENTROPY, DISSFACT */
   double dtImposed, dtMinLimit;  /* TIMESTEP, DTMINLIMIT */
+  int options;      /* RFLU_OPT_* bits of the device layout (no deck key; 0 = default) */
 } rflu_num_desc;
+
+/* rflu_num_desc::options */
+#define RFLU_OPT_UNTILED 1  /* mixed mode: never stage tiles in shared memory (the gather-based gradient kernels
+                               that meshes too irregular for the tile plan take) */
 
 typedef struct {
   long long nanCells;      /* RFLU_CheckValidity events */
@@ -191,6 +196,13 @@ int rflu_gpu_fp64_rate(double *tflops);
  * float midpoints) and returns the number of differing results. */
 int rflu_gpu_check_conversions(long long n, unsigned long long seed, unsigned long long *mismatches);
 
+/* Diagnostics: the mixed mode's FP64 reciprocal of rho and sound speed,
+ * refined once by Newton-Raphson from FP32 seeds, against IEEE FP64 division
+ * and square root on n generated values 2^e*m (m in [1,2), |e| <= 100):
+ * maxRelErr[0] the largest relative error of the reciprocal, maxRelErr[1]
+ * of the square root. */
+int rflu_gpu_check_refinements(long long n, unsigned long long seed, double *maxRelErr);
+
 /* Residual without any allocation (no counterpart in the reference).
  * Same result as rflu_gpu_residual (rhs only), for callers that cannot
  * allocate device memory at call time: hosts that reserve all device memory
@@ -206,9 +218,16 @@ int rflu_gpu_check_conversions(long long n, unsigned long long seed, unsigned lo
  * device current); make that first call before any stream capture.  All
  * calls share the array: calls that overlap on the GPU (other host threads,
  * other contexts on the same device) race and must be serialised by the
- * caller.  The call runs on the context's stream and returns after it
- * finishes; it calls no cudaMalloc, cudaFree or allocating routine and
- * leaves the context's own state untouched. */
+ * caller.  Both buffers must be device memory on the context's device (or
+ * managed memory), and that device must be current: anything else is
+ * refused with RFLU_ERR_ARG before a kernel is launched.
+ * Ordering: the call runs on the context's stream (rflu_gpu_stream) and does
+ * not wait for the caller's streams, so whatever writes cvDev must be
+ * complete before the call (a device or stream synchronisation, or an event
+ * the caller has waited on); rhsDev is complete when the call returns,
+ * because it synchronises the context's stream before returning.  It calls
+ * no cudaMalloc, cudaFree or allocating routine and leaves the context's own
+ * state untouched (its cv, dv and status counters). */
 int rflu_gpu_residual_static(rflu_gpu_ctx *ctx, const double *cvDev, double *rhsDev);
 
 /* ------------------------------------------------------------------------ */

@@ -2,9 +2,19 @@
  * CPU oracle: FP64 restatement of the RocfluMP explicit residual-and-update
  * path (thierrydaoud/Rocflu).  TEST INFRASTRUCTURE ONLY -- see oracle.h.
  *
- * Build: g++ -O2 -ffp-contract=off -fPIC -shared (oracle/Makefile).  The
- * reference release flags are -O / -O2 -ffp-contract=off (CMakeLists.txt:44,
- * machines/dane.sh:6): no fused multiply-add, left-to-right evaluation.
+ * Build: g++ -O2 -ffp-contract=off -fopenmp -fPIC -shared (oracle/Makefile).
+ * The reference release flags are -O / -O2 -ffp-contract=off
+ * (CMakeLists.txt:44, machines/dane.sh:6): no fused multiply-add,
+ * left-to-right evaluation.
+ *
+ * Threads: the reference's face loops scatter into both cells of a face
+ * (rhs(:,c1) += F, rhs(:,c2) -= F and the limiters' running min/max).  Each
+ * cell sees its faces in face order there, interior faces first and then
+ * the patches in order, so the same sums and min/max taken per cell over its
+ * faces in that order (the cfOff/cfEnt lists below) give the same bits, NaN
+ * propagation included, and every cell can be done by its own thread.  Face
+ * values (fluxes, spectral radii) are formed once per face first.  Built
+ * without OpenMP the pragmas are ignored and every loop runs in order.
  */
 #include "oracle.h"
 
@@ -16,6 +26,9 @@
 #include <map>
 #include <array>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace {
 
@@ -180,8 +193,15 @@ struct orc_ctx {
   int nrkSteps;
   double ark[5], grk[5];
   double refCp, refGamma, gvMol, gvCp;
+  /* cell -> face entries in the order the reference's face loops reach a
+     cell: its interior faces by face id (entry 2*f + side, side 1 when the
+     cell is the face's second cell f2c(2)), then its boundary faces patch
+     by patch (entry -(1 + b), b numbering the boundary faces of all patches
+     in order, bPatch/bFace giving the patch and the index in it) */
+  std::vector<int> cfOff, cfEnt, bPatch, bFace;
   /* state */
   std::vector<double> cv, dv, cvOld, rhs, rhsSum, diss, grad, lim;
+  std::vector<double> flux;     /* 5 per interior face, then 5 per boundary face */
   long long posFixCount = 0, negPCount = 0, nanCount = 0;
   double dtCells;
 };
@@ -251,6 +271,32 @@ void buildFaceList(orc_ctx *c) {
       p.bf2c[i] = rec[it->second].c1;
     }
   }
+}
+
+/* The per-cell face lists of orc_ctx (cfOff, cfEnt) from f2c and bf2c. */
+void buildCellFaces(orc_ctx *c) {
+  const int nc = c->nCells;
+  c->bPatch.clear();
+  c->bFace.clear();
+  for (int ip = 0; ip < (int)c->patches.size(); ++ip)
+    for (int i = 0; i < c->patches[ip].n; ++i) {
+      c->bPatch.push_back(ip);
+      c->bFace.push_back(i);
+    }
+  const int nb = (int)c->bPatch.size();
+  std::vector<int> cnt(nc + 1, 0);
+  for (int f = 0; f < c->nFaces; ++f) { cnt[c->f2c[2 * f] + 1]++; cnt[c->f2c[2 * f + 1] + 1]++; }
+  for (int b = 0; b < nb; ++b) cnt[c->patches[c->bPatch[b]].bf2c[c->bFace[b]] + 1]++;
+  c->cfOff.assign(nc + 1, 0);
+  for (int ic = 0; ic < nc; ++ic) c->cfOff[ic + 1] = c->cfOff[ic] + cnt[ic + 1];
+  c->cfEnt.assign(c->cfOff[nc], 0);
+  std::vector<int> fill(c->cfOff.begin(), c->cfOff.end() - 1);
+  for (int f = 0; f < c->nFaces; ++f) {
+    c->cfEnt[fill[c->f2c[2 * f]]++] = 2 * f;
+    c->cfEnt[fill[c->f2c[2 * f + 1]]++] = 2 * f + 1;
+  }
+  for (int b = 0; b < nb; ++b) c->cfEnt[fill[c->patches[c->bPatch[b]].bf2c[c->bFace[b]]]++] = -(1 + b);
+  c->flux.assign(5 * ((size_t)c->nFaces + nb), 0.0);
 }
 
 /* FaceVectorTria / FaceVectorQuad (libfloflu/FaceVector.F90),
@@ -526,6 +572,7 @@ void setDependentVars(orc_ctx *c, int ic) {
 /* var = cv in DUVWP state (rho,u,v,w,p).                                    */
 /* ------------------------------------------------------------------------ */
 void computeGradCells(orc_ctx *c, const std::vector<double> &var, std::vector<double> &grad) {
+#pragma omp parallel for schedule(static)
   for (int icg = 0; icg < c->nCells; ++icg) {
     const double *m = &c->moms[10 * icg];
     double r11 = m[0], r12 = m[1], r22 = m[2], r13 = m[3], r23 = m[4], r33 = m[5];
@@ -561,42 +608,54 @@ void computeGradCells(orc_ctx *c, const std::vector<double> &var, std::vector<do
 /* ------------------------------------------------------------------------ */
 /* Limiters: modflu/RFLU_ModLimiters.F90                                      */
 /* ------------------------------------------------------------------------ */
-/* RFLU_ComputeLimiterBarthJesp (:132-322); skipVel excludes vars 2..4. */
+/* The neighbour extremes of the limiters' first face loop: per face,
+ * vmin(c1) = min(vmin(c1), var(c2)), vmin(c2) = min(vmin(c2), var(c1)) and
+ * the same for vmax, here per cell over its interior faces in face order. */
+void neighbourExtremes(orc_ctx *c, const std::vector<double> &var, std::vector<double> &vmin,
+                       std::vector<double> &vmax, bool skipVel) {
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < c->nCells; ++ic) {
+    for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      if (code < 0) continue;
+      const int other = c->f2c[(code & ~1) + 1 - (code & 1)];
+      for (int iv = 0; iv < 5; ++iv) {
+        if (skipVel && iv >= 1 && iv <= 3) continue;
+        double vo = var[5 * other + iv];
+        vmin[5 * ic + iv] = fmin2(vmin[5 * ic + iv], vo);
+        vmax[5 * ic + iv] = fmax2(vmax[5 * ic + iv], vo);
+      }
+    }
+  }
+}
+
+/* RFLU_ComputeLimiterBarthJesp (:132-322); skipVel excludes vars 2..4.  The
+ * second face loop's two sides (c1 with dx1 = cofg(c1) - fc, c2 with dx2)
+ * per cell over its interior faces in face order. */
 void limiterBarthJesp(orc_ctx *c, const std::vector<double> &var, const std::vector<double> &grad,
                       std::vector<double> &lim, bool skipVel) {
   const int nc = c->nCells;
   std::vector<double> vmin(var), vmax(var);
   for (int k = 0; k < 5 * nc; ++k) lim[k] = 1.0;
-  auto limitVar = [&](int iv) { return !(skipVel && iv >= 1 && iv <= 3); };
-  for (int f = 0; f < c->nFaces; ++f) {
-    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
-    for (int iv = 0; iv < 5; ++iv) {
-      if (!limitVar(iv)) continue;
-      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
-      vmin[5 * c1 + iv] = fmin2(vmin[5 * c1 + iv], v2);
-      vmin[5 * c2 + iv] = fmin2(vmin[5 * c2 + iv], v1);
-      vmax[5 * c1 + iv] = fmax2(vmax[5 * c1 + iv], v2);
-      vmax[5 * c2 + iv] = fmax2(vmax[5 * c2 + iv], v1);
-    }
-  }
-  for (int f = 0; f < c->nFaces; ++f) {
-    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
-    double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
-    double dx1 = c->cofg[3 * c1] - xc, dy1 = c->cofg[3 * c1 + 1] - yc, dz1 = c->cofg[3 * c1 + 2] - zc;
-    double dx2 = c->cofg[3 * c2] - xc, dy2 = c->cofg[3 * c2 + 1] - yc, dz2 = c->cofg[3 * c2 + 2] - zc;
-    for (int iv = 0; iv < 5; ++iv) {
-      if (!limitVar(iv)) continue;
-      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
-      double d1min1 = vmin[5 * c1 + iv] - v1, d1max1 = vmax[5 * c1 + iv] - v1;
-      double d1min2 = vmin[5 * c2 + iv] - v2, d1max2 = vmax[5 * c2 + iv] - v2;
-      const double *g1 = &grad[15 * c1 + 3 * iv], *g2 = &grad[15 * c2 + 3 * iv];
-      double d21 = g1[0] * dx1 + g1[1] * dy1 + g1[2] * dz1;
-      double d22 = g2[0] * dx2 + g2[1] * dy2 + g2[2] * dz2;
-      double term;
-      if (d21 > 0.0) { term = fmin2(1.0, d1max1 / d21); lim[5 * c1 + iv] = fmin2(term, lim[5 * c1 + iv]); }
-      else if (d21 < 0.0) { term = fmin2(1.0, d1min1 / d21); lim[5 * c1 + iv] = fmin2(term, lim[5 * c1 + iv]); }
-      if (d22 > 0.0) { term = fmin2(1.0, d1max2 / d22); lim[5 * c2 + iv] = fmin2(term, lim[5 * c2 + iv]); }
-      else if (d22 < 0.0) { term = fmin2(1.0, d1min2 / d22); lim[5 * c2 + iv] = fmin2(term, lim[5 * c2 + iv]); }
+  neighbourExtremes(c, var, vmin, vmax, skipVel);
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < nc; ++ic) {
+    for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
+      double dx1 = c->cofg[3 * ic] - xc, dy1 = c->cofg[3 * ic + 1] - yc, dz1 = c->cofg[3 * ic + 2] - zc;
+      for (int iv = 0; iv < 5; ++iv) {
+        if (skipVel && iv >= 1 && iv <= 3) continue;
+        double v1 = var[5 * ic + iv];
+        double d1min1 = vmin[5 * ic + iv] - v1, d1max1 = vmax[5 * ic + iv] - v1;
+        const double *g1 = &grad[15 * ic + 3 * iv];
+        double d21 = g1[0] * dx1 + g1[1] * dy1 + g1[2] * dz1;
+        double term;
+        if (d21 > 0.0) { term = fmin2(1.0, d1max1 / d21); lim[5 * ic + iv] = fmin2(term, lim[5 * ic + iv]); }
+        else if (d21 < 0.0) { term = fmin2(1.0, d1min1 / d21); lim[5 * ic + iv] = fmin2(term, lim[5 * ic + iv]); }
+      }
     }
   }
 }
@@ -608,40 +667,30 @@ void limiterVenkat(orc_ctx *c, const std::vector<double> &var, const std::vector
   const double THRD = 1.0 / 3.0, TINY = 1.0e-12, K = 1.0;
   std::vector<double> vmin(var), vmax(var);
   for (int k = 0; k < 5 * nc; ++k) lim[k] = 1.0;
-  for (int f = 0; f < c->nFaces; ++f) {
-    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
-    for (int iv = 0; iv < 5; ++iv) {
-      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
-      vmin[5 * c1 + iv] = fmin2(vmin[5 * c1 + iv], v2);
-      vmin[5 * c2 + iv] = fmin2(vmin[5 * c2 + iv], v1);
-      vmax[5 * c1 + iv] = fmax2(vmax[5 * c1 + iv], v2);
-      vmax[5 * c2 + iv] = fmax2(vmax[5 * c2 + iv], v1);
-    }
-  }
+  neighbourExtremes(c, var, vmin, vmax, false);
   auto venk = [&](double dmm, double d2, double epsq) {
     double numer = (dmm * dmm + epsq) * d2 + 2 * d2 * d2 * dmm;
     double denom = d2 * (dmm * dmm + 2 * d2 * d2 + dmm * d2 + epsq);
     return numer / (denom + TINY);
   };
-  for (int f = 0; f < c->nFaces; ++f) {
-    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
-    double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
-    double dx1 = c->cofg[3 * c1] - xc, dy1 = c->cofg[3 * c1 + 1] - yc, dz1 = c->cofg[3 * c1 + 2] - zc;
-    double dx2 = c->cofg[3 * c2] - xc, dy2 = c->cofg[3 * c2 + 1] - yc, dz2 = c->cofg[3 * c2 + 2] - zc;
-    double ds1 = std::pow(c->vol[c1], THRD), ds2 = std::pow(c->vol[c2], THRD);
-    double epsq1 = (K * ds1) * (K * ds1) * (K * ds1);
-    double epsq2 = (K * ds2) * (K * ds2) * (K * ds2);
-    for (int iv = 0; iv < 5; ++iv) {
-      double v1 = var[5 * c1 + iv], v2 = var[5 * c2 + iv];
-      double d1min1 = vmin[5 * c1 + iv] - v1, d1max1 = vmax[5 * c1 + iv] - v1;
-      double d1min2 = vmin[5 * c2 + iv] - v2, d1max2 = vmax[5 * c2 + iv] - v2;
-      const double *g1 = &grad[15 * c1 + 3 * iv], *g2 = &grad[15 * c2 + 3 * iv];
-      double d21 = g1[0] * dx1 + g1[1] * dy1 + g1[2] * dz1;
-      double d22 = g2[0] * dx2 + g2[1] * dy2 + g2[2] * dz2;
-      if (d21 > 0.0) lim[5 * c1 + iv] = fmin2(venk(d1max1, d21, epsq1), lim[5 * c1 + iv]);
-      else if (d21 < 0.0) lim[5 * c1 + iv] = fmin2(venk(d1min1, d21, epsq1), lim[5 * c1 + iv]);
-      if (d22 > 0.0) lim[5 * c2 + iv] = fmin2(venk(d1max2, d22, epsq2), lim[5 * c2 + iv]);
-      else if (d22 < 0.0) lim[5 * c2 + iv] = fmin2(venk(d1min2, d22, epsq2), lim[5 * c2 + iv]);
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < nc; ++ic) {
+    for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
+      double dx1 = c->cofg[3 * ic] - xc, dy1 = c->cofg[3 * ic + 1] - yc, dz1 = c->cofg[3 * ic + 2] - zc;
+      double ds1 = std::pow(c->vol[ic], THRD);
+      double epsq1 = (K * ds1) * (K * ds1) * (K * ds1);
+      for (int iv = 0; iv < 5; ++iv) {
+        double v1 = var[5 * ic + iv];
+        double d1min1 = vmin[5 * ic + iv] - v1, d1max1 = vmax[5 * ic + iv] - v1;
+        const double *g1 = &grad[15 * ic + 3 * iv];
+        double d21 = g1[0] * dx1 + g1[1] * dy1 + g1[2] * dz1;
+        if (d21 > 0.0) lim[5 * ic + iv] = fmin2(venk(d1max1, d21, epsq1), lim[5 * ic + iv]);
+        else if (d21 < 0.0) lim[5 * ic + iv] = fmin2(venk(d1min1, d21, epsq1), lim[5 * ic + iv]);
+      }
     }
   }
 }
@@ -714,6 +763,7 @@ void symmetricEigen3(const double m[9], double vec[9], double val[3]) {
 void wenoGradCells(orc_ctx *c, std::vector<double> &grad, bool xyz) {
   const int nc = c->nCells;
   std::vector<double> out(grad.size());
+#pragma omp parallel for schedule(static)
   for (int icg = 0; icg < nc; ++icg) {
     const int sb = c->stOff[icg], se = c->stOff[icg + 1];
     for (int iv = 0; iv < 5; ++iv) {
@@ -764,28 +814,32 @@ void wenoGradCells(orc_ctx *c, std::vector<double> &grad, bool xyz) {
    zeroed when its reconstruction at a face of the cell,
    ((var + gx*dx) + gy*dy) + gz*dz with d = fc - cofg, is <= 0.  The
    reference's face loop stops at the first such face; whether any face
-   does is independent of the order, so the faces are visited face by face
-   here (interior, then the patches) and the gradients zeroed afterwards. */
+   does is independent of the order, so each cell's faces are visited
+   (interior, then the patches) and its gradients zeroed afterwards. */
 void limitGradCellsSimple(orc_ctx *c, const std::vector<double> &var, std::vector<double> &grad) {
   const int nc = c->nCells;
-  std::vector<char> zero(5 * (size_t)nc, 0);
-  auto check = [&](int ic, const double *fcp) {
-    const double dx = fcp[0] - c->cofg[3 * ic], dy = fcp[1] - c->cofg[3 * ic + 1], dz = fcp[2] - c->cofg[3 * ic + 2];
-    for (int iv = 0; iv < 5; iv += 4) {
-      const double *g = &grad[15 * ic + 3 * iv];
-      const double varf = var[5 * ic + iv] + g[0] * dx + g[1] * dy + g[2] * dz;
-      if (varf <= 0.0) zero[5 * ic + iv] = 1;
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < nc; ++ic) {
+    bool zero[5] = {false, false, false, false, false};
+    for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      const double *fcp;
+      if (code >= 0) {
+        fcp = &c->fc[3 * (code >> 1)];
+      } else {
+        const int b = -code - 1;
+        fcp = &c->patches[c->bPatch[b]].fc[3 * c->bFace[b]];
+      }
+      const double dx = fcp[0] - c->cofg[3 * ic], dy = fcp[1] - c->cofg[3 * ic + 1], dz = fcp[2] - c->cofg[3 * ic + 2];
+      for (int iv = 0; iv < 5; iv += 4) {
+        const double *g = &grad[15 * ic + 3 * iv];
+        const double varf = var[5 * ic + iv] + g[0] * dx + g[1] * dy + g[2] * dz;
+        if (varf <= 0.0) zero[iv] = true;
+      }
     }
-  };
-  for (int f = 0; f < c->nFaces; ++f) {
-    check(c->f2c[2 * f], &c->fc[3 * f]);
-    check(c->f2c[2 * f + 1], &c->fc[3 * f]);
-  }
-  for (const Patch &p : c->patches)
-    for (size_t b = 0; b < p.bf2c.size(); ++b) check(p.bf2c[b], &p.fc[3 * b]);
-  for (int ic = 0; ic < nc; ++ic)
     for (int iv = 0; iv < 5; ++iv)
-      if (zero[5 * ic + iv]) grad[15 * ic + 3 * iv] = grad[15 * ic + 3 * iv + 1] = grad[15 * ic + 3 * iv + 2] = 0.0;
+      if (zero[iv]) grad[15 * ic + 3 * iv] = grad[15 * ic + 3 * iv + 1] = grad[15 * ic + 3 * iv + 2] = 0.0;
+  }
 }
 
 /* RFLU_LimitGradVelocityBarthJesp (:588-790). gradVel(iComp,dir) = grad(dir, 2+iComp). */
@@ -795,18 +849,23 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
   const double EQUAL_EIG_TOL = 1.0e-3;
   std::vector<double> axes(9 * nc), eig(3 * nc), alpha(3 * nc, 1.0), dmin(3 * nc, 0.0), dmax(3 * nc, 0.0);
   auto gv = [&](int ic, int i, int j) -> double & { return grad[15 * ic + 3 * (1 + (i - 1)) + (j - 1)]; };
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < nc; ++ic) {
     double S[9];
     for (int i = 1; i <= 3; ++i)
       for (int j = 1; j <= 3; ++j) S[(i - 1) + 3 * (j - 1)] = 0.5 * (gv(ic, i, j) + gv(ic, j, i));
     symmetricEigen3(S, &axes[9 * ic], &eig[3 * ic]);
   }
-  for (int f = 0; f < c->nFaces; ++f) {
-    int cc[2] = {c->f2c[2 * f], c->f2c[2 * f + 1]};
-    double du[3];
-    for (int k = 0; k < 3; ++k) du[k] = var[5 * cc[1] + 1 + k] - var[5 * cc[0] + 1 + k];
-    for (int side = 0; side < 2; ++side) {
-      int icl = cc[side];
+  /* both face loops per cell (icl) over its interior faces in face order */
+#pragma omp parallel for schedule(static)
+  for (int icl = 0; icl < nc; ++icl) {
+    for (int e = c->cfOff[icl]; e < c->cfOff[icl + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      if (code < 0) continue;
+      const int f = code >> 1, side = code & 1;
+      int cc[2] = {c->f2c[2 * f], c->f2c[2 * f + 1]};
+      double du[3];
+      for (int k = 0; k < 3; ++k) du[k] = var[5 * cc[1] + 1 + k] - var[5 * cc[0] + 1 + k];
       for (int j = 0; j < 3; ++j) {
         const double *a = &axes[9 * icl + 3 * j];
         double proj = 0.0;
@@ -817,9 +876,12 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
       }
     }
   }
-  for (int f = 0; f < c->nFaces; ++f) {
-    for (int side = 0; side < 2; ++side) {
-      int icl = c->f2c[2 * f + side];
+#pragma omp parallel for schedule(static)
+  for (int icl = 0; icl < nc; ++icl) {
+    for (int e = c->cfOff[icl]; e < c->cfOff[icl + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      if (code < 0) continue;
+      const int f = code >> 1;
       double off[3];
       for (int k = 0; k < 3; ++k) off[k] = c->cofg[3 * icl + k] - c->fc[3 * f + k];
       double shift[3];
@@ -837,6 +899,7 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
       }
     }
   }
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < nc; ++ic) {
     double *e = &eig[3 * ic], *al = &alpha[3 * ic];
     double mx = std::fabs(e[0]);
@@ -852,6 +915,7 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
       double m = fmin2(al[1], al[2]); al[1] = al[2] = m;
     }
   }
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < nc; ++ic) {
     const double *A = &axes[9 * ic];
     double G[3][3], Rm[3][3];
@@ -885,6 +949,7 @@ void cellGradients(orc_ctx *c) {
   if (c->num.spaceOrder <= 1) return;
   const int nc = c->nCells;
   /* RFLU_ConvertCvCons2Prim, DUVWP (modflu/RFLU_ModConvertCv.F90:124-397) */
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < nc; ++ic) {
     double *cv = &c->cv[5 * ic];
     double ir = 1.0 / cv[0];
@@ -911,6 +976,7 @@ void cellGradients(orc_ctx *c) {
   }
   if (c->num.reconst == 10 || c->num.reconst == 100 || c->num.reconst == 11) {
     /* RFLU_LimitGradCells (RFLU_ModLimiters.F90:1061-1146) */
+#pragma omp parallel for schedule(static)
     for (int ic = 0; ic < nc; ++ic)
       for (int iv = 0; iv < 5; ++iv) {
         double l = c->lim[5 * ic + iv];
@@ -920,6 +986,7 @@ void cellGradients(orc_ctx *c) {
   }
   /* RFLU_ConvertCvPrim2Cons (RFLU_ModConvertCv.F90:545-575) */
   double gc = MixtPerf_R_M(c->gvMol), g = MixtPerf_G_CpR(c->gvCp, gc);
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < nc; ++ic) {
     double *cv = &c->cv[5 * ic];
     double r = cv[0], u = cv[1], v = cv[2], w = cv[3], p = c->dv[3 * ic];
@@ -1226,23 +1293,34 @@ void patchFlux(orc_ctx *c, const Patch &p, int i, double flx[5]) {
 }
 
 /* ConvectiveFluxes (libfloflu/ConvectiveFluxes.F90:120-175): rhs = -diss,
- * interior face loop with the +/- scatter, then the patch loop. */
+ * interior face loop with the +/- scatter (rhs(c1) += F, rhs(c2) -= F), then
+ * the patch loop (slip walls leave rhs(DENS)).  The face fluxes are formed
+ * first; each cell then adds its faces' contributions in the loops' order. */
 void convectiveFluxes(orc_ctx *c) {
-  const int nc = c->nCells;
-  for (int k = 0; k < 5 * nc; ++k) c->rhs[k] = -c->diss[k];
-  double flx[5];
-  for (int f = 0; f < c->nFaces; ++f) {
-    interiorFlux(c, f, flx);
-    int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
-    for (int k = 0; k < 5; ++k) c->rhs[5 * c1 + k] = c->rhs[5 * c1 + k] + flx[k];
-    for (int k = 0; k < 5; ++k) c->rhs[5 * c2 + k] = c->rhs[5 * c2 + k] - flx[k];
-  }
-  for (const Patch &p : c->patches) {
-    for (int i = 0; i < p.n; ++i) {
-      patchFlux(c, p, i, flx);
-      int c1 = p.bf2c[i];
-      int k0 = (p.bcType == ORC_BC_SLIPWALL) ? 1 : 0;
-      for (int k = k0; k < 5; ++k) c->rhs[5 * c1 + k] = c->rhs[5 * c1 + k] + flx[k];
+  const int nc = c->nCells, nf = c->nFaces, nb = (int)c->bPatch.size();
+#pragma omp parallel for schedule(static)
+  for (int f = 0; f < nf; ++f) interiorFlux(c, f, &c->flux[5 * (size_t)f]);
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < nb; ++b)
+    patchFlux(c, c->patches[c->bPatch[b]], c->bFace[b], &c->flux[5 * ((size_t)nf + b)]);
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < nc; ++ic) {
+    double *rhs = &c->rhs[5 * ic];
+    for (int k = 0; k < 5; ++k) rhs[k] = -c->diss[5 * ic + k];
+    for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      if (code >= 0) {
+        const double *flx = &c->flux[5 * (size_t)(code >> 1)];
+        if (code & 1)
+          for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] - flx[k];
+        else
+          for (int k = 0; k < 5; ++k) rhs[k] = rhs[k] + flx[k];
+      } else {
+        const int b = -code - 1;
+        const double *flx = &c->flux[5 * ((size_t)nf + b)];
+        const int k0 = (c->patches[c->bPatch[b]].bcType == ORC_BC_SLIPWALL) ? 1 : 0;
+        for (int k = k0; k < 5; ++k) rhs[k] = rhs[k] + flx[k];
+      }
     }
   }
 }
@@ -1251,8 +1329,10 @@ void convectiveFluxes(orc_ctx *c) {
 void rkInit(orc_ctx *c, int iStage) {
   const int n = 5 * c->nCells;
   if (c->num.rkScheme == 1 && iStage != 1) {
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < n; ++k) c->diss[k] = 0.0;
   } else {
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < n; ++k) { c->cvOld[k] = c->cv[k]; c->diss[k] = 0.0; }
   }
 }
@@ -1261,6 +1341,7 @@ void rkInit(orc_ctx *c, int iStage) {
 void rkUpdate(orc_ctx *c, int iStage, double dtMin) {
   const double fac = c->ark[iStage - 1] * dtMin;
   const double grk = c->grk[iStage - 1];
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < c->nCells; ++ic) {
     double adtv = fac / c->vol[ic];
     for (int iv = 0; iv < 5; ++iv) {
@@ -1290,16 +1371,19 @@ void rkUpdate(orc_ctx *c, int iStage, double dtMin) {
  * (libflu/RFLU_CheckPositivity.F90:173-193). */
 void afterUpdate(orc_ctx *c) {
   const int nc = c->nCells;
+  long long nNan = 0, nNegP = 0, nPosFix = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nNan)
   for (int ic = 0; ic < nc; ++ic) {
     const double *cv = &c->cv[5 * ic];
     double rho = cv[0], rrho = 1.0 / rho;
     double u = rrho * cv[1], v = rrho * cv[2], w = rrho * cv[3];
     double p = c->dv[3 * ic], t = c->dv[3 * ic + 1];
     if (std::isnan(rho) || std::isnan(u) || std::isnan(v) || std::isnan(w) || std::isnan(p) || std::isnan(t))
-      c->nanCount++;
+      nNan++;
   }
   const double pTol = 1.0e-12;
   double rgas = MixtPerf_R_M(c->gvMol), gamma = MixtPerf_G_CpR(c->gvCp, rgas);
+#pragma omp parallel for schedule(static) reduction(+ : nNegP)
   for (int ic = 0; ic < nc; ++ic) {
     double *cv = &c->cv[5 * ic];
     double r = cv[0], ir = 1.0 / r;
@@ -1308,11 +1392,12 @@ void afterUpdate(orc_ctx *c) {
     double Vm2 = u * u + v * v + w * w;
     double p = MixtPerf_P_DEoGVm2(r, Eo, gamma, Vm2);
     if (p <= 0.0 && std::fabs(p) <= pTol) {
-      c->negPCount++;
+      nNegP++;
       p = pTol;
       cv[4] = r * MixtPerf_Eo_DGPUVW(r, gamma, p, u, v, w);
     }
   }
+#pragma omp parallel for schedule(static) reduction(+ : nPosFix)
   for (int ic = 0; ic < nc; ++ic) {
     double *cv = &c->cv[5 * ic];
     double rho = cv[0], rrho = 1.0 / rho;
@@ -1320,12 +1405,15 @@ void afterUpdate(orc_ctx *c) {
     double Vm2 = u * u + v * v + w * w;
     double p = c->dv[3 * ic];
     if (p <= 0.0) {
-      c->posFixCount++;
+      nPosFix++;
       double Eo = 1.0e4 + 0.5 * Vm2;
       cv[4] = rho * Eo;
       setDependentVars(c, ic);
     }
   }
+  c->nanCount += nNan;
+  c->negPCount += nNegP;
+  c->posFixCount += nPosFix;
 }
 
 void rkStage(orc_ctx *c, int iStage, double dtMin) {
@@ -1333,6 +1421,7 @@ void rkStage(orc_ctx *c, int iStage, double dtMin) {
   cellGradients(c);
   convectiveFluxes(c);
   rkUpdate(c, iStage, dtMin);
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < c->nCells; ++ic) setDependentVars(c, ic);
   afterUpdate(c);
 }
@@ -1340,9 +1429,12 @@ void rkStage(orc_ctx *c, int iStage, double dtMin) {
 /* RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:120-333) and
  * RFLU_MinimumTimeStep (rocflu/RFLU_MinimumTimeStep.F90:100-245), one region. */
 double timeStep(orc_ctx *c, double currentTime) {
-  const int nc = c->nCells;
-  std::vector<double> dt(nc, 0.0);
-  for (int f = 0; f < c->nFaces; ++f) {
+  const int nc = c->nCells, nf = c->nFaces;
+  std::vector<double> dt(nc, 0.0), srad(nf);
+  /* the interior faces' spectral radius, added to both cells (c1, then c2
+     in the reference's loop), then each patch face's to its cell */
+#pragma omp parallel for schedule(static)
+  for (int f = 0; f < nf; ++f) {
     int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
     double nx = c->fn[4 * f], ny = c->fn[4 * f + 1], nz = c->fn[4 * f + 2], nm = c->fn[4 * f + 3];
     double fsu = 0.0;
@@ -1353,13 +1445,19 @@ double timeStep(orc_ctx *c, double currentTime) {
     double a2 = c->dv[3 * c2 + 2];
     double vc = 0.5 * ((u1 + u2) * nx + (v1 + v2) * ny + (w1 + w2) * nz);
     double as = 0.5 * (a1 + a2);
-    double srad = (std::fabs(vc - fsu) + as) * nm;
-    dt[c1] = dt[c1] + srad;
-    dt[c2] = dt[c2] + srad;
+    srad[f] = (std::fabs(vc - fsu) + as) * nm;
   }
-  for (const Patch &p : c->patches) {
-    for (int i = 0; i < p.n; ++i) {
-      int c1 = p.bf2c[i];
+#pragma omp parallel for schedule(static)
+  for (int ic = 0; ic < nc; ++ic) {
+    for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
+      const int code = c->cfEnt[e];
+      if (code >= 0) {
+        dt[ic] = dt[ic] + srad[code >> 1];
+        continue;
+      }
+      const int b = -code - 1;
+      const Patch &p = c->patches[c->bPatch[b]];
+      const int i = c->bFace[b], c1 = ic;
       double nx = p.fn[4 * i], ny = p.fn[4 * i + 1], nz = p.fn[4 * i + 2], nm = p.fn[4 * i + 3];
       double fsu = 0.0;
       double ir1 = 1.0 / c->cv[5 * c1];
@@ -1368,12 +1466,10 @@ double timeStep(orc_ctx *c, double currentTime) {
       double vc = u1 * nx + v1 * ny + w1 * nz;
       dt[c1] = dt[c1] + (std::fabs(vc - fsu) + a1) * nm;
     }
+    dt[ic] = c->vol[ic] / dt[ic];
   }
   double dtMin = 1.79769313486231571e308;
-  for (int ic = 0; ic < nc; ++ic) {
-    dt[ic] = c->vol[ic] / dt[ic];
-    dtMin = fmin2(dtMin, dt[ic]);
-  }
+  for (int ic = 0; ic < nc; ++ic) dtMin = fmin2(dtMin, dt[ic]);
   /* RFLU_MinimumTimeStep */
   double cfl = c->num.cfl;
   if (c->num.rkScheme == 1) cfl = fmin2(cfl, 3.0);
@@ -1413,6 +1509,7 @@ orc_ctx *orc_create(const orc_mesh_desc *m, const orc_num_desc *num) {
   }
   c->num = *num;
   buildFaceList(c);
+  buildCellFaces(c);
   buildGeometry(c);
   if (num->spaceOrder > 1) {
     buildStencils(c);
@@ -1476,6 +1573,7 @@ void orc_get_stencil(orc_ctx *c, int *off, int *idx, double *moms) {
 
 void orc_set_state(orc_ctx *c, const double *cv) {
   std::memcpy(c->cv.data(), cv, sizeof(double) * 5 * c->nCells);
+#pragma omp parallel for schedule(static)
   for (int ic = 0; ic < c->nCells; ++ic) setDependentVars(c, ic);
 }
 void orc_get_state(orc_ctx *c, double *cv, double *dv) {
@@ -1515,6 +1613,23 @@ int orc_run(orc_ctx *c, int nSteps, double *time, double endTime) {
 void orc_run_fixed_dt(orc_ctx *c, int nSteps, double dt) {
   for (int n = 0; n < nSteps; ++n)
     for (int s = 1; s <= c->nrkSteps; ++s) rkStage(c, s, dt);
+}
+
+void orc_set_dt_imposed(orc_ctx *c, double dt) { c->num.dtImposed = dt; }
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int orc_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
 }
 
 void orc_counters(orc_ctx *c, long long *posFix, long long *negP, long long *nan) {

@@ -96,6 +96,15 @@ int orc_run(orc_ctx *c, int nSteps, double *time, double endTime);
 void orc_run_fixed_dt(orc_ctx *c, int nSteps, double dt);
 int orc_nstages(orc_ctx *c);
 
+/* Replaces TIMESTEP (the imposed first time step) of the numerics. */
+void orc_set_dt_imposed(orc_ctx *c, double dt);
+
+/* Threads of the OpenMP loops (every call of this process); n <= 0 keeps
+ * the current count.  orc_threads: the count the next loop will use (1 when
+ * built without OpenMP).  Results do not depend on the count. */
+void orc_set_threads(int n);
+int orc_threads(void);
+
 /* Positivity / bounds counters accumulated since creation. */
 void orc_counters(orc_ctx *c, long long *posFix, long long *negP, long long *nan);
 

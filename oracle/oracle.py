@@ -33,11 +33,12 @@ class NumDesc(C.Structure):
 
 def build():
     """Compile oracle.cpp as the committed Makefile does (-O2
-    -ffp-contract=off); g++ is called directly so make is not required."""
+    -ffp-contract=off -fopenmp); g++ is called directly so make is not
+    required."""
     out = os.path.join(_HERE, "_build")
     os.makedirs(out, exist_ok=True)
     tmp = os.path.join(out, "liboracle.so.tmp")
-    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-std=c++17", "-shared", "-o", tmp,
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-std=c++17", "-shared", "-o", tmp,
                     os.path.join(_HERE, "oracle.cpp")], check=True)
     os.replace(tmp, os.path.join(out, "liboracle.so"))
 
@@ -77,12 +78,28 @@ def lib():
         L.orc_get_grad.argtypes = [P, DP]
         L.orc_residual.argtypes = [P, DP, DP]
         L.orc_counters.argtypes = [P, LLP, LLP, LLP]
+        L.orc_set_dt_imposed.argtypes = [P, C.c_double]
+        L.orc_set_dt_imposed.restype = None
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_threads.restype = None
+        L.orc_threads.argtypes = []
+        L.orc_threads.restype = C.c_int
         for name in ("orc_get_faces", "orc_get_cells", "orc_get_patch", "orc_get_stencil", "orc_set_state",
                      "orc_get_state", "orc_get_rhs", "orc_get_grad", "orc_residual", "orc_counters",
                      "orc_rk_stage", "orc_run_fixed_dt", "orc_destroy"):
             getattr(L, name).restype = None
         _LIB = L
     return _LIB
+
+
+def set_threads(n):
+    """Threads of the oracle's OpenMP loops in this process (results do not
+    depend on it)."""
+    lib().orc_set_threads(int(n))
+
+
+def threads():
+    return lib().orc_threads()
 
 
 def _ptr(a, t):
@@ -190,6 +207,14 @@ class Oracle:
         tt = C.c_double(t)
         done = lib().orc_run(self.h, n_steps, C.byref(tt), end_time)
         return done, tt.value
+
+    def n_stages(self):
+        return lib().orc_nstages(self.h)
+
+    def set_dt_imposed(self, dt):
+        """TIMESTEP, the imposed first time step (the numerics are copied at
+        creation)."""
+        lib().orc_set_dt_imposed(self.h, dt)
 
     def run_fixed_dt(self, n_steps, dt):
         lib().orc_run_fixed_dt(self.h, n_steps, dt)

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <initializer_list>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -16,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/rflu_gpu.h"
+#include "args.h"
 #include "convert.cuh"
 #include "ctx.h"
 #include "errors.h"
@@ -149,14 +151,19 @@ int staticScratchAddress(void **out) {
   return RFLU_OK;
 }
 
-// True when p is device (or managed) memory the kernels may read or write.
-bool isDevicePointer(const void *p) {
+// The kind of memory p points to and the device it lives on.
+ArgMem pointerKind(const void *p, int *device) {
   cudaPointerAttributes a;
+  *device = -1;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return ArgMem::Unknown;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  *device = a.device;
+  if (a.type == cudaMemoryTypeDevice) return ArgMem::Device;
+  if (a.type == cudaMemoryTypeManaged) return ArgMem::Managed;
+  if (a.type == cudaMemoryTypeHost) return ArgMem::Host;
+  return ArgMem::Unknown;
 }
 
 // FP64 FMA throughput probe: 8 independent chains per thread.
@@ -254,6 +261,7 @@ struct CtxBase {
   virtual int unrolledAdjoint(const double *cv0, int nSteps, double dt, int every, int iPatch, double *J,
                               double *cvBar0, double *stats) = 0;
   cudaStream_t stream = nullptr;
+  int device = -1;  // the device the context was created on
   // host transfers: the copy stream and one event per chunk (+ one)
   static constexpr int kMaxChunks = 8;
   cudaStream_t copyStream = nullptr;
@@ -622,8 +630,14 @@ struct Ctx : CtxBase {
   // same call.
   int residualStatic(const double *cvDev, double *rhsDev) override {
     if (!cvDev || !rhsDev) return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: null argument");
-    if (!isDevicePointer(cvDev) || !isDevicePointer(rhsDev))
-      return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: cv and rhs must be device (or managed) memory");
+    int cur = -1;
+    RFLU_CUDA(cudaGetDevice(&cur));
+    for (const void *q : {(const void *)cvDev, (const void *)rhsDev}) {
+      int qDev = -1;
+      const ArgMem kind = pointerKind(q, &qDev);
+      if (const char *why = deviceArgProblem(kind, qDev, device, cur))
+        return fail(RFLU_ERR_ARG, std::string("rflu_gpu_residual_static: ") + why);
+    }
     const size_t nc = V.nc, nT = (size_t)V.nf + V.nb;
     auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t bCv = up(5 * nc * sizeof(double)), bDv = up(3 * nc * sizeof(double));
@@ -912,6 +926,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   const int nc = g->nCells, nf = g->nFaces, np = g->nPatches;
   const int nb = np > 0 ? g->patchFaceOff[np] : 0;
   nPatches = np;
+  RFLU_CUDA(cudaGetDevice(&device));
   RFLU_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   RFLU_CUDA(cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking));
   for (auto &e : chunkEv) RFLU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1118,9 +1133,11 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     // weights formed in the gradient kernel from the R factor and centroids
     PUT(V.cgx, cgx, R); PUT(V.cgy, cgy, R); PUT(V.cgz, cgz, R);
     PUT(V.lsq, lsq, R); PUT(V.ivol, ivol, R);
-    if (num->spaceOrder > 1) {
+    if (num->spaceOrder > 1 && !(num->options & RFLU_OPT_UNTILED)) {
       if ((rc = buildTiles(cfOff, cfEnt, stOff, stIdx, fc1, fc2, fnx, fny, fnz, fnm, dL, dR, bnx, bny, bnz, bnm, bd)))
         return rc;
+    }
+    if (num->spaceOrder > 1) {
       // the width of the adjoint's transposed-stencil weights, allocated and
       // filled with the adjoint workspace on the first adjoint call
       int w = 0;
@@ -1218,6 +1235,7 @@ int rflu_gpu_create(const rflu_grid_desc *grid, const rflu_num_desc *num, rflu_g
     return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: RECONST must be 0, 1, 2, 10, 11 or 100");
   if (num->rkScheme < 1 || num->rkScheme > 3) return fail(RFLU_ERR_ARG, "rflu_gpu_create: RKSCHEME must be 1, 2 or 3");
   if (num->precision < 0 || num->precision > 2) return fail(RFLU_ERR_ARG, "rflu_gpu_create: bad precision");
+  if (num->options & ~RFLU_OPT_UNTILED) return fail(RFLU_ERR_ARG, "rflu_gpu_create: unknown option bits");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(RFLU_ERR_CUDA, "rflu_gpu_create: no CUDA device");
   rflu_gpu_ctx *c = new (std::nothrow) rflu_gpu_ctx();
@@ -1359,6 +1377,13 @@ int rflu_gpu_check_conversions(long long n, unsigned long long seed, unsigned lo
   }
   cudaFree(bad);
   if (err != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("rflu_gpu_check_conversions: ") + cudaGetErrorString(err));
+  return RFLU_OK;
+}
+
+int rflu_gpu_check_refinements(long long n, unsigned long long seed, double *maxRelErr) {
+  if (!maxRelErr || n < 0) return fail(RFLU_ERR_ARG, "rflu_gpu_check_refinements: bad argument");
+  const cudaError_t e = rflu::mixedRefineCheck(n, seed, maxRelErr);
+  if (e != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("rflu_gpu_check_refinements: ") + cudaGetErrorString(e));
   return RFLU_OK;
 }
 

@@ -268,18 +268,32 @@ __device__ inline void loadFlux(const T *flux, size_t nT, int t, T *f) {
 }
 
 
+// FP64 reciprocal of x from an FP32 seed y ~ 1/x: one Newton-Raphson step
+// y + y*(1 - x*y).  The error of the seed (rounding x to FP32 and the
+// approximate FP32 division, ~2^-22 relative) is squared: ~2^-44.
+__device__ inline double refinedRecip(double x, float seed) {
+  const double y = f2d(seed);
+  return fma(y, fma(-x, y, 1.0), y);
+}
+// FP64 square root of x > 0 from an FP32 reciprocal-square-root seed y: h =
+// x*y, then h + h*(1 - h*y)/2 (relative error 1.5 e^2 for a seed error e).
+__device__ inline double refinedSqrt(double x) {
+  const double y = f2d(rsqrtf(d2f(x)));
+  const double h = x * y;
+  return fma(0.5 * h, fma(-h, y, 1.0), h);
+}
+
 // Mixed mode: primitive state from the FP64 master cv.  1/rho from an FP32
-// seed y (also the FP32 velocities' reciprocal) refined once in FP64,
-// y + y*(1 - rho*y) (quadratic convergence: ~2^-44), and the pressure in FP64
-// from the kinetic energy (the cancellation at strong shocks).
+// seed (also the FP32 velocities' reciprocal) refined once in FP64
+// (refinedRecip), and the pressure in FP64 from the kinetic energy (the
+// cancellation at strong shocks).
 struct MixedPrim {
   float rf, irf, uf, vf, wf;
   double ir, ke, pr;
   __device__ MixedPrim(const Params &P, const double *cv) {
     rf = d2f(cv[0]);
     irf = 1.0f / rf;
-    ir = f2d(irf);
-    ir = fma(ir, fma(-cv[0], ir, 1.0), ir);
+    ir = refinedRecip(cv[0], irf);
     const double msq = cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3];
     ke = 0.5 * msq * ir;
     pr = (P.gRT - 1.0) * (cv[4] - ke);
@@ -1923,12 +1937,8 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
   for (int k = 0; k < 5; ++k) V.cv[k * n + i] = cv[k];
   V.dv[i] = pr;
   if (!P.dvPOnly) {
-    const double c2 = P.gRT * pr * ir;
-    // sqrt(c2): FP32 seed y ~ 1/sqrt(c2), h = c2*y, then h + h*(1 - h*y)/2
-    const double y = f2d(rsqrtf(d2f(c2)));
-    const double h = c2 * y;
     V.dv[n + i] = pr * ir * P.igcR;
-    V.dv[2 * n + i] = fma(0.5 * h, fma(-h, y, 1.0), h);
+    V.dv[2 * n + i] = refinedSqrt(P.gRT * pr * ir);
   }
   storePrimRec(V, i, (R)rf, (R)uf, (R)vf, (R)wf, (R)d2f(pr));
 }
@@ -2071,6 +2081,33 @@ __global__ void kStepEnd(View<R> V) {
   if (V.sc->finished < 0) return;
   V.sc->time = V.sc->time + V.sc->dtMin;
   V.sc->stepsDone += 1;
+}
+
+// Self-check of refinedRecip and refinedSqrt against IEEE FP64 division and
+// square root, compiled with this translation unit's flags (the FP32 seeds of
+// the mixed mode use its approximate division): x = 2^e * m with m uniform in
+// [1, 2) and e uniform in [-emax, emax] from a 64-bit hash of (seed, k); the
+// largest relative error of each, as the bits of a positive double
+// (monotone in the value), in out[0] and out[1].
+__device__ inline unsigned long long refineHash(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+__global__ void kRefineCheck(long long n, unsigned long long seed, int emax, unsigned long long *out) {
+  double eR = 0.0, eS = 0.0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long h = refineHash(seed ^ refineHash((unsigned long long)k));
+    const int e = (int)((h >> 52) % (unsigned long long)(2 * emax + 1)) - emax;
+    const double x = ldexp(1.0 + (double)(h & 0xFFFFFFFFFFFFFull) * 0x1p-52, e);
+    const double r = refinedRecip(x, 1.0f / d2f(x));
+    eR = fmax(eR, fabs(r - 1.0 / x) * x);
+    const double sx = sqrt(x);
+    eS = fmax(eS, fabs(refinedSqrt(x) - sx) / sx);
+  }
+  atomicMax(&out[0], (unsigned long long)__double_as_longlong(eR));
+  atomicMax(&out[1], (unsigned long long)__double_as_longlong(eS));
 }
 
 // ---------------------------------------------------------------------------

@@ -30,6 +30,11 @@ struct Ops {
   void (*adjointSetup)(const View<R> &, cudaStream_t);
 };
 
+// The mixed mode's Newton-refined FP64 reciprocal and square root against
+// IEEE FP64 division and sqrt on n generated values: the largest relative
+// errors (kernels_mixed.cu).
+cudaError_t mixedRefineCheck(long long n, unsigned long long seed, double *maxRel);
+
 const Ops<double> *opsFp64();
 const Ops<double> *opsFp64Exact();
 const Ops<float> *opsMixed();

@@ -45,7 +45,10 @@ class NumDesc(C.Structure):
     _fields_ = [("spaceOrder", C.c_int), ("spaceDiscr", C.c_int), ("reconst", C.c_int), ("rkScheme", C.c_int),
                 ("piclBuild", C.c_int), ("precision", C.c_int), ("cp", C.c_double), ("gamma", C.c_double),
                 ("cfl", C.c_double), ("epsEntr", C.c_double), ("dissFact", C.c_double),
-                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double)]
+                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double), ("options", C.c_int)]
+
+
+OPT_UNTILED = 1
 
 
 class Status(C.Structure):
@@ -69,7 +72,7 @@ EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_g
            "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
            "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_residual", "rflu_gpu_vjp",
            "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_unrolled_adjoint", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
-           "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_gpu_check_conversions", "rflu_setup_build", "rflu_setup_grid",
+           "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_gpu_check_conversions", "rflu_gpu_check_refinements", "rflu_setup_build", "rflu_setup_grid",
            "rflu_setup_destroy")
 
 
@@ -113,6 +116,7 @@ def lib(build_if_missing=True):
     L.rflu_gpu_adjoint_times.argtypes = [P, I, DP]
     L.rflu_gpu_fp64_rate.argtypes = [DP]
     L.rflu_gpu_check_conversions.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong)]
+    L.rflu_gpu_check_refinements.argtypes = [C.c_longlong, C.c_ulonglong, DP]
     L.rflu_setup_build.argtypes = [C.POINTER(MeshDesc), I, C.POINTER(P)]
     L.rflu_setup_grid.argtypes = [P, C.POINTER(GridDesc)]
     L.rflu_setup_destroy.argtypes = [P]
@@ -134,10 +138,10 @@ def _p(a, t=C.c_double):
     return a.ctypes.data_as(C.POINTER(t))
 
 
-def num_desc(num, precision):
+def num_desc(num, precision, options=0):
     return NumDesc(num.space_order, num.space_discr, num.reconst, num.rk_scheme, num.picl_build,
                    PREC[precision] if isinstance(precision, str) else int(precision), num.cp, num.gamma, num.cfl,
-                   num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit)
+                   num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit, int(options))
 
 
 class Setup:
@@ -189,10 +193,11 @@ class Region:
     """Device mirror of one region (t_region) in the given precision:
     'fp64', 'fp64_exact' or 'mixed'."""
 
-    def __init__(self, case, precision="fp64", grid=None):
+    def __init__(self, case, precision="fp64", grid=None, options=0):
         """grid: the reference's setup products (an object with f2c (1-based),
         fn, fc, vol, cofg, bf2c (1-based), bfn, bfc, patch_off, c2cs_off,
-        c2cs (1-based), moms); built by rflu_setup_build when omitted."""
+        c2cs (1-based), moms); built by rflu_setup_build when omitted.
+        options: rflu_num_desc::options bits (OPT_UNTILED)."""
         L = lib()
         self.case = case
         self.precision = precision
@@ -219,7 +224,7 @@ class Region:
                       _p(a["cofg"]), len(case.patches), _p(a["off"], C.c_int), _p(a["bf2c"], C.c_int), _p(a["bfn"]),
                       _p(a["bfc"]), _p(a["pt"], C.c_int), _p(a["po"], C.c_int), _p(a["pp"]), _p(a["pr"], C.c_int),
                       _p(a["soff"], C.c_int), _p(a["smem"], C.c_int), _p(a["moms"]))
-        self.nd = num_desc(case.num, precision)
+        self.nd = num_desc(case.num, precision, options)
         h = C.c_void_p()
         _check(L.rflu_gpu_create(C.byref(gd), C.byref(self.nd), C.byref(h)))
         self.h = h
@@ -356,6 +361,14 @@ def check_conversions(n, seed=1):
     m = C.c_ulonglong()
     _check(lib().rflu_gpu_check_conversions(n, seed, C.byref(m)))
     return m.value
+
+
+def check_refinements(n, seed=1):
+    """Largest relative errors of the mixed mode's Newton-refined FP64
+    reciprocal and square root against IEEE division and sqrt."""
+    out = np.zeros(2)
+    _check(lib().rflu_gpu_check_refinements(n, seed, _p(out)))
+    return float(out[0]), float(out[1])
 
 
 # --- the reference's subroutine names ---------------------------------------

@@ -48,13 +48,15 @@ def test_reference_arm_other_ranks_exit_quietly():
 
 
 def test_reference_arm_line_on_one_rank():
-    """The reference arm on rank 0 (CPU only, a tiny sample): one JSON line
-    with the ours-arm's metric and unit, impl 'reference', a cpu_baseline
-    describing the run and an e2e without host transfers."""
+    """The reference arm on rank 0 (CPU only, a tiny mesh): one JSON line
+    with the ours-arm's metric, unit and workload config, impl 'reference',
+    a cpu_baseline describing the run and an e2e without host transfers."""
+    sys.path.insert(0, ROOT)
+    import bench
+
     env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
-    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "3", "--cpu-n", "8", "--cpu-steps", "1"], env=env, capture_output=True, text=True,
-                       timeout=600)
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2",
+                        "--warmup", "3", "--n", "8"], env=env, capture_output=True, text=True, timeout=600)
     assert p.returncode == 0, p.stderr
     lines = [ln for ln in p.stdout.strip().splitlines() if ln.startswith("{")]
     assert len(lines) == 1
@@ -65,3 +67,6 @@ def test_reference_arm_line_on_one_rank():
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # the same workload block the device arm prints for this mesh
+    assert d["config"] == bench.workload_config(8, 512, 3 * 8 * 8 * 7, 1)
+    assert d["steps"] == 2 and d["ms_per_step"] > 0

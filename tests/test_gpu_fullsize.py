@@ -4,8 +4,8 @@ on smaller meshes in test_gpu_parity.py):
 
 * C3, 128^3 hexes (2,097,152 cells), shock-sphere, HLLC + BJ eigenframe
   limiter: the mixed path's density and pressure L1 error against the FP64
-  path after 10 steps (target <= 1e-5), and bit-identical reruns (no atomics
-  anywhere on the path);
+  path after 10 steps and after the configured 500 steps (target <= 1e-5),
+  and bit-identical reruns (no atomics anywhere on the path);
 * C2 mesh, 64^3 x 6 jittered tetrahedra (1,572,864 cells), HLLC +
   Venkatakrishnan, a p = 4 blast: a closed slip-wall box, so every step
   conserves the totals of mass and energy as long as no cell takes the
@@ -48,6 +48,29 @@ def test_c3_mixed_accuracy_and_reruns(gpu_lib):
         r.step(10, 0.0)
         again, _ = r.download()
         np.testing.assert_array_equal(again, ref)
+
+
+def test_c3_mixed_accuracy_after_500_steps(gpu_lib):
+    """The configuration's full run: 500 steps of the mixed and the FP64
+    path from the same initial state (CFL time step each step); the shock
+    crosses the sphere on the way.  L1 of density and pressure against the
+    FP64 path <= 1e-5, no invalid or floored cells in either."""
+    c = cases.shock_sphere(128)
+    probe = gpu.Region(c, "fp64")
+    c.num.dt_imposed = probe.timestep(1.0)
+    probe.close()
+    out = {}
+    for prec in ("fp64", "mixed"):
+        r = gpu.Region(c, prec)
+        n, t, rc = r.step(500, 0.0)
+        st = r.status()
+        assert n == 500 and rc == 0 and st["nanCells"] == 0 and st["posFixCells"] == 0, st
+        out[prec] = r.download() + (t,)
+        r.close()
+    (cv64, dv64, t64), (cvm, dvm, tm) = out["fp64"], out["mixed"]
+    assert abs(tm - t64) <= 1e-5 * t64  # the mixed time step is an FP32 sum
+    assert np.abs(cvm[:, 0] - cv64[:, 0]).mean() <= 1e-5
+    assert np.abs(dvm[:, 0] - dv64[:, 0]).mean() <= 1e-5
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed", 1e-8)])

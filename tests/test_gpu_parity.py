@@ -252,14 +252,17 @@ def test_mixed_precision_density_error(gpu_lib):
     assert np.abs(dva[:, 0] - dvb[:, 0]).mean() / np.abs(dva[:, 0]).mean() < 1e-4
 
 
+@pytest.mark.parametrize("layout", ["tiled", "untiled"])
 @pytest.mark.parametrize("mesh", ["hex", "tets"])
 @pytest.mark.parametrize("reconst", LIMITERS)
 @pytest.mark.parametrize("discr,dname", FLUXES)
-def test_mixed_matches_fp64_all_limiters(gpu_lib, mesh, reconst, discr, dname):
+def test_mixed_matches_fp64_all_limiters(gpu_lib, mesh, reconst, discr, dname, layout):
     """The mixed path (tiled gradient kernel specialised per limiter, packed
-    records) against the FP64 device run, every limiter and flux, hexahedra
-    and jittered tetrahedra: density L1 error <= 1e-5 (Venkatakrishnan 5e-5)
-    after 10 Wray steps from the same state with the same dt."""
+    records; and the gather-based gradient kernels that meshes too irregular
+    for the tile plan take, forced by RFLU_OPT_UNTILED) against the FP64
+    device run, every limiter and flux, hexahedra and jittered tetrahedra:
+    density L1 error <= 1e-5 (Venkatakrishnan 5e-5) after 10 Wray steps from
+    the same state with the same dt."""
     num = cases.Numerics(space_order=2, space_discr=discr, reconst=reconst, cfl=0.4)
     # a blast every flux/limiter pair of the reference scheme carries stably
     # (unlimited second order only across a weak jump)
@@ -271,7 +274,7 @@ def test_mixed_matches_fp64_all_limiters(gpu_lib, mesh, reconst, discr, dname):
     r64 = gpu.Region(c, "fp64")
     dt = r64.timestep(1.0)
     r64.run_fixed_dt(10, dt)
-    rmx = gpu.Region(c, "mixed")
+    rmx = gpu.Region(c, "mixed", options=gpu.OPT_UNTILED if layout == "untiled" else 0)
     rmx.run_fixed_dt(10, dt)
     a, _ = r64.download()
     b, _ = rmx.download()
@@ -369,6 +372,19 @@ def test_mixed_conversions_match_hardware(gpu_lib):
     rounding ties, widened floats and float midpoints)."""
     for seed in (1, 2):
         assert gpu.check_conversions(1 << 26, seed) == 0
+
+
+def test_mixed_newton_refinements_error_bound(gpu_lib):
+    """The mixed update's FP64 1/rho and sound speed come from FP32 seeds
+    (approximate division, rsqrtf) refined by one Newton-Raphson step; over
+    2^24 values 2^e*m (|e| <= 100) per seed they stay within 2^-40 relative
+    of IEEE FP64 division and sqrt (a seed error e becomes ~e^2 ~ 2^-44, plus
+    the FP64 rounding of the step), far below the FP32 increments they
+    multiply."""
+    for seed in (1, 2):
+        rr, rs = gpu.check_refinements(1 << 24, seed)
+        assert 0.0 < rr <= 2.0 ** -40, rr
+        assert 0.0 < rs <= 2.0 ** -40, rs
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])

@@ -261,3 +261,43 @@ def test_gas_jump_closed_box_matches_reference_golden():
     ix = gas_jump.layer_of_cells(c)
     err = np.abs(cv - layers[ix]) / scales
     assert err.max() <= 1e-10, err.max(axis=0)
+
+
+@pytest.mark.parametrize("mesh,discr,reconst,p_in", [
+    ("hex", cases.DISCR_HLLC, cases.RECONST_BJ, None),
+    ("hex", cases.DISCR_AUSM, cases.RECONST_VENKAT, None),
+    ("hex", cases.DISCR_ROE, cases.RECONST_WENO_XYZ, None),
+    ("tet", cases.DISCR_HLLC, cases.RECONST_BJ_COMP, 10.0),
+    ("tet", cases.DISCR_HLLC, cases.RECONST_VENKAT, 100.0),  # NaN cells within a few steps
+])
+def test_oracle_results_independent_of_threads(mesh, discr, reconst, p_in):
+    """The oracle's face loops run as per-cell gathers over each cell's faces
+    in the reference's loop order, so one thread and several give the same
+    bits: residual, gradients, states after whole steps (NaN cells included)
+    and the event counters."""
+    from oracle import oracle as orc
+
+    num = cases.Numerics(space_order=2, space_discr=discr, reconst=reconst, cfl=0.4)
+    if mesh == "hex":
+        c = cases.shock_sphere(10, num=num)
+    else:
+        c = cases.blast_tets(6, num=num, p_in=p_in)
+    c.num.dt_imposed = 1e-3
+    out = []
+    prev = orc.threads()
+    try:
+        for nt in (1, 4):
+            orc.set_threads(nt)
+            o = Oracle(c)
+            rhs, grad = o.residual()
+            done, t = o.run(6, 0.0)
+            cv, dv = o.state()
+            out.append((rhs, grad, t, cv, dv, o.counters()))
+    finally:
+        orc.set_threads(prev)
+    a, b = out
+    for x, y in zip(a, b):
+        if isinstance(x, np.ndarray):
+            np.testing.assert_array_equal(x, y)
+        else:
+            assert x == y
