@@ -16,7 +16,7 @@ RK stages on the device.
   roofline  dominant kernel of the mixed path against the measured HBM copy
          bandwidth
   tets   the same metric on the 64^3 x 6 jittered-tetrahedron blast mesh
-         (1,572,864 cells), HLLC + Venkatakrishnan, mixed and FP64, with
+         (1,572,864 cells), HLLC + Barth-Jespersen, mixed and FP64, with
          its whole-stage roofline at the mesh's measured S and Nf/Nc
   cpu_baseline  the CPU oracle (the FP64 restatement of the reference,
          OpenMP over all host cores) on a bounded sample of the same 128^3
@@ -613,15 +613,17 @@ def accuracy_run(regions, case, n_steps, marks=(100, 250)):
 def tet_block(args, cases, gpu):
     """Throughput on the tetrahedral blast mesh of the 3-D blast
     configuration: 64^3 hexes split into 6 jittered tetrahedra (1,572,864
-    cells, seed 0), HLLC, second order with the Venkatakrishnan limiter,
-    Wray RK3, CFL 0.4, slip walls, at p = 4 inside r < 0.1 (the p = 100 of
-    the configuration drives the reference scheme's face pressures negative
-    within a few steps, the CPU oracle and the device alike).  Mixed and
-    FP64 step rates and each one's whole-stage roofline with this mesh's
-    measured S (stencil members per cell) and Nf/Nc."""
+    cells, seed 0), HLLC, second order, Wray RK3, CFL 0.4, slip walls, at
+    p = 4 inside r < 0.1, with the Barth-Jespersen limiter (RECONST 10).  In
+    the reference scheme the configuration's p = 100 drives face pressures
+    negative within a few steps with every limiter, and at p = 4 the
+    Venkatakrishnan limiter gives non-finite cells from step 5 on (the CPU
+    oracle and the FP64 device path alike); Barth-Jespersen carries p = 4
+    cleanly.  Mixed and FP64 step rates and each one's whole-stage roofline
+    with this mesh's measured S (stencil members per cell) and Nf/Nc."""
     import torch
 
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_VENKAT, cfl=0.4)
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ, cfl=0.4)
     c = cases.blast_tets(args.tet_n, num=num, p_in=4.0)
     t0 = time.time()
     setup = gpu.Setup(c)
@@ -633,7 +635,7 @@ def tet_block(args, cases, gpu):
     sb = stage_bytes_per_cell(nc, nf, nnz)
     peaks, peak_kind = measured_peaks()
     steps, warm = 10, 3
-    out = {"workload": "blast_tets%dx6_hllc_venkat_wray3_p4" % args.tet_n, "cells": nc, "faces": nf,
+    out = {"workload": "blast_tets%dx6_hllc_bj_wray3_p4" % args.tet_n, "cells": nc, "faces": nf,
            "boundary_faces": int(setup.bf2c.shape[0]), "S": sb["S"], "nf_per_nc": sb["nf_per_nc"],
            "steps": steps, "warmup": warm, "setup_s": setup_s, "peak_gbs": peaks["hbm_gbs"], "peak_source": peak_kind}
     for prec in ("mixed", "fp64"):

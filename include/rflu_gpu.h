@@ -137,6 +137,46 @@ int rflu_gpu_step(rflu_gpu_ctx *ctx, int nSteps, double *time, double endTime, i
 /* nSteps RungeKuttaMP calls with a fixed dtMin (no CFL evaluation). */
 int rflu_gpu_run_fixed_dt(rflu_gpu_ctx *ctx, int nSteps, double dtMin);
 
+/* One RK stage at the reference's subroutine granularity, so that the host
+ * can change the residual between the fluxes and the update as
+ * SourceTermsMP and PICL_Runge do (libfloflu/RungeKuttaMP.F90:209-348).
+ * Per stage, in this order:
+ *   rflu_gpu_cell_gradients(ctx)        CellGradientsMP(region)
+ *       (libfloflu/CellGradientsMP.F90:75; modfloflu/ModInterfaces.F90:100-103)
+ *   rflu_gpu_convective_fluxes(ctx)     ConvectiveFluxesMP(region)
+ *       (libfloflu/ConvectiveFluxesMP.F90:73; ModInterfaces.F90:116-119):
+ *       rhs = -diss + the face fluxes, kept on the device
+ *   rflu_gpu_add_rhs(ctx, src, onDevice), any number of times:
+ *       rhs += src, src(5,nCells) in the reference's cell order and the
+ *       units of rhs (SourceTermsMP subtracts vol*S for a source density S);
+ *       the sum is formed in FP64 and stored in the mode's residual type
+ *   rflu_gpu_rk_update(ctx, iStage, dtMin)  RKUpdateMP(region,iReg,istage)
+ *       (libfloflu/RkUpdateMP.F90:75; ModInterfaces.F90:210-214) +
+ *       RFLU_SetVarsContWrapper + AfterUpdateMP; returns RFLU_EVENT_NAN like
+ *       rflu_gpu_rk_stage
+ * RKInitMP (cvOld = cv, diss = 0; RkInitMP.F90:74) needs no call: the
+ * device keeps cv unchanged until the update.  Without source terms the
+ * sequence leaves the state rflu_gpu_rk_stage leaves, bit for bit.  A call
+ * out of this order (fluxes without gradients of the current state, a
+ * source or an update without fluxes) returns RFLU_ERR_STATE; every other
+ * entry point that changes the state or evaluates a residual ends the
+ * sequence.  onDevice = 0: src is host memory, reusable when the call
+ * returns; onDevice = 1: device memory on the context's device (or managed),
+ * which must be complete before the call (it runs on the context's stream
+ * and waits for no other). */
+int rflu_gpu_cell_gradients(rflu_gpu_ctx *ctx);
+int rflu_gpu_convective_fluxes(rflu_gpu_ctx *ctx);
+int rflu_gpu_add_rhs(rflu_gpu_ctx *ctx, const double *src, int onDevice);
+int rflu_gpu_rk_update(rflu_gpu_ctx *ctx, int iStage, double dtMin);
+/* Read-outs of the sequence above in the reference's cell order: rhs(5,nCells)
+ * after rflu_gpu_convective_fluxes (and any rflu_gpu_add_rhs), the limited
+ * gradCell(3,5,nCells) after rflu_gpu_cell_gradients (zero at first order),
+ * as region%mixt%rhs and region%mixt%gradCell hold them there (PICL_Runge
+ * interpolates gradCell).  onDevice as for rflu_gpu_add_rhs; both return
+ * once the data are in place. */
+int rflu_gpu_get_rhs(rflu_gpu_ctx *ctx, double *rhs, int onDevice);
+int rflu_gpu_get_grad(rflu_gpu_ctx *ctx, double *grad, int onDevice);
+
 /* One residual evaluation, CellGradientsMP (libfloflu/CellGradientsMP.F90:75)
  * + ConvectiveFluxesMP (libfloflu/ConvectiveFluxesMP.F90:73), for the host
  * state cv(5,nCells): rhs(5,nCells) and the limited gradCell(3,5,nCells)

@@ -1416,14 +1416,19 @@ void afterUpdate(orc_ctx *c) {
   c->posFixCount += nPosFix;
 }
 
-void rkStage(orc_ctx *c, int iStage, double dtMin) {
-  rkInit(c, iStage);
-  cellGradients(c);
-  convectiveFluxes(c);
+/* RKUpdateMP, RFLU_SetVarsContWrapper, AfterUpdateMP (RungeKuttaMP.F90:328-372). */
+void updateStage(orc_ctx *c, int iStage, double dtMin) {
   rkUpdate(c, iStage, dtMin);
 #pragma omp parallel for schedule(static)
   for (int ic = 0; ic < c->nCells; ++ic) setDependentVars(c, ic);
   afterUpdate(c);
+}
+
+void rkStage(orc_ctx *c, int iStage, double dtMin) {
+  rkInit(c, iStage);
+  cellGradients(c);
+  convectiveFluxes(c);
+  updateStage(c, iStage, dtMin);
 }
 
 /* RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:120-333) and
@@ -1594,6 +1599,13 @@ void orc_residual(orc_ctx *c, double *rhs, double *grad) {
 }
 
 double orc_timestep(orc_ctx *c, double t) { return timeStep(c, t); }
+void orc_rk_init(orc_ctx *c, int iStage) { rkInit(c, iStage); }
+void orc_cell_gradients(orc_ctx *c) { cellGradients(c); }
+void orc_convective_fluxes(orc_ctx *c) { convectiveFluxes(c); }
+void orc_add_rhs(orc_ctx *c, const double *src) {
+  for (size_t k = 0; k < 5 * (size_t)c->nCells; ++k) c->rhs[k] = c->rhs[k] + src[k];
+}
+void orc_rk_update(orc_ctx *c, int iStage, double dtMin) { updateStage(c, iStage, dtMin); }
 void orc_rk_stage(orc_ctx *c, int iStage, double dtMin) { rkStage(c, iStage, dtMin); }
 
 int orc_run(orc_ctx *c, int nSteps, double *time, double endTime) {

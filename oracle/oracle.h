@@ -89,6 +89,16 @@ void orc_residual(orc_ctx *c, double *rhs, double *grad);
 double orc_timestep(orc_ctx *c, double currentTime);
 /* One RK stage of RungeKuttaMP with the given dtMin. */
 void orc_rk_stage(orc_ctx *c, int iStage, double dtMin);
+/* One RK stage in the pieces of RungeKuttaMP's stage body
+ * (libfloflu/RungeKuttaMP.F90:209-348): RKInitMP; CellGradientsMP;
+ * ConvectiveFluxesMP; rhs += src(5,nCells) (the SourceTermsMP / PICL_Runge
+ * slot); RKUpdateMP + RFLU_SetVarsContWrapper + AfterUpdateMP.  Without a
+ * source they are orc_rk_stage. */
+void orc_rk_init(orc_ctx *c, int iStage);
+void orc_cell_gradients(orc_ctx *c);
+void orc_convective_fluxes(orc_ctx *c);
+void orc_add_rhs(orc_ctx *c, const double *src);
+void orc_rk_update(orc_ctx *c, int iStage, double dtMin);
 /* Whole time steps: dt from the CFL condition each step, last step clipped to
  * endTime (endTime <= 0: no clip). Returns steps done; *time updated. */
 int orc_run(orc_ctx *c, int nSteps, double *time, double endTime);

@@ -78,6 +78,13 @@ def lib():
         L.orc_get_grad.argtypes = [P, DP]
         L.orc_residual.argtypes = [P, DP, DP]
         L.orc_counters.argtypes = [P, LLP, LLP, LLP]
+        L.orc_rk_init.argtypes = [P, C.c_int]
+        L.orc_cell_gradients.argtypes = [P]
+        L.orc_convective_fluxes.argtypes = [P]
+        L.orc_add_rhs.argtypes = [P, DP]
+        L.orc_rk_update.argtypes = [P, C.c_int, C.c_double]
+        for name in ("orc_rk_init", "orc_cell_gradients", "orc_convective_fluxes", "orc_add_rhs", "orc_rk_update"):
+            getattr(L, name).restype = None
         L.orc_set_dt_imposed.argtypes = [P, C.c_double]
         L.orc_set_dt_imposed.restype = None
         L.orc_set_threads.argtypes = [C.c_int]
@@ -207,6 +214,33 @@ class Oracle:
         tt = C.c_double(t)
         done = lib().orc_run(self.h, n_steps, C.byref(tt), end_time)
         return done, tt.value
+
+    # one stage in the pieces of RungeKuttaMP's stage body
+    def rk_init(self, istage):
+        lib().orc_rk_init(self.h, istage)
+
+    def cell_gradients(self):
+        lib().orc_cell_gradients(self.h)
+
+    def convective_fluxes(self):
+        lib().orc_convective_fluxes(self.h)
+
+    def add_rhs(self, src):
+        s = np.ascontiguousarray(src, dtype=np.float64)
+        lib().orc_add_rhs(self.h, _ptr(s, C.c_double))
+
+    def rk_update(self, istage, dt):
+        lib().orc_rk_update(self.h, istage, dt)
+
+    def rhs(self):
+        r = np.zeros((self.n_cells, 5))
+        lib().orc_get_rhs(self.h, _ptr(r, C.c_double))
+        return r
+
+    def grad(self):
+        g = np.zeros((self.n_cells, 5, 3))
+        lib().orc_get_grad(self.h, _ptr(g, C.c_double))
+        return g
 
     def n_stages(self):
         return lib().orc_nstages(self.h)

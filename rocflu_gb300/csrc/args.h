@@ -16,7 +16,7 @@ enum class ArgMem { Unknown, Host, Device, Managed };
 inline const char *deviceArgProblem(ArgMem kind, int ptrDevice, int ctxDevice, int currentDevice) {
   if (currentDevice != ctxDevice) return "the current device is not the device the context was created on";
   if (kind == ArgMem::Managed) return nullptr;
-  if (kind != ArgMem::Device) return "cv and rhs must be device (or managed) memory";
+  if (kind != ArgMem::Device) return "the buffers must be device (or managed) memory";
   if (ptrDevice != ctxDevice) return "a buffer lives on another device than the context";
   return nullptr;
 }

@@ -257,6 +257,12 @@ struct CtxBase {
   virtual int status(rflu_status *s) = 0;
   virtual int kernelTimes(int nIter, double *ms) = 0;
   virtual int residualStatic(const double *cvDev, double *rhsDev) = 0;
+  virtual int cellGradients() = 0;
+  virtual int convectiveFluxes() = 0;
+  virtual int addRhs(const double *src, int onDevice) = 0;
+  virtual int rkUpdate(int iStage, double dt) = 0;
+  virtual int getRhs(double *rhs, int onDevice) = 0;
+  virtual int getGrad(double *grad, int onDevice) = 0;
   virtual int adjointTimes(int nIter, double *ms) = 0;
   virtual int unrolledAdjoint(const double *cv0, int nSteps, double dt, int every, int iPatch, double *J,
                               double *cvBar0, double *stats) = 0;
@@ -277,7 +283,14 @@ struct Ctx : CtxBase {
   double *work = nullptr;        // adjoint workspace (allocated by the first adjoint call)
   int tsWidthLazy = 0;           // ... and the width of its transposed-stencil weights
   size_t workBytes = 0;
-  double *cvSave = nullptr;
+  // scratch state (allocated by the first call that needs it): master cv,
+  // dependent variables, primitive records, RK accumulator and scalars of the
+  // states that the residual, tangent, adjoint, functional and diagnostic
+  // calls evaluate, so that those calls leave the context's own state as it
+  // was, bit for bit
+  double *sCv = nullptr, *sDv = nullptr;
+  R *sPrim = nullptr, *sRhsSum = nullptr;
+  Scalars *sSc = nullptr;
   cudaGraphExec_t stepGraph = nullptr, fixedGraph = nullptr;
   long long lastNan = 0;
 
@@ -336,10 +349,38 @@ struct Ctx : CtxBase {
     }
     return RFLU_OK;
   }
-  void stageKernels(int iStage) {
-    ops->gradLimit(V, stream);
-    ops->faceFlux(V, stream);
-    ops->gatherUpdate(V, iStage, &V.sc->dtMin, stream);
+  void stageKernels(int iStage) { stageKernelsOf(V, iStage); }
+  void stageKernelsOf(const View<R> &X, int iStage) {
+    ops->gradLimit(X, stream);
+    ops->faceFlux(X, stream);
+    ops->gatherUpdate(X, iStage, &X.sc->dtMin, stream);
+  }
+  // A view on the scratch state (its arrays allocated on first use); the
+  // mesh, geometry and the between-kernel arrays (gradients, face fluxes,
+  // residual) are the context's.  copyState: start from a copy of the
+  // context's state and scalars.
+  int scratchView(View<R> *W, bool copyState) {
+    const size_t nc = V.nc;
+    if (!sCv) {
+      int rc = 0;
+      if ((rc = alloc(&sCv, 5 * nc)) || (rc = alloc(&sDv, 3 * nc)) || (rc = alloc(&sPrim, Layout<R>::prim * nc)) ||
+          (rc = alloc(&sRhsSum, 5 * nc)) || (rc = alloc(&sSc, 1)))
+        return rc;
+    }
+    *W = V;
+    W->cv = sCv;
+    W->dv = sDv;
+    W->prim = sPrim;
+    W->rhsSum = sRhsSum;
+    W->sc = sSc;
+    RFLU_CUDA(cudaMemcpyAsync(sSc, V.sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, stream));
+    if (copyState) {
+      RFLU_CUDA(cudaMemcpyAsync(sCv, V.cv, sizeof(double) * 5 * nc, cudaMemcpyDeviceToDevice, stream));
+      RFLU_CUDA(cudaMemcpyAsync(sDv, V.dv, sizeof(double) * 3 * nc, cudaMemcpyDeviceToDevice, stream));
+      RFLU_CUDA(cudaMemcpyAsync(sPrim, V.prim, sizeof(R) * Layout<R>::prim * nc, cudaMemcpyDeviceToDevice, stream));
+      RFLU_CUDA(cudaMemcpyAsync(sRhsSum, V.rhsSum, sizeof(R) * 5 * nc, cudaMemcpyDeviceToDevice, stream));
+    }
+    return RFLU_OK;
   }
   // Host <-> device transfers in reference order go through the staging
   // buffer in chunks of reference cells: chunk c's copy runs on copyStream
@@ -349,7 +390,8 @@ struct Ctx : CtxBase {
   // ~200 GB/s; kernels reading the host buffer directly measured 2x slower).
   int nChunks() const { return V.nc >= (1 << 18) ? kMaxChunks : 1; }
   int chunkBegin(int c) const { return (int)(((long long)V.nc * c) / nChunks()); }
-  int setState(const double *cv) {
+  int setState(const double *cv) { return setStateOf(V, cv); }
+  int setStateOf(const View<R> &X, const double *cv) {
     const int K = nChunks();
     // staging is free once the work queued on the stream so far is done
     RFLU_CUDA(cudaEventRecord(chunkEv[kMaxChunks], stream));
@@ -360,7 +402,7 @@ struct Ctx : CtxBase {
                                 cudaMemcpyHostToDevice, copyStream));
       RFLU_CUDA(cudaEventRecord(chunkEv[c], copyStream));
       RFLU_CUDA(cudaStreamWaitEvent(stream, chunkEv[c], 0));
-      ops->initFromRef(V, staging, o0, o1, stream);
+      ops->initFromRef(X, staging, o0, o1, stream);
     }
     return checkLaunch("upload");
   }
@@ -384,6 +426,7 @@ struct Ctx : CtxBase {
   }
 
   int upload(const double *cv) override {
+    invalidate();
     if (!cv) return fail(RFLU_ERR_ARG, "rflu_gpu_upload_state: null cv");
     int rc = setState(cv);
     if (rc) return rc;
@@ -410,6 +453,7 @@ struct Ctx : CtxBase {
     return RFLU_OK;
   }
   int rkStage(int iStage, double dt) override {
+    invalidate();
     if (iStage < 1 || iStage > V.p.nrkSteps) return fail(RFLU_ERR_ARG, "rflu_gpu_rk_stage: stage out of range");
     kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
     stageKernels(iStage);
@@ -418,6 +462,7 @@ struct Ctx : CtxBase {
     return syncEvents(true);
   }
   int rungeKutta(double dt) override {
+    invalidate();
     kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
     for (int s = 1; s <= V.p.nrkSteps; ++s) stageKernels(s);
     int rc = checkLaunch("runge_kutta");
@@ -452,6 +497,7 @@ struct Ctx : CtxBase {
     return RFLU_OK;
   }
   int step(int nSteps, double *time, double endTime, int *done) override {
+    invalidate();
     if (!time || nSteps < 0) return fail(RFLU_ERR_ARG, "rflu_gpu_step: bad arguments");
     int rc = ensureStepGraph();
     if (rc) return rc;
@@ -474,6 +520,7 @@ struct Ctx : CtxBase {
     return rc;
   }
   int runFixedDt(int nSteps, double dt) override {
+    invalidate();
     int rc = ensureFixedGraph();
     if (rc) return rc;
     kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
@@ -481,14 +528,15 @@ struct Ctx : CtxBase {
     return syncEvents(true);
   }
   int residual(const double *cv, double *rhs, double *grad) override {
+    invalidate();
     if (!cv || !rhs) return fail(RFLU_ERR_ARG, "rflu_gpu_residual: null argument");
     const size_t nc = V.nc;
-    RFLU_CUDA(cudaMemcpyAsync(cvSave, V.cv, sizeof(double) * 5 * nc, cudaMemcpyDeviceToDevice, stream));
-    int rc = setState(cv);
-    if (rc) return rc;
-    ops->gradLimit(V, stream);
-    ops->faceFlux(V, stream);
-    ops->gatherRhs(V, stream);
+    View<R> W;
+    int rc = scratchView(&W, false);
+    if (rc || (rc = setStateOf(W, cv))) return rc;
+    ops->gradLimit(W, stream);
+    ops->faceFlux(W, stream);
+    ops->gatherRhs(W, stream);
     kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(V.rhs, staging, V.refId, V.nc, 5, V.nc, 1);
     RFLU_CUDA(cudaMemcpyAsync(rhs, staging, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
     if (grad) {
@@ -503,10 +551,6 @@ struct Ctx : CtxBase {
         std::memset(grad, 0, sizeof(double) * 15 * nc);
       }
     }
-    RFLU_CUDA(cudaStreamSynchronize(stream));
-    // restore the context state
-    RFLU_CUDA(cudaMemcpyAsync(V.cv, cvSave, sizeof(double) * 5 * nc, cudaMemcpyDeviceToDevice, stream));
-    ops->initState(V, stream);
     rc = checkLaunch("residual");
     if (rc) return rc;
     return syncEvents(false);
@@ -525,60 +569,156 @@ struct Ctx : CtxBase {
     }
     return checkLaunch("adjoint set-up");
   }
-  int adjointPrep(const double *cv) {
+  // the host state cv in the scratch state W (the adjoint kernels then run on W)
+  int adjointPrep(const double *cv, View<R> *W) {
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "no adjoint kernels in this precision mode");
     int rc = ensureAdjoint();
-    if (rc) return rc;
-    RFLU_CUDA(cudaMemcpyAsync(cvSave, V.cv, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToDevice, stream));
-    return setState(cv);
+    if (rc || (rc = scratchView(W, false))) return rc;
+    return setStateOf(*W, cv);
   }
   int adjointDone() {
-    RFLU_CUDA(cudaMemcpyAsync(V.cv, cvSave, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyDeviceToDevice, stream));
-    ops->initState(V, stream);
     int rc = checkLaunch("adjoint");
     if (rc) return rc;
     return syncEvents(false);
   }
   int vjp(const double *cv, const double *rhsBar, double *cvBar) override {
+    invalidate();
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
     if (V.p.reconst == 10)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: the eigen-frame velocity limiter (RECONST 10) has a tangent only");
     if (V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through WENO smoothing (RECONST 1, 2)");
-    int rc = adjointPrep(cv);
+    View<R> W;
+    int rc = adjointPrep(cv, &W);
     if (rc) return rc;
     const size_t nc = V.nc;
     RFLU_CUDA(cudaMemcpyAsync(staging, rhsBar, sizeof(double) * 5 * nc, cudaMemcpyHostToDevice, stream));
-    ops->vjp(V, staging, staging + 5 * nc, work, stream);
+    ops->vjp(W, staging, staging + 5 * nc, work, stream);
     RFLU_CUDA(cudaMemcpyAsync(cvBar, staging + 5 * nc, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
     return adjointDone();
   }
   int jvp(const double *cv, const double *cvDot, double *rhsDot) override {
+    invalidate();
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
     if (V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through WENO smoothing (RECONST 1, 2)");
-    int rc = adjointPrep(cv);
+    View<R> W;
+    int rc = adjointPrep(cv, &W);
     if (rc) return rc;
     const size_t nc = V.nc;
     RFLU_CUDA(cudaMemcpyAsync(staging, cvDot, sizeof(double) * 5 * nc, cudaMemcpyHostToDevice, stream));
-    ops->jvp(V, staging, staging + 5 * nc, work, stream);
+    ops->jvp(W, staging, staging + 5 * nc, work, stream);
     RFLU_CUDA(cudaMemcpyAsync(rhsDot, staging + 5 * nc, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
     return adjointDone();
   }
   int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) override {
+    invalidate();
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
     if (cvBar && (V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2))
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through RECONST 10, 1 or 2");
-    int rc = adjointPrep(cv);
+    View<R> W;
+    int rc = adjointPrep(cv, &W);
     if (rc) return rc;
     const size_t nc = V.nc;
-    ops->patchPressure(V, iPatch, staging + 10 * nc, cvBar ? staging + 5 * nc : nullptr, work, stream);
+    ops->patchPressure(W, iPatch, staging + 10 * nc, cvBar ? staging + 5 * nc : nullptr, work, stream);
     RFLU_CUDA(cudaMemcpyAsync(J, staging + 10 * nc, sizeof(double), cudaMemcpyDeviceToHost, stream));
     if (cvBar)
       RFLU_CUDA(cudaMemcpyAsync(cvBar, staging + 5 * nc, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
     return adjointDone();
   }
+  // ---- one RK stage at the reference's subroutine granularity --------------
+  // Whether V.grad holds the limited gradients of the current state and V.rhs
+  // its residual (set by cellGradients / convectiveFluxes); every other call
+  // that changes the state or reuses those arrays clears both.
+  bool gradValid = false, rhsValid = false;
+  void invalidate() { gradValid = rhsValid = false; }
+  // A caller's device buffer must live on this context's device, with that
+  // device current (args.h).
+  int checkDeviceArg(const void *q, const char *who) {
+    int cur = -1, qDev = -1;
+    RFLU_CUDA(cudaGetDevice(&cur));
+    const ArgMem kind = pointerKind(q, &qDev);
+    if (const char *why = deviceArgProblem(kind, qDev, device, cur)) return fail(RFLU_ERR_ARG, std::string(who) + ": " + why);
+    return RFLU_OK;
+  }
+  int cellGradients() override {
+    invalidate();
+    ops->gradLimit(V, stream);
+    if (int rc = checkLaunch("rflu_gpu_cell_gradients")) return rc;
+    gradValid = true;
+    return RFLU_OK;
+  }
+  int convectiveFluxes() override {
+    if (V.p.spaceOrder > 1 && !gradValid)
+      return fail(RFLU_ERR_STATE, "rflu_gpu_convective_fluxes: no gradients of this state (call rflu_gpu_cell_gradients)");
+    ops->faceFlux(V, stream);
+    ops->gatherRhs(V, stream);
+    if (int rc = checkLaunch("rflu_gpu_convective_fluxes")) return rc;
+    rhsValid = true;
+    return RFLU_OK;
+  }
+  int addRhs(const double *src, int onDevice) override {
+    if (!src) return fail(RFLU_ERR_ARG, "rflu_gpu_add_rhs: null src");
+    if (!rhsValid) return fail(RFLU_ERR_STATE, "rflu_gpu_add_rhs: no residual (call rflu_gpu_convective_fluxes)");
+    const double *d = src;
+    if (onDevice) {
+      if (int rc = checkDeviceArg(src, "rflu_gpu_add_rhs")) return rc;
+    } else {
+      RFLU_CUDA(cudaMemcpyAsync(staging, src, sizeof(double) * 5 * (size_t)V.nc, cudaMemcpyHostToDevice, stream));
+      d = staging;
+    }
+    ops->addRhs(V, d, stream);
+    if (int rc = checkLaunch("rflu_gpu_add_rhs")) return rc;
+    if (!onDevice) RFLU_CUDA(cudaStreamSynchronize(stream));  // src may be reused on return
+    return RFLU_OK;
+  }
+  int rkUpdate(int iStage, double dt) override {
+    if (iStage < 1 || iStage > V.p.nrkSteps) return fail(RFLU_ERR_ARG, "rflu_gpu_rk_update: stage out of range");
+    if (!rhsValid) return fail(RFLU_ERR_STATE, "rflu_gpu_rk_update: no residual (call rflu_gpu_convective_fluxes)");
+    invalidate();
+    kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
+    ops->updateFromRhs(V, iStage, &V.sc->dtMin, stream);
+    if (int rc = checkLaunch("rflu_gpu_rk_update")) return rc;
+    return syncEvents(true);
+  }
+  // ncomp rows of per-cell data (component k of renumbered cell i at
+  // src[k*kStride + i*iStride]) to the reference's layout, on the device
+  // (onDevice) or through the staging buffer to the host
+  int readOut(const R *src, int ncomp, size_t kStride, size_t iStride, double *dst, int onDevice, const char *who) {
+    if (onDevice) {
+      if (int rc = checkDeviceArg(dst, who)) return rc;
+      kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(src, dst, V.refId, V.nc, ncomp, kStride, iStride);
+    } else {
+      kPermuteOut<R><<<nblk(V.nc), 256, 0, stream>>>(src, staging, V.refId, V.nc, ncomp, kStride, iStride);
+      RFLU_CUDA(cudaMemcpyAsync(dst, staging, sizeof(double) * ncomp * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
+    }
+    if (int rc = checkLaunch(who)) return rc;
+    RFLU_CUDA(cudaStreamSynchronize(stream));
+    return RFLU_OK;
+  }
+  int getRhs(double *rhs, int onDevice) override {
+    if (!rhs) return fail(RFLU_ERR_ARG, "rflu_gpu_get_rhs: null rhs");
+    if (!rhsValid) return fail(RFLU_ERR_STATE, "rflu_gpu_get_rhs: no residual (call rflu_gpu_convective_fluxes)");
+    return readOut(V.rhs, 5, V.nc, 1, rhs, onDevice, "rflu_gpu_get_rhs");
+  }
+  int getGrad(double *grad, int onDevice) override {
+    if (!grad) return fail(RFLU_ERR_ARG, "rflu_gpu_get_grad: null grad");
+    if (!gradValid) return fail(RFLU_ERR_STATE, "rflu_gpu_get_grad: no gradients (call rflu_gpu_cell_gradients)");
+    if (V.p.spaceOrder < 2) {
+      if (onDevice) {
+        if (int rc = checkDeviceArg(grad, "rflu_gpu_get_grad")) return rc;
+        RFLU_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * 15 * (size_t)V.nc, stream));
+        RFLU_CUDA(cudaStreamSynchronize(stream));
+      } else {
+        std::memset(grad, 0, sizeof(double) * 15 * (size_t)V.nc);
+      }
+      return RFLU_OK;
+    }
+    if (Layout<R>::packed) return readOut(V.grad, 15, 1, 16, grad, onDevice, "rflu_gpu_get_grad");
+    return readOut(V.grad, 15, V.nc, 1, grad, onDevice, "rflu_gpu_get_grad");
+  }
+
   int status(rflu_status *st) override {
     Scalars s;
     RFLU_CUDA(cudaStreamSynchronize(stream));
@@ -593,23 +733,28 @@ struct Ctx : CtxBase {
     return RFLU_OK;
   }
   int kernelTimes(int nIter, double *ms) override {
+    invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_kernel_times: bad arguments");
+    // on a copy of the state (the same kernels on the same data), so that the
+    // context's state, time and accumulator stay as they are
+    View<R> W;
+    if (int rc0 = scratchView(&W, true)) return rc0;
     cudaEvent_t ev[5];
     for (auto &e : ev) RFLU_CUDA(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
-    kSetScalars<<<1, 1, 0, stream>>>(V.sc, 1.0, 0.0, 0);
-    kSetDt<<<1, 1, 0, stream>>>(V.sc, 0.0);  // dt = 0: the state stays put
+    kSetScalars<<<1, 1, 0, stream>>>(W.sc, 1.0, 0.0, 0);
+    kSetDt<<<1, 1, 0, stream>>>(W.sc, 0.0);  // dt = 0: the state stays put
     // iteration 0 is an untimed warm-up (the first launch of a kernel also
     // loads its module)
     for (int it = 0; it <= nIter; ++it) {
       cudaEventRecord(ev[0], stream);
-      ops->gradLimit(V, stream);
+      ops->gradLimit(W, stream);
       cudaEventRecord(ev[1], stream);
-      ops->faceFlux(V, stream);
+      ops->faceFlux(W, stream);
       cudaEventRecord(ev[2], stream);
-      ops->gatherUpdate(V, 1 + it % V.p.nrkSteps, &V.sc->dtMin, stream);
+      ops->gatherUpdate(W, 1 + it % V.p.nrkSteps, &W.sc->dtMin, stream);
       cudaEventRecord(ev[3], stream);
-      ops->timestep(V, stream);
+      ops->timestep(W, stream);
       cudaEventRecord(ev[4], stream);
       RFLU_CUDA(cudaEventSynchronize(ev[4]));
       for (int k = 0; k < 4 && it > 0; ++k) {
@@ -630,14 +775,8 @@ struct Ctx : CtxBase {
   // same call.
   int residualStatic(const double *cvDev, double *rhsDev) override {
     if (!cvDev || !rhsDev) return fail(RFLU_ERR_ARG, "rflu_gpu_residual_static: null argument");
-    int cur = -1;
-    RFLU_CUDA(cudaGetDevice(&cur));
-    for (const void *q : {(const void *)cvDev, (const void *)rhsDev}) {
-      int qDev = -1;
-      const ArgMem kind = pointerKind(q, &qDev);
-      if (const char *why = deviceArgProblem(kind, qDev, device, cur))
-        return fail(RFLU_ERR_ARG, std::string("rflu_gpu_residual_static: ") + why);
-    }
+    for (const void *q : {(const void *)cvDev, (const void *)rhsDev})
+      if (int rc = checkDeviceArg(q, "rflu_gpu_residual_static")) return rc;
     const size_t nc = V.nc, nT = (size_t)V.nf + V.nb;
     auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t bCv = up(5 * nc * sizeof(double)), bDv = up(3 * nc * sizeof(double));
@@ -679,6 +818,7 @@ struct Ctx : CtxBase {
   //   lambda(s-1) = lambda(s) - R'(cv(s-1))^T sum_{t>=s} (ark_t dt W[t][s]/vol) lambda(t).
   int unrolledAdjoint(const double *cv0, int nSteps, double dt, int every, int iPatch, double *Jout, double *cvBar0,
                       double *stats) override {
+    invalidate();
     if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
       return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
@@ -686,6 +826,9 @@ struct Ctx : CtxBase {
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: RECONST 10, 1 and 2 have no adjoint");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     if (int rc0 = ensureAdjoint()) return rc0;
+    // the whole forward and reverse sweep runs on the scratch state X
+    View<R> X;
+    if (int rc0 = scratchView(&X, false)) return rc0;
     const int nrk = V.p.nrkSteps;
     double W[6][6] = {};
     for (int t = 1; t <= nrk; ++t) W[t][t] = 1.0;
@@ -734,18 +877,17 @@ struct Ctx : CtxBase {
       return r;
     };
     const int nb = nblk((long long)n5);
-    cp(cvSave, V.cv, b5, cudaMemcpyDeviceToDevice);
-    if ((rc = setState(cv0))) return finish(rc);
+    if ((rc = setStateOf(X, cv0))) return finish(rc);
     zero(jd, 3 * sizeof(double));
-    kSetDt<<<1, 1, 0, stream>>>(V.sc, dt);
+    kSetDt<<<1, 1, 0, stream>>>(X.sc, dt);
     // forward sweep: checkpoints (and J when no gradient is asked for)
     cudaEventRecord(ev[0], stream);
     for (int n = 0; n < nSteps; ++n) {
       if (n % every == 0)
-        cp(ck + (size_t)(n / every) * n5, V.cv, b5, cudaMemcpyDeviceToDevice);
-      for (int st = 1; st <= nrk; ++st) stageKernels(st);
+        cp(ck + (size_t)(n / every) * n5, X.cv, b5, cudaMemcpyDeviceToDevice);
+      for (int st = 1; st <= nrk; ++st) stageKernelsOf(X, st);
       if (!grad) {
-        ops->patchPressure(V, iPatch, jStep, nullptr, work, stream);
+        ops->patchPressure(X, iPatch, jStep, nullptr, work, stream);
         kAccumJ<<<1, 1, 0, stream>>>(jAcc, jStep, dt);
       }
     }
@@ -754,22 +896,22 @@ struct Ctx : CtxBase {
       double *lamTop = lam + (size_t)nrk * n5;  // lambda at the end of the current step
       zero(lamTop, b5);
       auto loadState = [&](const double *src) {
-        cp(V.cv, src, b5, cudaMemcpyDeviceToDevice);
-        ops->initState(V, stream);
+        cp(X.cv, src, b5, cudaMemcpyDeviceToDevice);
+        ops->initState(X, stream);
       };
       for (int sg = nCk - 1; sg >= 0; --sg) {
         const int n0 = sg * every, n1 = std::min(nSteps, n0 + every);
         loadState(ck + (size_t)sg * n5);
         for (int n = n0; n < n1; ++n)
           for (int st = 1; st <= nrk; ++st) {
-            cp(seg + ((size_t)(n - n0) * nrk + st - 1) * n5, V.cv, b5, cudaMemcpyDeviceToDevice);
-            stageKernels(st);
+            cp(seg + ((size_t)(n - n0) * nrk + st - 1) * n5, X.cv, b5, cudaMemcpyDeviceToDevice);
+            stageKernelsOf(X, st);
           }
-        cp(seg + (size_t)(n1 - n0) * nrk * n5, V.cv, b5, cudaMemcpyDeviceToDevice);
+        cp(seg + (size_t)(n1 - n0) * nrk * n5, X.cv, b5, cudaMemcpyDeviceToDevice);
         for (int n = n1 - 1; n >= n0; --n) {
           // the functional's term at the state after step n
           loadState(seg + (size_t)(n + 1 - n0) * nrk * n5);
-          ops->patchPressure(V, iPatch, jStep, pg, work, stream);
+          ops->patchPressure(X, iPatch, jStep, pg, work, stream);
           kAccumJ<<<1, 1, 0, stream>>>(jAcc, jStep, dt);
           kAxpyInPlace<<<nb, 256, 0, stream>>>(lamTop, dt, pg, n5);
           for (int st = nrk; st >= 1; --st) {
@@ -782,7 +924,7 @@ struct Ctx : CtxBase {
               }
             kStageSeed<<<nblk(V.nc), 256, 0, stream>>>(sigma, T, V.vol, V.refId, V.nc);
             loadState(seg + ((size_t)(n - n0) * nrk + st - 1) * n5);
-            ops->vjp(V, sigma, wv, work, stream);
+            ops->vjp(X, sigma, wv, work, stream);
             kSubInto<<<nb, 256, 0, stream>>>(lam + (size_t)(st - 1) * n5, lam + (size_t)st * n5, wv, n5);
           }
           cp(lamTop, lam, b5, cudaMemcpyDeviceToDevice);
@@ -792,9 +934,6 @@ struct Ctx : CtxBase {
     }
     cudaEventRecord(ev[2], stream);
     cp(Jout, jAcc, sizeof(double), cudaMemcpyDeviceToHost);
-    // the context state as it was
-    cp(V.cv, cvSave, b5, cudaMemcpyDeviceToDevice);
-    ops->initState(V, stream);
     if ((rc = checkLaunch("rflu_gpu_unrolled_adjoint"))) return finish(rc);
     const cudaError_t es = cudaStreamSynchronize(stream);
     if (err == cudaSuccess) err = es;
@@ -812,6 +951,7 @@ struct Ctx : CtxBase {
     return finish(syncEvents(false));
   }
   int adjointTimes(int nIter, double *ms) override {
+    invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
     if (!ops->vjp || V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
@@ -1162,7 +1302,6 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   if ((rc = alloc(&V.rhs, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.sc, 1))) return rc;
   if ((rc = alloc(&staging, 15 * (size_t)nc + 16))) return rc;
-  if ((rc = alloc(&cvSave, 5 * (size_t)nc))) return rc;
   RFLU_CUDA(cudaMemset(V.grad, 0, sizeof(R) * Layout<R>::grad * (size_t)nc));
   RFLU_CUDA(cudaMemset(V.rhsSum, 0, sizeof(R) * 5 * (size_t)nc));
   RFLU_CUDA(cudaMemset(V.cv, 0, sizeof(double) * 5 * (size_t)nc));
@@ -1378,6 +1517,31 @@ int rflu_gpu_check_conversions(long long n, unsigned long long seed, unsigned lo
   cudaFree(bad);
   if (err != cudaSuccess) return fail(RFLU_ERR_CUDA, std::string("rflu_gpu_check_conversions: ") + cudaGetErrorString(err));
   return RFLU_OK;
+}
+
+int rflu_gpu_cell_gradients(rflu_gpu_ctx *ctx) {
+  CTX_CHECK("rflu_gpu_cell_gradients");
+  return ctx->impl->cellGradients();
+}
+int rflu_gpu_convective_fluxes(rflu_gpu_ctx *ctx) {
+  CTX_CHECK("rflu_gpu_convective_fluxes");
+  return ctx->impl->convectiveFluxes();
+}
+int rflu_gpu_add_rhs(rflu_gpu_ctx *ctx, const double *src, int onDevice) {
+  CTX_CHECK("rflu_gpu_add_rhs");
+  return ctx->impl->addRhs(src, onDevice);
+}
+int rflu_gpu_rk_update(rflu_gpu_ctx *ctx, int iStage, double dtMin) {
+  CTX_CHECK("rflu_gpu_rk_update");
+  return ctx->impl->rkUpdate(iStage, dtMin);
+}
+int rflu_gpu_get_rhs(rflu_gpu_ctx *ctx, double *rhs, int onDevice) {
+  CTX_CHECK("rflu_gpu_get_rhs");
+  return ctx->impl->getRhs(rhs, onDevice);
+}
+int rflu_gpu_get_grad(rflu_gpu_ctx *ctx, double *grad, int onDevice) {
+  CTX_CHECK("rflu_gpu_get_grad");
+  return ctx->impl->getGrad(grad, onDevice);
 }
 
 int rflu_gpu_check_refinements(long long n, unsigned long long seed, double *maxRelErr) {

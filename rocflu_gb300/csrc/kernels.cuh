@@ -294,7 +294,9 @@ struct MixedPrim {
     rf = d2f(cv[0]);
     irf = 1.0f / rf;
     ir = refinedRecip(cv[0], irf);
-    const double msq = cv[1] * cv[1] + cv[2] * cv[2] + cv[3] * cv[3];
+    // explicit fused multiply-adds: the same bits wherever the compiler
+    // inlines this (the update and the state set-up agree)
+    const double msq = fma(cv[3], cv[3], fma(cv[2], cv[2], cv[1] * cv[1]));
     ke = 0.5 * msq * ir;
     pr = (P.gRT - 1.0) * (cv[4] - ke);
     uf = d2f(cv[1]) * irf;
@@ -322,10 +324,9 @@ __device__ inline void initCell(const View<R> &V, int i, const double *cv) {
     const MixedPrim m(V.p, cv);
     V.dv[i] = m.pr;
     if (!V.p.dvPOnly) {
-      double pr, t, c;
-      dependentVars(V.p, cv, pr, t, c);
-      V.dv[(size_t)V.nc + i] = t;
-      V.dv[2 * (size_t)V.nc + i] = c;
+      // T and c with the mixed update's formulas
+      V.dv[(size_t)V.nc + i] = m.pr * m.ir * V.p.igcR;
+      V.dv[2 * (size_t)V.nc + i] = refinedSqrt(V.p.gRT * m.pr * m.ir);
     }
     storePrimRec(V, i, m.rf, m.uf, m.vf, m.wf, (float)m.pr);
   } else {
@@ -1822,6 +1823,21 @@ __global__ void __launch_bounds__(kBlock) kGatherRhs(View<R> V) {
   for (int k = 0; k < 5; ++k) V.rhs[(size_t)k * V.nc + i] = rhs[k];
 }
 
+// rhs += src, src(5,nCells) in the reference's cell order and layout (the
+// SourceTermsMP / PICL_Runge slot of RungeKuttaMP, libfloflu/
+// RungeKuttaMP.F90:274-290); the sum in FP64, stored in the residual's type.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAddRhs(View<R> V, const double *src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  const size_t o = (size_t)V.refId[i];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    R &r = V.rhs[(size_t)k * V.nc + i];
+    r = (R)((double)r + src[5 * o + k]);
+  }
+}
+
 // RFLU_CheckValidity / RFLU_EnforceBounds / RFLU_CheckPositivity for one cell
 // (libflu/RFLU_CheckValidity.F90:165-214, RFLU_EnforceBounds.F90:165-230,
 // RFLU_CheckPositivity.F90:173-193); cv and dv updated in place.
@@ -1946,14 +1962,21 @@ __device__ inline void mixedUpdate(const View<R> &V, int i, int iStage, float fa
 // Gather + RKUpdateMP (RkUpdateGeneric, static grid, libfloflu/
 // RkUpdateGeneric.F90:257-322) + RFLU_SetVarsContWrapper + AfterUpdateMP.
 // cvOld of RkInitGeneric is cv itself: nothing writes cv before this kernel.
-template <typename R>
+// kFromRhs: the residual is read from V.rhs (formed by kGatherRhs and
+// perhaps changed by the caller's source terms) instead of gathered here.
+template <typename R, bool kFromRhs>
 __global__ void __launch_bounds__(kBlock) kGatherUpdate(View<R> V, int iStage, const double *dtp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc || V.sc->finished < 0) return;
   const Params &P = V.p;
   const size_t n = V.nc;
   R rhs[5];
-  gatherRhs(V, (const R *)V.flux, i, rhs);
+  if constexpr (kFromRhs) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) rhs[k] = V.rhs[k * n + i];
+  } else {
+    gatherRhs(V, (const R *)V.flux, i, rhs);
+  }
   double cv[5];
   loadCv(V, i, cv);
   if constexpr (!Ref<R>::on) {
@@ -2199,7 +2222,13 @@ struct Launch {
   }
   static void gatherRhs(const View<R> &V, cudaStream_t s) { kGatherRhs<R><<<blocks(V.nc), kBlock, 0, s>>>(V); }
   static void gatherUpdate(const View<R> &V, int iStage, const double *dtp, cudaStream_t s) {
-    kGatherUpdate<R><<<blocks(V.nc), kBlock, 0, s>>>(V, iStage, dtp);
+    kGatherUpdate<R, false><<<blocks(V.nc), kBlock, 0, s>>>(V, iStage, dtp);
+  }
+  static void updateFromRhs(const View<R> &V, int iStage, const double *dtp, cudaStream_t s) {
+    kGatherUpdate<R, true><<<blocks(V.nc), kBlock, 0, s>>>(V, iStage, dtp);
+  }
+  static void addRhs(const View<R> &V, const double *src, cudaStream_t s) {
+    kAddRhs<R><<<blocks(V.nc), kBlock, 0, s>>>(V, src);
   }
   // The FP64 modes: RFLU_TimeStepInviscid in FP64 from cv and dv; the mixed
   // mode: the FP32 sum from the primitive state, as its steps take it.

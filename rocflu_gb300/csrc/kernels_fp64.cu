@@ -9,7 +9,8 @@ const Ops<double> *opsFp64() {
   using L = fp64::Launch<double>;
   static const Ops<double> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, fp64::AdjointOps<double>::jvp, fp64::AdjointOps<double>::vjp,
-                                 fp64::AdjointOps<double>::patchPressure, L::adjointSetup};
+                                 fp64::AdjointOps<double>::patchPressure, L::adjointSetup,
+                                 L::updateFromRhs, L::addRhs};
   return &ops;
 }
 }  // namespace rflu

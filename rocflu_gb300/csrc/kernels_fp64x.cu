@@ -9,7 +9,8 @@ const Ops<double> *opsFp64Exact() {
   using L = fp64x::Launch<double>;
   static const Ops<double> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, fp64x::AdjointOps<double>::jvp, fp64x::AdjointOps<double>::vjp,
-                                 fp64x::AdjointOps<double>::patchPressure, L::adjointSetup};
+                                 fp64x::AdjointOps<double>::patchPressure, L::adjointSetup,
+                                 L::updateFromRhs, L::addRhs};
   return &ops;
 }
 }  // namespace rflu

@@ -30,7 +30,8 @@ const Ops<float> *opsMixed() {
   using L = mixed::Launch<float>;
   static const Ops<float> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, mixed::AdjointOps<float>::jvp, mixed::AdjointOps<float>::vjp,
-                                 mixed::AdjointOps<float>::patchPressure, L::adjointSetup};
+                                 mixed::AdjointOps<float>::patchPressure, L::adjointSetup,
+                                 L::updateFromRhs, L::addRhs};
   return &ops;
 }
 }  // namespace rflu

@@ -28,6 +28,10 @@ struct Ops {
   void (*patchPressure)(const View<R> &, int iPatch, double *J, double *cvBar, double *work, cudaStream_t);
   // fills the adjoint's mesh-dependent arrays (View::tsW) once they exist
   void (*adjointSetup)(const View<R> &, cudaStream_t);
+  // RKUpdateMP + RFLU_SetVarsContWrapper + AfterUpdateMP from View::rhs
+  void (*updateFromRhs)(const View<R> &, int, const double *, cudaStream_t);
+  // View::rhs += a (5,nCells) array in the reference's cell order
+  void (*addRhs)(const View<R> &, const double *, cudaStream_t);
 };
 
 // The mixed mode's Newton-refined FP64 reciprocal and square root against

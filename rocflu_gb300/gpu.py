@@ -9,6 +9,10 @@ calls, under the reference's names:
   RungeKuttaMP(regions)                          -> RungeKuttaMP(region, dtMin)
   RKInitMP/CellGradientsMP/ConvectiveFluxesMP/RKUpdateMP/AfterUpdateMP
                                                  -> Region.rk_stage(iStage, dtMin)
+  CellGradientsMP(region)                        -> CellGradientsMP(region)
+  ConvectiveFluxesMP(region)                     -> ConvectiveFluxesMP(region)
+  SourceTermsMP / PICL_Runge's rhs changes       -> Region.add_rhs(src)
+  RKUpdateMP(region, iReg, iStage)               -> RKUpdateMP(region, iReg, iStage, dtMin)
   the RFLU_TimeStepping loop                     -> Region.step(nSteps, time, endTime)
 
 Arrays crossing the boundary use the reference layouts as (nCells, k)
@@ -70,7 +74,9 @@ class RfluError(RuntimeError):
 
 EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_gpu_stream",
            "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
-           "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_residual", "rflu_gpu_vjp",
+           "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_cell_gradients",
+           "rflu_gpu_convective_fluxes", "rflu_gpu_add_rhs", "rflu_gpu_rk_update", "rflu_gpu_get_rhs",
+           "rflu_gpu_get_grad", "rflu_gpu_residual", "rflu_gpu_vjp",
            "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_unrolled_adjoint", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
            "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_gpu_check_conversions", "rflu_gpu_check_refinements", "rflu_setup_build", "rflu_setup_grid",
            "rflu_setup_destroy")
@@ -105,6 +111,12 @@ def lib(build_if_missing=True):
     L.rflu_gpu_runge_kutta.argtypes = [P, D]
     L.rflu_gpu_step.argtypes = [P, I, DP, D, C.POINTER(I)]
     L.rflu_gpu_run_fixed_dt.argtypes = [P, I, D]
+    L.rflu_gpu_cell_gradients.argtypes = [P]
+    L.rflu_gpu_convective_fluxes.argtypes = [P]
+    L.rflu_gpu_add_rhs.argtypes = [P, P, I]
+    L.rflu_gpu_rk_update.argtypes = [P, I, D]
+    L.rflu_gpu_get_rhs.argtypes = [P, P, I]
+    L.rflu_gpu_get_grad.argtypes = [P, P, I]
     L.rflu_gpu_residual.argtypes = [P, DP, DP, DP]
     L.rflu_gpu_vjp.argtypes = [P, DP, DP, DP]
     L.rflu_gpu_jvp.argtypes = [P, DP, DP, DP]
@@ -283,6 +295,50 @@ class Region:
     def run_fixed_dt(self, n_steps, dt):
         return _check(lib().rflu_gpu_run_fixed_dt(self.h, n_steps, dt), allow_events=True)
 
+    # one stage at the reference's subroutine granularity
+    def cell_gradients(self):
+        """CellGradientsMP (libfloflu/CellGradientsMP.F90:75) on the device state."""
+        _check(lib().rflu_gpu_cell_gradients(self.h))
+
+    def convective_fluxes(self):
+        """ConvectiveFluxesMP (libfloflu/ConvectiveFluxesMP.F90:73): rhs kept on
+        the device."""
+        _check(lib().rflu_gpu_convective_fluxes(self.h))
+
+    def add_rhs(self, src):
+        """rhs += src (the SourceTermsMP / PICL_Runge slot): src a host
+        (nCells, 5) array, or an int device address of one."""
+        if isinstance(src, int):
+            _check(lib().rflu_gpu_add_rhs(self.h, C.c_void_p(src), 1))
+        else:
+            s = np.ascontiguousarray(src, np.float64)
+            assert s.shape == (self.n_cells, 5)
+            _check(lib().rflu_gpu_add_rhs(self.h, s.ctypes.data_as(C.c_void_p), 0))
+
+    def rk_update(self, istage, dt):
+        """RKUpdateMP + RFLU_SetVarsContWrapper + AfterUpdateMP from the rhs."""
+        return _check(lib().rflu_gpu_rk_update(self.h, istage, dt), allow_events=True)
+
+    def get_rhs(self, out=None):
+        """rhs(5,nCells) of the last convective_fluxes (and add_rhs): a host
+        (nCells, 5) array, or written to an int device address."""
+        if isinstance(out, int):
+            _check(lib().rflu_gpu_get_rhs(self.h, C.c_void_p(out), 1))
+            return None
+        r = np.empty((self.n_cells, 5)) if out is None else out
+        _check(lib().rflu_gpu_get_rhs(self.h, r.ctypes.data_as(C.c_void_p), 0))
+        return r
+
+    def get_grad(self, out=None):
+        """gradCell(3,5,nCells) of the last cell_gradients as (nCells, 5, 3),
+        or written to an int device address."""
+        if isinstance(out, int):
+            _check(lib().rflu_gpu_get_grad(self.h, C.c_void_p(out), 1))
+            return None
+        g = np.empty((self.n_cells, 5, 3)) if out is None else out
+        _check(lib().rflu_gpu_get_grad(self.h, g.ctypes.data_as(C.c_void_p), 0))
+        return g
+
     def residual(self, cv, with_grad=True):
         cv = np.ascontiguousarray(cv, np.float64)
         rhs = np.empty((self.n_cells, 5))
@@ -380,6 +436,23 @@ def RungeKuttaMP(region, dt_min):
 def RFLU_TimeStep(region, current_time):
     """rocflu/RFLU_TimeStepInviscid.F90:75 + rocflu/RFLU_MinimumTimeStep.F90:75."""
     return region.timestep(current_time)
+
+
+def CellGradientsMP(region):
+    """libfloflu/CellGradientsMP.F90:75 on the region's device state."""
+    region.cell_gradients()
+
+
+def ConvectiveFluxesMP(region):
+    """libfloflu/ConvectiveFluxesMP.F90:73: the residual, kept on the device."""
+    region.convective_fluxes()
+
+
+def RKUpdateMP(region, i_reg, istage, dt_min):
+    """libfloflu/RkUpdateMP.F90:75 (+ RFLU_SetVarsContWrapper, AfterUpdateMP);
+    i_reg is the reference's region index, kept for the call's shape."""
+    del i_reg
+    return region.rk_update(istage, dt_min)
 
 
 def CellGradientsMP_ConvectiveFluxesMP(region, cv):

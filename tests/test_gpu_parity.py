@@ -438,3 +438,33 @@ def test_gas_jump_closed_box_matches_reference_golden(gpu_lib, prec, tol):
         n_o, _ = o.run(100000, 0.0, c.end_time)
         assert n_o == steps
         np.testing.assert_array_equal(cv, o.state()[0])
+
+
+@pytest.mark.parametrize("prec", ["fp64_exact", "fp64", "mixed"])
+def test_evaluations_leave_the_context_state_untouched(gpu_lib, prec):
+    """The residual, tangent, adjoint, functional, unrolled-adjoint and
+    kernel-timing calls evaluate other states in the context's scratch
+    state: the context's cv, dv and status (time, counters) are the same bits
+    before and after, and the next stage continues as if they had not run."""
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=cases.RECONST_BJ_COMP, cfl=0.4)
+    c = cases.adjoint_tets(4, num=num)
+    a, b = gpu.Region(c, prec), gpu.Region(c, prec)
+    dt = a.timestep(1.0)
+    for r in (a, b):
+        r.rk_stage(1, dt)
+    before = b.download(), b.status()
+    cv = _perturbed(c, seed=9)
+    b.residual(cv)
+    b.vjp(cv, cv)
+    b.jvp(cv, cv)
+    b.patch_pressure(cv, 1)
+    b.unrolled_adjoint(cv, 2, dt, 1, 1)
+    b.kernel_times(1)
+    after = b.download(), b.status()
+    np.testing.assert_array_equal(after[0][0], before[0][0])
+    np.testing.assert_array_equal(after[0][1], before[0][1])
+    assert after[1] == before[1]
+    for r in (a, b):
+        r.rk_stage(2, dt)
+        r.rk_stage(3, dt)
+    np.testing.assert_array_equal(b.download()[0], a.download()[0])

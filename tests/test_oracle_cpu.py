@@ -301,3 +301,35 @@ def test_oracle_results_independent_of_threads(mesh, discr, reconst, p_in):
             np.testing.assert_array_equal(x, y)
         else:
             assert x == y
+
+
+def test_oracle_stage_pieces_equal_whole_stage():
+    """orc_rk_init, orc_cell_gradients, orc_convective_fluxes, orc_add_rhs
+    (a zero source) and orc_rk_update give orc_rk_stage's state; a nonzero
+    source changes the update by exactly -adtv * src in the first stage."""
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ, cfl=0.4)
+    c = cases.shock_sphere(8, num=num)
+    c.num.dt_imposed = 1e-3
+    a, b = Oracle(c), Oracle(c)
+    dt = a.timestep(1.0)
+    for s in range(1, 4):
+        a.rk_stage(s, dt)
+        b.rk_init(s)
+        b.cell_gradients()
+        b.convective_fluxes()
+        b.add_rhs(np.zeros_like(c.cv0))
+        b.rk_update(s, dt)
+        np.testing.assert_array_equal(a.state()[0], b.state()[0])
+        np.testing.assert_array_equal(a.state()[1], b.state()[1])
+    p, q = Oracle(c), Oracle(c)
+    vol, _ = p.cells()
+    src = np.outer(vol, [0.0, 0.0, 1.0, 0.0, 0.0])
+    for o, add in ((p, False), (q, True)):
+        o.rk_init(1)
+        o.cell_gradients()
+        o.convective_fluxes()
+        if add:
+            o.add_rhs(src)
+        o.rk_update(1, dt)
+    dmom = q.state()[0][:, 2] - p.state()[0][:, 2]
+    np.testing.assert_allclose(dmom, -(8.0 / 15.0) * dt * np.ones_like(dmom), rtol=1e-9, atol=1e-15)
