@@ -167,7 +167,7 @@ int svdSingularCount(int nRows, int nCols, const std::vector<double> &a) {
 }
 
 struct Patch {
-  int bcType, outflowType, order;
+  int bcType, outflowType, order, related = -1;
   double pOut;
   int n;
   std::vector<int> bf2v, bf2c;
@@ -180,10 +180,16 @@ struct orc_ctx {
   /* mesh */
   int nVert, nCells, nvc;
   std::vector<double> xyz;
-  std::vector<int> c2v;
+  /* c2vGeo: the cells' own vertex ids (their coordinates); c2v: the same
+     after the vertices of translational periodic patch pairs are identified
+     (topology: faces, stencils) */
+  std::vector<int> c2v, c2vGeo;
+  std::vector<std::array<double, 3>> perShift;  /* translation of each periodic pair */
   int nFaces;
   std::vector<int> f2c, f2v;
-  std::vector<double> fn, fc, vol, cofg;
+  /* fc2: face centroid in the frame of the face's second cell (fc translated
+     for a periodic face, else fc) */
+  std::vector<double> fn, fc, fc2, vol, cofg;
   std::vector<Patch> patches;
   std::vector<int> stOff, stIdx;
   std::vector<double> moms;
@@ -207,6 +213,126 @@ struct orc_ctx {
 };
 
 namespace {
+
+/* ------------------------------------------------------------------------ */
+/* Translational periodic patch pairs (BC_PERIODIC, RELPATCH).  The reference */
+/* copies cells near the related patch as virtual cells beyond each periodic  */
+/* patch (modflu/RFLU_ModSymmetryPeriodic.F90:148-335, 471-787) and copies    */
+/* the actual cells' state and gradients into them every stage               */
+/* (libfloflu/RungeKuttaMP.F90:225-236, 448-459).  Here the two patches'      */
+/* vertices are identified instead: their faces pair up as interior faces of */
+/* a periodic mesh, every cell keeps its own vertex coordinates for its       */
+/* geometry, and each face across the period and each stencil member seen    */
+/* across it carries the translation between the two cells' frames.  A cell's */
+/* gradient, fluxes and residual then see the neighbours its virtual cells   */
+/* stand for; what differs is the order of the sums (the reference numbers    */
+/* actual-virtual faces after the actual ones; so do periodic faces here) and */
+/* the virtual cells' own raw gradients, which enter the WENO smoothing of    */
+/* the cells next to the patch: for a flow that varies along the period only, */
+/* as in the reference's periodic gas-jump golden, those equal their actual   */
+/* cells' because every stencil stays symmetric along the period.            */
+/* ------------------------------------------------------------------------ */
+int findRep(std::vector<int> &rep, int v) {
+  while (rep[v] != v) {
+    rep[v] = rep[rep[v]];
+    v = rep[v];
+  }
+  return v;
+}
+
+void identifyPeriodicVertices(orc_ctx *c) {
+  std::vector<int> rep(c->nVert);
+  for (int v = 0; v < c->nVert; ++v) rep[v] = v;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int v = 0; v < c->nVert; ++v)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], c->xyz[3 * v + d]);
+      hi[d] = std::max(hi[d], c->xyz[3 * v + d]);
+    }
+  const double tol = 1e-7 * std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  auto verts = [&](const Patch &p) {
+    std::vector<int> v;
+    for (int i = 0; i < p.n; ++i)
+      for (int k = 0; k < 4; ++k)
+        if (p.bf2v[4 * i + k] >= 0) v.push_back(p.bf2v[4 * i + k]);
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    return v;
+  };
+  for (int ip = 0; ip < (int)c->patches.size(); ++ip) {
+    const Patch &P = c->patches[ip];
+    if (P.bcType != ORC_BC_PERIODIC || P.related <= ip) continue;
+    const Patch &Q = c->patches[P.related];
+    const std::vector<int> vp = verts(P), vq = verts(Q);
+    if (vp.size() != vq.size() || vp.empty()) {
+      std::fprintf(stderr, "oracle: periodic patches %d and %d do not match\n", ip, P.related);
+      std::abort();
+    }
+    std::array<double, 3> T;
+    for (int d = 0; d < 3; ++d) {
+      double sp = 0.0, sq = 0.0;
+      for (int v : vp) sp += c->xyz[3 * v + d];
+      for (int v : vq) sq += c->xyz[3 * v + d];
+      T[d] = (sq - sp) / (double)vp.size();
+    }
+    c->perShift.push_back(T);
+    std::map<std::array<long long, 3>, int> grid;
+    for (int w : vq) {
+      std::array<long long, 3> k;
+      for (int d = 0; d < 3; ++d) k[d] = std::llround(c->xyz[3 * w + d] / tol);
+      grid[k] = w;
+    }
+    for (int v : vp) {
+      int w = -1;
+      std::array<long long, 3> k0;
+      for (int d = 0; d < 3; ++d) k0[d] = std::llround((c->xyz[3 * v + d] + T[d]) / tol);
+      for (int a = -1; a <= 1 && w < 0; ++a)
+        for (int b = -1; b <= 1 && w < 0; ++b)
+          for (int e = -1; e <= 1 && w < 0; ++e) {
+            auto it = grid.find({k0[0] + a, k0[1] + b, k0[2] + e});
+            if (it != grid.end()) w = it->second;
+          }
+      if (w < 0) {
+        std::fprintf(stderr, "oracle: periodic vertex %d has no image on patch %d\n", v, P.related);
+        std::abort();
+      }
+      const int rv = findRep(rep, v), rw = findRep(rep, w);
+      if (rv != rw) rep[std::max(rv, rw)] = std::min(rv, rw);
+    }
+  }
+  for (size_t k = 0; k < c->c2v.size(); ++k) c->c2v[k] = findRep(rep, c->c2vGeo[k]);
+  /* the periodic patches' faces are interior faces now */
+  for (Patch &p : c->patches)
+    if (p.bcType == ORC_BC_PERIODIC) p.n = 0;
+}
+
+/* Offset of stencil member j from cell i, cofg(j) - cofg(i), for the image
+ * of j nearest to i when the mesh is periodic (the virtual cell standing for
+ * j in the reference). */
+void memberOffset(const orc_ctx *c, int i, int j, double &dx, double &dy, double &dz) {
+  dx = c->cofg[3 * j] - c->cofg[3 * i];
+  dy = c->cofg[3 * j + 1] - c->cofg[3 * i + 1];
+  dz = c->cofg[3 * j + 2] - c->cofg[3 * i + 2];
+  if (c->perShift.empty()) return;
+  double best = dx * dx + dy * dy + dz * dz, bx = dx, by = dy, bz = dz;
+  const int np = (int)c->perShift.size();
+  int combos = 1;
+  for (int p = 0; p < np; ++p) combos *= 3;
+  for (int m = 1; m < combos; ++m) {
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    int r = m;
+    for (int p = 0; p < np; ++p, r /= 3) {
+      const double f = (double)(r % 3 == 2 ? -1 : r % 3);
+      sx += f * c->perShift[p][0];
+      sy += f * c->perShift[p][1];
+      sz += f * c->perShift[p][2];
+    }
+    const double ex = dx + sx, ey = dy + sy, ez = dz + sz;
+    const double d2 = ex * ex + ey * ey + ez * ez;
+    if (d2 < best) { best = d2; bx = ex; by = ey; bz = ez; }
+  }
+  dx = bx; dy = by; dz = bz;
+}
 
 /* ------------------------------------------------------------------------ */
 /* Face list: RFLU_BuildFaceList (modflu/RFLU_ModFaceList.F90:784-1585) with  */
@@ -241,19 +367,26 @@ void buildFaceList(orc_ctx *c) {
       }
     }
   }
-  /* interior (AA) faces keep the first-insertion order */
+  /* interior (AA) faces keep the first-insertion order; faces across a
+     period (the reference's actual-virtual faces) follow them in the same
+     order.  f2v: the first cell's own vertex ids (geometry) */
   c->f2c.clear(); c->f2v.clear();
-  for (const Rec &r : rec) {
-    if (r.c2 < 0) continue;
-    c->f2c.push_back(r.c1);
-    c->f2c.push_back(r.c2);
-    for (int k = 0; k < 4; ++k) {
-      int v = -1;
-      if (fvs == 3) { if (k < 3) v = c->c2v[c->nvc * r.c1 + f2vTet[r.ifl][k] - 1]; }
-      else v = c->c2v[c->nvc * r.c1 + f2vHex[r.ifl][k] - 1];
-      c->f2v.push_back(v);
+  for (int pass = 0; pass < 2; ++pass)
+    for (const Rec &r : rec) {
+      if (r.c2 < 0) continue;
+      int fvGeo[4] = {-1, -1, -1, -1};
+      for (int k = 0; k < fvs; ++k)
+        fvGeo[k] = c->c2vGeo[c->nvc * r.c1 + ((fvs == 3) ? f2vTet[r.ifl][k] : f2vHex[r.ifl][k]) - 1];
+      /* across a period: the second cell holds the face's first vertex
+         under another vertex id */
+      bool across = true;
+      for (int k = 0; k < c->nvc; ++k)
+        if (c->c2vGeo[c->nvc * r.c2 + k] == fvGeo[0]) across = false;
+      if (across != (pass == 1)) continue;
+      c->f2c.push_back(r.c1);
+      c->f2c.push_back(r.c2);
+      for (int k = 0; k < 4; ++k) c->f2v.push_back(fvGeo[k]);
     }
-  }
   c->nFaces = (int)c->f2c.size() / 2;
   /* boundary faces: RFLU_UnHashBFace gives the owning cell */
   for (Patch &p : c->patches) {
@@ -333,7 +466,7 @@ void buildGeometry(orc_ctx *c) {
   const int nc = c->nCells;
   std::vector<double> app(3 * nc);
   for (int ic = 0; ic < nc; ++ic) {
-    const int *v = &c->c2v[c->nvc * ic];
+    const int *v = &c->c2vGeo[c->nvc * ic];
     for (int d = 0; d < 3; ++d) {
       double s = c->xyz[3 * v[0] + d];
       for (int k = 1; k < c->nvc; ++k) s = s + c->xyz[3 * v[k] + d];
@@ -344,6 +477,7 @@ void buildGeometry(orc_ctx *c) {
   c->cofg.assign(3 * nc, 0.0);
   c->fn.assign(4 * c->nFaces, 0.0);
   c->fc.assign(3 * c->nFaces, 0.0);
+  c->fc2.assign(3 * c->nFaces, 0.0);
   auto accum = [&](int cell, double sgn, double fx, double fy, double fz, double cx, double cy, double cz) {
     double term = (cx - app[3 * cell]) * fx + (cy - app[3 * cell + 1]) * fy + (cz - app[3 * cell + 2]) * fz;
     if (sgn > 0) c->vol[cell] = c->vol[cell] + term; else c->vol[cell] = c->vol[cell] - term;
@@ -370,7 +504,26 @@ void buildGeometry(orc_ctx *c) {
     faceVectorCentroid(c->xyz.data(), &c->f2v[4 * f], nv, fx, fy, fz, cx, cy, cz);
     store(&c->fn[4 * f], &c->fc[3 * f], fx, fy, fz, cx, cy, cz);
     accum(c->f2c[2 * f], 1.0, fx, fy, fz, cx, cy, cz);
-    accum(c->f2c[2 * f + 1], -1.0, fx, fy, fz, cx, cy, cz);
+    /* the second cell's frame: the translation between the two cells' own
+       coordinates of the face's first vertex (zero unless across a period) */
+    const int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1], a = c->f2v[4 * f];
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < c->nvc; ++k) {
+      if (c->c2vGeo[c->nvc * c1 + k] != a) continue;
+      for (int k2 = 0; k2 < c->nvc; ++k2)
+        if (c->c2v[c->nvc * c2 + k2] == c->c2v[c->nvc * c1 + k]) {
+          const int b = c->c2vGeo[c->nvc * c2 + k2];
+          if (b != a)
+            for (int d = 0; d < 3; ++d) s[d] = c->xyz[3 * b + d] - c->xyz[3 * a + d];
+        }
+    }
+    double *f2 = &c->fc2[3 * f];
+    if (s[0] == 0.0 && s[1] == 0.0 && s[2] == 0.0) {
+      f2[0] = cx; f2[1] = cy; f2[2] = cz;
+    } else {
+      f2[0] = cx + s[0]; f2[1] = cy + s[1]; f2[2] = cz + s[2];
+    }
+    accum(c2, -1.0, fx, fy, fz, f2[0], f2[1], f2[2]);
   }
   for (Patch &p : c->patches) {
     p.fn.assign(4 * p.n, 0.0);
@@ -459,9 +612,8 @@ void buildStencils(orc_ctx *c) {
         std::vector<double> a(degr * 4);
         for (int isl = 0; isl < degr; ++isl) {
           int j = c2cs[isl];
-          double dx = c->cofg[3 * j] - c->cofg[3 * icg];
-          double dy = c->cofg[3 * j + 1] - c->cofg[3 * icg + 1];
-          double dz = c->cofg[3 * j + 2] - c->cofg[3 * icg + 2];
+          double dx, dy, dz;
+          memberOffset(c, icg, j, dx, dy, dz);
           double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
           a[isl] = term; a[isl + degr] = term * dx; a[isl + 2 * degr] = term * dy; a[isl + 3 * degr] = term * dz;
         }
@@ -519,9 +671,8 @@ void buildMoments(orc_ctx *c) {
     for (int k = 0; k < 10; ++k) x[k] = 0.0;
     for (int s = c->stOff[icg]; s < c->stOff[icg + 1]; ++s) {
       int j = c->stIdx[s];
-      double dx = c->cofg[3 * j] - c->cofg[3 * icg];
-      double dy = c->cofg[3 * j + 1] - c->cofg[3 * icg + 1];
-      double dz = c->cofg[3 * j + 2] - c->cofg[3 * icg + 2];
+      double dx, dy, dz;
+      memberOffset(c, icg, j, dx, dy, dz);
       double wt = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
       dx = wt * dx; dy = wt * dy; dz = wt * dz;
       x[0] = x[0] + dx * dx; x[1] = x[1] + dx * dy; x[2] = x[2] + dy * dy;
@@ -583,10 +734,10 @@ void computeGradCells(orc_ctx *c, const std::vector<double> &var, std::vector<do
     double c1111 = c11 * c11, c2222 = c22 * c22, c3333 = c33 * c33;
     double *g = &grad[15 * icg];
     for (int k = 0; k < 15; ++k) g[k] = 0.0;
-    const double xi = c->cofg[3 * icg], yi = c->cofg[3 * icg + 1], zi = c->cofg[3 * icg + 2];
     for (int s = c->stOff[icg]; s < c->stOff[icg + 1]; ++s) {
       int j = c->stIdx[s];
-      double dx = c->cofg[3 * j] - xi, dy = c->cofg[3 * j + 1] - yi, dz = c->cofg[3 * j + 2] - zi;
+      double dx, dy, dz;
+      memberOffset(c, icg, j, dx, dy, dz);
       double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
       dx = term * dx; dy = term * dy; dz = term * dz;
       double term1 = c1111 * (dx);
@@ -644,7 +795,8 @@ void limiterBarthJesp(orc_ctx *c, const std::vector<double> &var, const std::vec
       const int code = c->cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
-      double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
+      const double *fcs = (code & 1) ? &c->fc2[3 * f] : &c->fc[3 * f];
+      double xc = fcs[0], yc = fcs[1], zc = fcs[2];
       double dx1 = c->cofg[3 * ic] - xc, dy1 = c->cofg[3 * ic + 1] - yc, dz1 = c->cofg[3 * ic + 2] - zc;
       for (int iv = 0; iv < 5; ++iv) {
         if (skipVel && iv >= 1 && iv <= 3) continue;
@@ -679,7 +831,8 @@ void limiterVenkat(orc_ctx *c, const std::vector<double> &var, const std::vector
       const int code = c->cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
-      double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
+      const double *fcs = (code & 1) ? &c->fc2[3 * f] : &c->fc[3 * f];
+      double xc = fcs[0], yc = fcs[1], zc = fcs[2];
       double dx1 = c->cofg[3 * ic] - xc, dy1 = c->cofg[3 * ic + 1] - yc, dz1 = c->cofg[3 * ic + 2] - zc;
       double ds1 = std::pow(c->vol[ic], THRD);
       double epsq1 = (K * ds1) * (K * ds1) * (K * ds1);
@@ -825,7 +978,7 @@ void limitGradCellsSimple(orc_ctx *c, const std::vector<double> &var, std::vecto
       const int code = c->cfEnt[e];
       const double *fcp;
       if (code >= 0) {
-        fcp = &c->fc[3 * (code >> 1)];
+        fcp = (code & 1) ? &c->fc2[3 * (code >> 1)] : &c->fc[3 * (code >> 1)];
       } else {
         const int b = -code - 1;
         fcp = &c->patches[c->bPatch[b]].fc[3 * c->bFace[b]];
@@ -882,8 +1035,9 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
       const int code = c->cfEnt[e];
       if (code < 0) continue;
       const int f = code >> 1;
+      const double *fcs = (code & 1) ? &c->fc2[3 * f] : &c->fc[3 * f];
       double off[3];
-      for (int k = 0; k < 3; ++k) off[k] = c->cofg[3 * icl + k] - c->fc[3 * f + k];
+      for (int k = 0; k < 3; ++k) off[k] = c->cofg[3 * icl + k] - fcs[k];
       double shift[3];
       for (int i = 1; i <= 3; ++i) {
         double s = 0.0;
@@ -1188,7 +1342,7 @@ void interiorFlux(orc_ctx *c, int f, double flx[5]) {
   }
   const double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
   FaceState L = reconstruct(c, c1, xc, yc, zc);
-  FaceState Rr = reconstruct(c, c2, xc, yc, zc);
+  FaceState Rr = reconstruct(c, c2, c->fc2[3 * f], c->fc2[3 * f + 1], c->fc2[3 * f + 2]);
   if (disc == 1) {
     double gc = MixtPerf_R_CpG(cp, g);
     double tl = MixtPerf_T_DPR(L.r, L.p, gc), Hl = MixtPerf_Ho_CpTUVW(cp, tl, L.u, L.v, L.w);
@@ -1507,12 +1661,17 @@ orc_ctx *orc_create(const orc_mesh_desc *m, const orc_num_desc *num) {
     p.outflowType = m->patchOutflowType[ip];
     p.pOut = m->patchPout[ip];
     p.order = m->patchOrder[ip];
+    p.related = m->patchRelated ? m->patchRelated[ip] : -1;
     int b = m->patchFaceOff[ip], e = m->patchFaceOff[ip + 1];
     p.n = e - b;
     p.bf2v.assign(m->bf2v + 4 * b, m->bf2v + 4 * e);
     c->patches.push_back(p);
   }
   c->num = *num;
+  c->c2vGeo = c->c2v;
+  bool periodic = false;
+  for (const Patch &p : c->patches) periodic = periodic || p.bcType == ORC_BC_PERIODIC;
+  if (periodic) identifyPeriodicVertices(c);
   buildFaceList(c);
   buildCellFaces(c);
   buildGeometry(c);
@@ -1569,6 +1728,22 @@ void orc_get_patch(orc_ctx *c, int ip, int *bf2c, double *fn, double *fc) {
   if (bf2c) std::memcpy(bf2c, p.bf2c.data(), sizeof(int) * p.n);
   if (fn) std::memcpy(fn, p.fn.data(), sizeof(double) * 4 * p.n);
   if (fc) std::memcpy(fc, p.fc.data(), sizeof(double) * 3 * p.n);
+}
+void orc_get_periodic(orc_ctx *c, double *fc2, double *stShift) {
+  if (fc2) std::memcpy(fc2, c->fc2.data(), sizeof(double) * 3 * c->nFaces);
+  if (stShift)
+    for (int i = 0; i < c->nCells; ++i)
+      for (int s = c->stOff[i]; s < c->stOff[i + 1]; ++s) {
+        const int j = c->stIdx[s];
+        double dx, dy, dz;
+        memberOffset(c, i, j, dx, dy, dz);
+        /* the translation of the member's image, exactly as applied */
+        const double px = c->cofg[3 * j] - c->cofg[3 * i], py = c->cofg[3 * j + 1] - c->cofg[3 * i + 1],
+                     pz = c->cofg[3 * j + 2] - c->cofg[3 * i + 2];
+        stShift[3 * s] = (dx == px) ? 0.0 : dx - px;
+        stShift[3 * s + 1] = (dy == py) ? 0.0 : dy - py;
+        stShift[3 * s + 2] = (dz == pz) ? 0.0 : dz - pz;
+      }
 }
 void orc_get_stencil(orc_ctx *c, int *off, int *idx, double *moms) {
   if (off) std::memcpy(off, c->stOff.data(), sizeof(int) * (c->nCells + 1));

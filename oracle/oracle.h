@@ -31,9 +31,10 @@
 extern "C" {
 #endif
 
-/* Boundary condition types (modfloflu/ModParameters.F90:401,413). */
+/* Boundary condition types (modfloflu/ModParameters.F90:401,413,438). */
 #define ORC_BC_OUTFLOW 20
 #define ORC_BC_SLIPWALL 60
+#define ORC_BC_PERIODIC 110
 
 typedef struct {
   int nVert;
@@ -48,6 +49,11 @@ typedef struct {
   const int *patchOutflowType; /* 0 supersonic, 1 subsonic, 2 mixed */
   const double *patchPout; /* outflow static pressure */
   const int *patchOrder;   /* 1 or 2 */
+  /* translational periodic patch pairs (BC_PERIODIC with RELPATCH): the
+     0-based related patch of each patch, -1 for none; NULL: no periodic
+     patches.  The two patches' faces are paired by their vertex
+     coordinates, which differ by one translation per pair. */
+  const int *patchRelated;
 } orc_mesh_desc;
 
 typedef struct {
@@ -74,6 +80,10 @@ void orc_get_faces(orc_ctx *c, int *f2c, int *f2v, double *fn, double *fc);
 void orc_get_cells(orc_ctx *c, double *vol, double *cofg);
 void orc_get_patch(orc_ctx *c, int iPatch, int *bf2c, double *fn, double *fc);
 void orc_get_stencil(orc_ctx *c, int *off, int *idx, double *moms);
+/* Periodic meshes: fc2(3,nFaces) each face's centroid in its second cell's
+ * frame (= fc off the periods) and stShift(3,nnz) the translation of each
+ * stencil member's image (0 off the periods); either may be NULL. */
+void orc_get_periodic(orc_ctx *c, double *fc2, double *stShift);
 
 /* State. cv(5,nCells) conserved; dv(3,nCells) = p,T,c. */
 void orc_set_state(orc_ctx *c, const double *cv);

@@ -20,7 +20,7 @@ class MeshDesc(C.Structure):
                 ("nPatches", C.c_int), ("patchFaceOff", C.POINTER(C.c_int)),
                 ("bf2v", C.POINTER(C.c_int)), ("patchBcType", C.POINTER(C.c_int)),
                 ("patchOutflowType", C.POINTER(C.c_int)), ("patchPout", C.POINTER(C.c_double)),
-                ("patchOrder", C.POINTER(C.c_int))]
+                ("patchOrder", C.POINTER(C.c_int)), ("patchRelated", C.POINTER(C.c_int))]
 
 
 class NumDesc(C.Structure):
@@ -72,6 +72,8 @@ def lib():
         L.orc_get_cells.argtypes = [P, DP, DP]
         L.orc_get_patch.argtypes = [P, C.c_int, IP, DP, DP]
         L.orc_get_stencil.argtypes = [P, IP, IP, DP]
+        L.orc_get_periodic.argtypes = [P, DP, DP]
+        L.orc_get_periodic.restype = None
         L.orc_set_state.argtypes = [P, DP]
         L.orc_get_state.argtypes = [P, DP, DP]
         L.orc_get_rhs.argtypes = [P, DP]
@@ -124,7 +126,8 @@ def _mesh_arrays(case):
     oft = np.array([p.outflow_type for p in case.patches], dtype=np.int32)
     pout = np.array([p.p_out for p in case.patches], dtype=np.float64)
     order = np.array([p.order for p in case.patches], dtype=np.int32)
-    return xyz, c2v, off, bf2v, bct, oft, pout, order
+    rel = np.array([getattr(p, "related", -1) for p in case.patches], dtype=np.int32)
+    return xyz, c2v, off, bf2v, bct, oft, pout, order, rel
 
 
 def num_desc(num):
@@ -139,10 +142,11 @@ class Oracle:
     def __init__(self, case):
         self.case = case
         self._keep = _mesh_arrays(case)
-        xyz, c2v, off, bf2v, bct, oft, pout, order = self._keep
+        xyz, c2v, off, bf2v, bct, oft, pout, order, rel = self._keep
         md = MeshDesc(xyz.shape[0], c2v.shape[0], c2v.shape[1], _ptr(xyz, C.c_double), _ptr(c2v, C.c_int),
                       len(case.patches), _ptr(off, C.c_int), _ptr(bf2v, C.c_int), _ptr(bct, C.c_int),
-                      _ptr(oft, C.c_int), _ptr(pout, C.c_double), _ptr(order, C.c_int))
+                      _ptr(oft, C.c_int), _ptr(pout, C.c_double), _ptr(order, C.c_int),
+                      _ptr(rel, C.c_int) if (rel >= 0).any() else None)
         self.nd = num_desc(case.num)
         self.h = lib().orc_create(C.byref(md), C.byref(self.nd))
         self.n_cells = c2v.shape[0]
@@ -178,6 +182,15 @@ class Oracle:
         fc = np.zeros((n, 3))
         lib().orc_get_patch(self.h, ip, _ptr(bf2c, C.c_int), _ptr(fn, C.c_double), _ptr(fc, C.c_double))
         return bf2c, fn, fc
+
+    def periodic(self):
+        """(fc2 (nFaces, 3), stShift (nnz, 3)): face centroids in the second
+        cell's frame and the translation of each stencil member's image."""
+        nnz = lib().orc_stencil_nnz(self.h)
+        fc2 = np.zeros((self.n_faces, 3))
+        sh = np.zeros((max(nnz, 1), 3))
+        lib().orc_get_periodic(self.h, _ptr(fc2, C.c_double), _ptr(sh, C.c_double))
+        return fc2, sh[:nnz]
 
     def stencil(self):
         off = np.zeros(self.n_cells + 1, np.int32)

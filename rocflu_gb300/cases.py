@@ -19,6 +19,7 @@ from . import meshgen
 
 BC_OUTFLOW = 20
 BC_SLIPWALL = 60
+BC_PERIODIC = 110
 
 DISCR_ROE, DISCR_HLLC, DISCR_AUSM = 1, 3, 4
 RECONST_NONE, RECONST_BJ, RECONST_VENKAT, RECONST_BJ_COMP = 0, 10, 11, 100
@@ -34,6 +35,7 @@ class Patch:
     p_out: float = 0.0
     order: int = 1
     name: str = ""
+    related: int = -1       # BC_PERIODIC: the 0-based related patch (RELPATCH)
 
 
 @dataclass
@@ -113,6 +115,24 @@ def gas_jump_closed(n=8, length=0.008, x_jump=0.0043, left=(1.2, 0.0, 101325.0),
     z = np.zeros_like(d)
     cv0 = np.stack([d, d * u, z, z, d * (p / (d * (g - 1.0)) + 0.5 * (u * u))], axis=1)
     return Case("gas_jump_closed", mesh["xyz"], mesh["c2v"], patches, num, cv0, end_time=1.05e-4)
+
+
+def gas_jump_periodic(n=8, length=0.008, x_jump=0.0043, left=(1.2, 0.0, 101325.0), right=(0.97, 82700.0)):
+    """The reference test suite's periodic gas-jump box (tests/goldens/box/
+    gas-jump/periodic/np1; the deck of gas_jump_closed with the golden's
+    overrides, one region): the same n^3 hexes and hard-coded jump, periodic
+    on all three axes (the harness's bc layout 'periodic', tests/
+    rocpicl_tests/case.py:230-235: x-low/x-high, y-low/y-high and
+    z-low/z-high translational pairs), so the jump at x_jump and the one at
+    x = 0 = length both evolve; HLLC, second order, WENO-XYZ + the simple
+    limiter, Wray RK3, CFL 0.4, TIMESTEP 1e-9, run to t = 1.05e-4."""
+    c = gas_jump_closed(n, length, x_jump, left, right)
+    for i, p in enumerate(c.patches):
+        p.bc_type = BC_PERIODIC
+        p.related = i ^ 1
+        p.order = 1
+    c.name = "gas_jump_periodic"
+    return c
 
 
 def sod(nx=400, ny=4, nz=4, num=None):

@@ -333,3 +333,52 @@ def test_oracle_stage_pieces_equal_whole_stage():
         o.rk_update(1, dt)
     dmom = q.state()[0][:, 2] - p.state()[0][:, 2]
     np.testing.assert_allclose(dmom, -(8.0 / 15.0) * dt * np.ones_like(dmom), rtol=1e-9, atol=1e-15)
+
+
+def test_periodic_gas_jump_against_reference_golden():
+    """Translational periodic patches (BC_PERIODIC) as a periodic mesh: the
+    reference's periodic gas-jump box (tests/goldens/box/gas-jump/periodic/
+    np1, extracted by tests/golden/make_gas_jump_periodic.py) to t = 1.05e-4.
+    The oracle conserves mass and energy to round-off and keeps the flow
+    one-dimensional.  The reference's result is not one-dimensional: its
+    virtual cells near the box's edges and corners (copies built per patch,
+    modflu/RFLU_ModSymmetryPeriodic.F90:471-787, whose own stencils and raw
+    gradients enter the WENO smoothing of the cells next to the patches)
+    leave a y/z variation of 6.4e-5 of the density maximum in the golden.
+    The oracle's x profile lies within that variation of the golden's y/z
+    mean (6.6e-5 in density, 1e-5 in energy), not within the harness's 1e-10,
+    which would need those virtual cells restated."""
+    import json
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gas_jump_periodic_np1.json")
+    with open(path) as f:
+        golden = json.load(f)
+    G = np.stack([np.array(golden["gas"]["0"][n]) for n in ("q1", "q2", "q3", "q4", "q5")], axis=1)
+    G = G.reshape(8, 8, 8, 5)  # z, y, x
+    c = cases.gas_jump_periodic()
+    o = Oracle(c)
+    vol, _ = o.cells()
+    m0, e0 = (c.cv0[:, 0] * vol).sum(), (c.cv0[:, 4] * vol).sum()
+    _, t = o.run(100000, 0.0, c.end_time)
+    assert abs(t - golden["time"]) <= 1e-9 * golden["time"]
+    cv, _ = o.state()
+    assert abs((cv[:, 0] * vol).sum() - m0) <= 1e-13 * m0
+    assert abs((cv[:, 4] * vol).sum() - e0) <= 1e-13 * e0
+    assert abs((cv[:, 0] * vol).sum() - golden["totals"]["gas_rho"]) <= 1e-13 * m0
+    ix = gas_jump_layer(c)
+    prof = np.array([cv[ix == k].mean(axis=0) for k in range(8)])
+    for k in range(8):
+        assert np.abs(cv[ix == k] - prof[k]).max() <= 1e-9 * np.abs(prof).max()
+    scale = np.abs(G[..., 0]).max()
+    golden_spread = np.abs(G[..., 0] - G[..., 0].mean(axis=(0, 1))).max() / scale
+    assert 5e-5 < golden_spread < 1e-4
+    gm = G.mean(axis=(0, 1))
+    assert np.abs(prof[:, 0] - gm[:, 0]).max() / scale <= 1.2 * golden_spread
+    assert np.abs(prof[:, 4] - gm[:, 4]).max() / np.abs(G[..., 4]).max() <= 2e-5
+
+
+def gas_jump_layer(case):
+    from golden import gas_jump
+
+    return gas_jump.layer_of_cells(case)
