@@ -374,6 +374,9 @@ def run_ours(args):
     adjoint = None
     if not args.skip_adjoint:
         adjoint = single_adjoint(args, cases, gpu)
+        # the headline's limiter: Barth-Jespersen with the eigen-frame
+        # velocity limiter (RECONST 10)
+        adjoint["eigenframe"] = single_adjoint(args, cases, gpu, reconst=cases.RECONST_BJ, n_dirs=32)
     unrolled = None if args.skip_unrolled else unrolled_adjoint(args, cases, gpu)
     weno = None if args.skip_weno else weno_variant(args, cases, gpu, setup, case.num.dt_imposed)
     tets = None if args.skip_tets else tet_block(args, cases, gpu)
@@ -418,26 +421,36 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def single_adjoint(args, cases, gpu):
+def single_adjoint(args, cases, gpu, reconst=None, n_dirs=64):
     """One VJP of the residual and the gradient of J = sum_{x=1 patch} p_f |A_f|
     on the 32^3 x 6 jittered-tet case, FP64 and mixed: times, VJP/primal,
-    and central differences (eps = 1e-6, FP64 residual) of J on 64 seeded
-    directions."""
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=cases.RECONST_BJ_COMP)
+    and central differences (eps = 1e-6, FP64 residual) of J on seeded
+    directions.  Each direction is classified by whether any cell's limiter
+    changes its active branch (face or extreme neighbour) between U - eps v,
+    U and U + eps v (rflu_gpu_limiter_branches): the functional is smooth
+    along the others, which the adjoint must match to 1e-6."""
+    if reconst is None:
+        reconst = cases.RECONST_BJ_COMP
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=reconst)
     ac = cases.adjoint_tets(args.adj_n, num=num)
     areg, mreg = gpu.Region(ac, "fp64"), gpu.Region(ac, "mixed")
-    out = {"workload": "adjoint_tets%d_roe_bjcomp" % args.adj_n, "cells": areg.n_cells,
+    tag = {cases.RECONST_BJ_COMP: "bjcomp", cases.RECONST_BJ: "bj_eigenframe", cases.RECONST_VENKAT: "venkat"}[reconst]
+    out = {"workload": "adjoint_tets%d_roe_%s" % (args.adj_n, tag), "cells": areg.n_cells,
            "functional": "sum_{x=1 patch} p_f |A_f|"}
     rng = np.random.default_rng(2)
     scale = np.abs(ac.cv0).mean(axis=0)
-    dirs = [rng.standard_normal(ac.cv0.shape) * scale for _ in range(64)]
+    dirs = [rng.standard_normal(ac.cv0.shape) * scale for _ in range(n_dirs)]
     eps = 1e-6
-    fd = []
+    fd, switch = [], []
+    b0 = areg.limiter_branches(ac.cv0)
     for v in dirs:
         jp, _ = areg.patch_pressure(ac.cv0 + eps * v, 1, with_grad=False)
         jm, _ = areg.patch_pressure(ac.cv0 - eps * v, 1, with_grad=False)
         fd.append((jp - jm) / (2 * eps))
-    fd = np.array(fd)
+        bp, bm = areg.limiter_branches(ac.cv0 + eps * v), areg.limiter_branches(ac.cv0 - eps * v)
+        switch.append(int((bp != b0).any(axis=2).sum() + (bm != b0).any(axis=2).sum()))
+    fd, switch = np.array(fd), np.array(switch)
+    smooth = switch == 0
     lam = np.random.default_rng(5).standard_normal(ac.cv0.shape)
     g_ref = None
     for name, reg in (("fp64", areg), ("mixed", mreg)):
@@ -448,7 +461,14 @@ def single_adjoint(args, cases, gpu):
         res = {"primal_residual_ms": at[0], "vjp_ms": at[1], "vjp_over_primal": at[1] / at[0], "J": J,
                "fd_eps": eps, "fd_dirs": len(err), "fd_rel_err_median": float(np.median(err)),
                "fd_rel_err_max": float(err.max()), "fd_dirs_below_1e-6": int((err < 1e-6).sum()),
-               "fd_dirs_below_1e-5": int((err < 1e-5).sum())}
+               "fd_dirs_below_1e-5": int((err < 1e-5).sum()),
+               "branch_switch": {"dirs_without_switch": int(smooth.sum()),
+                                 "without_switch_below_1e-6": int((err[smooth] < 1e-6).sum()),
+                                 "without_switch_err_max": float(err[smooth].max()) if smooth.any() else None,
+                                 "with_switch": int((~smooth).sum()),
+                                 "with_switch_below_1e-6": int((err[~smooth] < 1e-6).sum()),
+                                 "switching_cell_variables_median": float(np.median(switch[~smooth]))
+                                 if (~smooth).any() else None}}
         if g_ref is None:
             g_ref = g
             out.update(res)

@@ -225,6 +225,13 @@ MODULE RFLU_ModGPU
       REAL(C_DOUBLE), INTENT(OUT) :: rhsDot(*)
     END FUNCTION rflu_gpu_jvp
 
+    INTEGER(C_INT) FUNCTION rflu_gpu_limiter_branches(ctx, cv, branches) BIND(C, NAME='rflu_gpu_limiter_branches')
+      IMPORT :: C_INT, C_PTR, C_DOUBLE
+      TYPE(C_PTR), VALUE :: ctx
+      REAL(C_DOUBLE), INTENT(IN) :: cv(*)
+      INTEGER(C_INT), INTENT(OUT) :: branches(*)
+    END FUNCTION rflu_gpu_limiter_branches
+
     INTEGER(C_INT) FUNCTION rflu_gpu_patch_pressure(ctx, cv, iPatch, J, cvBar) BIND(C, NAME='rflu_gpu_patch_pressure')
       IMPORT :: C_INT, C_PTR, C_DOUBLE
       TYPE(C_PTR), VALUE :: ctx

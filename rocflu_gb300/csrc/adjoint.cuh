@@ -28,8 +28,9 @@
 //      then prim/dv -> cv through the local Jacobian (Dual<5> in FP64; the
 //      mixed mode's closed form in FP32).
 // No atomics: every sum is a gather in a fixed order.  The adjoint covers
-// RECONST 0, 11 (Venkatakrishnan) and 100 (componentwise BJ); the
-// eigen-frame velocity limiter of RECONST 10 is covered by the tangent only.
+// RECONST 0, 11 (Venkatakrishnan), 100 (componentwise BJ) and 10 (BJ with the
+// eigen-frame velocity limiter, whose eigenvectors are differentiated by
+// first-order perturbation in the tangent and the adjoint alike).
 #pragma once
 #include "dual.cuh"
 #include "roe_adjoint.cuh"
@@ -41,24 +42,26 @@ template <typename R>
 struct AdjWork {
   R *cvd, *primd, *dvd, *gradd, *fluxd;  // tangent state / lambda in cvd
   R *G, *lim, *faceAdj, *Gbar, *qbar, *nbBar, *cvbarD, *dvbar;
+  R *nbVel;                              // FP64 layouts, RECONST 10: per axis the neighbour's velocity share (9 Nc)
   int *estar, *jstar;                    // 5 per cell each
   // packed layout: per cell i a 16-float record (L_i Gbar_i for the five
   // variables, 15 floats; pad), so that a transposed stencil entry of cell j
   // costs two 256-bit loads next to its weights from View::tsW:
   // w_s . Gbar_i = (d/|d|^2) . (L_i Gbar_i), d = x_j - x_i (L symmetric)
   R *adjRec;
-  // packed layout: per cell a 12-word record of the limiter's extreme-
+  // packed layout: per cell a 20-word record of the limiter's extreme-
   // neighbour terms: for each variable the neighbour that receives one (-1:
-  // none; int bits), then its value, then pad
+  // none; int bits; RECONST 10: the eigen-frame axes in slots 1-3), then the
+  // variables' values, then the axes' velocity vectors, then pad
   R *nbRec;
   // packed layout: per cell the sum over its stencil of d/|d|^2 (3 Nc, SoA),
   // so that the gradient's own term in the adjoint is one dot product
   R *ssum;
 };
 
-// The workspace carved from the context's adjoint buffer: 81 Nc + 21 (Nf+Nb)
-// values of R, 10 Nc ints and (packed layout) 16 + 12 + 3 Nc floats on a 32-byte
-// boundary (the context allocates sizeof(R)*(120 Nc + 24 (Nf+Nb) + 64) +
+// The workspace carved from the context's adjoint buffer: 90 Nc + 21 (Nf+Nb)
+// values of R, 10 Nc ints and (packed layout) 16 + 20 + 3 Nc floats on a 32-byte
+// boundary (the context allocates sizeof(R)*(130 Nc + 24 (Nf+Nb) + 64) +
 // 4*10 Nc + 256 bytes).
 template <typename R>
 inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
@@ -82,6 +85,7 @@ inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
   a.nbBar = take(5 * nc);
   a.cvbarD = take(5 * nc);
   a.dvbar = take(3 * nc);
+  a.nbVel = take(9 * nc);
   a.estar = reinterpret_cast<int *>(p);
   p += sizeof(int) * 5 * nc;
   a.jstar = reinterpret_cast<int *>(p);
@@ -89,7 +93,7 @@ inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
   p = reinterpret_cast<char *>((reinterpret_cast<size_t>(p) + 31) & ~size_t(31));
   a.adjRec = reinterpret_cast<R *>(p);
   a.nbRec = a.adjRec + 16 * nc;
-  a.ssum = a.nbRec + 12 * nc;
+  a.ssum = a.nbRec + 20 * nc;
   return a;
 }
 
@@ -245,9 +249,263 @@ __device__ inline S venkat(S dext, S d2, S epsq) {
   return numer / (denom + S(1.0e-12));
 }
 
+// The eigen-frame velocity limiter of one cell (RECONST 10,
+// RFLU_LimitGradVelocityBarthJesp, modflu/RFLU_ModLimiters.F90:588-790) as
+// the tangent kernels evaluate it (gradLimitCell on dual numbers: per-face
+// minima, eigenpairs of the strain rate with perturbation derivatives), with
+// the branch each axis's factor takes, for the reverse pass.  G is the
+// unlimited velocity gradient, G[a + 3c] = d u_a / d x_c.
+template <typename R>
+struct VelFrame {
+  R A[9], ev[3];   // eigenvectors (component r of axis j at A[r + 3j]) and eigenvalues
+  R B[9];          // A^T G: B[j + 3c] = sum_a A[a + 3j] G[a + 3c]
+  R alRaw[3];      // each axis's factor before the merge of equal eigenvalues
+  R al[3];         // after it
+  int src[3];      // the axis whose raw factor al[j] equals
+  int side[3];     // 0: alRaw = 1; 1: dmx / pr; 2: dmn / pr
+  int face[3];     // cell-face entry of the active projection pr
+  int nb[3];       // neighbour of the active extreme dmx or dmn (-1: the extreme is the initial 0)
+  R dext[3], pext[3];
+};
+
+template <typename R, typename L>
+__device__ inline void velFrameForward(const View<R> &V, const L &ld, int i, const R *G, VelFrame<R> &F) {
+  R Sy[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) Sy[a + 3 * b] = R(0.5) * (G[a + 3 * b] + G[b + 3 * a]);
+  symmetricEigen3(Sy, F.A, F.ev);
+  const R *A = F.A;
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      R s = R(0);
+      s = s + A[3 * j] * G[3 * c];
+      s = s + A[3 * j + 1] * G[1 + 3 * c];
+      s = s + A[3 * j + 2] * G[2 + 3 * c];
+      F.B[j + 3 * c] = s;
+    }
+  R dmn[3] = {R(0), R(0), R(0)}, dmx[3] = {R(0), R(0), R(0)};
+  int nmn[3] = {-1, -1, -1}, nmx[3] = {-1, -1, -1};
+  const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  for (int e = cb; e < ce; ++e) {
+    const int code = V.cfEnt[e];
+    if (code < 0) continue;
+    int c1, c2;
+    faceCells(V, code >> 1, c1, c2);
+    R a1[4], a2[4], du[3];
+    ld.prim4(c1, a1);
+    ld.prim4(c2, a2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) du[k] = a2[1 + k] - a1[1 + k];
+    const int other = (code & 1) ? c1 : c2;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      R pr = R(0);
+      pr = pr + A[3 * j] * du[0];
+      pr = pr + A[3 * j + 1] * du[1];
+      pr = pr + A[3 * j + 2] * du[2];
+      if (code & 1) pr = -pr;
+      if (pr < dmn[j]) { dmn[j] = pr; nmn[j] = other; }
+      if (pr > dmx[j]) { dmx[j] = pr; nmx[j] = other; }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    F.alRaw[j] = R(1); F.side[j] = 0; F.face[j] = -1; F.nb[j] = -1; F.dext[j] = R(0); F.pext[j] = R(1);
+  }
+  for (int e = cb; e < ce; ++e) {
+    const int code = V.cfEnt[e];
+    if (code < 0) continue;
+    R d[3];
+    faceOffset(V, code >> 1, code & 1, d);
+    const R off[3] = {-d[0], -d[1], -d[2]};
+    R sh[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      R s = R(0);
+      s = s + G[a] * off[0];
+      s = s + G[a + 3] * off[1];
+      s = s + G[a + 6] * off[2];
+      sh[a] = s;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      R pr = R(0);
+      pr = pr + A[3 * j] * sh[0];
+      pr = pr + A[3 * j + 1] * sh[1];
+      pr = pr + A[3 * j + 2] * sh[2];
+      if (pr > R(0)) {
+        const R t = dmx[j] / pr;
+        if (t < F.alRaw[j]) { F.alRaw[j] = t; F.side[j] = 1; F.face[j] = e; F.nb[j] = nmx[j]; F.dext[j] = dmx[j]; F.pext[j] = pr; }
+      } else if (pr < R(0)) {
+        const R t = dmn[j] / pr;
+        if (t < F.alRaw[j]) { F.alRaw[j] = t; F.side[j] = 2; F.face[j] = e; F.nb[j] = nmn[j]; F.dext[j] = dmn[j]; F.pext[j] = pr; }
+      }
+    }
+  }
+  // merge the factors of equal eigenvalues (within 1e-3 of the largest magnitude)
+  R mx = fabs_(F.ev[0]);
+  mx = fmax2(mx, fabs_(F.ev[1]));
+  mx = fmax2(mx, fabs_(F.ev[2]));
+  const R scale = R(1.0e-3) * mx;
+  const bool e12 = (F.ev[1] - F.ev[0] <= scale), e23 = (F.ev[2] - F.ev[1] <= scale);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) { F.al[j] = F.alRaw[j]; F.src[j] = j; }
+  // fmin2's choice (the first of equal values), by selects only (no
+  // run-time array index)
+  if (e12 && e23) {
+    const bool b01 = F.alRaw[1] < F.alRaw[0];
+    const R v01 = b01 ? F.alRaw[1] : F.alRaw[0];
+    const bool b2 = F.alRaw[2] < v01;
+    const R v = b2 ? F.alRaw[2] : v01;
+    const int m = b2 ? 2 : (b01 ? 1 : 0);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { F.al[j] = v; F.src[j] = m; }
+  } else if (e12) {
+    const bool b = F.alRaw[1] < F.alRaw[0];
+    F.al[0] = F.al[1] = b ? F.alRaw[1] : F.alRaw[0];
+    F.src[0] = F.src[1] = b ? 1 : 0;
+  } else if (e23) {
+    const bool b = F.alRaw[2] < F.alRaw[1];
+    F.al[1] = F.al[2] = b ? F.alRaw[2] : F.alRaw[1];
+    F.src[1] = F.src[2] = b ? 2 : 1;
+  }
+}
+
+// Limited velocity gradient from the frame: A diag(al) A^T G, in the
+// primal's operation order; gl[3 * (1 + a) + c].
+template <typename R>
+__device__ inline void velFrameApply(const VelFrame<R> &F, R *gl) {
+  R Rm[9];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Rm[j + 3 * c] = F.al[j] * F.B[j + 3 * c];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      R s = R(0);
+      s = s + F.A[a] * Rm[3 * c];
+      s = s + F.A[a + 3] * Rm[1 + 3 * c];
+      s = s + F.A[a + 6] * Rm[2 + 3 * c];
+      gl[3 * (1 + a) + c] = s;
+    }
+}
+
+// Reverse of the limiter: from glb (adjoint of the limited velocity
+// gradient, glb[a + 3c]) to Gb (of the unlimited one), ub (of the cell's
+// own velocity) and, per axis j, the velocity adjoint nbv[3j..3j+2] that
+// neighbour F.nb[j] receives (when F.side[j] and F.nb[j] >= 0).  The
+// transpose of the tangent's linear map: Gl = sum_j al_j A_j B_j with
+// B = A^T G; the active factor al = dext / pr, dext = A_j . (u_nb - u_i),
+// pr = A_j . G (cofg - fc); the eigenvectors' perturbation
+// da_j = sum_{k != j} a_k (a_k' dS a_j) / (l_j - l_k), S = sym(G).
+template <typename R, typename L>
+__device__ inline void velFrameReverse(const View<R> &V, const L &ld, int i, const R *G, const VelFrame<R> &F,
+                                       const R *glb, R *Gb, R *ub, R *nbv) {
+  const R *A = F.A;
+  R Ab[9], Bb[9], alb[3] = {R(0), R(0), R(0)};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { Ab[k] = R(0); Gb[k] = R(0); nbv[k] = R(0); }
+  ub[0] = ub[1] = ub[2] = R(0);
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      // M = diag(al) B, Gl = A M
+      R mb = R(0);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        mb += A[a + 3 * j] * glb[a + 3 * c];
+        Ab[a + 3 * j] += glb[a + 3 * c] * F.al[j] * F.B[j + 3 * c];
+      }
+      Bb[j + 3 * c] = F.al[j] * mb;
+      alb[j] += mb * F.B[j + 3 * c];
+    }
+  R albRaw[3] = {R(0), R(0), R(0)};
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int t = 0; t < 3; ++t)
+      if (F.src[j] == t) albRaw[t] += alb[j];
+  R ui[4];
+  ld.prim4(i, ui);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    if (F.side[j] == 0 || albRaw[j] == R(0)) continue;
+    // alRaw = dext / pr: the same guarded form as the scalar limiter's
+    const R r = albRaw[j] / F.pext[j];
+    const R dextb = r, prb = -r * (F.dext[j] / F.pext[j]);
+    if (F.nb[j] >= 0) {
+      R un[4];
+      ld.prim4(F.nb[j], un);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        Ab[a + 3 * j] += dextb * (un[1 + a] - ui[1 + a]);
+        nbv[3 * j + a] = dextb * A[a + 3 * j];
+        ub[a] -= dextb * A[a + 3 * j];
+      }
+    }
+    // pr = A_j . G off, off = cofg - fc of the active face
+    const int code = V.cfEnt[F.face[j]];
+    R d[3];
+    faceOffset(V, code >> 1, code & 1, d);
+    const R off[3] = {-d[0], -d[1], -d[2]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const R sh = G[a] * off[0] + G[a + 3] * off[1] + G[a + 6] * off[2];
+      Ab[a + 3 * j] += prb * sh;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Gb[a + 3 * c] += prb * A[a + 3 * j] * off[c];
+    }
+  }
+  // B = A^T G
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        Ab[a + 3 * j] += G[a + 3 * c] * Bb[j + 3 * c];
+        Gb[a + 3 * c] += A[a + 3 * j] * Bb[j + 3 * c];
+      }
+  // eigenvectors of S = sym(G): Sb = sum_{j<k} coef_jk sym(a_k a_j')
+  R Sb[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Sb[k] = R(0);
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int k = j + 1; k < 3; ++k) {
+      if (F.ev[j] == F.ev[k]) continue;
+      R ajk = R(0), akj = R(0);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        ajk += Ab[a + 3 * j] * A[a + 3 * k];
+        akj += Ab[a + 3 * k] * A[a + 3 * j];
+      }
+      const R coef = (ajk - akj) / (F.ev[j] - F.ev[k]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) Sb[a + 3 * b] += coef * R(0.5) * (A[a + 3 * k] * A[b + 3 * j] + A[a + 3 * j] * A[b + 3 * k]);
+    }
+  // S = (G + G') / 2
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) Gb[a + 3 * b] += R(0.5) * (Sb[a + 3 * b] + Sb[b + 3 * a]);
+}
+
 // Forward pass of the limited gradient with the limiter's active branch;
 // with lamRef, also kAdjLambda's copy of the cell's adjoint seed.
-template <typename R>
+// kVel: compiled with the eigen-frame velocity limiter (RECONST 10), so that
+// the other limiters keep their smaller register allocation.
+template <typename R, bool kVel>
 __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, const double *lamRef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
@@ -320,7 +578,7 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
   const int rc = V.p.reconst;
   R lim[5] = {R(1), R(1), R(1), R(1), R(1)};
   int es[5] = {-1, -1, -1, -1, -1}, js[5] = {-1, -1, -1, -1, -1};
-  if (rc == 11 || rc == 100) {
+  if (rc == 11 || rc == 100 || rc == 10) {
     R vmin[5], vmax[5];
     int jmin[5], jmax[5];
 #pragma unroll
@@ -348,6 +606,7 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
       faceOffset(V, code >> 1, code & 1, d);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
+        if (rc == 10 && k >= 1 && k <= 3) continue;  // the eigen-frame limiter below
         const R d2 = -(g[3 * k] * d[0] + g[3 * k + 1] * d[1] + g[3 * k + 2] * d[2]);
         if (!(d2 > R(0)) && !(d2 < R(0))) continue;
         const bool up = d2 > R(0);
@@ -378,6 +637,16 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
     W.jstar[k * n + i] = js[k];
 #pragma unroll
     for (int c = 0; c < 3; ++c) gl[3 * k + c] = lim[k] * g[3 * k + c];
+  }
+  if constexpr (kVel) {
+    R G[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) G[a + 3 * c] = g[3 * (1 + a) + c];
+    VelFrame<R> F;
+    velFrameForward(V, ld, i, G, F);
+    velFrameApply(F, gl);
   }
   storeGrad(V, i, gl);
 }
@@ -506,8 +775,8 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int 
 }
 
 // Side adjoints -> primitive / gradient adjoints of the cell, limiter reverse,
-// gradient own-term.
-template <typename R>
+// gradient own-term.  kVel: with the eigen-frame velocity limiter (RECONST 10).
+template <typename R, bool kVel>
 __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.nc) return;
@@ -573,6 +842,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     if (P.spaceOrder < 2) break;
+    if (rc == 10 && k >= 1 && k <= 3) continue;  // the eigen-frame limiter below
     const R l = W.lim[k * n + i];
     R lb = R(0);
 #pragma unroll
@@ -581,7 +851,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
       lb += gtb[3 * k + c] * W.G[(3 * k + c) * n + i];
     }
     const int es = W.estar[k * n + i];
-    if ((rc == 11 || rc == 100) && es >= 0) {
+    if ((rc == 11 || rc == 100 || rc == 10) && es >= 0) {
       const int code = V.cfEnt[es];
       R dxyz[3];
       faceOffset(V, code >> 1, code & 1, dxyz);
@@ -615,6 +885,34 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
         nbt[k] = js;
       }
     }
+  }
+  // the eigen-frame velocity limiter in reverse; the neighbours' shares go
+  // out per axis (velocity vectors), gathered by kAdjCell2
+  R nbv[9];
+  int nbAx[3] = {-1, -1, -1};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) nbv[k] = R(0);
+  if (kVel && P.spaceOrder > 1) {
+    R G[9], glb[9], Gb[9], ub[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        G[a + 3 * c] = W.G[(3 * (1 + a) + c) * n + i];
+        glb[a + 3 * c] = gtb[3 * (1 + a) + c];
+      }
+    VelFrame<R> F;
+    velFrameForward(V, ld, i, G, F);
+    velFrameReverse(V, ld, i, G, F, glb, Gb, ub, nbv);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      qb[1 + a] += ub[a];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gb[3 * (1 + a) + c] = Gb[a + 3 * c];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (F.side[j] != 0 && F.nb[j] >= 0) nbAx[j] = F.nb[j];
   }
   // gradient own-term: G_i = sum_s w_s (q_{m_s} - q_i)
   if constexpr (!Layout<R>::packed) {
@@ -656,13 +954,29 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     W.cvbarD[k * n + i] = cvb[k];
   }
   if constexpr (Layout<R>::packed) {
-    float *nr = W.nbRec + 12 * (size_t)i;
+    // 20-word record: the variables' receiving neighbours (the eigen-frame
+    // limiter's axes in slots 1-3), their values, the axes' vectors
+    float *nr = W.nbRec + 20 * (size_t)i;
+    if (kVel) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) nbt[1 + j] = nbAx[j];
+    }
     st4(nr, __int_as_float(nbt[0]), __int_as_float(nbt[1]), __int_as_float(nbt[2]), __int_as_float(nbt[3]));
     st4(nr + 4, __int_as_float(nbt[4]), nbb[0], nbb[1], nbb[2]);
-    st4(nr + 8, nbb[3], nbb[4], 0.f, 0.f);
+    st4(nr + 8, nbb[3], nbb[4], nbv[0], nbv[1]);
+    st4(nr + 12, nbv[2], nbv[3], nbv[4], nbv[5]);
+    st4(nr + 16, nbv[6], nbv[7], nbv[8], 0.f);
   } else {
 #pragma unroll
     for (int k = 0; k < 5; ++k) W.nbBar[k * n + i] = nbb[k];
+    if (kVel) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        W.jstar[(1 + j) * n + i] = nbAx[j];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) W.nbVel[(3 * j + a) * n + i] = nbv[3 * j + a];
+      }
+    }
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) W.dvbar[k * n + i] = dvb[k];
@@ -710,18 +1024,45 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
     faceCells(V, code >> 1, c1, c2);
     const int i = (code & 1) ? c1 : c2;
     if constexpr (Layout<R>::packed) {
-      const float *nr = W.nbRec + 12 * (size_t)i;
+      const float *nr = W.nbRec + 20 * (size_t)i;
       const float4 a = ld4(nr), b = ld4(nr + 4), c = ld4(nr + 8);
       const int t[5] = {__float_as_int(a.x), __float_as_int(a.y), __float_as_int(a.z), __float_as_int(a.w),
                         __float_as_int(b.x)};
-      const float v[5] = {b.y, b.z, b.w, c.x, c.y};
+      if (V.p.reconst == 10) {
+        if (t[0] == j) qb[0] += b.y;
+        if (t[4] == j) qb[4] += c.y;
+        if (t[1] == j || t[2] == j || t[3] == j) {
+          const float4 d = ld4(nr + 12), e = ld4(nr + 16);
+          const float vv[9] = {c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y, e.z};
 #pragma unroll
-      for (int k = 0; k < 5; ++k)
-        if (t[k] == j) qb[k] += v[k];
+          for (int ax = 0; ax < 3; ++ax)
+            if (t[1 + ax] == j) {
+              qb[1] += vv[3 * ax];
+              qb[2] += vv[3 * ax + 1];
+              qb[3] += vv[3 * ax + 2];
+            }
+        }
+      } else {
+        const float v[5] = {b.y, b.z, b.w, c.x, c.y};
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+          if (t[k] == j) qb[k] += v[k];
+      }
     } else {
+      const bool velo = V.p.reconst == 10;
 #pragma unroll
-      for (int k = 0; k < 5; ++k)
+      for (int k = 0; k < 5; ++k) {
+        if (velo && k >= 1 && k <= 3) continue;
         if (W.jstar[k * n + i] == j && W.estar[k * n + i] >= 0) qb[k] += W.nbBar[k * n + i];
+      }
+      if (velo) {
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+          if (W.jstar[(1 + ax) * n + i] == j) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) qb[1 + a] += W.nbVel[(3 * ax + a) * n + i];
+          }
+      }
     }
   }
   const int o = V.refId[j];
@@ -775,6 +1116,44 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
   }
 }
 
+// The limiter's active branches of every cell after kAdjGradFwd, in the
+// reference's cell order: per variable k, out[10 o + 2k] = the active face as
+// the index of the cell's face entry (-1: the factor is 1, not limited), and
+// out[10 o + 2k + 1] = the reference id of the neighbour whose value is the
+// active extreme (-1: none or the cell itself).  The eigen-frame limiter
+// (RECONST 10) reports its axes in k = 1..3, the face index times 4 plus the
+// side (1: the largest increment, 2: the smallest).  A residual whose every
+// cell keeps these branches is a smooth function of the state.
+template <typename R>
+__global__ void kLimiterBranches(View<R> V, AdjWork<R> W, int *outRef) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  const size_t n = V.nc;
+  int *out = outRef + 10 * (size_t)V.refId[i];
+  const int cb = V.cfOff[i];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int es = W.estar[k * n + i], js = W.jstar[k * n + i];
+    out[2 * k] = es >= 0 ? es - cb : -1;
+    out[2 * k + 1] = (es >= 0 && js >= 0) ? V.refId[js] : -1;
+  }
+  if (V.p.reconst == 10 && V.p.spaceOrder > 1) {
+    const PlainLoad<R> ld{V};
+    R G[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) G[a + 3 * c] = W.G[(3 * (1 + a) + c) * n + i];
+    VelFrame<R> F;
+    velFrameForward(V, ld, i, G, F);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      out[2 * (1 + j)] = F.side[j] ? 4 * (F.face[j] - cb) + F.side[j] : -1;
+      out[2 * (1 + j) + 1] = (F.side[j] && F.nb[j] >= 0) ? V.refId[F.nb[j]] : -1;
+    }
+  }
+}
+
 // Boundary-pressure functional: per-face p_f |A_f| on patch ip and the seed
 // of the face adjoint (dJ/dp_f = |A_f|); the sum is a fixed-order block
 // reduction.
@@ -820,8 +1199,13 @@ struct AdjointOps {
     kTanFlux<R><<<blocks((long long)nT), kBlock, 0, s>>>(V, W);
     kTanGather<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsDotRef);
   }
+  static void gradFwd(const View<R> &V, const AdjWork<R> &W, const double *lamRef, cudaStream_t s) {
+    if (V.p.reconst == 10) kAdjGradFwd<R, true><<<blocks(V.nc), kBlock, 0, s>>>(V, W, lamRef);
+    else kAdjGradFwd<R, false><<<blocks(V.nc), kBlock, 0, s>>>(V, W, lamRef);
+  }
   static void cellAdjoint(const View<R> &V, AdjWork<R> &W, double *cvBarRef, cudaStream_t s) {
-    kAdjCell1<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    if (V.p.reconst == 10 && V.p.spaceOrder > 1) kAdjCell1<R, true><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    else kAdjCell1<R, false><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     kAdjCell2<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvBarRef);
   }
   static void faceAdjoint(const View<R> &V, const AdjWork<R> &W, cudaStream_t s) {
@@ -838,16 +1222,22 @@ struct AdjointOps {
     AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
     // every face-adjoint entry the cell kernels read is written by the face
     // kernels: no clearing of faceAdj here
-    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
+    if (V.p.spaceOrder > 1) gradFwd(V, W, rhsBarRef, s);
     else kAdjLambda<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsBarRef);
     (void)nT;
     faceAdjoint(V, W, s);
     cellAdjoint(V, W, cvBarRef, s);
   }
+  static void limiterBranches(const View<R> &V, int *outRef, double *work, cudaStream_t s) {
+    const size_t nT = (size_t)V.nf + V.nb;
+    AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
+    gradFwd(V, W, nullptr, s);
+    kLimiterBranches<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, outRef);
+  }
   static void patchPressure(const View<R> &V, int ip, double *J, double *cvBarRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
     AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
-    if (V.p.spaceOrder > 1) kAdjGradFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, nullptr);
+    if (V.p.spaceOrder > 1) gradFwd(V, W, nullptr, s);
     cudaMemsetAsync(W.faceAdj, 0, sizeof(R) * 16 * nT, s);
     kPatchSeed<R><<<1, kBlock, 0, s>>>(V, W, ip, J);
     if (cvBarRef) cellAdjoint(V, W, cvBarRef, s);

@@ -263,6 +263,7 @@ struct CtxBase {
   virtual int rkUpdate(int iStage, double dt) = 0;
   virtual int getRhs(double *rhs, int onDevice) = 0;
   virtual int getGrad(double *grad, int onDevice) = 0;
+  virtual int limiterBranches(const double *cv, int *branches) = 0;
   virtual int adjointTimes(int nIter, double *ms) = 0;
   virtual int unrolledAdjoint(const double *cv0, int nSteps, double dt, int every, int iPatch, double *J,
                               double *cvBar0, double *stats) = 0;
@@ -584,8 +585,6 @@ struct Ctx : CtxBase {
   int vjp(const double *cv, const double *rhsBar, double *cvBar) override {
     invalidate();
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
-    if (V.p.reconst == 10)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: the eigen-frame velocity limiter (RECONST 10) has a tangent only");
     if (V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through WENO smoothing (RECONST 1, 2)");
     View<R> W;
@@ -611,12 +610,24 @@ struct Ctx : CtxBase {
     RFLU_CUDA(cudaMemcpyAsync(rhsDot, staging + 5 * nc, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost, stream));
     return adjointDone();
   }
+  int limiterBranches(const double *cv, int *branches) override {
+    invalidate();
+    if (!cv || !branches) return fail(RFLU_ERR_ARG, "rflu_gpu_limiter_branches: null argument");
+    if (V.p.spaceOrder < 2) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_limiter_branches: first order has no limiter");
+    View<R> W;
+    int rc = adjointPrep(cv, &W);
+    if (rc) return rc;
+    int *dev = reinterpret_cast<int *>(staging);  // 10 ints per cell fit in the 15 doubles per cell
+    ops->limiterBranches(W, dev, work, stream);
+    RFLU_CUDA(cudaMemcpyAsync(branches, dev, sizeof(int) * 10 * (size_t)V.nc, cudaMemcpyDeviceToHost, stream));
+    return adjointDone();
+  }
   int patchPressure(const double *cv, int iPatch, double *J, double *cvBar) override {
     invalidate();
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
-    if (cvBar && (V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2))
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through RECONST 10, 1 or 2");
+    if (cvBar && (V.p.reconst == 1 || V.p.reconst == 2))
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through the WENO smoothing (RECONST 1, 2)");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -822,8 +833,8 @@ struct Ctx : CtxBase {
     if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
       return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
-    if (V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: RECONST 10, 1 and 2 have no adjoint");
+    if (V.p.reconst == 1 || V.p.reconst == 2)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: the WENO smoothing (RECONST 1, 2) has no adjoint");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     if (int rc0 = ensureAdjoint()) return rc0;
     // the whole forward and reverse sweep runs on the scratch state X
@@ -953,7 +964,7 @@ struct Ctx : CtxBase {
   int adjointTimes(int nIter, double *ms) override {
     invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
-    if (!ops->vjp || V.p.reconst == 10 || V.p.reconst == 1 || V.p.reconst == 2)
+    if (!ops->vjp || V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
     if (int rc0 = ensureAdjoint()) return rc0;
     const size_t nc = V.nc;
@@ -1341,7 +1352,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   P.dvPOnly = (num->precision == RFLU_PREC_MIXED && num->spaceOrder > 1) ? 1 : 0;
   // adjoint workspace (adjoint.cuh: carveAdjWork): gradients, limiter
   // factors and branches, face adjoints of one residual, in the mode's type
-  workBytes = sizeof(R) * (size_t)(120 * (size_t)nc + 24 * ((size_t)nf + nb) + 64) + sizeof(int) * 10 * (size_t)nc + 256;
+  workBytes = sizeof(R) * (size_t)(130 * (size_t)nc + 24 * ((size_t)nf + nb) + 64) + sizeof(int) * 10 * (size_t)nc + 256;
   ops->configure(V);
   RFLU_CUDA(cudaDeviceSynchronize());
   V.tileGrid = ops->tileGrid(V, 0);
@@ -1542,6 +1553,11 @@ int rflu_gpu_get_rhs(rflu_gpu_ctx *ctx, double *rhs, int onDevice) {
 int rflu_gpu_get_grad(rflu_gpu_ctx *ctx, double *grad, int onDevice) {
   CTX_CHECK("rflu_gpu_get_grad");
   return ctx->impl->getGrad(grad, onDevice);
+}
+
+int rflu_gpu_limiter_branches(rflu_gpu_ctx *ctx, const double *cv, int *branches) {
+  CTX_CHECK("rflu_gpu_limiter_branches");
+  return ctx->impl->limiterBranches(cv, branches);
 }
 
 int rflu_gpu_check_refinements(long long n, unsigned long long seed, double *maxRelErr) {

@@ -10,7 +10,7 @@ const Ops<double> *opsFp64() {
   static const Ops<double> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, fp64::AdjointOps<double>::jvp, fp64::AdjointOps<double>::vjp,
                                  fp64::AdjointOps<double>::patchPressure, L::adjointSetup,
-                                 L::updateFromRhs, L::addRhs};
+                                 L::updateFromRhs, L::addRhs, fp64::AdjointOps<double>::limiterBranches};
   return &ops;
 }
 }  // namespace rflu

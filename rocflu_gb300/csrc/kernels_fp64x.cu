@@ -10,7 +10,7 @@ const Ops<double> *opsFp64Exact() {
   static const Ops<double> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, fp64x::AdjointOps<double>::jvp, fp64x::AdjointOps<double>::vjp,
                                  fp64x::AdjointOps<double>::patchPressure, L::adjointSetup,
-                                 L::updateFromRhs, L::addRhs};
+                                 L::updateFromRhs, L::addRhs, fp64x::AdjointOps<double>::limiterBranches};
   return &ops;
 }
 }  // namespace rflu

@@ -31,7 +31,7 @@ const Ops<float> *opsMixed() {
   static const Ops<float> ops = {L::initState, L::initFromRef, L::gradLimit, L::faceFlux,  L::gatherRhs, L::gatherUpdate,
                                  L::timestep,  L::stepEnd,   L::stepStart, L::configure, L::tileGrid, mixed::AdjointOps<float>::jvp, mixed::AdjointOps<float>::vjp,
                                  mixed::AdjointOps<float>::patchPressure, L::adjointSetup,
-                                 L::updateFromRhs, L::addRhs};
+                                 L::updateFromRhs, L::addRhs, mixed::AdjointOps<float>::limiterBranches};
   return &ops;
 }
 }  // namespace rflu

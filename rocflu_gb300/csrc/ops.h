@@ -32,6 +32,8 @@ struct Ops {
   void (*updateFromRhs)(const View<R> &, int, const double *, cudaStream_t);
   // View::rhs += a (5,nCells) array in the reference's cell order
   void (*addRhs)(const View<R> &, const double *, cudaStream_t);
+  // the limiter's active branches of every cell (second order; adjoint.cuh)
+  void (*limiterBranches)(const View<R> &, int *, double *work, cudaStream_t);
 };
 
 // The mixed mode's Newton-refined FP64 reciprocal and square root against

@@ -5,6 +5,8 @@
 #pragma once
 #include <cmath>
 
+#include "dual.cuh"
+
 namespace rflu {
 
 __host__ __device__ inline double sqrt_(double x) { return sqrt(x); }
@@ -281,6 +283,42 @@ __host__ __device__ inline void symmetricEigen3(const S m[9], S vec[9], S val[3]
   if (m2) swapCols(0, 2);
   else if (m1) swapCols(0, 1);
   if (val[2] < val[1]) swapCols(1, 2);
+}
+
+// The same on dual numbers (the tangent kernels): values by the Jacobi
+// iteration above, derivatives by first-order perturbation of the computed
+// eigenpairs of the symmetric m, dl_j = a_j' dm a_j and
+// da_j = sum over k != j of a_k (a_k' dm a_j) / (l_j - l_k), terms with
+// equal eigenvalues dropped.  The tangent of the eigen-frame limiter is then
+// the linear map whose transpose its adjoint applies (adjoint.cuh:
+// velFrameReverse).
+template <int N, typename T>
+__host__ __device__ inline void symmetricEigen3(const Dual<N, T> m[9], Dual<N, T> vec[9], Dual<N, T> val[3]) {
+  T mv[9], a[9], l[3];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) mv[k] = m[k].v;
+  symmetricEigen3(mv, a, l);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) vec[k] = Dual<N, T>(a[k]);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) val[j] = Dual<N, T>(l[j]);
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T sa[3];  // dm a_j
+#pragma unroll
+      for (int r = 0; r < 3; ++r) sa[r] = m[r].d[q] * a[3 * j] + m[r + 3].d[q] * a[3 * j + 1] + m[r + 6].d[q] * a[3 * j + 2];
+      val[j].d[q] = a[3 * j] * sa[0] + a[3 * j + 1] * sa[1] + a[3 * j + 2] * sa[2];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k == j || l[j] == l[k]) continue;
+        const T coef = (a[3 * k] * sa[0] + a[3 * k + 1] * sa[1] + a[3 * k + 2] * sa[2]) / (l[j] - l[k]);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) vec[r + 3 * j].d[q] += coef * a[r + 3 * k];
+      }
+    }
+  }
 }
 
 }  // namespace rflu

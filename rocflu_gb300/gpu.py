@@ -75,7 +75,7 @@ class RfluError(RuntimeError):
 EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_gpu_stream",
            "rflu_gpu_upload_state", "rflu_gpu_download_state", "rflu_gpu_timestep", "rflu_gpu_rk_stage",
            "rflu_gpu_runge_kutta", "rflu_gpu_step", "rflu_gpu_run_fixed_dt", "rflu_gpu_cell_gradients",
-           "rflu_gpu_convective_fluxes", "rflu_gpu_add_rhs", "rflu_gpu_rk_update", "rflu_gpu_get_rhs",
+           "rflu_gpu_convective_fluxes", "rflu_gpu_add_rhs", "rflu_gpu_rk_update", "rflu_gpu_get_rhs", "rflu_gpu_limiter_branches",
            "rflu_gpu_get_grad", "rflu_gpu_residual", "rflu_gpu_vjp",
            "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_unrolled_adjoint", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
            "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_gpu_check_conversions", "rflu_gpu_check_refinements", "rflu_setup_build", "rflu_setup_grid",
@@ -121,6 +121,7 @@ def lib(build_if_missing=True):
     L.rflu_gpu_vjp.argtypes = [P, DP, DP, DP]
     L.rflu_gpu_jvp.argtypes = [P, DP, DP, DP]
     L.rflu_gpu_patch_pressure.argtypes = [P, DP, I, DP, DP]
+    L.rflu_gpu_limiter_branches.argtypes = [P, DP, C.POINTER(C.c_int)]
     L.rflu_gpu_unrolled_adjoint.argtypes = [P, DP, I, D, I, I, DP, DP, DP]
     L.rflu_gpu_status.argtypes = [P, C.POINTER(Status)]
     L.rflu_gpu_kernel_times.argtypes = [P, I, DP]
@@ -358,6 +359,14 @@ class Region:
         cd = np.ascontiguousarray(cv_dot, np.float64)
         out = np.empty((self.n_cells, 5))
         _check(lib().rflu_gpu_jvp(self.h, _p(cv), _p(cd), _p(out)))
+        return out
+
+    def limiter_branches(self, cv):
+        """(nCells, 5, 2) int: per variable the active face index and the
+        reference id of the active extreme neighbour (rflu_gpu_limiter_branches)."""
+        cv = np.ascontiguousarray(cv, np.float64)
+        out = np.empty((self.n_cells, 5, 2), np.int32)
+        _check(lib().rflu_gpu_limiter_branches(self.h, _p(cv), _p(out, C.c_int)))
         return out
 
     def patch_pressure(self, cv, ipatch, with_grad=True):

@@ -1,7 +1,12 @@
 """Tangent (JVP) and discrete adjoint (VJP) of the second-order residual.
 
-* dot-product test: <lambda, J v> = <J^T lambda, v> to round-off;
-* FP64 central finite differences (eps = 1e-6) against the VJP;
+* dot-product test: <lambda, J v> = <J^T lambda, v> to round-off, every
+  limiter with an adjoint (none, Venkatakrishnan, componentwise BJ and BJ
+  with the eigen-frame velocity limiter);
+* FP64 central finite differences (eps = 1e-6) against the VJP: every
+  direction along which no cell changes its limiter's active branch between
+  U - eps v and U + eps v (rflu_gpu_limiter_branches) agrees to 1e-6; the
+  others cross a kink of the limiter and are reported, not held to it;
 * the boundary-pressure functional's gradient against finite differences.
 """
 import numpy as np
@@ -28,8 +33,19 @@ def _dirs(case, k, seed):
     return [rng.standard_normal(case.cv0.shape) * scale for _ in range(k)]
 
 
+ADJ_LIMITERS = [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ]
+
+
+def _switches(r, cv, v, eps):
+    """Whether any cell's limiter branch differs between cv - eps v, cv and
+    cv + eps v."""
+    b0 = r.limiter_branches(cv)
+    return not (np.array_equal(r.limiter_branches(cv + eps * v), b0) and
+                np.array_equal(r.limiter_branches(cv - eps * v), b0))
+
+
 @pytest.mark.parametrize("discr,name", FLUXES)
-@pytest.mark.parametrize("reconst", [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP])
+@pytest.mark.parametrize("reconst", ADJ_LIMITERS)
 @pytest.mark.parametrize("patch_order", [1, 2])
 def test_dot_product(gpu_lib, discr, name, reconst, patch_order):
     c = _case(discr, reconst, patch_order=patch_order)
@@ -44,8 +60,9 @@ def test_dot_product(gpu_lib, discr, name, reconst, patch_order):
 
 
 def test_tangent_covers_eigen_frame_limiter(gpu_lib):
-    """RECONST 10: the tangent differentiates through the Jacobi eigen-solve;
-    checked against central differences."""
+    """RECONST 10: the tangent differentiates through the eigen-frame of the
+    strain rate (first-order perturbation of the Jacobi eigenpairs); checked
+    against central differences."""
     c = _case(cases.DISCR_HLLC, cases.RECONST_BJ)
     r = gpu.Region(c, "fp64")
     v = _dirs(c, 1, 5)[0]
@@ -59,30 +76,33 @@ def test_tangent_covers_eigen_frame_limiter(gpu_lib):
 
 
 @pytest.mark.parametrize("discr,name", FLUXES)
-def test_vjp_vs_central_differences(gpu_lib, discr, name):
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ])
+def test_vjp_vs_central_differences(gpu_lib, discr, name, reconst):
     """64 random directions, eps = 1e-6 relative to the state's scale:
-    <lambda, (R(U+eps v) - R(U-eps v)) / 2 eps> against <J^T lambda, v>."""
-    c = _case(discr, cases.RECONST_VENKAT)
+    <lambda, (R(U+eps v) - R(U-eps v)) / 2 eps> against <J^T lambda, v>.
+    Every direction that keeps all limiter branches agrees to 1e-6; at least
+    half of the directions keep them."""
+    c = _case(discr, reconst)
     r = gpu.Region(c, "fp64")
     lam = np.random.default_rng(11).standard_normal(c.cv0.shape)
     g = r.vjp(c.cv0, lam)
     eps = 1e-6
-    errs = []
+    errs, sw = [], []
     for v in _dirs(c, 64, 3):
         rp, _ = r.residual(c.cv0 + eps * v, with_grad=False)
         rm, _ = r.residual(c.cv0 - eps * v, with_grad=False)
         fd = (lam * (rp - rm)).sum() / (2 * eps)
         ad = (g * v).sum()
         errs.append(abs(fd - ad) / max(abs(ad), 1e-30))
-    errs = np.array(errs)
-    # directions whose +-eps perturbation crosses a limiter/flux branch switch
-    # are not differentiable there; all others agree to 1e-6
-    assert np.median(errs) < 1e-7, errs
-    assert (errs < 1e-6).mean() >= 0.9, errs
+        sw.append(_switches(r, c.cv0, v, eps))
+    errs, sw = np.array(errs), np.array(sw)
+    assert (~sw).sum() >= 32, sw.sum()
+    assert (errs[~sw] < 1e-6).all(), (errs[~sw].max(), np.flatnonzero(~sw & (errs >= 1e-6)))
 
 
-def test_patch_pressure_gradient(gpu_lib):
-    c = _case(cases.DISCR_ROE, cases.RECONST_VENKAT)
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ])
+def test_patch_pressure_gradient(gpu_lib, reconst):
+    c = _case(cases.DISCR_ROE, reconst)
     r = gpu.Region(c, "fp64")
     ip = 1  # x = 1 patch
     J, g = r.patch_pressure(c.cv0, ip)
@@ -96,11 +116,33 @@ def test_patch_pressure_gradient(gpu_lib):
         assert abs(fd - ad) <= 1e-6 * abs(ad) + 1e-12, (fd, ad)
 
 
-def test_adjoint_rejects_eigen_frame(gpu_lib):
-    c2 = _case(cases.DISCR_ROE, cases.RECONST_BJ)
-    for prec in ("fp64", "mixed"):
-        with pytest.raises(gpu.RfluError):
-            gpu.Region(c2, prec).vjp(c2.cv0, c2.cv0)
+def test_adjoint_rejects_weno(gpu_lib):
+    """The WENO smoothing (RECONST 1, 2) has no adjoint or tangent."""
+    for reconst in (cases.RECONST_WENO_SIMPLE, cases.RECONST_WENO_XYZ):
+        c2 = _case(cases.DISCR_ROE, reconst)
+        for prec in ("fp64", "mixed"):
+            with pytest.raises(gpu.RfluError):
+                gpu.Region(c2, prec).vjp(c2.cv0, c2.cv0)
+            with pytest.raises(gpu.RfluError):
+                gpu.Region(c2, prec).jvp(c2.cv0, c2.cv0)
+
+
+def test_limiter_branches_record(gpu_lib):
+    """rflu_gpu_limiter_branches: componentwise BJ reports per variable the
+    active face (an index among the cell's faces) and the neighbour holding
+    the active extreme; RECONST 10 reports its velocity axes with a side."""
+    for reconst in (cases.RECONST_BJ_COMP, cases.RECONST_BJ):
+        c = _case(cases.DISCR_ROE, reconst)
+        r = gpu.Region(c, "fp64")
+        b = r.limiter_branches(c.cv0)
+        assert b.shape == (c.n_cells, 5, 2)
+        assert (b[..., 0] >= -1).all() and (b[..., 1] >= -1).all() and (b[..., 1] < c.n_cells).all()
+        assert (b[..., 0] >= 0).any()
+        if reconst == cases.RECONST_BJ:
+            sides = b[:, 1:4, 0][b[:, 1:4, 0] >= 0] % 4
+            assert set(np.unique(sides)) <= {1, 2} and len(sides) > 0
+        else:
+            assert (b[:, :, 0] < 4).all()  # tetrahedra: 4 faces
 
 
 # Mixed precision: the adjoint and tangent kernels evaluate the flux,
@@ -109,7 +151,7 @@ def test_adjoint_rejects_eigen_frame(gpu_lib):
 
 
 @pytest.mark.parametrize("discr,name", FLUXES)
-@pytest.mark.parametrize("reconst", [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP])
+@pytest.mark.parametrize("reconst", ADJ_LIMITERS)
 def test_mixed_dot_product(gpu_lib, discr, name, reconst):
     """<lambda, J v> = <J^T lambda, v> for the mixed tangent and adjoint, to
     FP32 accumulation: 1e-5 of the summed magnitudes of the products (the
@@ -127,7 +169,7 @@ def test_mixed_dot_product(gpu_lib, discr, name, reconst):
 
 
 @pytest.mark.parametrize("discr,name", FLUXES)
-@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP])
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ])
 def test_mixed_vjp_against_fp64(gpu_lib, discr, name, reconst):
     """The mixed VJP against the FP64 VJP and against FP64 central
     differences (eps = 1e-6) of the FP64 residual on 16 directions: the

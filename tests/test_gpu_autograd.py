@@ -156,8 +156,10 @@ def test_unrolled_adjoint_finite_differences(gpu_lib, reconst):
 
 
 def test_unrolled_adjoint_rejections(gpu_lib):
+    """The WENO smoothing (RECONST 1, 2) has no adjoint; a zero checkpoint
+    interval is an argument error."""
     c = _blast()
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ)
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_WENO_XYZ)
     cb = cases.blast_hex(6, num=num)
     for prec in ("fp64", "mixed"):
         with pytest.raises(gpu.RfluError):
