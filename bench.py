@@ -518,11 +518,11 @@ def weno_variant(args, cases, gpu, setup, dt_imposed):
 
 def unrolled_adjoint(args, cases, gpu):
     """Time-unrolled adjoint: spherical blast on n^3 hexes (p=10 inside
-    r=0.15, p=1 outside, rho=1), HLLC, second order with the componentwise
-    Barth-Jespersen limiter (RECONST 100: the eigen-frame BJ limiter has a
-    tangent only, and the reference's Venkatakrishnan limiter, whose face
-    offsets are taken as cofg - fc, lets face pressures of this blast go
-    negative within the first step), Wray RK3, dt fixed from the initial
+    r=0.15, p=1 outside, rho=1), HLLC, second order with the Barth-Jespersen
+    limiter and its eigen-frame velocity limiting (RECONST 10; the
+    reference's Venkatakrishnan limiter, whose face offsets are taken as
+    cofg - fc, lets face pressures of this blast go negative within the
+    first step), Wray RK3, dt fixed from the initial
     CFL 0.4, the functional the time-integrated pressure on the x=1 patch.  Gradient w.r.t. the initial
     density by the checkpointed reverse sweep; central differences on seeded
     density blobs, on the case as stated and on the same case with a smooth
@@ -531,13 +531,13 @@ def unrolled_adjoint(args, cases, gpu):
     pressure is a stationary contact, so J = steps * dt * p_ambient * area
     exactly and its gradient is ~0; the smooth variant is the one whose
     differences test the adjoint."""
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ_COMP, cfl=0.4)
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ, cfl=0.4)
     c = cases.blast_hex(args.unrolled_n, num=num, p_in=10.0, radius=0.15)
     x = gpu.Setup(c).cofg
     reg = gpu.Region(c, "fp64")
     dt = reg.timestep(1.0)
     n, every = args.unrolled_steps, args.unrolled_every
-    out = {"workload": "blast_hex%d_hllc_bjcomp_wray3" % args.unrolled_n, "cells": reg.n_cells, "steps": n,
+    out = {"workload": "blast_hex%d_hllc_bj_wray3" % args.unrolled_n, "cells": reg.n_cells, "steps": n,
            "checkpoint_every": every, "dt": dt, "functional": "sum_n dt * sum_{x=1 patch} p_f |A_f|"}
     bg = np.sin(2 * np.pi * x[:, 0] + 0.3) * np.sin(2 * np.pi * x[:, 1] + 0.7) * np.sin(2 * np.pi * x[:, 2] + 1.1)
     smooth = c.cv0.copy()

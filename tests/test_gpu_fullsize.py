@@ -14,9 +14,10 @@ on smaller meshes in test_gpu_parity.py):
   blast reconstruct negative face pressures within a few steps, floor one
   cell at p = 10 in step 2, and give 2 non-finite cells in step 3 at p = 2,
   the CPU oracle and the device alike; p = 4 stays clean for 3 steps;
-* C4, 32^3 x 6 jittered tetrahedra (196,608 cells), Roe + componentwise BJ:
-  the tangent/adjoint dot-product identity;
-* C5, 64^3 hexes (262,144 cells), HLLC + componentwise BJ blast: the
+* C4, 32^3 x 6 jittered tetrahedra (196,608 cells), Roe + componentwise BJ
+  and BJ with the eigen-frame velocity limiter: the tangent/adjoint
+  dot-product identity;
+* C5, 64^3 hexes (262,144 cells), HLLC + BJ (eigen-frame) blast: the
   time-unrolled adjoint's value and gradient do not depend on the
   checkpoint interval.
 """
@@ -89,11 +90,13 @@ def test_c2_tets_closed_box_conserves(gpu_lib, prec, tol):
     assert abs((cv[:, 4] * vol).sum() - e0) / e0 < tol
 
 
+@pytest.mark.parametrize("reconst", [cases.RECONST_BJ_COMP, cases.RECONST_BJ])
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
-def test_c4_dot_product(gpu_lib, prec, tol):
+def test_c4_dot_product(gpu_lib, prec, tol, reconst):
     """<lambda, J v> = <J^T lambda, v> to the mode's accumulation error,
-    relative to the summed magnitudes of the products."""
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=cases.RECONST_BJ_COMP)
+    relative to the summed magnitudes of the products; componentwise BJ and
+    BJ with the eigen-frame velocity limiter."""
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=reconst)
     c = cases.adjoint_tets(32, num=num)
     r = gpu.Region(c, prec)
     rng = np.random.default_rng(3)
@@ -109,7 +112,7 @@ def test_c4_dot_product(gpu_lib, prec, tol):
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_c5_unrolled_adjoint_checkpoint_invariance(gpu_lib, prec):
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ_COMP, cfl=0.4)
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ, cfl=0.4)
     c = cases.blast_hex(64, num=num, p_in=10.0, radius=0.15)
     r = gpu.Region(c, prec)
     dt = r.timestep(1.0)
