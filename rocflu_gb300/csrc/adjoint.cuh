@@ -403,7 +403,8 @@ __device__ inline void velFrameApply(const VelFrame<R> &F, R *gl) {
 // transpose of the tangent's linear map: Gl = sum_j al_j A_j B_j with
 // B = A^T G; the active factor al = dext / pr, dext = A_j . (u_nb - u_i),
 // pr = A_j . G (cofg - fc); the eigenvectors' perturbation
-// da_j = sum_{k != j} a_k (a_k' dS a_j) / (l_j - l_k), S = sym(G).
+// da_j = sum_{k != j} a_k (a_k' dS a_j) / (l_j - l_k), S = sym(G), without
+// the pairs the limiter merges (physics.cuh: mergedPair).
 template <typename R, typename L>
 __device__ inline void velFrameReverse(const View<R> &V, const L &ld, int i, const R *G, const VelFrame<R> &F,
                                        const R *glb, R *Gb, R *ub, R *nbv) {
@@ -481,7 +482,7 @@ __device__ inline void velFrameReverse(const View<R> &V, const L &ld, int i, con
   for (int j = 0; j < 3; ++j)
 #pragma unroll
     for (int k = j + 1; k < 3; ++k) {
-      if (F.ev[j] == F.ev[k]) continue;
+      if (F.ev[j] == F.ev[k] || mergedPair(F.ev, j, k)) continue;
       R ajk = R(0), akj = R(0);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {

@@ -285,13 +285,33 @@ __host__ __device__ inline void symmetricEigen3(const S m[9], S vec[9], S val[3]
   if (val[2] < val[1]) swapCols(1, 2);
 }
 
+// Whether eigenvalues j < k (ascending) lie in one group of the eigen-frame
+// limiter's merge (RFLU_LimitGradVelocityBarthJesp, modflu/
+// RFLU_ModLimiters.F90:728-760: neighbours within 1e-3 of the largest
+// magnitude share one factor).
+template <typename T>
+__host__ __device__ inline bool mergedPair(const T *l, int j, int k) {
+  T mx = fabs_(l[0]);
+  mx = fmax2(mx, fabs_(l[1]));
+  mx = fmax2(mx, fabs_(l[2]));
+  const T scale = T(1.0e-3) * mx;
+  const bool e12 = (l[1] - l[0] <= scale), e23 = (l[2] - l[1] <= scale);
+  if (j == 0 && k == 1) return e12;
+  if (j == 1 && k == 2) return e23;
+  return e12 && e23;
+}
+
 // The same on dual numbers (the tangent kernels): values by the Jacobi
 // iteration above, derivatives by first-order perturbation of the computed
 // eigenpairs of the symmetric m, dl_j = a_j' dm a_j and
-// da_j = sum over k != j of a_k (a_k' dm a_j) / (l_j - l_k), terms with
-// equal eigenvalues dropped.  The tangent of the eigen-frame limiter is then
-// the linear map whose transpose its adjoint applies (adjoint.cuh:
-// velFrameReverse).
+// da_j = sum over k != j of a_k (a_k' dm a_j) / (l_j - l_k).  Pairs the
+// limiter merges are one eigenspace to the derivative: their axes are held
+// fixed within it (their rotation there is of order 1 for a change of
+// order l_j - l_k, a sensitivity of the basis the merged factor follows only
+// through its minimum; keeping it would scale rounding by 1/(l_j - l_k) in
+// the near-symmetric flows where such pairs arise).  The tangent of the
+// eigen-frame limiter is then the linear map whose transpose its adjoint
+// applies (adjoint.cuh: velFrameReverse).
 template <int N, typename T>
 __host__ __device__ inline void symmetricEigen3(const Dual<N, T> m[9], Dual<N, T> vec[9], Dual<N, T> val[3]) {
   T mv[9], a[9], l[3];
@@ -312,7 +332,7 @@ __host__ __device__ inline void symmetricEigen3(const Dual<N, T> m[9], Dual<N, T
       val[j].d[q] = a[3 * j] * sa[0] + a[3 * j + 1] * sa[1] + a[3 * j + 2] * sa[2];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        if (k == j || l[j] == l[k]) continue;
+        if (k == j || l[j] == l[k] || mergedPair(l, j < k ? j : k, j < k ? k : j)) continue;
         const T coef = (a[3 * k] * sa[0] + a[3 * k + 1] * sa[1] + a[3 * k + 2] * sa[2]) / (l[j] - l[k]);
 #pragma unroll
         for (int r = 0; r < 3; ++r) vec[r + 3 * j].d[q] += coef * a[r + 3 * k];
