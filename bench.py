@@ -431,7 +431,8 @@ def single_adjoint(args, cases, gpu, reconst=None, n_dirs=64):
     active branch (face or extreme neighbour) between U - eps v, U and
     U + eps v (rflu_gpu_limiter_branches): the functional is smooth along
     the others, which the adjoint must match to 1e-6.  Switches anywhere in
-    the mesh are counted too."""
+    the mesh are counted too.  A second pass at eps = 1e-8 repeats the
+    classification with fewer kinks crossed."""
     if reconst is None:
         reconst = cases.RECONST_BJ_COMP
     num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=reconst)
@@ -443,21 +444,30 @@ def single_adjoint(args, cases, gpu, reconst=None, n_dirs=64):
     rng = np.random.default_rng(2)
     scale = np.abs(ac.cv0).mean(axis=0)
     dirs = [rng.standard_normal(ac.cv0.shape) * scale for _ in range(n_dirs)]
-    eps = 1e-6
-    fd, switch, switch_all = [], [], []
     g = areg.grid
     support = np.unique(g.bf2c[g.patch_off[1]:g.patch_off[2]] - 1)
     b0 = areg.limiter_branches(ac.cv0)
-    for v in dirs:
-        jp, _ = areg.patch_pressure(ac.cv0 + eps * v, 1, with_grad=False)
-        jm, _ = areg.patch_pressure(ac.cv0 - eps * v, 1, with_grad=False)
-        fd.append((jp - jm) / (2 * eps))
-        bp, bm = areg.limiter_branches(ac.cv0 + eps * v), areg.limiter_branches(ac.cv0 - eps * v)
-        changed = (bp != b0).any(axis=2) | (bm != b0).any(axis=2)
-        switch.append(int(changed[support].sum()))
-        switch_all.append(int(changed.sum()))
-    fd, switch = np.array(fd), np.array(switch)
+
+    def differences(eps):
+        fd, switch, switch_all = [], [], []
+        for v in dirs:
+            jp, _ = areg.patch_pressure(ac.cv0 + eps * v, 1, with_grad=False)
+            jm, _ = areg.patch_pressure(ac.cv0 - eps * v, 1, with_grad=False)
+            fd.append((jp - jm) / (2 * eps))
+            bp, bm = areg.limiter_branches(ac.cv0 + eps * v), areg.limiter_branches(ac.cv0 - eps * v)
+            changed = (bp != b0).any(axis=2) | (bm != b0).any(axis=2)
+            switch.append(int(changed[support].sum()))
+            switch_all.append(int(changed.sum()))
+        return np.array(fd), np.array(switch), np.array(switch_all)
+
+    eps = 1e-6
+    fd, switch, switch_all = differences(eps)
     smooth = switch == 0
+    # the same at eps = 1e-8: fewer directions cross a kink, at the price of
+    # the difference's rounding (about 1e-16 |J| / eps)
+    eps_s = 1e-8
+    fd_s, switch_s, _ = differences(eps_s)
+    smooth_s = switch_s == 0
     lam = np.random.default_rng(5).standard_normal(ac.cv0.shape)
     g_ref = None
     for name, reg in (("fp64", areg), ("mixed", mreg)):
@@ -478,6 +488,12 @@ def single_adjoint(args, cases, gpu, reconst=None, n_dirs=64):
                                  if (~smooth).any() else None,
                                  "support_cells": int(len(support)),
                                  "switching_cell_variables_anywhere_median": float(np.median(switch_all))}}
+        err_s = np.abs(fd_s - np.array([(gJ * v).sum() for v in dirs])) / np.abs(fd_s)
+        res["fd_small_eps"] = {"fd_eps": eps_s, "fd_rel_err_median": float(np.median(err_s)),
+                               "dirs_without_switch": int(smooth_s.sum()),
+                               "without_switch_below_1e-6": int((err_s[smooth_s] < 1e-6).sum()),
+                               "without_switch_err_max": float(err_s[smooth_s].max()) if smooth_s.any() else None,
+                               "with_switch_below_1e-6": int((err_s[~smooth_s] < 1e-6).sum())}
         if g_ref is None:
             g_ref = g
             out.update(res)

@@ -265,6 +265,7 @@ struct VelFrame {
   int side[3];     // 0: alRaw = 1; 1: dmx / pr; 2: dmn / pr
   int face[3];     // cell-face entry of the active projection pr
   int nb[3];       // neighbour of the active extreme dmx or dmn (-1: the extreme is the initial 0)
+  bool held[3];    // idle axis (physics.cuh: idleAxis): the factor is held at its value
   R dext[3], pext[3];
 };
 
@@ -346,6 +347,8 @@ __device__ inline void velFrameForward(const View<R> &V, const L &ld, int i, con
       }
     }
   }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) F.held[j] = idleAxis(A, G, j);
   // merge the factors of equal eigenvalues (within 1e-3 of the largest magnitude)
   R mx = fabs_(F.ev[0]);
   mx = fmax2(mx, fabs_(F.ev[1]));
@@ -399,7 +402,8 @@ __device__ inline void velFrameApply(const VelFrame<R> &F, R *gl) {
 // Reverse of the limiter: from glb (adjoint of the limited velocity
 // gradient, glb[a + 3c]) to Gb (of the unlimited one), ub (of the cell's
 // own velocity) and, per axis j, the velocity adjoint nbv[3j..3j+2] that
-// neighbour F.nb[j] receives (when F.side[j] and F.nb[j] >= 0).  The
+// neighbour F.nb[j] receives (when F.side[j], not F.held[j], and
+// F.nb[j] >= 0).  The
 // transpose of the tangent's linear map: Gl = sum_j al_j A_j B_j with
 // B = A^T G; the active factor al = dext / pr, dext = A_j . (u_nb - u_i),
 // pr = A_j . G (cofg - fc); the eigenvectors' perturbation
@@ -437,7 +441,7 @@ __device__ inline void velFrameReverse(const View<R> &V, const L &ld, int i, con
   ld.prim4(i, ui);
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    if (F.side[j] == 0 || albRaw[j] == R(0)) continue;
+    if (F.side[j] == 0 || F.held[j] || albRaw[j] == R(0)) continue;
     // alRaw = dext / pr: the same guarded form as the scalar limiter's
     const R r = albRaw[j] / F.pext[j];
     const R dextb = r, prb = -r * (F.dext[j] / F.pext[j]);
@@ -913,7 +917,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     }
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-      if (F.side[j] != 0 && F.nb[j] >= 0) nbAx[j] = F.nb[j];
+      if (F.side[j] != 0 && !F.held[j] && F.nb[j] >= 0) nbAx[j] = F.nb[j];
   }
   // gradient own-term: G_i = sum_s w_s (q_{m_s} - q_i)
   if constexpr (!Layout<R>::packed) {

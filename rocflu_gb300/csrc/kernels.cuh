@@ -577,6 +577,7 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
           if (snx[j] < S(0)) al[j] = fmin2(al[j], dmn[j] / snx[j]);
         }
       }
+      holdIdleAxes(A, G, al);
       S mx = fabs_(ev[0]);
       mx = fmax2(mx, fabs_(ev[1]));
       mx = fmax2(mx, fabs_(ev[2]));

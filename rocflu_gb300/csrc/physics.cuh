@@ -301,6 +301,51 @@ __host__ __device__ inline bool mergedPair(const T *l, int j, int k) {
   return e12 && e23;
 }
 
+// Whether axis j of the eigen-frame carries no velocity gradient: its row
+// A_j' G is at the level of the eigenvectors' rounding (the Jacobi
+// iteration stops at off-diagonals of 1e-12 |S|, so eigenvectors of
+// eigenvalues 1e-3 |S| apart carry errors up to 1e-9; FP32 about 1e-4).  In
+// a flow whose velocity varies in fewer than three directions (one velocity
+// component zero, a plane or axis of symmetry) the strain rate has such an
+// axis, and the limiter's factor on it, dext / pr with dext = A_j . du and
+// pr = A_j . G off, is a ratio of two rounding residues: a value anywhere in
+// [0, 1] that multiplies A_j' G and so changes the limited gradient only at
+// rounding level, but whose derivative is of order 1 / rounding.  The
+// tangent and the adjoint hold such a factor at its value (at the exact
+// configuration the primal is not differentiable: the factor along a
+// perturbation is the ratio of the perturbation's own projections).
+template <typename T>
+__host__ __device__ inline bool idleAxis(const T *A, const T *G, int j) {
+  const T tol = sizeof(T) >= 8 ? T(1.0e-8) : T(1.0e-3);
+  T gm = T(0), bm = T(0);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) gm = fmax2(gm, fabs_(G[k]));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    T s = T(0);
+    s = s + A[3 * j] * G[3 * c];
+    s = s + A[3 * j + 1] * G[1 + 3 * c];
+    s = s + A[3 * j + 2] * G[2 + 3 * c];
+    bm = fmax2(bm, fabs_(s));
+  }
+  return bm <= tol * gm;
+}
+
+// The eigen-frame limiter's factors al[3] on the tangent types: idle axes
+// (idleAxis) keep their value and lose their derivative.  A no-op on plain
+// floating-point types (the primal).
+template <typename S>
+__host__ __device__ inline void holdIdleAxes(const S *, const S *, S *) {}
+template <int N, typename T>
+__host__ __device__ inline void holdIdleAxes(const Dual<N, T> *A, const Dual<N, T> *G, Dual<N, T> *al) {
+  T a[9], g[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { a[k] = A[k].v; g[k] = G[k].v; }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    if (idleAxis(a, g, j)) al[j] = Dual<N, T>(al[j].v);
+}
+
 // The same on dual numbers (the tangent kernels): values by the Jacobi
 // iteration above, derivatives by first-order perturbation of the computed
 // eigenpairs of the symmetric m, dl_j = a_j' dm a_j and

@@ -223,3 +223,46 @@ def test_adjoint_finite_with_tiny_differences(gpu_lib, reconst):
     assert np.isfinite(g).all()
     _, gp = r.patch_pressure(cv, 1)
     assert np.isfinite(gp).all()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_eigen_frame_one_dimensional_velocity(gpu_lib, prec):
+    """RECONST 10 on a state whose velocity has an x component only (v = w
+    = 0 exactly, u varying in all three directions): the strain rate then
+    has an axis along which the velocity does not vary, and the limiter's
+    factor on it is a ratio of two rounding residues.  Its derivative (of
+    order 1 / rounding, 1e13 here) is held at zero in the tangent and the
+    adjoint, so both stay bounded, stay each other's transpose, and follow
+    central differences.  The held factor's value is itself a ratio of
+    rounding residues, different in FP32 and FP64; it multiplies the idle
+    axis's O(1) projection derivative, so the mixed mode's adjoint follows
+    the FP64 one only to the share of those terms (2% here)."""
+    c = _case(cases.DISCR_HLLC, cases.RECONST_BJ)
+    x = gpu.Setup(c).cofg
+    cv = c.cv0.copy()
+    bg = np.sin(2 * np.pi * x[:, 0] + 0.3) * np.sin(2 * np.pi * x[:, 1] + 0.7) * np.sin(2 * np.pi * x[:, 2] + 1.1)
+    cv[:, 0] *= 1 + 0.05 * bg
+    cv[:, 1] = 0.2 * cv[:, 0] * (1 + 0.5 * np.roll(bg, 3))
+    cv[:, 2:4] = 0.0
+    r = gpu.Region(c, prec)
+    ref = gpu.Region(c, "fp64")
+    rng = np.random.default_rng(3)
+    lam = rng.standard_normal(cv.shape)
+    g = r.vjp(cv, lam)
+    g64 = ref.vjp(cv, lam)
+    assert np.abs(g64).max() < 1e3, np.abs(g64).max()
+    if prec == "mixed":
+        assert np.linalg.norm(g - g64) <= 5e-2 * np.linalg.norm(g64)
+        return
+    eps = 1e-7
+    errs = []
+    for v in _dirs(c, 8, 9):
+        jv = r.jvp(cv, v)
+        a, b = (lam * jv).sum(), (g * v).sum()
+        assert abs(a - b) <= 1e-11 * max(abs(a), abs(b)), (a, b)
+        rp, _ = r.residual(cv + eps * v, with_grad=False)
+        rm, _ = r.residual(cv - eps * v, with_grad=False)
+        fd = (rp - rm) / (2 * eps)
+        errs.append(np.abs(fd - jv).max() / np.abs(fd).max())
+    print("relative max-norm error of J v against central differences:", errs)
+    assert np.median(errs) < 1e-2 and max(errs) < 0.2, errs
