@@ -1060,8 +1060,26 @@ int Ctx<R>::buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cf
     }
   (void)nb;
   int rc = 0;
+  // per tile {halo list start, its slots, stLoc words [w0, w1)}: one 16-byte
+  // load gives the gradient kernel what it needs to stage the tile
+  const int nTiles = (nc + kTile - 1) / kTile;
+  std::vector<int> desc(4 * (size_t)nTiles);
+  for (int t = 0; t < nTiles; ++t) {
+    const int b0 = t * kTile, b1 = std::min(nc, b0 + kTile);
+    desc[4 * t] = haloOff[t];
+    desc[4 * t + 1] = haloOff[t + 1] - haloOff[t];
+    desc[4 * t + 2] = stOff[b0] >> 3;
+    desc[4 * t + 3] = (stOff[b1] + 7) >> 3;
+  }
+  std::vector<int> haloPadded(haloIdx);
+  haloPadded.resize(haloPadded.size() + 4, -1);
   if ((rc = put<int>(&V.haloOff, haloOff))) return rc;
-  if ((rc = put<int>(&V.haloIdx, haloIdx))) return rc;
+  if ((rc = put<int>(&V.haloIdx, haloPadded))) return rc;
+  {
+    const int *d = nullptr;
+    if ((rc = put<int>(&d, desc))) return rc;
+    V.tileDesc = reinterpret_cast<const int4 *>(d);
+  }
   if ((rc = put<unsigned short>(&V.stLoc, stLoc))) return rc;
   if ((rc = put<float>(&V.feD, feD))) return rc;
   if ((rc = put<float>(&V.feN, feN))) return rc;

@@ -50,11 +50,14 @@ struct Params {
 constexpr int kTile = 256;
 // Shared-memory footprint of one staged tile of the mixed-mode gradient
 // kernel: 8 floats per record, the stencil ids as whole 16-byte words (plus
-// one for the misalignment of the first), kTileOffInts stencil offsets.
+// one for the misalignment of the first), kTileOffInts stencil offsets, and
+// the halo cell ids of the tile two ahead in the pipeline (a multiple of 4
+// ints: every tile's halo list starts on a 16-byte boundary).
 constexpr int kTileOffInts = kTile + 4;
 __host__ __device__ inline size_t tileIdWordsFor(int maxTileSt) { return ((size_t)maxTileSt + 7) / 8 + 1; }
+__host__ __device__ inline size_t tileHaloIntsFor(int maxRecs) { return ((size_t)(maxRecs - kTile) + 3) / 4 * 4; }
 __host__ __device__ inline size_t tileBufFloatsFor(int maxRecs, int maxTileSt) {
-  return 8 * (size_t)maxRecs + 4 * tileIdWordsFor(maxTileSt) + kTileOffInts;
+  return 8 * (size_t)maxRecs + 4 * tileIdWordsFor(maxTileSt) + kTileOffInts + tileHaloIntsFor(maxRecs);
 }
 
 template <typename R> struct Layout {
@@ -118,7 +121,10 @@ struct View {
   int tileGrid;                     // CTAs of the persistent tiled kernels
   int tileGridDt;                   // ... of the variant with the time-step sum
   int cfW;                          // max faces per cell (entries of feD/feN)
-  const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids by slot (-1: unused)
+  const int *haloOff, *haloIdx;     // CSR over tiles of global halo cell ids by slot (-1: unused);
+                                    // each tile's list starts on a 16-byte boundary
+  const int4 *tileDesc;             // per tile: haloOff[t], its halo slots, and the
+                                    // 16-byte words [w0, w1) of stLoc its stencils use
   const unsigned short *stLoc;      // local id of each stencil member (stIdx order),
                                     // 16-byte aligned and padded by 8 ids
   // per cell-face entry, entry-major (entry k of cell i at [k*nc + i]), in

@@ -1117,19 +1117,37 @@ __device__ inline void prefetchTile(const View<R> &V, int t) {
   }
 }
 
-// Issue the copies of tile t into buf (this thread's share).
+// Tile staging, in two steps a tile apart so that no thread waits on a
+// global load before it computes: stageHalo copies the halo cell ids of a
+// tile into its buffer's id area (given the tile's descriptor, a plain load
+// one tile earlier still), and stageRecs, once those ids have landed, copies
+// the tile's own records, its halo records (addresses from shared memory),
+// stencil ids and offsets.  Both are this thread's share of cp.async copies.
 template <typename R>
-__device__ inline void stageTile(const View<R> &V, int t, float *buf) {
+__device__ inline int *tileHaloIds(const View<R> &V, float *buf) {
+  return reinterpret_cast<int *>(buf + 8 * (size_t)V.maxRecs + 4 * tileIdWords(V) + kTileOffInts);
+}
+template <typename R>
+__device__ inline int4 loadTileDesc(const View<R> &V, int t, int nTiles) {
+  return t < nTiles ? __ldg(V.tileDesc + t) : make_int4(0, 0, 0, 0);
+}
+template <typename R>
+__device__ inline void stageHalo(const View<R> &V, int4 d, float *buf) {
+  int *ids = tileHaloIds(V, buf);
+  const int nw = (d.y + 3) >> 2;
+  for (int w = threadIdx.x; w < nw; w += kBlock) cpAsync16(ids + 4 * w, V.haloIdx + d.x + 4 * w);
+}
+template <typename R>
+__device__ inline void stageRecs(const View<R> &V, int t, int4 d, float *buf) {
   const int base = t * kTile, nIn = min(kTile, V.nc - base);
-  const int hb = V.haloOff[t], nh = V.haloOff[t + 1] - hb;
   uint4 *ids = reinterpret_cast<uint4 *>(buf + 8 * (size_t)V.maxRecs);
-  const int w0 = V.stOff[base] >> 3, w1 = (V.stOff[base + nIn] + 7) >> 3;
   const uint4 *src4 = reinterpret_cast<const uint4 *>(V.stLoc);
-  for (int w = w0 + (int)threadIdx.x; w < w1; w += kBlock) cpAsync16(ids + (w - w0), src4 + w);
+  for (int w = d.z + (int)threadIdx.x; w < d.w; w += kBlock) cpAsync16(ids + (w - d.z), src4 + w);
   int *offs = reinterpret_cast<int *>(ids + tileIdWords(V));
   for (int r = threadIdx.x; r <= nIn; r += kBlock) cpAsync4(offs + r, V.stOff + base + r);
-  for (int r = threadIdx.x; r < nIn + nh; r += kBlock) {
-    const int src = r < nIn ? base + r : V.haloIdx[hb + r - nIn];
+  const int *halo = tileHaloIds(V, buf);
+  for (int r = threadIdx.x; r < nIn + d.y; r += kBlock) {
+    const int src = r < nIn ? base + r : halo[r - nIn];
     if (src < 0) continue;  // an unused halo slot
     const int dst = r < nIn ? r : kTile + (r - nIn);
     const float *g = V.prim + 8 * (size_t)src;
@@ -1139,6 +1157,11 @@ __device__ inline void stageTile(const View<R> &V, int t, float *buf) {
   }
 }
 
+// The pipeline over a CTA's tiles t = blockIdx.x, + G, ... (G = gridDim.x):
+// while tile t is computed from buffer b, the records of t + G are in flight
+// into buffer b ^ 1 and the halo ids of t + 2 G into buffer b's id area
+// (free: t's ids were read when t was staged), and the descriptor of t + 3 G
+// is loading into registers.
 template <typename R, bool kDt, int kRc>
 __global__ void __launch_bounds__(kBlock, kDt ? 2 : 3) kGradTile(View<R> V) {
   if constexpr (Layout<R>::packed) {
@@ -1147,35 +1170,49 @@ __global__ void __launch_bounds__(kBlock, kDt ? 2 : 3) kGradTile(View<R> V) {
     float *const smem = reinterpret_cast<float *>(tileSmem);
     float *dc = smem + 2 * bufFloats;
     const int nTiles = (V.nc + kTile - 1) / kTile;
+    const int G = gridDim.x;
     // a step after the clipped last step does nothing (uniform over the CTA)
     const bool live = !kDt || V.sc->finished >= 0;
     double dt = 1.79769313486231571e308;
     int t = blockIdx.x, b = 0;
-    if (live && t < nTiles) stageTile(V, t, smem);
-    cpAsyncCommit();
-    if (live && t < nTiles) prefetchTile<R, kDt, kRc>(V, t);
-    for (; live && t < nTiles; t += gridDim.x, b ^= 1) {
-      const int tn = t + gridDim.x;
-      if (tn < nTiles) {
-        stageTile(V, tn, smem + (b ^ 1) * bufFloats);
-        prefetchTile<R, kDt, kRc>(V, tn);
-      }
+    if (live && t < nTiles) {
+      const int4 d0 = loadTileDesc(V, t, nTiles);
+      stageHalo(V, d0, smem);
       cpAsyncCommit();
-      cpAsyncWait<1>();  // this thread's copies of tile t have landed
-      __syncthreads();   // and everyone else's
-      float *buf = smem + b * bufFloats;
-      const int base = t * kTile;
-      const int i = base + threadIdx.x;
-      if (i < V.nc) {
-        const float *ids = buf + 8 * (size_t)V.maxRecs;
-        float g[15];
-        const float sum = gradLimitPacked<kDt, true, kRc>(
-            V, i, g, dc + threadIdx.x, buf, threadIdx.x, reinterpret_cast<const unsigned short *>(ids),
-            reinterpret_cast<const int *>(ids + 4 * tileIdWords(V)));
-        storeGrad(V, i, g);
-        if (kDt) dt = fmin(dt, V.vol[i] / (double)sum);
+      cpAsyncWait<0>();
+      __syncthreads();
+      int4 d1 = loadTileDesc(V, t + G, nTiles);
+      stageRecs(V, t, d0, smem);
+      if (t + G < nTiles) stageHalo(V, d1, smem + bufFloats);
+      cpAsyncCommit();
+      prefetchTile<R, kDt, kRc>(V, t);
+      int4 d2 = loadTileDesc(V, t + 2 * G, nTiles);
+      for (; t < nTiles; t += G, b ^= 1) {
+        cpAsyncWait<0>();  // this thread's copies of tile t and of t + G's halo ids have landed
+        __syncthreads();   // and everyone else's
+        const int tn = t + G;
+        float *buf = smem + b * bufFloats;
+        if (tn < nTiles) {
+          stageRecs(V, tn, d1, smem + (b ^ 1) * bufFloats);
+          prefetchTile<R, kDt, kRc>(V, tn);
+        }
+        if (tn + G < nTiles) stageHalo(V, d2, buf);
+        cpAsyncCommit();
+        d1 = d2;
+        d2 = loadTileDesc(V, tn + 2 * G, nTiles);
+        const int base = t * kTile;
+        const int i = base + threadIdx.x;
+        if (i < V.nc) {
+          const float *ids = buf + 8 * (size_t)V.maxRecs;
+          float g[15];
+          const float sum = gradLimitPacked<kDt, true, kRc>(
+              V, i, g, dc + threadIdx.x, buf, threadIdx.x, reinterpret_cast<const unsigned short *>(ids),
+              reinterpret_cast<const int *>(ids + 4 * tileIdWords(V)));
+          storeGrad(V, i, g);
+          if (kDt) dt = fmin(dt, V.vol[i] / (double)sum);
+        }
+        __syncthreads();  // buffer b is free for the tile after next
       }
-      __syncthreads();  // buffer b is free for the tile after next
     }
     cpAsyncWait<0>();
     if (kDt) blockMinDt(V.sc, dt);

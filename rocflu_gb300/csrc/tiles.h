@@ -34,8 +34,11 @@ struct TilePlan {
 // differ in those bits, and with the record swizzle their 16-byte loads hit
 // 8 different shared-memory bank groups.  The aligned slots are taken
 // unless their larger buffers would fit fewer CTAs per SM (unstructured
-// meshes, whose residues are uneven).  Returns false when a tile would need
-// more than 65535 records (the mesh then stays untiled).
+// meshes, whose residues are uneven).  Either way every tile's list holds a
+// multiple of 4 slots (unused ones -1), so that each starts on a 16-byte
+// boundary and the kernels copy it as whole 16-byte words.  Returns false
+// when a tile would need more than 65535 records (the mesh then stays
+// untiled).
 template <class CtasPerSm>
 inline bool planTiles(int nc, int tile, const std::vector<int> &cfOff, const std::vector<int> &cfEnt,
                       const std::vector<int> &stOff, const std::vector<int> &stIdx, const std::vector<int> &fc1,
@@ -78,7 +81,7 @@ inline bool planTiles(int nc, int tile, const std::vector<int> &cfOff, const std
   for (int t = 0; t < nTiles; ++t) {
     int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int j : halos[t]) cnt[j & 7]++;
-    compactRecs = std::max(compactRecs, tile + (int)halos[t].size());
+    compactRecs = std::max(compactRecs, tile + ((int)halos[t].size() + 3) / 4 * 4);
     alignedRecs = std::max(alignedRecs, tile + 8 * *std::max_element(cnt, cnt + 8));
   }
   p.aligned = tile % 8 == 0 && alignedRecs <= 65535 &&
@@ -109,7 +112,7 @@ inline bool planTiles(int nc, int tile, const std::vector<int> &cfOff, const std
         if (cfEnt[e] >= 0) p.entLoc[e] = local(other(e));
     }
     const size_t h0 = p.haloIdx.size();
-    p.haloIdx.resize(h0 + (p.aligned ? 8 * (size_t)rows : halo.size()), -1);
+    p.haloIdx.resize(h0 + (p.aligned ? 8 * (size_t)rows : (halo.size() + 3) / 4 * 4), -1);
     for (int j : halo) p.haloIdx[h0 + slot[j]] = j;
     p.haloOff[t + 1] = (int)p.haloIdx.size();
   }
