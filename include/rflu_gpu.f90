@@ -24,8 +24,16 @@ MODULE RFLU_ModGPU
   INTEGER(C_INT), PARAMETER :: RFLU_PREC_FP64 = 0, &
                                RFLU_PREC_FP64_EXACT = 1, &
                                RFLU_PREC_MIXED = 2
-  INTEGER(C_INT), PARAMETER :: RFLU_BC_OUTFLOW = 20, &
-                               RFLU_BC_SLIPWALL = 60
+  INTEGER(C_INT), PARAMETER :: RFLU_BC_INFLOW_TOTANG = 10, &
+                               RFLU_BC_INFLOW_VELTEMP = 11, &
+                               RFLU_BC_OUTFLOW = 20, &
+                               RFLU_BC_SLIPWALL = 60, &
+                               RFLU_BC_NOSLIPWALL_HFLUX = 70, &
+                               RFLU_BC_NOSLIPWALL_TEMP = 71, &
+                               RFLU_BC_FARFIELD = 80, &
+                               RFLU_BC_INJECTION = 90
+  INTEGER(C_INT), PARAMETER :: RFLU_BCDAT_N = 8, &
+                               RFLU_BCSWI_N = 2
   INTEGER(C_INT), PARAMETER :: RFLU_OPT_UNTILED = 1
 
   TYPE, BIND(C) :: rflu_grid_desc
@@ -48,6 +56,8 @@ MODULE RFLU_ModGPU
     TYPE(C_PTR) :: c2csOff
     TYPE(C_PTR) :: c2csMembs
     TYPE(C_PTR) :: xyzMoms
+    TYPE(C_PTR) :: patchVals
+    TYPE(C_PTR) :: patchSwitches
   END TYPE rflu_grid_desc
 
   TYPE, BIND(C) :: rflu_num_desc

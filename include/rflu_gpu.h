@@ -40,9 +40,26 @@ extern "C" {
 #define RFLU_PREC_FP64_EXACT 1  /* all FP64, reference evaluation order, no FMA: bit-exact with the CPU restatement */
 #define RFLU_PREC_MIXED 2       /* FP32 state/gradients/fluxes, FP64 master cv, p/c recovery, checks, RK combination */
 
-/* Boundary types, modfloflu/ModParameters.F90:401,413 */
+/* Boundary types, modfloflu/ModParameters.F90:396-441 */
+#define RFLU_BC_INFLOW_TOTANG 10
+#define RFLU_BC_INFLOW_VELTEMP 11
 #define RFLU_BC_OUTFLOW 20
 #define RFLU_BC_SLIPWALL 60
+#define RFLU_BC_NOSLIPWALL_HFLUX 70
+#define RFLU_BC_NOSLIPWALL_TEMP 71
+#define RFLU_BC_FARFIELD 80
+#define RFLU_BC_INJECTION 90
+/* Per-patch boundary values and switches (pPatch%mixt%vals(:,0) and
+ * pPatch%mixt%switches, modfloflu/ModParameters.F90:452-511), uniform over
+ * the patch: RFLU_BCDAT_N values and RFLU_BCSWI_N switches per patch, in
+ * the reference's BCDAT_* / BCSWI_* order (1-based there, 0-based here):
+ *   inflow TOTANG:  PTOT, TTOT, BETAH, BETAV, MACH; switches TYPE, FIXED
+ *   inflow VELTEMP: U, V, W, T, P;                  switches TYPE
+ *   farfield:       MACH, ATTACK, SLIP, PRESS, TEMP; switches CORR (must be 0)
+ *   injection:      MFRATE, TEMP
+ * Outflow keeps patchOutflowType / patchPout. */
+#define RFLU_BCDAT_N 8
+#define RFLU_BCSWI_N 2
 
 /* The reference's setup products for one region, as RFLU_InitFlowSolver
  * leaves them (rocflu/RFLU_InitFlowSolver.F90:496,646,888-931):
@@ -62,13 +79,16 @@ typedef struct {
   const double *bfn;        /* (4,nBFaces) */
   const double *bfc;        /* (3,nBFaces) */
   const int *patchBcType;   /* RFLU_BC_* */
-  const int *patchOutflowType; /* BCOPT_SUPERSONIC 0, SUBSONIC 1, MIXED 2 */
+  const int *patchOutflowType; /* outflow: BCOPT_SUPERSONIC 0, SUBSONIC 1, MIXED 2 */
   const double *patchPout;  /* outflow static pressure */
   const int *patchOrder;    /* pPatch%spaceOrder, 1 or 2 */
   /* C2C stencils (pGrid%c2cs(icg)%cellMembs) as CSR; ignored for ORDER 1 */
   const int *c2csOff;       /* nCells+1, 0-based offsets */
   const int *c2csMembs;     /* 1-based cell ids */
   const double *xyzMoms;    /* (10,nCells) */
+  /* inflow, farfield and injection patches (may be NULL when there are none) */
+  const double *patchVals;  /* (RFLU_BCDAT_N, nPatches) */
+  const int *patchSwitches; /* (RFLU_BCSWI_N, nPatches) */
 } rflu_grid_desc;
 
 /* Numerics, the reference input deck keys (libfloflu/ReadNumericsSection.F90,

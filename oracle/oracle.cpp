@@ -169,6 +169,8 @@ int svdSingularCount(int nRows, int nCols, const std::vector<double> &a) {
 struct Patch {
   int bcType, outflowType, order, related = -1;
   double pOut;
+  double vals[ORC_BCDAT_N] = {0, 0, 0, 0, 0, 0, 0, 0}; /* pPatch%mixt%vals(:,0), BCDAT order */
+  int sw[ORC_BCSWI_N] = {0, 0};                         /* pPatch%mixt%switches, BCSWI order */
   int n;
   std::vector<int> bf2v, bf2c;
   std::vector<double> fn, fc;
@@ -1395,19 +1397,193 @@ void bcondOutflowPerf(int bcOpt, double pout, double sxn, double syn, double szn
   }
 }
 
+/* BcondInflowPerf (libfloflu/BcondInflowPerf.F90), TCPERF gas.  A subsonic
+ * patch whose face sees |ql| >= al leaves the outputs unset in the
+ * reference; they are NaN here. */
+void bcondInflowPerf(int bcOptType, int bcOptFixed, double ptot, double ttot, double betah, double betav,
+                     double mach, double sxn, double syn, double szn, double cpgas, double mm, double rl, double rul,
+                     double rvl, double rwl, double &rr, double &rur, double &rvr, double &rwr, double &rer,
+                     double &pr) {
+  const double rgas = MixtPerf_R_M(mm);
+  const double g = MixtPerf_G_CpR(cpgas, rgas);
+  auto supersonic = [&]() {
+    pr = ptot / std::pow(1.0 + 0.5 * (g - 1.0) * mach * mach, g / (g - 1.0)); /* MixtPerf_P_GMaPo */
+    double tr = ttot / (1.0 + 0.5 * (g - 1.0) * mach * mach);                 /* MixtPerf_T_GMaTo */
+    rr = pr / (rgas * tr);                                                    /* MixtPerf_D_PRT */
+    double ar = std::sqrt(g * rgas * tr);                                     /* MixtPerf_C_GRT */
+    double ur = mach * ar * std::cos(betah) * std::cos(betav);
+    double vr = mach * ar * std::sin(betah);
+    double wr = mach * ar * std::cos(betah) * std::sin(betav);
+    rer = rr * MixtPerf_Eo_DGPUVW(rr, g, pr, ur, vr, wr);
+    rur = rr * ur;
+    rvr = rr * vr;
+    rwr = rr * wr;
+  };
+  if (bcOptType == 1 || bcOptType == 2) { /* BCOPT_SUBSONIC, BCOPT_MIXED */
+    double gm1 = g - 1.0;
+    double ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+    double a02 = g * rgas * ttot;                                             /* MixtPerf_C2_GRT */
+    double al = std::sqrt(a02 - 0.5 * (g - 1.0) * (ul * ul + vl * vl + wl * wl)); /* MixtPerf_C_Co2GUVW */
+    double ql = ul * sxn + vl * syn + wl * szn;
+    if (std::fabs(ql) < al) {
+      double sl = std::sqrt(ul * ul + vl * vl + wl * wl);
+      double eta;
+      if (bcOptFixed == 0) /* BCOPT_FIXED_NO */
+        eta = (sl > 1.0e-6) ? ql / sl : -1.0;
+      else
+        eta = -1.0;
+      double Rm = al - 0.5 * gm1 * ql;
+      double disc = 0.5 * gm1 * (eta * eta) * (a02 / (Rm * Rm) * (1.0 + 0.5 * gm1 * (eta * eta)) - 1.0);
+      double ar, tr, sr;
+      if (disc < 0.0) {
+        ar = std::sqrt(a02);
+        tr = ttot;
+        pr = ptot;
+        sr = 0.0;
+      } else {
+        ar = Rm / (1.0 + 0.5 * gm1 * eta * eta) * (1.0 + std::sqrt(disc));
+        tr = ar * ar / (g * rgas);                                           /* MixtPerf_T_CGR */
+        pr = ptot * std::pow(tr / ttot, g / (g - 1.0));                      /* MixtPerf_P_GPoTTo */
+        double c2 = ar * ar;                                                 /* MixtPerf_Vm_C2Co2G */
+        sr = (a02 > c2) ? std::sqrt(2.0 / (g - 1.0) * (a02 - c2)) : 0.0;
+      }
+      rr = pr / (rgas * tr);
+      double ur = sr * std::cos(betah) * std::cos(betav);
+      double vr = sr * std::sin(betah);
+      double wr = sr * std::cos(betah) * std::sin(betav);
+      rer = rr * (pr / (rr * (g - 1.0)) + 0.5 * sr * sr);                   /* MixtPerf_Eo_DGPVm */
+      rur = rr * ur;
+      rvr = rr * vr;
+      rwr = rr * wr;
+    } else if (bcOptType == 2) {
+      supersonic();
+    } else {
+      rr = rur = rvr = rwr = rer = pr = std::nan("");
+    }
+  } else {
+    supersonic();
+  }
+}
+
+/* RFLU_SetRindStateFarfieldPerf, corrFlag false
+ * (modflu/RFLU_ModRindStates.F90:248-420). */
+void rindStateFarfieldPerf(double cpGas, double mmGas, double nx, double ny, double nz, double machInf, double pInf,
+                           double tInf, double alphaInf, double betaInf, double rl, double rul, double rvl,
+                           double rwl, double rel, double &rr, double &rur, double &rvr, double &rwr, double &rer,
+                           double &pr) {
+  double rGas = MixtPerf_R_M(mmGas);
+  double gGas = MixtPerf_G_CpR(cpGas, rGas);
+  double ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+  double ql = ul * nx + vl * ny + wl * nz;
+  double el = rel / rl;
+  double sl2 = ul * ul + vl * vl + wl * wl;
+  double pl = MixtPerf_P_DEoGVm2(rl, el, gGas, sl2);
+  double ri = pInf / (rGas * tInf); /* MixtPerf_D_PRT */
+  double pi = pInf;
+  double qi = machInf * MixtPerf_C_GRT(gGas, rGas, tInf);
+  double ui = qi * std::cos(alphaInf) * std::cos(betaInf);
+  double vi = qi * std::sin(alphaInf) * std::cos(betaInf);
+  double wi = qi * std::sin(betaInf);
+  if (machInf < 1.0) {
+    double al = MixtPerf_C_DGP(rl, gGas, pl);
+    double pb, rb, ub, vb, wb;
+    if (ql < 0.0) {
+      pb = 0.5 * (pi + pl - rl * al * ((ui - ul) * nx + (vi - vl) * ny + (wi - wl) * nz));
+      rb = ri - (pi - pb) / (al * al);
+      ub = ui - nx * (pi - pb) / (rl * al);
+      vb = vi - ny * (pi - pb) / (rl * al);
+      wb = wi - nz * (pi - pb) / (rl * al);
+    } else {
+      pb = pi;
+      rb = rl - (pl - pi) / (al * al);
+      ub = ul + nx * (pl - pi) / (rl * al);
+      vb = vl + ny * (pl - pi) / (rl * al);
+      wb = wl + nz * (pl - pi) / (rl * al);
+    }
+    rr = rb;
+    rur = rb * ub;
+    rvr = rb * vb;
+    rwr = rb * wb;
+    rer = rb * MixtPerf_Eo_DGPUVW(rb, gGas, pb, ub, vb, wb);
+    pr = pb;
+  } else if (ql < 0.0) {
+    rr = ri;
+    rur = ri * ui;
+    rvr = ri * vi;
+    rwr = ri * wi;
+    rer = ri * (pi / (ri * (gGas - 1.0)) + 0.5 * qi * qi); /* MixtPerf_Eo_DGPVm */
+    pr = pi;
+  } else {
+    rr = rl; rur = rul; rvr = rvl; rwr = rwl; rer = rel; pr = pl;
+  }
+}
+
+/* RFLU_SetRindStateSlipWallPerf, fs = 0 (modflu/RFLU_ModRindStates.F90:
+ * 535-584): returns the modified pl. */
+double rindStateSlipWallPerf(double cpGas, double mmGas, double nx, double ny, double nz, double rl, double rul,
+                             double rvl, double rwl, double pl) {
+  double rGas = MixtPerf_R_M(mmGas);
+  double gGas = MixtPerf_G_CpR(cpGas, rGas);
+  double irl = 1.0 / rl;
+  double ul = irl * rul, vl = irl * rvl, wl = irl * rwl;
+  double ql = ul * nx + vl * ny + wl * nz - 0.0;
+  double al = MixtPerf_C_DGP(rl, gGas, pl);
+  if (ql < 0.0) {
+    double term = 1.0 + 0.5 * (gGas - 1.0) * ql / al;
+    return pl * std::pow(term, 2.0 * gGas / (gGas - 1.0));
+  }
+  double term = (gGas + 1.0) / 4.0;
+  return pl + term * rl * ql * (ql + std::sqrt(al * al + term * term * ql * ql) / term);
+}
+
+/* The central boundary flux of the inflow/outflow/farfield cases
+ * (rocflu/RFLU_CentralFirstPatch.F90:281-287), fs = 0. */
+void centralBoundaryFlux(double nx, double ny, double nz, double nm, double rl, double rul, double rvl, double rwl,
+                         double rel, double pl, double rr, double rur, double rvr, double rwr, double rer, double pr,
+                         double flx[5]) {
+  const double fs = 0.0;
+  double ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
+  double qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
+  flx[0] = 0.5 * (ql * rl + qr * rr) * nm;
+  flx[1] = 0.5 * (ql * rul + pl * nx + qr * rur + pr * nx) * nm;
+  flx[2] = 0.5 * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
+  flx[3] = 0.5 * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
+  flx[4] = 0.5 * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+}
+
+/* Injection (RFLU_CentralFirstPatch.F90:1043-1127 and
+ * RFLU_CentralSecondPatch.F90:1229-1343 with RFLU_SetRindStateInjectPerf,
+ * RFLU_ModRindStates.F90:459-501), fs = fsu = 0. */
+void injectionFlux(const orc_ctx *c, const Patch &p, double nx, double ny, double nz, double nm, double rl,
+                   double rul, double rvl, double rwl, double pl, double flx[5]);
+
+/* The inflow, farfield and injection cases of the two patch routines, from
+ * the interior state (rl, rul, rvl, rwl, rel, pl): cv and dv at first
+ * order, the reconstructed face state at second. */
+void remainingPatchFlux(const orc_ctx *c, const Patch &p, double nx, double ny, double nz, double nm, double rl,
+                        double rul, double rvl, double rwl, double rel, double pl, double flx[5]);
+
 /* Patch flux of one boundary face: RFLU_CentralFirstPatch
- * (rocflu/RFLU_CentralFirstPatch.F90:571-911) and RFLU_CentralSecondPatch
- * (rocflu/RFLU_CentralSecondPatch.F90:634-1029), slip wall and outflow. */
+ * (rocflu/RFLU_CentralFirstPatch.F90:222-1146) and RFLU_CentralSecondPatch
+ * (rocflu/RFLU_CentralSecondPatch.F90:233-1360): inflow (TOTANG, VELTEMP),
+ * outflow, slip and no-slip walls, farfield (no vortex correction) and
+ * injection, TCPERF gas, static grid. */
 void patchFlux(orc_ctx *c, const Patch &p, int i, double flx[5]) {
   const int c1 = p.bf2c[i];
   const double nx = p.fn[4 * i], ny = p.fn[4 * i + 1], nz = p.fn[4 * i + 2], nm = p.fn[4 * i + 3];
   const double fs = 0.0;
   const double *cv = &c->cv[5 * c1];
   flx[0] = 0.0;
+  const bool wall = p.bcType == ORC_BC_SLIPWALL || p.bcType == ORC_BC_NOSLIPWALL_HFLUX ||
+                    p.bcType == ORC_BC_NOSLIPWALL_TEMP;
   if (p.order == 1) {
     double rl = cv[0], rul = cv[1], rvl = cv[2], rwl = cv[3], rel = cv[4], pl = c->dv[3 * c1];
-    if (p.bcType == ORC_BC_SLIPWALL) {
+    if (wall) {
       flx[1] = pl * nx * nm; flx[2] = pl * ny * nm; flx[3] = pl * nz * nm; flx[4] = pl * fs * nm;
+      return;
+    }
+    if (p.bcType != ORC_BC_OUTFLOW) {
+      remainingPatchFlux(c, p, nx, ny, nz, nm, rl, rul, rvl, rwl, rel, pl, flx);
       return;
     }
     double pr = (p.outflowType != 0) ? p.pOut : pl;
@@ -1427,13 +1603,21 @@ void patchFlux(orc_ctx *c, const Patch &p, int i, double flx[5]) {
   FaceState L = reconstruct(c, c1, xc, yc, zc);
   double rl = L.r, ul = L.u, vl = L.v, wl = L.w, pl = L.p;
   double rul = rl * ul, rvl = rl * vl, rwl = rl * wl;
-  if (p.bcType == ORC_BC_SLIPWALL) {
+  if (wall) {
     flx[1] = pl * nx * nm; flx[2] = pl * ny * nm; flx[3] = pl * nz * nm; flx[4] = pl * fs * nm;
+    return;
+  }
+  if (p.bcType == ORC_BC_INJECTION) {
+    injectionFlux(c, p, nx, ny, nz, nm, rl, rul, rvl, rwl, pl, flx);
     return;
   }
   double pr = (p.outflowType != 0) ? p.pOut : pl;
   double rgas = MixtPerf_R_M(c->gvMol), g = MixtPerf_G_CpR(c->gvCp, rgas);
   double rel = rl * MixtPerf_Eo_DGPUVW(rl, g, pl, ul, vl, wl);
+  if (p.bcType != ORC_BC_OUTFLOW) {
+    remainingPatchFlux(c, p, nx, ny, nz, nm, rl, rul, rvl, rwl, rel, pl, flx);
+    return;
+  }
   double rr, rur, rvr, rwr, rer;
   bcondOutflowPerf(p.outflowType, pr, nx, ny, nz, c->gvCp, c->gvMol, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr,
                    rer);
@@ -1444,6 +1628,66 @@ void patchFlux(orc_ctx *c, const Patch &p, int i, double flx[5]) {
   flx[2] = 0.5 * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
   flx[3] = 0.5 * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
   flx[4] = 0.5 * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+}
+
+void injectionFlux(const orc_ctx *c, const Patch &p, double nx, double ny, double nz, double nm, double rl,
+                   double rul, double rvl, double rwl, double pl, double flx[5]) {
+  const double fs = 0.0;
+  const double minj = p.vals[0]; /* BCDAT_INJECT_MFRATE */
+  if (minj > 0.0) {
+    const double tinj = p.vals[1]; /* BCDAT_INJECT_TEMP */
+    double rGas = MixtPerf_R_M(c->gvMol);
+    double rb = pl / (rGas * tinj); /* MixtPerf_D_PRT */
+    double qb = -minj / rb + fs;
+    double ub = qb * nx, vb = qb * ny, wb = qb * nz;
+    double hb = MixtPerf_Ho_CpTUVW(c->gvCp, tinj, ub, vb, wb);
+    flx[0] = -minj * nm;
+    flx[1] = (-minj * ub + pl * nx) * nm;
+    flx[2] = (-minj * vb + pl * ny) * nm;
+    flx[3] = (-minj * wb + pl * nz) * nm;
+    flx[4] = (-minj * hb + pl * fs) * nm;
+  } else {
+    double pw = rindStateSlipWallPerf(c->gvCp, c->gvMol, nx, ny, nz, rl, rul, rvl, rwl, pl);
+    flx[0] = 0.0;
+    flx[1] = pw * nx * nm;
+    flx[2] = pw * ny * nm;
+    flx[3] = pw * nz * nm;
+    flx[4] = pw * fs * nm;
+  }
+}
+
+void remainingPatchFlux(const orc_ctx *c, const Patch &p, double nx, double ny, double nz, double nm, double rl,
+                        double rul, double rvl, double rwl, double rel, double pl, double flx[5]) {
+  if (p.bcType == ORC_BC_INJECTION) {
+    injectionFlux(c, p, nx, ny, nz, nm, rl, rul, rvl, rwl, pl, flx);
+    return;
+  }
+  double rr, rur, rvr, rwr, rer, pr;
+  const double *v = p.vals;
+  if (p.bcType == ORC_BC_FARFIELD) {
+    rindStateFarfieldPerf(c->gvCp, c->gvMol, nx, ny, nz, v[0], v[3], v[4], v[1], v[2], rl, rul, rvl, rwl, rel, rr,
+                          rur, rvr, rwr, rer, pr);
+  } else if (p.bcType == ORC_BC_INFLOW_TOTANG) {
+    const double mach = (p.sw[0] != 1) ? v[4] : 0.0; /* BCDAT_INFLOW_MACH unless subsonic */
+    bcondInflowPerf(p.sw[0], p.sw[1], v[0], v[1], v[2], v[3], mach, nx, ny, nz, c->gvCp, c->gvMol, rl, rul, rvl,
+                    rwl, rr, rur, rvr, rwr, rer, pr);
+  } else { /* ORC_BC_INFLOW_VELTEMP (RFLU_CentralFirstPatch.F90:375-570) */
+    const double ur = v[0], vr = v[1], wr = v[2], tr = v[3];
+    double rgas = MixtPerf_R_M(c->gvMol);
+    double g = MixtPerf_G_CpR(c->gvCp, rgas);
+    if (p.sw[0] != 1) {
+      pr = v[4];
+      rr = pr / (rgas * tr); /* MixtPerf_D_PRT */
+    } else {
+      rr = rl;
+      pr = rr * rgas * tr; /* MixtPerf_P_DRT */
+    }
+    rer = rr * MixtPerf_Eo_DGPUVW(rr, g, pr, ur, vr, wr);
+    rur = rr * ur;
+    rvr = rr * vr;
+    rwr = rr * wr;
+  }
+  centralBoundaryFlux(nx, ny, nz, nm, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr, rer, pr, flx);
 }
 
 /* ConvectiveFluxes (libfloflu/ConvectiveFluxes.F90:120-175): rhs = -diss,
@@ -1472,7 +1716,8 @@ void convectiveFluxes(orc_ctx *c) {
       } else {
         const int b = -code - 1;
         const double *flx = &c->flux[5 * ((size_t)nf + b)];
-        const int k0 = (c->patches[c->bPatch[b]].bcType == ORC_BC_SLIPWALL) ? 1 : 0;
+        const int bt = c->patches[c->bPatch[b]].bcType;
+        const int k0 = (bt == ORC_BC_SLIPWALL || bt == ORC_BC_NOSLIPWALL_HFLUX || bt == ORC_BC_NOSLIPWALL_TEMP) ? 1 : 0;
         for (int k = k0; k < 5; ++k) rhs[k] = rhs[k] + flx[k];
       }
     }
@@ -1662,6 +1907,10 @@ orc_ctx *orc_create(const orc_mesh_desc *m, const orc_num_desc *num) {
     p.pOut = m->patchPout[ip];
     p.order = m->patchOrder[ip];
     p.related = m->patchRelated ? m->patchRelated[ip] : -1;
+    if (m->patchVals)
+      for (int k = 0; k < ORC_BCDAT_N; ++k) p.vals[k] = m->patchVals[ORC_BCDAT_N * ip + k];
+    if (m->patchSwitches)
+      for (int k = 0; k < ORC_BCSWI_N; ++k) p.sw[k] = m->patchSwitches[ORC_BCSWI_N * ip + k];
     int b = m->patchFaceOff[ip], e = m->patchFaceOff[ip + 1];
     p.n = e - b;
     p.bf2v.assign(m->bf2v + 4 * b, m->bf2v + 4 * e);

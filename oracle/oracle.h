@@ -31,10 +31,18 @@
 extern "C" {
 #endif
 
-/* Boundary condition types (modfloflu/ModParameters.F90:401,413,438). */
+/* Boundary condition types (modfloflu/ModParameters.F90:396-441). */
+#define ORC_BC_INFLOW_TOTANG 10
+#define ORC_BC_INFLOW_VELTEMP 11
 #define ORC_BC_OUTFLOW 20
 #define ORC_BC_SLIPWALL 60
+#define ORC_BC_NOSLIPWALL_HFLUX 70
+#define ORC_BC_NOSLIPWALL_TEMP 71
+#define ORC_BC_FARFIELD 80
+#define ORC_BC_INJECTION 90
 #define ORC_BC_PERIODIC 110
+#define ORC_BCDAT_N 8
+#define ORC_BCSWI_N 2
 
 typedef struct {
   int nVert;
@@ -54,6 +62,11 @@ typedef struct {
      patches.  The two patches' faces are paired by their vertex
      coordinates, which differ by one translation per pair. */
   const int *patchRelated;
+  /* pPatch%mixt%vals(:,0) and pPatch%mixt%switches of each patch in the
+     reference's BCDAT_* / BCSWI_* order (ORC_BCDAT_N and ORC_BCSWI_N per
+     patch); NULL when no patch needs them (inflow, farfield, injection) */
+  const double *patchVals;
+  const int *patchSwitches;
 } orc_mesh_desc;
 
 typedef struct {

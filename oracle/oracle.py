@@ -20,7 +20,8 @@ class MeshDesc(C.Structure):
                 ("nPatches", C.c_int), ("patchFaceOff", C.POINTER(C.c_int)),
                 ("bf2v", C.POINTER(C.c_int)), ("patchBcType", C.POINTER(C.c_int)),
                 ("patchOutflowType", C.POINTER(C.c_int)), ("patchPout", C.POINTER(C.c_double)),
-                ("patchOrder", C.POINTER(C.c_int)), ("patchRelated", C.POINTER(C.c_int))]
+                ("patchOrder", C.POINTER(C.c_int)), ("patchRelated", C.POINTER(C.c_int)),
+                ("patchVals", C.POINTER(C.c_double)), ("patchSwitches", C.POINTER(C.c_int))]
 
 
 class NumDesc(C.Structure):
@@ -127,7 +128,14 @@ def _mesh_arrays(case):
     pout = np.array([p.p_out for p in case.patches], dtype=np.float64)
     order = np.array([p.order for p in case.patches], dtype=np.int32)
     rel = np.array([getattr(p, "related", -1) for p in case.patches], dtype=np.int32)
-    return xyz, c2v, off, bf2v, bct, oft, pout, order, rel
+    np_ = max(len(case.patches), 1)
+    vals = np.zeros((np_, 8), dtype=np.float64)
+    sw = np.zeros((np_, 2), dtype=np.int32)
+    for i, p in enumerate(case.patches):
+        v, w = tuple(getattr(p, "vals", ()) or ()), tuple(getattr(p, "switches", ()) or ())
+        vals[i, :len(v)] = v
+        sw[i, :len(w)] = w
+    return xyz, c2v, off, bf2v, bct, oft, pout, order, rel, vals, sw
 
 
 def num_desc(num):
@@ -142,11 +150,12 @@ class Oracle:
     def __init__(self, case):
         self.case = case
         self._keep = _mesh_arrays(case)
-        xyz, c2v, off, bf2v, bct, oft, pout, order, rel = self._keep
+        xyz, c2v, off, bf2v, bct, oft, pout, order, rel, vals, sw = self._keep
         md = MeshDesc(xyz.shape[0], c2v.shape[0], c2v.shape[1], _ptr(xyz, C.c_double), _ptr(c2v, C.c_int),
                       len(case.patches), _ptr(off, C.c_int), _ptr(bf2v, C.c_int), _ptr(bct, C.c_int),
                       _ptr(oft, C.c_int), _ptr(pout, C.c_double), _ptr(order, C.c_int),
-                      _ptr(rel, C.c_int) if (rel >= 0).any() else None)
+                      _ptr(rel, C.c_int) if (rel >= 0).any() else None, _ptr(vals, C.c_double),
+                      _ptr(sw, C.c_int))
         self.nd = num_desc(case.num)
         self.h = lib().orc_create(C.byref(md), C.byref(self.nd))
         self.n_cells = c2v.shape[0]

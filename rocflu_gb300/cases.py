@@ -17,9 +17,16 @@ import numpy as np
 
 from . import meshgen
 
+BC_INFLOW_TOTANG = 10
+BC_INFLOW_VELTEMP = 11
 BC_OUTFLOW = 20
 BC_SLIPWALL = 60
+BC_NOSLIPWALL_HFLUX = 70
+BC_NOSLIPWALL_TEMP = 71
+BC_FARFIELD = 80
+BC_INJECTION = 90
 BC_PERIODIC = 110
+BCOPT_SUPERSONIC, BCOPT_SUBSONIC, BCOPT_MIXED = 0, 1, 2
 
 DISCR_ROE, DISCR_HLLC, DISCR_AUSM = 1, 3, 4
 RECONST_NONE, RECONST_BJ, RECONST_VENKAT, RECONST_BJ_COMP = 0, 10, 11, 100
@@ -36,6 +43,10 @@ class Patch:
     order: int = 1
     name: str = ""
     related: int = -1       # BC_PERIODIC: the 0-based related patch (RELPATCH)
+    # inflow, farfield, injection: pPatch%mixt%vals(:,0) and switches in the
+    # reference's BCDAT_* / BCSWI_* order (modfloflu/ModParameters.F90:452-511)
+    vals: tuple = ()
+    switches: tuple = ()
 
 
 @dataclass
@@ -245,3 +256,50 @@ def blast_hex(n=64, num=None, p_in=10.0, radius=0.15):
     cv0 = conserved(one, z, z, z, p, num.gamma)
     num.dt_imposed = 1.0
     return Case("blast_hex", mesh["xyz"], mesh["c2v"], patches, num, cv0, n_steps=200)
+
+
+def open_channel(n=8, num=None, inflow=BC_INFLOW_TOTANG, inflow_type=BCOPT_SUBSONIC, order=2, mach=0.3,
+                 seed=3, pert=0.02, injection=0.05, tets=False):
+    """A box open to the outside on every side type the path carries: n x
+    n/2 x n/2 hexes (or 6 jittered tetrahedra per hex) on [0,1] x [0,0.5]^2,
+    uniform Mach-`mach` flow along x (rho = 1, p = 1/gamma, so c = 1 and,
+    with cp = 3.5, R = 1) with a seeded +-`pert` perturbation.  x-low: inflow
+    (TOTANG: the flow's total pressure and temperature, zero angles; VELTEMP:
+    its velocity, temperature and pressure) of the given BCOPT type; x-high:
+    subsonic outflow at the static pressure; y faces: farfield at the flow's
+    Mach number, pressure and temperature; z-low: injection of
+    `injection` mass flux at the flow's temperature (0: a non-burning
+    injection wall); z-high: no-slip wall."""
+    ny = max(n // 2, 2)
+    if tets:
+        mesh = meshgen.tet_box(n, jitter=0.2, seed=0)
+    else:
+        mesh = meshgen.hex_box(n, ny, ny, hi=(1.0, 0.5, 0.5))
+    if num is None:
+        num = Numerics(space_order=order, space_discr=DISCR_HLLC, reconst=RECONST_BJ, cfl=0.4)
+    g = num.gamma
+    rgas = num.cp - num.cp / g
+    p0, rho0 = 1.0 / g, 1.0
+    t0 = p0 / (rho0 * rgas)
+    u0 = mach * math.sqrt(g * p0 / rho0)
+    fac = 1.0 + 0.5 * (g - 1.0) * mach * mach
+    if inflow == BC_INFLOW_TOTANG:
+        inl = {"bc_type": inflow, "vals": (p0 * fac ** (g / (g - 1.0)), t0 * fac, 0.0, 0.0, mach),
+               "switches": (inflow_type, 0)}
+    else:
+        inl = {"bc_type": inflow, "vals": (u0, 0.0, 0.0, t0, p0), "switches": (inflow_type, 0)}
+    out = {"bc_type": BC_OUTFLOW, "outflow_type": BCOPT_SUBSONIC, "p_out": p0}
+    far = {"bc_type": BC_FARFIELD, "vals": (mach, 0.0, 0.0, p0, t0), "switches": (0, 0)}
+    inj = {"bc_type": BC_INJECTION, "vals": (injection, t0)}
+    wall = {"bc_type": BC_NOSLIPWALL_HFLUX}
+    kinds = [inl, out, far, far, inj, wall]
+    patches = _patches(mesh, [dict(k, order=min(order, num.space_order)) for k in kinds])
+    nc = mesh["c2v"].shape[0]
+    one = np.ones(nc)
+    cv0 = conserved(rho0 * one, u0 * one, 0 * one, 0 * one, p0 * one, g)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cv0 = cv0 * (1.0 + pert * rng.standard_normal(cv0.shape))
+    cv0[:, 2] = pert * u0 * rng.standard_normal(nc)
+    cv0[:, 3] = pert * u0 * rng.standard_normal(nc)
+    num.dt_imposed = 1.0e-3
+    return Case("open_channel", mesh["xyz"], mesh["c2v"], patches, num, cv0, n_steps=20)

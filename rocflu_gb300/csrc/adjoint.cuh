@@ -748,7 +748,7 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int 
     const int type = V.patchType[ip], order = V.patchOrder[ip];
 #pragma unroll
     for (int k = 0; k < 5; ++k) fbar[k] = W.cvd[k * n + c];
-    if (type == 60) fbar[0] = R(0);  // slip walls leave rhs(DENS)
+    if (patchLeavesDensity(type)) fbar[0] = R(0);  // walls leave rhs(DENS)
     if (order == 1) {
       using D6 = Dual<6>;
       D6 cv[5], flx[5];
@@ -759,8 +759,8 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int 
         fb[k] = (double)fbar[k];
       }
       D6 pl = D6::seed(V.dv[c], 5);
-      patch1(P, type, V.patchOutflow[ip], V.patchPout[ip], cv, pl, D6((double)V.bnx[b]), D6((double)V.bny[b]),
-             D6((double)V.bnz[b]), D6((double)V.bnm[b]), flx);
+      patch1(P, type, V.patchOutflow[ip], V.patchK + kPatchK * ip, cv, pl, D6((double)V.bnx[b]),
+             D6((double)V.bny[b]), D6((double)V.bnz[b]), D6((double)V.bnm[b]), flx);
       contract(flx, fb, o6);
 #pragma unroll
       for (int m = 0; m < 6; ++m) out[m] = (R)o6[m];
@@ -772,8 +772,8 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int 
       D5 a[5], flx[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) a[k] = D5::seed(L[k], k);
-      patch2(P, type, V.patchOutflow[ip], V.patchPout[ip], a, D5(V.bnx[b]), D5(V.bny[b]), D5(V.bnz[b]), D5(V.bnm[b]),
-             flx);
+      patch2(P, type, V.patchOutflow[ip], V.patchK + kPatchK * ip, a, D5(V.bnx[b]), D5(V.bny[b]), D5(V.bnz[b]),
+             D5(V.bnm[b]), flx);
       contract(flx, fbar, out);
     }
   }

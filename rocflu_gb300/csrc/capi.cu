@@ -328,6 +328,7 @@ struct Ctx : CtxBase {
   }
 
   int create(const rflu_grid_desc *g, const rflu_num_desc *num);
+  int patchConstants(const rflu_grid_desc *g, int ip, const rflu_num_desc *num, int *bcOpt, double *K);
   int buildTiles(const std::vector<int> &cfOff, const std::vector<int> &cfEnt, const std::vector<int> &stOff,
                  const std::vector<int> &stIdx, const std::vector<int> &fc1, const std::vector<int> &fc2,
                  const std::vector<double> &fnx, const std::vector<double> &fny, const std::vector<double> &fnz,
@@ -995,6 +996,91 @@ struct Ctx : CtxBase {
   int nPatches = 0;
 };
 
+// The per-patch constants of the device's patch fluxes (physics.cuh:
+// kPatchK) from the patch's boundary values, in the reference's operation
+// order: the parts of RFLU_SetRindStateFarfieldPerf
+// (modflu/RFLU_ModRindStates.F90:272-290) and BcondInflowPerf
+// (libfloflu/BcondInflowPerf.F90: the supersonic branch) that depend on the
+// patch alone, with gas constants MixtPerf_R_M and MixtPerf_G_CpR
+// (libfloflu/MixtPerf_R.F90:93, MixtPerf_G.F90:78).  *bcOpt receives the
+// patch's BCOPT type switch (outflow: patchOutflowType; inflow:
+// BCSWI_INFLOW_TYPE).
+template <typename R>
+int Ctx<R>::patchConstants(const rflu_grid_desc *g, int ip, const rflu_num_desc *num, int *bcOpt, double *K) {
+  const int type = g->patchBcType[ip];
+  // the gas constants of the device's Params (cp, and the molecular mass
+  // MixtPerf_M_R(MixtPerf_R_CpG(cp, gamma)))
+  const double gcp = num->cp, gmol = 8314.3 / (num->cp - num->cp / num->gamma);
+  const double Rg = 8314.3 / gmol, gam = gcp / (gcp - Rg);
+  const double *vals = g->patchVals ? g->patchVals + (size_t)RFLU_BCDAT_N * ip : nullptr;
+  const int *sw = g->patchSwitches ? g->patchSwitches + (size_t)RFLU_BCSWI_N * ip : nullptr;
+  auto need = [&](bool withSwitches) {
+    if (!vals || (withSwitches && !sw))
+      return fail(RFLU_ERR_ARG, "rflu_gpu_create: inflow, farfield and injection patches need patchVals/patchSwitches");
+    return RFLU_OK;
+  };
+  switch (type) {
+    case RFLU_BC_SLIPWALL:
+    case RFLU_BC_NOSLIPWALL_HFLUX:
+    case RFLU_BC_NOSLIPWALL_TEMP:
+      return RFLU_OK;
+    case RFLU_BC_OUTFLOW:
+      K[0] = g->patchPout[ip];
+      return RFLU_OK;
+    case RFLU_BC_FARFIELD: {
+      if (int rc = need(true)) return rc;
+      if (sw[0] != 0)
+        return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: the farfield vortex correction (CORR 1) is not on this path");
+      const double mf = vals[0], aoa = vals[1], aos = vals[2], pf = vals[3], tf = vals[4];
+      const double ri = pf / (Rg * tf);                                  // MixtPerf_D_PRT
+      const double qi = mf * std::sqrt(gam * Rg * tf);                   // MixtPerf_C_GRT
+      const double ui = qi * std::cos(aoa) * std::cos(aos), vi = qi * std::sin(aoa) * std::cos(aos),
+                   wi = qi * std::sin(aos);
+      const double k[8] = {mf, ri, pf, qi, ui, vi, wi, ri * (pf / (ri * (gam - 1.0)) + 0.5 * qi * qi)};
+      std::memcpy(K, k, sizeof(k));
+      return RFLU_OK;
+    }
+    case RFLU_BC_INFLOW_TOTANG: {
+      if (int rc = need(true)) return rc;
+      *bcOpt = sw[0];
+      if (sw[0] < 0 || sw[0] > 2 || sw[1] < 0 || sw[1] > 1)
+        return fail(RFLU_ERR_ARG, "rflu_gpu_create: bad inflow TYPE or FIXED switch");
+      const double ptot = vals[0], ttot = vals[1], bh = vals[2], bv = vals[3];
+      const double k[7] = {ptot, ttot, std::cos(bh), std::sin(bh), std::cos(bv), std::sin(bv), (double)sw[1]};
+      std::memcpy(K, k, sizeof(k));
+      if (sw[0] != 1) {  // the supersonic state (BCOPT_SUPERSONIC, and MIXED beyond the sound speed)
+        const double mach = vals[4];
+        const double pr = ptot / std::pow(1.0 + 0.5 * (gam - 1.0) * mach * mach, gam / (gam - 1.0));  // MixtPerf_P_GMaPo
+        const double tr = ttot / (1.0 + 0.5 * (gam - 1.0) * mach * mach);                              // MixtPerf_T_GMaTo
+        const double rr = pr / (Rg * tr);
+        const double ar = std::sqrt(gam * Rg * tr);
+        const double ur = mach * ar * std::cos(bh) * std::cos(bv), vr = mach * ar * std::sin(bh),
+                     wr = mach * ar * std::cos(bh) * std::sin(bv);
+        const double rer = rr * (pr / (rr * (gam - 1.0)) + 0.5 * (ur * ur + vr * vr + wr * wr));  // MixtPerf_Eo_DGPUVW
+        const double s[6] = {rr, rr * ur, rr * vr, rr * wr, rer, pr};
+        std::memcpy(K + 7, s, sizeof(s));
+      }
+      return RFLU_OK;
+    }
+    case RFLU_BC_INFLOW_VELTEMP: {
+      if (int rc = need(true)) return rc;
+      *bcOpt = sw[0];
+      if (sw[0] < 0 || sw[0] > 2) return fail(RFLU_ERR_ARG, "rflu_gpu_create: bad inflow TYPE switch");
+      const double k[6] = {vals[0], vals[1], vals[2], vals[3], vals[4], vals[4] / (Rg * vals[3])};
+      std::memcpy(K, k, sizeof(k));
+      return RFLU_OK;
+    }
+    case RFLU_BC_INJECTION: {
+      if (int rc = need(false)) return rc;
+      K[0] = vals[0];
+      K[1] = vals[1];
+      return RFLU_OK;
+    }
+    default:
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: patch type " + std::to_string(type) + " is not on this path");
+  }
+}
+
 // Tiles of the mixed-mode gradient kernel (ctx.h): per tile of kTile
 // consecutive cells, its halo cells in slots (planTiles, tiles.h: aligned to
 // the shared-memory banks where that costs no occupancy); the local id of
@@ -1148,14 +1234,12 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   std::vector<int> bcell(nb), bpatch(nb);
   std::vector<double> bnx(nb), bny(nb), bnz(nb), bnm(nb), bd(3 * (size_t)nb);
   std::vector<int> pType(std::max(np, 1)), pOut(std::max(np, 1)), pOrder(std::max(np, 1));
-  std::vector<double> pP(std::max(np, 1));
+  std::vector<double> pK((size_t)kPatchK * std::max(np, 1), 0.0);
   for (int ip = 0; ip < np; ++ip) {
     pType[ip] = g->patchBcType[ip];
     pOut[ip] = g->patchOutflowType[ip];
     pOrder[ip] = g->patchOrder[ip];
-    pP[ip] = g->patchPout[ip];
-    if (pType[ip] != RFLU_BC_OUTFLOW && pType[ip] != RFLU_BC_SLIPWALL)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: only slip-wall and outflow patches are on this path");
+    if (int rc = patchConstants(g, ip, num, &pOut[ip], &pK[(size_t)kPatchK * ip])) return rc;
     if (pOrder[ip] == 2 && num->spaceOrder < 2)
       return fail(RFLU_ERR_ARG, "rflu_gpu_create: 2nd-order patch needs ORDER 2");
     for (int b = g->patchFaceOff[ip]; b < g->patchFaceOff[ip + 1]; ++b) {
@@ -1293,7 +1377,7 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   PUT(V.bnx, bnx, R); PUT(V.bny, bny, R); PUT(V.bnz, bnz, R); PUT(V.bnm, bnm, R);
   PUT(V.bd, bd, R);
   PUT(V.patchType, pType, int); PUT(V.patchOutflow, pOut, int); PUT(V.patchOrder, pOrder, int);
-  PUT(V.patchPout, pP, double);
+  PUT(V.patchK, pK, double);
   PUT(V.cfOff, cfOff, int); PUT(V.cfEnt, cfEnt, int);
   PUT(V.stOff, stOff, int); PUT(V.stIdx, stIdx, int);
   PUT(V.vol, vol, double); PUT(V.epsq, epsq, R);

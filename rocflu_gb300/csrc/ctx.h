@@ -47,6 +47,18 @@ struct Params {
 // floats per cell) = the 15 components in the order 3*var + dir and one pad;
 // flux = one float4 (mass and momentum) per face followed by the nT energy
 // fluxes.
+// Per-patch constants of the remaining boundary types, formed on the host
+// from the patch's values (pPatch%mixt%vals, uniform distribution) in the
+// reference's operation order (rflu_gpu_create, capi.cu: patchConstants), so that no trigonometric
+// function or constant power is evaluated per face:
+//   outflow         K[0] = p_out
+//   farfield        K[0] = M_inf, K[1..6] = (rho, p, q, u, v, w)_inf, K[7] = rho E_inf
+//   inflow TOTANG   K[0] = p_tot, K[1] = T_tot, K[2..5] = cos/sin(beta_h), cos/sin(beta_v),
+//                   K[6] = BCSWI_INFLOW_FIXED, K[7..12] = the supersonic state (rho, rho u, rho v,
+//                   rho w, rho E, p)
+//   inflow VELTEMP  K[0..3] = u, v, w, T, K[4] = p, K[5] = rho (not subsonic)
+//   injection       K[0] = mass flux, K[1] = T_inj
+constexpr int kPatchK = 16;
 constexpr int kTile = 256;
 // Shared-memory footprint of one staged tile of the mixed-mode gradient
 // kernel: 8 floats per record, the stencil ids as whole 16-byte words (plus
@@ -85,8 +97,8 @@ struct View {
   const int *bpatch;                // patch index
   const R *bnx, *bny, *bnz, *bnm;
   const R *bd;                      // (3, nb): fc - cofg(cell)
-  const int *patchType, *patchOutflow, *patchOrder;
-  const double *patchPout;
+  const int *patchType, *patchOutflow, *patchOrder;  // patchOutflow: the BCOPT type switch
+  const double *patchK;             // kPatchK constants per patch (physics.cuh)
   // cell -> faces CSR in reference summation order; entry e >= 0: interior
   // face (e >> 1) seen from side (e & 1); e < 0: boundary face -(e+1)
   const int *cfOff, *cfEnt;

@@ -83,6 +83,16 @@ __host__ __device__ inline Dual<N, T> sqrt_(const Dual<N, T> &a) {
   for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * h;
   return r;
 }
+// x ** y with y a constant of the gas model: d(x^y) = y x^(y-1) dx
+template <int N, typename T>
+__host__ __device__ inline Dual<N, T> powConstExp(const Dual<N, T> &a, const Dual<N, T> &y) {
+  Dual<N, T> r;
+  r.v = pow(a.v, y.v);
+  const T s = y.v * pow(a.v, y.v - T(1));
+#pragma unroll
+  for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * s;
+  return r;
+}
 template <int N, typename T>
 __host__ __device__ inline Dual<N, T> fabs_(const Dual<N, T> &a) {
   return (a.v < T(0)) ? -a : a;

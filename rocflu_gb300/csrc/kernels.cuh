@@ -1680,13 +1680,15 @@ __device__ inline void riemann1(const Params &P, const H *cl, const H *dvl, cons
   }
 }
 
-// First-order patch flux (RFLU_CentralFirstPatch, slip wall :785-911 and
-// outflow :571-784) from the cell's cv and p.  RFLU_CentralFirstPatch reads
-// cv as CellGradientsMP left it: in a 2nd-order run the momentum went
-// through the prim round trip and, in the PICL build, the energy slot holds
-// the pressure.
+// First-order patch flux (rocflu/RFLU_CentralFirstPatch.F90: inflow :228-570,
+// outflow :571-784, slip wall :785-911, no-slip walls :912-947, farfield
+// :948-1042, injection :1043-1127) from the cell's cv and p; K: the patch's
+// constants (physics.cuh: kPatchK).  RFLU_CentralFirstPatch reads cv as
+// CellGradientsMP left it: in a 2nd-order run the momentum went through the
+// prim round trip and, in the PICL build, the energy slot holds the
+// pressure.
 template <typename H>
-__device__ inline void patch1(const Params &P, int type, int outflowType, double pOut, const H *cvIn, H pl, H nx, H ny,
+__device__ inline void patch1(const Params &P, int type, int bcOpt, const double *K, const H *cvIn, H pl, H nx, H ny,
                               H nz, H nm, H *fd) {
   H cv[5];
 #pragma unroll
@@ -1704,37 +1706,65 @@ __device__ inline void patch1(const Params &P, int type, int outflowType, double
       cv[4] = cv[0] * perfEo(cv[0], g, pl, up, vp, wp);
     }
   }
-  if (type == 60) {
+  if (patchLeavesDensity(type)) {
     fd[0] = H(0);
     fd[1] = pl * nx * nm;
     fd[2] = pl * ny * nm;
     fd[3] = pl * nz * nm;
     fd[4] = pl * H(0) * nm;
-  } else {
-    outflowPatchFlux(outflowType, H(pOut), H(P.gvCp), H(P.gvMol), nx, ny, nz, nm, cv[0], cv[1], cv[2], cv[3], cv[4],
-                     pl, fd);
+    return;
   }
+  if (type == 20) {
+    outflowPatchFlux(bcOpt, H(K[0]), H(P.gvCp), H(P.gvMol), nx, ny, nz, nm, cv[0], cv[1], cv[2], cv[3], cv[4], pl,
+                     fd);
+    return;
+  }
+  const H cp = H(P.gvCp), rgas = H(8314.3) / H(P.gvMol);
+  const H g = cp / (cp - rgas);
+  if (type == 90) {
+    injectionPatchFlux(K, g, cp, rgas, nx, ny, nz, nm, cv[0], cv[1], cv[2], cv[3], pl, fd);
+    return;
+  }
+  H rr, rur, rvr, rwr, rer, pr;
+  if (type == 80) farfieldRindPerf(K, g, nx, ny, nz, cv[0], cv[1], cv[2], cv[3], cv[4], rr, rur, rvr, rwr, rer, pr);
+  else if (type == 10) inflowTotAngPerf(bcOpt, K, g, rgas, nx, ny, nz, cv[0], cv[1], cv[2], cv[3], rr, rur, rvr, rwr, rer, pr);
+  else inflowVelTempPerf(bcOpt, K, g, rgas, cv[0], rr, rur, rvr, rwr, rer, pr);
+  centralPatchFlux(nx, ny, nz, nm, cv[0], cv[1], cv[2], cv[3], cv[4], pl, rr, rur, rvr, rwr, rer, pr, fd);
 }
 
-// Second-order patch flux (RFLU_CentralSecondPatch, slip wall :858-1029,
-// outflow :634-857) from the reconstructed face state L.
+// Second-order patch flux (rocflu/RFLU_CentralSecondPatch.F90: inflow
+// :239-633, outflow :634-857, slip wall :858-1029, no-slip walls :1030-1087,
+// farfield :1088-1228, injection :1229-1343) from the reconstructed face
+// state L = (rho, u, v, w, p).
 template <typename S>
-__device__ inline void patch2(const Params &P, int type, int outflowType, double pOut, const S *L, S nx, S ny, S nz,
+__device__ inline void patch2(const Params &P, int type, int bcOpt, const double *K, const S *L, S nx, S ny, S nz,
                               S nm, S *flx) {
-  if (type == 60) {
+  if (patchLeavesDensity(type)) {
     flx[0] = S(0);
     flx[1] = L[4] * nx * nm;
     flx[2] = L[4] * ny * nm;
     flx[3] = L[4] * nz * nm;
     flx[4] = L[4] * S(0) * nm;
-  } else {
-    const S cp = prm<S>(P.gvCp, P.gvCpF), mol = prm<S>(P.gvMol, P.gvMolF);
-    S rgas = S(8314.3) / mol;
-    S g = cp / (cp - rgas);
-    S rul = L[0] * L[1], rvl = L[0] * L[2], rwl = L[0] * L[3];
-    S rel = L[0] * perfEo(L[0], g, L[4], L[1], L[2], L[3]);
-    outflowPatchFlux(outflowType, S(pOut), cp, mol, nx, ny, nz, nm, L[0], rul, rvl, rwl, rel, L[4], flx);
+    return;
   }
+  const S cp = prm<S>(P.gvCp, P.gvCpF), mol = prm<S>(P.gvMol, P.gvMolF);
+  S rgas = S(8314.3) / mol;
+  S g = cp / (cp - rgas);
+  S rul = L[0] * L[1], rvl = L[0] * L[2], rwl = L[0] * L[3];
+  if (type == 90) {
+    injectionPatchFlux(K, g, cp, rgas, nx, ny, nz, nm, L[0], rul, rvl, rwl, L[4], flx);
+    return;
+  }
+  S rel = L[0] * perfEo(L[0], g, L[4], L[1], L[2], L[3]);
+  if (type == 20) {
+    outflowPatchFlux(bcOpt, S(K[0]), cp, mol, nx, ny, nz, nm, L[0], rul, rvl, rwl, rel, L[4], flx);
+    return;
+  }
+  S rr, rur, rvr, rwr, rer, pr;
+  if (type == 80) farfieldRindPerf(K, g, nx, ny, nz, L[0], rul, rvl, rwl, rel, rr, rur, rvr, rwr, rer, pr);
+  else if (type == 10) inflowTotAngPerf(bcOpt, K, g, rgas, nx, ny, nz, L[0], rul, rvl, rwl, rr, rur, rvr, rwr, rer, pr);
+  else inflowVelTempPerf(bcOpt, K, g, rgas, L[0], rr, rur, rvr, rwr, rer, pr);
+  centralPatchFlux(nx, ny, nz, nm, L[0], rul, rvl, rwl, rel, L[4], rr, rur, rvr, rwr, rer, pr, flx);
 }
 
 template <typename To, typename From> __device__ inline To cvt(const From &x) { return To(x); }
@@ -1776,7 +1806,7 @@ __device__ inline void faceFluxEval(const View<R> &V, const L &ld, int t, typena
       H cv[5], fd[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) cv[k] = ld.cv(k, c);
-      patch1(P, type, V.patchOutflow[ip], V.patchPout[ip], cv, ld.dv(0, c), H((double)V.bnx[b]),
+      patch1(P, type, V.patchOutflow[ip], V.patchK + kPatchK * ip, cv, ld.dv(0, c), H((double)V.bnx[b]),
              H((double)V.bny[b]), H((double)V.bnz[b]), H((double)V.bnm[b]), fd);
 #pragma unroll
       for (int k = 0; k < 5; ++k) flx[k] = cvt<S>(fd[k]);
@@ -1784,8 +1814,8 @@ __device__ inline void faceFluxEval(const View<R> &V, const L &ld, int t, typena
       const size_t nb = V.nb;
       S Lf[5], irl;
       faceState(V, ld, c, S(V.bd[b]), S(V.bd[nb + b]), S(V.bd[2 * nb + b]), Lf, irl);
-      patch2(P, type, V.patchOutflow[ip], V.patchPout[ip], Lf, S(V.bnx[b]), S(V.bny[b]), S(V.bnz[b]), S(V.bnm[b]),
-             flx);
+      patch2(P, type, V.patchOutflow[ip], V.patchK + kPatchK * ip, Lf, S(V.bnx[b]), S(V.bny[b]), S(V.bnz[b]),
+             S(V.bnm[b]), flx);
     }
   }
 }
@@ -1841,7 +1871,7 @@ __device__ inline void gatherRhs(const View<R> &V, const T *flux, int i, T *rhs)
       }
     } else {
       const int b = -code - 1;
-      const int k0 = (V.patchType[V.bpatch[b]] == 60) ? 1 : 0;  // slip walls leave rhs(DENS)
+      const int k0 = patchLeavesDensity(V.patchType[V.bpatch[b]]) ? 1 : 0;  // walls leave rhs(DENS)
       T fl[5];
       loadFlux<R>(flux, nT, V.nf + b, fl);
 #pragma unroll

@@ -15,6 +15,10 @@ __host__ __device__ inline double fabs_(double x) { return fabs(x); }
 __host__ __device__ inline float fabs_(float x) { return fabsf(x); }
 __host__ __device__ inline double copysign_(double a, double b) { return copysign(a, b); }
 __host__ __device__ inline float copysign_(float a, float b) { return copysignf(a, b); }
+// x ** y where the exponent is a gas constant (g / (g - 1) and the like):
+// the dual-number overload differentiates in x only
+__host__ __device__ inline double powConstExp(double x, double y) { return pow(x, y); }
+__host__ __device__ inline float powConstExp(float x, float y) { return powf(x, y); }
 // Fortran MIN/MAX of two reals (first argument kept on ties)
 template <typename S> __host__ __device__ inline S fmin2(const S &a, const S &b) { return (b < a) ? b : a; }
 template <typename S> __host__ __device__ inline S fmax2(const S &a, const S &b) { return (b > a) ? b : a; }
@@ -204,15 +208,14 @@ __host__ __device__ inline void bcondOutflowPerf(int bcOpt, S pout, S sxn, S syn
   }
 }
 
-// Central patch flux on outflow faces (rocflu/RFLU_CentralFirstPatch.F90:
-// 571-784, RFLU_CentralSecondPatch.F90:634-857).
+// The central patch flux of the inflow, outflow and farfield cases of
+// rocflu/RFLU_CentralFirstPatch.F90 (:281-287, :571-784, :1001-1007) and
+// RFLU_CentralSecondPatch.F90: the average of the interior state l and the
+// boundary state r, static grid (fs = 0).
 template <typename S>
-__host__ __device__ inline void outflowPatchFlux(int bcOpt, S pOut, S cp, S mol, S nx, S ny, S nz, S nm, S rl, S rul,
-                                                 S rvl, S rwl, S rel, S pl, S *flx) {
+__host__ __device__ inline void centralPatchFlux(S nx, S ny, S nz, S nm, S rl, S rul, S rvl, S rwl, S rel, S pl, S rr,
+                                                 S rur, S rvr, S rwr, S rer, S pr, S *flx) {
   const S fs = S(0);
-  S pr = (bcOpt != 0) ? pOut : pl;
-  S rr, rur, rvr, rwr, rer;
-  bcondOutflowPerf(bcOpt, pr, nx, ny, nz, cp, mol, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr, rer);
   S ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
   S qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
   S h = S(0.5);
@@ -222,6 +225,189 @@ __host__ __device__ inline void outflowPatchFlux(int bcOpt, S pOut, S cp, S mol,
   flx[3] = h * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
   flx[4] = h * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
 }
+
+// Central patch flux on outflow faces (rocflu/RFLU_CentralFirstPatch.F90:
+// 571-784, RFLU_CentralSecondPatch.F90:634-857).
+template <typename S>
+__host__ __device__ inline void outflowPatchFlux(int bcOpt, S pOut, S cp, S mol, S nx, S ny, S nz, S nm, S rl, S rul,
+                                                 S rvl, S rwl, S rel, S pl, S *flx) {
+  S pr = (bcOpt != 0) ? pOut : pl;
+  S rr, rur, rvr, rwr, rer;
+  bcondOutflowPerf(bcOpt, pr, nx, ny, nz, cp, mol, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr, rer);
+  centralPatchFlux(nx, ny, nz, nm, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr, rer, pr, flx);
+}
+
+// The boundary types below read their patch's constants K (ctx.h: kPatchK),
+// formed on the host by rflu_gpu_create.
+
+// RFLU_SetRindStateFarfieldPerf without the vortex correction
+// (modflu/RFLU_ModRindStates.F90:248-420).
+template <typename S>
+__host__ __device__ inline void farfieldRindPerf(const double *K, S g, S nx, S ny, S nz, S rl, S rul, S rvl, S rwl,
+                                                 S rel, S &rr, S &rur, S &rvr, S &rwr, S &rer, S &pr) {
+  S ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+  S ql = ul * nx + vl * ny + wl * nz;
+  S el = rel / rl;
+  S sl2 = ul * ul + vl * vl + wl * wl;
+  S pl = (g - S(1)) * rl * (el - S(0.5) * sl2);  // MixtPerf_P_DEoGVm2
+  const S ri = S(K[1]), pi = S(K[2]), ui = S(K[4]), vi = S(K[5]), wi = S(K[6]);
+  if (K[0] < 1.0) {
+    S al = sqrt_(g * pl / rl);  // MixtPerf_C_DGP
+    S pb, rb, ub, vb, wb;
+    if (ql < S(0)) {
+      pb = S(0.5) * (pi + pl - rl * al * ((ui - ul) * nx + (vi - vl) * ny + (wi - wl) * nz));
+      rb = ri - (pi - pb) / (al * al);
+      ub = ui - nx * (pi - pb) / (rl * al);
+      vb = vi - ny * (pi - pb) / (rl * al);
+      wb = wi - nz * (pi - pb) / (rl * al);
+    } else {
+      pb = pi;
+      rb = rl - (pl - pi) / (al * al);
+      ub = ul + nx * (pl - pi) / (rl * al);
+      vb = vl + ny * (pl - pi) / (rl * al);
+      wb = wl + nz * (pl - pi) / (rl * al);
+    }
+    rr = rb;
+    rur = rb * ub;
+    rvr = rb * vb;
+    rwr = rb * wb;
+    rer = rb * perfEo(rb, g, pb, ub, vb, wb);
+    pr = pb;
+  } else if (ql < S(0)) {
+    rr = ri;
+    rur = ri * ui;
+    rvr = ri * vi;
+    rwr = ri * wi;
+    rer = S(K[7]);
+    pr = pi;
+  } else {
+    rr = rl; rur = rul; rvr = rvl; rwr = rwl; rer = rel; pr = pl;
+  }
+}
+
+// BcondInflowPerf (libfloflu/BcondInflowPerf.F90): the boundary state of an
+// inflow given by total pressure and temperature and flow angles.  A
+// subsonic-type patch whose face sees |q| >= c gets no state in the
+// reference (its outputs stay unset); here it gets NaN, which the validity
+// check reports.
+template <typename S>
+__host__ __device__ inline void inflowTotAngPerf(int bcOpt, const double *K, S g, S rgas, S nx, S ny, S nz, S rl,
+                                                 S rul, S rvl, S rwl, S &rr, S &rur, S &rvr, S &rwr, S &rer,
+                                                 S &pr) {
+  if (bcOpt == 1 || bcOpt == 2) {  // BCOPT_SUBSONIC, BCOPT_MIXED
+    const S ptot = S(K[0]), ttot = S(K[1]);
+    S gm1 = g - S(1);
+    S ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+    S a02 = g * rgas * ttot;                                           // MixtPerf_C2_GRT
+    S al = sqrt_(a02 - S(0.5) * (g - S(1)) * (ul * ul + vl * vl + wl * wl));  // MixtPerf_C_Co2GUVW
+    S ql = ul * nx + vl * ny + wl * nz;
+    if (fabs_(ql) < al) {
+      S sl = sqrt_(ul * ul + vl * vl + wl * wl);
+      S eta = S(-1);
+      if (K[6] == 0.0 && sl > S(1.0e-6)) eta = ql / sl;  // BCOPT_FIXED_NO, a well-defined angle
+      S Rm = al - S(0.5) * gm1 * ql;
+      S disc = S(0.5) * gm1 * (eta * eta) * (a02 / (Rm * Rm) * (S(1) + S(0.5) * gm1 * (eta * eta)) - S(1));
+      S ar, tr, sr;
+      if (disc < S(0)) {
+        ar = sqrt_(a02);
+        tr = ttot;
+        pr = ptot;
+        sr = S(0);
+      } else {
+        ar = Rm / (S(1) + S(0.5) * gm1 * eta * eta) * (S(1) + sqrt_(disc));
+        tr = ar * ar / (g * rgas);                              // MixtPerf_T_CGR
+        pr = ptot * powConstExp(tr / ttot, g / (g - S(1)));     // MixtPerf_P_GPoTTo
+        S c2 = ar * ar;                                          // MixtPerf_Vm_C2Co2G
+        sr = (a02 > c2) ? sqrt_(S(2) / (g - S(1)) * (a02 - c2)) : S(0);
+      }
+      rr = pr / (rgas * tr);  // MixtPerf_D_PRT
+      S ur = sr * S(K[2]) * S(K[4]);
+      S vr = sr * S(K[3]);
+      S wr = sr * S(K[2]) * S(K[5]);
+      rer = rr * (pr / (rr * (g - S(1))) + S(0.5) * sr * sr);  // MixtPerf_Eo_DGPVm
+      rur = rr * ur;
+      rvr = rr * vr;
+      rwr = rr * wr;
+      return;
+    }
+    if (bcOpt == 1) {
+      rr = rur = rvr = rwr = rer = pr = S(nan(""));
+      return;
+    }
+  }
+  rr = S(K[7]); rur = S(K[8]); rvr = S(K[9]); rwr = S(K[10]); rer = S(K[11]); pr = S(K[12]);
+}
+
+// The inflow state given by velocity and temperature (RFLU_CentralFirstPatch.
+// F90:375-570): prescribed pressure unless subsonic, else the interior
+// density.
+template <typename S>
+__host__ __device__ inline void inflowVelTempPerf(int bcOpt, const double *K, S g, S rgas, S rl, S &rr, S &rur,
+                                                  S &rvr, S &rwr, S &rer, S &pr) {
+  const S ur = S(K[0]), vr = S(K[1]), wr = S(K[2]), tr = S(K[3]);
+  if (bcOpt != 1) {  // not BCOPT_SUBSONIC: rr = MixtPerf_D_PRT(pr, rgas, tr), formed on the host
+    pr = S(K[4]);
+    rr = S(K[5]);
+  } else {
+    rr = rl;
+    pr = rr * rgas * tr;  // MixtPerf_P_DRT
+  }
+  rer = rr * perfEo(rr, g, pr, ur, vr, wr);
+  rur = rr * ur;
+  rvr = rr * vr;
+  rwr = rr * wr;
+}
+
+// RFLU_SetRindStateSlipWallPerf (modflu/RFLU_ModRindStates.F90:535-584):
+// the wall pressure of a non-burning injection face, static grid.
+template <typename S>
+__host__ __device__ inline S slipWallRindPerf(S g, S nx, S ny, S nz, S rl, S rul, S rvl, S rwl, S pl) {
+  const S fs = S(0);
+  S irl = S(1) / rl;
+  S ul = irl * rul, vl = irl * rvl, wl = irl * rwl;
+  S ql = ul * nx + vl * ny + wl * nz - fs;
+  S al = sqrt_(g * pl / rl);
+  if (ql < S(0)) {
+    S term = S(1) + S(0.5) * (g - S(1)) * ql / al;
+    return pl * powConstExp(term, S(2) * g / (g - S(1)));
+  }
+  S term = (g + S(1)) / S(4);
+  return pl + term * rl * ql * (ql + sqrt_(al * al + term * term * ql * ql) / term);
+}
+
+// Injection patch flux (RFLU_CentralFirstPatch.F90:1043-1127,
+// RFLU_CentralSecondPatch.F90:1229-1343): a burning face (mass flux > 0)
+// injects gas at T_inj through RFLU_SetRindStateInjectPerf
+// (RFLU_ModRindStates.F90:459-501); a non-burning one is a wall with the
+// slip-wall rind pressure.  All five components enter rhs.
+template <typename S>
+__host__ __device__ inline void injectionPatchFlux(const double *K, S g, S cp, S rgas, S nx, S ny, S nz, S nm, S rl,
+                                                   S rul, S rvl, S rwl, S pl, S *flx) {
+  const S fs = S(0);
+  if (K[0] > 0.0) {
+    const S minj = S(K[0]), tinj = S(K[1]);
+    S rb = pl / (rgas * tinj);  // MixtPerf_D_PRT
+    S qb = -minj / rb + fs;
+    S ub = qb * nx, vb = qb * ny, wb = qb * nz;
+    S hb = perfHo(cp, tinj, ub, vb, wb);
+    flx[0] = -minj * nm;
+    flx[1] = (-minj * ub + pl * nx) * nm;
+    flx[2] = (-minj * vb + pl * ny) * nm;
+    flx[3] = (-minj * wb + pl * nz) * nm;
+    flx[4] = (-minj * hb + pl * fs) * nm;
+  } else {
+    S pw = slipWallRindPerf(g, nx, ny, nz, rl, rul, rvl, rwl, pl);
+    flx[0] = S(0);
+    flx[1] = pw * nx * nm;
+    flx[2] = pw * ny * nm;
+    flx[3] = pw * nz * nm;
+    flx[4] = pw * fs * nm;
+  }
+}
+
+// Walls (slip, no-slip) leave rhs(DENS) as it is; every other patch adds
+// all five components (ConvectiveFluxes' patch loop).
+__host__ __device__ inline bool patchLeavesDensity(int type) { return type == 60 || type == 70 || type == 71; }
 
 // Cyclic Jacobi eigen-decomposition of a symmetric 3x3 (RFLU_SymmetricEigen3,
 // modflu/RFLU_ModLimiters.F90:791-912): ascending eigenvalues, eigenvectors

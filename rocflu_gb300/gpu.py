@@ -42,7 +42,23 @@ class GridDesc(C.Structure):
                 ("patchBcType", C.POINTER(C.c_int)), ("patchOutflowType", C.POINTER(C.c_int)),
                 ("patchPout", C.POINTER(C.c_double)), ("patchOrder", C.POINTER(C.c_int)),
                 ("c2csOff", C.POINTER(C.c_int)), ("c2csMembs", C.POINTER(C.c_int)),
-                ("xyzMoms", C.POINTER(C.c_double))]
+                ("xyzMoms", C.POINTER(C.c_double)), ("patchVals", C.POINTER(C.c_double)),
+                ("patchSwitches", C.POINTER(C.c_int))]
+
+BCDAT_N, BCSWI_N = 8, 2
+
+
+def patch_values(case):
+    """(nPatches, BCDAT_N) boundary values and (nPatches, BCSWI_N) switches of
+    the case's patches (Patch.vals / Patch.switches, zero-padded)."""
+    np_ = max(len(case.patches), 1)
+    vals = np.zeros((np_, BCDAT_N), np.float64)
+    sw = np.zeros((np_, BCSWI_N), np.int32)
+    for i, p in enumerate(case.patches):
+        v, w = tuple(getattr(p, "vals", ()) or ()), tuple(getattr(p, "switches", ()) or ())
+        vals[i, :len(v)] = v
+        sw[i, :len(w)] = w
+    return vals, sw
 
 
 class NumDesc(C.Structure):
@@ -223,6 +239,7 @@ class Region:
         po = np.array([p.outflow_type for p in case.patches], np.int32)
         pp = np.array([p.p_out for p in case.patches], np.float64)
         pr = np.array([p.order for p in case.patches], np.int32)
+        pv, psw = patch_values(case)
         arrs = dict(
             f2c=np.ascontiguousarray(grid.f2c, np.int32), fn=np.ascontiguousarray(grid.fn, np.float64),
             fc=np.ascontiguousarray(grid.fc, np.float64), vol=np.ascontiguousarray(grid.vol, np.float64),
@@ -231,12 +248,13 @@ class Region:
             bfc=np.ascontiguousarray(grid.bfc, np.float64), pt=pt, po=po, pp=pp, pr=pr,
             soff=np.ascontiguousarray(grid.c2cs_off, np.int32),
             smem=np.ascontiguousarray(grid.c2cs if len(grid.c2cs) else np.zeros(1), np.int32),
-            moms=np.ascontiguousarray(grid.moms, np.float64))
+            moms=np.ascontiguousarray(grid.moms, np.float64), pv=pv, psw=psw)
         a = arrs
         gd = GridDesc(nc, int(a["f2c"].shape[0]), _p(a["f2c"], C.c_int), _p(a["fn"]), _p(a["fc"]), _p(a["vol"]),
                       _p(a["cofg"]), len(case.patches), _p(a["off"], C.c_int), _p(a["bf2c"], C.c_int), _p(a["bfn"]),
                       _p(a["bfc"]), _p(a["pt"], C.c_int), _p(a["po"], C.c_int), _p(a["pp"]), _p(a["pr"], C.c_int),
-                      _p(a["soff"], C.c_int), _p(a["smem"], C.c_int), _p(a["moms"]))
+                      _p(a["soff"], C.c_int), _p(a["smem"], C.c_int), _p(a["moms"]), _p(a["pv"]),
+                      _p(a["psw"], C.c_int))
         self.nd = num_desc(case.num, precision, options)
         h = C.c_void_p()
         _check(L.rflu_gpu_create(C.byref(gd), C.byref(self.nd), C.byref(h)))
