@@ -329,24 +329,67 @@ def numerics_from_deck(deck):
 
 def patch_kinds_from_bc(bc_deck, n_patches, order_default=1):
     """Boundary conditions per patch from a .bc file's sections (read_deck of
-    its text): BC_SLIPW (slip wall) and BC_OUTFLOW (TYPE 0 supersonic, 1
-    subsonic at PRESS, 2 mixed), each over PATCH lo hi (1-based), ORDER 2 or
-    the boundary-face order; other conditions raise ValueError."""
+    its text), as modflu/RFLU_ModReadBcInputFile.F90 reads them: BC_SLIPW;
+    BC_OUTFLOW (TYPE 0 supersonic, 1 subsonic at PRESS, 2 mixed);
+    BC_NOSLIP / BC_NOSLIP_HFLUX and BC_NOSLIP_TEMP; BC_FARF (MACH, ATTACK and
+    SLIP in degrees, PRESS, TEMP, CORR); BC_INFLOW / BC_INFLOW_TOTANG (TYPE,
+    FIXED, PTOT, TTOT, BETAH and BETAV in degrees, MACH unless subsonic);
+    BC_INFLOW_VELTEMP (TYPE, VELX, VELY, VELZ, TEMP, PRESS unless subsonic);
+    BC_INJECT (MFRATE, TEMP); each over PATCH lo hi (1-based), ORDER 2 or the
+    boundary-face order.  Angles are converted with the reference's
+    global%deg2rad (libflu/RFLU_InitGlobal.F90:331-333).  Other conditions
+    raise ValueError."""
+    import math
+
     from . import cases
 
+    deg2rad = 1.0 / (180.0 / (4.0 * math.atan(1.0)))
+
+    def f(s, key, default=None):
+        if key in s:
+            return float(s[key])
+        if default is None:
+            raise ValueError("bc: %s is required" % key)
+        return default
+
+    def kind_of(sec, s):
+        if sec == "BC_SLIPW":
+            return {"bc_type": cases.BC_SLIPWALL}
+        if sec == "BC_OUTFLOW":
+            return {"bc_type": cases.BC_OUTFLOW, "outflow_type": int(f(s, "TYPE", 0)), "p_out": f(s, "PRESS", 0.0)}
+        if sec in ("BC_NOSLIP", "BC_NOSLIP_HFLUX"):
+            return {"bc_type": cases.BC_NOSLIPWALL_HFLUX}
+        if sec == "BC_NOSLIP_TEMP":
+            return {"bc_type": cases.BC_NOSLIPWALL_TEMP}
+        if sec == "BC_FARF":
+            return {"bc_type": cases.BC_FARFIELD, "switches": (int(f(s, "CORR", 0)), 0),
+                    "vals": (f(s, "MACH"), f(s, "ATTACK") * deg2rad, f(s, "SLIP") * deg2rad, f(s, "PRESS"),
+                             f(s, "TEMP"))}
+        if sec in ("BC_INFLOW", "BC_INFLOW_TOTANG"):
+            t = int(f(s, "TYPE"))
+            mach = f(s, "MACH") if t != cases.BCOPT_SUBSONIC else 0.0
+            return {"bc_type": cases.BC_INFLOW_TOTANG, "switches": (t, int(f(s, "FIXED", 0))),
+                    "vals": (f(s, "PTOT"), f(s, "TTOT"), f(s, "BETAH") * deg2rad, f(s, "BETAV") * deg2rad, mach)}
+        if sec == "BC_INFLOW_VELTEMP":
+            t = int(f(s, "TYPE"))
+            press = f(s, "PRESS") if t != cases.BCOPT_SUBSONIC else 0.0
+            return {"bc_type": cases.BC_INFLOW_VELTEMP, "switches": (t, 0),
+                    "vals": (f(s, "VELX"), f(s, "VELY"), f(s, "VELZ"), f(s, "TEMP"), press)}
+        if sec == "BC_INJECT":
+            return {"bc_type": cases.BC_INJECTION, "vals": (f(s, "MFRATE"), f(s, "TEMP"))}
+        return None
+
+    known = ("BC_SLIPW", "BC_OUTFLOW", "BC_NOSLIP", "BC_NOSLIP_HFLUX", "BC_NOSLIP_TEMP", "BC_FARF", "BC_INFLOW",
+             "BC_INFLOW_TOTANG", "BC_INFLOW_VELTEMP", "BC_INJECT")
     kinds = [None] * n_patches
-    for sec, kind in (("BC_SLIPW", "slip"), ("BC_OUTFLOW", "outflow")):
+    for sec in known:
         for s in bc_deck.get(sec + "*", []):
             lo, hi = (int(float(v)) for v in s["PATCH"].split()[:2])
-            order = 2 if int(float(s.get("ORDER", order_default))) == 2 else 1
-            if kind == "slip":
-                k = {"bc_type": cases.BC_SLIPWALL, "order": order}
-            else:
-                k = {"bc_type": cases.BC_OUTFLOW, "outflow_type": int(float(s.get("TYPE", 0))),
-                     "p_out": float(s.get("PRESS", 0.0)), "order": order}
+            k = kind_of(sec, s)
+            k["order"] = 2 if int(float(s.get("ORDER", order_default))) == 2 else 1
             for p in range(lo, hi + 1):
                 kinds[p - 1] = k
-    others = [k for k in bc_deck if k.startswith("BC_") and not k.endswith("*") and k not in ("BC_SLIPW", "BC_OUTFLOW")]
+    others = [k for k in bc_deck if k.startswith("BC_") and not k.endswith("*") and k not in known]
     if others or any(k is None for k in kinds):
-        raise ValueError("bc: only slip walls and outflow patches are on this path (%s)" % ", ".join(others))
+        raise ValueError("bc: conditions not on this path (%s)" % ", ".join(others))
     return kinds

@@ -142,3 +142,62 @@ ORDER      2
         refio.numerics_from_deck(refio.apply_overrides(deck, {"NUMERICS/CRECONSTC": 1}))
     with pytest.raises(ValueError):
         refio.patch_kinds_from_bc(refio.read_deck("# BC_PERIODIC\nPATCH 1 6\n#\n"), 6)
+
+
+def test_bc_sections_of_the_open_patches():
+    """Inflow, farfield, injection and no-slip sections in the .bc syntax of
+    modflu/RFLU_ModReadBcInputFile.F90: keys to BCDAT / BCSWI order, angles
+    in degrees converted with the reference's deg2rad, MACH and PRESS only
+    read for a non-subsonic inflow."""
+    import math
+
+    bc = refio.read_deck("""
+# BC_INFLOW_VELTEMP
+PATCH       1 1
+TYPE        1   ! subsonic: PRESS not needed
+TEMP        348.29
+VELX        138.92
+VELY        0.0
+VELZ        0.0
+ORDER       2
+#
+# BC_FARF
+PATCH      2 2
+MACH       0.5
+ATTACK     90.0
+SLIP       0.0
+PRESS      1.0E+05
+TEMP       300.0
+#
+# BC_INFLOW
+PATCH      3 3
+TYPE       0
+PTOT       2.0E+05
+TTOT       400.0
+BETAH      30.0
+BETAV      0.0
+MACH       1.5
+#
+# BC_INJECT
+PATCH      4 4
+MFRATE     2.0
+TEMP       2500.0
+#
+# BC_NOSLIP
+PATCH      5 5
+#
+# BC_NOSLIP_TEMP
+PATCH      6 6
+TEMP       300.0
+#
+# END
+""")
+    k = refio.patch_kinds_from_bc(bc, 6)
+    assert k[0] == {"bc_type": cases.BC_INFLOW_VELTEMP, "switches": (1, 0), "vals": (138.92, 0.0, 0.0, 348.29, 0.0),
+                    "order": 2}
+    assert k[1]["bc_type"] == cases.BC_FARFIELD and k[1]["switches"] == (0, 0)
+    assert abs(k[1]["vals"][1] - math.pi / 2) <= 1e-15 and k[1]["vals"][3:] == (1.0e5, 300.0)
+    assert k[2]["bc_type"] == cases.BC_INFLOW_TOTANG and k[2]["switches"] == (0, 0)
+    assert abs(k[2]["vals"][2] - math.pi / 6) <= 1e-15 and k[2]["vals"][4] == 1.5
+    assert k[3] == {"bc_type": cases.BC_INJECTION, "vals": (2.0, 2500.0), "order": 1}
+    assert k[4]["bc_type"] == cases.BC_NOSLIPWALL_HFLUX and k[5]["bc_type"] == cases.BC_NOSLIPWALL_TEMP
