@@ -31,7 +31,8 @@ MODULE RFLU_ModGPU
                                RFLU_BC_NOSLIPWALL_HFLUX = 70, &
                                RFLU_BC_NOSLIPWALL_TEMP = 71, &
                                RFLU_BC_FARFIELD = 80, &
-                               RFLU_BC_INJECTION = 90
+                               RFLU_BC_INJECTION = 90, &
+                               RFLU_BC_PERIODIC = 110
   INTEGER(C_INT), PARAMETER :: RFLU_BCDAT_N = 8, &
                                RFLU_BCSWI_N = 2
   INTEGER(C_INT), PARAMETER :: RFLU_OPT_UNTILED = 1
@@ -58,6 +59,8 @@ MODULE RFLU_ModGPU
     TYPE(C_PTR) :: xyzMoms
     TYPE(C_PTR) :: patchVals
     TYPE(C_PTR) :: patchSwitches
+    TYPE(C_PTR) :: fc2
+    TYPE(C_PTR) :: c2csShift
   END TYPE rflu_grid_desc
 
   TYPE, BIND(C) :: rflu_num_desc
@@ -75,6 +78,8 @@ MODULE RFLU_ModGPU
     REAL(C_DOUBLE) :: dtImposed
     REAL(C_DOUBLE) :: dtMinLimit
     INTEGER(C_INT) :: options
+    INTEGER(C_INT) :: cReconstCells
+    REAL(C_DOUBLE) :: cReconstCellsWeight
   END TYPE rflu_num_desc
 
   TYPE, BIND(C) :: rflu_status
@@ -96,6 +101,8 @@ MODULE RFLU_ModGPU
     INTEGER(C_INT) :: nPatches
     TYPE(C_PTR) :: patchFaceOff
     TYPE(C_PTR) :: bf2v
+    TYPE(C_PTR) :: patchBcType
+    TYPE(C_PTR) :: patchRelated
   END TYPE rflu_mesh_desc
 
   INTERFACE
@@ -330,6 +337,13 @@ MODULE RFLU_ModGPU
       IMPORT :: C_INT, C_PTR
       TYPE(C_PTR), VALUE :: setup
     END FUNCTION rflu_setup_destroy
+
+    INTEGER(C_INT) FUNCTION rflu_setup_bface_stencil(grid, off, faces) BIND(C, NAME='rflu_setup_bface_stencil')
+      IMPORT :: C_INT, C_PTR, rflu_grid_desc
+      TYPE(rflu_grid_desc), INTENT(IN) :: grid
+      INTEGER(C_INT) :: off(*)
+      TYPE(C_PTR), VALUE :: faces
+    END FUNCTION rflu_setup_bface_stencil
 
   END INTERFACE
 

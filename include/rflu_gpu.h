@@ -49,6 +49,7 @@ extern "C" {
 #define RFLU_BC_NOSLIPWALL_TEMP 71
 #define RFLU_BC_FARFIELD 80
 #define RFLU_BC_INJECTION 90
+#define RFLU_BC_PERIODIC 110      /* translational pairs: no boundary faces left (rflu_setup_build identifies them) */
 /* Per-patch boundary values and switches (pPatch%mixt%vals(:,0) and
  * pPatch%mixt%switches, modfloflu/ModParameters.F90:452-511), uniform over
  * the patch: RFLU_BCDAT_N values and RFLU_BCSWI_N switches per patch, in
@@ -89,6 +90,12 @@ typedef struct {
   /* inflow, farfield and injection patches (may be NULL when there are none) */
   const double *patchVals;  /* (RFLU_BCDAT_N, nPatches) */
   const int *patchSwitches; /* (RFLU_BCSWI_N, nPatches) */
+  /* translational periodic meshes (may be NULL: none): the centroid of each
+   * face in its second cell's frame (= fc off the periods) and the
+   * translation of each stencil member's image (0 off the periods), so that
+   * a member's offset is cofg(member) - cofg(cell) + c2csShift */
+  const double *fc2;        /* (3,nFaces) */
+  const double *c2csShift;  /* (3,c2csOff[nCells]) */
 } rflu_grid_desc;
 
 /* Numerics, the reference input deck keys (libfloflu/ReadNumericsSection.F90,
@@ -106,6 +113,8 @@ typedef struct {
   double cfl, epsEntr, dissFact; /* CFL, ENTROPY, DISSFACT */
   double dtImposed, dtMinLimit;  /* TIMESTEP, DTMINLIMIT */
   int options;      /* RFLU_OPT_* bits of the device layout (no deck key; 0 = default) */
+  int cReconstCells;          /* CRECONSTC: 0 none, 1 gradients constrained at wall and injection faces */
+  double cReconstCellsWeight; /* CRECONSTCW: weight of the constraint rows (the reference's default is 1) */
 } rflu_num_desc;
 
 /* rflu_num_desc::options */
@@ -318,6 +327,11 @@ typedef struct {
   int nPatches;
   const int *patchFaceOff;          /* nPatches+1 */
   const int *bf2v;                  /* (4,nBFaces), 1-based, 0 in slot 4 for triangles */
+  /* translational periodic patch pairs (may be NULL: none): the patches'
+   * RFLU_BC_* types and the 0-based related patch of each BC_PERIODIC (110)
+   * patch (RELPATCH), -1 otherwise */
+  const int *patchBcType;
+  const int *patchRelated;
 } rflu_mesh_desc;
 
 typedef struct rflu_setup rflu_setup;
@@ -329,6 +343,12 @@ int rflu_setup_build(const rflu_mesh_desc *mesh, int spaceOrder, rflu_setup **se
  * caller's to set. */
 int rflu_setup_grid(rflu_setup *setup, rflu_grid_desc *grid);
 int rflu_setup_destroy(rflu_setup *setup);
+/* The boundary-face stencil of CRECONSTC 1 (RFLU_AddBFaces + RFLU_SortBFaces,
+ * modflu/RFLU_ModStencilsUtils.F90:134-298,1501-1585, at most 9 faces per
+ * cell) of a grid description (its stencils, boundary faces and patch
+ * types): off (nCells+1) and faces (off[nCells] entries, 0-based boundary
+ * face index, patch after patch, nearest first); faces may be NULL. */
+int rflu_setup_bface_stencil(const rflu_grid_desc *grid, int *off, int *faces);
 
 #ifdef __cplusplus
 }

@@ -195,6 +195,8 @@ struct orc_ctx {
   std::vector<Patch> patches;
   std::vector<int> stOff, stIdx;
   std::vector<double> moms;
+  /* CRECONSTC 1: the boundary-face stencil (global boundary face index) */
+  std::vector<int> bfOff, bfIdx;
   std::vector<double> epsq;     /* unused cache slot kept empty: Venkat recomputes vol**(1/3) per face */
   /* numerics */
   orc_num_desc num;
@@ -1101,6 +1103,170 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
 /* CellGradientsMP (libfloflu/CellGradientsMP.F90:160-295).  Works on c->cv  */
 /* in place, as the reference does (cons -> prim -> cons round trip).        */
 /* ------------------------------------------------------------------------ */
+/* ------------------------------------------------------------------------ */
+/* Constrained gradients (CRECONSTC 1).                                      */
+/* The boundary-face stencil: RFLU_AddBFaces (modflu/RFLU_ModStencilsUtils.  */
+/* F90:134-298) visits the cell and its stencil members in stencil order and */
+/* for each the wall and injection patches in order, taking the cell's face  */
+/* on the patch (the patch's face list keyed through a sorted copy of bf2c:  */
+/* for a cell with several faces on one patch the last one), at most 18;    */
+/* RFLU_SortBFaces (:1501-1585) orders them by squared distance to the      */
+/* centroid with QuickSortRFREALInteger; RFLU_BuildC2CStencil keeps 9       */
+/* (RFLU_SetInfoC2CStencil, modflu/RFLU_ModStencilsCells.F90:2816-2909).   */
+/* ------------------------------------------------------------------------ */
+bool wallOrInjection(int t) {
+  return t == ORC_BC_NOSLIPWALL_HFLUX || t == ORC_BC_NOSLIPWALL_TEMP || t == ORC_BC_SLIPWALL || t == ORC_BC_INJECTION;
+}
+
+void buildBFaceStencil(orc_ctx *c) {
+  const int nc = c->nCells, np = (int)c->patches.size();
+  std::vector<int> off(np + 1, 0);
+  for (int ip = 0; ip < np; ++ip) off[ip + 1] = off[ip] + c->patches[ip].n;
+  std::vector<std::vector<int>> last(np);
+  for (int ip = 0; ip < np; ++ip) {
+    const Patch &p = c->patches[ip];
+    if (!wallOrInjection(p.bcType) || p.n == 0) continue;
+    last[ip].assign(nc, -1);
+    for (int ifl = 0; ifl < p.n; ++ifl) last[ip][p.bf2c[ifl]] = ifl;
+  }
+  c->bfOff.assign(nc + 1, 0);
+  c->bfIdx.clear();
+  for (int icg = 0; icg < nc; ++icg) {
+    int memb[18][2];
+    int n = 0;
+    bool done = false;
+    for (int isl = 0; isl <= c->stOff[icg + 1] - c->stOff[icg] && !done; ++isl) {
+      const int isg = (isl == 0) ? icg : c->stIdx[c->stOff[icg] + isl - 1];
+      for (int ip = 0; ip < np && !done; ++ip) {
+        if (last[ip].empty() || last[ip][isg] < 0) continue;
+        if (n < 18) {
+          memb[n][0] = ip;
+          memb[n][1] = last[ip][isg];
+          ++n;
+        } else {
+          done = true;
+        }
+      }
+    }
+    std::vector<double> dist(n);
+    std::vector<int> key(n);
+    const double *x = &c->cofg[3 * icg];
+    for (int isl = 0; isl < n; ++isl) {
+      const double *f = &c->patches[memb[isl][0]].fc[3 * memb[isl][1]];
+      key[isl] = isl;
+      dist[isl] = (f[0] - x[0]) * (f[0] - x[0]) + (f[1] - x[1]) * (f[1] - x[1]) + (f[2] - x[2]) * (f[2] - x[2]);
+    }
+    if (n > 0) QuickSortRFREALInteger(dist.data(), key.data(), n);
+    for (int isl = 0; isl < std::min(n, 9); ++isl) c->bfIdx.push_back(off[memb[key[isl]][0]] + memb[key[isl]][1]);
+    c->bfOff[icg + 1] = (int)c->bfIdx.size();
+  }
+}
+
+/* FloatEqual (modfloflu/ModTools.F90:129-148). */
+bool floatEqual(double a, double b, double tol) { return std::fabs(a - b) <= (1.0 + 0.5 * std::fabs(a + b)) * tol; }
+
+/* RFLU_GetConstrType (modflu/RFLU_ModConstraintUtils.F90:122-334), TCPERF,
+ * the primitive variables (rho, u, v, w, p). */
+bool constrDirichlet(const Patch &p, int ifl, int iv) {
+  const double *n = &p.fn[4 * ifl];
+  switch (iv) {
+  case 0: return p.bcType == ORC_BC_INJECTION && p.vals[0] > 0.0;
+  case 1: case 2: case 3:
+    if (p.bcType == ORC_BC_NOSLIPWALL_HFLUX || p.bcType == ORC_BC_NOSLIPWALL_TEMP) return true;
+    if (p.bcType == ORC_BC_SLIPWALL || p.bcType == ORC_BC_INJECTION)
+      return floatEqual(std::fabs(n[iv - 1]), 1.0, 1.0e-6);
+    return false;
+  default: return false;
+  }
+}
+
+/* RFLU_GetConstrValue (:366-745), TCPERF, static grid (fs = fsu = 0). */
+double constrValue(const orc_ctx *c, const Patch &p, int ifl, int iv) {
+  if (p.bcType != ORC_BC_INJECTION) return 0.0;
+  const double *n = &p.fn[4 * ifl];
+  const double minj = p.vals[0];
+  if (!(minj > 0.0)) return 0.0 * n[iv - 1]; /* fsu*nx */
+  /* RFLU_SetRindStateInjectPerf from the face cell's pressure */
+  const double pl = c->dv[3 * p.bf2c[ifl]];
+  const double rGas = MixtPerf_R_M(c->gvMol);
+  const double rl = pl / (rGas * p.vals[1]);
+  if (iv == 0) return rl;
+  const double ql = -minj / rl + 0.0;
+  return ql * n[iv - 1];
+}
+
+/* RFLU_ComputeGradCellsConstr (modflu/RFLU_ModDifferentiationCells.F90:
+ * 1180-1563), 3-D: for each cell with boundary-face members and each
+ * variable some of them constrain, the least-squares fit to the stencil
+ * differences (rows d/|d|) and to the constraint values (rows cwt d/|d|
+ * from the centroid to the face centroid), gx = gx + term*aInv(1,row)*dVar
+ * row by row.  aInv: the pseudo-inverse of the row matrix; the reference
+ * takes it from LAPACK dgesdd (after scaling the columns), here from the
+ * normal equations, (A^T A)^-1 A^T with the inverse by cofactors: the same
+ * matrix for the full-rank systems the reference accepts, to rounding. */
+void constrainedGradCells(orc_ctx *c, const std::vector<double> &var, std::vector<double> &grad) {
+  const int nc = c->nCells, np = (int)c->patches.size();
+  std::vector<int> patchOf, faceOf;
+  for (int ip = 0; ip < np; ++ip)
+    for (int ifl = 0; ifl < c->patches[ip].n; ++ifl) { patchOf.push_back(ip); faceOf.push_back(ifl); }
+  const double cwt = c->num.cReconstCellsWeight;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int icg = 0; icg < nc; ++icg) {
+    if (c->bfOff[icg + 1] == c->bfOff[icg]) continue;
+    const double *x = &c->cofg[3 * icg];
+    const int nm = c->stOff[icg + 1] - c->stOff[icg];
+    for (int iv = 0; iv < 5; ++iv) {
+      std::vector<int> rowB;
+      for (int e = c->bfOff[icg]; e < c->bfOff[icg + 1]; ++e) {
+        const int b = c->bfIdx[e];
+        if (constrDirichlet(c->patches[patchOf[b]], faceOf[b], iv)) rowB.push_back(b);
+      }
+      if (rowB.empty()) continue;
+      const int nr = nm + (int)rowB.size();
+      std::vector<double> a(3 * (size_t)nr), term(nr), dVar(nr);
+      for (int r = 0; r < nr; ++r) {
+        double dx, dy, dz, t;
+        if (r < nm) {
+          const int j = c->stIdx[c->stOff[icg] + r];
+          dx = c->cofg[3 * j] - x[0]; dy = c->cofg[3 * j + 1] - x[1]; dz = c->cofg[3 * j + 2] - x[2];
+          t = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+          dVar[r] = var[5 * j + iv] - var[5 * icg + iv];
+        } else {
+          const Patch &p = c->patches[patchOf[rowB[r - nm]]];
+          const int ifl = faceOf[rowB[r - nm]];
+          dx = p.fc[3 * ifl] - x[0]; dy = p.fc[3 * ifl + 1] - x[1]; dz = p.fc[3 * ifl + 2] - x[2];
+          t = cwt / std::sqrt(dx * dx + dy * dy + dz * dz);
+          dVar[r] = constrValue(c, p, ifl, iv) - var[5 * icg + iv];
+        }
+        term[r] = t;
+        a[3 * r] = t * dx; a[3 * r + 1] = t * dy; a[3 * r + 2] = t * dz;
+      }
+      double m00 = 0, m01 = 0, m02 = 0, m11 = 0, m12 = 0, m22 = 0;
+      for (int r = 0; r < nr; ++r) {
+        m00 = m00 + a[3 * r] * a[3 * r]; m01 = m01 + a[3 * r] * a[3 * r + 1]; m02 = m02 + a[3 * r] * a[3 * r + 2];
+        m11 = m11 + a[3 * r + 1] * a[3 * r + 1]; m12 = m12 + a[3 * r + 1] * a[3 * r + 2];
+        m22 = m22 + a[3 * r + 2] * a[3 * r + 2];
+      }
+      const double c00 = m11 * m22 - m12 * m12, c01 = m02 * m12 - m01 * m22, c02 = m01 * m12 - m02 * m11;
+      const double c11 = m00 * m22 - m02 * m02, c12 = m01 * m02 - m00 * m12, c22 = m00 * m11 - m01 * m01;
+      const double id = 1.0 / (m00 * c00 + m01 * c01 + m02 * c02);
+      const double i00 = id * c00, i01 = id * c01, i02 = id * c02, i11 = id * c11, i12 = id * c12, i22 = id * c22;
+      double gx = 0.0, gy = 0.0, gz = 0.0;
+      for (int r = 0; r < nr; ++r) {
+        const double a0 = a[3 * r], a1 = a[3 * r + 1], a2 = a[3 * r + 2];
+        const double w0 = term[r] * (i00 * a0 + i01 * a1 + i02 * a2);
+        const double w1 = term[r] * (i01 * a0 + i11 * a1 + i12 * a2);
+        const double w2 = term[r] * (i02 * a0 + i12 * a1 + i22 * a2);
+        gx = gx + w0 * dVar[r];
+        gy = gy + w1 * dVar[r];
+        gz = gz + w2 * dVar[r];
+      }
+      double *g = &grad[15 * icg + 3 * iv];
+      g[0] = gx; g[1] = gy; g[2] = gz;
+    }
+  }
+}
+
 void cellGradients(orc_ctx *c) {
   if (c->num.spaceOrder <= 1) return;
   const int nc = c->nCells;
@@ -1115,6 +1281,7 @@ void cellGradients(orc_ctx *c) {
     cv[4] = c->dv[3 * ic];
   }
   computeGradCells(c, c->cv, c->grad);
+  if (c->num.cReconstCells == 1) constrainedGradCells(c, c->cv, c->grad);
   switch (c->num.reconst) {
   case 0: break;
   case 1:
@@ -1930,6 +2097,7 @@ orc_ctx *orc_create(const orc_mesh_desc *m, const orc_num_desc *num) {
   } else {
     c->stOff.assign(c->nCells + 1, 0);
   }
+  buildBFaceStencil(c);
   /* RFLU_DerivedInputValues (libflu/RFLU_DerivedInputValues.F90:309-410) */
   for (int k = 0; k < 5; ++k) c->ark[k] = c->grk[k] = 0.0;
   if (num->rkScheme == 1) {
@@ -1960,6 +2128,10 @@ void orc_destroy(orc_ctx *c) { delete c; }
 int orc_nfaces(orc_ctx *c) { return c->nFaces; }
 int orc_patch_nfaces(orc_ctx *c, int ip) { return c->patches[ip].n; }
 int orc_stencil_nnz(orc_ctx *c) { return c->stOff[c->nCells]; }
+void orc_get_bface_stencil(orc_ctx *c, int *off, int *faces) {
+  if (off) std::memcpy(off, c->bfOff.data(), sizeof(int) * (c->nCells + 1));
+  if (faces && !c->bfIdx.empty()) std::memcpy(faces, c->bfIdx.data(), sizeof(int) * c->bfIdx.size());
+}
 int orc_nstages(orc_ctx *c) { return c->nrkSteps; }
 
 void orc_get_faces(orc_ctx *c, int *f2c, int *f2v, double *fn, double *fc) {

@@ -78,6 +78,8 @@ typedef struct {
   double cp, gamma;
   double cfl, epsEntr, dissFact;
   double dtImposed, dtMinLimit;
+  int cReconstCells;          /* CRECONSTC: 1 constrains gradients at wall and injection faces */
+  double cReconstCellsWeight; /* CRECONSTCW */
 } orc_num_desc;
 
 typedef struct orc_ctx orc_ctx;
@@ -93,6 +95,11 @@ void orc_get_faces(orc_ctx *c, int *f2c, int *f2v, double *fn, double *fc);
 void orc_get_cells(orc_ctx *c, double *vol, double *cofg);
 void orc_get_patch(orc_ctx *c, int iPatch, int *bf2c, double *fn, double *fc);
 void orc_get_stencil(orc_ctx *c, int *off, int *idx, double *moms);
+/* CRECONSTC 1: the boundary-face stencil, off (nCells+1) and faces
+ * (0-based boundary face index, patch after patch, nearest first); faces
+ * may be NULL.  Built whatever CRECONSTC is (the reference always builds
+ * it). */
+void orc_get_bface_stencil(orc_ctx *c, int *off, int *faces);
 /* Periodic meshes: fc2(3,nFaces) each face's centroid in its second cell's
  * frame (= fc off the periods) and stShift(3,nnz) the translation of each
  * stencil member's image (0 off the periods); either may be NULL. */

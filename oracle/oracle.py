@@ -29,7 +29,8 @@ class NumDesc(C.Structure):
                 ("rkScheme", C.c_int), ("piclBuild", C.c_int),
                 ("cp", C.c_double), ("gamma", C.c_double), ("cfl", C.c_double),
                 ("epsEntr", C.c_double), ("dissFact", C.c_double),
-                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double)]
+                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double),
+                ("cReconstCells", C.c_int), ("cReconstCellsWeight", C.c_double)]
 
 
 def build():
@@ -73,6 +74,7 @@ def lib():
         L.orc_get_cells.argtypes = [P, DP, DP]
         L.orc_get_patch.argtypes = [P, C.c_int, IP, DP, DP]
         L.orc_get_stencil.argtypes = [P, IP, IP, DP]
+        L.orc_get_bface_stencil.argtypes = [P, IP, IP]
         L.orc_get_periodic.argtypes = [P, DP, DP]
         L.orc_get_periodic.restype = None
         L.orc_set_state.argtypes = [P, DP]
@@ -94,7 +96,8 @@ def lib():
         L.orc_set_threads.restype = None
         L.orc_threads.argtypes = []
         L.orc_threads.restype = C.c_int
-        for name in ("orc_get_faces", "orc_get_cells", "orc_get_patch", "orc_get_stencil", "orc_set_state",
+        for name in ("orc_get_faces", "orc_get_cells", "orc_get_patch", "orc_get_stencil", "orc_get_bface_stencil",
+                     "orc_set_state",
                      "orc_get_state", "orc_get_rhs", "orc_get_grad", "orc_residual", "orc_counters",
                      "orc_rk_stage", "orc_run_fixed_dt", "orc_destroy"):
             getattr(L, name).restype = None
@@ -140,7 +143,8 @@ def _mesh_arrays(case):
 
 def num_desc(num):
     return NumDesc(num.space_order, num.space_discr, num.reconst, num.rk_scheme, num.picl_build,
-                   num.cp, num.gamma, num.cfl, num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit)
+                   num.cp, num.gamma, num.cfl, num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit,
+                   int(getattr(num, "c_reconst", 0)), float(getattr(num, "c_reconst_weight", 1.0)))
 
 
 class Oracle:
@@ -208,6 +212,15 @@ class Oracle:
         moms = np.zeros((self.n_cells, 10))
         lib().orc_get_stencil(self.h, _ptr(off, C.c_int), _ptr(idx, C.c_int), _ptr(moms, C.c_double))
         return off, idx[:nnz], moms
+
+    def bface_stencil(self):
+        """CRECONSTC 1's boundary-face stencil: (off, faces), 0-based boundary
+        face indices, patch after patch, nearest first."""
+        off = np.zeros(self.n_cells + 1, np.int32)
+        lib().orc_get_bface_stencil(self.h, _ptr(off, C.c_int), None)
+        faces = np.zeros(max(int(off[-1]), 1), np.int32)
+        lib().orc_get_bface_stencil(self.h, _ptr(off, C.c_int), _ptr(faces, C.c_int))
+        return off, faces[:int(off[-1])]
 
     # state
     def set_state(self, cv):

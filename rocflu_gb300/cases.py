@@ -63,6 +63,8 @@ class Numerics:
     diss_fact: float = 1.0
     dt_imposed: float = 1.0e-5
     dt_min_limit: float = 1.0e-10
+    c_reconst: int = 0            # CRECONSTC: 1 constrains gradients at wall and injection faces
+    c_reconst_weight: float = 1.0  # CRECONSTCW
 
 
 @dataclass

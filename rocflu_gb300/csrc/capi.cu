@@ -19,6 +19,7 @@
 #include "../../include/rflu_gpu.h"
 #include "args.h"
 #include "convert.cuh"
+#include "constr.h"
 #include "ctx.h"
 #include "errors.h"
 #include "ops.h"
@@ -281,6 +282,7 @@ struct Ctx : CtxBase {
   const Ops<R> *ops = nullptr;
   std::vector<void *> allocs;
   double *staging = nullptr;     // (15, nc) doubles: transfers in reference order
+  bool periodicMesh = false;     // the grid came with periodic images (fc2 / c2csShift)
   double *work = nullptr;        // adjoint workspace (allocated by the first adjoint call)
   int tsWidthLazy = 0;           // ... and the width of its transposed-stencil weights
   size_t workBytes = 0;
@@ -588,6 +590,8 @@ struct Ctx : CtxBase {
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
     if (V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through WENO smoothing (RECONST 1, 2)");
+    if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through constrained gradients (CRECONSTC 1)");
+    if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint on a periodic mesh");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -602,6 +606,8 @@ struct Ctx : CtxBase {
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
     if (V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through WENO smoothing (RECONST 1, 2)");
+    if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through constrained gradients (CRECONSTC 1)");
+    if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent on a periodic mesh");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -627,6 +633,10 @@ struct Ctx : CtxBase {
     invalidate();
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
+    if (cvBar && periodicMesh)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient on a periodic mesh");
+    if (cvBar && V.cSlot)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through constrained gradients (CRECONSTC 1)");
     if (cvBar && (V.p.reconst == 1 || V.p.reconst == 2))
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through the WENO smoothing (RECONST 1, 2)");
     View<R> W;
@@ -836,6 +846,9 @@ struct Ctx : CtxBase {
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
     if (V.p.reconst == 1 || V.p.reconst == 2)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: the WENO smoothing (RECONST 1, 2) has no adjoint");
+    if (V.cSlot)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: constrained gradients (CRECONSTC 1) have no adjoint");
+    if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint on a periodic mesh");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     if (int rc0 = ensureAdjoint()) return rc0;
     // the whole forward and reverse sweep runs on the scratch state X
@@ -1023,6 +1036,11 @@ int Ctx<R>::patchConstants(const rflu_grid_desc *g, int ip, const rflu_num_desc 
     case RFLU_BC_SLIPWALL:
     case RFLU_BC_NOSLIPWALL_HFLUX:
     case RFLU_BC_NOSLIPWALL_TEMP:
+      return RFLU_OK;
+    case RFLU_BC_PERIODIC:  // its faces are interior faces of the identified mesh (fc2, c2csShift)
+      if (g->patchFaceOff[ip + 1] != g->patchFaceOff[ip])
+        return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: a periodic patch must hold no boundary faces (its faces are "
+                                          "interior faces of the identified mesh, rflu_setup_build)");
       return RFLU_OK;
     case RFLU_BC_OUTFLOW:
       K[0] = g->patchPout[ip];
@@ -1223,11 +1241,13 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     fc1[s] = newId[o1];
     fc2[s] = newId[o2];
     const double *fn = g->fn + 4 * (size_t)f, *fcp = g->fc + 3 * (size_t)f;
+    // a periodic mesh's second side sees the face centroid in its own frame
+    const double *fcq = g->fc2 ? g->fc2 + 3 * (size_t)f : fcp;
     fnx[s] = fn[0]; fny[s] = fn[1]; fnz[s] = fn[2]; fnm[s] = fn[3];
     for (int d = 0; d < 3; ++d) {
       // dx = xc - pGrid%cofg(XCOORD,c1), as the 2nd-order flux routines form it
       dL[(size_t)d * nf + s] = fcp[d] - g->cofg[3 * (size_t)o1 + d];
-      dR[(size_t)d * nf + s] = fcp[d] - g->cofg[3 * (size_t)o2 + d];
+      dR[(size_t)d * nf + s] = fcq[d] - g->cofg[3 * (size_t)o2 + d];
     }
   }
   // ---- boundary faces --------------------------------------------------------
@@ -1280,6 +1300,8 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   // unit offset, in FP64 and in the reference's order of operations
   std::vector<int> stOff(nc + 1, 0), stIdx;
   std::vector<double> wx, wy, wz, epsq(nc, 0.0), lsq;
+  std::vector<float> stShift;  // mixed mode on a periodic mesh: the members' translations
+  periodicMesh = g->c2csShift != nullptr || g->fc2 != nullptr;
   const bool mixed = num->precision == RFLU_PREC_MIXED;
   if (mixed && num->spaceOrder > 1) lsq.resize(6 * (size_t)nc);
   if (num->spaceOrder > 1) {
@@ -1308,6 +1330,11 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
         if (j < 0 || j >= nc) return fail(RFLU_ERR_ARG, "rflu_gpu_create: stencil member out of range");
         double dx = g->cofg[3 * (size_t)j] - xi[0], dy = g->cofg[3 * (size_t)j + 1] - xi[1],
                dz = g->cofg[3 * (size_t)j + 2] - xi[2];
+        if (g->c2csShift) {  // the member's periodic image
+          const double *sh = g->c2csShift + 3 * (size_t)e;
+          dx = dx + sh[0]; dy = dy + sh[1]; dz = dz + sh[2];
+          if (mixed) { stShift.push_back((float)sh[0]); stShift.push_back((float)sh[1]); stShift.push_back((float)sh[2]); }
+        }
         const double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
         dx = term * dx; dy = term * dy; dz = term * dz;
         const double t1 = c1111 * (dx);
@@ -1386,7 +1413,10 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     // weights formed in the gradient kernel from the R factor and centroids
     PUT(V.cgx, cgx, R); PUT(V.cgy, cgy, R); PUT(V.cgz, cgz, R);
     PUT(V.lsq, lsq, R); PUT(V.ivol, ivol, R);
-    if (num->spaceOrder > 1 && !(num->options & RFLU_OPT_UNTILED)) {
+    if (!stShift.empty()) PUT(V.stShift, stShift, float);
+    // the tile plan stages records with their own centroids; a periodic
+    // mesh's members need their images' (the gather kernel adds stShift)
+    if (num->spaceOrder > 1 && !(num->options & RFLU_OPT_UNTILED) && stShift.empty()) {
       if ((rc = buildTiles(cfOff, cfEnt, stOff, stIdx, fc1, fc2, fnx, fny, fnz, fnm, dL, dR, bnx, bny, bnz, bnm, bd)))
         return rc;
     }
@@ -1402,6 +1432,33 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   }
   // transposed stencil (adjoint of the LSQ gradient, every mode)
   PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
+  // constrained gradients (CRECONSTC 1): the plan in the reference's cell
+  // numbering (constr.h), moved to the renumbered cells; the stencil rows
+  // keep the reference's member order, which the device's stencil keeps too
+  if (num->cReconstCells == 1 && num->spaceOrder > 1 && g->c2csShift)
+    return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: constrained gradients (CRECONSTC 1) on a periodic mesh");
+  if (num->cReconstCells == 1 && num->spaceOrder > 1) {
+    std::vector<int> stOffRef(g->c2csOff, g->c2csOff + nc + 1), stIdxRef(g->c2csOff[nc]);
+    for (int e = 0; e < g->c2csOff[nc]; ++e) stIdxRef[e] = g->c2csMembs[e] - 1;
+    std::vector<int> bf2cRef(nb);
+    for (int b = 0; b < nb; ++b) bf2cRef[b] = g->bf2c[b] - 1;
+    std::vector<double> minj(std::max(np, 1), 0.0);
+    for (int ip = 0; ip < np; ++ip)
+      if (pType[ip] == RFLU_BC_INJECTION) minj[ip] = pK[(size_t)kPatchK * ip];
+    ConstrInput in{nc, g->cofg, stOffRef.data(), stIdxRef.data(), np, g->patchFaceOff, pType.data(), minj.data(),
+                   bf2cRef.data(), g->bfn, g->bfc, num->cReconstCellsWeight};
+    ConstrPlan plan;
+    int bad = -1;
+    if (planConstrained(in, plan, &bad) != 0)
+      return fail(RFLU_ERR_ARG, "rflu_gpu_create: the constrained gradient matrix of cell " + std::to_string(bad + 1) +
+                                    " is singular (RFLU_ComputeGradCellsConstr stops there)");
+    std::vector<int> slot(nc, -1);
+    for (size_t k = 0; k < plan.cells.size(); ++k) slot[newId[plan.cells[k]]] = (int)k;
+    std::vector<R> w(plan.w.begin(), plan.w.end());
+    if (plan.cells.empty()) plan.rowFace.push_back(-1);
+    PUT(V.cSlot, slot, int); PUT(V.cNcon, plan.nCon, int); PUT(V.cRowOff, plan.rowOff, int);
+    PUT(V.cRowFace, plan.rowFace, int); PUT(V.cW, w, R);
+  }
 #undef PUT
   if ((rc = alloc(&V.cv, 5 * (size_t)nc))) return rc;
   if ((rc = alloc(&V.dv, 3 * (size_t)nc))) return rc;
@@ -1488,6 +1545,10 @@ int rflu_gpu_create(const rflu_grid_desc *grid, const rflu_num_desc *num, rflu_g
   if (num->rkScheme < 1 || num->rkScheme > 3) return fail(RFLU_ERR_ARG, "rflu_gpu_create: RKSCHEME must be 1, 2 or 3");
   if (num->precision < 0 || num->precision > 2) return fail(RFLU_ERR_ARG, "rflu_gpu_create: bad precision");
   if (num->options & ~RFLU_OPT_UNTILED) return fail(RFLU_ERR_ARG, "rflu_gpu_create: unknown option bits");
+  if (num->cReconstCells != 0 && num->cReconstCells != 1)
+    return fail(RFLU_ERR_ARG, "rflu_gpu_create: CRECONSTC must be 0 or 1");
+  if (num->cReconstCells == 1 && !(num->cReconstCellsWeight >= 0.0))
+    return fail(RFLU_ERR_ARG, "rflu_gpu_create: CRECONSTCW must be >= 0");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(RFLU_ERR_CUDA, "rflu_gpu_create: no CUDA device");
   rflu_gpu_ctx *c = new (std::nothrow) rflu_gpu_ctx();

@@ -99,6 +99,15 @@ struct View {
   const R *bd;                      // (3, nb): fc - cofg(cell)
   const int *patchType, *patchOutflow, *patchOrder;  // patchOutflow: the BCOPT type switch
   const double *patchK;             // kPatchK constants per patch (physics.cuh)
+  // constrained gradients (CRECONSTC 1, constr.h): per cell its slot or -1
+  // (null: none), per slot the constraint-row counts of the five variables
+  // and its first row, per row three weights and the boundary face of a
+  // constraint row (-1: a stencil member's row)
+  const int *cSlot, *cNcon, *cRowOff, *cRowFace;
+  const R *cW;
+  // mixed mode on a periodic mesh (untiled): each stencil member's
+  // translation to its image, added to the centroid difference (null: none)
+  const float *stShift;
   // cell -> faces CSR in reference summation order; entry e >= 0: interior
   // face (e >> 1) seen from side (e & 1); e < 0: boundary face -(e+1)
   const int *cfOff, *cfEnt;

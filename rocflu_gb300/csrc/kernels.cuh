@@ -367,6 +367,61 @@ __global__ void kInitFromRef(View<R> V, const double *ref, int o0, int o1) {
 }
 
 // ---------------------------------------------------------------------------
+// Constraint value of primitive variable k at boundary face b
+// (RFLU_GetConstrValue, modflu/RFLU_ModConstraintUtils.F90:366-745, TCPERF,
+// static grid): 0 for the velocity at walls; at an injection face, fsu * n
+// (fsu = 0) when it does not burn, else the density and velocity of
+// RFLU_SetRindStateInjectPerf (modflu/RFLU_ModRindStates.F90:459-501) from
+// the face cell's pressure.
+template <typename S, typename R>
+__device__ inline S constrValue(const View<R> &V, int b, int k) {
+  const int ip = V.bpatch[b];
+  if (V.patchType[ip] != 90) return S(0);
+  const double *K = V.patchK + kPatchK * ip;
+  const S n = (k == 1) ? S(V.bnx[b]) : (k == 2) ? S(V.bny[b]) : S(V.bnz[b]);
+  if (!(K[0] > 0.0)) return S(0) * n;
+  const S rgas = S(8314.3) / S(V.p.gvMol);
+  const S rl = S(V.dv[V.bcell[b]]) / (rgas * S(K[1]));  // MixtPerf_D_PRT(pl, rGas, tInj)
+  if (k == 0) return rl;
+  const S ql = -S(K[0]) / rl + S(0);
+  return ql * n;
+}
+
+// The constrained gradients of cell i (slot sl) for CRECONSTC 1
+// (RFLU_ComputeGradCellsConstr, modflu/RFLU_ModDifferentiationCells.F90:
+// 1180-1563): every variable some face of the cell's boundary-face stencil
+// constrains gets the fit to its stencil differences and constraint values
+// through the planned weights (constr.h), rows in the reference's order;
+// the others keep their least-squares gradient.
+template <typename R, typename L>
+__device__ inline void constrainedGrad(const View<R> &V, const L &ld, int i, int sl, const typename L::S *q,
+                                       typename L::S *g) {
+  using S = typename L::S;
+  int r = V.cRowOff[sl];
+  const int sb = V.stOff[i], se = V.stOff[i + 1];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int nCon = V.cNcon[5 * sl + k];
+    if (nCon == 0) continue;
+    S gx = S(0), gy = S(0), gz = S(0);
+    for (int s = sb; s < se; ++s, ++r) {
+      const S d = ld.prim(k, V.stIdx[s]) - q[k];
+      gx = gx + S(V.cW[3 * (size_t)r]) * d;
+      gy = gy + S(V.cW[3 * (size_t)r + 1]) * d;
+      gz = gz + S(V.cW[3 * (size_t)r + 2]) * d;
+    }
+    for (int c = 0; c < nCon; ++c, ++r) {
+      const S d = constrValue<S>(V, V.cRowFace[r], k) - q[k];
+      gx = gx + S(V.cW[3 * (size_t)r]) * d;
+      gy = gy + S(V.cW[3 * (size_t)r + 1]) * d;
+      gz = gz + S(V.cW[3 * (size_t)r + 2]) * d;
+    }
+    g[3 * k] = gx;
+    g[3 * k + 1] = gy;
+    g[3 * k + 2] = gz;
+  }
+}
+
 // Gradient + limiter of one cell.
 // LSQ gradient: RFLU_ComputeGradCellsFast_3D (modflu/RFLU_ModDifferentiationCells.F90:
 // 931-1178) with the per-member weights precomputed at set-up.
@@ -396,6 +451,10 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
         g[3 * k + 1] = g[3 * k + 1] + wy * d;
         g[3 * k + 2] = g[3 * k + 2] + wz * d;
       }
+    }
+    if (V.cSlot) {
+      const int sl = V.cSlot[i];
+      if (sl >= 0) constrainedGrad(V, ld, i, sl, q, g);
     }
   } else {
     // mixed mode (the tangent kernels): G = L sum_j (q_j - q_i) d_j/|d_j|^2,
@@ -788,7 +847,12 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
       for (int s = sb; s < se; ++s) {
         float r[8];
         ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
-        const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+        float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+        if (V.stShift) {  // a periodic mesh: the member's image
+          dx = dx + V.stShift[3 * (size_t)s];
+          dy = dy + V.stShift[3 * (size_t)s + 1];
+          dz = dz + V.stShift[3 * (size_t)s + 2];
+        }
         const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
         const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
 #pragma unroll
@@ -820,6 +884,10 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
       g[3 * k] = lxx * x + lxy * y + lxz * z;
       g[3 * k + 1] = lxy * x + lyy * y + lyz * z;
       g[3 * k + 2] = lxz * x + lyz * y + lzz * z;
+    }
+    if (V.cSlot) {  // constrained cells (CRECONSTC 1) read their members from global memory
+      const int sl = V.cSlot[i];
+      if (sl >= 0) constrainedGrad(V, PlainLoad<float>{V}, i, sl, q, g);
     }
   }
   const bool velo = lim && rc == 10;

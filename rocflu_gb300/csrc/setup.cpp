@@ -10,7 +10,10 @@
 // (cell, local face) slot gets a vertex key, slots are bucketed by smallest
 // vertex and sorted, and a matched pair's face id is the rank of its lower
 // slot -- the same order, built without a hash table and in parallel.
+#include "constr.h"
 #include <algorithm>
+#include <map>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -95,9 +98,43 @@ void sortFractions(double *a, int *b, int n) {
 }
 
 // Singular-value ratio test of RFLU_InvertMatrixSVD (libflu/
-// RFLU_InvertMatrixSVD.F90): the eigenvalues of the 4x4 normal matrix
-// A^T A (cyclic Jacobi) give the singular values of the column-scaled
-// stencil matrix; returns how many count as zero.
+// RFLU_InvertMatrixSVD.F90) on the n x n normal matrix g = A^T A of a
+// column-scaled matrix A (n <= 4): its eigenvalues (cyclic Jacobi) are the
+// squared singular values; returns how many count as zero.
+int normalSingularCount(double g[4][4], int n) {
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = 0; q < n; ++q) (p == q ? tot : off) += g[p][q] * g[p][q];
+    if (off <= 1e-30 * tot) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        if (g[p][q] == 0.0) continue;
+        double th = (g[q][q] - g[p][p]) / (2.0 * g[p][q]);
+        double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {
+          double gkp = g[k][p], gkq = g[k][q];
+          g[k][p] = c * gkp - s * gkq;
+          g[k][q] = s * gkp + c * gkq;
+        }
+        for (int k = 0; k < n; ++k) {
+          double gpk = g[p][k], gqk = g[q][k];
+          g[p][k] = c * gpk - s * gqk;
+          g[q][k] = s * gpk + c * gqk;
+        }
+      }
+  }
+  double sv[4];
+  for (int p = 0; p < n; ++p) sv[p] = std::sqrt(std::max(g[p][p], 0.0));
+  std::sort(sv, sv + n, [](double x, double y) { return x > y; });
+  int count = (sv[0] > 100.0 * 2.220446049250313e-16) ? 0 : 1;
+  for (int i = 1; i < n; ++i)
+    if (!(sv[i] > 0.01 * sv[i - 1])) { count += n - i; break; }
+  return count;
+}
+
+// The same for a rows x 4 stencil matrix A (row-major).
 int singularCount(const std::vector<double> &A, int rows) {
   double g[4][4] = {};
   for (int p = 0; p < 4; ++p)
@@ -106,39 +143,154 @@ int singularCount(const std::vector<double> &A, int rows) {
       for (int r = 0; r < rows; ++r) s += A[r * 4 + p] * A[r * 4 + q];
       g[p][q] = g[q][p] = s;
     }
-  for (int sweep = 0; sweep < 64; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int p = 0; p < 4; ++p)
-      for (int q = 0; q < 4; ++q) (p == q ? tot : off) += g[p][q] * g[p][q];
-    if (off <= 1e-30 * tot) break;
-    for (int p = 0; p < 3; ++p)
-      for (int q = p + 1; q < 4; ++q) {
-        if (g[p][q] == 0.0) continue;
-        double th = (g[q][q] - g[p][p]) / (2.0 * g[p][q]);
-        double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
-        double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < 4; ++k) {
-          double gkp = g[k][p], gkq = g[k][q];
-          g[k][p] = c * gkp - s * gkq;
-          g[k][q] = s * gkp + c * gkq;
-        }
-        for (int k = 0; k < 4; ++k) {
-          double gpk = g[p][k], gqk = g[q][k];
-          g[p][k] = c * gpk - s * gqk;
-          g[q][k] = s * gpk + c * gqk;
-        }
-      }
-  }
-  double sv[4];
-  for (int p = 0; p < 4; ++p) sv[p] = std::sqrt(std::max(g[p][p], 0.0));
-  std::sort(sv, sv + 4, [](double x, double y) { return x > y; });
-  int count = (sv[0] > 100.0 * 2.220446049250313e-16) ? 0 : 1;
-  for (int i = 1; i < 4; ++i)
-    if (!(sv[i] > 0.01 * sv[i - 1])) { count += 4 - i; break; }
-  return count;
+  return normalSingularCount(g, 4);
 }
 
 }  // namespace
+
+namespace rflu {
+
+namespace {
+// FloatEqual (modfloflu/ModTools.F90:129-148)
+bool floatEqual(double a, double b, double tol) { return std::fabs(a - b) <= (1.0 + 0.5 * std::fabs(a + b)) * tol; }
+
+bool isWallOrInjection(int t) { return t == 70 || t == 71 || t == 60 || t == 90; }
+
+// RFLU_GetConstrType for a TCPERF gas and the variables (rho, u, v, w, p):
+// whether boundary face b of a patch of type t constrains variable k.
+bool dirichlet(int t, double minj, const double *n, int k) {
+  if (k == 0) return t == 90 && minj > 0.0;
+  if (k == 4) return false;
+  if (t == 70 || t == 71) return true;
+  if (t == 60 || t == 90) return floatEqual(std::fabs(n[k - 1]), 1.0, 1.0e-6);
+  return false;
+}
+}  // namespace
+
+int planConstrained(const ConstrInput &in, ConstrPlan &P, int *bad, bool withWeights) {
+  const int nc = in.nCells;
+  const int maxTemp = 18, maxMembs = 9;
+  // per wall/injection patch: each cell's face on it (the last one when a
+  // cell has several: RFLU_AddBFaces keys its sorted copy of bf2c face by
+  // face, so equal cells end up with the last face's key)
+  std::vector<std::vector<int>> faceOf(in.nPatches);
+  for (int ip = 0; ip < in.nPatches; ++ip) {
+    if (!isWallOrInjection(in.patchType[ip]) || in.patchFaceOff[ip + 1] == in.patchFaceOff[ip]) continue;
+    faceOf[ip].assign(nc, -1);
+    for (int b = in.patchFaceOff[ip]; b < in.patchFaceOff[ip + 1]; ++b) faceOf[ip][in.bf2c[b]] = b;
+  }
+  P.bfOff.assign(nc + 1, 0);
+  P.bfIdx.clear();
+  std::vector<int> found;
+  std::vector<double> dist;
+  std::vector<int> key;
+  for (int ic = 0; ic < nc; ++ic) {
+    found.clear();
+    bool full = false;
+    for (int m = -1; m < in.stOff[ic + 1] - in.stOff[ic] && !full; ++m) {
+      const int cell = (m < 0) ? ic : in.stIdx[in.stOff[ic] + m];
+      for (int ip = 0; ip < in.nPatches; ++ip) {
+        if (faceOf[ip].empty()) continue;
+        const int b = faceOf[ip][cell];
+        if (b < 0) continue;
+        if ((int)found.size() >= maxTemp) {
+          full = true;
+          break;
+        }
+        found.push_back(b);
+      }
+    }
+    const int n = (int)found.size();
+    dist.resize(n);
+    key.resize(n);
+    const double *x = &in.cofg[3 * (size_t)ic];
+    for (int k = 0; k < n; ++k) {
+      const double *f = &in.bfc[3 * (size_t)found[k]];
+      const double dx = f[0] - x[0], dy = f[1] - x[1], dz = f[2] - x[2];
+      dist[k] = dx * dx + dy * dy + dz * dz;
+      key[k] = k;
+    }
+    sortFractions(dist.data(), key.data(), n);
+    for (int k = 0; k < std::min(n, maxMembs); ++k) P.bfIdx.push_back(found[key[k]]);
+    P.bfOff[ic + 1] = (int)P.bfIdx.size();
+  }
+  if (!withWeights) return 0;
+  // patch of each boundary face
+  std::vector<int> patchOf(in.patchFaceOff[in.nPatches]);
+  for (int ip = 0; ip < in.nPatches; ++ip)
+    for (int b = in.patchFaceOff[ip]; b < in.patchFaceOff[ip + 1]; ++b) patchOf[b] = ip;
+  P.cells.clear(); P.nCon.clear(); P.rowOff.clear(); P.w.clear(); P.rowFace.clear();
+  std::vector<double> A;
+  std::vector<double> term;
+  std::vector<int> rowB;
+  for (int ic = 0; ic < nc; ++ic) {
+    if (P.bfOff[ic + 1] == P.bfOff[ic]) continue;
+    const double *x = &in.cofg[3 * (size_t)ic];
+    P.cells.push_back(ic);
+    P.rowOff.push_back((int)P.rowFace.size());
+    for (int k = 0; k < 5; ++k) {
+      rowB.clear();
+      for (int e = P.bfOff[ic]; e < P.bfOff[ic + 1]; ++e) {
+        const int b = P.bfIdx[e], ip = patchOf[b];
+        if (dirichlet(in.patchType[ip], in.patchMinj[ip], &in.bfn[4 * (size_t)b], k)) rowB.push_back(b);
+      }
+      P.nCon.push_back((int)rowB.size());
+      if (rowB.empty()) continue;
+      const int nm = in.stOff[ic + 1] - in.stOff[ic], nr = nm + (int)rowB.size();
+      A.assign(3 * (size_t)nr, 0.0);
+      term.assign(nr, 0.0);
+      for (int r = 0; r < nr; ++r) {
+        const double *y = (r < nm) ? &in.cofg[3 * (size_t)in.stIdx[in.stOff[ic] + r]] : &in.bfc[3 * (size_t)rowB[r - nm]];
+        const double dx = y[0] - x[0], dy = y[1] - x[1], dz = y[2] - x[2];
+        const double t = ((r < nm) ? 1.0 : in.cwt) / std::sqrt(dx * dx + dy * dy + dz * dz);
+        term[r] = t;
+        A[3 * r] = t * dx; A[3 * r + 1] = t * dy; A[3 * r + 2] = t * dz;
+      }
+      // pinv(A) = (A^T A)^-1 A^T, the inverse by cofactors
+      double m00 = 0, m01 = 0, m02 = 0, m11 = 0, m12 = 0, m22 = 0;
+      for (int r = 0; r < nr; ++r) {
+        const double a0 = A[3 * r], a1 = A[3 * r + 1], a2 = A[3 * r + 2];
+        m00 = m00 + a0 * a0; m01 = m01 + a0 * a1; m02 = m02 + a0 * a2;
+        m11 = m11 + a1 * a1; m12 = m12 + a1 * a2; m22 = m22 + a2 * a2;
+      }
+      const double c00 = m11 * m22 - m12 * m12, c01 = m02 * m12 - m01 * m22, c02 = m01 * m12 - m02 * m11;
+      const double c11 = m00 * m22 - m02 * m02, c12 = m01 * m02 - m00 * m12, c22 = m00 * m11 - m01 * m01;
+      const double det = m00 * c00 + m01 * c01 + m02 * c02;
+      // the singular-value test of RFLU_InvertMatrixSVD on the matrix with
+      // its columns scaled by their largest magnitude, as the reference
+      // scales it before the decomposition
+      {
+        double cm[3] = {0.0, 0.0, 0.0};
+        for (int r = 0; r < nr; ++r)
+          for (int c = 0; c < 3; ++c) cm[c] = std::max(cm[c], std::fabs(A[3 * r + c]));
+        double g[4][4] = {};
+        const double m[3][3] = {{m00, m01, m02}, {m01, m11, m12}, {m02, m12, m22}};
+        for (int p = 0; p < 3; ++p)
+          for (int q = 0; q < 3; ++q) g[p][q] = m[p][q] / (cm[p] * cm[q]);
+        if (normalSingularCount(g, 3) != 0 || !(det != 0.0)) {
+          if (bad) *bad = ic;
+          return -1;
+        }
+      }
+      const double id = 1.0 / det;
+      const double i00 = id * c00, i01 = id * c01, i02 = id * c02, i11 = id * c11, i12 = id * c12, i22 = id * c22;
+      for (int r = 0; r < nr; ++r) {
+        const double a0 = A[3 * r], a1 = A[3 * r + 1], a2 = A[3 * r + 2];
+        const double p0 = i00 * a0 + i01 * a1 + i02 * a2;
+        const double p1 = i01 * a0 + i11 * a1 + i12 * a2;
+        const double p2 = i02 * a0 + i12 * a1 + i22 * a2;
+        P.w.push_back(term[r] * p0);
+        P.w.push_back(term[r] * p1);
+        P.w.push_back(term[r] * p2);
+        P.rowFace.push_back(r < nm ? -1 : rowB[r - nm]);
+      }
+    }
+  }
+  P.rowOff.push_back((int)P.rowFace.size());
+  return 0;
+}
+
+}  // namespace rflu
 
 struct rflu_setup {
   int nCells = 0, nFaces = 0, nPatches = 0;
@@ -148,6 +300,7 @@ struct rflu_setup {
   std::vector<double> bfn, bfc;
   std::vector<int> c2csOff, c2csMembs;
   std::vector<double> xyzMoms;
+  std::vector<double> fc2, c2csShift;  // periodic meshes only
 };
 
 extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_setup **out) {
@@ -161,24 +314,147 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
   auto localFace = [&](int lf, int k) { return (nvc == 4) ? kTetFace[lf][k] : kHexFace[lf][k]; };
   S->nCells = nc;
 
+  // ---- translational periodic patch pairs ------------------------------------
+  // The reference builds virtual cells beyond each periodic patch (modflu/
+  // RFLU_ModSymmetryPeriodic.F90:471-787); here, as in the CPU restatement,
+  // the two patches' vertices are identified (their coordinates differ by
+  // one translation per pair, the mean difference of the two vertex sets,
+  // matched within 1e-7 of the box's extent): faces and stencils are built
+  // on the identified vertex ids (vid), geometry on each cell's own
+  // vertices, and a face or stencil member across a period carries the
+  // translation between the two cells' frames.
+  std::vector<int> rep;
+  std::vector<std::array<double, 3>> perShift;
+  std::vector<char> periodicPatch(std::max(m->nPatches, 1), 0);
+  if (m->patchBcType && m->patchRelated && m->patchFaceOff) {
+    for (int ip = 0; ip < m->nPatches; ++ip) periodicPatch[ip] = (m->patchBcType[ip] == 110);
+    bool any = false;
+    for (int ip = 0; ip < m->nPatches; ++ip) any = any || periodicPatch[ip];
+    if (any) {
+      rep.resize(nv);
+      std::iota(rep.begin(), rep.end(), 0);
+      auto find = [&](int v) {
+        while (rep[v] != v) { rep[v] = rep[rep[v]]; v = rep[v]; }
+        return v;
+      };
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int v = 0; v < nv; ++v)
+        for (int d = 0; d < 3; ++d) { lo[d] = std::min(lo[d], m->xyz[3 * (size_t)v + d]); hi[d] = std::max(hi[d], m->xyz[3 * (size_t)v + d]); }
+      const double tol = 1e-7 * std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+      auto patchVerts = [&](int ip) {
+        std::vector<int> v;
+        for (int b = m->patchFaceOff[ip]; b < m->patchFaceOff[ip + 1]; ++b)
+          for (int k = 0; k < 4; ++k)
+            if (m->bf2v[4 * (size_t)b + k] > 0) v.push_back(m->bf2v[4 * (size_t)b + k] - 1);
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        return v;
+      };
+      for (int ip = 0; ip < m->nPatches; ++ip) {
+        const int iq = m->patchRelated[ip];
+        if (!periodicPatch[ip] || iq <= ip) continue;
+        if (iq >= m->nPatches || m->patchBcType[iq] != 110 || m->patchRelated[iq] != ip) {
+          delete S;
+          return rflu::fail(RFLU_ERR_ARG, "rflu_setup_build: periodic patches must relate to each other in pairs");
+        }
+        const std::vector<int> vp = patchVerts(ip), vq = patchVerts(iq);
+        if (vp.size() != vq.size() || vp.empty()) {
+          delete S;
+          return rflu::fail(RFLU_ERR_ARG, "rflu_setup_build: periodic patches do not match");
+        }
+        std::array<double, 3> T;
+        for (int d = 0; d < 3; ++d) {
+          double sp = 0.0, sq = 0.0;
+          for (int v : vp) sp += m->xyz[3 * (size_t)v + d];
+          for (int v : vq) sq += m->xyz[3 * (size_t)v + d];
+          T[d] = (sq - sp) / (double)vp.size();
+        }
+        perShift.push_back(T);
+        std::map<std::array<long long, 3>, int> grid;
+        for (int w : vq) {
+          std::array<long long, 3> k;
+          for (int d = 0; d < 3; ++d) k[d] = std::llround(m->xyz[3 * (size_t)w + d] / tol);
+          grid[k] = w;
+        }
+        for (int v : vp) {
+          int w = -1;
+          std::array<long long, 3> k0;
+          for (int d = 0; d < 3; ++d) k0[d] = std::llround((m->xyz[3 * (size_t)v + d] + T[d]) / tol);
+          for (int a = -1; a <= 1 && w < 0; ++a)
+            for (int b = -1; b <= 1 && w < 0; ++b)
+              for (int e = -1; e <= 1 && w < 0; ++e) {
+                auto it = grid.find({k0[0] + a, k0[1] + b, k0[2] + e});
+                if (it != grid.end()) w = it->second;
+              }
+          if (w < 0) {
+            delete S;
+            return rflu::fail(RFLU_ERR_ARG, "rflu_setup_build: a periodic vertex has no image on its related patch");
+          }
+          const int rv = find(v), rw = find(w);
+          if (rv != rw) rep[std::max(rv, rw)] = std::min(rv, rw);
+        }
+      }
+      for (int v = 0; v < nv; ++v) rep[v] = find(v);
+    }
+  }
+  const bool periodic = !rep.empty();
+  auto vid = [&](int ic, int k) { const int v = vert(ic, k); return periodic ? rep[v] : v; };
+  // offset of stencil member j from cell i for the image of j nearest to i
+  // (the virtual cell standing for j in the reference), and its translation
+  auto memberOffset = [&](const double *cg, int i, int j, double &dx, double &dy, double &dz, double *sh) {
+    dx = cg[3 * (size_t)j] - cg[3 * (size_t)i];
+    dy = cg[3 * (size_t)j + 1] - cg[3 * (size_t)i + 1];
+    dz = cg[3 * (size_t)j + 2] - cg[3 * (size_t)i + 2];
+    if (sh) sh[0] = sh[1] = sh[2] = 0.0;
+    if (perShift.empty()) return;
+    double best = dx * dx + dy * dy + dz * dz, bx = dx, by = dy, bz = dz, s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    const int np = (int)perShift.size();
+    int combos = 1;
+    for (int p = 0; p < np; ++p) combos *= 3;
+    for (int mm = 1; mm < combos; ++mm) {
+      double sx = 0.0, sy = 0.0, sz = 0.0;
+      int r = mm;
+      for (int p = 0; p < np; ++p, r /= 3) {
+        const double f = (double)(r % 3 == 2 ? -1 : r % 3);
+        sx += f * perShift[p][0];
+        sy += f * perShift[p][1];
+        sz += f * perShift[p][2];
+      }
+      const double ex = dx + sx, ey = dy + sy, ez = dz + sz;
+      const double d2 = ex * ex + ey * ey + ez * ez;
+      if (d2 < best) { best = d2; bx = ex; by = ey; bz = ez; s0 = sx; s1 = sy; s2 = sz; }
+    }
+    dx = bx; dy = by; dz = bz;
+    if (sh) { sh[0] = s0; sh[1] = s1; sh[2] = s2; }
+  };
+
   // ---- slot keys, bucketed by smallest vertex (counting sort) -------------
   const int64_t nSlots = (int64_t)nc * nfl;
-  const int nb = m->patchFaceOff ? m->patchFaceOff[m->nPatches] : 0;
+  // the boundary faces that stay boundary faces: those of periodic patches
+  // become interior faces of the identified mesh
+  std::vector<int> keep;
+  std::vector<int> patchOffKept(m->nPatches + 1, 0);
+  for (int ip = 0; ip < m->nPatches; ++ip) {
+    if (!(periodic && periodicPatch[ip]))
+      for (int b = m->patchFaceOff[ip]; b < m->patchFaceOff[ip + 1]; ++b) keep.push_back(b);
+    patchOffKept[ip + 1] = (int)keep.size();
+  }
+  const int nb = (int)keep.size();
   std::vector<int> bucketOff(nv + 1, 0);
   std::vector<int> smallest(nSlots + nb);
   std::vector<SlotKey> keys(nSlots + nb);
 #pragma omp parallel for schedule(static)
   for (int64_t s = 0; s < nSlots; ++s) {
     int ic = (int)(s / nfl), lf = (int)(s % nfl), fv[4];
-    for (int k = 0; k < fvs; ++k) fv[k] = vert(ic, localFace(lf, k));
+    for (int k = 0; k < fvs; ++k) fv[k] = vid(ic, localFace(lf, k));
     std::sort(fv, fv + fvs);
     smallest[s] = fv[0];
     keys[s] = {fv[1], fv[2], s};
   }
   for (int b = 0; b < nb; ++b) {
-    const int *bv = m->bf2v + 4 * (size_t)b;
+    const int *bv = m->bf2v + 4 * (size_t)keep[b];
     int n = (bv[3] <= 0) ? 3 : 4, fv[4];
-    for (int k = 0; k < n; ++k) fv[k] = bv[k] - 1;
+    for (int k = 0; k < n; ++k) fv[k] = periodic ? rep[bv[k] - 1] : bv[k] - 1;
     std::sort(fv, fv + n);
     smallest[nSlots + b] = fv[0];
     keys[nSlots + b] = {fv[1], fv[2], -(int64_t)(b + 1)};
@@ -239,6 +515,20 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
   std::vector<int> order(nf);
   std::iota(order.begin(), order.end(), 0);
   std::sort(order.begin(), order.end(), [&](int a, int b) { return lowSlot[a] < lowSlot[b]; });
+  if (periodic) {
+    // faces across a period (the reference's actual-virtual faces) follow
+    // the others, both in first-insertion order: across when the second
+    // cell holds the face's first vertex under another vertex id
+    auto across = [&](int o) {
+      const int64_t sl = lowSlot[o];
+      const int ic = (int)(sl / nfl), lf = (int)(sl % nfl), c2 = highCell[o];
+      const int a = vert(ic, localFace(lf, 0));
+      for (int k = 0; k < nvc; ++k)
+        if (vert(c2, k) == a) return false;
+      return true;
+    };
+    std::stable_partition(order.begin(), order.end(), [&](int o) { return !across(o); });
+  }
   S->nFaces = nf;
   S->f2c.resize(2 * (size_t)nf);
   std::vector<int> f2v(4 * (size_t)nf, -1);
@@ -275,14 +565,35 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
     n[0] = v[0] * inv; n[1] = v[1] * inv; n[2] = v[2] * inv; n[3] = mag;
   }
   S->nPatches = m->nPatches;
-  S->patchFaceOff.assign(m->patchFaceOff, m->patchFaceOff + m->nPatches + 1);
+  S->patchFaceOff = patchOffKept;
+  // each face's centroid in its second cell's frame: the translation between
+  // the two cells' own coordinates of the face's first vertex (zero unless
+  // across a period)
+  if (periodic) {
+    S->fc2.assign(S->fc.begin(), S->fc.end());
+    for (int f = 0; f < nf; ++f) {
+      const int c1 = S->f2c[2 * (size_t)f], c2 = S->f2c[2 * (size_t)f + 1], a = f2v[4 * (size_t)f];
+      double sh[3] = {0.0, 0.0, 0.0};
+      for (int k = 0; k < nvc; ++k) {
+        if (vert(c1, k) != a) continue;
+        for (int k2 = 0; k2 < nvc; ++k2)
+          if (vid(c2, k2) == vid(c1, k)) {
+            const int b = vert(c2, k2);
+            if (b != a)
+              for (int d = 0; d < 3; ++d) sh[d] = xyz[3 * (size_t)b + d] - xyz[3 * (size_t)a + d];
+          }
+      }
+      if (sh[0] != 0.0 || sh[1] != 0.0 || sh[2] != 0.0)
+        for (int d = 0; d < 3; ++d) S->fc2[3 * (size_t)f + d] = S->fc[3 * (size_t)f + d] + sh[d];
+    }
+  }
   S->bf2c.resize(nb);
   S->bfn.resize(4 * (size_t)nb);
   S->bfc.resize(3 * (size_t)nb);
   std::vector<double> bvec(3 * (size_t)nb);
   for (int b = 0; b < nb; ++b) {
     int v[4];
-    const int *bv = m->bf2v + 4 * (size_t)b;
+    const int *bv = m->bf2v + 4 * (size_t)keep[b];
     int nvf = (bv[3] <= 0) ? 3 : 4;
     for (int k = 0; k < nvf; ++k) v[k] = bv[k] - 1;
     double *vv = &bvec[3 * (size_t)b], *cen = &S->bfc[3 * (size_t)b];
@@ -320,8 +631,8 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
       bool minus = false;
       if (code < 2 * nf) {
         vv = &fvec[3 * (size_t)(code >> 1)];
-        cen = &S->fc[3 * (size_t)(code >> 1)];
         minus = code & 1;
+        cen = (minus && periodic) ? &S->fc2[3 * (size_t)(code >> 1)] : &S->fc[3 * (size_t)(code >> 1)];
       } else {
         vv = &bvec[3 * (size_t)(code - 2 * nf)];
         cen = &S->bfc[3 * (size_t)(code - 2 * nf)];
@@ -343,13 +654,13 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
     const int minSize = 4, maxSize = 40, maxLayers = 6;
     std::vector<int> v2cOff(nv + 1, 0);
     for (int ic = 0; ic < nc; ++ic)
-      for (int k = 0; k < nvc; ++k) v2cOff[vert(ic, k) + 1]++;
+      for (int k = 0; k < nvc; ++k) v2cOff[vid(ic, k) + 1]++;
     for (int v = 0; v < nv; ++v) v2cOff[v + 1] += v2cOff[v];
     std::vector<int> v2c(v2cOff[nv]);
     {
       std::vector<int> fill(v2cOff.begin(), v2cOff.end() - 1);
       for (int ic = 0; ic < nc; ++ic)
-        for (int k = 0; k < nvc; ++k) v2c[fill[vert(ic, k)]++] = ic;
+        for (int k = 0; k < nvc; ++k) v2c[fill[vid(ic, k)]++] = ic;
     }
     std::vector<std::vector<int>> memb(nc);
     const double invNv = 1.0 / (double)nvc;
@@ -362,18 +673,18 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
       for (int ic = 0; ic < nc; ++ic) {
         cand.clear();
         for (int k = 0; k < nvc; ++k) {
-          int v = vert(ic, k);
+          int v = vid(ic, k);
           cand.insert(cand.end(), v2c.begin() + v2cOff[v], v2c.begin() + v2cOff[v + 1]);
         }
         std::sort(cand.begin(), cand.end());
         cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
         cand.erase(std::lower_bound(cand.begin(), cand.end(), ic));
         const int nCand = (int)cand.size();
-        for (int k = 0; k < nvc; ++k) sv[k] = vert(ic, k);
+        for (int k = 0; k < nvc; ++k) sv[k] = vid(ic, k);
         std::sort(sv.begin(), sv.end());
         frac.resize(nCand);
         for (int i = 0; i < nCand; ++i) {
-          for (int k = 0; k < nvc; ++k) sv2[k] = vert(cand[i], k);
+          for (int k = 0; k < nvc; ++k) sv2[k] = vid(cand[i], k);
           std::sort(sv2.begin(), sv2.end());
           int shared = 0;
           for (int a = 0, b = 0; a < nvc && b < nvc;) {
@@ -394,9 +705,8 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
             A.assign(4 * (size_t)degr, 0.0);
             for (int r = 0; r < degr; ++r) {
               int j = st[r];
-              double dx = cg[3 * (size_t)j] - cg[3 * (size_t)ic];
-              double dy = cg[3 * (size_t)j + 1] - cg[3 * (size_t)ic + 1];
-              double dz = cg[3 * (size_t)j + 2] - cg[3 * (size_t)ic + 2];
+              double dx, dy, dz;
+              memberOffset(cg, ic, j, dx, dy, dz, nullptr);
               double t = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
               A[4 * r] = t; A[4 * r + 1] = t * dx; A[4 * r + 2] = t * dy; A[4 * r + 3] = t * dz;
             }
@@ -416,7 +726,7 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
           bool full = false;
           for (int i = layerBeg; i < layerEnd && !full; ++i)
             for (int k = 0; k < nvc && !full; ++k) {
-              int v = vert(st[i], k);
+              int v = vid(st[i], k);
               for (int e = v2cOff[v]; e < v2cOff[v + 1]; ++e) {
                 int c2 = v2c[e];
                 if (c2 == ic || std::binary_search(have.begin(), have.end(), c2)) continue;
@@ -440,14 +750,14 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
       for (size_t k = 0; k < memb[ic].size(); ++k) S->c2csMembs[S->c2csOff[ic] + k] = memb[ic][k] + 1;
     // stencil moments: RFLU_ComputeStencilMoments3D1 (modflu/RFLU_ModWeights.F90:1770-1915)
     S->xyzMoms.assign(10 * (size_t)nc, 0.0);
+    if (periodic) S->c2csShift.assign(3 * (size_t)S->c2csOff[nc], 0.0);
 #pragma omp parallel for schedule(static)
     for (int ic = 0; ic < nc; ++ic) {
       double mm[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (int e = S->c2csOff[ic]; e < S->c2csOff[ic + 1]; ++e) {
         int j = S->c2csMembs[e] - 1;
-        double dx = cg[3 * (size_t)j] - cg[3 * (size_t)ic];
-        double dy = cg[3 * (size_t)j + 1] - cg[3 * (size_t)ic + 1];
-        double dz = cg[3 * (size_t)j + 2] - cg[3 * (size_t)ic + 2];
+        double dx, dy, dz;
+        memberOffset(cg, ic, j, dx, dy, dz, periodic ? &S->c2csShift[3 * (size_t)e] : nullptr);
         double wt = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
         dx = wt * dx; dy = wt * dy; dz = wt * dz;
         mm[0] = mm[0] + dx * dx; mm[1] = mm[1] + dx * dy; mm[2] = mm[2] + dy * dy;
@@ -494,10 +804,30 @@ extern "C" int rflu_setup_grid(rflu_setup *S, rflu_grid_desc *g) {
   g->c2csOff = S->c2csOff.data();
   g->c2csMembs = S->c2csMembs.empty() ? nullptr : S->c2csMembs.data();
   g->xyzMoms = S->xyzMoms.empty() ? nullptr : S->xyzMoms.data();
+  g->fc2 = S->fc2.empty() ? nullptr : S->fc2.data();
+  g->c2csShift = S->c2csShift.empty() ? nullptr : S->c2csShift.data();
   return RFLU_OK;
 }
 
 extern "C" int rflu_setup_destroy(rflu_setup *S) {
   delete S;
+  return RFLU_OK;
+}
+
+extern "C" int rflu_setup_bface_stencil(const rflu_grid_desc *g, int *off, int *faces) {
+  if (!g || !off || !g->cofg || !g->c2csOff || (!g->c2csMembs && g->c2csOff[g->nCells] > 0) || !g->patchFaceOff ||
+      (g->nPatches > 0 && (!g->patchBcType || !g->bf2c || !g->bfc)))
+    return rflu::fail(RFLU_ERR_ARG, "rflu_setup_bface_stencil: incomplete grid description");
+  const int nc = g->nCells, nb = g->patchFaceOff[g->nPatches];
+  std::vector<int> stIdx(g->c2csOff[nc]), bf2c(nb);
+  for (int e = 0; e < g->c2csOff[nc]; ++e) stIdx[e] = g->c2csMembs[e] - 1;
+  for (int b = 0; b < nb; ++b) bf2c[b] = g->bf2c[b] - 1;
+  std::vector<double> minj(std::max(g->nPatches, 1), 0.0);
+  rflu::ConstrInput in{nc, g->cofg, g->c2csOff, stIdx.data(), g->nPatches, g->patchFaceOff, g->patchBcType,
+                       minj.data(), bf2c.data(), g->bfn, g->bfc, 1.0};
+  rflu::ConstrPlan plan;
+  rflu::planConstrained(in, plan, nullptr, false);
+  std::memcpy(off, plan.bfOff.data(), sizeof(int) * (nc + 1));
+  if (faces && !plan.bfIdx.empty()) std::memcpy(faces, plan.bfIdx.data(), sizeof(int) * plan.bfIdx.size());
   return RFLU_OK;
 }

@@ -43,7 +43,8 @@ class GridDesc(C.Structure):
                 ("patchPout", C.POINTER(C.c_double)), ("patchOrder", C.POINTER(C.c_int)),
                 ("c2csOff", C.POINTER(C.c_int)), ("c2csMembs", C.POINTER(C.c_int)),
                 ("xyzMoms", C.POINTER(C.c_double)), ("patchVals", C.POINTER(C.c_double)),
-                ("patchSwitches", C.POINTER(C.c_int))]
+                ("patchSwitches", C.POINTER(C.c_int)), ("fc2", C.POINTER(C.c_double)),
+                ("c2csShift", C.POINTER(C.c_double))]
 
 BCDAT_N, BCSWI_N = 8, 2
 
@@ -65,7 +66,8 @@ class NumDesc(C.Structure):
     _fields_ = [("spaceOrder", C.c_int), ("spaceDiscr", C.c_int), ("reconst", C.c_int), ("rkScheme", C.c_int),
                 ("piclBuild", C.c_int), ("precision", C.c_int), ("cp", C.c_double), ("gamma", C.c_double),
                 ("cfl", C.c_double), ("epsEntr", C.c_double), ("dissFact", C.c_double),
-                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double), ("options", C.c_int)]
+                ("dtImposed", C.c_double), ("dtMinLimit", C.c_double), ("options", C.c_int),
+                ("cReconstCells", C.c_int), ("cReconstCellsWeight", C.c_double)]
 
 
 OPT_UNTILED = 1
@@ -79,7 +81,8 @@ class Status(C.Structure):
 class MeshDesc(C.Structure):
     _fields_ = [("nVert", C.c_int), ("nCells", C.c_int), ("nVertPerCell", C.c_int), ("xyz", C.POINTER(C.c_double)),
                 ("c2v", C.POINTER(C.c_int)), ("nPatches", C.c_int), ("patchFaceOff", C.POINTER(C.c_int)),
-                ("bf2v", C.POINTER(C.c_int))]
+                ("bf2v", C.POINTER(C.c_int)), ("patchBcType", C.POINTER(C.c_int)),
+                ("patchRelated", C.POINTER(C.c_int))]
 
 
 class RfluError(RuntimeError):
@@ -94,7 +97,7 @@ EXPORTS = ("rflu_gpu_create", "rflu_gpu_destroy", "rflu_gpu_last_error", "rflu_g
            "rflu_gpu_convective_fluxes", "rflu_gpu_add_rhs", "rflu_gpu_rk_update", "rflu_gpu_get_rhs", "rflu_gpu_limiter_branches",
            "rflu_gpu_get_grad", "rflu_gpu_residual", "rflu_gpu_vjp",
            "rflu_gpu_jvp", "rflu_gpu_patch_pressure", "rflu_gpu_unrolled_adjoint", "rflu_gpu_status", "rflu_gpu_kernel_times", "rflu_gpu_residual_static",
-           "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_gpu_check_conversions", "rflu_gpu_check_refinements", "rflu_setup_build", "rflu_setup_grid",
+           "rflu_gpu_adjoint_times", "rflu_gpu_fp64_rate", "rflu_gpu_check_conversions", "rflu_gpu_check_refinements", "rflu_setup_build", "rflu_setup_grid", "rflu_setup_bface_stencil",
            "rflu_setup_destroy")
 
 
@@ -148,6 +151,7 @@ def lib(build_if_missing=True):
     L.rflu_gpu_check_refinements.argtypes = [C.c_longlong, C.c_ulonglong, DP]
     L.rflu_setup_build.argtypes = [C.POINTER(MeshDesc), I, C.POINTER(P)]
     L.rflu_setup_grid.argtypes = [P, C.POINTER(GridDesc)]
+    L.rflu_setup_bface_stencil.argtypes = [C.POINTER(GridDesc), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.rflu_setup_destroy.argtypes = [P]
     for name in EXPORTS:
         if name not in ("rflu_gpu_last_error", "rflu_gpu_stream"):
@@ -170,7 +174,8 @@ def _p(a, t=C.c_double):
 def num_desc(num, precision, options=0):
     return NumDesc(num.space_order, num.space_discr, num.reconst, num.rk_scheme, num.picl_build,
                    PREC[precision] if isinstance(precision, str) else int(precision), num.cp, num.gamma, num.cfl,
-                   num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit, int(options))
+                   num.eps_entr, num.diss_fact, num.dt_imposed, num.dt_min_limit, int(options),
+                   int(getattr(num, "c_reconst", 0)), float(getattr(num, "c_reconst_weight", 1.0)))
 
 
 class Setup:
@@ -186,15 +191,20 @@ class Setup:
             off[i + 1] = off[i] + len(p.bf2v)
         bf2v = np.concatenate([p.bf2v for p in case.patches]).astype(np.int32) + 1  # triangles: -1 -> 0
         bf2v = np.ascontiguousarray(bf2v)
-        self._in = (xyz, c2v, off, bf2v)
+        bct = np.array([p.bc_type for p in case.patches], np.int32)
+        rel = np.array([getattr(p, "related", -1) for p in case.patches], np.int32)
+        self._in = (xyz, c2v, off, bf2v, bct, rel)
         md = MeshDesc(xyz.shape[0], c2v.shape[0], c2v.shape[1], _p(xyz), _p(c2v, C.c_int), len(case.patches),
-                      _p(off, C.c_int), _p(bf2v, C.c_int))
+                      _p(off, C.c_int), _p(bf2v, C.c_int), _p(bct, C.c_int), _p(rel, C.c_int))
         h = C.c_void_p()
         _check(L.rflu_setup_build(C.byref(md), case.num.space_order, C.byref(h)))
         self.h = h
         g = GridDesc()
         _check(L.rflu_setup_grid(self.h, C.byref(g)))
         nc, nf = g.nCells, g.nFaces
+        # periodic patches' faces are interior faces of the identified mesh:
+        # the set-up's own patch offsets count them as none
+        off = np.ctypeslib.as_array(g.patchFaceOff, (len(case.patches) + 1,)).copy()
         nb = int(off[-1])
         self.n_cells, self.n_faces = nc, nf
         self.f2c = np.ctypeslib.as_array(g.f2c, (nf, 2)).copy()
@@ -203,9 +213,12 @@ class Setup:
         self.vol = np.ctypeslib.as_array(g.vol, (nc,)).copy()
         self.cofg = np.ctypeslib.as_array(g.cofg, (nc, 3)).copy()
         self.patch_off = off
-        self.bf2c = np.ctypeslib.as_array(g.bf2c, (max(nb, 1),))[:nb].copy()
-        self.bfn = np.ctypeslib.as_array(g.bfn, (max(nb, 1), 4))[:nb].copy()
-        self.bfc = np.ctypeslib.as_array(g.bfc, (max(nb, 1), 3))[:nb].copy()
+        if nb:
+            self.bf2c = np.ctypeslib.as_array(g.bf2c, (nb,)).copy()
+            self.bfn = np.ctypeslib.as_array(g.bfn, (nb, 4)).copy()
+            self.bfc = np.ctypeslib.as_array(g.bfc, (nb, 3)).copy()
+        else:  # every patch periodic
+            self.bf2c, self.bfn, self.bfc = np.zeros(0, np.int32), np.zeros((0, 4)), np.zeros((0, 3))
         self.c2cs_off = np.ctypeslib.as_array(g.c2csOff, (nc + 1,)).copy()
         nnz = int(self.c2cs_off[-1])
         if nnz:
@@ -214,8 +227,59 @@ class Setup:
         else:
             self.c2cs = np.zeros(0, np.int32)
             self.moms = np.zeros((nc, 10))
+        # periodic meshes: face centroids in the second cells' frames and the
+        # stencil members' image translations
+        self.fc2 = np.ctypeslib.as_array(g.fc2, (nf, 3)).copy() if g.fc2 else None
+        self.c2cs_shift = np.ctypeslib.as_array(g.c2csShift, (max(nnz, 1), 3))[:nnz].copy() if g.c2csShift else None
         L.rflu_setup_destroy(self.h)
         self.h = None
+
+
+def grid_desc(case, grid):
+    """rflu_grid_desc of a case and its setup products (an object with the
+    fields of Setup); returns the descriptor and the arrays it points into,
+    which the caller keeps alive while the descriptor is used."""
+    nc = int(grid.vol.shape[0])
+    pt = np.array([p.bc_type for p in case.patches], np.int32)
+    po = np.array([p.outflow_type for p in case.patches], np.int32)
+    pp = np.array([p.p_out for p in case.patches], np.float64)
+    pr = np.array([p.order for p in case.patches], np.int32)
+    pv, psw = patch_values(case)
+    arrs = dict(
+        f2c=np.ascontiguousarray(grid.f2c, np.int32), fn=np.ascontiguousarray(grid.fn, np.float64),
+        fc=np.ascontiguousarray(grid.fc, np.float64), vol=np.ascontiguousarray(grid.vol, np.float64),
+        cofg=np.ascontiguousarray(grid.cofg, np.float64), off=np.ascontiguousarray(grid.patch_off, np.int32),
+        bf2c=np.ascontiguousarray(grid.bf2c, np.int32), bfn=np.ascontiguousarray(grid.bfn, np.float64),
+        bfc=np.ascontiguousarray(grid.bfc, np.float64), pt=pt, po=po, pp=pp, pr=pr,
+        soff=np.ascontiguousarray(grid.c2cs_off, np.int32),
+        smem=np.ascontiguousarray(grid.c2cs if len(grid.c2cs) else np.zeros(1), np.int32),
+        moms=np.ascontiguousarray(grid.moms, np.float64), pv=pv, psw=psw)
+    fc2 = getattr(grid, "fc2", None)
+    shift = getattr(grid, "c2cs_shift", None)
+    arrs["fc2"] = None if fc2 is None else np.ascontiguousarray(fc2, np.float64)
+    arrs["shift"] = None if shift is None else np.ascontiguousarray(shift, np.float64)
+    a = arrs
+    gd = GridDesc(nc, int(a["f2c"].shape[0]), _p(a["f2c"], C.c_int), _p(a["fn"]), _p(a["fc"]), _p(a["vol"]),
+                  _p(a["cofg"]), len(case.patches), _p(a["off"], C.c_int), _p(a["bf2c"], C.c_int), _p(a["bfn"]),
+                  _p(a["bfc"]), _p(a["pt"], C.c_int), _p(a["po"], C.c_int), _p(a["pp"]), _p(a["pr"], C.c_int),
+                  _p(a["soff"], C.c_int), _p(a["smem"], C.c_int), _p(a["moms"]), _p(a["pv"]),
+                  _p(a["psw"], C.c_int), None if a["fc2"] is None else _p(a["fc2"]),
+                  None if a["shift"] is None else _p(a["shift"]))
+    return gd, arrs
+
+
+def bface_stencil(case, grid=None):
+    """The boundary-face stencil of CRECONSTC 1 (rflu_setup_bface_stencil):
+    per cell (reference order) its wall and injection faces, nearest first,
+    as 0-based boundary face indices; returns (off, faces)."""
+    grid = Setup(case) if grid is None else grid
+    gd, keep = grid_desc(case, grid)
+    nc = int(grid.vol.shape[0])
+    off = np.zeros(nc + 1, np.int32)
+    _check(lib().rflu_setup_bface_stencil(C.byref(gd), _p(off, C.c_int), None))
+    faces = np.zeros(max(int(off[-1]), 1), np.int32)
+    _check(lib().rflu_setup_bface_stencil(C.byref(gd), _p(off, C.c_int), _p(faces, C.c_int)))
+    return off, faces[:int(off[-1])]
 
 
 class Region:
@@ -235,26 +299,7 @@ class Region:
         self.grid = grid
         nc = int(grid.vol.shape[0])
         self.n_cells = nc
-        pt = np.array([p.bc_type for p in case.patches], np.int32)
-        po = np.array([p.outflow_type for p in case.patches], np.int32)
-        pp = np.array([p.p_out for p in case.patches], np.float64)
-        pr = np.array([p.order for p in case.patches], np.int32)
-        pv, psw = patch_values(case)
-        arrs = dict(
-            f2c=np.ascontiguousarray(grid.f2c, np.int32), fn=np.ascontiguousarray(grid.fn, np.float64),
-            fc=np.ascontiguousarray(grid.fc, np.float64), vol=np.ascontiguousarray(grid.vol, np.float64),
-            cofg=np.ascontiguousarray(grid.cofg, np.float64), off=np.ascontiguousarray(grid.patch_off, np.int32),
-            bf2c=np.ascontiguousarray(grid.bf2c, np.int32), bfn=np.ascontiguousarray(grid.bfn, np.float64),
-            bfc=np.ascontiguousarray(grid.bfc, np.float64), pt=pt, po=po, pp=pp, pr=pr,
-            soff=np.ascontiguousarray(grid.c2cs_off, np.int32),
-            smem=np.ascontiguousarray(grid.c2cs if len(grid.c2cs) else np.zeros(1), np.int32),
-            moms=np.ascontiguousarray(grid.moms, np.float64), pv=pv, psw=psw)
-        a = arrs
-        gd = GridDesc(nc, int(a["f2c"].shape[0]), _p(a["f2c"], C.c_int), _p(a["fn"]), _p(a["fc"]), _p(a["vol"]),
-                      _p(a["cofg"]), len(case.patches), _p(a["off"], C.c_int), _p(a["bf2c"], C.c_int), _p(a["bfn"]),
-                      _p(a["bfc"]), _p(a["pt"], C.c_int), _p(a["po"], C.c_int), _p(a["pp"]), _p(a["pr"], C.c_int),
-                      _p(a["soff"], C.c_int), _p(a["smem"], C.c_int), _p(a["moms"]), _p(a["pv"]),
-                      _p(a["psw"], C.c_int))
+        gd, self._desc_arrays = grid_desc(case, grid)
         self.nd = num_desc(case.num, precision, options)
         h = C.c_void_p()
         _check(L.rflu_gpu_create(C.byref(gd), C.byref(self.nd), C.byref(h)))

@@ -314,8 +314,9 @@ def numerics_from_deck(deck):
         raise ValueError("deck: only the Euler model (MODEL 0) is on this path")
     if val(ts, "FLOWTYPE", 1, int) != 1:
         raise ValueError("deck: only unsteady flow (FLOWTYPE 1) is on this path")
-    if val(num, "CRECONSTC", 0, int) != 0:
-        raise ValueError("deck: constrained cell gradients (CRECONSTC 1) are not on this path")
+    creconst = val(num, "CRECONSTC", 0, int)
+    if creconst not in (0, 1):
+        raise ValueError("deck: CRECONSTC must be 0 or 1")
     discr = val(num, "DISCR", 1, int)
     if discr not in (1, 3, 4):
         raise ValueError("deck: DISCR must be 1 (Roe), 3 (HLLC) or 4 (AUSM+)")
@@ -323,7 +324,8 @@ def numerics_from_deck(deck):
                        rk_scheme=val(ts, "RKSCHEME", None, int), cfl=val(num, "CFL", 3.0),
                        cp=val(ref, "CP"), gamma=val(ref, "GAMMA"), eps_entr=val(num, "ENTROPY", 0.05),
                        diss_fact=val(num, "DISSFACT", 1.0), dt_imposed=val(ts, "TIMESTEP"),
-                       dt_min_limit=val(ts, "DTMINLIMIT"))
+                       dt_min_limit=val(ts, "DTMINLIMIT"), c_reconst=creconst,
+                       c_reconst_weight=abs(val(num, "CRECONSTCW", 1.0)))
     return n, val(ts, "MAXTIME"), val(num, "ORDERBF", 1, int)
 
 

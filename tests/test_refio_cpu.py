@@ -94,7 +94,9 @@ def test_gas_jump_case_is_what_the_reference_deck_states():
 
     fx = json.load(open(os.path.join(GOLDEN, "gas_jump_closed_creconst0_np2.json")))["deck"]
     c = cases.gas_jump_closed()
-    assert dataclasses.asdict(c.num) == fx["numerics"]
+    num = dataclasses.asdict(c.num)
+    assert {k: num[k] for k in fx["numerics"]} == fx["numerics"]
+    assert num["c_reconst"] == 0  # the golden's override CRECONSTC 0
     assert c.end_time == fx["end_time"]
     assert [{"bc_type": p.bc_type, "order": p.order} for p in c.patches] == fx["patch_kinds"]
 
@@ -138,8 +140,10 @@ ORDER      2
     kinds = refio.patch_kinds_from_bc(bc, 6)
     assert kinds[0] == kinds[1] == {"bc_type": cases.BC_OUTFLOW, "outflow_type": 1, "p_out": 82700.0, "order": 2}
     assert all(k == {"bc_type": cases.BC_SLIPWALL, "order": 1} for k in kinds[2:])
+    num1, _, _ = refio.numerics_from_deck(refio.apply_overrides(deck, {"NUMERICS/CRECONSTC": 1}))
+    assert num1.c_reconst == 1 and num1.c_reconst_weight == 1.0
     with pytest.raises(ValueError):
-        refio.numerics_from_deck(refio.apply_overrides(deck, {"NUMERICS/CRECONSTC": 1}))
+        refio.numerics_from_deck(refio.apply_overrides(deck, {"NUMERICS/CRECONSTC": 2}))
     with pytest.raises(ValueError):
         refio.patch_kinds_from_bc(refio.read_deck("# BC_PERIODIC\nPATCH 1 6\n#\n"), 6)
 

@@ -87,3 +87,36 @@ def test_library_exports_every_header_symbol():
     assert declared <= exported, declared - exported
     for name in declared:
         assert hasattr(L, name)
+
+
+def test_setup_periodic_mesh_matches_oracle():
+    """Translational periodic patch pairs: rflu_setup_build identifies the
+    pairs' vertices as the oracle does and gives the same faces (across-period
+    faces after the others), geometry in each cell's own frame, the faces'
+    centroids in their second cells' frames (fc2), stencils on the
+    identified mesh, moments with the members' nearest images, and those
+    images' translations (c2csShift), bit for bit; the periodic patches keep
+    no boundary faces."""
+    c = cases.gas_jump_periodic()
+    s = gpu.Setup(c)
+    o = Oracle(c)
+    f2c, _, fn, fc = o.faces()
+    np.testing.assert_array_equal(s.f2c - 1, f2c)
+    np.testing.assert_array_equal(s.fn, fn)
+    np.testing.assert_array_equal(s.fc, fc)
+    vol, cofg = o.cells()
+    np.testing.assert_array_equal(s.vol, vol)
+    np.testing.assert_array_equal(s.cofg, cofg)
+    off, idx, moms = o.stencil()
+    np.testing.assert_array_equal(s.c2cs_off, off)
+    np.testing.assert_array_equal(s.c2cs - 1, idx)
+    np.testing.assert_array_equal(s.moms, moms)
+    fc2, sh = o.periodic()
+    np.testing.assert_array_equal(s.fc2, fc2)
+    px = cofg[idx] - np.repeat(cofg, np.diff(off), axis=0)
+    np.testing.assert_array_equal(px + s.c2cs_shift, px + sh)
+    assert (np.abs(s.c2cs_shift).max(axis=1) > 0).sum() > 0
+    assert (s.patch_off == 0).all() and len(s.bf2c) == 0
+    # a non-periodic mesh exports neither
+    s2 = gpu.Setup(cases.gas_jump_closed())
+    assert s2.fc2 is None and s2.c2cs_shift is None
