@@ -1,11 +1,13 @@
-"""Writes tests/golden/gas_jump_closed_creconst0_np2.json from the reference's
-own golden of the closed gas-jump box (its tests/goldens/box/gas-jump/
-closed-creconst0/np2/golden.json: the state the Fortran solver reached at
-t = 1.05e-4 on two ranks, conserved variables per region in the region's
-cell order), keeping the run specification, the time, the per-region fields
-and the totals, plus the numerics and patch conditions that the reference's
-test deck and boundary file state for that run, as rocflu_gb300.refio reads
-them.  Run once where the reference source tree is present:
+"""Writes tests/golden/gas_jump_closed_creconst0_np2.json and
+tests/golden/gas_jump_closed_np2.json from the reference's own goldens of
+the closed gas-jump box (its tests/goldens/box/gas-jump/closed-creconst0/np2
+and closed/np2 golden.json, CRECONSTC 0 and 1: the state the Fortran solver
+reached at t = 1.05e-4 on two ranks, conserved variables per region in the
+region's cell order), keeping the run specification, the time, the
+per-region fields and the totals, plus the numerics and patch conditions
+that the reference's test deck and boundary file state for that run, as
+rocflu_gb300.refio reads them.  Run once where the reference source tree is
+present:
 
     python tests/golden/make_gas_jump_closed.py /root/reference
 """
@@ -19,7 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from rocflu_gb300 import refio  # noqa: E402
 
-SRC = os.path.join("tests", "goldens", "box", "gas-jump", "closed-creconst0", "np2", "golden.json")
+SRCS = {"gas_jump_closed_creconst0_np2.json": os.path.join("tests", "goldens", "box", "gas-jump", "closed-creconst0",
+                                                          "np2", "golden.json"),
+        "gas_jump_closed_np2.json": os.path.join("tests", "goldens", "box", "gas-jump", "closed", "np2", "golden.json")}
 DECK = os.path.join("tests", "templates", "rectshktb.inp")
 
 
@@ -39,15 +43,16 @@ def deck_settings(ref_root, spec):
 
 
 def main(ref_root):
-    with open(os.path.join(ref_root, SRC)) as f:
-        g = json.load(f)
-    out = {"source": SRC, "spec": g["spec"], "time": g["state"]["time"],
-           "gas": g["state"]["gas"], "totals": g["state"]["totals"],
-           "deck": deck_settings(ref_root, g["spec"])}
-    dst = os.path.join(HERE, "gas_jump_closed_creconst0_np2.json")
-    with open(dst, "w") as f:
-        json.dump(out, f, indent=0)
-    print("wrote", dst)
+    for name, src in SRCS.items():
+        with open(os.path.join(ref_root, src)) as f:
+            g = json.load(f)
+        out = {"source": src, "spec": g["spec"], "time": g["state"]["time"],
+               "gas": g["state"]["gas"], "totals": g["state"]["totals"],
+               "deck": deck_settings(ref_root, g["spec"])}
+        dst = os.path.join(HERE, name)
+        with open(dst, "w") as f:
+            json.dump(out, f, indent=0)
+        print("wrote", dst)
 
 
 if __name__ == "__main__":

@@ -152,3 +152,48 @@ def test_burning_injection_constrains_density():
     assert np.abs(g_free).max() == 0.0
     assert np.abs(g_con[:, 0]).max() <= 1e-12
     assert np.abs(g_con[:, 3]).max() > 1e-3
+
+
+def test_closed_gas_jump_golden_with_constrained_gradients():
+    """The reference's own CRECONSTC 1 result (tests/goldens/box/gas-jump/
+    closed/np2, extracted by tests/golden/make_gas_jump_closed.py): the
+    closed gas-jump box with gradients constrained at its six slip walls, run
+    on two ranks.  Its state is not one-dimensional: the two regions'
+    stencils and the ties of the 9-face cut leave a y/z variation of 2e-4 to
+    4e-4 of each field's maximum in density and energy.  The oracle, one
+    region, reaches the golden's y/z mean to within that variation (density
+    and energy within 1.5 times the golden's own spread), 10 times closer in
+    density and energy (3 times in x momentum) than the unconstrained run
+    does."""
+    import json
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from golden import gas_jump
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gas_jump_closed_np2.json")
+    with open(path) as f:
+        g = json.load(f)
+    names = ["q1", "q2", "q3", "q4", "q5"]
+    layers, spread = np.zeros((8, 5)), np.zeros(5)
+    allv = {n: [v for r in g["gas"].values() for v in r[n]] for n in names}
+    mom = max(abs(v) for n in ("q2", "q3", "q4") for v in allv[n])
+    scales = np.array([max(abs(v) for v in allv["q1"]), mom, mom, mom, max(abs(v) for v in allv["q5"])])
+    for region, first in (("1", 4), ("2", 0)):
+        for k, name in enumerate(names):
+            arr = np.array(g["gas"][region][name]).reshape(-1, 4)  # (y, z) rows x 4 layers
+            layers[first:first + 4, k] = arr.mean(axis=0)
+            spread[k] = max(spread[k], np.abs(arr - arr.mean(axis=0)).max() / scales[k])
+    runs = {}
+    for creconst in (1, 0):
+        c = cases.gas_jump_closed()
+        c.num.c_reconst = creconst
+        o = Oracle(c)
+        _, t = o.run(100000, 0.0, c.end_time)
+        assert abs(t - g["time"]) <= 1e-9 * g["time"]
+        cv, _ = o.state()
+        runs[creconst] = np.abs(cv - layers[gas_jump.layer_of_cells(c)]).max(axis=0) / scales
+    assert 1e-4 < spread[0] < 1e-3 and 1e-4 < spread[4] < 1e-3
+    assert runs[1][0] <= 1.5 * spread[0] and runs[1][4] <= 1.5 * spread[4], (runs[1], spread)
+    assert (runs[1][[0, 4]] * 10 <= runs[0][[0, 4]]).all() and runs[1][1] * 3 <= runs[0][1], (runs[1], runs[0])
