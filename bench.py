@@ -21,6 +21,11 @@ RK stages on the device.
   cpu_baseline  the CPU oracle (the FP64 restatement of the reference,
          OpenMP over all host cores) on a bounded sample of the same 128^3
          workload: a few whole steps, plus one step on one thread
+  weno   the same workload with WENO-XYZ smoothing + the simple limiter
+         (RECONST 2, the solver's default), mixed and FP64
+  adjoint, unrolled_adjoint  VJP/primal cost and central-difference checks
+         of the residual's adjoint (tetrahedral case) and of the checkpointed
+         time-unrolled adjoint (64^3 blast)
 
 The working set (state, gradients, face fluxes, geometry: > 0.5 GB) is far
 larger than the 126 MB L2, so no L2 flush is needed between steps.
