@@ -67,6 +67,27 @@ def test_residual_static_matches_allocating_entry(gpu_lib, precision, order, rec
     assert r.status() == status_before
 
 
+@pytest.mark.parametrize("creconst", [0, 1])
+@pytest.mark.parametrize("precision", ["fp64_exact", "mixed"])
+def test_residual_static_open_patches_and_constrained(gpu_lib, precision, creconst):
+    """Inflow, farfield, injection and no-slip patches (their per-patch
+    constants) and the constrained-gradient plan of CRECONSTC 1: context
+    data the static entry reads as the allocating one does."""
+    import torch
+
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_BJ, cfl=0.4,
+                         c_reconst=creconst)
+    c = cases.open_channel(6, num=num, inflow=cases.BC_INFLOW_VELTEMP)
+    r = gpu.Region(c, precision)
+    cv = _state(c, seed=3)
+    ref, _ = r.residual(cv, with_grad=False)
+    cv_dev = torch.from_numpy(cv).cuda()
+    rhs_dev = torch.full_like(cv_dev, float("nan"))
+    torch.cuda.synchronize()
+    r.residual_static(cv_dev.data_ptr(), rhs_dev.data_ptr())
+    np.testing.assert_array_equal(rhs_dev.cpu().numpy(), ref)
+
+
 def test_residual_static_rejects_oversized_mesh(gpu_lib):
     import torch
 
