@@ -24,8 +24,9 @@ RK stages on the device.
   weno   the same workload with WENO-XYZ smoothing + the simple limiter
          (RECONST 2, the solver's default), mixed and FP64
   adjoint, unrolled_adjoint  VJP/primal cost and central-difference checks
-         of the residual's adjoint (tetrahedral case) and of the checkpointed
-         time-unrolled adjoint (64^3 blast)
+         of the residual's adjoint (tetrahedral case; componentwise BJ, the
+         eigen-frame BJ and WENO-XYZ) and of the checkpointed time-unrolled
+         adjoint (64^3 blast)
 
 The working set (state, gradients, face fluxes, geometry: > 0.5 GB) is far
 larger than the 126 MB L2, so no L2 flush is needed between steps.
@@ -70,6 +71,8 @@ def parse():
     p.add_argument("--skip-adjoint", action="store_true")
     p.add_argument("--adj-n", type=int, default=32, help="hexes per side of the tet adjoint case")
     p.add_argument("--only-adjoint", action="store_true", help="time the adjoint case only")
+    p.add_argument("--adj-reconst", type=int, default=100,
+                   help="RECONST of --only-adjoint (100 componentwise BJ, 10 eigen-frame BJ, 2 WENO-XYZ, ...)")
     p.add_argument("--skip-unrolled", action="store_true", help="skip the time-unrolled adjoint case")
     p.add_argument("--skip-weno", action="store_true", help="skip the WENO-XYZ (RECONST 2) variant")
     p.add_argument("--unrolled-n", type=int, default=64, help="hexes per side of the unrolled-adjoint blast")
@@ -257,9 +260,9 @@ def run_ours(args):
     if args.only_adjoint:
         # the adjoint timing alone, on the single-VJP workload (profiling runs
         # of the adjoint kernels), for each precision in --precisions
-        num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=cases.RECONST_BJ_COMP)
+        num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=args.adj_reconst)
         ac = cases.adjoint_tets(args.adj_n, num=num)
-        out = {}
+        out = {"reconst": args.adj_reconst}
         for prec in [x for x in args.precisions.split(",") if x]:
             areg = gpu.Region(ac, prec)
             at = areg.adjoint_times(3)
@@ -373,15 +376,17 @@ def run_ours(args):
 
     # single-residual adjoint: 32^3 x 6 jittered tets, 2nd-order Roe,
     # componentwise Barth-Jespersen (crosses active limiter branches; the
-    # eigenframe limiter has no adjoint, and the reference's
-    # Venkatakrishnan factor jumps from 0 to 1 within |d2| ~ 1e-9, far
-    # inside what an eps = 1e-6 difference resolves)
+    # reference's Venkatakrishnan factor jumps from 0 to 1 within
+    # |d2| ~ 1e-9, far inside what an eps = 1e-6 difference resolves)
     adjoint = None
     if not args.skip_adjoint:
         adjoint = single_adjoint(args, cases, gpu)
         # the headline's limiter: Barth-Jespersen with the eigen-frame
         # velocity limiter (RECONST 10)
         adjoint["eigenframe"] = single_adjoint(args, cases, gpu, reconst=cases.RECONST_BJ, n_dirs=32)
+        # the solver's default reconstruction: WENO-XYZ smoothing with the
+        # simple limiter (RECONST 2)
+        adjoint["weno_xyz"] = single_adjoint(args, cases, gpu, reconst=cases.RECONST_WENO_XYZ, n_dirs=32)
     unrolled = None if args.skip_unrolled else unrolled_adjoint(args, cases, gpu)
     weno = None if args.skip_weno else weno_variant(args, cases, gpu, setup, case.num.dt_imposed)
     tets = None if args.skip_tets else tet_block(args, cases, gpu)
@@ -443,7 +448,8 @@ def single_adjoint(args, cases, gpu, reconst=None, n_dirs=64):
     num = cases.Numerics(space_order=2, space_discr=cases.DISCR_ROE, reconst=reconst)
     ac = cases.adjoint_tets(args.adj_n, num=num)
     areg, mreg = gpu.Region(ac, "fp64"), gpu.Region(ac, "mixed")
-    tag = {cases.RECONST_BJ_COMP: "bjcomp", cases.RECONST_BJ: "bj_eigenframe", cases.RECONST_VENKAT: "venkat"}[reconst]
+    tag = {cases.RECONST_BJ_COMP: "bjcomp", cases.RECONST_BJ: "bj_eigenframe", cases.RECONST_VENKAT: "venkat",
+           cases.RECONST_WENO_XYZ: "wenoxyz"}[reconst]
     out = {"workload": "adjoint_tets%d_roe_%s" % (args.adj_n, tag), "cells": areg.n_cells,
            "functional": "sum_{x=1 patch} p_f |A_f|"}
     rng = np.random.default_rng(2)

@@ -219,11 +219,13 @@ int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *
  * closed form: unlike the pressure recovery it differentiates, it has no
  * cancellation).  The eigen-frame velocity limiter (RECONST 10) is
  * differentiated through its active branch with the eigenvectors' first-
- * order perturbation (the tangent uses the same linearisation); RECONST 1
- * and 2 (WENO smoothing): RFLU_ERR_UNSUPPORTED. */
+ * order perturbation (the tangent uses the same linearisation).  RECONST 1
+ * and 2: the WENO averages are differentiated (weights included) and the
+ * simple limiter through its branch (a zeroed gradient has no derivative);
+ * the smoothing's transpose is a gather over the transposed stencil. */
 int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar);
-/* Tangent of the same residual: rhsDot = (dR/dcv) cvDot (every limiter but
- * the WENO smoothing, RECONST 1 and 2: RFLU_ERR_UNSUPPORTED). */
+/* Tangent of the same residual: rhsDot = (dR/dcv) cvDot (every limiter,
+ * the WENO smoothing included). */
 int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, double *rhsDot);
 /* Diagnostics (no reference counterpart): the limiter's active branches at
  * the host state cv(5,nCells), the branches through which rflu_gpu_vjp and
@@ -232,8 +234,10 @@ int rflu_gpu_jvp(rflu_gpu_ctx *ctx, const double *cv, const double *cvDot, doubl
  * in the reference's summation order (-1: the factor is 1), and the
  * 0-based reference id of the neighbour whose value is the active extreme
  * (-1: none).  RECONST 10 reports its velocity eigen-axes in k = 1..3, the
- * face index times 4 plus the side (1: largest increment, 2: smallest).
- * Second order only (first order: RFLU_ERR_UNSUPPORTED). */
+ * face index times 4 plus the side (1: largest increment, 2: smallest);
+ * RECONST 1 and 2 report -2 as the face of density (k = 0) and pressure
+ * (k = 4) where the simple limiter after the WENO smoothing zeroed the
+ * gradient.  Second order only (first order: RFLU_ERR_UNSUPPORTED). */
 int rflu_gpu_limiter_branches(rflu_gpu_ctx *ctx, const double *cv, int *branches);
 
 /* Boundary-pressure functional J = sum over the faces of patch iPatch
@@ -252,7 +256,7 @@ int rflu_gpu_patch_pressure(rflu_gpu_ctx *ctx, const double *cv, int iPatch, dou
  * be NULL): forward-sweep ms, reverse-sweep ms (recompute + adjoint), device
  * bytes held by the context and the call, number of checkpoints.  Every
  * precision mode (the mixed mode runs its own primal and FP32-Jacobian
- * adjoint); RECONST 1 and 2 have no adjoint.  Leaves the context state untouched. */
+ * adjoint).  Leaves the context state untouched. */
 int rflu_gpu_unrolled_adjoint(rflu_gpu_ctx *ctx, const double *cv0, int nSteps, double dtMin, int every, int iPatch,
                               double *J, double *cvBar0, double *stats);
 

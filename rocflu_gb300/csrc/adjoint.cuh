@@ -97,6 +97,11 @@ inline AdjWork<R> carveAdjWork(double *work, size_t nc, size_t nT) {
   return a;
 }
 
+// WENO smoothing of the gradients (RECONST 1, 2) on a second-order run.
+__host__ __device__ inline bool isWeno(const Params &P) {
+  return P.spaceOrder > 1 && (P.reconst == 1 || P.reconst == 2);
+}
+
 // Primitive state and dependent variables of one cell as functions of cv:
 // RFLU_ConvertCvCons2Prim (DUVWP) and RFLU_SetDependentVars.
 template <typename S>
@@ -196,6 +201,80 @@ __global__ void __launch_bounds__(kBlock) kTanGrad(View<R> V, AdjWork<R> W) {
   Dual<1, R> g[15];
   gradLimitCell(V, TanLoad<R>{V, W}, i, g);
   const size_t n = V.nc;
+  if (isWeno(V.p)) {
+    // the unsmoothed gradient and its derivative, for kTanWeno
+#pragma unroll
+    for (int k = 0; k < 15; ++k) {
+      W.G[k * n + i] = g[k].v;
+      W.Gbar[k * n + i] = g[k].d[0];
+    }
+    return;
+  }
+  R gv[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) {
+    gv[k] = g[k].v;
+    W.gradd[k * n + i] = g[k].d[0];
+  }
+  storeGrad(V, i, gv);
+}
+
+// The simple limiter after the WENO smoothing (RFLU_LimitGradCellsSimple,
+// modflu/RFLU_ModLimiters.F90:1147-1300) on one cell's smoothed gradient g,
+// generic in its scalar type: the zeroing is a branch, so a zeroed
+// gradient's derivative is zero too.  Returns the factors (0 or 1) of
+// density and pressure.
+template <typename R, typename S>
+__device__ inline void wenoPositivity(const View<R> &V, int i, S *g, R *f0, R *f4) {
+  const PlainLoad<R> ld{V};
+  const int cb = V.cfOff[i];
+  const size_t nb = V.nb;
+  const int z = simplePositivity(S(ld.prim(0, i)), S(ld.prim(4, i)), V.cfOff[i + 1] - cb,
+                   [&](int k, S *d) {
+                     const int code = V.cfEnt[cb + k];
+                     R e[3];
+                     if (code >= 0) {
+                       faceOffset(V, code >> 1, code & 1, e);
+                     } else {
+                       const int b = -code - 1;
+                       e[0] = V.bd[b];
+                       e[1] = V.bd[nb + b];
+                       e[2] = V.bd[2 * nb + b];
+                     }
+                     d[0] = S(e[0]);
+                     d[1] = S(e[1]);
+                     d[2] = S(e[2]);
+                     return true;
+                   },
+                   g);
+  *f0 = (z & 1) ? R(0) : R(1);
+  *f4 = (z & 2) ? R(0) : R(1);
+}
+
+// Tangent of the WENO smoothing (RECONST 1, 2): the averages of kWenoSmooth
+// on dual numbers from the unsmoothed gradients and their derivatives
+// (W.G, W.Gbar, written by kTanGrad), then the simple limiter.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kTanWeno(View<R> V, AdjWork<R> W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  using S = Dual<1, R>;
+  const size_t n = V.nc;
+  auto row = [&](int c, S *t) {
+#pragma unroll
+    for (int k = 0; k < 15; ++k) {
+      t[k] = S(W.G[k * n + c]);
+      t[k].d[0] = W.Gbar[k * n + c];
+    }
+  };
+  auto fetch = [&](int s, S *t) { row(V.stIdx[s], t); };
+  const int sb = V.stOff[i], se = V.stOff[i + 1];
+  S own[16], g[15];
+  row(i, own);
+  if (V.p.reconst == 2) wenoXyz(own, sb, se, fetch, g);
+  else wenoSimple(own, sb, se, fetch, g);
+  R f0, f4;
+  wenoPositivity(V, i, g, &f0, &f4);
   R gv[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) {
@@ -653,7 +732,48 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
     velFrameForward(V, ld, i, G, F);
     velFrameApply(F, gl);
   }
-  storeGrad(V, i, gl);
+  // packed layout with WENO smoothing: the unsmoothed gradient as a record
+  // in gradRaw (free outside the primal's gradient phase) for kAdjWenoFwd's
+  // member fetches
+  if (Layout<R>::packed && isWeno(V.p)) storeGradTo(V, V.gradRaw, i, gl);
+  else storeGrad(V, i, gl);
+}
+
+// Forward pass of the WENO smoothing (RECONST 1, 2) for the reverse pass:
+// each cell's smoothed and limited gradient from the unsmoothed ones
+// (written by kAdjGradFwd: W.G, and in the packed layout records in
+// gradRaw) into the view, the simple limiter's factors of density and
+// pressure (0: zeroed) in W.lim, and the weight sums in W.gradd (XYZ: 15 per
+// cell; simple form: 5).
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAdjWenoFwd(View<R> V, AdjWork<R> W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V.nc) return;
+  const size_t n = V.nc;
+  auto row = [&](int c, R *t) {
+    if constexpr (Layout<R>::packed) {
+      ld8(V.gradRaw + 16 * (size_t)c, t);
+      ld8(V.gradRaw + 16 * (size_t)c + 8, t + 8);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) t[k] = W.G[k * n + c];
+    }
+  };
+  auto fetch = [&](int s, R *t) { row(V.stIdx[s], t); };
+  const int sb = V.stOff[i], se = V.stOff[i + 1];
+  R own[16], g[15], sum[15];
+  row(i, own);
+  const bool xyz = V.p.reconst == 2;
+  if (xyz) wenoXyz(own, sb, se, fetch, g, sum);
+  else wenoSimple(own, sb, se, fetch, g, sum);
+  R f0, f4;
+  wenoPositivity(V, i, g, &f0, &f4);
+  W.lim[i] = f0;
+  W.lim[4 * n + i] = f4;
+#pragma unroll
+  for (int k = 0; k < 15; ++k)
+    if (xyz || k < 5) W.gradd[k * n + i] = sum[k];
+  storeGrad(V, i, g);
 }
 
 // Transposed flux Jacobian of one face applied to Fbar.
@@ -781,6 +901,34 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int 
 
 // Side adjoints -> primitive / gradient adjoints of the cell, limiter reverse,
 // gradient own-term.  kVel: with the eigen-frame velocity limiter (RECONST 10).
+// Packed layout: the own term of the LSQ gradient's transpose on the cell's
+// primitive adjoint, and the cell's record L_i Gbar_i for the neighbour terms
+// (kAdjCell2).  w_s = L_i d_s/|d_s|^2 with L_i symmetric: sum_s w_s . Gbar_k
+// = (sum_s d_s/|d_s|^2) . (L_i Gbar_k).
+template <typename R>
+__device__ inline void adjOwnTerm(const View<R> &V, const AdjWork<R> &W, int i, const float *gb, float *qb) {
+  const size_t n = V.nc;
+  const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
+  const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
+  float h[16];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const float x = gb[3 * k], y = gb[3 * k + 1], z = gb[3 * k + 2];
+    h[3 * k] = lxx * x + lxy * y + lxz * z;
+    h[3 * k + 1] = lxy * x + lyy * y + lyz * z;
+    h[3 * k + 2] = lxz * x + lyz * y + lzz * z;
+  }
+  if (V.p.spaceOrder > 1) {
+    const float sx = W.ssum[i], sy = W.ssum[n + i], sz = W.ssum[2 * n + i];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) qb[k] -= sx * h[3 * k] + sy * h[3 * k + 1] + sz * h[3 * k + 2];
+  }
+  h[15] = 0.f;
+  float *rec = W.adjRec + 16 * (size_t)i;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) st4(rec + 4 * q, h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+}
+
 template <typename R, bool kVel>
 __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -919,9 +1067,24 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     for (int j = 0; j < 3; ++j)
       if (F.side[j] != 0 && !F.held[j] && F.nb[j] >= 0) nbAx[j] = F.nb[j];
   }
+  const bool weno = isWeno(P);
+  if (weno) {
+    // WENO smoothing: gb is the adjoint of the smoothed gradient; its terms
+    // over the weight sums go to kAdjWeno, which gathers them over the cells
+    // whose averages hold a cell and applies the gradient's own term there
+    // (packed layout: as a record in gradRaw, whose unsmoothed gradients
+    // kAdjWenoFwd has consumed)
+    R sw[15], a[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) sw[k] = W.gradd[(rc == 2 ? k : k / 3) * n + i];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) a[k] = gb[k] / sw[k];
+    if constexpr (Layout<R>::packed) storeGradTo(V, V.gradRaw, i, a);
+    else storeGradTo(V, W.gradd, i, a);
+  }
   // gradient own-term: G_i = sum_s w_s (q_{m_s} - q_i)
   if constexpr (!Layout<R>::packed) {
-    for (int s = V.stOff[i]; s < V.stOff[i + 1] && P.spaceOrder > 1; ++s) {
+    for (int s = V.stOff[i]; s < V.stOff[i + 1] && P.spaceOrder > 1 && !weno; ++s) {
       R wx, wy, wz;
       lsqWeight(V, i, s, wx, wy, wz);
 #pragma unroll
@@ -929,29 +1092,10 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     }
   }
 #pragma unroll
-  for (int k = 0; k < 15; ++k) W.Gbar[k * n + i] = gb[k];
+  for (int k = 0; k < 15; ++k)
+    if (!weno) W.Gbar[k * n + i] = gb[k];
   if constexpr (Layout<R>::packed) {
-    const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
-    const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
-    float h[16];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      const float x = gb[3 * k], y = gb[3 * k + 1], z = gb[3 * k + 2];
-      h[3 * k] = lxx * x + lxy * y + lxz * z;
-      h[3 * k + 1] = lxy * x + lyy * y + lyz * z;
-      h[3 * k + 2] = lxz * x + lyz * y + lzz * z;
-    }
-    // w_s = L_i d_s/|d_s|^2 with L_i symmetric: sum_s w_s . Gbar_k =
-    // (sum_s d_s/|d_s|^2) . (L_i Gbar_k)
-    if (P.spaceOrder > 1) {
-      const float sx = W.ssum[i], sy = W.ssum[n + i], sz = W.ssum[2 * n + i];
-#pragma unroll
-      for (int k = 0; k < 5; ++k) qb[k] -= sx * h[3 * k] + sy * h[3 * k + 1] + sz * h[3 * k + 2];
-    }
-    h[15] = 0.f;
-    float *rec = W.adjRec + 16 * (size_t)i;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) st4(rec + 4 * q, h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+    if (!weno) adjOwnTerm(V, W, i, gb, qb);
   }
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
@@ -985,6 +1129,94 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) W.dvbar[k * n + i] = dvb[k];
+}
+
+// Reverse of the WENO smoothing (RECONST 1, 2) for cell m, after kAdjCell1:
+// the cell's unsmoothed gradient t enters its own average and those of the
+// cells whose stencils hold it (the transposed stencil).  With a_i cell i's
+// smoothed-gradient adjoint over its weight sums (kAdjCell1, in W.gradd;
+// packed layout: records in gradRaw) and
+// g_i its smoothed gradient, summed over those cells i (m first):
+//   XYZ, per component, w = 1/(t^2 + eps), w' = -2 t w^2:
+//     tbar = (w + w' t) sum a_i - w' sum a_i g_i;
+//   simple form, per variable, W = 1/(T^2 + eps), T = |tx| + |ty| + |tz|,
+//   W' = -2 T W^2:
+//     tbar_d = W sum a_i,d + W' (t . sum a_i - sum a_i . g_i) sgn(t_d)
+//   (sgn(0) = +1, as the tangent's |.|).
+// A gradient the simple limiter zeroed has a_i = 0 there, so the view's
+// limited gradient serves as g_i.  Then the LSQ gradient's own term on the
+// cell's primitive adjoint, and tbar for kAdjCell2's neighbour terms.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= V.nc) return;
+  const size_t n = V.nc;
+  const PlainLoad<R> ld{V};
+  R A[15], B[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) A[k] = B[k] = R(0);
+  auto add = [&](int i) {
+    if constexpr (Layout<R>::packed) {
+      float a[16], g[16];
+      ld8(V.gradRaw + 16 * (size_t)i, a);
+      ld8(V.gradRaw + 16 * (size_t)i + 8, a + 8);
+      ld8(V.grad + 16 * (size_t)i, g);
+      ld8(V.grad + 16 * (size_t)i + 8, g + 8);
+#pragma unroll
+      for (int k = 0; k < 15; ++k) {
+        A[k] += a[k];
+        B[k] += a[k] * g[k];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) {
+        const R a = W.gradd[k * n + i];
+        A[k] += a;
+        B[k] += a * ld.grad(k, i);
+      }
+    }
+  };
+  add(m);
+  for (int e = V.tsOff[m]; e < V.tsOff[m + 1]; ++e) add(V.tsCell[e]);
+  R t[15], tb[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) t[k] = W.G[k * n + m];
+  const R eps = R(1.0e-15);
+  if (V.p.reconst == 2) {
+#pragma unroll
+    for (int k = 0; k < 15; ++k) {
+      const R w = R(1) / (t[k] * t[k] + eps);
+      const R wp = R(-2) * t[k] * w * w;
+      tb[k] = (w + wp * t[k]) * A[k] - wp * B[k];
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const R *tv = t + 3 * v, *av = A + 3 * v, *bv = B + 3 * v;
+      const R T = fabs_(tv[0]) + fabs_(tv[1]) + fabs_(tv[2]);
+      const R w = R(1) / (T * T + eps);
+      const R c = R(-2) * T * w * w * (tv[0] * av[0] + tv[1] * av[1] + tv[2] * av[2] - (bv[0] + bv[1] + bv[2]));
+#pragma unroll
+      for (int d = 0; d < 3; ++d) tb[3 * v + d] = w * av[d] + (tv[d] < R(0) ? -c : c);
+    }
+  }
+  R qb[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) qb[k] = W.qbar[k * n + m];
+  if constexpr (Layout<R>::packed) {
+    adjOwnTerm(V, W, m, tb, qb);
+  } else {
+    for (int s = V.stOff[m]; s < V.stOff[m + 1]; ++s) {
+      R wx, wy, wz;
+      lsqWeight(V, m, s, wx, wy, wz);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) qb[k] -= wx * tb[3 * k] + wy * tb[3 * k + 1] + wz * tb[3 * k + 2];
+    }
+#pragma unroll
+    for (int k = 0; k < 15; ++k) W.Gbar[k * n + m] = tb[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) W.qbar[k * n + m] = qb[k];
 }
 
 // Neighbour terms, then (prim, dv) -> cv; output in reference order.
@@ -1127,8 +1359,10 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
 // out[10 o + 2k + 1] = the reference id of the neighbour whose value is the
 // active extreme (-1: none or the cell itself).  The eigen-frame limiter
 // (RECONST 10) reports its axes in k = 1..3, the face index times 4 plus the
-// side (1: the largest increment, 2: the smallest).  A residual whose every
-// cell keeps these branches is a smooth function of the state.
+// side (1: the largest increment, 2: the smallest).  The WENO smoothing
+// (RECONST 1, 2) reports -2 as the face of density and pressure where its
+// simple limiter zeroed the gradient.  A residual whose every cell keeps
+// these branches is a smooth function of the state.
 template <typename R>
 __global__ void kLimiterBranches(View<R> V, AdjWork<R> W, int *outRef) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1141,6 +1375,12 @@ __global__ void kLimiterBranches(View<R> V, AdjWork<R> W, int *outRef) {
     const int es = W.estar[k * n + i], js = W.jstar[k * n + i];
     out[2 * k] = es >= 0 ? es - cb : -1;
     out[2 * k + 1] = (es >= 0 && js >= 0) ? V.refId[js] : -1;
+  }
+  if (isWeno(V.p)) {
+    // the simple limiter after the WENO smoothing: -2 where it zeroed the
+    // density (k = 0) or the pressure (k = 4) gradient
+    if (W.lim[i] == R(0)) out[0] = -2;
+    if (W.lim[4 * n + i] == R(0)) out[8] = -2;
   }
   if (V.p.reconst == 10 && V.p.spaceOrder > 1) {
     const PlainLoad<R> ld{V};
@@ -1201,16 +1441,19 @@ struct AdjointOps {
     AdjWork<R> W = carveAdjWork<R>(work, V.nc, nT);
     kTanInit<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvDotRef);
     if (V.p.spaceOrder > 1) kTanGrad<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    if (isWeno(V.p)) kTanWeno<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     kTanFlux<R><<<blocks((long long)nT), kBlock, 0, s>>>(V, W);
     kTanGather<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, rhsDotRef);
   }
   static void gradFwd(const View<R> &V, const AdjWork<R> &W, const double *lamRef, cudaStream_t s) {
     if (V.p.reconst == 10) kAdjGradFwd<R, true><<<blocks(V.nc), kBlock, 0, s>>>(V, W, lamRef);
     else kAdjGradFwd<R, false><<<blocks(V.nc), kBlock, 0, s>>>(V, W, lamRef);
+    if (isWeno(V.p)) kAdjWenoFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
   }
   static void cellAdjoint(const View<R> &V, AdjWork<R> &W, double *cvBarRef, cudaStream_t s) {
     if (V.p.reconst == 10 && V.p.spaceOrder > 1) kAdjCell1<R, true><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     else kAdjCell1<R, false><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    if (isWeno(V.p)) kAdjWeno<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     kAdjCell2<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvBarRef);
   }
   static void faceAdjoint(const View<R> &V, const AdjWork<R> &W, cudaStream_t s) {

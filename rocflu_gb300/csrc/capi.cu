@@ -588,8 +588,6 @@ struct Ctx : CtxBase {
   int vjp(const double *cv, const double *rhsBar, double *cvBar) override {
     invalidate();
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
-    if (V.p.reconst == 1 || V.p.reconst == 2)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through WENO smoothing (RECONST 1, 2)");
     if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through constrained gradients (CRECONSTC 1)");
     if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint on a periodic mesh");
     View<R> W;
@@ -604,8 +602,6 @@ struct Ctx : CtxBase {
   int jvp(const double *cv, const double *cvDot, double *rhsDot) override {
     invalidate();
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
-    if (V.p.reconst == 1 || V.p.reconst == 2)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through WENO smoothing (RECONST 1, 2)");
     if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through constrained gradients (CRECONSTC 1)");
     if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent on a periodic mesh");
     View<R> W;
@@ -637,8 +633,6 @@ struct Ctx : CtxBase {
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient on a periodic mesh");
     if (cvBar && V.cSlot)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through constrained gradients (CRECONSTC 1)");
-    if (cvBar && (V.p.reconst == 1 || V.p.reconst == 2))
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through the WENO smoothing (RECONST 1, 2)");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -844,8 +838,6 @@ struct Ctx : CtxBase {
     if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
       return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
-    if (V.p.reconst == 1 || V.p.reconst == 2)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: the WENO smoothing (RECONST 1, 2) has no adjoint");
     if (V.cSlot)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: constrained gradients (CRECONSTC 1) have no adjoint");
     if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint on a periodic mesh");
@@ -978,7 +970,7 @@ struct Ctx : CtxBase {
   int adjointTimes(int nIter, double *ms) override {
     invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
-    if (!ops->vjp || V.p.reconst == 1 || V.p.reconst == 2)
+    if (!ops->vjp || V.cSlot || periodicMesh)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
     if (int rc0 = ensureAdjoint()) return rc0;
     const size_t nc = V.nc;

@@ -208,9 +208,9 @@ __device__ inline void lsqWeight(const View<R> &V, int i, int s, R &wx, R &wy, R
 
 // Store of one cell's gradient record.
 template <typename R>
-__device__ inline void storeGrad(const View<R> &V, int i, const R *g) {
+__device__ inline void storeGradTo(const View<R> &V, R *base, int i, const R *g) {
   if constexpr (Layout<R>::packed) {
-    float *p = V.grad + 16 * (size_t)i;
+    float *p = base + 16 * (size_t)i;
     st4(p, g[0], g[1], g[2], g[3]);
     st4(p + 4, g[4], g[5], g[6], g[7]);
     st4(p + 8, g[8], g[9], g[10], g[11]);
@@ -218,8 +218,12 @@ __device__ inline void storeGrad(const View<R> &V, int i, const R *g) {
   } else {
     const size_t n = V.nc;
 #pragma unroll
-    for (int k = 0; k < 15; ++k) V.grad[k * n + i] = g[k];
+    for (int k = 0; k < 15; ++k) base[k * n + i] = g[k];
   }
+}
+template <typename R>
+__device__ inline void storeGrad(const View<R> &V, int i, const R *g) {
+  storeGradTo(V, V.grad, i, g);
 }
 
 // Store of one cell's primitive record (the packed layout carries the centroid).
@@ -1407,11 +1411,12 @@ __device__ inline void wenoXyzPacked(const float *own, int sb, int se, Fetch fet
     if (q < 7) g[2 * q + 1] = gl[q].y * rcp(sum[q].y);
   }
 }
-// Every mode, XYZ in the reference's operation order.
+// Every mode, XYZ in the reference's operation order; sum receives the
+// weight sums (the reverse pass divides by them).  Generic in R so that the
+// tangent kernels run it on dual numbers.
 template <typename R, typename Fetch>
-__device__ inline void wenoXyz(const R *own, int sb, int se, Fetch fetch, R *g) {
+__device__ inline void wenoXyz(const R *own, int sb, int se, Fetch fetch, R *g, R *sum) {
   const R eps = R(1.0e-15);
-  R sum[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) {
     sum[k] = R(1) / (own[k] * own[k] + eps);
@@ -1430,15 +1435,21 @@ __device__ inline void wenoXyz(const R *own, int sb, int se, Fetch fetch, R *g) 
 #pragma unroll
   for (int k = 0; k < 15; ++k) g[k] = g[k] / sum[k];
 }
-// Every mode, the simple form (one weight per variable from |gx|+|gy|+|gz|,
-// normalised before it is applied) in the reference's operation order.
 template <typename R, typename Fetch>
-__device__ inline void wenoSimple(const R *own, int sb, int se, Fetch fetch, R *g) {
+__device__ inline void wenoXyz(const R *own, int sb, int se, Fetch fetch, R *g) {
+  R sum[15];
+  wenoXyz(own, sb, se, fetch, g, sum);
+}
+// Every mode, the simple form (one weight per variable from |gx|+|gy|+|gz|,
+// normalised before it is applied) in the reference's operation order; sum
+// receives the five weight sums.
+template <typename R, typename Fetch>
+__device__ inline void wenoSimple(const R *own, int sb, int se, Fetch fetch, R *g, R *sum) {
   const R eps = R(1.0e-15);
-  R w0[5], sum[5];
+  R w0[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
-    const R t = fabs(own[3 * v]) + fabs(own[3 * v + 1]) + fabs(own[3 * v + 2]);
+    const R t = fabs_(own[3 * v]) + fabs_(own[3 * v + 1]) + fabs_(own[3 * v + 2]);
     w0[v] = R(1) / (t * t + eps);
     sum[v] = w0[v];
   }
@@ -1447,7 +1458,7 @@ __device__ inline void wenoSimple(const R *own, int sb, int se, Fetch fetch, R *
     fetch(s, t);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
+      const R m = fabs_(t[3 * v]) + fabs_(t[3 * v + 1]) + fabs_(t[3 * v + 2]);
       sum[v] = sum[v] + R(1) / (m * m + eps);
     }
   }
@@ -1462,17 +1473,23 @@ __device__ inline void wenoSimple(const R *own, int sb, int se, Fetch fetch, R *
     fetch(s, t);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const R m = fabs(t[3 * v]) + fabs(t[3 * v + 1]) + fabs(t[3 * v + 2]);
+      const R m = fabs_(t[3 * v]) + fabs_(t[3 * v + 1]) + fabs_(t[3 * v + 2]);
       const R term = (R(1) / (m * m + eps)) / sum[v];
 #pragma unroll
       for (int d = 0; d < 3; ++d) g[3 * v + d] = g[3 * v + d] + term * t[3 * v + d];
     }
   }
 }
+template <typename R, typename Fetch>
+__device__ inline void wenoSimple(const R *own, int sb, int se, Fetch fetch, R *g) {
+  R sum[5];
+  wenoSimple(own, sb, se, fetch, g, sum);
+}
 // RFLU_LimitGradCellsSimple on one cell: face(k, d) gives the cell's k-th
-// face offset d = fc - cofg and returns false past its last face.
+// face offset d = fc - cofg and returns false past its last face.  Returns
+// which gradients it zeroed (1: density, 2: pressure).
 template <typename R, typename Face>
-__device__ inline void simplePositivity(R q0, R q4, int nFaces, Face face, R *g) {
+__device__ inline int simplePositivity(R q0, R q4, int nFaces, Face face, R *g) {
   bool z0 = false, z4 = false;
   for (int k = 0; k < nFaces; ++k) {
     R d[3];
@@ -1482,6 +1499,7 @@ __device__ inline void simplePositivity(R q0, R q4, int nFaces, Face face, R *g)
   }
   if (z0) g[0] = g[1] = g[2] = R(0);
   if (z4) g[12] = g[13] = g[14] = R(0);
+  return (z0 ? 1 : 0) | (z4 ? 2 : 0);
 }
 
 template <typename R>

@@ -1,8 +1,8 @@
 """Tangent (JVP) and discrete adjoint (VJP) of the second-order residual.
 
 * dot-product test: <lambda, J v> = <J^T lambda, v> to round-off, every
-  limiter with an adjoint (none, Venkatakrishnan, componentwise BJ and BJ
-  with the eigen-frame velocity limiter);
+  limiter (none, Venkatakrishnan, componentwise BJ, BJ with the eigen-frame
+  velocity limiter, the simple and XYZ WENO smoothing);
 * FP64 central finite differences (eps = 1e-6) against the VJP: every
   direction along which no cell changes its limiter's active branch between
   U - eps v and U + eps v (rflu_gpu_limiter_branches) agrees to 1e-6; the
@@ -33,7 +33,22 @@ def _dirs(case, k, seed):
     return [rng.standard_normal(case.cv0.shape) * scale for _ in range(k)]
 
 
-ADJ_LIMITERS = [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ]
+WENO = [cases.RECONST_WENO_SIMPLE, cases.RECONST_WENO_XYZ]
+ADJ_LIMITERS = [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ] + WENO
+
+
+def _cd(f, cv, v, eps, richardson):
+    """Central difference of f along v; with richardson, extrapolated from
+    eps and eps/2 so that the eps^2 term cancels.  The XYZ WENO weights
+    1/(t^2 + 1e-15) vary on the scale of the gradient component t itself,
+    and the smallest of the 5760 components of the 4^3-tet case is ~1e-5:
+    a plain difference at eps = 1e-6 moves it by a tenth of itself (errors
+    up to 2e-4); XYZ therefore takes eps = 1e-8 and the extrapolation."""
+    d = (f(cv + eps * v) - f(cv - eps * v)) / (2 * eps)
+    if not richardson:
+        return d
+    h = eps / 2
+    return (4 * (f(cv + h * v) - f(cv - h * v)) / (2 * h) - d) / 3
 
 
 def _switches(r, cv, v, eps):
@@ -76,11 +91,12 @@ def test_tangent_covers_eigen_frame_limiter(gpu_lib):
 
 
 @pytest.mark.parametrize("discr,name", FLUXES)
-@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ])
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ] + WENO)
 def test_vjp_vs_central_differences(gpu_lib, discr, name, reconst):
     """64 random directions, eps = 1e-6 relative to the state's scale:
     <lambda, (R(U+eps v) - R(U-eps v)) / 2 eps> against <J^T lambda, v>.
-    Barth-Jespersen (both forms): every direction that keeps all limiter
+    Barth-Jespersen (both forms) and the WENO smoothing (whose simple
+    limiter is its one branch): every direction that keeps all limiter
     branches agrees to 1e-6, and at least half of the directions keep them.
     Venkatakrishnan has no branch switch to blame: the reference's factor
     divides by (denominator + 1e-12), so it rises from 0 to 1 within
@@ -91,14 +107,18 @@ def test_vjp_vs_central_differences(gpu_lib, discr, name, reconst):
     r = gpu.Region(c, "fp64")
     lam = np.random.default_rng(11).standard_normal(c.cv0.shape)
     g = r.vjp(c.cv0, lam)
-    eps = 1e-6
+    eps = 1e-8 if reconst == cases.RECONST_WENO_XYZ else 1e-6
     errs, sw = [], []
+    f = lambda cv: (lam * r.residual(cv, with_grad=False)[0]).sum()  # noqa: E731
+    # XYZ: the round-off of the extrapolated difference at eps = 1e-8, a few
+    # ulps of the summed |lambda R| over eps, is taken off the error
+    ro = 0.0
+    if reconst == cases.RECONST_WENO_XYZ:
+        ro = 8 * np.finfo(float).eps * np.abs(lam * r.residual(c.cv0, with_grad=False)[0]).sum() / eps
     for v in _dirs(c, 64, 3):
-        rp, _ = r.residual(c.cv0 + eps * v, with_grad=False)
-        rm, _ = r.residual(c.cv0 - eps * v, with_grad=False)
-        fd = (lam * (rp - rm)).sum() / (2 * eps)
+        fd = _cd(f, c.cv0, v, eps, reconst == cases.RECONST_WENO_XYZ)
         ad = (g * v).sum()
-        errs.append(abs(fd - ad) / max(abs(ad), 1e-30))
+        errs.append(max(abs(fd - ad) - ro, 0.0) / max(abs(ad), 1e-30))
         sw.append(_switches(r, c.cv0, v, eps))
     errs, sw = np.array(errs), np.array(sw)
     assert (~sw).sum() >= 32, sw.sum()
@@ -109,31 +129,72 @@ def test_vjp_vs_central_differences(gpu_lib, discr, name, reconst):
         assert (errs[~sw] < 1e-6).all(), (errs[~sw].max(), np.flatnonzero(~sw & (errs >= 1e-6)))
 
 
-@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ])
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ, cases.RECONST_WENO_XYZ])
 def test_patch_pressure_gradient(gpu_lib, reconst):
     c = _case(cases.DISCR_ROE, reconst)
     r = gpu.Region(c, "fp64")
     ip = 1  # x = 1 patch
     J, g = r.patch_pressure(c.cv0, ip)
     assert J > 0
-    eps = 1e-6
+    eps = 1e-8 if reconst == cases.RECONST_WENO_XYZ else 1e-6
+    f = lambda cv: r.patch_pressure(cv, ip, with_grad=False)[0]  # noqa: E731
     for v in _dirs(c, 8, 9):
-        jp, _ = r.patch_pressure(c.cv0 + eps * v, ip, with_grad=False)
-        jm, _ = r.patch_pressure(c.cv0 - eps * v, ip, with_grad=False)
-        fd = (jp - jm) / (2 * eps)
+        fd = _cd(f, c.cv0, v, eps, reconst == cases.RECONST_WENO_XYZ)
         ad = (g * v).sum()
         assert abs(fd - ad) <= 1e-6 * abs(ad) + 1e-12, (fd, ad)
 
 
-def test_adjoint_rejects_weno(gpu_lib):
-    """The WENO smoothing (RECONST 1, 2) has no adjoint or tangent."""
-    for reconst in (cases.RECONST_WENO_SIMPLE, cases.RECONST_WENO_XYZ):
-        c2 = _case(cases.DISCR_ROE, reconst)
-        for prec in ("fp64", "mixed"):
-            with pytest.raises(gpu.RfluError):
-                gpu.Region(c2, prec).vjp(c2.cv0, c2.cv0)
-            with pytest.raises(gpu.RfluError):
-                gpu.Region(c2, prec).jvp(c2.cv0, c2.cv0)
+@pytest.mark.parametrize("reconst", WENO)
+def test_weno_tangent_vs_central_differences(gpu_lib, reconst):
+    """RECONST 1, 2: the tangent through the WENO averages (weights
+    differentiated) against central differences of the residual (XYZ:
+    extrapolated, see _cd) along directions in which the simple limiter
+    zeroes no gradient (it would make the residual non-differentiable)."""
+    c = _case(cases.DISCR_HLLC, reconst)
+    r = gpu.Region(c, "fp64")
+    eps = 1e-8 if reconst == cases.RECONST_WENO_XYZ else 1e-6
+    errs = []
+    f = lambda cv: r.residual(cv, with_grad=False)[0]  # noqa: E731
+    for v in _dirs(c, 4, 5):
+        assert not _switches(r, c.cv0, v, eps)
+        jv = r.jvp(c.cv0, v)
+        fd = _cd(f, c.cv0, v, eps, reconst == cases.RECONST_WENO_XYZ)
+        errs.append(np.abs(fd - jv).max() / np.abs(jv).max())
+    assert max(errs) < 1e-6, errs
+
+
+def test_weno_positivity_zeroing_has_no_derivative(gpu_lib):
+    """A state scaled by 5e-4 + x^2 (density and pressure fall towards x = 0
+    at fixed velocity and temperature; convex, so that a cell's gradient
+    overshoots towards x = 0, and of one sign, which the WENO averages
+    keep): the simple limiter zeroes density and pressure gradients near
+    x = 0 (reported as branch -2).  The tangent and the adjoint stay each
+    other's transpose, and differences along the directions that keep every
+    branch agree with the adjoint."""
+    c = _case(cases.DISCR_HLLC, cases.RECONST_WENO_XYZ)
+    x = gpu.Setup(c).cofg
+    ramp = 5e-4 + x[:, 0] ** 2
+    cv = c.cv0 * ramp[:, None]
+    r = gpu.Region(c, "fp64")
+    b = r.limiter_branches(cv)
+    assert (b[:, 0, 0] == -2).any() and set(np.unique(b[:, :, 0])) <= {-2, -1}
+    rng = np.random.default_rng(2)
+    lam = rng.standard_normal(cv.shape)
+    g = r.vjp(cv, lam)
+    eps = 1e-8
+    f = lambda u: (lam * r.residual(u, with_grad=False)[0]).sum()  # noqa: E731
+    kept = 0
+    for v in _dirs(c, 8, 8):
+        v = v * ramp[:, None]
+        jv = r.jvp(cv, v)
+        a, bb = (lam * jv).sum(), (g * v).sum()
+        assert abs(a - bb) <= 1e-11 * max(abs(a), abs(bb)), (a, bb)
+        if _switches(r, cv, v, eps):
+            continue
+        kept += 1
+        fd = _cd(f, cv, v, eps, True)
+        assert abs(fd - bb) <= 1e-6 * abs(bb), (fd, bb)
+    assert kept >= 4
 
 
 def test_limiter_branches_record(gpu_lib):
@@ -152,6 +213,10 @@ def test_limiter_branches_record(gpu_lib):
             assert set(np.unique(sides)) <= {1, 2} and len(sides) > 0
         else:
             assert (b[:, :, 0] < 4).all()  # tetrahedra: 4 faces
+    # the WENO smoothing limits nothing on this state (no zeroed gradient)
+    c = _case(cases.DISCR_ROE, cases.RECONST_WENO_SIMPLE)
+    b = gpu.Region(c, "fp64").limiter_branches(c.cv0)
+    assert (b == -1).all()
 
 
 # Mixed precision: the adjoint and tangent kernels evaluate the flux,
@@ -178,7 +243,7 @@ def test_mixed_dot_product(gpu_lib, discr, name, reconst):
 
 
 @pytest.mark.parametrize("discr,name", FLUXES)
-@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ])
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_BJ] + WENO)
 def test_mixed_vjp_against_fp64(gpu_lib, discr, name, reconst):
     """The mixed VJP against the FP64 VJP and against FP64 central
     differences (eps = 1e-6) of the FP64 residual on 16 directions: the

@@ -29,7 +29,8 @@ def _dirs(cv0, k, seed):
     return np.stack([rng.standard_normal(cv0.shape) * scale for _ in range(k)])
 
 
-@pytest.mark.parametrize("reconst", [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP])
+@pytest.mark.parametrize("reconst", [cases.RECONST_NONE, cases.RECONST_VENKAT, cases.RECONST_BJ_COMP,
+                                     cases.RECONST_WENO_XYZ])
 def test_gradcheck_residual(gpu_lib, reconst):
     c = _tets(reconst)
     r = gpu.Region(c, "fp64")
@@ -128,7 +129,7 @@ def test_unrolled_adjoint_checkpoint_interval_invariant(gpu_lib):
     assert s1["checkpoints"] == 12 and s5["checkpoints"] == 3
 
 
-@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP])
+@pytest.mark.parametrize("reconst", [cases.RECONST_VENKAT, cases.RECONST_BJ_COMP, cases.RECONST_WENO_XYZ])
 def test_unrolled_adjoint_finite_differences(gpu_lib, reconst):
     """dJ/drho0 along smooth density perturbations against FP64 central
     differences (eps = 1e-6) of the unrolled functional, 20 Wray steps with
@@ -156,14 +157,8 @@ def test_unrolled_adjoint_finite_differences(gpu_lib, reconst):
 
 
 def test_unrolled_adjoint_rejections(gpu_lib):
-    """The WENO smoothing (RECONST 1, 2) has no adjoint; a zero checkpoint
-    interval is an argument error."""
+    """A zero checkpoint interval is an argument error."""
     c = _blast()
-    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_WENO_XYZ)
-    cb = cases.blast_hex(6, num=num)
-    for prec in ("fp64", "mixed"):
-        with pytest.raises(gpu.RfluError):
-            gpu.Region(cb, prec).unrolled_adjoint(cb.cv0, 2, 1e-3, 1, 1)
     with pytest.raises(gpu.RfluError):
         gpu.Region(c, "fp64").unrolled_adjoint(c.cv0, 2, 1e-3, 0, 1)
 
