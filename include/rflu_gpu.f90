@@ -32,6 +32,7 @@ MODULE RFLU_ModGPU
                                RFLU_BC_NOSLIPWALL_TEMP = 71, &
                                RFLU_BC_FARFIELD = 80, &
                                RFLU_BC_INJECTION = 90, &
+                               RFLU_BC_SYMMETRY = 100, &
                                RFLU_BC_PERIODIC = 110
   INTEGER(C_INT), PARAMETER :: RFLU_BCDAT_N = 8, &
                                RFLU_BCSWI_N = 2
@@ -61,6 +62,9 @@ MODULE RFLU_ModGPU
     TYPE(C_PTR) :: patchSwitches
     TYPE(C_PTR) :: fc2
     TYPE(C_PTR) :: c2csShift
+    TYPE(C_PTR) :: c2csXf
+    INTEGER(C_INT) :: nXf
+    TYPE(C_PTR) :: xfQ
   END TYPE rflu_grid_desc
 
   TYPE, BIND(C) :: rflu_num_desc

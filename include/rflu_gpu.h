@@ -49,6 +49,7 @@ extern "C" {
 #define RFLU_BC_NOSLIPWALL_TEMP 71
 #define RFLU_BC_FARFIELD 80
 #define RFLU_BC_INJECTION 90
+#define RFLU_BC_SYMMETRY 100      /* planar mirror patches: a face is an interior face to the cell's reflection */
 #define RFLU_BC_PERIODIC 110      /* translational pairs: no boundary faces left (rflu_setup_build identifies them) */
 /* Per-patch boundary values and switches (pPatch%mixt%vals(:,0) and
  * pPatch%mixt%switches, modfloflu/ModParameters.F90:452-511), uniform over
@@ -96,6 +97,15 @@ typedef struct {
    * a member's offset is cofg(member) - cofg(cell) + c2csShift */
   const double *fc2;        /* (3,nFaces) */
   const double *c2csShift;  /* (3,c2csOff[nCells]) */
+  /* symmetry patches (may be NULL / 0: none; RFLU_ModSymmetryPeriodic's
+   * virtual cells): a stencil member seen through the reflections across
+   * one or more symmetry planes carries the index of that reflection
+   * (-1: none) and, in c2csShift, the offset of its reflected centroid from
+   * its own; its velocity is Q u with Q the reflection's 3x3 matrix, its
+   * density and pressure its own. */
+  const int *c2csXf;        /* (c2csOff[nCells]) */
+  int nXf;
+  const double *xfQ;        /* (3,3,nXf), row-major per reflection */
 } rflu_grid_desc;
 
 /* Numerics, the reference input deck keys (libfloflu/ReadNumericsSection.F90,

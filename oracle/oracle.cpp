@@ -193,6 +193,16 @@ struct orc_ctx {
      for a periodic face, else fc) */
   std::vector<double> fn, fc, fc2, vol, cofg;
   std::vector<Patch> patches;
+  /* symmetry (mirror) patches: the cells near them are also seen reflected
+     across them, as images with ids nCells + k in the stencils (stIdx):
+     the image's real cell, its reflection (an index into xfQ, the velocity
+     reflections, 9 values row-major), its centroid and its vertices (ids
+     past nVert for vertices off the reflecting planes); patchXf: each
+     symmetry patch's own reflection (-1 for the other patches) */
+  std::vector<int> imgCell, imgXf, imgC2v, patchXf;
+  std::vector<double> imgPos;
+  std::vector<std::array<double, 9>> xfQ;
+  int nVertExt = 0;
   std::vector<int> stOff, stIdx;
   std::vector<double> moms;
   /* CRECONSTC 1: the boundary-face stencil (global boundary face index) */
@@ -314,9 +324,10 @@ void identifyPeriodicVertices(orc_ctx *c) {
  * of j nearest to i when the mesh is periodic (the virtual cell standing for
  * j in the reference). */
 void memberOffset(const orc_ctx *c, int i, int j, double &dx, double &dy, double &dz) {
-  dx = c->cofg[3 * j] - c->cofg[3 * i];
-  dy = c->cofg[3 * j + 1] - c->cofg[3 * i + 1];
-  dz = c->cofg[3 * j + 2] - c->cofg[3 * i + 2];
+  const double *xj = (j < c->nCells) ? &c->cofg[3 * j] : &c->imgPos[3 * (size_t)(j - c->nCells)];
+  dx = xj[0] - c->cofg[3 * i];
+  dy = xj[1] - c->cofg[3 * i + 1];
+  dz = xj[2] - c->cofg[3 * i + 2];
   if (c->perShift.empty()) return;
   double best = dx * dx + dy * dy + dz * dz, bx = dx, by = dy, bz = dz;
   const int np = (int)c->perShift.size();
@@ -336,6 +347,283 @@ void memberOffset(const orc_ctx *c, int i, int j, double &dx, double &dy, double
     if (d2 < best) { best = d2; bx = ex; by = ey; bz = ez; }
   }
   dx = bx; dy = by; dz = bz;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Symmetry (mirror) patches (BC_SYMMETRY).  The reference copies the cells  */
+/* near each symmetry patch as virtual cells reflected across it (and copies */
+/* of earlier patches' virtual cells near it, which makes the corner images) */
+/* (modflu/RFLU_ModSymmetryPeriodic.F90:148-335, 471-787), sets their state  */
+/* from the actual cells with the momentum reflected (modflu/               */
+/* RFLU_ModRelatedPatches.F90:268-353) and, after the gradients, their       */
+/* gradients transformed (:380-435: Q g for density and pressure, Q G Q^T   */
+/* for the velocity gradient).  A face on the patch is an interior face to   */
+/* its virtual cell: the limiters see the reflected cell as a neighbour, the */
+/* time step counts the face as interior, and the flux is the interior flux  */
+/* against the reflected state.  Here each patch must be planar, two patches */
+/* parallel or perpendicular; the images are the cells within three vertex  */
+/* layers of a patch, reflected across every set of such patches without   */
+/* two parallel ones, and their vertices off the reflecting planes get new  */
+/* ids, so that the stencils grow across the planes as over virtual cells.  */
+/* An image's state and gradients are its cell's, reflected; the reference's */
+/* virtual cells compute raw gradients of their own from their (truncated)   */
+/* stencils, which only the WENO smoothing of the cells next to the patch   */
+/* reads (libfloflu/RungeKuttaMP.F90:225-236); the images here carry the     */
+/* reflected raw gradients instead.                                          */
+/* ------------------------------------------------------------------------ */
+const int kSymLayers = 3;
+
+/* y = Q x for a row-major Q, summed in index order */
+inline void reflect3(const double *Q, const double *x, double *y) {
+  for (int a = 0; a < 3; ++a) {
+    double s = Q[3 * a] * x[0];
+    s = s + Q[3 * a + 1] * x[1];
+    s = s + Q[3 * a + 2] * x[2];
+    y[a] = s;
+  }
+}
+
+void buildSymmetryImages(orc_ctx *c) {
+  const int nc = c->nCells, nvc = c->nvc;
+  struct Plane { int patch; double n[3], p0[3]; };
+  std::vector<Plane> planes;
+  c->patchXf.assign(c->patches.size(), -1);
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int v = 0; v < c->nVert; ++v)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], c->xyz[3 * v + d]);
+      hi[d] = std::max(hi[d], c->xyz[3 * v + d]);
+    }
+  const double tol = 1e-7 * std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  for (int ip = 0; ip < (int)c->patches.size(); ++ip) {
+    const Patch &p = c->patches[ip];
+    if (p.bcType != ORC_BC_SYMMETRY || p.n == 0) continue;
+    Plane P;
+    P.patch = ip;
+    for (int d = 0; d < 3; ++d) { P.n[d] = p.fn[d]; P.p0[d] = p.fc[d]; }
+    for (int i = 0; i < p.n; ++i) {
+      const double cosA = p.fn[4 * i] * P.n[0] + p.fn[4 * i + 1] * P.n[1] + p.fn[4 * i + 2] * P.n[2];
+      for (int k = 0; k < 4; ++k) {
+        const int v = p.bf2v[4 * i + k];
+        if (v < 0) continue;
+        const double h = (c->xyz[3 * v] - P.p0[0]) * P.n[0] + (c->xyz[3 * v + 1] - P.p0[1]) * P.n[1] +
+                         (c->xyz[3 * v + 2] - P.p0[2]) * P.n[2];
+        if (std::fabs(h) > tol || cosA < 1.0 - 1e-10) {
+          std::fprintf(stderr, "oracle: symmetry patch %d is not planar\n", ip);
+          std::abort();
+        }
+      }
+    }
+    planes.push_back(P);
+  }
+  const int np = (int)planes.size();
+  if (np == 0) return;
+  if (np > 30) { std::fprintf(stderr, "oracle: more than 30 symmetry patches\n"); std::abort(); }
+  std::vector<int> parallel(np, 0);  /* bit q of parallel[a]: planes a and q are parallel */
+  for (int a = 0; a < np; ++a)
+    for (int q = 0; q < np; ++q) {
+      if (q == a) continue;
+      const double d = std::fabs(planes[a].n[0] * planes[q].n[0] + planes[a].n[1] * planes[q].n[1] +
+                                 planes[a].n[2] * planes[q].n[2]);
+      if (d > 1.0 - 1e-10) parallel[a] |= 1 << q;
+      else if (d > 1e-10) {
+        std::fprintf(stderr, "oracle: symmetry patches %d and %d are neither parallel nor perpendicular\n",
+                     planes[a].patch, planes[q].patch);
+        std::abort();
+      }
+    }
+  /* vertices on each plane (its patch's vertices), cells near it */
+  std::vector<int> vmask(c->nVert, 0), nearMask(nc, 0);
+  std::vector<int> v2cOff(c->nVert + 1, 0), v2c;
+  for (int ic = 0; ic < nc; ++ic)
+    for (int k = 0; k < nvc; ++k) v2cOff[c->c2v[nvc * ic + k] + 1]++;
+  for (int v = 0; v < c->nVert; ++v) v2cOff[v + 1] += v2cOff[v];
+  v2c.resize(v2cOff[c->nVert]);
+  {
+    std::vector<int> fill(v2cOff.begin(), v2cOff.end() - 1);
+    for (int ic = 0; ic < nc; ++ic)
+      for (int k = 0; k < nvc; ++k) v2c[fill[c->c2v[nvc * ic + k]]++] = ic;
+  }
+  for (int a = 0; a < np; ++a) {
+    const Patch &p = c->patches[planes[a].patch];
+    std::vector<char> vIn(c->nVert, 0), cIn(nc, 0);
+    std::vector<int> front;
+    for (int i = 0; i < p.n; ++i)
+      for (int k = 0; k < 4; ++k) {
+        const int v = p.bf2v[4 * i + k];
+        if (v < 0) continue;
+        vmask[v] |= 1 << a;
+        if (!vIn[v]) { vIn[v] = 1; front.push_back(v); }
+      }
+    for (int layer = 0; layer < kSymLayers; ++layer) {
+      std::vector<int> next;
+      for (int v : front)
+        for (int e = v2cOff[v]; e < v2cOff[v + 1]; ++e) {
+          const int ic = v2c[e];
+          if (cIn[ic]) continue;
+          cIn[ic] = 1;
+          nearMask[ic] |= 1 << a;
+          for (int k = 0; k < nvc; ++k) {
+            const int w = c->c2v[nvc * ic + k];
+            if (!vIn[w]) { vIn[w] = 1; next.push_back(w); }
+          }
+        }
+      front.swap(next);
+    }
+  }
+  /* images: (cell, plane set) in the order of the set's highest plane, the
+     set, then the cell (the reference adds virtual cells patch by patch) */
+  struct Img { int top, set, cell; };
+  std::vector<Img> imgs;
+  for (int ic = 0; ic < nc; ++ic) {
+    const int m = nearMask[ic];
+    for (int S = m; S > 0; S = (S - 1) & m) {
+      bool ok = true;
+      for (int a = 0; a < np && ok; ++a)
+        if ((S >> a & 1) && (S & parallel[a])) ok = false;
+      if (!ok) continue;
+      int top = 0;
+      while ((S >> (top + 1)) != 0) ++top;
+      imgs.push_back({top, S, ic});
+    }
+  }
+  std::sort(imgs.begin(), imgs.end(), [](const Img &x, const Img &y) {
+    if (x.top != y.top) return x.top < y.top;
+    if (x.set != y.set) return x.set < y.set;
+    return x.cell < y.cell;
+  });
+  /* reflections: one per plane set, Q_S = Q_a1 Q_a2 ... in plane order */
+  std::map<int, int> xfOf;
+  auto planeQ = [&](int a, double *Q) {
+    const double nx = planes[a].n[0], ny = planes[a].n[1], nz = planes[a].n[2];
+    Q[0] = 1.0 - 2.0 * nx * nx; Q[1] = -2.0 * nx * ny;      Q[2] = -2.0 * nx * nz;
+    Q[3] = Q[1];                Q[4] = 1.0 - 2.0 * ny * ny; Q[5] = -2.0 * ny * nz;
+    Q[6] = Q[2];                Q[7] = Q[5];                Q[8] = 1.0 - 2.0 * nz * nz;
+  };
+  auto xfIndex = [&](int S) {
+    auto it = xfOf.find(S);
+    if (it != xfOf.end()) return it->second;
+    std::array<double, 9> Q;
+    bool first = true;
+    for (int a = 0; a < np; ++a) {
+      if (!(S >> a & 1)) continue;
+      double Qa[9];
+      planeQ(a, Qa);
+      if (first) {
+        for (int k = 0; k < 9; ++k) Q[k] = Qa[k];
+        first = false;
+      } else {
+        std::array<double, 9> P;
+        for (int r = 0; r < 3; ++r)
+          for (int col = 0; col < 3; ++col) {
+            double s = Q[3 * r] * Qa[col];
+            s = s + Q[3 * r + 1] * Qa[3 + col];
+            s = s + Q[3 * r + 2] * Qa[6 + col];
+            P[3 * r + col] = s;
+          }
+        Q = P;
+      }
+    }
+    const int idx = (int)c->xfQ.size();
+    c->xfQ.push_back(Q);
+    xfOf[S] = idx;
+    return idx;
+  };
+  for (int a = 0; a < np; ++a) c->patchXf[planes[a].patch] = xfIndex(1 << a);
+  std::map<std::pair<int, int>, int> vext;
+  int nextV = c->nVert;
+  for (const Img &im : imgs) {
+    c->imgCell.push_back(im.cell);
+    c->imgXf.push_back(xfIndex(im.set));
+    double x[3] = {c->cofg[3 * im.cell], c->cofg[3 * im.cell + 1], c->cofg[3 * im.cell + 2]};
+    for (int a = 0; a < np; ++a) {
+      if (!(im.set >> a & 1)) continue;
+      const double *n = planes[a].n, *p0 = planes[a].p0;
+      const double h = (x[0] - p0[0]) * n[0] + (x[1] - p0[1]) * n[1] + (x[2] - p0[2]) * n[2];
+      for (int d = 0; d < 3; ++d) x[d] = x[d] - 2.0 * h * n[d];
+    }
+    for (int d = 0; d < 3; ++d) c->imgPos.push_back(x[d]);
+    for (int k = 0; k < nvc; ++k) {
+      const int v = c->c2v[nvc * im.cell + k];
+      const int S = im.set & ~vmask[v];
+      if (S == 0) {
+        c->imgC2v.push_back(v);
+        continue;
+      }
+      auto it = vext.find({v, S});
+      if (it == vext.end()) it = vext.emplace(std::make_pair(v, S), nextV++).first;
+      c->imgC2v.push_back(it->second);
+    }
+  }
+  c->nVertExt = nextV;
+}
+
+/* A stencil member's primitive state (rho, u, v, w, p) and raw gradient:
+ * its cell's, reflected for an image. */
+inline void memberVar(const orc_ctx *c, const std::vector<double> &var, int j, double *out) {
+  if (j < c->nCells) {
+    for (int k = 0; k < 5; ++k) out[k] = var[5 * (size_t)j + k];
+    return;
+  }
+  const int cell = c->imgCell[j - c->nCells];
+  const double *v = &var[5 * (size_t)cell];
+  out[0] = v[0];
+  reflect3(c->xfQ[c->imgXf[j - c->nCells]].data(), v + 1, out + 1);
+  out[4] = v[4];
+}
+inline void transformGrad(const double *Q, const double *g, double *o) {
+  reflect3(Q, g, o);
+  reflect3(Q, g + 12, o + 12);
+  /* velocity gradient G[a][c] = g[3 (1 + a) + c]: Q (G Q^T) */
+  double T[9];
+  for (int b = 0; b < 3; ++b)
+    for (int col = 0; col < 3; ++col) {
+      double s = g[3 * (1 + b)] * Q[3 * col];
+      s = s + g[3 * (1 + b) + 1] * Q[3 * col + 1];
+      s = s + g[3 * (1 + b) + 2] * Q[3 * col + 2];
+      T[3 * b + col] = s;
+    }
+  for (int a = 0; a < 3; ++a)
+    for (int col = 0; col < 3; ++col) {
+      double s = Q[3 * a] * T[col];
+      s = s + Q[3 * a + 1] * T[3 + col];
+      s = s + Q[3 * a + 2] * T[6 + col];
+      o[3 * (1 + a) + col] = s;
+    }
+}
+inline void memberGrad(const orc_ctx *c, const std::vector<double> &grad, int j, double *out) {
+  if (j < c->nCells) {
+    for (int k = 0; k < 15; ++k) out[k] = grad[15 * (size_t)j + k];
+    return;
+  }
+  transformGrad(c->xfQ[c->imgXf[j - c->nCells]].data(), &grad[15 * (size_t)c->imgCell[j - c->nCells]], out);
+}
+/* the symmetry patch of a boundary face entry (code < 0) of a cell's face
+   list, else -1 */
+inline int symmetryPatchOf(const orc_ctx *c, int code) {
+  if (code >= 0 || c->patchXf.empty()) return -1;
+  const int ip = c->bPatch[-code - 1];
+  return c->patchXf[ip] >= 0 ? ip : -1;
+}
+/* The centroid the limiters' second face loop takes for a face entry of a
+   cell: an interior face's (in the cell's frame), a symmetry patch face's
+   (an interior face to the cell's reflection), else none. */
+inline const double *limiterFaceCentroid(const orc_ctx *c, int code) {
+  if (code >= 0) {
+    const int f = code >> 1;
+    return (code & 1) ? &c->fc2[3 * f] : &c->fc[3 * f];
+  }
+  const int ip = symmetryPatchOf(c, code);
+  if (ip < 0) return nullptr;
+  return &c->patches[ip].fc[3 * c->bFace[-code - 1]];
+}
+/* the cell's own state reflected across symmetry patch ip (its virtual
+   neighbour across a face of the patch) */
+inline void mirrorVar(const orc_ctx *c, const std::vector<double> &var, int ic, int ip, double *out) {
+  const double *v = &var[5 * (size_t)ic];
+  out[0] = v[0];
+  reflect3(c->xfQ[c->patchXf[ip]].data(), v + 1, out + 1);
+  out[4] = v[4];
 }
 
 /* ------------------------------------------------------------------------ */
@@ -560,15 +848,18 @@ void buildGeometry(orc_ctx *c) {
 void buildStencils(orc_ctx *c) {
   const int nc = c->nCells, nvc = c->nvc;
   const int stencilSizeMin = 4, stencilSizeMax = 40, nLayersMax = 6;
-  std::vector<int> v2cOff(c->nVert + 1, 0), v2c;
-  for (int ic = 0; ic < nc; ++ic)
-    for (int k = 0; k < nvc; ++k) v2cOff[c->c2v[nvc * ic + k] + 1]++;
-  for (int v = 0; v < c->nVert; ++v) v2cOff[v + 1] += v2cOff[v];
-  v2c.resize(v2cOff[c->nVert]);
+  /* the cells and the symmetry images (ids nc + k) with their vertices */
+  const int ne = nc + (int)c->imgCell.size(), nve = std::max(c->nVert, c->nVertExt);
+  auto cellVert = [&](int e, int k) { return e < nc ? c->c2v[nvc * e + k] : c->imgC2v[nvc * (size_t)(e - nc) + k]; };
+  std::vector<int> v2cOff(nve + 1, 0), v2c;
+  for (int ic = 0; ic < ne; ++ic)
+    for (int k = 0; k < nvc; ++k) v2cOff[cellVert(ic, k) + 1]++;
+  for (int v = 0; v < nve; ++v) v2cOff[v + 1] += v2cOff[v];
+  v2c.resize(v2cOff[nve]);
   {
     std::vector<int> fill(v2cOff.begin(), v2cOff.end() - 1);
-    for (int ic = 0; ic < nc; ++ic)
-      for (int k = 0; k < nvc; ++k) v2c[fill[c->c2v[nvc * ic + k]]++] = ic;
+    for (int ic = 0; ic < ne; ++ic)
+      for (int k = 0; k < nvc; ++k) v2c[fill[cellVert(ic, k)]++] = ic;
   }
   const double iNVert = 1.0 / (double)nvc;
   c->stOff.assign(nc + 1, 0);
@@ -593,7 +884,7 @@ void buildStencils(orc_ctx *c) {
     frac.resize(nCells2);
     for (int i = 0; i < nCells2; ++i) {
       int vT2[8];
-      for (int k = 0; k < nvc; ++k) vT2[k] = c->c2v[nvc * tmp[i] + k];
+      for (int k = 0; k < nvc; ++k) vT2[k] = cellVert(tmp[i], k);
       std::sort(vT2, vT2 + nvc);
       int nCommon = 0, a = 0, b = 0;
       while (a < nvc && b < nvc) {
@@ -638,7 +929,7 @@ void buildStencils(orc_ctx *c) {
         for (int isl = beg; isl <= end && !stop; ++isl) {
           int m = c2cs[isl - 1];
           for (int k = 0; k < nvc && !stop; ++k) {
-            int v = c->c2v[nvc * m + k];
+            int v = cellVert(m, k);
             for (int j = v2cOff[v]; j < v2cOff[v + 1]; ++j) {
               int icg2 = v2c[j];
               if (icg2 == icg) continue;
@@ -750,8 +1041,10 @@ void computeGradCells(orc_ctx *c, const std::vector<double> &var, std::vector<do
       double wtx = term * (term1 + c12 * term2 + c13 * term3);
       double wty = term * (term2 + c23 * term3);
       double wtz = term * (term3);
+      double vj[5];
+      memberVar(c, var, j, vj);
       for (int iv = 0; iv < 5; ++iv) {
-        double dVar = var[5 * j + iv] - var[5 * icg + iv];
+        double dVar = vj[iv] - var[5 * icg + iv];
         g[3 * iv] = g[3 * iv] + wtx * dVar;
         g[3 * iv + 1] = g[3 * iv + 1] + wty * dVar;
         g[3 * iv + 2] = g[3 * iv + 2] + wtz * dVar;
@@ -772,11 +1065,19 @@ void neighbourExtremes(orc_ctx *c, const std::vector<double> &var, std::vector<d
   for (int ic = 0; ic < c->nCells; ++ic) {
     for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
       const int code = c->cfEnt[e];
-      if (code < 0) continue;
-      const int other = c->f2c[(code & ~1) + 1 - (code & 1)];
+      double vother[5];
+      if (code < 0) {
+        /* a face on a symmetry patch: the neighbour is the reflected cell */
+        const int ip = symmetryPatchOf(c, code);
+        if (ip < 0) continue;
+        mirrorVar(c, var, ic, ip, vother);
+      } else {
+        const int other = c->f2c[(code & ~1) + 1 - (code & 1)];
+        for (int iv = 0; iv < 5; ++iv) vother[iv] = var[5 * other + iv];
+      }
       for (int iv = 0; iv < 5; ++iv) {
         if (skipVel && iv >= 1 && iv <= 3) continue;
-        double vo = var[5 * other + iv];
+        double vo = vother[iv];
         vmin[5 * ic + iv] = fmin2(vmin[5 * ic + iv], vo);
         vmax[5 * ic + iv] = fmax2(vmax[5 * ic + iv], vo);
       }
@@ -797,9 +1098,8 @@ void limiterBarthJesp(orc_ctx *c, const std::vector<double> &var, const std::vec
   for (int ic = 0; ic < nc; ++ic) {
     for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
       const int code = c->cfEnt[e];
-      if (code < 0) continue;
-      const int f = code >> 1;
-      const double *fcs = (code & 1) ? &c->fc2[3 * f] : &c->fc[3 * f];
+      const double *fcs = limiterFaceCentroid(c, code);
+      if (!fcs) continue;
       double xc = fcs[0], yc = fcs[1], zc = fcs[2];
       double dx1 = c->cofg[3 * ic] - xc, dy1 = c->cofg[3 * ic + 1] - yc, dz1 = c->cofg[3 * ic + 2] - zc;
       for (int iv = 0; iv < 5; ++iv) {
@@ -833,9 +1133,8 @@ void limiterVenkat(orc_ctx *c, const std::vector<double> &var, const std::vector
   for (int ic = 0; ic < nc; ++ic) {
     for (int e = c->cfOff[ic]; e < c->cfOff[ic + 1]; ++e) {
       const int code = c->cfEnt[e];
-      if (code < 0) continue;
-      const int f = code >> 1;
-      const double *fcs = (code & 1) ? &c->fc2[3 * f] : &c->fc[3 * f];
+      const double *fcs = limiterFaceCentroid(c, code);
+      if (!fcs) continue;
       double xc = fcs[0], yc = fcs[1], zc = fcs[2];
       double dx1 = c->cofg[3 * ic] - xc, dy1 = c->cofg[3 * ic + 1] - yc, dz1 = c->cofg[3 * ic + 2] - zc;
       double ds1 = std::pow(c->vol[ic], THRD);
@@ -923,6 +1222,9 @@ void wenoGradCells(orc_ctx *c, std::vector<double> &grad, bool xyz) {
 #pragma omp parallel for schedule(static)
   for (int icg = 0; icg < nc; ++icg) {
     const int sb = c->stOff[icg], se = c->stOff[icg + 1];
+    /* the members' raw gradients (reflected for symmetry images) */
+    std::vector<double> mg(15 * (size_t)(se - sb));
+    for (int s = sb; s < se; ++s) memberGrad(c, grad, c->stIdx[s], &mg[15 * (size_t)(s - sb)]);
     for (int iv = 0; iv < 5; ++iv) {
       const double *g0 = &grad[15 * icg + 3 * iv];
       double *o = &out[15 * icg + 3 * iv];
@@ -932,7 +1234,7 @@ void wenoGradCells(orc_ctx *c, std::vector<double> &grad, bool xyz) {
           double sum = 1.0 / (term * term + 1.0e-15);
           double gl = sum * term;
           for (int s = sb; s < se; ++s) {
-            term = grad[15 * c->stIdx[s] + 3 * iv + d];
+            term = mg[15 * (size_t)(s - sb) + 3 * iv + d];
             double w = 1.0 / (term * term + 1.0e-15);
             sum = sum + w;
             gl = gl + w * term;
@@ -944,7 +1246,7 @@ void wenoGradCells(orc_ctx *c, std::vector<double> &grad, bool xyz) {
         const double w0 = 1.0 / (term * term + 1.0e-15);
         double sum = w0;
         for (int s = sb; s < se; ++s) {
-          const double *gj = &grad[15 * c->stIdx[s] + 3 * iv];
+          const double *gj = &mg[15 * (size_t)(s - sb) + 3 * iv];
           term = std::fabs(gj[0]) + std::fabs(gj[1]) + std::fabs(gj[2]);
           sum = sum + 1.0 / (term * term + 1.0e-15);
         }
@@ -953,7 +1255,7 @@ void wenoGradCells(orc_ctx *c, std::vector<double> &grad, bool xyz) {
         o[1] = term * g0[1];
         o[2] = term * g0[2];
         for (int s = sb; s < se; ++s) {
-          const double *gj = &grad[15 * c->stIdx[s] + 3 * iv];
+          const double *gj = &mg[15 * (size_t)(s - sb) + 3 * iv];
           double t = std::fabs(gj[0]) + std::fabs(gj[1]) + std::fabs(gj[2]);
           term = (1.0 / (t * t + 1.0e-15)) / sum;
           o[0] = o[0] + term * gj[0];
@@ -1018,11 +1320,21 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
   for (int icl = 0; icl < nc; ++icl) {
     for (int e = c->cfOff[icl]; e < c->cfOff[icl + 1]; ++e) {
       const int code = c->cfEnt[e];
-      if (code < 0) continue;
-      const int f = code >> 1, side = code & 1;
-      int cc[2] = {c->f2c[2 * f], c->f2c[2 * f + 1]};
       double du[3];
-      for (int k = 0; k < 3; ++k) du[k] = var[5 * cc[1] + 1 + k] - var[5 * cc[0] + 1 + k];
+      int side = 0;
+      if (code < 0) {
+        /* a symmetry patch face: the reflected cell as the second cell */
+        const int ip = symmetryPatchOf(c, code);
+        if (ip < 0) continue;
+        double vm[5];
+        mirrorVar(c, var, icl, ip, vm);
+        for (int k = 0; k < 3; ++k) du[k] = vm[1 + k] - var[5 * icl + 1 + k];
+      } else {
+        const int f = code >> 1;
+        side = code & 1;
+        int cc[2] = {c->f2c[2 * f], c->f2c[2 * f + 1]};
+        for (int k = 0; k < 3; ++k) du[k] = var[5 * cc[1] + 1 + k] - var[5 * cc[0] + 1 + k];
+      }
       for (int j = 0; j < 3; ++j) {
         const double *a = &axes[9 * icl + 3 * j];
         double proj = 0.0;
@@ -1037,9 +1349,8 @@ void limitGradVelocityBarthJesp(orc_ctx *c, const std::vector<double> &var, std:
   for (int icl = 0; icl < nc; ++icl) {
     for (int e = c->cfOff[icl]; e < c->cfOff[icl + 1]; ++e) {
       const int code = c->cfEnt[e];
-      if (code < 0) continue;
-      const int f = code >> 1;
-      const double *fcs = (code & 1) ? &c->fc2[3 * f] : &c->fc[3 * f];
+      const double *fcs = limiterFaceCentroid(c, code);
+      if (!fcs) continue;
       double off[3];
       for (int k = 0; k < 3; ++k) off[k] = c->cofg[3 * icl + k] - fcs[k];
       double shift[3];
@@ -1137,6 +1448,7 @@ void buildBFaceStencil(orc_ctx *c) {
     bool done = false;
     for (int isl = 0; isl <= c->stOff[icg + 1] - c->stOff[icg] && !done; ++isl) {
       const int isg = (isl == 0) ? icg : c->stIdx[c->stOff[icg] + isl - 1];
+      if (isg >= nc) continue;  /* symmetry images: no constrained faces here (refused with walls) */
       for (int ip = 0; ip < np && !done; ++ip) {
         if (last[ip].empty() || last[ip][isg] < 0) continue;
         if (n < 18) {
@@ -1481,44 +1793,42 @@ void ausmFlux(double nx, double ny, double nz, double nm, double fs, double rl, 
   flx[4] = (af * (mfp * rl * Hl + mfm * rr * Hr) + pf * fs) * nm;
 }
 
-void interiorFlux(orc_ctx *c, int f, double flx[5]) {
-  const int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
-  const double nx = c->fn[4 * f], ny = c->fn[4 * f + 1], nz = c->fn[4 * f + 2], nm = c->fn[4 * f + 3];
+/* The interior flux of a face from its two sides: first order the cells'
+ * conserved (cl, cr) and dependent (dl, dr) variables, second order the
+ * reconstructed states L, Rr and the cells' densities (cl[0], cr[0]). */
+void sidesFlux(orc_ctx *c, double nx, double ny, double nz, double nm, const double *cl, const double *dl,
+               const double *cr, const double *dr, const FaceState &L, const FaceState &Rr, double flx[5]) {
   const double fs = 0.0;
   const double cp = c->refCp, g = c->refGamma;
   const int disc = c->num.spaceDiscr;
   if (c->num.spaceOrder == 1) {
-    const double *cl = &c->cv[5 * c1], *cr = &c->cv[5 * c2];
     double rl = cl[0], irl = 1.0 / rl, ul = cl[1] * irl, vl = cl[2] * irl, wl = cl[3] * irl;
     double rr = cr[0], irr = 1.0 / rr, ur = cr[1] * irr, vr = cr[2] * irr, wr = cr[3] * irr;
-    double pl = c->dv[3 * c1], pr = c->dv[3 * c2];
+    double pl = dl[0], pr = dr[0];
     if (disc == 1) {
-      double tl = c->dv[3 * c1 + 1], tr = c->dv[3 * c2 + 1];
+      double tl = dl[1], tr = dr[1];
       double Hl = MixtPerf_Ho_CpTUVW(cp, tl, ul, vl, wl), Hr = MixtPerf_Ho_CpTUVW(cp, tr, ur, vr, wr);
       roeFlux(c, nx, ny, nz, nm, fs, rl, ul, vl, wl, pl, Hl, rr, ur, vr, wr, pr, Hr, flx);
     } else if (disc == 3) {
       double el = cl[4] * irl, er = cr[4] * irr;
-      double al = c->dv[3 * c1 + 2], ar = c->dv[3 * c2 + 2];
+      double al = dl[2], ar = dr[2];
       double Hl = el + irl * pl, Hr = er + irr * pr;
       hllcFlux(c, nx, ny, nz, nm, fs, rl, ul, vl, wl, pl, el, al, Hl, rr, ur, vr, wr, pr, er, ar, Hr, flx);
     } else {
       /* RFLU_AUSM_ComputeFlux1 (RFLU_ModAUSMFlux.F90:550-1027) */
-      double al = c->dv[3 * c1 + 2], ar = c->dv[3 * c2 + 2];
+      double al = dl[2], ar = dr[2];
       double Hl = cl[4] * irl + pl / rl, Hr = cr[4] * irr + pr / rr;
       ausmFlux(nx, ny, nz, nm, fs, rl, ul, vl, wl, pl, Hl, al, rr, ur, vr, wr, pr, Hr, ar, flx);
     }
     return;
   }
-  const double xc = c->fc[3 * f], yc = c->fc[3 * f + 1], zc = c->fc[3 * f + 2];
-  FaceState L = reconstruct(c, c1, xc, yc, zc);
-  FaceState Rr = reconstruct(c, c2, c->fc2[3 * f], c->fc2[3 * f + 1], c->fc2[3 * f + 2]);
   if (disc == 1) {
     double gc = MixtPerf_R_CpG(cp, g);
     double tl = MixtPerf_T_DPR(L.r, L.p, gc), Hl = MixtPerf_Ho_CpTUVW(cp, tl, L.u, L.v, L.w);
     double tr = MixtPerf_T_DPR(Rr.r, Rr.p, gc), Hr = MixtPerf_Ho_CpTUVW(cp, tr, Rr.u, Rr.v, Rr.w);
     roeFlux(c, nx, ny, nz, nm, fs, L.r, L.u, L.v, L.w, L.p, Hl, Rr.r, Rr.u, Rr.v, Rr.w, Rr.p, Hr, flx);
   } else if (disc == 3) {
-    double irl = 1.0 / c->cv[5 * c1], irr = 1.0 / c->cv[5 * c2];
+    double irl = 1.0 / cl[0], irr = 1.0 / cr[0];
     double el = MixtPerf_Eo_DGPUVW(L.r, g, L.p, L.u, L.v, L.w), al = MixtPerf_C_DGP(L.r, g, L.p);
     double er = MixtPerf_Eo_DGPUVW(Rr.r, g, Rr.p, Rr.u, Rr.v, Rr.w), ar = MixtPerf_C_DGP(Rr.r, g, Rr.p);
     /* Hl = el + irl*pl with irl the inverse of the cell (unreconstructed) density */
@@ -1533,6 +1843,42 @@ void interiorFlux(orc_ctx *c, int f, double flx[5]) {
     double Hr = MixtPerf_Ho_CpTUVW(cp, tr, Rr.u, Rr.v, Rr.w);
     ausmFlux(nx, ny, nz, nm, fs, L.r, L.u, L.v, L.w, L.p, Hl, al, Rr.r, Rr.u, Rr.v, Rr.w, Rr.p, Hr, ar, flx);
   }
+}
+
+void interiorFlux(orc_ctx *c, int f, double flx[5]) {
+  const int c1 = c->f2c[2 * f], c2 = c->f2c[2 * f + 1];
+  const double nx = c->fn[4 * f], ny = c->fn[4 * f + 1], nz = c->fn[4 * f + 2], nm = c->fn[4 * f + 3];
+  FaceState L{}, Rr{};
+  if (c->num.spaceOrder > 1) {
+    L = reconstruct(c, c1, c->fc[3 * f], c->fc[3 * f + 1], c->fc[3 * f + 2]);
+    Rr = reconstruct(c, c2, c->fc2[3 * f], c->fc2[3 * f + 1], c->fc2[3 * f + 2]);
+  }
+  sidesFlux(c, nx, ny, nz, nm, &c->cv[5 * c1], &c->dv[3 * c1], &c->cv[5 * c2], &c->dv[3 * c2], L, Rr, flx);
+}
+
+/* A face of a symmetry patch: the interior flux between the cell and its
+ * reflection across the patch (the reference's virtual cell: momentum
+ * reflected, modflu/RFLU_ModRelatedPatches.F90:268-353); second order the
+ * reconstructed face state against its own reflection (the virtual cell's
+ * reflected gradient reconstructs it at the face). */
+void symmetryFlux(orc_ctx *c, const Patch &p, int ip, int i, double flx[5]) {
+  const int c1 = p.bf2c[i];
+  const double *Q = c->xfQ[c->patchXf[ip]].data();
+  const double *cl = &c->cv[5 * c1];
+  double cr[5];
+  cr[0] = cl[0];
+  reflect3(Q, cl + 1, cr + 1);
+  cr[4] = cl[4];
+  FaceState L{}, Rr{};
+  if (c->num.spaceOrder > 1) {
+    L = reconstruct(c, c1, p.fc[3 * i], p.fc[3 * i + 1], p.fc[3 * i + 2]);
+    const double ul[3] = {L.u, L.v, L.w};
+    double ur[3];
+    reflect3(Q, ul, ur);
+    Rr = {L.r, ur[0], ur[1], ur[2], L.p};
+  }
+  sidesFlux(c, p.fn[4 * i], p.fn[4 * i + 1], p.fn[4 * i + 2], p.fn[4 * i + 3], cl, &c->dv[3 * c1], cr,
+            &c->dv[3 * c1], L, Rr, flx);
 }
 
 /* BcondOutflowPerf (libfloflu/BcondOutflowPerf.F90:88-159). */
@@ -1736,6 +2082,10 @@ void remainingPatchFlux(const orc_ctx *c, const Patch &p, double nx, double ny, 
  * outflow, slip and no-slip walls, farfield (no vortex correction) and
  * injection, TCPERF gas, static grid. */
 void patchFlux(orc_ctx *c, const Patch &p, int i, double flx[5]) {
+  if (p.bcType == ORC_BC_SYMMETRY) {
+    symmetryFlux(c, p, (int)(&p - c->patches.data()), i, flx);
+    return;
+  }
   const int c1 = p.bf2c[i];
   const double nx = p.fn[4 * i], ny = p.fn[4 * i + 1], nz = p.fn[4 * i + 2], nm = p.fn[4 * i + 3];
   const double fs = 0.0;
@@ -2034,6 +2384,16 @@ double timeStep(orc_ctx *c, double currentTime) {
       double ir1 = 1.0 / c->cv[5 * c1];
       double u1 = c->cv[5 * c1 + 1] * ir1, v1 = c->cv[5 * c1 + 2] * ir1, w1 = c->cv[5 * c1 + 3] * ir1;
       double a1 = c->dv[3 * c1 + 2];
+      if (p.bcType == ORC_BC_SYMMETRY) {
+        /* an interior face to the cell's reflection (momentum reflected) */
+        double m2[3];
+        reflect3(c->xfQ[c->patchXf[c->bPatch[b]]].data(), &c->cv[5 * c1 + 1], m2);
+        double u2 = m2[0] * ir1, v2 = m2[1] * ir1, w2 = m2[2] * ir1;
+        double vc = 0.5 * ((u1 + u2) * nx + (v1 + v2) * ny + (w1 + w2) * nz);
+        double as = 0.5 * (a1 + a1);
+        dt[c1] = dt[c1] + (std::fabs(vc - fsu) + as) * nm;
+        continue;
+      }
       double vc = u1 * nx + v1 * ny + w1 * nz;
       dt[c1] = dt[c1] + (std::fabs(vc - fsu) + a1) * nm;
     }
@@ -2091,6 +2451,20 @@ orc_ctx *orc_create(const orc_mesh_desc *m, const orc_num_desc *num) {
   buildFaceList(c);
   buildCellFaces(c);
   buildGeometry(c);
+  c->nVertExt = c->nVert;
+  bool symmetry = false;
+  for (const Patch &p : c->patches) symmetry = symmetry || (p.bcType == ORC_BC_SYMMETRY && p.n > 0);
+  if (symmetry && periodic) {
+    std::fprintf(stderr, "oracle: symmetry and periodic patches in one mesh\n");
+    std::abort();
+  }
+  if (symmetry && num->cReconstCells == 1 && num->spaceOrder > 1)
+    for (const Patch &p : c->patches)
+      if (wallOrInjection(p.bcType) && p.n > 0) {
+        std::fprintf(stderr, "oracle: constrained gradients (CRECONSTC 1) with symmetry patches\n");
+        std::abort();
+      }
+  if (symmetry) buildSymmetryImages(c);
   if (num->spaceOrder > 1) {
     buildStencils(c);
     buildMoments(c);
@@ -2166,9 +2540,30 @@ void orc_get_periodic(orc_ctx *c, double *fc2, double *stShift) {
         stShift[3 * s + 2] = (dz == pz) ? 0.0 : dz - pz;
       }
 }
+int orc_n_reflections(orc_ctx *c) { return (int)c->xfQ.size(); }
+void orc_get_symmetry(orc_ctx *c, int *stXf, double *stShift, double *xfQ) {
+  const int nc = c->nCells;
+  for (int s = 0; s < c->stOff[nc]; ++s) {
+    const int j = c->stIdx[s];
+    if (j < nc) {
+      stXf[s] = -1;
+      stShift[3 * s] = stShift[3 * s + 1] = stShift[3 * s + 2] = 0.0;
+      continue;
+    }
+    stXf[s] = c->imgXf[j - nc];
+    for (int d = 0; d < 3; ++d) stShift[3 * s + d] = c->imgPos[3 * (size_t)(j - nc) + d] - c->cofg[3 * c->imgCell[j - nc] + d];
+  }
+  for (size_t t = 0; t < c->xfQ.size(); ++t)
+    for (int k = 0; k < 9; ++k) xfQ[9 * t + k] = c->xfQ[t][k];
+}
 void orc_get_stencil(orc_ctx *c, int *off, int *idx, double *moms) {
   if (off) std::memcpy(off, c->stOff.data(), sizeof(int) * (c->nCells + 1));
-  if (idx) std::memcpy(idx, c->stIdx.data(), sizeof(int) * c->stIdx.size());
+  /* a symmetry image as its real cell (orc_get_symmetry gives its reflection) */
+  if (idx)
+    for (size_t s = 0; s < c->stIdx.size(); ++s) {
+      const int j = c->stIdx[s];
+      idx[s] = j < c->nCells ? j : c->imgCell[j - c->nCells];
+    }
   if (moms && !c->moms.empty()) std::memcpy(moms, c->moms.data(), sizeof(double) * 10 * c->nCells);
 }
 

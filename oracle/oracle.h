@@ -40,6 +40,7 @@ extern "C" {
 #define ORC_BC_NOSLIPWALL_TEMP 71
 #define ORC_BC_FARFIELD 80
 #define ORC_BC_INJECTION 90
+#define ORC_BC_SYMMETRY 100
 #define ORC_BC_PERIODIC 110
 #define ORC_BCDAT_N 8
 #define ORC_BCSWI_N 2
@@ -104,6 +105,11 @@ void orc_get_bface_stencil(orc_ctx *c, int *off, int *faces);
  * frame (= fc off the periods) and stShift(3,nnz) the translation of each
  * stencil member's image (0 off the periods); either may be NULL. */
 void orc_get_periodic(orc_ctx *c, double *fc2, double *stShift);
+/* Symmetry patches: per stencil member the reflection it is seen through
+ * (-1: none; else an index into the nXf velocity reflections, 9 values each,
+ * row-major) and the offset of its reflected centroid from its own. */
+int orc_n_reflections(orc_ctx *c);
+void orc_get_symmetry(orc_ctx *c, int *stXf, double *stShift, double *xfQ);
 
 /* State. cv(5,nCells) conserved; dv(3,nCells) = p,T,c. */
 void orc_set_state(orc_ctx *c, const double *cv);

@@ -77,6 +77,10 @@ def lib():
         L.orc_get_bface_stencil.argtypes = [P, IP, IP]
         L.orc_get_periodic.argtypes = [P, DP, DP]
         L.orc_get_periodic.restype = None
+        L.orc_n_reflections.argtypes = [P]
+        L.orc_n_reflections.restype = C.c_int
+        L.orc_get_symmetry.argtypes = [P, IP, DP, DP]
+        L.orc_get_symmetry.restype = None
         L.orc_set_state.argtypes = [P, DP]
         L.orc_get_state.argtypes = [P, DP, DP]
         L.orc_get_rhs.argtypes = [P, DP]
@@ -204,6 +208,18 @@ class Oracle:
         sh = np.zeros((max(nnz, 1), 3))
         lib().orc_get_periodic(self.h, _ptr(fc2, C.c_double), _ptr(sh, C.c_double))
         return fc2, sh[:nnz]
+
+    def symmetry(self):
+        """(stXf (nnz,), stShift (nnz, 3), Q (nXf, 3, 3)): per stencil member
+        the reflection it is seen through (-1: none), the offset of its
+        reflected centroid from its own, and the velocity reflections."""
+        nnz = lib().orc_stencil_nnz(self.h)
+        nx = lib().orc_n_reflections(self.h)
+        xf = np.zeros(max(nnz, 1), np.int32)
+        sh = np.zeros((max(nnz, 1), 3))
+        q = np.zeros((max(nx, 1), 3, 3))
+        lib().orc_get_symmetry(self.h, _ptr(xf, C.c_int), _ptr(sh, C.c_double), _ptr(q, C.c_double))
+        return xf[:nnz], sh[:nnz], q[:nx]
 
     def stencil(self):
         off = np.zeros(self.n_cells + 1, np.int32)

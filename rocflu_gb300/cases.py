@@ -25,6 +25,7 @@ BC_NOSLIPWALL_HFLUX = 70
 BC_NOSLIPWALL_TEMP = 71
 BC_FARFIELD = 80
 BC_INJECTION = 90
+BC_SYMMETRY = 100
 BC_PERIODIC = 110
 BCOPT_SUPERSONIC, BCOPT_SUBSONIC, BCOPT_MIXED = 0, 1, 2
 
@@ -146,6 +147,62 @@ def gas_jump_periodic(n=8, length=0.008, x_jump=0.0043, left=(1.2, 0.0, 101325.0
         p.order = 1
     c.name = "gas_jump_periodic"
     return c
+
+
+def gas_jump_symmetry(n=8, length=0.008, x_jump=0.0043, left=(1.2, 0.0, 101325.0), right=(0.97, 82700.0)):
+    """The reference test suite's symmetry gas-jump box (tests/goldens/box/
+    gas-jump/symmetry/np1): the periodic box's deck and jump with symmetry
+    patches on all six sides (the harness's bc layout 'symmetry', tests/
+    rocpicl_tests/case.py:241-242); a face on a symmetry patch is an interior
+    face to the cell's reflection, so the patch order does not apply.  No
+    wall or injection patch, so CRECONSTC 1 of the deck constrains nothing."""
+    c = gas_jump_closed(n, length, x_jump, left, right)
+    for p in c.patches:
+        p.bc_type = BC_SYMMETRY
+    c.name = "gas_jump_symmetry"
+    return c
+
+
+def mirror_box(n=6, axes=(0,), doubled=False, num=None, tets=False):
+    """A smooth 3-D state (density and pressure bumps, all three velocity
+    components nonzero) on n^3 hexes of [0,1]^3 with symmetry patches on the
+    high sides of the given axes and first-order slip walls elsewhere; or,
+    doubled, the box extended to [0,2] along those axes with the state
+    mirrored about 1 (velocity component reversed) and slip walls all round.
+    A symmetry patch stands for the mirrored half, so the two runs agree on
+    [0,1]^3 wherever the scheme itself keeps the doubled box symmetric.
+    tets: 6 tetrahedra per hex (no doubled form: the split is not mirror
+    symmetric)."""
+    mult = [2 if (doubled and a in axes) else 1 for a in range(3)]
+    size = tuple(float(m) for m in mult)
+    mesh = meshgen.tet_box(n, hi=size, jitter=0.1) if tets else meshgen.hex_box(n * mult[0], n * mult[1], n * mult[2], hi=size)
+    if num is None:
+        num = Numerics(space_order=2, space_discr=DISCR_HLLC, reconst=RECONST_WENO_XYZ, rk_scheme=RK_WRAY3, cfl=0.4)
+    kinds = []
+    for ip in range(6):
+        ax, hi = ip // 2, ip % 2
+        if hi and ax in axes and not doubled:
+            kinds.append({"bc_type": BC_SYMMETRY, "order": 1})
+        else:
+            kinds.append(dict(SLIP, order=1))
+    patches = _patches(mesh, kinds)
+    c = meshgen.cell_centers(mesh)
+    x, y, z = c[:, 0].copy(), c[:, 1].copy(), c[:, 2].copy()
+    sgn = np.ones((len(x), 3))
+    for a, X in enumerate((x, y, z)):
+        if a in axes:
+            m = X > 1.0
+            X[m] = 2.0 - X[m]
+            sgn[m, a] = -1.0
+    rho = 1.2 + 0.3 * np.exp(-((x - 0.3) ** 2 + (y - 0.45) ** 2 + (z - 0.55) ** 2) / 0.02)
+    u = 0.3 * np.sin(np.pi * x) * (1 + 0.2 * y) * sgn[:, 0]
+    v = 0.2 * np.cos(2 * y + z) * (1 + 0.1 * x) * sgn[:, 1]
+    w = 0.15 * np.sin(3 * z + x) * sgn[:, 2]
+    p = 1.0 + 0.4 * np.exp(-((x - 0.6) ** 2 + (y - 0.3) ** 2 + (z - 0.4) ** 2) / 0.03)
+    g = num.gamma
+    cv0 = np.stack([rho, rho * u, rho * v, rho * w, p / (g - 1) + 0.5 * rho * (u * u + v * v + w * w)], axis=1)
+    num.dt_imposed = 1e-3
+    return Case("mirror_box", mesh["xyz"], mesh["c2v"], patches, num, cv0)
 
 
 def sod(nx=400, ny=4, nz=4, num=None):

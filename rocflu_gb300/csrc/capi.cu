@@ -282,7 +282,7 @@ struct Ctx : CtxBase {
   const Ops<R> *ops = nullptr;
   std::vector<void *> allocs;
   double *staging = nullptr;     // (15, nc) doubles: transfers in reference order
-  bool periodicMesh = false;     // the grid came with periodic images (fc2 / c2csShift)
+  bool imageMesh = false;        // the grid came with periodic or symmetry images (fc2 / c2csShift / c2csXf)
   double *work = nullptr;        // adjoint workspace (allocated by the first adjoint call)
   int tsWidthLazy = 0;           // ... and the width of its transposed-stencil weights
   size_t workBytes = 0;
@@ -589,7 +589,7 @@ struct Ctx : CtxBase {
     invalidate();
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
     if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through constrained gradients (CRECONSTC 1)");
-    if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint on a periodic mesh");
+    if (imageMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint on a mesh with periodic or symmetry patches");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -603,7 +603,7 @@ struct Ctx : CtxBase {
     invalidate();
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
     if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through constrained gradients (CRECONSTC 1)");
-    if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent on a periodic mesh");
+    if (imageMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent on a mesh with periodic or symmetry patches");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -629,8 +629,8 @@ struct Ctx : CtxBase {
     invalidate();
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
-    if (cvBar && periodicMesh)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient on a periodic mesh");
+    if (cvBar && imageMesh)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient on a mesh with periodic or symmetry patches");
     if (cvBar && V.cSlot)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through constrained gradients (CRECONSTC 1)");
     View<R> W;
@@ -840,7 +840,7 @@ struct Ctx : CtxBase {
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
     if (V.cSlot)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: constrained gradients (CRECONSTC 1) have no adjoint");
-    if (periodicMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint on a periodic mesh");
+    if (imageMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint on a mesh with periodic or symmetry patches");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     if (int rc0 = ensureAdjoint()) return rc0;
     // the whole forward and reverse sweep runs on the scratch state X
@@ -970,7 +970,7 @@ struct Ctx : CtxBase {
   int adjointTimes(int nIter, double *ms) override {
     invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
-    if (!ops->vjp || V.cSlot || periodicMesh)
+    if (!ops->vjp || V.cSlot || imageMesh)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
     if (int rc0 = ensureAdjoint()) return rc0;
     const size_t nc = V.nc;
@@ -1029,6 +1029,19 @@ int Ctx<R>::patchConstants(const rflu_grid_desc *g, int ip, const rflu_num_desc 
     case RFLU_BC_NOSLIPWALL_HFLUX:
     case RFLU_BC_NOSLIPWALL_TEMP:
       return RFLU_OK;
+    case RFLU_BC_SYMMETRY: {
+      // the reflection across the patch's plane, from its first face's
+      // normal (RFLU_RELP_TransformMatrix, modflu/RFLU_ModRelatedPatches.F90:
+      // 449-514; rflu_setup_build checks that the patch is planar)
+      if (g->patchFaceOff[ip + 1] == g->patchFaceOff[ip]) return RFLU_OK;
+      const double *n = g->bfn + 4 * (size_t)g->patchFaceOff[ip];
+      const double nx = n[0], ny = n[1], nz = n[2];
+      const double Q[9] = {1.0 - 2.0 * nx * nx, -2.0 * nx * ny, -2.0 * nx * nz,
+                           -2.0 * nx * ny, 1.0 - 2.0 * ny * ny, -2.0 * ny * nz,
+                           -2.0 * nx * nz, -2.0 * ny * nz, 1.0 - 2.0 * nz * nz};
+      for (int k = 0; k < 9; ++k) K[k] = Q[k];
+      return RFLU_OK;
+    }
     case RFLU_BC_PERIODIC:  // its faces are interior faces of the identified mesh (fc2, c2csShift)
       if (g->patchFaceOff[ip + 1] != g->patchFaceOff[ip])
         return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: a periodic patch must hold no boundary faces (its faces are "
@@ -1293,7 +1306,8 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   std::vector<int> stOff(nc + 1, 0), stIdx;
   std::vector<double> wx, wy, wz, epsq(nc, 0.0), lsq;
   std::vector<float> stShift;  // mixed mode on a periodic mesh: the members' translations
-  periodicMesh = g->c2csShift != nullptr || g->fc2 != nullptr;
+  imageMesh = g->c2csShift != nullptr || g->fc2 != nullptr || g->c2csXf != nullptr;
+  std::vector<int> stXf;  // symmetry meshes: the members' reflections
   const bool mixed = num->precision == RFLU_PREC_MIXED;
   if (mixed && num->spaceOrder > 1) lsq.resize(6 * (size_t)nc);
   if (num->spaceOrder > 1) {
@@ -1322,7 +1336,12 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
         if (j < 0 || j >= nc) return fail(RFLU_ERR_ARG, "rflu_gpu_create: stencil member out of range");
         double dx = g->cofg[3 * (size_t)j] - xi[0], dy = g->cofg[3 * (size_t)j + 1] - xi[1],
                dz = g->cofg[3 * (size_t)j + 2] - xi[2];
-        if (g->c2csShift) {  // the member's periodic image
+        if (g->c2csXf) {
+          const int x = g->c2csXf[e];
+          if (x < -1 || x >= g->nXf) return fail(RFLU_ERR_ARG, "rflu_gpu_create: c2csXf out of range");
+          stXf.push_back(x);
+        }
+        if (g->c2csShift) {  // the member's periodic or symmetry image
           const double *sh = g->c2csShift + 3 * (size_t)e;
           dx = dx + sh[0]; dy = dy + sh[1]; dz = dz + sh[2];
           if (mixed) { stShift.push_back((float)sh[0]); stShift.push_back((float)sh[1]); stShift.push_back((float)sh[2]); }
@@ -1406,6 +1425,8 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     PUT(V.cgx, cgx, R); PUT(V.cgy, cgy, R); PUT(V.cgz, cgz, R);
     PUT(V.lsq, lsq, R); PUT(V.ivol, ivol, R);
     if (!stShift.empty()) PUT(V.stShift, stShift, float);
+    if (g->c2csXf && !g->c2csShift)
+      return fail(RFLU_ERR_ARG, "rflu_gpu_create: c2csXf needs c2csShift (the reflected members' offsets)");
     // the tile plan stages records with their own centroids; a periodic
     // mesh's members need their images' (the gather kernel adds stShift)
     if (num->spaceOrder > 1 && !(num->options & RFLU_OPT_UNTILED) && stShift.empty()) {
@@ -1424,12 +1445,26 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   }
   // transposed stencil (adjoint of the LSQ gradient, every mode)
   PUT(V.tsOff, tsOff, int); PUT(V.tsCell, tsCell, int); PUT(V.tsEnt, tsEnt, int);
+  if (!stXf.empty()) {
+    if (!g->xfQ || g->nXf <= 0) return fail(RFLU_ERR_ARG, "rflu_gpu_create: c2csXf needs xfQ");
+    std::vector<R> q(g->xfQ, g->xfQ + 9 * (size_t)g->nXf);
+    PUT(V.stXf, stXf, int);
+    PUT(V.xfQ, q, R);
+  }
   // constrained gradients (CRECONSTC 1): the plan in the reference's cell
   // numbering (constr.h), moved to the renumbered cells; the stencil rows
   // keep the reference's member order, which the device's stencil keeps too
-  if (num->cReconstCells == 1 && num->spaceOrder > 1 && g->c2csShift)
-    return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_create: constrained gradients (CRECONSTC 1) on a periodic mesh");
-  if (num->cReconstCells == 1 && num->spaceOrder > 1) {
+  // (a mesh with periodic or symmetry images and no wall or injection patch
+  // has no constrained cell)
+  bool constrPatches = false;
+  for (int ip = 0; ip < np; ++ip)
+    if ((pType[ip] == RFLU_BC_SLIPWALL || pType[ip] == RFLU_BC_NOSLIPWALL_HFLUX || pType[ip] == RFLU_BC_NOSLIPWALL_TEMP ||
+         pType[ip] == RFLU_BC_INJECTION) && g->patchFaceOff[ip + 1] > g->patchFaceOff[ip])
+      constrPatches = true;
+  if (num->cReconstCells == 1 && num->spaceOrder > 1 && imageMesh && constrPatches)
+    return fail(RFLU_ERR_UNSUPPORTED,
+                "rflu_gpu_create: constrained gradients (CRECONSTC 1) on a mesh with periodic or symmetry patches");
+  if (num->cReconstCells == 1 && num->spaceOrder > 1 && !imageMesh) {
     std::vector<int> stOffRef(g->c2csOff, g->c2csOff + nc + 1), stIdxRef(g->c2csOff[nc]);
     for (int e = 0; e < g->c2csOff[nc]; ++e) stIdxRef[e] = g->c2csMembs[e] - 1;
     std::vector<int> bf2cRef(nb);

@@ -58,7 +58,11 @@ struct Params {
 //                   rho w, rho E, p)
 //   inflow VELTEMP  K[0..3] = u, v, w, T, K[4] = p, K[5] = rho (not subsonic)
 //   injection       K[0] = mass flux, K[1] = T_inj
+//   symmetry        K[0..8] = the reflection I - 2 n n^T across the patch's
+//                   plane, row-major (RFLU_RELP_TransformMatrix,
+//                   modflu/RFLU_ModRelatedPatches.F90:449-514)
 constexpr int kPatchK = 16;
+constexpr int kBcSymmetry = 100;
 constexpr int kTile = 256;
 // Shared-memory footprint of one staged tile of the mixed-mode gradient
 // kernel: 8 floats per record, the stencil ids as whole 16-byte words (plus
@@ -105,9 +109,15 @@ struct View {
   // constraint row (-1: a stencil member's row)
   const int *cSlot, *cNcon, *cRowOff, *cRowFace;
   const R *cW;
-  // mixed mode on a periodic mesh (untiled): each stencil member's
-  // translation to its image, added to the centroid difference (null: none)
+  // mixed mode on a periodic or symmetry mesh (untiled): each stencil
+  // member's translation to its image, added to the centroid difference
+  // (null: none)
   const float *stShift;
+  // symmetry meshes: each stencil member's reflection (-1: none; null: no
+  // member is reflected) and the reflections' 3x3 matrices, row-major; a
+  // reflected member's velocity is Q u (its density and pressure its own)
+  const int *stXf;
+  const R *xfQ;
   // cell -> faces CSR in reference summation order; entry e >= 0: interior
   // face (e >> 1) seen from side (e & 1); e < 0: boundary face -(e+1)
   const int *cfOff, *cfEnt;

@@ -426,6 +426,78 @@ __device__ inline void constrainedGrad(const View<R> &V, const L &ld, int i, int
   }
 }
 
+// Symmetry patches (RFLU_BC_SYMMETRY): a face on one is an interior face to
+// the cell's reflection across it (the reference's virtual cell, modflu/
+// RFLU_ModSymmetryPeriodic.F90:471-787, whose momentum is reflected,
+// modflu/RFLU_ModRelatedPatches.F90:268-353), and a stencil member may be
+// seen reflected (V.stXf).  y = Q x for a row-major 3x3 Q, summed in index
+// order.
+template <typename S, typename Qt>
+__device__ inline void reflect3(const Qt *Q, const S *x, S *y) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    S t = S(Q[3 * a]) * x[0];
+    t = t + S(Q[3 * a + 1]) * x[1];
+    t = t + S(Q[3 * a + 2]) * x[2];
+    y[a] = t;
+  }
+}
+// The reflection of a boundary face entry (code < 0) on a symmetry patch,
+// else null.
+template <typename R>
+__device__ inline const double *symmetryQ(const View<R> &V, int code) {
+  if (code >= 0) return nullptr;
+  const int ip = V.bpatch[-code - 1];
+  return V.patchType[ip] == kBcSymmetry ? V.patchK + kPatchK * ip : nullptr;
+}
+// The offset fc - cofg of a cell's face entry for the limiters' face loops:
+// an interior face's, a symmetry face's (an interior face to the cell's
+// reflection); false for the other boundary faces.
+template <typename R>
+__device__ inline bool limiterFaceOffset(const View<R> &V, int code, R *d) {
+  if (code >= 0) {
+    faceOffset(V, code >> 1, code & 1, d);
+    return true;
+  }
+  if (!symmetryQ(V, code)) return false;
+  const int b = -code - 1;
+  const size_t nb = V.nb;
+  d[0] = V.bd[b];
+  d[1] = V.bd[nb + b];
+  d[2] = V.bd[2 * nb + b];
+  return true;
+}
+// A reflected stencil member's raw gradient (15 components, 3 * var + dir):
+// Q g for density and pressure, Q G Q^T for the velocity gradient
+// (RFLU_RELP_TransformGradWrapper, modflu/RFLU_ModRelatedPatches.F90:380-435).
+template <typename S, typename Qt>
+__device__ inline void reflectGrad(const Qt *Q, S *g) {
+  S t[3];
+  reflect3(Q, g, t);
+  g[0] = t[0]; g[1] = t[1]; g[2] = t[2];
+  reflect3(Q, g + 12, t);
+  g[12] = t[0]; g[13] = t[1]; g[14] = t[2];
+  S T[9];
+#pragma unroll
+  for (int b = 0; b < 3; ++b)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      S x = g[3 * (1 + b)] * S(Q[3 * c]);
+      x = x + g[3 * (1 + b) + 1] * S(Q[3 * c + 1]);
+      x = x + g[3 * (1 + b) + 2] * S(Q[3 * c + 2]);
+      T[3 * b + c] = x;
+    }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      S x = S(Q[3 * a]) * T[c];
+      x = x + S(Q[3 * a + 1]) * T[3 + c];
+      x = x + S(Q[3 * a + 2]) * T[6 + c];
+      g[3 * (1 + a) + c] = x;
+    }
+}
+
 // Gradient + limiter of one cell.
 // LSQ gradient: RFLU_ComputeGradCellsFast_3D (modflu/RFLU_ModDifferentiationCells.F90:
 // 931-1178) with the per-member weights precomputed at set-up.
@@ -448,9 +520,18 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
     for (int s = sb; s < se; ++s) {
       const int j = V.stIdx[s];
       const S wx = S(V.wx[s]), wy = S(V.wy[s]), wz = S(V.wz[s]);
+      S qj[5];
+      ld.prim5(j, qj);
+      if (V.stXf) {  // a member seen reflected across symmetry patches
+        const int x = V.stXf[s];
+        if (x >= 0) {
+          const S u[3] = {qj[1], qj[2], qj[3]};
+          reflect3(V.xfQ + 9 * x, u, qj + 1);
+        }
+      }
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        S d = ld.prim(k, j) - q[k];
+        S d = qj[k] - q[k];
         g[3 * k] = g[3 * k] + wx * d;
         g[3 * k + 1] = g[3 * k + 1] + wy * d;
         g[3 * k + 2] = g[3 * k + 2] + wz * d;
@@ -500,13 +581,21 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
     for (int k = 0; k < 5; ++k) { vmin[k] = q[k]; vmax[k] = q[k]; lim[k] = S(1); }
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
-      if (code < 0) continue;
-      const int f = code >> 1;
-      int c1, c2;
-      faceCells(V, f, c1, c2);
-      const int nb = (code & 1) ? c1 : c2;
       S x[5];
-      ld.prim5(nb, x);
+      if (code < 0) {
+        // a symmetry face: the neighbour is the cell's reflection
+        const double *Q = symmetryQ(V, code);
+        if (!Q) continue;
+        x[0] = q[0];
+        reflect3(Q, q + 1, x + 1);
+        x[4] = q[4];
+      } else {
+        const int f = code >> 1;
+        int c1, c2;
+        faceCells(V, f, c1, c2);
+        const int nb = (code & 1) ? c1 : c2;
+        ld.prim5(nb, x);
+      }
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         vmin[k] = fmin2(vmin[k], x[k]);
@@ -526,10 +615,8 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
     for (int k = 0; k < 5; ++k) { pmx[k] = S(0); nmn[k] = S(0); }
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
-      if (code < 0) continue;
-      const int f = code >> 1;
       R d[3];
-      faceOffset(V, f, code & 1, d);
+      if (!limiterFaceOffset(V, code, d)) continue;
       const S dx = S(d[0]), dy = S(d[1]), dz = S(d[2]);
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
@@ -582,15 +669,27 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       S spx[3] = {S(0), S(0), S(0)}, snx[3] = {S(0), S(0), S(0)};  // extreme projections (one pass)
       for (int e = cb; e < ce; ++e) {
         const int code = V.cfEnt[e];
-        if (code < 0) continue;
-        const int f = code >> 1, side = code & 1;
-        int c1, c2;
-        faceCells(V, f, c1, c2);
-        S du[3], a1[4], a2[4];
-        ld.prim4(c1, a1);
-        ld.prim4(c2, a2);
+        S du[3];
+        int side = 0;
+        if (code < 0) {
+          // a symmetry face: the cell's reflection as the second cell
+          const double *Q = symmetryQ(V, code);
+          if (!Q) continue;
+          S um[3];
+          reflect3(Q, q + 1, um);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) du[k] = a2[1 + k] - a1[1 + k];
+          for (int k = 0; k < 3; ++k) du[k] = um[k] - q[1 + k];
+        } else {
+          const int f = code >> 1;
+          side = code & 1;
+          int c1, c2;
+          faceCells(V, f, c1, c2);
+          S a1[4], a2[4];
+          ld.prim4(c1, a1);
+          ld.prim4(c2, a2);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) du[k] = a2[1 + k] - a1[1 + k];
+        }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           S pr = S(0);
@@ -604,10 +703,8 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       }
       for (int e = cb; e < ce; ++e) {
         const int code = V.cfEnt[e];
-        if (code < 0) continue;
-        const int f = code >> 1;
         R d[3];
-        faceOffset(V, f, code & 1, d);
+        if (!limiterFaceOffset(V, code, d)) continue;
         const S off[3] = {-S(d[0]), -S(d[1]), -S(d[2])};
         S sh[3];
 #pragma unroll
@@ -852,10 +949,17 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
         float r[8];
         ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
         float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
-        if (V.stShift) {  // a periodic mesh: the member's image
+        if (V.stShift) {  // a periodic or symmetry mesh: the member's image
           dx = dx + V.stShift[3 * (size_t)s];
           dy = dy + V.stShift[3 * (size_t)s + 1];
           dz = dz + V.stShift[3 * (size_t)s + 2];
+          if (V.stXf) {
+            const int x = V.stXf[s];
+            if (x >= 0) {
+              const float u[3] = {r[1], r[2], r[3]};
+              reflect3(V.xfQ + 9 * x, u, r + 1);
+            }
+          }
         }
         const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
         const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
@@ -1003,6 +1107,19 @@ __device__ inline float gradLimitPacked(const View<float> &V, int i, float *g, f
           const float aj = sqrtf(gam * x[4] / x[0]);
           const float vc = 0.5f * ((q[1] + x[1]) * F0.x + (q[2] + x[2]) * F0.y + (q[3] + x[3]) * F0.z);
           sum += (fabsf(vc) + 0.5f * (ai + aj)) * F0.w;
+        }
+      } else if (const double *Q = symmetryQ(V, code)) {
+        // a symmetry face: an interior face to the cell's reflection
+        const int b = -code - 1;
+        const size_t nb = V.nb;
+        float x[8];
+        x[0] = q[0];
+        reflect3(Q, q + 1, x + 1);
+        x[4] = q[4];
+        if (lim) face(x, V.bd[b], V.bd[nb + b], V.bd[2 * nb + b]);
+        if (kDt) {
+          const float vc = 0.5f * ((q[1] + x[1]) * V.bnx[b] + (q[2] + x[2]) * V.bny[b] + (q[3] + x[3]) * V.bnz[b]);
+          sum += (fabsf(vc) + 0.5f * (ai + ai)) * V.bnm[b];
         }
       } else if (kDt) {
         const int b = -code - 1;
@@ -1320,6 +1437,13 @@ __device__ inline double cellDtPrim(const View<R> &V, int i) {
       faceNormal(V, f, nx, ny, nz, nm);
       const float vc = 0.5f * ((ui + uj) * (float)nx + (vi + vj) * (float)ny + (wi + wj) * (float)nz);
       sum += (fabsf(vc) + 0.5f * (ai + aj)) * (float)nm;
+    } else if (const double *Q = symmetryQ(V, code)) {
+      const int b = -code - 1;
+      const float u[3] = {ui, vi, wi};
+      float m[3];
+      reflect3(Q, u, m);
+      const float vc = 0.5f * ((ui + m[0]) * (float)V.bnx[b] + (vi + m[1]) * (float)V.bny[b] + (wi + m[2]) * (float)V.bnz[b]);
+      sum += (fabsf(vc) + 0.5f * (ai + ai)) * (float)V.bnm[b];
     } else {
       const int b = -code - 1;
       const float vc = ui * (float)V.bnx[b] + vi * (float)V.bny[b] + wi * (float)V.bnz[b];
@@ -1516,7 +1640,13 @@ __global__ void __launch_bounds__(kBlock) kWenoSmooth(View<R> V, const R *raw) {
       for (int k = 0; k < 15; ++k) t[k] = raw[k * n + c];
     }
   };
-  auto fetch = [&](int s, R *t) { rawRow(V.stIdx[s], t); };
+  auto fetch = [&](int s, R *t) {
+    rawRow(V.stIdx[s], t);
+    if (V.stXf) {  // a member seen reflected across symmetry patches
+      const int x = V.stXf[s];
+      if (x >= 0) reflectGrad(V.xfQ + 9 * x, t);
+    }
+  };
   const int sb = V.stOff[i], se = V.stOff[i + 1];
   R g[15], own[16];
   rawRow(i, own);
@@ -1888,6 +2018,35 @@ __device__ inline void faceFluxEval(const View<R> &V, const L &ld, int t, typena
   } else {
     const int b = t - V.nf, c = V.bcell[b], ip = V.bpatch[b];
     const int type = V.patchType[ip], order = V.patchOrder[ip];
+    if (type == kBcSymmetry) {
+      // an interior face to the cell's reflection, at the interior order:
+      // first order the cell against its reflected state, second order the
+      // reconstructed face state against its own reflection
+      const double *Q = V.patchK + kPatchK * ip;
+      if (P.spaceOrder == 1) {
+        H cl[5], cr[5], dl[3], fd[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) cl[k] = ld.cv(k, c);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dl[k] = ld.dv(k, c);
+        cr[0] = cl[0];
+        reflect3(Q, cl + 1, cr + 1);
+        cr[4] = cl[4];
+        riemann1(P, cl, dl, cr, dl, H((double)V.bnx[b]), H((double)V.bny[b]), H((double)V.bnz[b]),
+                 H((double)V.bnm[b]), fd);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) flx[k] = cvt<S>(fd[k]);
+      } else {
+        const size_t nb = V.nb;
+        S Lf[5], Rt[5], irl;
+        faceState(V, ld, c, S(V.bd[b]), S(V.bd[nb + b]), S(V.bd[2 * nb + b]), Lf, irl);
+        Rt[0] = Lf[0];
+        reflect3(Q, Lf + 1, Rt + 1);
+        Rt[4] = Lf[4];
+        riemann2(P, S(V.bnx[b]), S(V.bny[b]), S(V.bnz[b]), S(V.bnm[b]), Lf, irl, Rt, irl, flx);
+      }
+      return;
+    }
     if (order == 1) {
       H cv[5], fd[5];
 #pragma unroll
@@ -2209,6 +2368,18 @@ __global__ void __launch_bounds__(kBlock) kCellDt(View<R> V) {
         const double nx = V.bnx[b], ny = V.bny[b], nz = V.bnz[b], nm = V.bnm[b];
         const double ir1 = 1.0 / V.cv[i];
         const double u1 = V.cv[n + i] * ir1, v1 = V.cv[2 * n + i] * ir1, w1 = V.cv[3 * n + i] * ir1;
+        if (const double *Q = symmetryQ(V, code)) {
+          // an interior face to the cell's reflection (momentum reflected)
+          const double m1[3] = {V.cv[n + i], V.cv[2 * n + i], V.cv[3 * n + i]};
+          double m2[3];
+          reflect3(Q, m1, m2);
+          const double u2 = m2[0] * ir1, v2 = m2[1] * ir1, w2 = m2[2] * ir1;
+          const double a1 = V.dv[2 * n + i];
+          const double vc = 0.5 * ((u1 + u2) * nx + (v1 + v2) * ny + (w1 + w2) * nz);
+          const double as = 0.5 * (a1 + a1);
+          sum = sum + (fabs(vc - 0.0) + as) * nm;
+          continue;
+        }
         const double vc = u1 * nx + v1 * ny + w1 * nz;
         sum = sum + (fabs(vc - 0.0) + V.dv[2 * n + i]) * nm;
       }

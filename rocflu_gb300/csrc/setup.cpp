@@ -300,7 +300,9 @@ struct rflu_setup {
   std::vector<double> bfn, bfc;
   std::vector<int> c2csOff, c2csMembs;
   std::vector<double> xyzMoms;
-  std::vector<double> fc2, c2csShift;  // periodic meshes only
+  std::vector<double> fc2, c2csShift;  // periodic and symmetry meshes only
+  std::vector<int> c2csXf;             // symmetry meshes only
+  std::vector<double> xfQ;
 };
 
 extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_setup **out) {
@@ -401,7 +403,21 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
   auto vid = [&](int ic, int k) { const int v = vert(ic, k); return periodic ? rep[v] : v; };
   // offset of stencil member j from cell i for the image of j nearest to i
   // (the virtual cell standing for j in the reference), and its translation
+  // symmetry patches: the cells near them also seen reflected across them
+  // (images, stencil ids nc + k): real cell, reflection, centroid, vertices
+  std::vector<int> imgCell, imgXf, imgC2v;
+  std::vector<double> imgPos;
+  std::vector<std::array<double, 9>> xfQ;
+  int nvExt = nv;
   auto memberOffset = [&](const double *cg, int i, int j, double &dx, double &dy, double &dz, double *sh) {
+    if (j >= nc) {
+      const double *x = &imgPos[3 * (size_t)(j - nc)], *x0 = &cg[3 * (size_t)imgCell[j - nc]];
+      dx = x[0] - cg[3 * (size_t)i];
+      dy = x[1] - cg[3 * (size_t)i + 1];
+      dz = x[2] - cg[3 * (size_t)i + 2];
+      if (sh) for (int d = 0; d < 3; ++d) sh[d] = x[d] - x0[d];
+      return;
+    }
     dx = cg[3 * (size_t)j] - cg[3 * (size_t)i];
     dy = cg[3 * (size_t)j + 1] - cg[3 * (size_t)i + 1];
     dz = cg[3 * (size_t)j + 2] - cg[3 * (size_t)i + 2];
@@ -648,19 +664,195 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
     for (int d = 0; d < 3; ++d) S->cofg[3 * (size_t)ic + d] = t * cg[d];
   }
 
+  // ---- symmetry (mirror) patches -----------------------------------------------
+  // The reference adds the cells near each symmetry patch as virtual cells
+  // reflected across it, and reflected copies of earlier patches' virtual
+  // cells near it (the corner images) (modflu/RFLU_ModSymmetryPeriodic.F90:
+  // 148-335, 471-787); their state and gradients are the actual cells',
+  // reflected (modflu/RFLU_ModRelatedPatches.F90:268-435).  Here each
+  // symmetry patch must be planar and two patches parallel or
+  // perpendicular; the cells within three vertex layers of a patch are seen
+  // reflected across every set of such patches without two parallel ones,
+  // and an image's vertices off its reflecting planes get new ids, so that
+  // the stencils below grow across the planes as over virtual cells.
+  bool symmetry = false;
+  for (int ip = 0; ip < m->nPatches && m->patchBcType; ++ip)
+    symmetry = symmetry || (m->patchBcType[ip] == RFLU_BC_SYMMETRY && patchOffKept[ip + 1] > patchOffKept[ip]);
+  if (symmetry && periodic) {
+    delete S;
+    return rflu::fail(RFLU_ERR_UNSUPPORTED, "rflu_setup_build: symmetry and periodic patches in one mesh");
+  }
+  if (symmetry && spaceOrder > 1) {
+    struct Plane { double n[3], p0[3]; std::vector<int> verts; };
+    std::vector<Plane> planes;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int v = 0; v < nv; ++v)
+      for (int d = 0; d < 3; ++d) { lo[d] = std::min(lo[d], xyz[3 * (size_t)v + d]); hi[d] = std::max(hi[d], xyz[3 * (size_t)v + d]); }
+    const double tol = 1e-7 * std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+    for (int ip = 0; ip < m->nPatches; ++ip) {
+      if (m->patchBcType[ip] != RFLU_BC_SYMMETRY || patchOffKept[ip + 1] == patchOffKept[ip]) continue;
+      Plane P;
+      const int b0 = patchOffKept[ip];
+      for (int d = 0; d < 3; ++d) { P.n[d] = S->bfn[4 * (size_t)b0 + d]; P.p0[d] = S->bfc[3 * (size_t)b0 + d]; }
+      for (int b = b0; b < patchOffKept[ip + 1]; ++b) {
+        const double cosA = S->bfn[4 * (size_t)b] * P.n[0] + S->bfn[4 * (size_t)b + 1] * P.n[1] + S->bfn[4 * (size_t)b + 2] * P.n[2];
+        for (int k = 0; k < 4; ++k) {
+          const int v = m->bf2v[4 * (size_t)keep[b] + k] - 1;
+          if (v < 0) continue;
+          const double h = (xyz[3 * (size_t)v] - P.p0[0]) * P.n[0] + (xyz[3 * (size_t)v + 1] - P.p0[1]) * P.n[1] +
+                           (xyz[3 * (size_t)v + 2] - P.p0[2]) * P.n[2];
+          if (std::fabs(h) > tol || cosA < 1.0 - 1e-10) {
+            delete S;
+            return rflu::fail(RFLU_ERR_UNSUPPORTED, "rflu_setup_build: a symmetry patch is not planar");
+          }
+          P.verts.push_back(v);
+        }
+      }
+      planes.push_back(std::move(P));
+    }
+    const int np = (int)planes.size();
+    if (np > 30) { delete S; return rflu::fail(RFLU_ERR_UNSUPPORTED, "rflu_setup_build: more than 30 symmetry patches"); }
+    std::vector<int> parallel(np, 0);
+    for (int a = 0; a < np; ++a)
+      for (int q = 0; q < np; ++q) {
+        if (q == a) continue;
+        const double d = std::fabs(planes[a].n[0] * planes[q].n[0] + planes[a].n[1] * planes[q].n[1] + planes[a].n[2] * planes[q].n[2]);
+        if (d > 1.0 - 1e-10) parallel[a] |= 1 << q;
+        else if (d > 1e-10) {
+          delete S;
+          return rflu::fail(RFLU_ERR_UNSUPPORTED, "rflu_setup_build: two symmetry patches neither parallel nor perpendicular");
+        }
+      }
+    std::vector<int> vmask(nv, 0), nearMask(nc, 0);
+    std::vector<int> v2cOff0(nv + 1, 0);
+    for (int ic = 0; ic < nc; ++ic)
+      for (int k = 0; k < nvc; ++k) v2cOff0[vert(ic, k) + 1]++;
+    for (int v = 0; v < nv; ++v) v2cOff0[v + 1] += v2cOff0[v];
+    std::vector<int> v2c0(v2cOff0[nv]);
+    {
+      std::vector<int> fill(v2cOff0.begin(), v2cOff0.end() - 1);
+      for (int ic = 0; ic < nc; ++ic)
+        for (int k = 0; k < nvc; ++k) v2c0[fill[vert(ic, k)]++] = ic;
+    }
+    const int kLayers = 3;
+    for (int a = 0; a < np; ++a) {
+      std::vector<char> vIn(nv, 0), cIn(nc, 0);
+      std::vector<int> front;
+      for (int v : planes[a].verts) {
+        vmask[v] |= 1 << a;
+        if (!vIn[v]) { vIn[v] = 1; front.push_back(v); }
+      }
+      for (int layer = 0; layer < kLayers; ++layer) {
+        std::vector<int> next;
+        for (int v : front)
+          for (int e = v2cOff0[v]; e < v2cOff0[v + 1]; ++e) {
+            const int ic = v2c0[e];
+            if (cIn[ic]) continue;
+            cIn[ic] = 1;
+            nearMask[ic] |= 1 << a;
+            for (int k = 0; k < nvc; ++k) {
+              const int w = vert(ic, k);
+              if (!vIn[w]) { vIn[w] = 1; next.push_back(w); }
+            }
+          }
+        front.swap(next);
+      }
+    }
+    struct Img { int top, set, cell; };
+    std::vector<Img> imgs;
+    for (int ic = 0; ic < nc; ++ic) {
+      const int mk = nearMask[ic];
+      for (int Sm = mk; Sm > 0; Sm = (Sm - 1) & mk) {
+        bool ok = true;
+        for (int a = 0; a < np && ok; ++a)
+          if ((Sm >> a & 1) && (Sm & parallel[a])) ok = false;
+        if (!ok) continue;
+        int top = 0;
+        while ((Sm >> (top + 1)) != 0) ++top;
+        imgs.push_back({top, Sm, ic});
+      }
+    }
+    std::sort(imgs.begin(), imgs.end(), [](const Img &x, const Img &y) {
+      if (x.top != y.top) return x.top < y.top;
+      if (x.set != y.set) return x.set < y.set;
+      return x.cell < y.cell;
+    });
+    // reflections Q_S = Q_a1 Q_a2 ... in plane order (RFLU_RELP_TransformMatrix's I - 2 n n^T)
+    std::map<int, int> xfOf;
+    auto xfIndex = [&](int Sm) {
+      auto it = xfOf.find(Sm);
+      if (it != xfOf.end()) return it->second;
+      std::array<double, 9> Q{};
+      bool first = true;
+      for (int a = 0; a < np; ++a) {
+        if (!(Sm >> a & 1)) continue;
+        const double nx = planes[a].n[0], ny = planes[a].n[1], nz = planes[a].n[2];
+        const double Qa[9] = {1.0 - 2.0 * nx * nx, -2.0 * nx * ny, -2.0 * nx * nz,
+                              -2.0 * nx * ny, 1.0 - 2.0 * ny * ny, -2.0 * ny * nz,
+                              -2.0 * nx * nz, -2.0 * ny * nz, 1.0 - 2.0 * nz * nz};
+        if (first) {
+          for (int k = 0; k < 9; ++k) Q[k] = Qa[k];
+          first = false;
+          continue;
+        }
+        std::array<double, 9> P;
+        for (int r = 0; r < 3; ++r)
+          for (int col = 0; col < 3; ++col) {
+            double t = Q[3 * r] * Qa[col];
+            t = t + Q[3 * r + 1] * Qa[3 + col];
+            t = t + Q[3 * r + 2] * Qa[6 + col];
+            P[3 * r + col] = t;
+          }
+        Q = P;
+      }
+      const int idx = (int)xfQ.size();
+      xfQ.push_back(Q);
+      xfOf[Sm] = idx;
+      return idx;
+    };
+    for (int a = 0; a < np; ++a) xfIndex(1 << a);
+    std::map<std::pair<int, int>, int> vext;
+    for (const Img &im : imgs) {
+      imgCell.push_back(im.cell);
+      imgXf.push_back(xfIndex(im.set));
+      double x[3] = {S->cofg[3 * (size_t)im.cell], S->cofg[3 * (size_t)im.cell + 1], S->cofg[3 * (size_t)im.cell + 2]};
+      for (int a = 0; a < np; ++a) {
+        if (!(im.set >> a & 1)) continue;
+        const double *n = planes[a].n, *p0 = planes[a].p0;
+        const double h = (x[0] - p0[0]) * n[0] + (x[1] - p0[1]) * n[1] + (x[2] - p0[2]) * n[2];
+        for (int d = 0; d < 3; ++d) x[d] = x[d] - 2.0 * h * n[d];
+      }
+      for (int d = 0; d < 3; ++d) imgPos.push_back(x[d]);
+      for (int k = 0; k < nvc; ++k) {
+        const int v = vert(im.cell, k);
+        const int Sv = im.set & ~vmask[v];
+        if (Sv == 0) {
+          imgC2v.push_back(v);
+          continue;
+        }
+        auto it = vext.find({v, Sv});
+        if (it == vext.end()) it = vext.emplace(std::make_pair(v, Sv), nvExt++).first;
+        imgC2v.push_back(it->second);
+      }
+    }
+  }
+
   // ---- C2C stencils and moments (ORDER > 1) ---------------------------------
   S->c2csOff.assign(nc + 1, 0);
   if (spaceOrder > 1) {
     const int minSize = 4, maxSize = 40, maxLayers = 6;
-    std::vector<int> v2cOff(nv + 1, 0);
-    for (int ic = 0; ic < nc; ++ic)
-      for (int k = 0; k < nvc; ++k) v2cOff[vid(ic, k) + 1]++;
-    for (int v = 0; v < nv; ++v) v2cOff[v + 1] += v2cOff[v];
-    std::vector<int> v2c(v2cOff[nv]);
+    // the cells and the symmetry images (ids nc + k) with their vertices
+    const int ne = nc + (int)imgCell.size();
+    auto cellVert = [&](int e, int k) { return e < nc ? vid(e, k) : imgC2v[(size_t)nvc * (e - nc) + k]; };
+    std::vector<int> v2cOff(nvExt + 1, 0);
+    for (int ic = 0; ic < ne; ++ic)
+      for (int k = 0; k < nvc; ++k) v2cOff[cellVert(ic, k) + 1]++;
+    for (int v = 0; v < nvExt; ++v) v2cOff[v + 1] += v2cOff[v];
+    std::vector<int> v2c(v2cOff[nvExt]);
     {
       std::vector<int> fill(v2cOff.begin(), v2cOff.end() - 1);
-      for (int ic = 0; ic < nc; ++ic)
-        for (int k = 0; k < nvc; ++k) v2c[fill[vid(ic, k)]++] = ic;
+      for (int ic = 0; ic < ne; ++ic)
+        for (int k = 0; k < nvc; ++k) v2c[fill[cellVert(ic, k)]++] = ic;
     }
     std::vector<std::vector<int>> memb(nc);
     const double invNv = 1.0 / (double)nvc;
@@ -684,7 +876,7 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
         std::sort(sv.begin(), sv.end());
         frac.resize(nCand);
         for (int i = 0; i < nCand; ++i) {
-          for (int k = 0; k < nvc; ++k) sv2[k] = vid(cand[i], k);
+          for (int k = 0; k < nvc; ++k) sv2[k] = cellVert(cand[i], k);
           std::sort(sv2.begin(), sv2.end());
           int shared = 0;
           for (int a = 0, b = 0; a < nvc && b < nvc;) {
@@ -726,7 +918,7 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
           bool full = false;
           for (int i = layerBeg; i < layerEnd && !full; ++i)
             for (int k = 0; k < nvc && !full; ++k) {
-              int v = vid(st[i], k);
+              int v = cellVert(st[i], k);
               for (int e = v2cOff[v]; e < v2cOff[v + 1]; ++e) {
                 int c2 = v2c[e];
                 if (c2 == ic || std::binary_search(have.begin(), have.end(), c2)) continue;
@@ -747,17 +939,28 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
     for (int ic = 0; ic < nc; ++ic) S->c2csOff[ic + 1] = S->c2csOff[ic] + (int)memb[ic].size();
     S->c2csMembs.resize(S->c2csOff[nc]);
     for (int ic = 0; ic < nc; ++ic)
-      for (size_t k = 0; k < memb[ic].size(); ++k) S->c2csMembs[S->c2csOff[ic] + k] = memb[ic][k] + 1;
+      for (size_t k = 0; k < memb[ic].size(); ++k) {
+        const int j = memb[ic][k];
+        S->c2csMembs[S->c2csOff[ic] + k] = (j < nc ? j : imgCell[j - nc]) + 1;
+      }
+    if (!imgCell.empty()) {
+      S->c2csXf.assign(S->c2csOff[nc], -1);
+      for (int ic = 0; ic < nc; ++ic)
+        for (size_t k = 0; k < memb[ic].size(); ++k)
+          if (memb[ic][k] >= nc) S->c2csXf[S->c2csOff[ic] + k] = imgXf[memb[ic][k] - nc];
+      for (const auto &Q : xfQ) S->xfQ.insert(S->xfQ.end(), Q.begin(), Q.end());
+    }
     // stencil moments: RFLU_ComputeStencilMoments3D1 (modflu/RFLU_ModWeights.F90:1770-1915)
     S->xyzMoms.assign(10 * (size_t)nc, 0.0);
-    if (periodic) S->c2csShift.assign(3 * (size_t)S->c2csOff[nc], 0.0);
+    const bool shifts = periodic || !imgCell.empty();
+    if (shifts) S->c2csShift.assign(3 * (size_t)S->c2csOff[nc], 0.0);
 #pragma omp parallel for schedule(static)
     for (int ic = 0; ic < nc; ++ic) {
       double mm[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (int e = S->c2csOff[ic]; e < S->c2csOff[ic + 1]; ++e) {
-        int j = S->c2csMembs[e] - 1;
+        int j = memb[ic][e - S->c2csOff[ic]];
         double dx, dy, dz;
-        memberOffset(cg, ic, j, dx, dy, dz, periodic ? &S->c2csShift[3 * (size_t)e] : nullptr);
+        memberOffset(cg, ic, j, dx, dy, dz, shifts ? &S->c2csShift[3 * (size_t)e] : nullptr);
         double wt = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
         dx = wt * dx; dy = wt * dy; dz = wt * dz;
         mm[0] = mm[0] + dx * dx; mm[1] = mm[1] + dx * dy; mm[2] = mm[2] + dy * dy;
@@ -806,6 +1009,9 @@ extern "C" int rflu_setup_grid(rflu_setup *S, rflu_grid_desc *g) {
   g->xyzMoms = S->xyzMoms.empty() ? nullptr : S->xyzMoms.data();
   g->fc2 = S->fc2.empty() ? nullptr : S->fc2.data();
   g->c2csShift = S->c2csShift.empty() ? nullptr : S->c2csShift.data();
+  g->c2csXf = S->c2csXf.empty() ? nullptr : S->c2csXf.data();
+  g->nXf = (int)(S->xfQ.size() / 9);
+  g->xfQ = S->xfQ.empty() ? nullptr : S->xfQ.data();
   return RFLU_OK;
 }
 

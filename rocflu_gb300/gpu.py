@@ -44,7 +44,8 @@ class GridDesc(C.Structure):
                 ("c2csOff", C.POINTER(C.c_int)), ("c2csMembs", C.POINTER(C.c_int)),
                 ("xyzMoms", C.POINTER(C.c_double)), ("patchVals", C.POINTER(C.c_double)),
                 ("patchSwitches", C.POINTER(C.c_int)), ("fc2", C.POINTER(C.c_double)),
-                ("c2csShift", C.POINTER(C.c_double))]
+                ("c2csShift", C.POINTER(C.c_double)), ("c2csXf", C.POINTER(C.c_int)), ("nXf", C.c_int),
+                ("xfQ", C.POINTER(C.c_double))]
 
 BCDAT_N, BCSWI_N = 8, 2
 
@@ -231,6 +232,10 @@ class Setup:
         # stencil members' image translations
         self.fc2 = np.ctypeslib.as_array(g.fc2, (nf, 3)).copy() if g.fc2 else None
         self.c2cs_shift = np.ctypeslib.as_array(g.c2csShift, (max(nnz, 1), 3))[:nnz].copy() if g.c2csShift else None
+        # symmetry meshes: each stencil member's reflection (-1: none) and the
+        # reflections' velocity matrices
+        self.c2cs_xf = np.ctypeslib.as_array(g.c2csXf, (max(nnz, 1),))[:nnz].copy() if g.c2csXf else None
+        self.xf_q = np.ctypeslib.as_array(g.xfQ, (g.nXf, 3, 3)).copy() if g.xfQ else None
         L.rflu_setup_destroy(self.h)
         self.h = None
 
@@ -258,13 +263,18 @@ def grid_desc(case, grid):
     shift = getattr(grid, "c2cs_shift", None)
     arrs["fc2"] = None if fc2 is None else np.ascontiguousarray(fc2, np.float64)
     arrs["shift"] = None if shift is None else np.ascontiguousarray(shift, np.float64)
+    xf, xq = getattr(grid, "c2cs_xf", None), getattr(grid, "xf_q", None)
+    arrs["xf"] = None if xf is None else np.ascontiguousarray(xf, np.int32)
+    arrs["xq"] = None if xq is None else np.ascontiguousarray(xq, np.float64)
     a = arrs
     gd = GridDesc(nc, int(a["f2c"].shape[0]), _p(a["f2c"], C.c_int), _p(a["fn"]), _p(a["fc"]), _p(a["vol"]),
                   _p(a["cofg"]), len(case.patches), _p(a["off"], C.c_int), _p(a["bf2c"], C.c_int), _p(a["bfn"]),
                   _p(a["bfc"]), _p(a["pt"], C.c_int), _p(a["po"], C.c_int), _p(a["pp"]), _p(a["pr"], C.c_int),
                   _p(a["soff"], C.c_int), _p(a["smem"], C.c_int), _p(a["moms"]), _p(a["pv"]),
                   _p(a["psw"], C.c_int), None if a["fc2"] is None else _p(a["fc2"]),
-                  None if a["shift"] is None else _p(a["shift"]))
+                  None if a["shift"] is None else _p(a["shift"]),
+                  None if a["xf"] is None else _p(a["xf"], C.c_int), 0 if a["xq"] is None else len(a["xq"]),
+                  None if a["xq"] is None else _p(a["xq"]))
     return gd, arrs
 
 

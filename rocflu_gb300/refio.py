@@ -337,7 +337,8 @@ def patch_kinds_from_bc(bc_deck, n_patches, order_default=1):
     SLIP in degrees, PRESS, TEMP, CORR); BC_INFLOW / BC_INFLOW_TOTANG (TYPE,
     FIXED, PTOT, TTOT, BETAH and BETAV in degrees, MACH unless subsonic);
     BC_INFLOW_VELTEMP (TYPE, VELX, VELY, VELZ, TEMP, PRESS unless subsonic);
-    BC_INJECT (MFRATE, TEMP); each over PATCH lo hi (1-based), ORDER 2 or the
+    BC_INJECT (MFRATE, TEMP); BC_SYMMETRY; BC_PERIODIC with RELPATCH lo hi
+    (translational: ANGLE 0); each over PATCH lo hi (1-based), ORDER 2 or the
     boundary-face order.  Angles are converted with the reference's
     global%deg2rad (libflu/RFLU_InitGlobal.F90:331-333).  Other conditions
     raise ValueError."""
@@ -379,18 +380,31 @@ def patch_kinds_from_bc(bc_deck, n_patches, order_default=1):
                     "vals": (f(s, "VELX"), f(s, "VELY"), f(s, "VELZ"), f(s, "TEMP"), press)}
         if sec == "BC_INJECT":
             return {"bc_type": cases.BC_INJECTION, "vals": (f(s, "MFRATE"), f(s, "TEMP"))}
+        if sec == "BC_SYMMETRY":
+            return {"bc_type": cases.BC_SYMMETRY}
+        if sec == "BC_PERIODIC":
+            if f(s, "ANGLE", 0.0) != 0.0:
+                raise ValueError("bc: rotational periodic patches are not on this path")
+            return {"bc_type": cases.BC_PERIODIC}
         return None
 
     known = ("BC_SLIPW", "BC_OUTFLOW", "BC_NOSLIP", "BC_NOSLIP_HFLUX", "BC_NOSLIP_TEMP", "BC_FARF", "BC_INFLOW",
-             "BC_INFLOW_TOTANG", "BC_INFLOW_VELTEMP", "BC_INJECT")
+             "BC_INFLOW_TOTANG", "BC_INFLOW_VELTEMP", "BC_INJECT", "BC_SYMMETRY", "BC_PERIODIC")
     kinds = [None] * n_patches
     for sec in known:
         for s in bc_deck.get(sec + "*", []):
             lo, hi = (int(float(v)) for v in s["PATCH"].split()[:2])
             k = kind_of(sec, s)
+            # (a symmetry face is an interior face to its virtual cell: the
+            # device takes the interior order there whatever the patch's)
             k["order"] = 2 if int(float(s.get("ORDER", order_default))) == 2 else 1
+            rel = None
+            if sec == "BC_PERIODIC":
+                if "RELPATCH" not in s:
+                    raise ValueError("bc: BC_PERIODIC needs RELPATCH")
+                rel = int(float(s["RELPATCH"].split()[0]))
             for p in range(lo, hi + 1):
-                kinds[p - 1] = k
+                kinds[p - 1] = dict(k, related=(rel + p - lo - 1)) if rel is not None else k
     others = [k for k in bc_deck if k.startswith("BC_") and not k.endswith("*") and k not in known]
     if others or any(k is None for k in kinds):
         raise ValueError("bc: conditions not on this path (%s)" % ", ".join(others))

@@ -144,7 +144,7 @@ ORDER      2
     assert num1.c_reconst == 1 and num1.c_reconst_weight == 1.0
     with pytest.raises(ValueError):
         refio.numerics_from_deck(refio.apply_overrides(deck, {"NUMERICS/CRECONSTC": 2}))
-    with pytest.raises(ValueError):
+    with pytest.raises(ValueError, match="RELPATCH"):
         refio.patch_kinds_from_bc(refio.read_deck("# BC_PERIODIC\nPATCH 1 6\n#\n"), 6)
 
 

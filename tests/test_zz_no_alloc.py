@@ -88,6 +88,24 @@ def test_residual_static_open_patches_and_constrained(gpu_lib, precision, crecon
     np.testing.assert_array_equal(rhs_dev.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("precision", ["fp64_exact", "mixed"])
+def test_residual_static_symmetry_mesh(gpu_lib, precision):
+    """Symmetry patches: the reflected stencil members (their reflections and
+    offsets) and the patches' reflections are context data the static entry
+    reads as the allocating one does."""
+    import torch
+
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=cases.RECONST_WENO_XYZ, cfl=0.4)
+    c = cases.mirror_box(6, axes=(0, 1, 2), num=num)
+    r = gpu.Region(c, precision)
+    ref, _ = r.residual(c.cv0, with_grad=False)
+    cv_dev = torch.from_numpy(np.ascontiguousarray(c.cv0)).cuda()
+    rhs_dev = torch.full_like(cv_dev, float("nan"))
+    torch.cuda.synchronize()
+    r.residual_static(cv_dev.data_ptr(), rhs_dev.data_ptr())
+    np.testing.assert_array_equal(rhs_dev.cpu().numpy(), ref)
+
+
 def test_residual_static_rejects_oversized_mesh(gpu_lib):
     import torch
 
