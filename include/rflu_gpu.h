@@ -232,7 +232,12 @@ int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *
  * order perturbation (the tangent uses the same linearisation).  RECONST 1
  * and 2: the WENO averages are differentiated (weights included) and the
  * simple limiter through its branch (a zeroed gradient has no derivative);
- * the smoothing's transpose is a gather over the transposed stencil. */
+ * the smoothing's transpose is a gather over the transposed stencil.
+ * CRECONSTC 1: the constrained fit is differentiated through its planned
+ * weights (constant constraint values at the walls); a burning injection
+ * patch's constraints, whose values follow the pressure of the face's
+ * cell: RFLU_ERR_UNSUPPORTED.  Periodic and symmetry meshes:
+ * RFLU_ERR_UNSUPPORTED. */
 int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar);
 /* Tangent of the same residual: rhsDot = (dR/dcv) cvDot (every limiter,
  * the WENO smoothing included). */

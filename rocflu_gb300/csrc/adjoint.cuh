@@ -102,6 +102,48 @@ __host__ __device__ inline bool isWeno(const Params &P) {
   return P.spaceOrder > 1 && (P.reconst == 1 || P.reconst == 2);
 }
 
+// Constrained gradients (CRECONSTC 1) in the tangent and the adjoint: the
+// fit of a constrained variable is linear in its rows' differences (the
+// stencil members' and the constraint values, constant at the walls; the
+// burning injection's, which depend on the pressure, are refused), so its
+// transpose takes the plan's weights where the least-squares fit takes the
+// members' weights.  The plan's rows per constrained variable: its stencil
+// rows in stencil order, then its constraint rows.
+template <typename R>
+__device__ inline int constrMask(const View<R> &V, int i, int &sl) {
+  sl = V.cSlot ? V.cSlot[i] : -1;
+  if (sl < 0) return 0;
+  int m = 0;
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+    if (V.cNcon[5 * sl + k]) m |= 1 << k;
+  return m;
+}
+// the first row of constrained variable k of slot sl (nst stencil members)
+template <typename R>
+__device__ inline int constrRow0(const View<R> &V, int sl, int k, int nst) {
+  int r = V.cRowOff[sl];
+  for (int kk = 0; kk < k; ++kk) {
+    const int nc = V.cNcon[5 * sl + kk];
+    if (nc) r += nst + nc;
+  }
+  return r;
+}
+// the own term of cell i's constrained variables: every row's difference
+// subtracts the cell's value
+template <typename R>
+__device__ inline void constrOwnTerm(const View<R> &V, int i, int sl, const R *gb, R *qb) {
+  const int nst = V.stOff[i + 1] - V.stOff[i];
+  int r = V.cRowOff[sl];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int nc = V.cNcon[5 * sl + k];
+    for (int t = 0; t < (nc ? nst + nc : 0); ++t, ++r)
+      qb[k] -= V.cW[3 * (size_t)r] * gb[3 * k] + V.cW[3 * (size_t)r + 1] * gb[3 * k + 1] +
+               V.cW[3 * (size_t)r + 2] * gb[3 * k + 2];
+  }
+}
+
 // Primitive state and dependent variables of one cell as functions of cv:
 // RFLU_ConvertCvCons2Prim (DUVWP) and RFLU_SetDependentVars.
 template <typename S>
@@ -641,6 +683,10 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
     W.ssum[i] = sx0;
     W.ssum[n + i] = sy0;
     W.ssum[2 * n + i] = sz0;
+    if (V.cSlot) {
+      const int sl = V.cSlot[i];
+      if (sl >= 0) constrainedGrad(V, ld, i, sl, q, g);
+    }
   } else {
     for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
       const int j = V.stIdx[s];
@@ -655,6 +701,10 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
         g[3 * k + 1] = g[3 * k + 1] + wy * d;
         g[3 * k + 2] = g[3 * k + 2] + wz * d;
       }
+    }
+    if (V.cSlot) {
+      const int sl = V.cSlot[i];
+      if (sl >= 0) constrainedGrad(V, ld, i, sl, q, g);
     }
   }
 #pragma unroll
@@ -901,23 +951,46 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int 
 
 // Side adjoints -> primitive / gradient adjoints of the cell, limiter reverse,
 // gradient own-term.  kVel: with the eigen-frame velocity limiter (RECONST 10).
+// FP64 layouts: the own term of the LSQ gradient's transpose (or, for a
+// constrained variable, of its rows) on the cell's primitive adjoint.
+template <typename R>
+__device__ inline void adjOwnTermFp64(const View<R> &V, int i, const R *gb, R *qb) {
+  int sl;
+  const int cm = constrMask(V, i, sl);
+  for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
+    R wx, wy, wz;
+    lsqWeight(V, i, s, wx, wy, wz);
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+      if (!((cm >> k) & 1)) qb[k] -= wx * gb[3 * k] + wy * gb[3 * k + 1] + wz * gb[3 * k + 2];
+  }
+  if (cm) constrOwnTerm(V, i, sl, gb, qb);
+}
+
 // Packed layout: the own term of the LSQ gradient's transpose on the cell's
 // primitive adjoint, and the cell's record L_i Gbar_i for the neighbour terms
 // (kAdjCell2).  w_s = L_i d_s/|d_s|^2 with L_i symmetric: sum_s w_s . Gbar_k
 // = (sum_s d_s/|d_s|^2) . (L_i Gbar_k).
+// A constrained variable's record entries are zero (its rows' weights are
+// not of that form): its own term is taken here and its neighbour terms by
+// kAdjCell2's constrained pass.
 template <typename R>
 __device__ inline void adjOwnTerm(const View<R> &V, const AdjWork<R> &W, int i, const float *gb, float *qb) {
   const size_t n = V.nc;
   const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
   const float lyy = V.lsq[3 * n + i], lyz = V.lsq[4 * n + i], lzz = V.lsq[5 * n + i];
+  int sl;
+  const int cm = constrMask(V, i, sl);
   float h[16];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const float x = gb[3 * k], y = gb[3 * k + 1], z = gb[3 * k + 2];
-    h[3 * k] = lxx * x + lxy * y + lxz * z;
-    h[3 * k + 1] = lxy * x + lyy * y + lyz * z;
-    h[3 * k + 2] = lxz * x + lyz * y + lzz * z;
+    const bool con = (cm >> k) & 1;
+    h[3 * k] = con ? 0.f : lxx * x + lxy * y + lxz * z;
+    h[3 * k + 1] = con ? 0.f : lxy * x + lyy * y + lyz * z;
+    h[3 * k + 2] = con ? 0.f : lxz * x + lyz * y + lzz * z;
   }
+  if (cm) constrOwnTerm(V, i, sl, gb, qb);
   if (V.p.spaceOrder > 1) {
     const float sx = W.ssum[i], sy = W.ssum[n + i], sz = W.ssum[2 * n + i];
 #pragma unroll
@@ -1084,12 +1157,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   }
   // gradient own-term: G_i = sum_s w_s (q_{m_s} - q_i)
   if constexpr (!Layout<R>::packed) {
-    for (int s = V.stOff[i]; s < V.stOff[i + 1] && P.spaceOrder > 1 && !weno; ++s) {
-      R wx, wy, wz;
-      lsqWeight(V, i, s, wx, wy, wz);
-#pragma unroll
-      for (int k = 0; k < 5; ++k) qb[k] -= wx * gb[3 * k] + wy * gb[3 * k + 1] + wz * gb[3 * k + 2];
-    }
+    if (P.spaceOrder > 1 && !weno) adjOwnTermFp64(V, i, gb, qb);
   }
 #pragma unroll
   for (int k = 0; k < 15; ++k)
@@ -1206,12 +1274,11 @@ __global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
   if constexpr (Layout<R>::packed) {
     adjOwnTerm(V, W, m, tb, qb);
   } else {
-    for (int s = V.stOff[m]; s < V.stOff[m + 1]; ++s) {
-      R wx, wy, wz;
-      lsqWeight(V, m, s, wx, wy, wz);
-#pragma unroll
-      for (int k = 0; k < 5; ++k) qb[k] -= wx * tb[3 * k] + wy * tb[3 * k + 1] + wz * tb[3 * k + 2];
-    }
+    adjOwnTermFp64(V, m, tb, qb);
+  }
+  // the raw gradient's adjoint (the FP64 layouts' neighbour terms, and the
+  // constrained cells' in every layout)
+  if (!Layout<R>::packed || V.cSlot) {
 #pragma unroll
     for (int k = 0; k < 15; ++k) W.Gbar[k * n + m] = tb[k];
   }
@@ -1247,9 +1314,30 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
         const int i = V.tsCell[e], s = V.tsEnt[e];
         R wx, wy, wz;
         lsqWeight(V, i, s, wx, wy, wz);
+        int sl;
+        const int cm = V.cSlot ? constrMask(V, i, sl) : 0;
 #pragma unroll
-        for (int k = 0; k < 5; ++k)
+        for (int k = 0; k < 5; ++k) {
+          if ((cm >> k) & 1) continue;
           qb[k] += wx * W.Gbar[(3 * k) * n + i] + wy * W.Gbar[(3 * k + 1) * n + i] + wz * W.Gbar[(3 * k + 2) * n + i];
+        }
+      }
+    }
+    // constrained cells holding j: their constrained variables' rows
+    if (V.cSlot) {
+      for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
+        const int i = V.tsCell[e];
+        int sl;
+        const int cm = constrMask(V, i, sl);
+        if (!cm) continue;
+        const int nst = V.stOff[i + 1] - V.stOff[i], so = V.tsEnt[e] - V.stOff[i];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          if (!((cm >> k) & 1)) continue;
+          const int r = constrRow0(V, sl, k, nst) + so;
+          qb[k] += V.cW[3 * (size_t)r] * W.Gbar[(3 * k) * n + i] + V.cW[3 * (size_t)r + 1] * W.Gbar[(3 * k + 1) * n + i] +
+                   V.cW[3 * (size_t)r + 2] * W.Gbar[(3 * k + 2) * n + i];
+        }
       }
     }
   }

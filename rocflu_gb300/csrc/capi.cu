@@ -283,6 +283,7 @@ struct Ctx : CtxBase {
   std::vector<void *> allocs;
   double *staging = nullptr;     // (15, nc) doubles: transfers in reference order
   bool imageMesh = false;        // the grid came with periodic or symmetry images (fc2 / c2csShift / c2csXf)
+  bool constrBurning = false;    // a constrained gradient (CRECONSTC 1) holds a burning injection face's row
   double *work = nullptr;        // adjoint workspace (allocated by the first adjoint call)
   int tsWidthLazy = 0;           // ... and the width of its transposed-stencil weights
   size_t workBytes = 0;
@@ -588,7 +589,8 @@ struct Ctx : CtxBase {
   int vjp(const double *cv, const double *rhsBar, double *cvBar) override {
     invalidate();
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
-    if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through constrained gradients (CRECONSTC 1)");
+    if (constrBurning)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through a burning injection patch's constrained gradients (CRECONSTC 1)");
     if (imageMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint on a mesh with periodic or symmetry patches");
     View<R> W;
     int rc = adjointPrep(cv, &W);
@@ -602,7 +604,8 @@ struct Ctx : CtxBase {
   int jvp(const double *cv, const double *cvDot, double *rhsDot) override {
     invalidate();
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
-    if (V.cSlot) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through constrained gradients (CRECONSTC 1)");
+    if (constrBurning)
+      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through a burning injection patch's constrained gradients (CRECONSTC 1)");
     if (imageMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent on a mesh with periodic or symmetry patches");
     View<R> W;
     int rc = adjointPrep(cv, &W);
@@ -631,8 +634,9 @@ struct Ctx : CtxBase {
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
     if (cvBar && imageMesh)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient on a mesh with periodic or symmetry patches");
-    if (cvBar && V.cSlot)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient through constrained gradients (CRECONSTC 1)");
+    if (cvBar && constrBurning)
+      return fail(RFLU_ERR_UNSUPPORTED,
+                  "rflu_gpu_patch_pressure: no gradient through a burning injection patch's constrained gradients (CRECONSTC 1)");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -838,8 +842,9 @@ struct Ctx : CtxBase {
     if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
       return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
-    if (V.cSlot)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: constrained gradients (CRECONSTC 1) have no adjoint");
+    if (constrBurning)
+      return fail(RFLU_ERR_UNSUPPORTED,
+                  "rflu_gpu_unrolled_adjoint: a burning injection patch's constrained gradients (CRECONSTC 1) have no adjoint");
     if (imageMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint on a mesh with periodic or symmetry patches");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     if (int rc0 = ensureAdjoint()) return rc0;
@@ -970,7 +975,7 @@ struct Ctx : CtxBase {
   int adjointTimes(int nIter, double *ms) override {
     invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
-    if (!ops->vjp || V.cSlot || imageMesh)
+    if (!ops->vjp || constrBurning || imageMesh)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
     if (int rc0 = ensureAdjoint()) return rc0;
     const size_t nc = V.nc;
@@ -1481,6 +1486,14 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
                                     " is singular (RFLU_ComputeGradCellsConstr stops there)");
     std::vector<int> slot(nc, -1);
     for (size_t k = 0; k < plan.cells.size(); ++k) slot[newId[plan.cells[k]]] = (int)k;
+    // a burning injection face's constraint values follow the pressure of
+    // its cell, which the tangent and the adjoint do not differentiate
+    for (int b : plan.rowFace)
+      if (b >= 0) {
+        int ip = 0;
+        while (ip + 1 < np && b >= g->patchFaceOff[ip + 1]) ++ip;
+        if (pType[ip] == RFLU_BC_INJECTION && minj[ip] > 0.0) constrBurning = true;
+      }
     std::vector<R> w(plan.w.begin(), plan.w.end());
     if (plan.cells.empty()) plan.rowFace.push_back(-1);
     PUT(V.cSlot, slot, int); PUT(V.cNcon, plan.nCon, int); PUT(V.cRowOff, plan.rowOff, int);

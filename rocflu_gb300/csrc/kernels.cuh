@@ -571,6 +571,10 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       g[3 * k + 1] = lxy * x + lyy * y + lyz * z;
       g[3 * k + 2] = lxz * x + lyz * y + lzz * z;
     }
+    if (V.cSlot) {
+      const int sl = V.cSlot[i];
+      if (sl >= 0) constrainedGrad(V, ld, i, sl, q, g);
+    }
   }
   const int rc = V.p.reconst;
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];

@@ -197,6 +197,68 @@ def test_weno_positivity_zeroing_has_no_derivative(gpu_lib):
     assert kept >= 4
 
 
+def _constrained(which, reconst, prec_case=None):
+    num = cases.Numerics(space_order=2, space_discr=cases.DISCR_HLLC, reconst=reconst, cfl=0.4, c_reconst=1)
+    if which == "tets":
+        c = cases.adjoint_tets(4, num=num)  # slip walls on y and z
+        for p in c.patches:
+            p.order = 2
+        return c
+    # inflow, outflow, farfield, a no-slip wall and a non-burning injection wall
+    return cases.open_channel(6, num=num, inflow=cases.BC_INFLOW_VELTEMP, injection=0.0)
+
+
+@pytest.mark.parametrize("which", ["tets", "channel"])
+@pytest.mark.parametrize("reconst", [cases.RECONST_NONE, cases.RECONST_BJ, cases.RECONST_BJ_COMP, cases.RECONST_WENO_XYZ])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
+def test_constrained_dot_product(gpu_lib, which, reconst, prec, tol):
+    """CRECONSTC 1 (gradients constrained at the wall and injection faces):
+    the tangent through the constrained fit (dual numbers over the plan's
+    rows) and the adjoint (the plan's rows transposed over the transposed
+    stencil) are each other's transpose."""
+    c = _constrained(which, reconst)
+    r = gpu.Region(c, prec)
+    rng = np.random.default_rng(7)
+    for v in _dirs(c, 3, 1):
+        lam = rng.standard_normal(c.cv0.shape)
+        jv, jtl = r.jvp(c.cv0, v), r.vjp(c.cv0, lam)
+        a, b = (lam * jv).sum(), (jtl * v).sum()
+        if prec == "fp64":
+            assert abs(a - b) <= tol * max(abs(a), abs(b)), (a, b)
+        else:
+            scale = max(np.abs(lam * jv).sum(), np.abs(jtl * v).sum())
+            assert abs(a - b) <= tol * scale, (a, b, scale)
+
+
+@pytest.mark.parametrize("which", ["tets", "channel"])
+def test_constrained_vjp_vs_central_differences(gpu_lib, which):
+    """FP64, componentwise BJ with CRECONSTC 1: the VJP against central
+    differences of the residual (eps = 1e-6) on 32 directions; every
+    direction that keeps all limiter branches agrees to 1e-6."""
+    c = _constrained(which, cases.RECONST_BJ_COMP)
+    r = gpu.Region(c, "fp64")
+    lam = np.random.default_rng(11).standard_normal(c.cv0.shape)
+    g = r.vjp(c.cv0, lam)
+    eps = 1e-6
+    errs, sw = [], []
+    f = lambda cv: (lam * r.residual(cv, with_grad=False)[0]).sum()  # noqa: E731
+    for v in _dirs(c, 32, 3):
+        fd = _cd(f, c.cv0, v, eps, False)
+        ad = (g * v).sum()
+        errs.append(abs(fd - ad) / max(abs(ad), 1e-30))
+        sw.append(_switches(r, c.cv0, v, eps))
+    errs, sw = np.array(errs), np.array(sw)
+    assert (~sw).sum() >= 8, sw.sum()
+    assert (errs[~sw] < 1e-6).all(), (errs[~sw].max(), np.flatnonzero(~sw & (errs >= 1e-6)))
+
+
+def test_constrained_mixed_vjp_against_fp64(gpu_lib):
+    c = _constrained("channel", cases.RECONST_WENO_XYZ)
+    lam = np.random.default_rng(3).standard_normal(c.cv0.shape)
+    gm, g64 = gpu.Region(c, "mixed").vjp(c.cv0, lam), gpu.Region(c, "fp64").vjp(c.cv0, lam)
+    assert np.linalg.norm(gm - g64) <= 1e-4 * np.linalg.norm(g64)
+
+
 def test_limiter_branches_record(gpu_lib):
     """rflu_gpu_limiter_branches: componentwise BJ reports per variable the
     active face (an index among the cell's faces) and the neighbour holding

@@ -4,7 +4,9 @@ five RK steps) with the eigen-frame BJ limiter and with WENO-XYZ, on hex and
 tet meshes with slip walls, a no-slip wall and burning / non-burning
 injection; FP64 within 1e-10; the mixed mode (tiled and untiled gradient
 kernels) within L1(rho) 1e-5 after five steps.  The tangent and adjoint
-refuse the setting."""
+refuse a burning injection patch's constraints (their values follow the
+pressure of the face's cell); the others are differentiated
+(tests/test_gpu_adjoint.py)."""
 import numpy as np
 import pytest
 
@@ -75,10 +77,12 @@ def test_constrained_differs_from_unconstrained(gpu_lib):
     assert np.abs(g1 - g0).max() > 1e-4
 
 
-def test_constrained_adjoint_refused(gpu_lib):
-    c = _cases(cases.RECONST_BJ)[0]
+def test_constrained_burning_injection_adjoint_refused(gpu_lib):
+    c = _cases(cases.RECONST_BJ)[0]  # burning injection at z-low
     r = gpu.Region(c, "fp64")
     for call in (lambda: r.vjp(c.cv0, c.cv0), lambda: r.jvp(c.cv0, c.cv0)):
         with pytest.raises(gpu.RfluError) as e:
             call()
-        assert e.value.code == -3 and "CRECONSTC" in str(e.value)
+        assert e.value.code == -3 and "burning injection" in str(e.value)
+    c = _cases(cases.RECONST_BJ)[1]  # the same wall not burning: accepted
+    gpu.Region(c, "fp64").vjp(c.cv0, c.cv0)
