@@ -1522,6 +1522,23 @@ __global__ void kPatchSeed(View<R> V, AdjWork<R> W, int ip, double *Jout) {
   if (threadIdx.x == 0) *Jout = part[0];
 }
 
+// A second stream of the adjoint's launches, with the events that fork it
+// from and join it to the calling stream (created once per process).
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+inline SideStream &sideStream() {
+  static SideStream ss = [] {
+    SideStream x;
+    cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&x.fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming);
+    return x;
+  }();
+  return ss;
+}
+
 template <typename R>
 struct AdjointOps {
   static void jvp(const View<R> &V, const double *cvDotRef, double *rhsDotRef, double *work, cudaStream_t s) {
@@ -1544,14 +1561,27 @@ struct AdjointOps {
     if (isWeno(V.p)) kAdjWeno<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     kAdjCell2<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvBarRef);
   }
+  // The boundary faces' kernel (dual numbers through the patch fluxes; few
+  // faces, a small grid) runs on a second stream beside the interior faces'
+  // (they write disjoint face-adjoint entries), forked from and joined
+  // back to s by events, so that it fills the SMs the interior kernel's
+  // last wave leaves idle.
   static void faceAdjoint(const View<R> &V, const AdjWork<R> &W, cudaStream_t s) {
     const int nT = V.nf + V.nb;
-    if (V.p.spaceOrder > 1 && V.p.spaceDiscr == 1) {
-      if (V.nf > 0) kAdjFace<R, true><<<blocks((long long)V.nf), kBlock, 0, s>>>(V, W, 0, V.nf);
-      if (V.nb > 0) kAdjFace<R, false><<<blocks((long long)V.nb), kBlock, 0, s>>>(V, W, V.nf, nT);
-    } else if (nT > 0) {
-      kAdjFace<R, false><<<blocks((long long)nT), kBlock, 0, s>>>(V, W, 0, nT);
+    const bool roe2 = V.p.spaceOrder > 1 && V.p.spaceDiscr == 1;
+    if (V.nf == 0 || V.nb == 0) {
+      if (nT > 0 && !(roe2 && V.nb == 0)) kAdjFace<R, false><<<blocks((long long)nT), kBlock, 0, s>>>(V, W, 0, nT);
+      else if (nT > 0) kAdjFace<R, true><<<blocks((long long)nT), kBlock, 0, s>>>(V, W, 0, nT);
+      return;
     }
+    SideStream &ss = sideStream();
+    cudaEventRecord(ss.fork, s);
+    cudaStreamWaitEvent(ss.stream, ss.fork, 0);
+    kAdjFace<R, false><<<blocks((long long)V.nb), kBlock, 0, ss.stream>>>(V, W, V.nf, nT);
+    cudaEventRecord(ss.join, ss.stream);
+    if (roe2) kAdjFace<R, true><<<blocks((long long)V.nf), kBlock, 0, s>>>(V, W, 0, V.nf);
+    else kAdjFace<R, false><<<blocks((long long)V.nf), kBlock, 0, s>>>(V, W, 0, V.nf);
+    cudaStreamWaitEvent(s, ss.join, 0);
   }
   static void vjp(const View<R> &V, const double *rhsBarRef, double *cvBarRef, double *work, cudaStream_t s) {
     const size_t nT = (size_t)V.nf + V.nb;
