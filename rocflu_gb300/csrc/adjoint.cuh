@@ -1159,9 +1159,12 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
   if constexpr (!Layout<R>::packed) {
     if (P.spaceOrder > 1 && !weno) adjOwnTermFp64(V, i, gb, qb);
   }
+  // the raw gradient's adjoint: the FP64 layouts' neighbour terms read it,
+  // the packed layout's only for constrained cells (its records carry L Gbar)
+  if (!weno && (!Layout<R>::packed || V.cSlot)) {
 #pragma unroll
-  for (int k = 0; k < 15; ++k)
-    if (!weno) W.Gbar[k * n + i] = gb[k];
+    for (int k = 0; k < 15; ++k) W.Gbar[k * n + i] = gb[k];
+  }
   if constexpr (Layout<R>::packed) {
     if (!weno) adjOwnTerm(V, W, i, gb, qb);
   }
@@ -1181,8 +1184,10 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     st4(nr, __int_as_float(nbt[0]), __int_as_float(nbt[1]), __int_as_float(nbt[2]), __int_as_float(nbt[3]));
     st4(nr + 4, __int_as_float(nbt[4]), nbb[0], nbb[1], nbb[2]);
     st4(nr + 8, nbb[3], nbb[4], nbv[0], nbv[1]);
-    st4(nr + 12, nbv[2], nbv[3], nbv[4], nbv[5]);
-    st4(nr + 16, nbv[6], nbv[7], nbv[8], 0.f);
+    if (kVel) {  // the axes' vectors: read by kAdjCell2 for RECONST 10 only
+      st4(nr + 12, nbv[2], nbv[3], nbv[4], nbv[5]);
+      st4(nr + 16, nbv[6], nbv[7], nbv[8], 0.f);
+    }
   } else {
 #pragma unroll
     for (int k = 0; k < 5; ++k) W.nbBar[k * n + i] = nbb[k];
