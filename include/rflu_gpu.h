@@ -236,7 +236,8 @@ int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *
  * CRECONSTC 1: the constrained fit is differentiated through its planned
  * weights (constant constraint values at the walls); a burning injection
  * patch's constraints, whose values follow the pressure of the face's
- * cell: RFLU_ERR_UNSUPPORTED.  Periodic and symmetry meshes:
+ * cell: RFLU_ERR_UNSUPPORTED.  Periodic meshes: members and faces across
+ * a period through their images' translations; symmetry patches:
  * RFLU_ERR_UNSUPPORTED. */
 int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar);
 /* Tangent of the same residual: rhsDot = (dR/dcv) cvDot (every limiter,

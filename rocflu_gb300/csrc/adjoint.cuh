@@ -657,7 +657,12 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
     for (int s = V.stOff[i]; s < V.stOff[i + 1]; ++s) {
       float r[8];
       ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
-      const float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+      float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
+      if (V.stShift) {  // a periodic mesh: the member's image
+        dx = dx + V.stShift[3 * (size_t)s];
+        dy = dy + V.stShift[3 * (size_t)s + 1];
+        dz = dz + V.stShift[3 * (size_t)s + 2];
+      }
       const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
       const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
       sx0 += sx;

@@ -189,9 +189,14 @@ __device__ inline void lsqWeight(const View<R> &V, int i, int s, R &wx, R &wy, R
   if constexpr (Layout<R>::packed) {
     const int j = V.stIdx[s];
     const size_t n = V.nc;
-    const float dx = V.prim[8 * (size_t)j + 5] - V.prim[8 * (size_t)i + 5];
-    const float dy = V.prim[8 * (size_t)j + 6] - V.prim[8 * (size_t)i + 6];
-    const float dz = V.prim[8 * (size_t)j + 7] - V.prim[8 * (size_t)i + 7];
+    float dx = V.prim[8 * (size_t)j + 5] - V.prim[8 * (size_t)i + 5];
+    float dy = V.prim[8 * (size_t)j + 6] - V.prim[8 * (size_t)i + 6];
+    float dz = V.prim[8 * (size_t)j + 7] - V.prim[8 * (size_t)i + 7];
+    if (V.stShift) {  // a periodic mesh: the member's image
+      dx = dx + V.stShift[3 * (size_t)s];
+      dy = dy + V.stShift[3 * (size_t)s + 1];
+      dz = dz + V.stShift[3 * (size_t)s + 2];
+    }
     const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
     const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
     const float lxx = V.lsq[i], lxy = V.lsq[n + i], lxz = V.lsq[2 * n + i];
@@ -550,7 +555,12 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
     for (int s = sb; s < se; ++s) {
       S qj[5], xj[3];
       ld.primCg(V.stIdx[s], qj, xj);
-      const S dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = xj[2] - xi[2];
+      S dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = xj[2] - xi[2];
+      if (V.stShift) {  // a periodic mesh: the member's image
+        dx = dx + S(V.stShift[3 * (size_t)s]);
+        dy = dy + S(V.stShift[3 * (size_t)s + 1]);
+        dz = dz + S(V.stShift[3 * (size_t)s + 2]);
+      }
       const S inv = S(1) / (dx * dx + dy * dy + dz * dz);
       const S sx = inv * dx, sy = inv * dy, sz = inv * dz;
 #pragma unroll
@@ -1767,7 +1777,13 @@ __global__ void kTsWeights(View<R> V) {
       float4 w = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
       if (k < c) {
         const int i = V.tsCell[b + k];
-        const float dx = xj - V.cgx[i], dy = yj - V.cgy[i], dz = zj - V.cgz[i];
+        float dx = xj - V.cgx[i], dy = yj - V.cgy[i], dz = zj - V.cgz[i];
+        if (V.stShift) {  // a periodic mesh: j seen from i as its image
+          const size_t e = V.tsEnt[b + k];
+          dx = dx + V.stShift[3 * e];
+          dy = dy + V.stShift[3 * e + 1];
+          dz = dz + V.stShift[3 * e + 2];
+        }
         const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
         w = make_float4(inv * dx, inv * dy, inv * dz, __int_as_float(i));
       }
