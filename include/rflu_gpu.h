@@ -237,8 +237,9 @@ int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *
  * weights (constant constraint values at the walls); a burning injection
  * patch's constraints, whose values follow the pressure of the face's
  * cell: RFLU_ERR_UNSUPPORTED.  Periodic meshes: members and faces across
- * a period through their images' translations; symmetry patches:
- * RFLU_ERR_UNSUPPORTED. */
+ * a period through their images' translations; symmetry patches: the
+ * reflected members' values and gradients through their reflections, a
+ * symmetry face's flux and limiter terms through the cell's reflection. */
 int rflu_gpu_vjp(rflu_gpu_ctx *ctx, const double *cv, const double *rhsBar, double *cvBar);
 /* Tangent of the same residual: rhsDot = (dR/dcv) cvDot (every limiter,
  * the WENO smoothing included). */

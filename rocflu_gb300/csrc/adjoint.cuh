@@ -144,6 +144,19 @@ __device__ inline void constrOwnTerm(const View<R> &V, int i, int sl, const R *g
   }
 }
 
+// Symmetry patches in the tangent and the adjoint: a reflected stencil
+// member's velocity is Q u (memberReflection), and a face on a symmetry
+// patch is a face to the cell's own reflection, which the limiters' branch
+// records mark as the neighbour kMirrorNb - b (b the boundary face): its
+// extreme value's derivative goes back to the cell itself through Q.
+constexpr int kMirrorNb = -2;
+template <typename R>
+__device__ inline const R *memberReflection(const View<R> &V, int s) {
+  if (!V.stXf) return nullptr;
+  const int x = V.stXf[s];
+  return x >= 0 ? V.xfQ + 9 * x : nullptr;
+}
+
 // Primitive state and dependent variables of one cell as functions of cv:
 // RFLU_ConvertCvCons2Prim (DUVWP) and RFLU_SetDependentVars.
 template <typename S>
@@ -309,7 +322,10 @@ __global__ void __launch_bounds__(kBlock) kTanWeno(View<R> V, AdjWork<R> W) {
       t[k].d[0] = W.Gbar[k * n + c];
     }
   };
-  auto fetch = [&](int s, S *t) { row(V.stIdx[s], t); };
+  auto fetch = [&](int s, S *t) {
+    row(V.stIdx[s], t);
+    if (const R *Q = memberReflection(V, s)) reflectGrad(Q, t);
+  };
   const int sb = V.stOff[i], se = V.stOff[i + 1];
   S own[16], g[15];
   row(i, own);
@@ -412,24 +428,38 @@ __device__ inline void velFrameForward(const View<R> &V, const L &ld, int i, con
   R dmn[3] = {R(0), R(0), R(0)}, dmx[3] = {R(0), R(0), R(0)};
   int nmn[3] = {-1, -1, -1}, nmx[3] = {-1, -1, -1};
   const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
+  R ui[4];
+  ld.prim4(i, ui);
   for (int e = cb; e < ce; ++e) {
     const int code = V.cfEnt[e];
-    if (code < 0) continue;
-    int c1, c2;
-    faceCells(V, code >> 1, c1, c2);
-    R a1[4], a2[4], du[3];
-    ld.prim4(c1, a1);
-    ld.prim4(c2, a2);
+    R du[3];
+    int other;
+    if (code < 0) {
+      // a symmetry face: the cell's reflection as the second cell
+      const double *Q = symmetryQ(V, code);
+      if (!Q) continue;
+      R um[3];
+      reflect3(Q, ui + 1, um);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) du[k] = a2[1 + k] - a1[1 + k];
-    const int other = (code & 1) ? c1 : c2;
+      for (int k = 0; k < 3; ++k) du[k] = um[k] - ui[1 + k];
+      other = kMirrorNb - (-code - 1);
+    } else {
+      int c1, c2;
+      faceCells(V, code >> 1, c1, c2);
+      R a1[4], a2[4];
+      ld.prim4(c1, a1);
+      ld.prim4(c2, a2);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) du[k] = a2[1 + k] - a1[1 + k];
+      other = (code & 1) ? c1 : c2;
+    }
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       R pr = R(0);
       pr = pr + A[3 * j] * du[0];
       pr = pr + A[3 * j + 1] * du[1];
       pr = pr + A[3 * j + 2] * du[2];
-      if (code & 1) pr = -pr;
+      if (code >= 0 && (code & 1)) pr = -pr;
       if (pr < dmn[j]) { dmn[j] = pr; nmn[j] = other; }
       if (pr > dmx[j]) { dmx[j] = pr; nmx[j] = other; }
     }
@@ -440,9 +470,8 @@ __device__ inline void velFrameForward(const View<R> &V, const L &ld, int i, con
   }
   for (int e = cb; e < ce; ++e) {
     const int code = V.cfEnt[e];
-    if (code < 0) continue;
     R d[3];
-    faceOffset(V, code >> 1, code & 1, d);
+    if (!limiterFaceOffset(V, code, d)) continue;
     const R off[3] = {-d[0], -d[1], -d[2]};
     R sh[3];
 #pragma unroll
@@ -575,11 +604,25 @@ __device__ inline void velFrameReverse(const View<R> &V, const L &ld, int i, con
         nbv[3 * j + a] = dextb * A[a + 3 * j];
         ub[a] -= dextb * A[a + 3 * j];
       }
+    } else if (F.nb[j] <= kMirrorNb) {
+      // the extreme is the cell's reflection Q u across a symmetry face:
+      // dext = A_j . (Q u - u), its derivative (Q - I) A_j (Q symmetric)
+      const int ip = V.bpatch[kMirrorNb - F.nb[j]];
+      const double *Q = V.patchK + kPatchK * ip;
+      R un[3], qa[3];
+      reflect3(Q, ui + 1, un);
+      const R aj[3] = {A[3 * j], A[3 * j + 1], A[3 * j + 2]};
+      reflect3(Q, aj, qa);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        Ab[a + 3 * j] += dextb * (un[a] - ui[1 + a]);
+        ub[a] += dextb * (qa[a] - A[a + 3 * j]);
+      }
     }
     // pr = A_j . G off, off = cofg - fc of the active face
     const int code = V.cfEnt[F.face[j]];
     R d[3];
-    faceOffset(V, code >> 1, code & 1, d);
+    limiterFaceOffset(V, code, d);
     const R off[3] = {-d[0], -d[1], -d[2]};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -658,10 +701,14 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
       float r[8];
       ld8(V.prim + 8 * (size_t)V.stIdx[s], r);
       float dx = r[5] - rec[5], dy = r[6] - rec[6], dz = r[7] - rec[7];
-      if (V.stShift) {  // a periodic mesh: the member's image
+      if (V.stShift) {  // a periodic or symmetry mesh: the member's image
         dx = dx + V.stShift[3 * (size_t)s];
         dy = dy + V.stShift[3 * (size_t)s + 1];
         dz = dz + V.stShift[3 * (size_t)s + 2];
+        if (const float *Q = memberReflection(V, s)) {
+          const float u[3] = {r[1], r[2], r[3]};
+          reflect3(Q, u, r + 1);
+        }
       }
       const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
       const float sx = inv * dx, sy = inv * dy, sz = inv * dz;
@@ -699,6 +746,10 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
       lsqWeight(V, i, s, wx, wy, wz);
       R qj[5];
       ld.prim5(j, qj);
+      if (const R *Q = memberReflection(V, s)) {
+        const R u[3] = {qj[1], qj[2], qj[3]};
+        reflect3(Q, u, qj + 1);
+      }
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         R d = qj[k] - q[k];
@@ -725,12 +776,21 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
     const int cb = V.cfOff[i], ce = V.cfOff[i + 1];
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
-      if (code < 0) continue;
-      int c1, c2;
-      faceCells(V, code >> 1, c1, c2);
-      const int nb = (code & 1) ? c1 : c2;
+      int nb;
       R x[5];
-      ld.prim5(nb, x);
+      if (code < 0) {
+        const double *Q = symmetryQ(V, code);
+        if (!Q) continue;
+        nb = kMirrorNb - (-code - 1);  // the cell's reflection across this face
+        x[0] = q[0];
+        reflect3(Q, q + 1, x + 1);
+        x[4] = q[4];
+      } else {
+        int c1, c2;
+        faceCells(V, code >> 1, c1, c2);
+        nb = (code & 1) ? c1 : c2;
+        ld.prim5(nb, x);
+      }
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         if (x[k] < vmin[k]) { vmin[k] = x[k]; jmin[k] = nb; }
@@ -740,9 +800,8 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
     const R epsq = V.epsq[i];
     for (int e = cb; e < ce; ++e) {
       const int code = V.cfEnt[e];
-      if (code < 0) continue;
       R d[3];
-      faceOffset(V, code >> 1, code & 1, d);
+      if (!limiterFaceOffset(V, code, d)) continue;
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         if (rc == 10 && k >= 1 && k <= 3) continue;  // the eigen-frame limiter below
@@ -814,7 +873,10 @@ __global__ void __launch_bounds__(kBlock) kAdjWenoFwd(View<R> V, AdjWork<R> W) {
       for (int k = 0; k < 15; ++k) t[k] = W.G[k * n + c];
     }
   };
-  auto fetch = [&](int s, R *t) { row(V.stIdx[s], t); };
+  auto fetch = [&](int s, R *t) {
+    row(V.stIdx[s], t);
+    if (const R *Q = memberReflection(V, s)) reflectGrad(Q, t);
+  };
   const int sb = V.stOff[i], se = V.stOff[i + 1];
   R own[16], g[15], sum[15];
   row(i, own);
@@ -924,6 +986,49 @@ __global__ void __launch_bounds__(kBlock) kAdjFace(View<R> V, AdjWork<R> W, int 
 #pragma unroll
     for (int k = 0; k < 5; ++k) fbar[k] = W.cvd[k * n + c];
     if (patchLeavesDensity(type)) fbar[0] = R(0);  // walls leave rhs(DENS)
+    if (type == kBcSymmetry) {
+      // the interior flux against the cell's own reflection (faceFluxEval):
+      // both sides follow the cell, so the seeds are on its side only and
+      // the reflected side carries them through Q.  First order: (cv, dv)
+      // of the cell, 8 values; second order: the face state and the cell's
+      // 1/rho, 6 values, as an interior face's first side
+      const double *Q = V.patchK + kPatchK * ip;
+      if (P.spaceOrder == 1) {
+        using D8 = Dual<8>;
+        D8 cl[5], dl[3], cr[5], flx[5];
+        double fb[5], o8[8];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          cl[k] = D8::seed(V.cv[k * n + c], k);
+          fb[k] = (double)fbar[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dl[k] = D8::seed(V.dv[k * n + c], 5 + k);
+        cr[0] = cl[0];
+        reflect3(Q, cl + 1, cr + 1);
+        cr[4] = cl[4];
+        riemann1(P, cl, dl, cr, dl, D8((double)V.bnx[b]), D8((double)V.bny[b]), D8((double)V.bnz[b]),
+                 D8((double)V.bnm[b]), flx);
+        contract(flx, fb, o8);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) out[m] = (R)o8[m];
+      } else {
+        using D6 = Dual<6, R>;
+        const size_t nb = V.nb;
+        R L[5], irl;
+        faceState(V, ld, c, V.bd[b], V.bd[nb + b], V.bd[2 * nb + b], L, irl);
+        D6 a[5], r[5], ia, flx[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) a[k] = D6::seed(L[k], k);
+        ia = D6::seed(irl, 5);
+        r[0] = a[0];
+        reflect3(Q, a + 1, r + 1);
+        r[4] = a[4];
+        riemann2(P, D6(V.bnx[b]), D6(V.bny[b]), D6(V.bnz[b]), D6(V.bnm[b]), a, ia, r, ia, flx);
+        contract(flx, fbar, out);
+      }
+      return;
+    }
     if (order == 1) {
       using D6 = Dual<6>;
       D6 cv[5], flx[5];
@@ -1047,7 +1152,27 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     } else {
       const int b = -code - 1;
       const R *a = W.faceAdj + 16 * (size_t)(V.nf + b);
-      if (V.patchOrder[V.bpatch[b]] == 1) {
+      if (symmetryQ(V, code)) {
+        // an interior face to the cell's reflection, at the interior order:
+        // first order (cv, dv) adjoints, second order the face state's and
+        // the cell 1/rho's (kAdjFace)
+        if (P.spaceOrder == 1) {
+#pragma unroll
+          for (int k = 0; k < 5; ++k) cvb[k] += a[k];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) dvb[k] += a[5 + k];
+        } else {
+          const R dx = V.bd[b], dy = V.bd[nb + b], dz = V.bd[2 * nb + b];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            qb[k] += a[k];
+            gtb[3 * k] += a[k] * dx;
+            gtb[3 * k + 1] += a[k] * dy;
+            gtb[3 * k + 2] += a[k] * dz;
+          }
+          rbar += a[5];
+        }
+      } else if (V.patchOrder[V.bpatch[b]] == 1) {
 #pragma unroll
         for (int k = 0; k < 5; ++k) cvb[k] += a[k];
         dvb[0] += a[5];
@@ -1085,14 +1210,24 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
     if ((rc == 11 || rc == 100 || rc == 10) && es >= 0) {
       const int code = V.cfEnt[es];
       R dxyz[3];
-      faceOffset(V, code >> 1, code & 1, dxyz);
+      limiterFaceOffset(V, code, dxyz);
       R g3[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) g3[c] = W.G[(3 * k + c) * n + i];
       const R d2 = -(g3[0] * dxyz[0] + g3[1] * dxyz[1] + g3[2] * dxyz[2]);
       const int js = W.jstar[k * n + i];
       const R qi = ld.prim(k, i);
-      const R dext = (js >= 0 ? ld.prim(k, js) : qi) - qi;
+      // the extreme: a neighbour's value, none (the cell's own), or the
+      // cell's reflection across a symmetry face (velocity: (Q u)_k)
+      const double *Qm = (js <= kMirrorNb) ? V.patchK + kPatchK * V.bpatch[kMirrorNb - js] : nullptr;
+      R qm = qi;
+      if (Qm && k >= 1 && k <= 3) {
+        R u[3], um[3];
+        u[0] = ld.prim(1, i); u[1] = ld.prim(2, i); u[2] = ld.prim(3, i);
+        reflect3(Qm, u, um);
+        qm = um[k - 1];
+      }
+      const R dext = (js >= 0 ? ld.prim(k, js) : qm) - qi;
       R db, d2b;
       if (rc == 11) {
         using D2 = Dual<2, R>;
@@ -1114,6 +1249,11 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
         qb[k] -= db;
         nbb[k] = db;
         nbt[k] = js;
+      } else if (Qm && k >= 1 && k <= 3) {
+        // d((Q u)_k - u_k)/du = Q(k, :) - e_k
+        qb[k] -= db;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) qb[1 + a] += db * R(Qm[3 * (k - 1) + a]);
       }
     }
   }
@@ -1230,10 +1370,11 @@ __global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
   if (m >= V.nc) return;
   const size_t n = V.nc;
   const PlainLoad<R> ld{V};
-  R A[15], B[15];
+  R A[15], B[15], A2[15], B2[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) A[k] = B[k] = R(0);
-  auto add = [&](int i) {
+  // the a-terms and a g of cell i into (Ac, Bc)
+  auto addTo = [&](int i, R *Ac, R *Bc) {
     if constexpr (Layout<R>::packed) {
       float a[16], g[16];
       ld8(V.gradRaw + 16 * (size_t)i, a);
@@ -1242,42 +1383,75 @@ __global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
       ld8(V.grad + 16 * (size_t)i + 8, g + 8);
 #pragma unroll
       for (int k = 0; k < 15; ++k) {
-        A[k] += a[k];
-        B[k] += a[k] * g[k];
+        Ac[k] += a[k];
+        Bc[k] += a[k] * g[k];
       }
     } else {
 #pragma unroll
       for (int k = 0; k < 15; ++k) {
         const R a = W.gradd[k * n + i];
-        A[k] += a;
-        B[k] += a * ld.grad(k, i);
+        Ac[k] += a;
+        Bc[k] += a * ld.grad(k, i);
       }
     }
   };
-  add(m);
-  for (int e = V.tsOff[m]; e < V.tsOff[m + 1]; ++e) add(V.tsCell[e]);
+  auto add2 = [&](int i) { addTo(i, A2, B2); };
+  auto add = [&](int i) { addTo(i, A, B); };
+
   R t[15], tb[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) t[k] = W.G[k * n + m];
   const R eps = R(1.0e-15);
-  if (V.p.reconst == 2) {
+  const bool xyz = V.p.reconst == 2;
+  // the adjoint of a member gradient tt from (sums of) the averages' terms
+  // a and a g that hold it: linear in (a, a g) for a fixed tt
+  auto reverse = [&](const R *tt, const R *a, const R *ag, R *out) {
+    if (xyz) {
 #pragma unroll
-    for (int k = 0; k < 15; ++k) {
-      const R w = R(1) / (t[k] * t[k] + eps);
-      const R wp = R(-2) * t[k] * w * w;
-      tb[k] = (w + wp * t[k]) * A[k] - wp * B[k];
+      for (int k = 0; k < 15; ++k) {
+        const R w = R(1) / (tt[k] * tt[k] + eps);
+        const R wp = R(-2) * tt[k] * w * w;
+        out[k] = (w + wp * tt[k]) * a[k] - wp * ag[k];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const R *tv = tt + 3 * v, *av = a + 3 * v, *bv = ag + 3 * v;
+        const R T = fabs_(tv[0]) + fabs_(tv[1]) + fabs_(tv[2]);
+        const R w = R(1) / (T * T + eps);
+        const R c = R(-2) * T * w * w * (tv[0] * av[0] + tv[1] * av[1] + tv[2] * av[2] - (bv[0] + bv[1] + bv[2]));
+#pragma unroll
+        for (int d = 0; d < 3; ++d) out[3 * v + d] = w * av[d] + (tv[d] < R(0) ? -c : c);
+      }
     }
-  } else {
+  };
+  // symmetry meshes: a cell whose average holds m reflected sees Q(t); its
+  // share is evaluated there and goes back through the (symmetric) transform
+  R tr[15];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      const R *tv = t + 3 * v, *av = A + 3 * v, *bv = B + 3 * v;
-      const R T = fabs_(tv[0]) + fabs_(tv[1]) + fabs_(tv[2]);
-      const R w = R(1) / (T * T + eps);
-      const R c = R(-2) * T * w * w * (tv[0] * av[0] + tv[1] * av[1] + tv[2] * av[2] - (bv[0] + bv[1] + bv[2]));
-#pragma unroll
-      for (int d = 0; d < 3; ++d) tb[3 * v + d] = w * av[d] + (tv[d] < R(0) ? -c : c);
+  for (int k = 0; k < 15; ++k) tr[k] = R(0);
+  add(m);
+  for (int e = V.tsOff[m]; e < V.tsOff[m + 1]; ++e) {
+    const R *Q = memberReflection(V, V.tsEnt[e]);
+    if (!Q) {
+      add(V.tsCell[e]);
+      continue;
     }
+#pragma unroll
+    for (int k = 0; k < 15; ++k) A2[k] = B2[k] = R(0);
+    add2(V.tsCell[e]);
+    R tq[16], c[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) tq[k] = t[k];
+    reflectGrad(Q, tq);
+    reverse(tq, A2, B2, c);
+    reflectGrad(Q, c);
+#pragma unroll
+    for (int k = 0; k < 15; ++k) tr[k] += c[k];
   }
+  reverse(t, A, B, tb);
+#pragma unroll
+  for (int k = 0; k < 15; ++k) tb[k] += tr[k];
   R qb[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) qb[k] = W.qbar[k * n + m];
@@ -1310,14 +1484,26 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
 #pragma unroll 2
       for (int k = 0; k < V.tsWidth; ++k) {
         const float4 w = ld4(V.tsW + 4 * (k * n + j));
-        const int i = __float_as_int(w.w);
-        if (i < 0) break;
+        const int tag = __float_as_int(w.w);
+        if (tag < 0) break;
+        const int i = tag & ~kTsReflected;
         float h[16];
         const float *rec = W.adjRec + 16 * (size_t)i;
         ld8(rec, h);
         ld8(rec + 8, h + 8);
+        float cb[5];
 #pragma unroll
-        for (int c = 0; c < 5; ++c) qb[c] += w.x * h[3 * c] + w.y * h[3 * c + 1] + w.z * h[3 * c + 2];
+        for (int c = 0; c < 5; ++c) cb[c] = w.x * h[3 * c] + w.y * h[3 * c + 1] + w.z * h[3 * c + 2];
+        if (tag & kTsReflected) {
+          // j entered i's gradient reflected: its velocity's share goes back
+          // through Q (symmetric)
+          const float *Q = memberReflection(V, V.tsEnt[V.tsOff[j] + k]);
+          float u[3];
+          reflect3(Q, cb + 1, u);
+          cb[1] = u[0]; cb[2] = u[1]; cb[3] = u[2];
+        }
+#pragma unroll
+        for (int c = 0; c < 5; ++c) qb[c] += cb[c];
       }
     } else {
       for (int e = V.tsOff[j]; e < V.tsOff[j + 1]; ++e) {
@@ -1326,11 +1512,19 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
         lsqWeight(V, i, s, wx, wy, wz);
         int sl;
         const int cm = V.cSlot ? constrMask(V, i, sl) : 0;
+        R cb[5];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          if ((cm >> k) & 1) continue;
-          qb[k] += wx * W.Gbar[(3 * k) * n + i] + wy * W.Gbar[(3 * k + 1) * n + i] + wz * W.Gbar[(3 * k + 2) * n + i];
+        for (int k = 0; k < 5; ++k)
+          cb[k] = ((cm >> k) & 1) ? R(0)
+                                  : wx * W.Gbar[(3 * k) * n + i] + wy * W.Gbar[(3 * k + 1) * n + i] +
+                                        wz * W.Gbar[(3 * k + 2) * n + i];
+        if (const R *Q = memberReflection(V, s)) {  // j entered i's gradient reflected
+          R u[3];
+          reflect3(Q, cb + 1, u);
+          cb[1] = u[0]; cb[2] = u[1]; cb[3] = u[2];
         }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) qb[k] += cb[k];
       }
     }
     // constrained cells holding j: their constrained variables' rows

@@ -284,7 +284,6 @@ struct Ctx : CtxBase {
   double *staging = nullptr;     // (15, nc) doubles: transfers in reference order
   bool imageMesh = false;        // the grid came with periodic or symmetry images (fc2 / c2csShift / c2csXf)
   bool constrBurning = false;    // a constrained gradient (CRECONSTC 1) holds a burning injection face's row
-  bool symmetryMesh = false;     // symmetry patches: no tangent or adjoint (their reflections are not differentiated)
   double *work = nullptr;        // adjoint workspace (allocated by the first adjoint call)
   int tsWidthLazy = 0;           // ... and the width of its transposed-stencil weights
   size_t workBytes = 0;
@@ -592,7 +591,6 @@ struct Ctx : CtxBase {
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
     if (constrBurning)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through a burning injection patch's constrained gradients (CRECONSTC 1)");
-    if (symmetryMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint on a mesh with symmetry patches");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -607,7 +605,6 @@ struct Ctx : CtxBase {
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
     if (constrBurning)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through a burning injection patch's constrained gradients (CRECONSTC 1)");
-    if (symmetryMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent on a mesh with symmetry patches");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -633,8 +630,6 @@ struct Ctx : CtxBase {
     invalidate();
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
-    if (cvBar && symmetryMesh)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_patch_pressure: no gradient on a mesh with symmetry patches");
     if (cvBar && constrBurning)
       return fail(RFLU_ERR_UNSUPPORTED,
                   "rflu_gpu_patch_pressure: no gradient through a burning injection patch's constrained gradients (CRECONSTC 1)");
@@ -846,7 +841,6 @@ struct Ctx : CtxBase {
     if (constrBurning)
       return fail(RFLU_ERR_UNSUPPORTED,
                   "rflu_gpu_unrolled_adjoint: a burning injection patch's constrained gradients (CRECONSTC 1) have no adjoint");
-    if (symmetryMesh) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint on a mesh with symmetry patches");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     if (int rc0 = ensureAdjoint()) return rc0;
     // the whole forward and reverse sweep runs on the scratch state X
@@ -976,7 +970,7 @@ struct Ctx : CtxBase {
   int adjointTimes(int nIter, double *ms) override {
     invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
-    if (!ops->vjp || constrBurning || symmetryMesh)
+    if (!ops->vjp || constrBurning)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
     if (int rc0 = ensureAdjoint()) return rc0;
     const size_t nc = V.nc;
@@ -1313,9 +1307,6 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
   std::vector<double> wx, wy, wz, epsq(nc, 0.0), lsq;
   std::vector<float> stShift;  // mixed mode on a periodic mesh: the members' translations
   imageMesh = g->c2csShift != nullptr || g->fc2 != nullptr || g->c2csXf != nullptr;
-  symmetryMesh = g->c2csXf != nullptr;
-  for (int ip = 0; ip < np; ++ip)
-    if (g->patchBcType[ip] == RFLU_BC_SYMMETRY && g->patchFaceOff[ip + 1] > g->patchFaceOff[ip]) symmetryMesh = true;
   std::vector<int> stXf;  // symmetry meshes: the members' reflections
   const bool mixed = num->precision == RFLU_PREC_MIXED;
   if (mixed && num->spaceOrder > 1) lsq.resize(6 * (size_t)nc);

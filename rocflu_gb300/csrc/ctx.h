@@ -63,6 +63,9 @@ struct Params {
 //                   modflu/RFLU_ModRelatedPatches.F90:449-514)
 constexpr int kPatchK = 16;
 constexpr int kBcSymmetry = 100;
+// The adjoint's transposed-stencil weights (View::tsW): bit 30 of an
+// entry's cell id marks a member seen reflected across symmetry patches.
+constexpr int kTsReflected = 1 << 30;
 constexpr int kTile = 256;
 // Shared-memory footprint of one staged tile of the mixed-mode gradient
 // kernel: 8 floats per record, the stencil ids as whole 16-byte words (plus

@@ -556,10 +556,14 @@ __device__ inline void gradLimitCell(const View<R> &V, const L &ld, int i, typen
       S qj[5], xj[3];
       ld.primCg(V.stIdx[s], qj, xj);
       S dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = xj[2] - xi[2];
-      if (V.stShift) {  // a periodic mesh: the member's image
+      if (V.stShift) {  // a periodic or symmetry mesh: the member's image
         dx = dx + S(V.stShift[3 * (size_t)s]);
         dy = dy + S(V.stShift[3 * (size_t)s + 1]);
         dz = dz + S(V.stShift[3 * (size_t)s + 2]);
+        if (V.stXf && V.stXf[s] >= 0) {
+          const S u[3] = {qj[1], qj[2], qj[3]};
+          reflect3(V.xfQ + 9 * V.stXf[s], u, qj + 1);
+        }
       }
       const S inv = S(1) / (dx * dx + dy * dy + dz * dz);
       const S sx = inv * dx, sy = inv * dy, sz = inv * dz;
@@ -1778,14 +1782,16 @@ __global__ void kTsWeights(View<R> V) {
       if (k < c) {
         const int i = V.tsCell[b + k];
         float dx = xj - V.cgx[i], dy = yj - V.cgy[i], dz = zj - V.cgz[i];
-        if (V.stShift) {  // a periodic mesh: j seen from i as its image
+        int tag = i;
+        if (V.stShift) {  // a periodic or symmetry mesh: j seen from i as its image
           const size_t e = V.tsEnt[b + k];
           dx = dx + V.stShift[3 * e];
           dy = dy + V.stShift[3 * e + 1];
           dz = dz + V.stShift[3 * e + 2];
+          if (V.stXf && V.stXf[e] >= 0) tag |= kTsReflected;  // seen reflected
         }
         const float inv = 1.f / (dx * dx + dy * dy + dz * dz);
-        w = make_float4(inv * dx, inv * dy, inv * dz, __int_as_float(i));
+        w = make_float4(inv * dx, inv * dy, inv * dz, __int_as_float(tag));
       }
       *reinterpret_cast<float4 *>(V.tsW + 4 * (k * n + j)) = w;
     }
