@@ -234,9 +234,8 @@ int rflu_gpu_residual(rflu_gpu_ctx *ctx, const double *cv, double *rhs, double *
  * simple limiter through its branch (a zeroed gradient has no derivative);
  * the smoothing's transpose is a gather over the transposed stencil.
  * CRECONSTC 1: the constrained fit is differentiated through its planned
- * weights (constant constraint values at the walls); a burning injection
- * patch's constraints, whose values follow the pressure of the face's
- * cell: RFLU_ERR_UNSUPPORTED.  Periodic meshes: members and faces across
+ * weights (constant constraint values at the walls; a burning injection
+ * face's values through the pressure of the face's cell).  Periodic meshes: members and faces across
  * a period through their images' translations; symmetry patches: the
  * reflected members' values and gradients through their reflections, a
  * symmetry face's flux and limiter terms through the cell's reflection. */

@@ -104,11 +104,12 @@ __host__ __device__ inline bool isWeno(const Params &P) {
 
 // Constrained gradients (CRECONSTC 1) in the tangent and the adjoint: the
 // fit of a constrained variable is linear in its rows' differences (the
-// stencil members' and the constraint values, constant at the walls; the
-// burning injection's, which depend on the pressure, are refused), so its
-// transpose takes the plan's weights where the least-squares fit takes the
-// members' weights.  The plan's rows per constrained variable: its stencil
-// rows in stencil order, then its constraint rows.
+// stencil members' and the constraint values, constant at the walls; a
+// burning injection face's follow its cell's pressure, whose adjoint gathers
+// them through the per-cell lists V.cpOff/V.cpEnt), so its transpose takes
+// the plan's weights where the least-squares fit takes the members' weights.
+// The plan's rows per constrained variable: its stencil rows in stencil
+// order, then its constraint rows.
 template <typename R>
 __device__ inline int constrMask(const View<R> &V, int i, int &sl) {
   sl = V.cSlot ? V.cSlot[i] : -1;
@@ -1476,7 +1477,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= V.nc) return;
   const size_t n = V.nc;
-  R qb[5];
+  R qb[5], pcon = R(0);
 #pragma unroll
   for (int k = 0; k < 5; ++k) qb[k] = W.qbar[k * n + j];
   if (V.tsOff && V.p.spaceOrder > 1) {
@@ -1542,6 +1543,27 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
           qb[k] += V.cW[3 * (size_t)r] * W.Gbar[(3 * k) * n + i] + V.cW[3 * (size_t)r + 1] * W.Gbar[(3 * k + 1) * n + i] +
                    V.cW[3 * (size_t)r + 2] * W.Gbar[(3 * k + 2) * n + i];
         }
+      }
+    }
+    // burning injection faces of j: their constraint rows' values follow j's
+    // pressure (constrValue: rho = p/(rgas T_inj), v = -(minj/rho) n), and
+    // their share reaches j as an adjoint of its pressure
+    if (V.cpOff) {
+      const double rgas = 8314.3 / V.p.gvMol;
+      const double p = V.dv[j];
+      for (int e = V.cpOff[j]; e < V.cpOff[j + 1]; ++e) {
+        const int i = V.cpEnt[2 * e], rk = V.cpEnt[2 * e + 1];
+        const int r = rk >> 3, k = rk & 7, b = V.cRowFace[r];
+        const double *K = V.patchK + kPatchK * V.bpatch[b];
+        const double rt = rgas * K[1];
+        double dval = 1.0 / rt;  // d rho / dp
+        if (k > 0) {
+          const double rl = p / rt, nk = (k == 1) ? V.bnx[b] : (k == 2) ? V.bny[b] : V.bnz[b];
+          dval = K[0] * nk / (rl * rl) * dval;
+        }
+        const R dot = V.cW[3 * (size_t)r] * W.Gbar[(3 * k) * n + i] + V.cW[3 * (size_t)r + 1] * W.Gbar[(3 * k + 1) * n + i] +
+                      V.cW[3 * (size_t)r + 2] * W.Gbar[(3 * k + 2) * n + i];
+        pcon += dot * (R)dval;
       }
     }
   }
@@ -1613,7 +1635,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
     out[2] += ir * qb[2];
     out[3] += ir * qb[3];
     // dv = (p, T, c): T = p/(r gc), c = sqrt(g gc T)
-    const float b0 = W.dvbar[j], b1 = W.dvbar[n + j], b2 = W.dvbar[2 * n + j];
+    const float b0 = W.dvbar[j] + pcon, b1 = W.dvbar[n + j], b2 = W.dvbar[2 * n + j];
     if (b0 != 0.f || b1 != 0.f || b2 != 0.f) {
       const float t = pr * ir / gc, c = sqrtf(g * gc * t);
       const float tb = b1 + b2 * 0.5f * g * gc / c;  // adjoint of T
@@ -1633,6 +1655,7 @@ __global__ void __launch_bounds__(kBlock) kAdjCell2(View<R> V, AdjWork<R> W, dou
     double dvb[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) dvb[k] = W.dvbar[k * n + j];
+    dvb[0] += pcon;
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
       double s = W.cvbarD[m * n + j];

@@ -283,7 +283,7 @@ struct Ctx : CtxBase {
   std::vector<void *> allocs;
   double *staging = nullptr;     // (15, nc) doubles: transfers in reference order
   bool imageMesh = false;        // the grid came with periodic or symmetry images (fc2 / c2csShift / c2csXf)
-  bool constrBurning = false;    // a constrained gradient (CRECONSTC 1) holds a burning injection face's row
+  bool constrBurning = false;    // a constrained gradient (CRECONSTC 1) holds a burning injection face's row (cpOff/cpEnt)
   double *work = nullptr;        // adjoint workspace (allocated by the first adjoint call)
   int tsWidthLazy = 0;           // ... and the width of its transposed-stencil weights
   size_t workBytes = 0;
@@ -589,8 +589,6 @@ struct Ctx : CtxBase {
   int vjp(const double *cv, const double *rhsBar, double *cvBar) override {
     invalidate();
     if (!cv || !rhsBar || !cvBar) return fail(RFLU_ERR_ARG, "rflu_gpu_vjp: null argument");
-    if (constrBurning)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_vjp: no adjoint through a burning injection patch's constrained gradients (CRECONSTC 1)");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -603,8 +601,6 @@ struct Ctx : CtxBase {
   int jvp(const double *cv, const double *cvDot, double *rhsDot) override {
     invalidate();
     if (!cv || !cvDot || !rhsDot) return fail(RFLU_ERR_ARG, "rflu_gpu_jvp: null argument");
-    if (constrBurning)
-      return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_jvp: no tangent through a burning injection patch's constrained gradients (CRECONSTC 1)");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -630,9 +626,6 @@ struct Ctx : CtxBase {
     invalidate();
     if (!cv || !J) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: null argument");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_patch_pressure: bad patch");
-    if (cvBar && constrBurning)
-      return fail(RFLU_ERR_UNSUPPORTED,
-                  "rflu_gpu_patch_pressure: no gradient through a burning injection patch's constrained gradients (CRECONSTC 1)");
     View<R> W;
     int rc = adjointPrep(cv, &W);
     if (rc) return rc;
@@ -838,9 +831,6 @@ struct Ctx : CtxBase {
     if (!cv0 || !Jout || nSteps < 1 || every < 1 || !(dt > 0.0))
       return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad arguments");
     if (!ops->vjp) return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_unrolled_adjoint: no adjoint kernels in this precision mode");
-    if (constrBurning)
-      return fail(RFLU_ERR_UNSUPPORTED,
-                  "rflu_gpu_unrolled_adjoint: a burning injection patch's constrained gradients (CRECONSTC 1) have no adjoint");
     if (iPatch < 0 || iPatch >= nPatches) return fail(RFLU_ERR_ARG, "rflu_gpu_unrolled_adjoint: bad patch");
     if (int rc0 = ensureAdjoint()) return rc0;
     // the whole forward and reverse sweep runs on the scratch state X
@@ -970,7 +960,7 @@ struct Ctx : CtxBase {
   int adjointTimes(int nIter, double *ms) override {
     invalidate();
     if (nIter <= 0 || !ms) return fail(RFLU_ERR_ARG, "rflu_gpu_adjoint_times: bad arguments");
-    if (!ops->vjp || constrBurning)
+    if (!ops->vjp)
       return fail(RFLU_ERR_UNSUPPORTED, "rflu_gpu_adjoint_times: no adjoint here");
     if (int rc0 = ensureAdjoint()) return rc0;
     const size_t nc = V.nc;
@@ -1482,13 +1472,38 @@ int Ctx<R>::create(const rflu_grid_desc *g, const rflu_num_desc *num) {
     std::vector<int> slot(nc, -1);
     for (size_t k = 0; k < plan.cells.size(); ++k) slot[newId[plan.cells[k]]] = (int)k;
     // a burning injection face's constraint values follow the pressure of
-    // its cell, which the tangent and the adjoint do not differentiate
-    for (int b : plan.rowFace)
-      if (b >= 0) {
-        int ip = 0;
-        while (ip + 1 < np && b >= g->patchFaceOff[ip + 1]) ++ip;
-        if (pType[ip] == RFLU_BC_INJECTION && minj[ip] > 0.0) constrBurning = true;
+    // its cell: per cell the (constrained cell, row, variable) entries it
+    // feeds, for the adjoint's gather (kAdjCell2)
+    std::vector<std::vector<int>> cpList(nc);
+    for (size_t sl = 0; sl < plan.cells.size(); ++sl) {
+      const int ci = newId[plan.cells[sl]];
+      const int nst = g->c2csOff[plan.cells[sl] + 1] - g->c2csOff[plan.cells[sl]];
+      int r = plan.rowOff[sl];
+      for (int k = 0; k < 5; ++k) {
+        const int ncon = plan.nCon[5 * sl + k];
+        if (!ncon) continue;
+        r += nst;
+        for (int c = 0; c < ncon; ++c, ++r) {
+          const int b = plan.rowFace[r];
+          if (b < 0) continue;
+          int ip = 0;
+          while (ip + 1 < np && b >= g->patchFaceOff[ip + 1]) ++ip;
+          if (!(pType[ip] == RFLU_BC_INJECTION && minj[ip] > 0.0) || k > 3) continue;
+          constrBurning = true;
+          cpList[newId[g->bf2c[b] - 1]].push_back(ci);
+          cpList[newId[g->bf2c[b] - 1]].push_back(8 * r + k);
+        }
       }
+    }
+    if (constrBurning) {
+      std::vector<int> cpOff(nc + 1, 0), cpEnt;
+      for (int i = 0; i < nc; ++i) {
+        cpEnt.insert(cpEnt.end(), cpList[i].begin(), cpList[i].end());
+        cpOff[i + 1] = (int)cpEnt.size() / 2;
+      }
+      PUT(V.cpOff, cpOff, int);
+      PUT(V.cpEnt, cpEnt, int);
+    }
     std::vector<R> w(plan.w.begin(), plan.w.end());
     if (plan.cells.empty()) plan.rowFace.push_back(-1);
     PUT(V.cSlot, slot, int); PUT(V.cNcon, plan.nCon, int); PUT(V.cRowOff, plan.rowOff, int);

@@ -112,6 +112,11 @@ struct View {
   // constraint row (-1: a stencil member's row)
   const int *cSlot, *cNcon, *cRowOff, *cRowFace;
   const R *cW;
+  // the adjoint of a burning injection face's constraint values, which
+  // follow the pressure of the face's cell: per cell (CSR, null: none) the
+  // (constrained cell, 8 * row + variable) pairs of the rows its pressure
+  // feeds
+  const int *cpOff, *cpEnt;
   // mixed mode on a periodic or symmetry mesh (untiled): each stencil
   // member's translation to its image, added to the centroid difference
   // (null: none)

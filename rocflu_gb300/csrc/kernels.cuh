@@ -382,15 +382,17 @@ __global__ void kInitFromRef(View<R> V, const double *ref, int o0, int o1) {
 // (fsu = 0) when it does not burn, else the density and velocity of
 // RFLU_SetRindStateInjectPerf (modflu/RFLU_ModRindStates.F90:459-501) from
 // the face cell's pressure.
-template <typename S, typename R>
-__device__ inline S constrValue(const View<R> &V, int b, int k) {
+template <typename S, typename R, typename L>
+__device__ inline S constrValue(const View<R> &V, const L &ld, int b, int k) {
   const int ip = V.bpatch[b];
   if (V.patchType[ip] != 90) return S(0);
   const double *K = V.patchK + kPatchK * ip;
   const S n = (k == 1) ? S(V.bnx[b]) : (k == 2) ? S(V.bny[b]) : S(V.bnz[b]);
   if (!(K[0] > 0.0)) return S(0) * n;
   const S rgas = S(8314.3) / S(V.p.gvMol);
-  const S rl = S(V.dv[V.bcell[b]]) / (rgas * S(K[1]));  // MixtPerf_D_PRT(pl, rGas, tInj)
+  // the face's cell pressure through the loader (the tangent's carries its
+  // derivative)
+  const S rl = S(ld.dv(0, V.bcell[b])) / (rgas * S(K[1]));  // MixtPerf_D_PRT(pl, rGas, tInj)
   if (k == 0) return rl;
   const S ql = -S(K[0]) / rl + S(0);
   return ql * n;
@@ -420,7 +422,7 @@ __device__ inline void constrainedGrad(const View<R> &V, const L &ld, int i, int
       gz = gz + S(V.cW[3 * (size_t)r + 2]) * d;
     }
     for (int c = 0; c < nCon; ++c, ++r) {
-      const S d = constrValue<S>(V, V.cRowFace[r], k) - q[k];
+      const S d = constrValue<S>(V, ld, V.cRowFace[r], k) - q[k];
       gx = gx + S(V.cW[3 * (size_t)r]) * d;
       gy = gy + S(V.cW[3 * (size_t)r + 1]) * d;
       gz = gz + S(V.cW[3 * (size_t)r + 2]) * d;

@@ -204,18 +204,24 @@ def _constrained(which, reconst, prec_case=None):
         for p in c.patches:
             p.order = 2
         return c
+    if which == "burning":
+        # a burning injection wall: its constraint values follow the pressure
+        # of the face's cell
+        return cases.open_channel(6, num=num, inflow=cases.BC_INFLOW_VELTEMP)
     # inflow, outflow, farfield, a no-slip wall and a non-burning injection wall
     return cases.open_channel(6, num=num, inflow=cases.BC_INFLOW_VELTEMP, injection=0.0)
 
 
-@pytest.mark.parametrize("which", ["tets", "channel"])
+@pytest.mark.parametrize("which", ["tets", "channel", "burning"])
 @pytest.mark.parametrize("reconst", [cases.RECONST_NONE, cases.RECONST_BJ, cases.RECONST_BJ_COMP, cases.RECONST_WENO_XYZ])
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
 def test_constrained_dot_product(gpu_lib, which, reconst, prec, tol):
     """CRECONSTC 1 (gradients constrained at the wall and injection faces):
     the tangent through the constrained fit (dual numbers over the plan's
-    rows) and the adjoint (the plan's rows transposed over the transposed
-    stencil) are each other's transpose."""
+    rows, the burning injection's values through the face cell's pressure)
+    and the adjoint (the plan's rows transposed over the transposed stencil,
+    the burning rows gathered by the face cell) are each other's
+    transpose."""
     c = _constrained(which, reconst)
     r = gpu.Region(c, prec)
     rng = np.random.default_rng(7)
@@ -230,7 +236,7 @@ def test_constrained_dot_product(gpu_lib, which, reconst, prec, tol):
             assert abs(a - b) <= tol * scale, (a, b, scale)
 
 
-@pytest.mark.parametrize("which", ["tets", "channel"])
+@pytest.mark.parametrize("which", ["tets", "channel", "burning"])
 def test_constrained_vjp_vs_central_differences(gpu_lib, which):
     """FP64, componentwise BJ with CRECONSTC 1: the VJP against central
     differences of the residual (eps = 1e-6) on 32 directions; every
@@ -252,8 +258,33 @@ def test_constrained_vjp_vs_central_differences(gpu_lib, which):
     assert (errs[~sw] < 1e-6).all(), (errs[~sw].max(), np.flatnonzero(~sw & (errs >= 1e-6)))
 
 
-def test_constrained_mixed_vjp_against_fp64(gpu_lib):
-    c = _constrained("channel", cases.RECONST_WENO_XYZ)
+def test_constrained_burning_vjp_vs_central_differences_unlimited(gpu_lib):
+    """FP64, no limiter, CRECONSTC 1 with a burning injection wall: the
+    residual is smooth, so every one of 16 directions agrees with central
+    differences (Richardson) to 1e-7, among them four that change only the
+    energy, hence the pressure, of the cells on the burning wall (z-low)."""
+    c = _constrained("burning", cases.RECONST_NONE)
+    r = gpu.Region(c, "fp64")
+    lam = np.random.default_rng(12).standard_normal(c.cv0.shape)
+    g = r.vjp(c.cv0, lam)
+    f = lambda cv: (lam * r.residual(cv, with_grad=False)[0]).sum()  # noqa: E731
+    zc = c.xyz[c.c2v].mean(axis=1)[:, 2]
+    wall = np.isclose(zc, zc.min())
+    rng = np.random.default_rng(6)
+    dirs = _dirs(c, 12, 5)
+    for _ in range(4):
+        v = np.zeros_like(c.cv0)
+        v[wall, 4] = rng.standard_normal(wall.sum()) * np.abs(c.cv0[:, 4]).mean()
+        dirs.append(v)
+    for v in dirs:
+        fd = _cd(f, c.cv0, v, 1e-5, True)
+        ad = (g * v).sum()
+        assert abs(fd - ad) <= 1e-7 * max(abs(ad), 1e-30), (fd, ad)
+
+
+@pytest.mark.parametrize("which", ["channel", "burning"])
+def test_constrained_mixed_vjp_against_fp64(gpu_lib, which):
+    c = _constrained(which, cases.RECONST_WENO_XYZ)
     lam = np.random.default_rng(3).standard_normal(c.cv0.shape)
     gm, g64 = gpu.Region(c, "mixed").vjp(c.cv0, lam), gpu.Region(c, "fp64").vjp(c.cv0, lam)
     assert np.linalg.norm(gm - g64) <= 1e-4 * np.linalg.norm(g64)
