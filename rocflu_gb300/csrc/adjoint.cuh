@@ -151,6 +151,16 @@ __device__ inline void constrOwnTerm(const View<R> &V, int i, int sl, const R *g
 // records mark as the neighbour kMirrorNb - b (b the boundary face): its
 // extreme value's derivative goes back to the cell itself through Q.
 constexpr int kMirrorNb = -2;
+
+// Threads per cell of the packed layout's WENO gathers (kAdjWeno over the
+// transposed stencil, kAdjWenoFwdLanes over the stencil): each lane every
+// second entry, the sums joined by shuffles.  (Measured: the same split of
+// kAdjCell2's and kAdjGradFwd's gathers, by entries or by record halves,
+// made them slower.)
+template <typename R>
+__host__ __device__ constexpr int adjLanes() {
+  return Layout<R>::packed ? 2 : 1;
+}
 template <typename R>
 __device__ inline const R *memberReflection(const View<R> &V, int s) {
   if (!V.stXf) return nullptr;
@@ -854,6 +864,21 @@ __global__ void __launch_bounds__(kBlock) kAdjGradFwd(View<R> V, AdjWork<R> W, c
   else storeGrad(V, i, gl);
 }
 
+// the simple positivity limiter, the factors, the weight sums and the
+// smoothed gradient of cell i
+template <typename R>
+__device__ inline void wenoFwdFinish(const View<R> &V, AdjWork<R> &W, int i, R *g, const R *sum, bool xyz) {
+  const size_t n = V.nc;
+  R f0, f4;
+  wenoPositivity(V, i, g, &f0, &f4);
+  W.lim[i] = f0;
+  W.lim[4 * n + i] = f4;
+#pragma unroll
+  for (int k = 0; k < 15; ++k)
+    if (xyz || k < 5) W.gradd[k * n + i] = sum[k];
+  storeGrad(V, i, g);
+}
+
 // Forward pass of the WENO smoothing (RECONST 1, 2) for the reverse pass:
 // each cell's smoothed and limited gradient from the unsmoothed ones
 // (written by kAdjGradFwd: W.G, and in the packed layout records in
@@ -884,14 +909,99 @@ __global__ void __launch_bounds__(kBlock) kAdjWenoFwd(View<R> V, AdjWork<R> W) {
   const bool xyz = V.p.reconst == 2;
   if (xyz) wenoXyz(own, sb, se, fetch, g, sum);
   else wenoSimple(own, sb, se, fetch, g, sum);
-  R f0, f4;
-  wenoPositivity(V, i, g, &f0, &f4);
-  W.lim[i] = f0;
-  W.lim[4 * n + i] = f4;
+  wenoFwdFinish(V, W, i, g, sum, xyz);
+}
+// The packed layout: adjLanes threads per cell, each over every
+// adjLanes-th member, the sums joined by shuffles (the averages' terms are
+// the ones of wenoXyz / wenoSimple, summed in another order).
+template <typename R>
+__global__ void __launch_bounds__(kBlock) kAdjWenoFwdLanes(View<R> V, AdjWork<R> W) {
+  if constexpr (Layout<R>::packed) {
+    constexpr int kL = adjLanes<R>();
+    const int th = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = th / kL, h = th % kL;
+    const bool live = i < V.nc;
+    const R eps = R(1.0e-15);
+    R own[16], t[16], g[15], sum[15];
 #pragma unroll
-  for (int k = 0; k < 15; ++k)
-    if (xyz || k < 5) W.gradd[k * n + i] = sum[k];
-  storeGrad(V, i, g);
+    for (int k = 0; k < 16; ++k) own[k] = R(0);
+    if (live) {
+      ld8(V.gradRaw + 16 * (size_t)i, own);
+      ld8(V.gradRaw + 16 * (size_t)i + 8, own + 8);
+    }
+    const int sb = live ? V.stOff[i] : 0, se = live ? V.stOff[i + 1] : 0;
+    auto fetch = [&](int s) {
+      const int c = V.stIdx[s];
+      ld8(V.gradRaw + 16 * (size_t)c, t);
+      ld8(V.gradRaw + 16 * (size_t)c + 8, t + 8);
+      if (const R *Q = memberReflection(V, s)) reflectGrad(Q, t);
+    };
+    auto join = [&](R *x, int m) {
+#pragma unroll
+      for (int o = 1; o < kL; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < 15; ++k)
+          if (k < m) x[k] += __shfl_xor_sync(0xffffffffu, x[k], o);
+    };
+    const bool xyz = V.p.reconst == 2;
+    if (xyz) {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) {
+        const R w = h == 0 ? R(1) / (own[k] * own[k] + eps) : R(0);
+        sum[k] = w;
+        g[k] = w * own[k];
+      }
+      for (int s = sb + h; s < se; s += kL) {
+        fetch(s);
+#pragma unroll
+        for (int k = 0; k < 15; ++k) {
+          const R w = R(1) / (t[k] * t[k] + eps);
+          sum[k] = sum[k] + w;
+          g[k] = g[k] + w * t[k];
+        }
+      }
+      join(sum, 15);
+      join(g, 15);
+#pragma unroll
+      for (int k = 0; k < 15; ++k) g[k] = g[k] / sum[k];
+    } else {
+      R w0[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const R m = fabs_(own[3 * v]) + fabs_(own[3 * v + 1]) + fabs_(own[3 * v + 2]);
+        w0[v] = R(1) / (m * m + eps);
+        sum[v] = h == 0 ? w0[v] : R(0);
+      }
+      for (int s = sb + h; s < se; s += kL) {
+        fetch(s);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const R m = fabs_(t[3 * v]) + fabs_(t[3 * v + 1]) + fabs_(t[3 * v + 2]);
+          sum[v] = sum[v] + R(1) / (m * m + eps);
+        }
+      }
+      join(sum, 5);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const R term = h == 0 ? w0[v] / sum[v] : R(0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g[3 * v + d] = term * own[3 * v + d];
+      }
+      for (int s = sb + h; s < se; s += kL) {
+        fetch(s);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const R m = fabs_(t[3 * v]) + fabs_(t[3 * v + 1]) + fabs_(t[3 * v + 2]);
+          const R term = (R(1) / (m * m + eps)) / sum[v];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) g[3 * v + d] = g[3 * v + d] + term * t[3 * v + d];
+        }
+      }
+      join(g, 15);
+    }
+    if (!live || h) return;
+    wenoFwdFinish(V, W, i, g, sum, xyz);
+  }
 }
 
 // Transposed flux Jacobian of one face applied to Fbar.
@@ -1367,8 +1477,11 @@ __global__ void __launch_bounds__(kBlock) kAdjCell1(View<R> V, AdjWork<R> W) {
 // cell's primitive adjoint, and tbar for kAdjCell2's neighbour terms.
 template <typename R>
 __global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= V.nc) return;
+  constexpr int kL = adjLanes<R>();  // lanes per cell for the gather
+  const int th = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = th / kL, h = th % kL;
+  if (kL == 1 && m >= V.nc) return;
+  const bool live = m < V.nc;
   const size_t n = V.nc;
   const PlainLoad<R> ld{V};
   R A[15], B[15], A2[15], B2[15];
@@ -1401,7 +1514,7 @@ __global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
 
   R t[15], tb[15];
 #pragma unroll
-  for (int k = 0; k < 15; ++k) t[k] = W.G[k * n + m];
+  for (int k = 0; k < 15; ++k) t[k] = live ? W.G[k * n + m] : R(0);
   const R eps = R(1.0e-15);
   const bool xyz = V.p.reconst == 2;
   // the adjoint of a member gradient tt from (sums of) the averages' terms
@@ -1431,8 +1544,8 @@ __global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
   R tr[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) tr[k] = R(0);
-  add(m);
-  for (int e = V.tsOff[m]; e < V.tsOff[m + 1]; ++e) {
+  if (live && h == 0) add(m);
+  for (int e = live ? V.tsOff[m] + h : 0, ee = live ? V.tsOff[m + 1] : 0; e < ee; e += kL) {
     const R *Q = memberReflection(V, V.tsEnt[e]);
     if (!Q) {
       add(V.tsCell[e]);
@@ -1449,6 +1562,17 @@ __global__ void __launch_bounds__(kBlock) kAdjWeno(View<R> V, AdjWork<R> W) {
     reflectGrad(Q, c);
 #pragma unroll
     for (int k = 0; k < 15; ++k) tr[k] += c[k];
+  }
+  if constexpr (kL > 1) {
+#pragma unroll
+    for (int k = 0; k < 15; ++k)
+#pragma unroll
+      for (int o = 1; o < kL; o <<= 1) {
+        A[k] += __shfl_xor_sync(0xffffffffu, A[k], o);
+        B[k] += __shfl_xor_sync(0xffffffffu, B[k], o);
+        tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], o);
+      }
+    if (!live || h) return;
   }
   reverse(t, A, B, tb);
 #pragma unroll
@@ -1780,12 +1904,17 @@ struct AdjointOps {
   static void gradFwd(const View<R> &V, const AdjWork<R> &W, const double *lamRef, cudaStream_t s) {
     if (V.p.reconst == 10) kAdjGradFwd<R, true><<<blocks(V.nc), kBlock, 0, s>>>(V, W, lamRef);
     else kAdjGradFwd<R, false><<<blocks(V.nc), kBlock, 0, s>>>(V, W, lamRef);
-    if (isWeno(V.p)) kAdjWenoFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    if (isWeno(V.p)) {
+      if constexpr (Layout<R>::packed)
+        kAdjWenoFwdLanes<R><<<blocks((long long)V.nc * adjLanes<R>()), kBlock, 0, s>>>(V, W);
+      else
+        kAdjWenoFwd<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    }
   }
   static void cellAdjoint(const View<R> &V, AdjWork<R> &W, double *cvBarRef, cudaStream_t s) {
     if (V.p.reconst == 10 && V.p.spaceOrder > 1) kAdjCell1<R, true><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
     else kAdjCell1<R, false><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
-    if (isWeno(V.p)) kAdjWeno<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W);
+    if (isWeno(V.p)) kAdjWeno<R><<<blocks((long long)V.nc * adjLanes<R>()), kBlock, 0, s>>>(V, W);
     kAdjCell2<R><<<blocks(V.nc), kBlock, 0, s>>>(V, W, cvBarRef);
   }
   // The boundary faces' kernel (dual numbers through the patch fluxes; few
