@@ -322,9 +322,18 @@ void identifyPeriodicVertices(orc_ctx *c) {
 
 /* Offset of stencil member j from cell i, cofg(j) - cofg(i), for the image
  * of j nearest to i when the mesh is periodic (the virtual cell standing for
- * j in the reference). */
+ * j in the reference).  A symmetry image's offset is its cell's offset plus
+ * the image's translation from its cell, (cofg(cell) - cofg(i)) + (image -
+ * cofg(cell)), summed in that order like a periodic image's. */
 void memberOffset(const orc_ctx *c, int i, int j, double &dx, double &dy, double &dz) {
-  const double *xj = (j < c->nCells) ? &c->cofg[3 * j] : &c->imgPos[3 * (size_t)(j - c->nCells)];
+  if (j >= c->nCells) {
+    const double *x = &c->imgPos[3 * (size_t)(j - c->nCells)], *x0 = &c->cofg[3 * c->imgCell[j - c->nCells]];
+    dx = (x0[0] - c->cofg[3 * i]) + (x[0] - x0[0]);
+    dy = (x0[1] - c->cofg[3 * i + 1]) + (x[1] - x0[1]);
+    dz = (x0[2] - c->cofg[3 * i + 2]) + (x[2] - x0[2]);
+    return;
+  }
+  const double *xj = &c->cofg[3 * j];
   dx = xj[0] - c->cofg[3 * i];
   dy = xj[1] - c->cofg[3 * i + 1];
   dz = xj[2] - c->cofg[3 * i + 2];

@@ -411,10 +411,12 @@ extern "C" int rflu_setup_build(const rflu_mesh_desc *m, int spaceOrder, rflu_se
   int nvExt = nv;
   auto memberOffset = [&](const double *cg, int i, int j, double &dx, double &dy, double &dz, double *sh) {
     if (j >= nc) {
+      // the image's cell's offset plus the image's translation from its
+      // cell, summed in that order (as the kernels add c2csShift)
       const double *x = &imgPos[3 * (size_t)(j - nc)], *x0 = &cg[3 * (size_t)imgCell[j - nc]];
-      dx = x[0] - cg[3 * (size_t)i];
-      dy = x[1] - cg[3 * (size_t)i + 1];
-      dz = x[2] - cg[3 * (size_t)i + 2];
+      dx = (x0[0] - cg[3 * (size_t)i]) + (x[0] - x0[0]);
+      dy = (x0[1] - cg[3 * (size_t)i + 1]) + (x[1] - x0[1]);
+      dz = (x0[2] - cg[3 * (size_t)i + 2]) + (x[2] - x0[2]);
       if (sh) for (int d = 0; d < 3; ++d) sh[d] = x[d] - x0[d];
       return;
     }
