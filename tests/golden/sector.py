@@ -4,10 +4,10 @@ oracle's and the device's comparisons with them.
 
 The runs: a 90-degree annulus sector about z (r from 2 mm to 12 mm, 16
 cells around, square-graded rings, two z layers), a cylindrical gas jump
-at r = 6 mm at rest (RFLU_InitFlowHardCode.F90, case "cylds": the
-post-shock state inside, ambient outside), HLLC, Wray RK3, eigen-frame
-Barth-Jespersen (RECONST 10), to t = 4e-6 s; theta0-3.7 is the same sector
-turned by 3.7 degrees.  The reference's patches: the two planes as a
+at r = 6 mm at rest (utilities/init/RFLU_InitFlowHardCode.F90:839-905,
+case "cylds": the post-shock state inside, ambient outside), HLLC, Wray
+RK3, eigen-frame Barth-Jespersen (RECONST 10), to t = 4e-6 s; theta0-3.7
+is the same sector turned by 3.7 degrees.  The reference's patches: the two planes as a
 rotational periodic pair, an NSCBC outflow at r_out, a slip wall at r_in,
 the z planes as a translational periodic pair.  Here:
 
